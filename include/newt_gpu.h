@@ -1,0 +1,186 @@
+/*
+ * newt_gpu.h - C ABI of the GB300 batched stepping engine for newt.
+ *
+ * newt (hwang2409/tooling, newt/) is a single-world, single-threaded Rust
+ * rigid-body engine whose public surface is `World::step(&mut self)`
+ * (newt/src/world.rs:1459), scene loading (newt/src/model.rs:179,
+ * newt/src/mjcf.rs:119) and MuJoCo-layout state setters
+ * (newt/src/world.rs:519-623).  It has no FFI (newt/Cargo.toml:9-10) and
+ * reports errors by panicking.  This header is the drop-in boundary a newt
+ * caller binds with `extern "C"`: plain pointers and sizes, int status codes,
+ * no C++ exceptions and no device traps crossing it.
+ *
+ * Ownership: the library owns model and world state on the device.  Host
+ * buffers passed in are caller-owned, copied during the call and never
+ * retained.  One context = one CUDA stream; a context is not thread-safe.
+ *
+ * State layout (MuJoCo convention, the one newt's differential tests use,
+ * newt/tests/differential.rs:548-640):
+ *   qpos: free bodies first (pos xyz, quat wxyz), then the tree joints in link
+ *         order (free root: pos xyz + quat wxyz; hinge/slide: 1; ball: quat wxyz).
+ *   qvel: free bodies (v_world xyz, omega_body xyz), then tree joints
+ *         (free root: v_world xyz, omega_body xyz; hinge/slide: 1; ball: 3).
+ */
+#ifndef NEWT_GPU_H
+#define NEWT_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (replace newt's panics, newt/src/world.rs:874-894,
+ *      newt/src/solver.rs:2856-2858, newt/src/world.rs:1462-1464) ---------- */
+#define NEWT_OK 0
+#define NEWT_E_INVALID 1          /* bad argument / malformed model */
+#define NEWT_E_UNSUPPORTED_PAIR 2 /* shape pair with no narrowphase (world.rs:874) */
+#define NEWT_E_NOT_PD 3           /* mass matrix or Hessian factorisation failed */
+#define NEWT_E_OVERFLOW 4         /* a per-world contact buffer overflowed */
+#define NEWT_E_TIMEOUT 5          /* a bounded device wait gave up */
+#define NEWT_E_CUDA 6             /* CUDA runtime error */
+#define NEWT_E_NOMEM 7            /* device memory / admission budget exhausted */
+#define NEWT_E_NOT_FINITE 8       /* NaN or Inf produced in a world */
+
+/* per-world status bits (newt_gpu_world_status) */
+#define NEWT_WS_NONFINITE 0x1u
+#define NEWT_WS_NOT_PD 0x2u
+#define NEWT_WS_CONTACT_OVERFLOW 0x4u
+#define NEWT_WS_ITER_CAP 0x8u
+#define NEWT_WS_FP64_FALLBACK 0x10u
+
+/* ---- model description (flattened newt `World`; newt/src/tree.rs:79-237,
+ *      newt/src/body.rs:22-47, newt/src/geom.rs:352) ----------------------- */
+#define NEWT_JOINT_FREE 0
+#define NEWT_JOINT_FIXED 1
+#define NEWT_JOINT_HINGE 2
+#define NEWT_JOINT_SLIDE 3
+#define NEWT_JOINT_BALL 4
+
+#define NEWT_SHAPE_PLANE 0
+#define NEWT_SHAPE_SPHERE 1
+#define NEWT_SHAPE_BOX 2
+#define NEWT_SHAPE_CAPSULE 3
+
+#define NEWT_SOLVER_PGS 1
+#define NEWT_SOLVER_NEWTON 2
+
+typedef struct newt_link_desc {      /* newt::tree::Link */
+  int32_t parent;                    /* -1 for the root (link 0) */
+  int32_t joint;                     /* NEWT_JOINT_* */
+  float axis[3];                     /* hinge/slide axis, parent frame */
+  float damping;                     /* hinge/slide/ball joint damping */
+  float armature;
+  float free_damping;                /* free root only */
+  float jp_pos[3], jp_quat[4];       /* joint_offset_in_parent, quat xyzw */
+  float jc_pos[3], jc_quat[4];       /* joint_offset_in_child, quat xyzw */
+  float mass;
+  float inertia[9];                  /* about the COM, body axes, column-major */
+} newt_link_desc;
+
+typedef struct newt_body_desc {      /* newt::body::Body (free rigid body) */
+  float mass;
+  float inertia[9];                  /* column-major */
+} newt_body_desc;
+
+typedef struct newt_geom_desc {      /* newt::geom::Geom */
+  int32_t shape;                     /* NEWT_SHAPE_* */
+  int32_t body;                      /* free-body index, or -1 */
+  int32_t link;                      /* link index in the world's tree, or -1 */
+  float size[3];                     /* sphere r | box half extents | capsule r, half_height */
+  float local_pos[3], local_quat[4]; /* offset in the body/link frame; static: world pose */
+  float friction;
+  float solref[2];                   /* timeconst, dampratio */
+  float solimp[5];                   /* dmin, dmax, width, midpoint, power */
+  float margin, gap;
+  int32_t condim;                    /* 1 or 3 (pyramidal cone) */
+  uint32_t group, mask;              /* collision filter (newt/src/broadphase.rs:16) */
+} newt_geom_desc;
+
+typedef struct newt_model_desc {     /* one world's model: at most one tree */
+  int32_t n_links, n_bodies, n_geoms;
+  const newt_link_desc* links;
+  const newt_body_desc* bodies;
+  const newt_geom_desc* geoms;
+  float dt;
+  float gravity[3];
+  int32_t solver;                    /* NEWT_SOLVER_PGS | NEWT_SOLVER_NEWTON */
+  int32_t iterations;                /* PGS sweeps / Newton iteration cap */
+  int32_t tree_self_collision;       /* 0: in-tree geom pairs are skipped */
+} newt_model_desc;
+
+/* ---- context ------------------------------------------------------------ */
+typedef struct newt_gpu_ctx newt_gpu_ctx;
+
+typedef struct newt_gpu_opts {
+  int32_t device;                    /* CUDA device ordinal */
+  int32_t max_worlds;                /* slot capacity */
+  uint64_t hbm_budget_bytes;         /* 0 = free HBM at creation minus a reserve */
+} newt_gpu_opts;
+
+/* Replaces building a `World` (newt/src/world.rs:325). */
+int newt_gpu_create(const newt_gpu_opts* opts, newt_gpu_ctx** out);
+int newt_gpu_destroy(newt_gpu_ctx* ctx);
+const char* newt_gpu_last_error(const newt_gpu_ctx* ctx);
+
+/* Replaces the loaders' `World::add_tree/add_body/add_geom`
+ * (newt/src/world.rs:950-981): validates and copies `n` models to the device.
+ * Rejects unsupported shape pairs with NEWT_E_UNSUPPORTED_PAIR (the
+ * deferred-pair panic of newt/src/world.rs:874-894). */
+int newt_gpu_upload_models(newt_gpu_ctx* ctx, const newt_model_desc* models, int32_t n,
+                           int32_t* model_ids_out);
+/* MuJoCo-layout dimensions of a model: nq, nv (and nu = nv actuated DoF). */
+int newt_gpu_model_dims(const newt_gpu_ctx* ctx, int32_t model_id, int32_t* nq, int32_t* nv);
+
+/* Allocate world slots for models (admission by the HBM budget). */
+int newt_gpu_alloc_worlds(newt_gpu_ctx* ctx, const int32_t* model_ids, int32_t n, int32_t* slots_out);
+int newt_gpu_free_worlds(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n);
+
+/* State in/out, MuJoCo layout, the worlds' vectors concatenated in `slots`
+ * order.  Mirrors `World::apply_mujoco_qpos/qvel` (newt/src/world.rs:519-623). */
+int newt_gpu_set_state(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, const float* qpos,
+                       const float* qvel);
+int newt_gpu_get_state(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, float* qpos, float* qvel);
+/* Generalised applied forces (`Tree::qfrc_applied`, newt/src/tree.rs:207),
+ * nv per world, concatenated; persists across steps like newt's field. */
+int newt_gpu_set_qfrc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, const float* qfrc);
+
+/* Replaces `World::step()` (newt/src/world.rs:1459) for every live world.
+ * mode NEWT_STEP_PLAIN: one launch per stage per step, fixed tiles.
+ * mode NEWT_STEP_BATCHED: fused persistent launch over the whole horizon,
+ *   worlds pulled from a size-class-sorted queue, captured in a CUDA graph. */
+#define NEWT_STEP_PLAIN 0
+#define NEWT_STEP_BATCHED 1
+int newt_gpu_step(newt_gpu_ctx* ctx, int32_t n_steps, int32_t mode);
+/* Waits for the context's stream (bounded host wait; NEWT_E_TIMEOUT). */
+int newt_gpu_sync(newt_gpu_ctx* ctx, int32_t timeout_ms);
+
+/* Per-world status words (NEWT_WS_*), accumulated since the last clear. */
+int newt_gpu_world_status(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, uint32_t* status,
+                          int32_t clear);
+
+/* ---- diagnostics (parity surfaces) -------------------------------------- */
+/* Generalised acceleration of the last step, newt layout (qdot order), nv per
+ * world.  Mirrors the qacc that `euler_step_with_workspace` integrates
+ * (newt/src/tree.rs:1406-1417). */
+int newt_gpu_get_qacc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, float* qacc);
+/* Contacts detected at the start of the last step for one world:
+ * per contact (geom_a, geom_b) pairs into `pairs` (2*cap ints) and
+ * pos xyz, normal xyz, penetration into `data` (7*cap floats). */
+int newt_gpu_get_contacts(newt_gpu_ctx* ctx, int32_t slot, int32_t cap, int32_t* n_out,
+                          int32_t* pairs, float* data);
+/* Row impulses of the last step's constraint solve for one world, in the
+ * solver's row order (4 pyramidal facet rows per contact). */
+int newt_gpu_get_impulses(newt_gpu_ctx* ctx, int32_t slot, int32_t cap, int32_t* n_out, float* impulses);
+
+/* ---- timing helpers for the benchmark (CUDA events on the ctx stream) ---- */
+int newt_gpu_event_record(newt_gpu_ctx* ctx, int32_t which);          /* which: 0 start, 1 stop */
+int newt_gpu_event_elapsed_ms(newt_gpu_ctx* ctx, float* ms);
+int newt_gpu_flush_l2(newt_gpu_ctx* ctx);                              /* writes a buffer > L2 */
+/* Kernel launches issued by this context since creation. */
+int64_t newt_gpu_launch_count(const newt_gpu_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NEWT_GPU_H */

@@ -1,0 +1,75 @@
+// Oracle (test infrastructure only): World::step in its semi-implicit Euler
+// form, plus the free-body RK4 path with zero-order-hold solver wrenches
+// (used only to replay newt's RK4 solver goldens).
+//
+// Sources (paths inside hwang2409/tooling):
+//   newt/src/world.rs:1459-1537  World::step
+//   newt/src/world.rs:1790-1817  step_bodies_euler
+//   newt/src/world.rs:1952-2051  step_trees_euler
+//   newt/src/world.rs:2097-2152  compute_solver_wrenches
+//   newt/src/world.rs:3223-3286  evaluate, clamp_velocity
+#pragma once
+#include "newt_world.hpp"
+#include "newt_treecontact.hpp"
+
+namespace oracle {
+
+template <class R> struct Deriv { Vec3<R> dlin, dang; };
+
+template <class R> Deriv<R> evaluate(const Body<R>& s, Vec3<R> g, Vec3<R> f, Vec3<R> tq) {  // world.rs:3223-3245
+  Vec3<R> dlin = g + f / s.mass;
+  Vec3<R> iw = s.inertia * s.omega_body;
+  Vec3<R> gyro = -(s.omega_body.cross(iw));
+  Vec3<R> tb = s.ori.inverse_rotate(tq);
+  Vec3<R> dang = s.inertia_inv * (tb + gyro);
+  return {dlin, dang};
+}
+
+template <class R> void World<R>::step() {
+  const bool solver = solver_mode == M_PGS || solver_mode == M_NEWTON;
+  std::vector<Contact<R>> contacts;
+  if (solver) detect_contacts(contacts);
+  // Tree-involved contacts are solved jointly first (world.rs:2154-2175).
+  std::vector<Contact<R>> tree_contacts, free_contacts;
+  for (const Contact<R>& c : contacts) {
+    bool tl = geoms[c.ga].att_kind() == 2 || geoms[c.gb].att_kind() == 2;
+    (tl ? tree_contacts : free_contacts).push_back(c);
+  }
+  tree_qfrc.assign(trees.size(), std::vector<R>());
+  for (size_t t = 0; t < trees.size(); ++t) tree_qfrc[t].assign(trees[t].nv(), R(0));
+  tree_body_wrenches.assign(bodies.size(), Wrench<R>{Vec3<R>(), Vec3<R>()});
+  if (solver) solve_tree_contacts(*this, tree_contacts, solver_mode == M_NEWTON);
+  // step_trees_euler (world.rs:1952-2051)
+  for (size_t ti = 0; ti < trees.size(); ++ti) {
+    Tree<R>& tree = trees[ti];
+    bool prior = tree.disable_penalty_limits;
+    std::vector<R> delta;
+    if (solver) {
+      delta.assign(tree.nv(), R(0));
+      for (int s = 0; s < tree.nv(); ++s) delta[s] += tree_qfrc[ti][s];
+      for (int s = 0; s < tree.nv(); ++s) tree.qfrc_applied[s] += delta[s];
+      tree.disable_penalty_limits = true;
+    }
+    euler_step_tree(tree, gravity, dt);
+    for (size_t s = 0; s < delta.size(); ++s) tree.qfrc_applied[s] -= delta[s];
+    tree.disable_penalty_limits = prior;
+  }
+  // step_bodies_euler (world.rs:1790-1817)
+  std::vector<Wrench<R>> ext(bodies.size(), Wrench<R>{Vec3<R>(), Vec3<R>()});
+  if (solver) {
+    solve_free_bodies_pgs(bodies, geoms, free_contacts, gravity, dt, iterations, ext);
+    for (size_t i = 0; i < bodies.size(); ++i) { ext[i].f += tree_body_wrenches[i].f; ext[i].t += tree_body_wrenches[i].t; }
+  }
+  for (size_t i = 0; i < bodies.size(); ++i) {
+    Body<R>& b = bodies[i];
+    Deriv<R> d = evaluate(b, gravity, ext[i].f, ext[i].t);
+    Vec3<R> lv = b.vel + d.dlin * dt;
+    Vec3<R> av = b.omega_body + d.dang * dt;
+    b.pos += lv * dt;
+    b.ori = b.ori.integrate_body_angular_velocity(av, dt);
+    b.vel = lv;
+    b.omega_body = av;
+  }
+}
+
+}  // namespace oracle

@@ -1,0 +1,339 @@
+// Oracle (test infrastructure only): C entry points over the C++
+// restatement of newt's step, used by the CPU test suite, the GPU parity
+// tests and the benchmark's CPU-baseline leg.  Never linked into the shipped
+// GPU library.
+//
+// Worlds are described with the same `newt_model_desc` the GPU C ABI takes
+// (include/newt_gpu.h), so a test builds one description and feeds both.
+// `precision` 0 runs the f32 mirror of newt's arithmetic, 1 the FP64 oracle.
+// `layout` 0 = MuJoCo qpos/qvel (newt/src/world.rs:519-623), 1 = newt's own
+// q/qdot order (bodies: pos, quat xyzw, v_world, omega_body).
+#include <atomic>
+#include <chrono>
+#include <cstdio>
+#include <stdexcept>
+#include <thread>
+#include <vector>
+#include "../include/newt_gpu.h"
+#include "newt_step.hpp"
+
+using namespace oracle;
+
+namespace {
+
+template <class R> Quat<R> quat_xyzw(const float* q) { return Quat<R>(q[0], q[1], q[2], q[3]); }
+template <class R> Vec3<R> v3(const float* v) { return Vec3<R>(v[0], v[1], v[2]); }
+template <class R> Mat3<R> m3(const float* m) { Mat3<R> o; for (int i = 0; i < 9; ++i) o.d[i] = m[i]; return o; }
+
+template <class R> World<R> build_world(const newt_model_desc& d) {
+  World<R> w;
+  w.dt = d.dt;
+  w.gravity = v3<R>(d.gravity);
+  w.solver_mode = d.solver == NEWT_SOLVER_NEWTON ? M_NEWTON : (d.solver == NEWT_SOLVER_PGS ? M_PGS : M_PENALTY);
+  w.iterations = d.iterations;
+  for (int i = 0; i < d.n_bodies; ++i) {
+    const newt_body_desc& b = d.bodies[i];
+    w.bodies.push_back(make_body<R>(b.mass, m3<R>(b.inertia), Vec3<R>(), Quat<R>()));
+  }
+  if (d.n_links > 0) {
+    Tree<R> t;
+    for (int i = 0; i < d.n_links; ++i) {
+      const newt_link_desc& L = d.links[i];
+      Link<R> l;
+      l.parent = L.parent; l.type = L.joint; l.axis = v3<R>(L.axis);
+      l.damping = L.damping; l.armature = L.armature; l.free_damping = L.free_damping;
+      l.jp_pos = v3<R>(L.jp_pos); l.jp_ori = quat_xyzw<R>(L.jp_quat);
+      l.jc_pos = v3<R>(L.jc_pos); l.jc_ori = quat_xyzw<R>(L.jc_quat);
+      l.mass = L.mass; l.inertia = m3<R>(L.inertia);
+      t.push_link(l);
+    }
+    w.trees.push_back(t);
+    w.disabled_self_collision.push_back(d.tree_self_collision ? 0 : 1);
+  }
+  for (int i = 0; i < d.n_geoms; ++i) {
+    const newt_geom_desc& G = d.geoms[i];
+    Geom<R> g;
+    g.shape = G.shape;
+    for (int k = 0; k < 3; ++k) g.size[k] = G.size[k];
+    g.body = G.body; g.link = G.link; g.tree = G.link >= 0 ? 0 : -1;
+    g.local_pos = v3<R>(G.local_pos); g.local_ori = quat_xyzw<R>(G.local_quat);
+    g.friction = G.friction;
+    g.solref.timeconst = G.solref[0]; g.solref.dampratio = G.solref[1];
+    g.solimp.dmin = G.solimp[0]; g.solimp.dmax = G.solimp[1]; g.solimp.width = G.solimp[2];
+    g.solimp.midpoint = G.solimp[3]; g.solimp.power = (int)G.solimp[4];
+    g.margin = G.margin; g.gap = G.gap; g.condim = G.condim;
+    g.group = G.group; g.mask = G.mask;
+    w.geoms.push_back(g);
+  }
+  return w;
+}
+
+template <class R> void set_state(World<R>& w, const float* qpos, const float* qvel, int layout) {
+  int c = 0;
+  for (Body<R>& b : w.bodies) {
+    b.pos = Vec3<R>(qpos[c], qpos[c + 1], qpos[c + 2]);
+    if (layout == 0) b.ori = Quat<R>(qpos[c + 4], qpos[c + 5], qpos[c + 6], qpos[c + 3]).renormalize();
+    else b.ori = Quat<R>(qpos[c + 3], qpos[c + 4], qpos[c + 5], qpos[c + 6]);
+    c += 7;
+  }
+  for (Tree<R>& t : w.trees) {
+    for (size_t i = 0; i < t.links.size(); ++i) {
+      int qo = t.q_off[i];
+      switch (t.links[i].type) {
+        case J_FREE: {
+          for (int k = 0; k < 3; ++k) t.q[qo + k] = qpos[c + k];
+          Quat<R> q = layout == 0 ? Quat<R>(qpos[c + 4], qpos[c + 5], qpos[c + 6], qpos[c + 3]).renormalize()
+                                  : Quat<R>(qpos[c + 3], qpos[c + 4], qpos[c + 5], qpos[c + 6]);
+          t.q[qo + 3] = q.x; t.q[qo + 4] = q.y; t.q[qo + 5] = q.z; t.q[qo + 6] = q.w;
+          c += 7; break;
+        }
+        case J_BALL: {
+          Quat<R> q = layout == 0 ? Quat<R>(qpos[c + 1], qpos[c + 2], qpos[c + 3], qpos[c]).renormalize()
+                                  : Quat<R>(qpos[c], qpos[c + 1], qpos[c + 2], qpos[c + 3]);
+          t.q[qo] = q.x; t.q[qo + 1] = q.y; t.q[qo + 2] = q.z; t.q[qo + 3] = q.w;
+          c += 4; break;
+        }
+        case J_HINGE: case J_SLIDE: t.q[qo] = qpos[c]; c += 1; break;
+        default: break;
+      }
+    }
+  }
+  c = 0;
+  for (Body<R>& b : w.bodies) {
+    b.vel = Vec3<R>(qvel[c], qvel[c + 1], qvel[c + 2]);
+    b.omega_body = Vec3<R>(qvel[c + 3], qvel[c + 4], qvel[c + 5]);
+    c += 6;
+  }
+  for (Tree<R>& t : w.trees) {
+    for (size_t i = 0; i < t.links.size(); ++i) {
+      int vo = t.v_off[i], qo = t.q_off[i];
+      switch (t.links[i].type) {
+        case J_FREE: {
+          if (layout == 0) {
+            Quat<R> o(t.q[qo + 3], t.q[qo + 4], t.q[qo + 5], t.q[qo + 6]);
+            Vec3<R> vb = o.inverse_rotate(Vec3<R>(qvel[c], qvel[c + 1], qvel[c + 2]));
+            R v[6] = {R(qvel[c + 3]), R(qvel[c + 4]), R(qvel[c + 5]), vb.x, vb.y, vb.z};
+            for (int k = 0; k < 6; ++k) t.qdot[vo + k] = v[k];
+          } else {
+            for (int k = 0; k < 6; ++k) t.qdot[vo + k] = qvel[c + k];
+          }
+          c += 6; break;
+        }
+        case J_BALL: for (int k = 0; k < 3; ++k) t.qdot[vo + k] = qvel[c + k]; c += 3; break;
+        case J_HINGE: case J_SLIDE: t.qdot[vo] = qvel[c]; c += 1; break;
+        default: break;
+      }
+    }
+  }
+}
+
+template <class R> void get_state(const World<R>& w, double* qpos, double* qvel, int layout) {
+  int c = 0;
+  for (const Body<R>& b : w.bodies) {
+    qpos[c] = b.pos.x; qpos[c + 1] = b.pos.y; qpos[c + 2] = b.pos.z;
+    if (layout == 0) { qpos[c + 3] = b.ori.w; qpos[c + 4] = b.ori.x; qpos[c + 5] = b.ori.y; qpos[c + 6] = b.ori.z; }
+    else { qpos[c + 3] = b.ori.x; qpos[c + 4] = b.ori.y; qpos[c + 5] = b.ori.z; qpos[c + 6] = b.ori.w; }
+    c += 7;
+  }
+  for (const Tree<R>& t : w.trees)
+    for (size_t i = 0; i < t.links.size(); ++i) {
+      int qo = t.q_off[i];
+      switch (t.links[i].type) {
+        case J_FREE:
+          for (int k = 0; k < 3; ++k) qpos[c + k] = t.q[qo + k];
+          if (layout == 0) { qpos[c + 3] = t.q[qo + 6]; qpos[c + 4] = t.q[qo + 3]; qpos[c + 5] = t.q[qo + 4]; qpos[c + 6] = t.q[qo + 5]; }
+          else for (int k = 3; k < 7; ++k) qpos[c + k] = t.q[qo + k];
+          c += 7; break;
+        case J_BALL:
+          if (layout == 0) { qpos[c] = t.q[qo + 3]; qpos[c + 1] = t.q[qo]; qpos[c + 2] = t.q[qo + 1]; qpos[c + 3] = t.q[qo + 2]; }
+          else for (int k = 0; k < 4; ++k) qpos[c + k] = t.q[qo + k];
+          c += 4; break;
+        case J_HINGE: case J_SLIDE: qpos[c] = t.q[qo]; c += 1; break;
+        default: break;
+      }
+    }
+  c = 0;
+  for (const Body<R>& b : w.bodies) {
+    qvel[c] = b.vel.x; qvel[c + 1] = b.vel.y; qvel[c + 2] = b.vel.z;
+    qvel[c + 3] = b.omega_body.x; qvel[c + 4] = b.omega_body.y; qvel[c + 5] = b.omega_body.z;
+    c += 6;
+  }
+  for (const Tree<R>& t : w.trees)
+    for (size_t i = 0; i < t.links.size(); ++i) {
+      int vo = t.v_off[i], qo = t.q_off[i];
+      switch (t.links[i].type) {
+        case J_FREE:
+          if (layout == 0) {
+            Quat<R> o(t.q[qo + 3], t.q[qo + 4], t.q[qo + 5], t.q[qo + 6]);
+            Vec3<R> vw = o.rotate(Vec3<R>(t.qdot[vo + 3], t.qdot[vo + 4], t.qdot[vo + 5]));
+            qvel[c] = vw.x; qvel[c + 1] = vw.y; qvel[c + 2] = vw.z;
+            qvel[c + 3] = t.qdot[vo]; qvel[c + 4] = t.qdot[vo + 1]; qvel[c + 5] = t.qdot[vo + 2];
+          } else for (int k = 0; k < 6; ++k) qvel[c + k] = t.qdot[vo + k];
+          c += 6; break;
+        case J_BALL: for (int k = 0; k < 3; ++k) qvel[c + k] = t.qdot[vo + k]; c += 3; break;
+        case J_HINGE: case J_SLIDE: qvel[c] = t.qdot[vo]; c += 1; break;
+        default: break;
+      }
+    }
+}
+
+int dims(const newt_model_desc& d, int* nq, int* nv) {
+  int q = 7 * d.n_bodies, v = 6 * d.n_bodies;
+  for (int i = 0; i < d.n_links; ++i) { q += joint_nq(d.links[i].joint); v += joint_nv(d.links[i].joint); }
+  *nq = q; *nv = v;
+  return 0;
+}
+
+template <class R> void set_qfrc(World<R>& w, const float* qfrc) {
+  // qfrc is nv per world in qvel order; only tree DoF carry qfrc_applied.
+  int c = 6 * (int)w.bodies.size();
+  for (Tree<R>& t : w.trees) for (int k = 0; k < t.nv(); ++k) t.qfrc_applied[k] = qfrc ? qfrc[c + k] : R(0);
+}
+
+template <class R>
+int run_one(const newt_model_desc& d, const float* qpos, const float* qvel, const float* qfrc, int n_steps, int layout,
+            double* qpos_out, double* qvel_out, double* qacc_out) {
+  World<R> w = build_world<R>(d);
+  set_state(w, qpos, qvel, layout);
+  set_qfrc(w, qfrc);
+  std::vector<R> qacc;
+  for (int s = 0; s < n_steps; ++s) {
+    if (qacc_out && s == n_steps - 1 && !w.trees.empty() && w.geoms.empty()) {
+      // one-step qacc of a contact-free tree: the ABA output the step integrates
+      std::vector<Pose<R>> poses; forward_kinematics(w.trees[0], poses);
+      std::vector<Wrench<R>> ext(w.trees[0].links.size(), Wrench<R>{Vec3<R>(), Vec3<R>()});
+      Tree<R> t = w.trees[0];
+      if (w.solver_mode != M_PENALTY) t.disable_penalty_limits = true;
+      aba(t, poses, w.gravity, ext, w.dt, qacc);
+    }
+    w.step();
+  }
+  get_state(w, qpos_out, qvel_out, layout);
+  if (qacc_out) {
+    int nb = 6 * (int)w.bodies.size();
+    for (int k = 0; k < nb; ++k) qacc_out[k] = 0.0;
+    for (size_t k = 0; k < qacc.size(); ++k) qacc_out[nb + k] = qacc[k];
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int oracle_model_dims(const newt_model_desc* d, int* nq, int* nv) { return dims(*d, nq, nv); }
+
+// Steps `n_worlds` worlds independently.  World w uses models[model_of_world[w]]
+// and the w-th qpos/qvel/qfrc block (blocks concatenated).  Outputs are double.
+// n_threads > 1 partitions worlds statically across host threads.
+int oracle_run(const newt_model_desc* models, int n_worlds, const int* model_of_world, const float* qpos,
+               const float* qvel, const float* qfrc, int n_steps, int precision, int layout, double* qpos_out,
+               double* qvel_out, double* qacc_out, int n_threads) {
+  std::vector<long> qo(n_worlds + 1, 0), vo(n_worlds + 1, 0);
+  for (int w = 0; w < n_worlds; ++w) {
+    int nq, nv; dims(models[model_of_world[w]], &nq, &nv);
+    qo[w + 1] = qo[w] + nq; vo[w + 1] = vo[w] + nv;
+  }
+  std::atomic<int> err{0};
+  auto work = [&](int begin, int end) {
+    for (int w = begin; w < end; ++w) {
+      const newt_model_desc& d = models[model_of_world[w]];
+      try {
+        if (precision == 0)
+          run_one<float>(d, qpos + qo[w], qvel + vo[w], qfrc ? qfrc + vo[w] : nullptr, n_steps, layout,
+                         qpos_out + qo[w], qvel_out + vo[w], qacc_out ? qacc_out + vo[w] : nullptr);
+        else
+          run_one<double>(d, qpos + qo[w], qvel + vo[w], qfrc ? qfrc + vo[w] : nullptr, n_steps, layout,
+                          qpos_out + qo[w], qvel_out + vo[w], qacc_out ? qacc_out + vo[w] : nullptr);
+      } catch (const std::exception& e) {
+        std::fprintf(stderr, "oracle_run world %d: %s\n", w, e.what());
+        err = 1;
+      }
+    }
+  };
+  if (n_threads <= 1) work(0, n_worlds);
+  else {
+    std::vector<std::thread> th;
+    for (int t = 0; t < n_threads; ++t) {
+      int b = (int)((long)n_worlds * t / n_threads), e = (int)((long)n_worlds * (t + 1) / n_threads);
+      th.emplace_back(work, b, e);
+    }
+    for (auto& x : th) x.join();
+  }
+  return err.load();
+}
+
+// Contacts of one world at its given state (MuJoCo layout), detected exactly
+// as the step's collision phase does.  data: pos xyz, normal xyz, penetration.
+int oracle_contacts(const newt_model_desc* d, const float* qpos, const float* qvel, int precision, int cap,
+                    int* n_out, int* pairs, double* data) {
+  auto go = [&](auto tag) {
+    using R = decltype(tag);
+    World<R> w = build_world<R>(*d);
+    set_state(w, qpos, qvel, 0);
+    std::vector<Contact<R>> cs;
+    w.detect_contacts(cs);
+    *n_out = (int)cs.size();
+    for (int i = 0; i < (int)cs.size() && i < cap; ++i) {
+      pairs[2 * i] = cs[i].ga; pairs[2 * i + 1] = cs[i].gb;
+      double v[7] = {(double)cs[i].pos.x, (double)cs[i].pos.y, (double)cs[i].pos.z, (double)cs[i].n.x,
+                     (double)cs[i].n.y, (double)cs[i].n.z, (double)cs[i].pen};
+      for (int k = 0; k < 7; ++k) data[7 * i + k] = v[k];
+    }
+  };
+  if (precision == 0) go(0.0f); else go(0.0);
+  return 0;
+}
+
+// PGS row impulses of one free-body world at its state (one step's solve).
+int oracle_impulses(const newt_model_desc* d, const float* qpos, const float* qvel, int precision, int iterations,
+                    int cap, int* n_out, double* impulses) {
+  auto go = [&](auto tag) {
+    using R = decltype(tag);
+    World<R> w = build_world<R>(*d);
+    set_state(w, qpos, qvel, 0);
+    std::vector<Contact<R>> cs;
+    w.detect_contacts(cs);
+    std::vector<Wrench<R>> wr;
+    std::vector<R> imp;
+    solve_free_bodies_pgs(w.bodies, w.geoms, cs, w.gravity, w.dt, iterations > 0 ? iterations : w.iterations, wr, &imp);
+    *n_out = (int)imp.size();
+    for (int i = 0; i < (int)imp.size() && i < cap; ++i) impulses[i] = imp[i];
+  };
+  if (precision == 0) go(0.0f); else go(0.0);
+  return 0;
+}
+
+// Dense CRB mass matrix (newt layout) of the world's tree at native q.
+int oracle_mass_matrix(const newt_model_desc* d, const float* q_native, int precision, double* out) {
+  auto go = [&](auto tag) {
+    using R = decltype(tag);
+    World<R> w = build_world<R>(*d);
+    Tree<R>& t = w.trees[0];
+    for (int i = 0; i < t.nq(); ++i) t.q[i] = q_native[i];
+    std::vector<R> M;
+    mass_matrix(t, M);
+    for (size_t i = 0; i < M.size(); ++i) out[i] = M[i];
+  };
+  if (precision == 0) go(0.0f); else go(0.0);
+  return 0;
+}
+
+// Raw f32 bits of newt's deterministic sin/cos (for the polynomial KATs).
+float oracle_newt_sin(float x) { return newt_sin(x); }
+float oracle_newt_cos(float x) { return newt_cos(x); }
+
+// Wall-clock timing of the f32 mirror over `n_threads` host threads: the CPU
+// baseline (one world per thread, static partition).  Returns seconds.
+double oracle_time_run(const newt_model_desc* models, int n_worlds, const int* model_of_world, const float* qpos,
+                       const float* qvel, const float* qfrc, int n_steps, int n_threads) {
+  long nq = 0, nv = 0;
+  for (int w = 0; w < n_worlds; ++w) { int a, b; dims(models[model_of_world[w]], &a, &b); nq += a; nv += b; }
+  std::vector<double> qo(nq), vo(nv);
+  auto t0 = std::chrono::steady_clock::now();
+  oracle_run(models, n_worlds, model_of_world, qpos, qvel, qfrc, n_steps, 0, 0, qo.data(), vo.data(), nullptr, n_threads);
+  auto t1 = std::chrono::steady_clock::now();
+  return std::chrono::duration<double>(t1 - t0).count();
+}
+
+}  // extern "C"

@@ -1,0 +1,112 @@
+"""Oracle (test infrastructure only): ctypes bindings to ``liboracle.so``.
+
+Only the test suite, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this module.  The shipped GPU path never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from typing import Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(LIB_PATH) or _stale():
+        subprocess.check_call(["make", "-s", "-C", HERE])
+    return LIB_PATH
+
+
+def _stale() -> bool:
+    t = os.path.getmtime(LIB_PATH)
+    srcs = [os.path.join(HERE, f) for f in os.listdir(HERE) if f.endswith((".hpp", ".cpp"))]
+    srcs.append(os.path.join(HERE, "..", "include", "newt_gpu.h"))
+    return any(os.path.getmtime(s) > t for s in srcs)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        P = C.c_void_p
+        L.oracle_run.argtypes = [P, C.c_int, P, P, P, P, C.c_int, C.c_int, C.c_int, P, P, P, C.c_int]
+        L.oracle_run.restype = C.c_int
+        L.oracle_contacts.argtypes = [P, P, P, C.c_int, C.c_int, P, P, P]
+        L.oracle_impulses.argtypes = [P, P, P, C.c_int, C.c_int, C.c_int, P, P]
+        L.oracle_mass_matrix.argtypes = [P, P, C.c_int, P]
+        L.oracle_newt_sin.argtypes = [C.c_float]
+        L.oracle_newt_sin.restype = C.c_float
+        L.oracle_newt_cos.argtypes = [C.c_float]
+        L.oracle_newt_cos.restype = C.c_float
+        L.oracle_time_run.argtypes = [P, C.c_int, P, P, P, P, C.c_int, C.c_int]
+        L.oracle_time_run.restype = C.c_double
+        _lib = L
+    return _lib
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def run(packed, model_of_world: np.ndarray, qpos: np.ndarray, qvel: np.ndarray, qfrc: Optional[np.ndarray],
+        n_steps: int, precision: int = 1, layout: int = 0, want_qacc: bool = False, n_threads: int = 1):
+    """Step worlds on the CPU; returns (qpos, qvel[, qacc]) as float64 arrays."""
+    mow = np.ascontiguousarray(model_of_world, dtype=np.int32)
+    qpos = np.ascontiguousarray(qpos, dtype=np.float32)
+    qvel = np.ascontiguousarray(qvel, dtype=np.float32)
+    qf = None if qfrc is None else np.ascontiguousarray(qfrc, dtype=np.float32)
+    qo = np.zeros(qpos.shape[0], dtype=np.float64)
+    vo = np.zeros(qvel.shape[0], dtype=np.float64)
+    qa = np.zeros(qvel.shape[0], dtype=np.float64) if want_qacc else None
+    rc = lib().oracle_run(C.cast(packed.descs, C.c_void_p), len(mow), _ptr(mow), _ptr(qpos), _ptr(qvel), _ptr(qf),
+                          int(n_steps), int(precision), int(layout), _ptr(qo), _ptr(vo), _ptr(qa), int(n_threads))
+    if rc != 0:
+        raise RuntimeError("oracle_run failed")
+    return (qo, vo, qa) if want_qacc else (qo, vo)
+
+
+def contacts(packed, index: int, qpos: np.ndarray, qvel: np.ndarray, precision: int = 1, cap: int = 4096):
+    qpos = np.ascontiguousarray(qpos, dtype=np.float32)
+    qvel = np.ascontiguousarray(qvel, dtype=np.float32)
+    n = C.c_int(0)
+    pairs = np.zeros(2 * cap, dtype=np.int32)
+    data = np.zeros(7 * cap, dtype=np.float64)
+    d = C.cast(C.byref(packed.descs[index]), C.c_void_p)
+    lib().oracle_contacts(d, _ptr(qpos), _ptr(qvel), precision, cap, C.byref(n), _ptr(pairs), _ptr(data))
+    k = min(n.value, cap)
+    return pairs[: 2 * k].reshape(k, 2), data[: 7 * k].reshape(k, 7)
+
+
+def impulses(packed, index: int, qpos: np.ndarray, qvel: np.ndarray, precision: int = 1, iterations: int = 0,
+             cap: int = 16384):
+    qpos = np.ascontiguousarray(qpos, dtype=np.float32)
+    qvel = np.ascontiguousarray(qvel, dtype=np.float32)
+    n = C.c_int(0)
+    out = np.zeros(cap, dtype=np.float64)
+    d = C.cast(C.byref(packed.descs[index]), C.c_void_p)
+    lib().oracle_impulses(d, _ptr(qpos), _ptr(qvel), precision, iterations, cap, C.byref(n), _ptr(out))
+    return out[: min(n.value, cap)]
+
+
+def mass_matrix(packed, index: int, q_native: np.ndarray, nv: int, precision: int = 1) -> np.ndarray:
+    q = np.ascontiguousarray(q_native, dtype=np.float32)
+    out = np.zeros(nv * nv, dtype=np.float64)
+    d = C.cast(C.byref(packed.descs[index]), C.c_void_p)
+    lib().oracle_mass_matrix(d, _ptr(q), precision, _ptr(out))
+    return out.reshape(nv, nv)
+
+
+def time_run(packed, model_of_world, qpos, qvel, qfrc, n_steps: int, n_threads: int) -> float:
+    mow = np.ascontiguousarray(model_of_world, dtype=np.int32)
+    qpos = np.ascontiguousarray(qpos, dtype=np.float32)
+    qvel = np.ascontiguousarray(qvel, dtype=np.float32)
+    qf = None if qfrc is None else np.ascontiguousarray(qfrc, dtype=np.float32)
+    return lib().oracle_time_run(C.cast(packed.descs, C.c_void_p), len(mow), _ptr(mow), _ptr(qpos), _ptr(qvel),
+                                 _ptr(qf), int(n_steps), int(n_threads))

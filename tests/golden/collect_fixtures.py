@@ -1,0 +1,41 @@
+"""Copy newt's own golden vectors for the stepping path into tests/golden/.
+
+Runs only where the reference checkout is mounted (never on the GPU machine).
+The files are byte goldens written by newt's test suite (f32 little-endian
+state snapshots, newt/tests/goldens/*.bin) and MuJoCo 3.11.0 FP64 captures in
+newt's NEWTDIF1 format (newt/tests/references/*.bin), plus the scene files
+those captures were made from.  They are data, copied verbatim.
+"""
+import os
+import shutil
+import sys
+
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/newt/tests"
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+FILES = [
+    "goldens/integrator_euler.bin",
+    "goldens/integrator_rk4.bin",
+    "goldens/dynamics_mass_bias.bin",
+    "goldens/joints_chain_and_floating.bin",
+    "goldens/solver_stack.bin",
+    "goldens/solver_newton_stack.bin",
+    "goldens/solver_tree.bin",
+    "goldens/solver_newton_tree.bin",
+    "references/double_pendulum_euler.bin",
+    "references/ballistic_euler.bin",
+    "references/sphere_drop_euler.bin",
+    "references/sphere_drop_newton_euler.bin",
+    "references/box_stack_euler.bin",
+    "references/box_stack_newton_euler.bin",
+    "references/tree_chain_contact_newton_euler.bin",
+    "references/tree_chain_contact_pgs_euler.bin",
+    "references/box_plane_mujoco_anchors.json",
+    "references/constraint_factor_diagnostics.json",
+]
+
+for rel in FILES:
+    src = os.path.join(REF, rel)
+    dst = os.path.join(OUT, os.path.basename(rel))
+    shutil.copyfile(src, dst)
+    print(f"{rel} -> {os.path.relpath(dst)} ({os.path.getsize(dst)} bytes)")

@@ -1,0 +1,127 @@
+"""Pins the oracle to newt's own golden vectors (CPU only).
+
+The f32 mirror must reproduce newt's byte goldens exactly; the FP64 oracle
+must stay inside the windows newt's differential tests allow against MuJoCo.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle_py
+from f32util import f32, quat_from_axis_angle
+from tooling_gb300 import model as M
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _read_f32(name):
+    return np.fromfile(os.path.join(GOLD, name), dtype="<f4")
+
+
+def _integrator_scene():
+    # newt/tests/integrators_golden.rs:10-25
+    w = M.WorldModel(dt=0.005, gravity=(0.0, 0.0, -9.81), solver=0)
+    w.add_body(1.25, M._diag9(0.7, 1.3, 2.1))
+    q = quat_from_axis_angle((1.0, 0.2, -0.4), 0.6)
+    qpos = np.array([0.4, -0.7, 2.0] + q, dtype=np.float32)
+    qvel = np.array([0.8, -0.4, 1.2, 0.4, 1.1, -0.3], dtype=np.float32)
+    return w, qpos, qvel
+
+
+def test_integrator_euler_golden_is_byte_identical():
+    """newt/tests/integrators_golden.rs:84-91 (Euler)."""
+    w, qpos, qvel = _integrator_scene()
+    packed = M.PackedModels([w])
+    gold = _read_f32("integrator_euler.bin").reshape(3, 13)
+    got = [np.concatenate([qpos, qvel])]
+    for n in (20, 100):
+        qo, vo = oracle_py.run(packed, np.zeros(1, np.int32), qpos, qvel, None, n, precision=0, layout=1)
+        got.append(np.concatenate([qo, vo]).astype(np.float32))
+    got = np.stack(got)
+    assert got.tobytes() == gold.tobytes(), np.abs(got - gold).max()
+
+
+def _renormalize(q):
+    n = np.sqrt(f32(f32(f32(q[0] * q[0] + q[1] * q[1]) + q[2] * q[2]) + q[3] * q[3]))
+    return [x / n for x in q]
+
+
+def _box_inertia(mass, hx, hy, hz):
+    m3 = f32(mass) / f32(3.0)
+    hx2, hy2, hz2 = f32(hx) * f32(hx), f32(hy) * f32(hy), f32(hz) * f32(hz)
+    return M._diag9(m3 * (hy2 + hz2), m3 * (hx2 + hz2), m3 * (hx2 + hy2))
+
+
+def _mixed_tree():
+    """newt/tests/dynamics_golden.rs:28-89."""
+    from f32util import normalize
+    w = M.WorldModel()
+    w.push_link(M.Link(parent=-1, joint=M.JOINT_FIXED, mass=1.0, inertia=M._diag9(1.0, 1.0, 1.0)))
+    w.push_link(M.Link(parent=0, joint=M.JOINT_HINGE, axis=normalize((1.0, 0.3, -0.2)), armature=0.02,
+                       jp_pos=(0.05, 0.0, -0.1), jc_pos=(-0.15, 0.0, 0.3), mass=0.9,
+                       inertia=_box_inertia(0.9, 0.15, 0.1, 0.3)))
+    w.push_link(M.Link(parent=1, joint=M.JOINT_SLIDE, axis=normalize((0.2, 1.0, 0.4)), armature=0.05,
+                       jp_pos=(0.0, 0.0, -0.3), jc_pos=(0.1, -0.2, 0.15), mass=0.7,
+                       inertia=_box_inertia(0.7, 0.1, 0.2, 0.15)))
+    w.push_link(M.Link(parent=2, joint=M.JOINT_BALL, armature=0.01, jp_pos=(0.1, -0.2, -0.15),
+                       jc_pos=(-0.05, 0.1, 0.2), mass=0.5, inertia=M._diag9(0.02, 0.03, 0.04)))
+    ball = _renormalize(quat_from_axis_angle(normalize((0.4, 1.0, -0.3)), 0.55))
+    q_native = np.array([0.35, 0.12] + ball, dtype=np.float32)
+    return w, q_native
+
+
+def test_mass_matrix_golden_is_byte_identical():
+    """CRB mass matrix part of newt/tests/goldens/dynamics_mass_bias.bin."""
+    w, q = _mixed_tree()
+    packed = M.PackedModels([w])
+    got = oracle_py.mass_matrix(packed, 0, q, 5, precision=0).astype(np.float32)
+    gold = _read_f32("dynamics_mass_bias.bin")[:25].reshape(5, 5)
+    assert got.tobytes() == gold.tobytes(), np.abs(got - gold).max()
+
+
+def read_newtdif(name):
+    """NEWTDIF1 reader (newt/tests/differential.rs:239-301)."""
+    import struct
+    d = open(os.path.join(GOLD, name), "rb").read()
+    assert d[:8] == b"NEWTDIF1"
+    n = struct.unpack("<I", d[8:12])[0]
+    o = 12 + n
+    nq, nv, stride, ns, nsteps = struct.unpack("<5I", d[o:o + 20])
+    o += 20
+    steps, qpos, qvel = [], [], []
+    for _ in range(ns):
+        steps.append(struct.unpack("<I", d[o:o + 4])[0]); o += 4
+        qpos.append(np.frombuffer(d, "<f8", nq, o)); o += 8 * nq
+        qvel.append(np.frombuffer(d, "<f8", nv, o)); o += 8 * nv
+    return dict(stride=stride, n_steps=nsteps, steps=steps, qpos=np.array(qpos), qvel=np.array(qvel))
+
+
+def _double_pendulum():
+    """tests/references/double_pendulum.xml as newt's MJCF loader builds it
+    (newt/src/mjcf.rs:1079-1110 root, :1258-1262 joint offsets)."""
+    w = M.WorldModel(dt=0.002, gravity=(0.0, 0.0, -9.81), solver=M.SOLVER_PGS, iterations=20)
+    w.push_link(M.Link(parent=-1, joint=M.JOINT_FIXED, jp_pos=(0.0, 0.0, 1.5), mass=1.0,
+                       inertia=M._diag9(1.0, 1.0, 1.0)))
+    w.push_link(M.Link(parent=0, joint=M.JOINT_HINGE, axis=(1.0, 0.0, 0.0),
+                       jp_pos=(0.0, 0.0, float(f32(-0.45) + f32(0.45))), jc_pos=(0.0, 0.0, 0.45), mass=1.3,
+                       inertia=M._diag9(0.08775, 0.08775, 1e-6)))
+    w.push_link(M.Link(parent=1, joint=M.JOINT_HINGE, axis=(1.0, 0.0, 0.0),
+                       jp_pos=(0.0, 0.0, float(f32(-0.75) + f32(0.3))), jc_pos=(0.0, 0.0, 0.3), mass=0.7,
+                       inertia=M._diag9(0.021, 0.021, 1e-6)))
+    return w
+
+
+@pytest.mark.parametrize("precision,qtol,vtol", [(0, 4.0e-7, 1.0e-6), (1, 4.0e-7, 1.0e-6)])
+def test_double_pendulum_euler_matches_mujoco_capture(precision, qtol, vtol):
+    """Matched-Euler row of newt/tests/differential.rs:1594-1599 (window :1281-1284)."""
+    ref = read_newtdif("double_pendulum_euler.bin")
+    packed = M.PackedModels([_double_pendulum()])
+    qpos = np.array([0.35, -0.15], np.float32)
+    qvel = np.zeros(2, np.float32)
+    worst_q = worst_v = 0.0
+    for k, step in enumerate(ref["steps"]):
+        qo, vo = oracle_py.run(packed, np.zeros(1, np.int32), qpos, qvel, None, step, precision=precision)
+        worst_q = max(worst_q, np.abs(qo - ref["qpos"][k]).max())
+        worst_v = max(worst_v, np.abs(vo - ref["qvel"][k]).max())
+    assert worst_q <= qtol and worst_v <= vtol, (worst_q, worst_v)

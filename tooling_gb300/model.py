@@ -1,0 +1,216 @@
+"""Host-side model description for the newt GPU C ABI (include/newt_gpu.h).
+
+The ctypes structures below are the exact layout of ``newt_link_desc``,
+``newt_body_desc``, ``newt_geom_desc`` and ``newt_model_desc``.  ``WorldModel``
+is a small builder that mirrors how a newt ``World`` is assembled
+(``World::add_body`` / ``add_tree`` / ``add_geom``, newt/src/world.rs:950-981;
+``Tree::push_link``, newt/src/tree.rs:275-331; the ``Geom`` constructors,
+newt/src/geom.rs:494-760), so a scene written against newt reads the same
+here.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+JOINT_FREE, JOINT_FIXED, JOINT_HINGE, JOINT_SLIDE, JOINT_BALL = 0, 1, 2, 3, 4
+SHAPE_PLANE, SHAPE_SPHERE, SHAPE_BOX, SHAPE_CAPSULE = 0, 1, 2, 3
+SOLVER_PGS, SOLVER_NEWTON = 1, 2
+JOINT_NQ = {JOINT_FREE: 7, JOINT_FIXED: 0, JOINT_HINGE: 1, JOINT_SLIDE: 1, JOINT_BALL: 4}
+JOINT_NV = {JOINT_FREE: 6, JOINT_FIXED: 0, JOINT_HINGE: 1, JOINT_SLIDE: 1, JOINT_BALL: 3}
+
+
+class LinkDesc(C.Structure):
+    _fields_ = [
+        ("parent", C.c_int32), ("joint", C.c_int32), ("axis", C.c_float * 3),
+        ("damping", C.c_float), ("armature", C.c_float), ("free_damping", C.c_float),
+        ("jp_pos", C.c_float * 3), ("jp_quat", C.c_float * 4),
+        ("jc_pos", C.c_float * 3), ("jc_quat", C.c_float * 4),
+        ("mass", C.c_float), ("inertia", C.c_float * 9),
+    ]
+
+
+class BodyDesc(C.Structure):
+    _fields_ = [("mass", C.c_float), ("inertia", C.c_float * 9)]
+
+
+class GeomDesc(C.Structure):
+    _fields_ = [
+        ("shape", C.c_int32), ("body", C.c_int32), ("link", C.c_int32), ("size", C.c_float * 3),
+        ("local_pos", C.c_float * 3), ("local_quat", C.c_float * 4), ("friction", C.c_float),
+        ("solref", C.c_float * 2), ("solimp", C.c_float * 5), ("margin", C.c_float), ("gap", C.c_float),
+        ("condim", C.c_int32), ("group", C.c_uint32), ("mask", C.c_uint32),
+    ]
+
+
+class ModelDesc(C.Structure):
+    _fields_ = [
+        ("n_links", C.c_int32), ("n_bodies", C.c_int32), ("n_geoms", C.c_int32),
+        ("links", C.POINTER(LinkDesc)), ("bodies", C.POINTER(BodyDesc)), ("geoms", C.POINTER(GeomDesc)),
+        ("dt", C.c_float), ("gravity", C.c_float * 3), ("solver", C.c_int32), ("iterations", C.c_int32),
+        ("tree_self_collision", C.c_int32),
+    ]
+
+
+def _diag9(a, b, c):
+    return [a, 0.0, 0.0, 0.0, b, 0.0, 0.0, 0.0, c]
+
+
+def solid_sphere_inertia(mass: float, r: float) -> List[float]:
+    """newt/src/geom.rs:934-937 (evaluated in f32)."""
+    f = np.float32
+    i = f(f(f(f(2.0) / f(5.0)) * f(mass)) * f(r)) * f(r)
+    return _diag9(i, i, i)
+
+
+def solid_box_inertia(mass: float, h: Sequence[float]) -> List[float]:
+    """newt/src/geom.rs:939-947 (evaluated in f32)."""
+    f = np.float32
+    hx2, hy2, hz2 = f(h[0]) * f(h[0]), f(h[1]) * f(h[1]), f(h[2]) * f(h[2])
+    m3 = f(mass) / f(3.0)
+    return _diag9(m3 * (hy2 + hz2), m3 * (hx2 + hz2), m3 * (hx2 + hy2))
+
+
+def solid_capsule_inertia(mass: float, radius: float, half_height: float) -> List[float]:
+    """newt/src/geom.rs:949-966 (evaluated in f32)."""
+    f = np.float32
+    r, h, m = f(radius), f(half_height), f(mass)
+    vol_cyl = r * r * (f(2.0) * h)
+    vol_caps = (f(4.0) / f(3.0)) * r * r * r
+    total = vol_cyl + vol_caps
+    m_c = m * (vol_cyl / total)
+    m_s = m - m_c
+    i_zz = f(0.5) * m_c * r * r + (f(2.0) / f(5.0)) * m_s * r * r
+    offset = h + f(3.0) / f(8.0) * r
+    hemi = (f(83.0) / f(320.0)) * m_s * r * r
+    i_xx = (f(1.0) / f(12.0)) * m_c * (f(3.0) * r * r + f(4.0) * h * h) + hemi + m_s * offset * offset
+    return _diag9(i_xx, i_xx, i_zz)
+
+
+@dataclass
+class Link:
+    parent: int
+    joint: int
+    axis: Sequence[float] = (0.0, 0.0, 1.0)
+    damping: float = 0.0
+    armature: float = 0.0
+    free_damping: float = 0.0
+    jp_pos: Sequence[float] = (0.0, 0.0, 0.0)
+    jp_quat: Sequence[float] = (0.0, 0.0, 0.0, 1.0)
+    jc_pos: Sequence[float] = (0.0, 0.0, 0.0)
+    jc_quat: Sequence[float] = (0.0, 0.0, 0.0, 1.0)
+    mass: float = 1.0
+    inertia: Sequence[float] = tuple(_diag9(1.0, 1.0, 1.0))
+
+
+@dataclass
+class Geom:
+    shape: int
+    body: int = -1
+    link: int = -1
+    size: Sequence[float] = (0.0, 0.0, 0.0)
+    local_pos: Sequence[float] = (0.0, 0.0, 0.0)
+    local_quat: Sequence[float] = (0.0, 0.0, 0.0, 1.0)
+    friction: float = 1.0
+    solref: Sequence[float] = (0.02, 1.0)
+    solimp: Sequence[float] = (0.9, 0.95, 0.001, 0.5, 2.0)
+    margin: float = 0.0
+    gap: float = 0.0
+    condim: int = 3
+    group: int = 0xFFFFFFFF
+    mask: int = 0xFFFFFFFF
+
+
+@dataclass
+class WorldModel:
+    """One world's model: at most one kinematic tree plus free bodies and geoms."""
+
+    dt: float = 0.005
+    gravity: Sequence[float] = (0.0, 0.0, -9.81)
+    solver: int = SOLVER_PGS
+    iterations: int = 20
+    tree_self_collision: int = 0
+    links: List[Link] = field(default_factory=list)
+    bodies: List[tuple] = field(default_factory=list)  # (mass, inertia9)
+    geoms: List[Geom] = field(default_factory=list)
+
+    def add_body(self, mass: float, inertia9: Sequence[float]) -> int:
+        self.bodies.append((float(mass), list(inertia9)))
+        return len(self.bodies) - 1
+
+    def push_link(self, link: Link) -> int:
+        self.links.append(link)
+        return len(self.links) - 1
+
+    def add_geom(self, g: Geom) -> int:
+        self.geoms.append(g)
+        return len(self.geoms) - 1
+
+    # MuJoCo-layout dimensions (include/newt_gpu.h header comment)
+    @property
+    def nq(self) -> int:
+        return 7 * len(self.bodies) + sum(JOINT_NQ[l.joint] for l in self.links)
+
+    @property
+    def nv(self) -> int:
+        return 6 * len(self.bodies) + sum(JOINT_NV[l.joint] for l in self.links)
+
+
+class PackedModels:
+    """ctypes arrays for a list of WorldModel, kept alive with the descriptors."""
+
+    def __init__(self, models: Sequence[WorldModel]):
+        self._keep = []
+        self.descs = (ModelDesc * len(models))()
+        for i, m in enumerate(models):
+            links = (LinkDesc * max(1, len(m.links)))()
+            for k, l in enumerate(m.links):
+                d = links[k]
+                d.parent, d.joint = l.parent, l.joint
+                d.axis[:] = list(l.axis)
+                d.damping, d.armature, d.free_damping = l.damping, l.armature, l.free_damping
+                d.jp_pos[:] = list(l.jp_pos); d.jp_quat[:] = list(l.jp_quat)
+                d.jc_pos[:] = list(l.jc_pos); d.jc_quat[:] = list(l.jc_quat)
+                d.mass = l.mass
+                d.inertia[:] = list(l.inertia)
+            bodies = (BodyDesc * max(1, len(m.bodies)))()
+            for k, (mass, inertia) in enumerate(m.bodies):
+                bodies[k].mass = mass
+                bodies[k].inertia[:] = list(inertia)
+            geoms = (GeomDesc * max(1, len(m.geoms)))()
+            for k, g in enumerate(m.geoms):
+                d = geoms[k]
+                d.shape, d.body, d.link = g.shape, g.body, g.link
+                d.size[:] = list(g.size)
+                d.local_pos[:] = list(g.local_pos); d.local_quat[:] = list(g.local_quat)
+                d.friction = g.friction
+                d.solref[:] = list(g.solref); d.solimp[:] = list(g.solimp)
+                d.margin, d.gap, d.condim = g.margin, g.gap, g.condim
+                d.group, d.mask = g.group & 0xFFFFFFFF, g.mask & 0xFFFFFFFF
+            self._keep += [links, bodies, geoms]
+            md = self.descs[i]
+            md.n_links, md.n_bodies, md.n_geoms = len(m.links), len(m.bodies), len(m.geoms)
+            md.links = C.cast(links, C.POINTER(LinkDesc))
+            md.bodies = C.cast(bodies, C.POINTER(BodyDesc))
+            md.geoms = C.cast(geoms, C.POINTER(GeomDesc))
+            md.dt = m.dt
+            md.gravity[:] = list(m.gravity)
+            md.solver, md.iterations = m.solver, m.iterations
+            md.tree_self_collision = m.tree_self_collision
+
+    def __len__(self) -> int:
+        return len(self.descs)
+
+
+def static_plane(point=(0.0, 0.0, 0.0), normal=(0.0, 0.0, 1.0), friction: float = 1.0) -> Geom:
+    """``Geom::static_plane`` (newt/src/geom.rs:494) for an upward normal."""
+    n = np.asarray(normal, dtype=np.float64)
+    n = n / np.linalg.norm(n)
+    if n[2] > 1.0 - 1e-6:
+        quat = (0.0, 0.0, 0.0, 1.0)
+    else:
+        raise ValueError("only +Z planes are used by this package's scenes")
+    return Geom(shape=SHAPE_PLANE, local_pos=tuple(point), local_quat=quat, friction=friction)
