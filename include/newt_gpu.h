@@ -26,6 +26,12 @@
 
 #include <stdint.h>
 
+#if defined(__GNUC__)
+#define NEWT_API __attribute__((visibility("default")))
+#else
+#define NEWT_API
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -119,31 +125,31 @@ typedef struct newt_gpu_opts {
 } newt_gpu_opts;
 
 /* Replaces building a `World` (newt/src/world.rs:325). */
-int newt_gpu_create(const newt_gpu_opts* opts, newt_gpu_ctx** out);
-int newt_gpu_destroy(newt_gpu_ctx* ctx);
-const char* newt_gpu_last_error(const newt_gpu_ctx* ctx);
+NEWT_API int newt_gpu_create(const newt_gpu_opts* opts, newt_gpu_ctx** out);
+NEWT_API int newt_gpu_destroy(newt_gpu_ctx* ctx);
+NEWT_API const char* newt_gpu_last_error(const newt_gpu_ctx* ctx);
 
 /* Replaces the loaders' `World::add_tree/add_body/add_geom`
  * (newt/src/world.rs:950-981): validates and copies `n` models to the device.
  * Rejects unsupported shape pairs with NEWT_E_UNSUPPORTED_PAIR (the
  * deferred-pair panic of newt/src/world.rs:874-894). */
-int newt_gpu_upload_models(newt_gpu_ctx* ctx, const newt_model_desc* models, int32_t n,
+NEWT_API int newt_gpu_upload_models(newt_gpu_ctx* ctx, const newt_model_desc* models, int32_t n,
                            int32_t* model_ids_out);
 /* MuJoCo-layout dimensions of a model: nq, nv (and nu = nv actuated DoF). */
-int newt_gpu_model_dims(const newt_gpu_ctx* ctx, int32_t model_id, int32_t* nq, int32_t* nv);
+NEWT_API int newt_gpu_model_dims(const newt_gpu_ctx* ctx, int32_t model_id, int32_t* nq, int32_t* nv);
 
 /* Allocate world slots for models (admission by the HBM budget). */
-int newt_gpu_alloc_worlds(newt_gpu_ctx* ctx, const int32_t* model_ids, int32_t n, int32_t* slots_out);
-int newt_gpu_free_worlds(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n);
+NEWT_API int newt_gpu_alloc_worlds(newt_gpu_ctx* ctx, const int32_t* model_ids, int32_t n, int32_t* slots_out);
+NEWT_API int newt_gpu_free_worlds(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n);
 
 /* State in/out, MuJoCo layout, the worlds' vectors concatenated in `slots`
  * order.  Mirrors `World::apply_mujoco_qpos/qvel` (newt/src/world.rs:519-623). */
-int newt_gpu_set_state(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, const float* qpos,
+NEWT_API int newt_gpu_set_state(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, const float* qpos,
                        const float* qvel);
-int newt_gpu_get_state(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, float* qpos, float* qvel);
+NEWT_API int newt_gpu_get_state(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, float* qpos, float* qvel);
 /* Generalised applied forces (`Tree::qfrc_applied`, newt/src/tree.rs:207),
  * nv per world, concatenated; persists across steps like newt's field. */
-int newt_gpu_set_qfrc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, const float* qfrc);
+NEWT_API int newt_gpu_set_qfrc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, const float* qfrc);
 
 /* Replaces `World::step()` (newt/src/world.rs:1459) for every live world.
  * mode NEWT_STEP_PLAIN: one launch per stage per step, fixed tiles.
@@ -151,34 +157,34 @@ int newt_gpu_set_qfrc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, const 
  *   worlds pulled from a size-class-sorted queue, captured in a CUDA graph. */
 #define NEWT_STEP_PLAIN 0
 #define NEWT_STEP_BATCHED 1
-int newt_gpu_step(newt_gpu_ctx* ctx, int32_t n_steps, int32_t mode);
+NEWT_API int newt_gpu_step(newt_gpu_ctx* ctx, int32_t n_steps, int32_t mode);
 /* Waits for the context's stream (bounded host wait; NEWT_E_TIMEOUT). */
-int newt_gpu_sync(newt_gpu_ctx* ctx, int32_t timeout_ms);
+NEWT_API int newt_gpu_sync(newt_gpu_ctx* ctx, int32_t timeout_ms);
 
 /* Per-world status words (NEWT_WS_*), accumulated since the last clear. */
-int newt_gpu_world_status(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, uint32_t* status,
+NEWT_API int newt_gpu_world_status(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, uint32_t* status,
                           int32_t clear);
 
 /* ---- diagnostics (parity surfaces) -------------------------------------- */
 /* Generalised acceleration of the last step, newt layout (qdot order), nv per
  * world.  Mirrors the qacc that `euler_step_with_workspace` integrates
  * (newt/src/tree.rs:1406-1417). */
-int newt_gpu_get_qacc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, float* qacc);
+NEWT_API int newt_gpu_get_qacc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, float* qacc);
 /* Contacts detected at the start of the last step for one world:
  * per contact (geom_a, geom_b) pairs into `pairs` (2*cap ints) and
  * pos xyz, normal xyz, penetration into `data` (7*cap floats). */
-int newt_gpu_get_contacts(newt_gpu_ctx* ctx, int32_t slot, int32_t cap, int32_t* n_out,
+NEWT_API int newt_gpu_get_contacts(newt_gpu_ctx* ctx, int32_t slot, int32_t cap, int32_t* n_out,
                           int32_t* pairs, float* data);
 /* Row impulses of the last step's constraint solve for one world, in the
  * solver's row order (4 pyramidal facet rows per contact). */
-int newt_gpu_get_impulses(newt_gpu_ctx* ctx, int32_t slot, int32_t cap, int32_t* n_out, float* impulses);
+NEWT_API int newt_gpu_get_impulses(newt_gpu_ctx* ctx, int32_t slot, int32_t cap, int32_t* n_out, float* impulses);
 
 /* ---- timing helpers for the benchmark (CUDA events on the ctx stream) ---- */
-int newt_gpu_event_record(newt_gpu_ctx* ctx, int32_t which);          /* which: 0 start, 1 stop */
-int newt_gpu_event_elapsed_ms(newt_gpu_ctx* ctx, float* ms);
-int newt_gpu_flush_l2(newt_gpu_ctx* ctx);                              /* writes a buffer > L2 */
+NEWT_API int newt_gpu_event_record(newt_gpu_ctx* ctx, int32_t which);          /* which: 0 start, 1 stop */
+NEWT_API int newt_gpu_event_elapsed_ms(newt_gpu_ctx* ctx, float* ms);
+NEWT_API int newt_gpu_flush_l2(newt_gpu_ctx* ctx);                              /* writes a buffer > L2 */
 /* Kernel launches issued by this context since creation. */
-int64_t newt_gpu_launch_count(const newt_gpu_ctx* ctx);
+NEWT_API int64_t newt_gpu_launch_count(const newt_gpu_ctx* ctx);
 
 #ifdef __cplusplus
 }

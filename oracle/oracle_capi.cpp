@@ -319,6 +319,38 @@ int oracle_mass_matrix(const newt_model_desc* d, const float* q_native, int prec
   return 0;
 }
 
+// Total mechanical energy (kinetic + gravitational potential) of each world
+// at the given MuJoCo-layout state, in FP64: 0.5 qd^T M qd - sum m g.p for
+// the tree (CRB mass matrix, FK positions) plus 0.5 m v^2 + 0.5 w.Iw - m g.p
+// for free bodies.
+int oracle_energy(const newt_model_desc* models, int n_worlds, const int* model_of_world, const float* qpos,
+                  const float* qvel, double* out) {
+  long qo = 0, vo = 0;
+  for (int w = 0; w < n_worlds; ++w) {
+    const newt_model_desc& d = models[model_of_world[w]];
+    int nq, nv; dims(d, &nq, &nv);
+    World<double> wd = build_world<double>(d);
+    set_state(wd, qpos + qo, qvel + vo, 0);
+    double e = 0.0;
+    for (const Body<double>& b : wd.bodies) {
+      Vec3<double> iw = b.inertia * b.omega_body;
+      e += 0.5 * b.mass * b.vel.dot(b.vel) + 0.5 * b.omega_body.dot(iw) - b.mass * wd.gravity.dot(b.pos);
+    }
+    for (const Tree<double>& t : wd.trees) {
+      std::vector<double> M;
+      mass_matrix(t, M);
+      int n = t.nv();
+      for (int i = 0; i < n; ++i) for (int j = 0; j < n; ++j) e += 0.5 * t.qdot[i] * M[i * n + j] * t.qdot[j];
+      std::vector<Pose<double>> poses;
+      forward_kinematics(t, poses);
+      for (size_t i = 0; i < t.links.size(); ++i) e -= t.links[i].mass * wd.gravity.dot(poses[i].p);
+    }
+    out[w] = e;
+    qo += nq; vo += nv;
+  }
+  return 0;
+}
+
 // Raw f32 bits of newt's deterministic sin/cos (for the polynomial KATs).
 float oracle_newt_sin(float x) { return newt_sin(x); }
 float oracle_newt_cos(float x) { return newt_cos(x); }

@@ -103,6 +103,17 @@ def mass_matrix(packed, index: int, q_native: np.ndarray, nv: int, precision: in
     return out.reshape(nv, nv)
 
 
+def energy(packed, model_of_world, qpos, qvel) -> np.ndarray:
+    mow = np.ascontiguousarray(model_of_world, dtype=np.int32)
+    qpos = np.ascontiguousarray(qpos, dtype=np.float32)
+    qvel = np.ascontiguousarray(qvel, dtype=np.float32)
+    out = np.zeros(len(mow), np.float64)
+    L = lib()
+    L.oracle_energy.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.oracle_energy(C.cast(packed.descs, C.c_void_p), len(mow), _ptr(mow), _ptr(qpos), _ptr(qvel), _ptr(out))
+    return out
+
+
 def time_run(packed, model_of_world, qpos, qvel, qfrc, n_steps: int, n_threads: int) -> float:
     mow = np.ascontiguousarray(model_of_world, dtype=np.int32)
     qpos = np.ascontiguousarray(qpos, dtype=np.float32)

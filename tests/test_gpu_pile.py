@@ -1,0 +1,120 @@
+"""GPU parity for free-body contact worlds (pile workload) through the C ABI.
+
+Bars (stated here, checked below):
+  * contact pair lists identical to the FP64 oracle's wherever no
+    penetration lies within 1e-6 of the margin (ties at the activation
+    threshold may legitimately flip);
+  * PGS row impulses within 1e-3 relative (of the world's largest impulse) at
+    equal iteration counts;
+  * short-horizon trajectories within 1e-3 m / 1e-2 m/s.
+"""
+import numpy as np
+import pytest
+
+import oracle_py
+from tooling_gb300 import Engine, STEP_BATCHED, STEP_PLAIN, scenes
+
+pytestmark = pytest.mark.gpu
+
+IMPULSE_RTOL = 1e-3
+MARGIN_BAND = 1e-6
+
+
+@pytest.fixture(scope="module")
+def eng():
+    from tooling_gb300 import build as B
+    B.build()
+    e = Engine(device=0)
+    yield e
+    e.close()
+
+
+@pytest.fixture(scope="module")
+def settled():
+    """Pile worlds advanced 300 steps by the FP64 oracle: a state with
+    resting, stacked and sliding contacts."""
+    b = scenes.pile_batch(n_worlds=48, first_world=500)
+    rq, rv = oracle_py.run(b, np.arange(len(b)), b.qpos, b.qvel, None, 300, precision=1)
+    b.qpos[:] = rq.astype(np.float32)
+    b.qvel[:] = rv.astype(np.float32)
+    return b
+
+
+def _load(eng, b):
+    ids = eng.upload(b)
+    slots = eng.alloc(ids)
+    eng.set_state(slots, b.qpos, b.qvel)
+    return slots
+
+
+@pytest.mark.parametrize("mode", [STEP_PLAIN, STEP_BATCHED])
+def test_contact_pair_lists_match_oracle(eng, settled, mode):
+    b = settled
+    slots = _load(eng, b)
+    eng.step(1, mode)
+    eng.sync()
+    total = 0
+    for w in range(len(b)):
+        qp = b.qpos[b.q_off[w]:b.q_off[w] + b.nq[w]]
+        qv = b.qvel[b.v_off[w]:b.v_off[w] + b.nv[w]]
+        rp, rd = oracle_py.contacts(b, w, qp, qv)
+        gp, gd = eng.contacts(int(slots[w]))
+        near = np.abs(rd[:, 6]) < MARGIN_BAND if len(rd) else np.zeros(0, bool)
+        if near.any():
+            continue
+        assert gp.tolist() == rp.tolist(), f"world {w}"
+        if len(rd):
+            assert np.abs(gd[:, 6] - rd[:, 6]).max() < 1e-4
+            assert np.abs(gd[:, 3:6] - rd[:, 3:6]).max() < 1e-3
+        total += len(rp)
+    assert total > 100
+    eng.free(slots)
+
+
+def test_pgs_impulses_match_oracle_at_equal_iterations(eng, settled):
+    b = settled
+    slots = _load(eng, b)
+    eng.step(1, STEP_BATCHED)
+    eng.sync()
+    worst = 0.0
+    for w in range(len(b)):
+        qp = b.qpos[b.q_off[w]:b.q_off[w] + b.nq[w]]
+        qv = b.qvel[b.v_off[w]:b.v_off[w] + b.nv[w]]
+        rp, rd = oracle_py.contacts(b, w, qp, qv)
+        if len(rd) and (np.abs(rd[:, 6]) < MARGIN_BAND).any():
+            continue
+        ref = oracle_py.impulses(b, w, qp, qv)
+        gimp = eng.impulses(int(slots[w])).reshape(-1, 4)
+        active = rd[:, 6] > 0 if len(rd) else np.zeros(0, bool)
+        g = gimp[active].reshape(-1)
+        assert len(g) == len(ref), f"world {w}"
+        if len(ref):
+            worst = max(worst, np.abs(g - ref).max() / max(1e-9, np.abs(ref).max()))
+    assert worst <= IMPULSE_RTOL, worst
+    eng.free(slots)
+
+
+def test_short_trajectory_tracks_oracle(eng, settled):
+    b = settled
+    slots = _load(eng, b)
+    eng.step(20, STEP_BATCHED)
+    qp, qv = eng.get_state(slots, int(b.nq.sum()), int(b.nv.sum()))
+    rq, rv = oracle_py.run(b, np.arange(len(b)), b.qpos, b.qvel, None, 20, precision=1)
+    assert np.abs(qp - rq).max() < 1e-3
+    assert np.abs(qv - rv).max() < 1e-2
+    st = eng.status(slots)
+    assert not (st & 0x5).any()  # no NaN, no contact overflow
+    eng.free(slots)
+
+
+def test_plain_and_batched_agree(eng, settled):
+    b = settled
+    s1 = _load(eng, b)
+    eng.step(10, STEP_PLAIN)
+    q1, v1 = eng.get_state(s1, int(b.nq.sum()), int(b.nv.sum()))
+    eng.free(s1)
+    s2 = _load(eng, b)
+    eng.step(10, STEP_BATCHED)
+    q2, v2 = eng.get_state(s2, int(b.nq.sum()), int(b.nv.sum()))
+    eng.free(s2)
+    assert np.abs(q1 - q2).max() < 1e-5 and np.abs(v1 - v2).max() < 1e-4

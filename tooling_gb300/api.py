@@ -1,0 +1,207 @@
+"""Python host binding of the newt GPU C ABI (include/newt_gpu.h).
+
+This is a thin ctypes layer: every call goes straight to ``libnewt_gpu.so``.
+There is no CPU fallback; constructing an :class:`Engine` without the built
+library or without a CUDA device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import model as M
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libnewt_gpu.so")
+
+OK = 0
+ERRORS = {1: "NEWT_E_INVALID", 2: "NEWT_E_UNSUPPORTED_PAIR", 3: "NEWT_E_NOT_PD", 4: "NEWT_E_OVERFLOW",
+          5: "NEWT_E_TIMEOUT", 6: "NEWT_E_CUDA", 7: "NEWT_E_NOMEM", 8: "NEWT_E_NOT_FINITE"}
+STEP_PLAIN, STEP_BATCHED = 0, 1
+WS_NONFINITE, WS_NOT_PD, WS_CONTACT_OVERFLOW, WS_ITER_CAP, WS_FP64_FALLBACK = 0x1, 0x2, 0x4, 0x8, 0x10
+
+EXPORTED = [
+    "newt_gpu_create", "newt_gpu_destroy", "newt_gpu_last_error", "newt_gpu_upload_models", "newt_gpu_model_dims",
+    "newt_gpu_alloc_worlds", "newt_gpu_free_worlds", "newt_gpu_set_state", "newt_gpu_get_state",
+    "newt_gpu_set_qfrc", "newt_gpu_step", "newt_gpu_sync", "newt_gpu_world_status", "newt_gpu_get_qacc",
+    "newt_gpu_get_contacts", "newt_gpu_get_impulses", "newt_gpu_event_record", "newt_gpu_event_elapsed_ms",
+    "newt_gpu_flush_l2", "newt_gpu_launch_count",
+]
+
+
+class NewtError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Opts(C.Structure):
+    _fields_ = [("device", C.c_int32), ("max_worlds", C.c_int32), ("hbm_budget_bytes", C.c_uint64)]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load the shared library (never builds; call ``tooling_gb300.build.build()``)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: run tooling_gb300.build.build() first (no CPU fallback)")
+    L = C.CDLL(path)
+    P, I32 = C.c_void_p, C.c_int32
+    sig = {
+        "newt_gpu_create": ([P, P], C.c_int),
+        "newt_gpu_destroy": ([P], C.c_int),
+        "newt_gpu_last_error": ([P], C.c_char_p),
+        "newt_gpu_upload_models": ([P, P, I32, P], C.c_int),
+        "newt_gpu_model_dims": ([P, I32, P, P], C.c_int),
+        "newt_gpu_alloc_worlds": ([P, P, I32, P], C.c_int),
+        "newt_gpu_free_worlds": ([P, P, I32], C.c_int),
+        "newt_gpu_set_state": ([P, P, I32, P, P], C.c_int),
+        "newt_gpu_get_state": ([P, P, I32, P, P], C.c_int),
+        "newt_gpu_set_qfrc": ([P, P, I32, P], C.c_int),
+        "newt_gpu_step": ([P, I32, I32], C.c_int),
+        "newt_gpu_sync": ([P, I32], C.c_int),
+        "newt_gpu_world_status": ([P, P, I32, P, I32], C.c_int),
+        "newt_gpu_get_qacc": ([P, P, I32, P], C.c_int),
+        "newt_gpu_get_contacts": ([P, I32, I32, P, P, P], C.c_int),
+        "newt_gpu_get_impulses": ([P, I32, I32, P, P], C.c_int),
+        "newt_gpu_event_record": ([P, I32], C.c_int),
+        "newt_gpu_event_elapsed_ms": ([P, P], C.c_int),
+        "newt_gpu_flush_l2": ([P], C.c_int),
+        "newt_gpu_launch_count": ([P], C.c_int64),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _p(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Engine:
+    """One context = one CUDA stream on one device (not thread-safe)."""
+
+    def __init__(self, device: int = 0, max_worlds: int = 0, hbm_budget_bytes: int = 0):
+        self.L = load_library()
+        self.ctx = C.c_void_p()
+        o = Opts(device, max_worlds, hbm_budget_bytes)
+        rc = self.L.newt_gpu_create(C.byref(o), C.byref(self.ctx))
+        if rc != OK:
+            raise NewtError(rc, "newt_gpu_create failed (is a CUDA device visible?)")
+        self._dims = {}
+
+    def _ck(self, rc: int):
+        if rc != OK:
+            raise NewtError(rc, self.L.newt_gpu_last_error(self.ctx).decode())
+
+    def close(self):
+        if self.ctx:
+            self.L.newt_gpu_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- models / worlds ----------------------------------------------------
+    def upload(self, packed: "M.PackedModels") -> np.ndarray:
+        ids = np.zeros(len(packed), np.int32)
+        self._ck(self.L.newt_gpu_upload_models(self.ctx, C.cast(packed.descs, C.c_void_p), len(packed), _p(ids)))
+        return ids
+
+    def dims(self, model_id: int):
+        if model_id not in self._dims:
+            nq, nv = C.c_int32(), C.c_int32()
+            self._ck(self.L.newt_gpu_model_dims(self.ctx, int(model_id), C.byref(nq), C.byref(nv)))
+            self._dims[model_id] = (nq.value, nv.value)
+        return self._dims[model_id]
+
+    def alloc(self, model_ids: Sequence[int]) -> np.ndarray:
+        ids = np.ascontiguousarray(model_ids, np.int32)
+        slots = np.zeros(len(ids), np.int32)
+        self._ck(self.L.newt_gpu_alloc_worlds(self.ctx, _p(ids), len(ids), _p(slots)))
+        return slots
+
+    def free(self, slots: Sequence[int]):
+        s = np.ascontiguousarray(slots, np.int32)
+        self._ck(self.L.newt_gpu_free_worlds(self.ctx, _p(s), len(s)))
+
+    # -- state --------------------------------------------------------------
+    def set_state(self, slots, qpos: np.ndarray, qvel: np.ndarray):
+        s = np.ascontiguousarray(slots, np.int32)
+        qp = np.ascontiguousarray(qpos, np.float32)
+        qv = np.ascontiguousarray(qvel, np.float32)
+        self._ck(self.L.newt_gpu_set_state(self.ctx, _p(s), len(s), _p(qp), _p(qv)))
+
+    def get_state(self, slots, nq_total: int, nv_total: int):
+        s = np.ascontiguousarray(slots, np.int32)
+        qp = np.zeros(nq_total, np.float32)
+        qv = np.zeros(nv_total, np.float32)
+        self._ck(self.L.newt_gpu_get_state(self.ctx, _p(s), len(s), _p(qp), _p(qv)))
+        return qp, qv
+
+    def set_qfrc(self, slots, qfrc: np.ndarray):
+        s = np.ascontiguousarray(slots, np.int32)
+        q = np.ascontiguousarray(qfrc, np.float32)
+        self._ck(self.L.newt_gpu_set_qfrc(self.ctx, _p(s), len(s), _p(q)))
+
+    def get_qacc(self, slots, nv_total: int) -> np.ndarray:
+        s = np.ascontiguousarray(slots, np.int32)
+        out = np.zeros(nv_total, np.float32)
+        self._ck(self.L.newt_gpu_get_qacc(self.ctx, _p(s), len(s), _p(out)))
+        return out
+
+    # -- stepping -------------------------------------------------------------
+    def step(self, n_steps: int = 1, mode: int = STEP_BATCHED):
+        self._ck(self.L.newt_gpu_step(self.ctx, int(n_steps), int(mode)))
+
+    def sync(self, timeout_ms: int = 600000):
+        self._ck(self.L.newt_gpu_sync(self.ctx, int(timeout_ms)))
+
+    def status(self, slots, clear: bool = False) -> np.ndarray:
+        s = np.ascontiguousarray(slots, np.int32)
+        out = np.zeros(len(s), np.uint32)
+        self._ck(self.L.newt_gpu_world_status(self.ctx, _p(s), len(s), _p(out), int(clear)))
+        return out
+
+    # -- diagnostics ----------------------------------------------------------
+    def contacts(self, slot: int, cap: int = 1024):
+        n = C.c_int32()
+        pairs = np.zeros(2 * cap, np.int32)
+        data = np.zeros(7 * cap, np.float32)
+        self._ck(self.L.newt_gpu_get_contacts(self.ctx, int(slot), cap, C.byref(n), _p(pairs), _p(data)))
+        k = min(n.value, cap)
+        return pairs[: 2 * k].reshape(k, 2), data[: 7 * k].reshape(k, 7)
+
+    def impulses(self, slot: int, cap: int = 4096) -> np.ndarray:
+        n = C.c_int32()
+        out = np.zeros(cap, np.float32)
+        self._ck(self.L.newt_gpu_get_impulses(self.ctx, int(slot), cap, C.byref(n), _p(out)))
+        return out[: min(n.value, cap)]
+
+    # -- timing ---------------------------------------------------------------
+    def event(self, which: int):
+        self._ck(self.L.newt_gpu_event_record(self.ctx, int(which)))
+
+    def elapsed_ms(self) -> float:
+        ms = C.c_float()
+        self._ck(self.L.newt_gpu_event_elapsed_ms(self.ctx, C.byref(ms)))
+        return ms.value
+
+    def flush_l2(self):
+        self._ck(self.L.newt_gpu_flush_l2(self.ctx))
+
+    def launch_count(self) -> int:
+        return int(self.L.newt_gpu_launch_count(self.ctx))

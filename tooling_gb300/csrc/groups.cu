@@ -1,0 +1,524 @@
+// World-group storage: row layouts, host mirrors, growth, model/state
+// staging and MuJoCo <-> newt state conversion
+// (newt/src/world.rs:519-623 apply_mujoco_qpos/qvel;
+//  newt/tests/differential.rs:548-640 the inverse mapping).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "runtime.h"
+
+#define CKG(call)                                                               \
+  do {                                                                          \
+    cudaError_t e_ = (call);                                                    \
+    if (e_ != cudaSuccess) { ctx->err = std::string(#call ": ") + cudaGetErrorString(e_); return NEWT_E_CUDA; } \
+  } while (0)
+
+static void q_rotT(const float q[4], const float v[3], float o[3]) {  // R(q)^T v
+  float x = -q[0], y = -q[1], z = -q[2], w = q[3];
+  float tx = 2.f * (y * v[2] - z * v[1]), ty = 2.f * (z * v[0] - x * v[2]), tz = 2.f * (x * v[1] - y * v[0]);
+  o[0] = v[0] + w * tx + (y * tz - z * ty);
+  o[1] = v[1] + w * ty + (z * tx - x * tz);
+  o[2] = v[2] + w * tz + (x * ty - y * tx);
+}
+static void q_rot(const float q[4], const float v[3], float o[3]) {
+  float c[4] = {-q[0], -q[1], -q[2], q[3]};
+  q_rotT(c, v, o);
+}
+static void q_norm(float q[4]) {
+  float n = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  if (n == 0.f) { q[0] = q[1] = q[2] = 0.f; q[3] = 1.f; return; }
+  for (int k = 0; k < 4; ++k) q[k] /= n;
+}
+static void sym6(const float m9[9], float* o) {  // column-major 3x3 -> xx yy zz xy xz yz
+  o[0] = m9[0]; o[1] = m9[4]; o[2] = m9[8]; o[3] = m9[3]; o[4] = m9[6]; o[5] = m9[7];
+}
+static bool inv6(const float m9[9], float* o) {
+  double a = m9[0], b = m9[3], c = m9[6], d = m9[1], e = m9[4], f = m9[7], g = m9[2], h = m9[5], i = m9[8];
+  double det = a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
+  if (det == 0.0 || !std::isfinite(det)) return false;
+  double inv = 1.0 / det;
+  o[0] = (float)((e * i - f * h) * inv); o[1] = (float)((a * i - c * g) * inv); o[2] = (float)((a * e - b * d) * inv);
+  o[3] = (float)((c * h - b * i) * inv); o[4] = (float)((b * f - c * e) * inv); o[5] = (float)((c * d - a * f) * inv);
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// layout
+// ---------------------------------------------------------------------------
+static void tree_rows(HostGroup& g) {
+  const int L = g.size;
+  size_t r = 0;
+  g.r_axis = r; r += 3 * L;
+  g.r_jp = r; r += 3 * L;
+  g.r_jc = r; r += 3 * L;
+  g.r_rootq = r; r += 4;
+  g.r_mass = r; r += L;
+  g.r_inert = r; r += 6 * L;
+  g.r_damp = r; r += L;
+  g.r_arm = r; r += L;
+  g.r_dtg = r; r += 4;
+  g.r_q = r; r += g.nq;
+  g.r_qd = r; r += g.nv;
+  g.r_qfrc = r; r += g.nv;
+  g.r_qacc = r; r += g.nv;
+  g.frows = r;
+  g.ri_solver = 0; g.ri_live = 1; g.ri_status = 2;
+  g.irows = 3;
+}
+
+static int pile_maxc(int nb, int np) {
+  int c = 6 * nb + 4 * nb * np;
+  c = (c + 31) / 32 * 32;
+  return std::min(std::max(c, 64), 512);
+}
+
+static void pile_rows(HostGroup& g) {
+  const int nb = g.size, np = g.np, ng = nb + np;
+  g.maxc = pile_maxc(nb, np);
+  PileLayout& l = g.lay;
+  int r = 0;
+  l.mass = r; r += nb;
+  l.inert = r; r += 6 * nb;
+  l.iinv = r; r += 6 * nb;
+  l.size = r; r += 3 * nb;
+  l.gpos = r; r += 3 * nb;
+  l.gquat = r; r += 4 * nb;
+  l.fric = r; r += ng;
+  l.margin = r; r += ng;
+  l.soft = r; r += 7;
+  l.plane = r; r += 7 * np;
+  l.dtg = r; r += 4;
+  r = (r + 3) / 4 * 4;
+  l.pos = r; r += 3 * nb;
+  l.quat = r; r += 4 * nb;
+  l.vel = r; r += 3 * nb;
+  l.omg = r; r += 3 * nb;
+  r = (r + 3) / 4 * 4;
+  l.cdata = r; r += 7 * g.maxc;
+  l.imp = r; r += 4 * g.maxc;
+  r = (r + 31) / 32 * 32;
+  l.fstride = r;
+  int q = 0;
+  l.shape = q; q += nb;
+  l.gent = q; q += ng;
+  l.iters = q; q += 1;
+  l.status = q; q += 1;
+  l.ncon = q; q += 1;
+  l.live = q; q += 1;
+  l.cpair = q; q += 2 * g.maxc;
+  q = (q + 31) / 32 * 32;
+  l.istride = q;
+  g.frows = l.fstride;
+  g.irows = l.istride;
+}
+
+size_t HostGroup::bytes_per_world() const { return frows * sizeof(float) + irows * sizeof(int); }
+
+// ---------------------------------------------------------------------------
+// capacity
+// ---------------------------------------------------------------------------
+static int grow(newt_gpu_ctx* ctx, HostGroup& g, int need) {
+  if (g.frows == 0) {
+    if (g.kind == GK_TREE) tree_rows(g);
+    else if (g.kind == GK_PILE) pile_rows(g);
+  }
+  if (need <= g.cap) return NEWT_OK;
+  int ncap = std::max(need, std::max(64, g.cap * 2));
+  if (ncap > ctx->max_worlds) ncap = std::max(need, ctx->max_worlds);
+  uint64_t add = (uint64_t)(ncap - g.cap) * g.bytes_per_world();
+  if (ctx->used + add > ctx->budget) {
+    ctx->err = "HBM admission budget exhausted";
+    return NEWT_E_NOMEM;
+  }
+  std::vector<float> nF(g.frows * (size_t)ncap, 0.f);
+  std::vector<int> nI(g.irows * (size_t)ncap, 0);
+  if (g.kind == GK_TREE) {
+    for (size_t r = 0; r < g.frows; ++r)
+      for (int w = 0; w < g.cap; ++w) nF[r * ncap + w] = g.hF[r * g.cap + w];
+    for (size_t r = 0; r < g.irows; ++r)
+      for (int w = 0; w < g.cap; ++w) nI[r * ncap + w] = g.hI[r * g.cap + w];
+  } else {
+    std::copy(g.hF.begin(), g.hF.end(), nF.begin());
+    std::copy(g.hI.begin(), g.hI.end(), nI.begin());
+  }
+  // device: pull the current device contents into the new host mirror first
+  if (g.dF && g.n > 0) {
+    std::vector<float> cur(g.frows * (size_t)g.cap);
+    std::vector<int> curI(g.irows * (size_t)g.cap);
+    CKG(cudaStreamSynchronize(ctx->stream));
+    CKG(cudaMemcpy(cur.data(), g.dF, cur.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    CKG(cudaMemcpy(curI.data(), g.dI, curI.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    if (g.kind == GK_TREE) {
+      for (size_t r = 0; r < g.frows; ++r)
+        for (int w = 0; w < g.cap; ++w) nF[r * ncap + w] = cur[r * g.cap + w];
+      for (size_t r = 0; r < g.irows; ++r)
+        for (int w = 0; w < g.cap; ++w) nI[r * ncap + w] = curI[r * g.cap + w];
+    } else {
+      std::copy(cur.begin(), cur.end(), nF.begin());
+      std::copy(curI.begin(), curI.end(), nI.begin());
+    }
+  }
+  if (g.dF) { cudaFree(g.dF); cudaFree(g.dI); ctx->used -= (uint64_t)g.cap * g.bytes_per_world(); }
+  g.dF = nullptr; g.dI = nullptr;
+  CKG(cudaMalloc(&g.dF, nF.size() * sizeof(float)));
+  CKG(cudaMalloc(&g.dI, nI.size() * sizeof(int)));
+  ctx->used += (uint64_t)ncap * g.bytes_per_world();
+  g.hF.swap(nF);
+  g.hI.swap(nI);
+  g.cap = ncap;
+  g.slot_of.resize(ncap, -1);
+  g.status_host.resize(ncap, 0);
+  CKG(cudaMemcpyAsync(g.dF, g.hF.data(), g.hF.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  CKG(cudaMemcpyAsync(g.dI, g.hI.data(), g.hI.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  CKG(cudaStreamSynchronize(ctx->stream));
+  ctx->graph_dirty = true;
+  return NEWT_OK;
+}
+
+int HostGroup::reserve_indices(newt_gpu_ctx* ctx, int k, std::vector<int>& out) {
+  out.clear();
+  while ((int)out.size() < k && !free_idx.empty()) { out.push_back(free_idx.back()); free_idx.pop_back(); }
+  int extra = k - (int)out.size();
+  if (extra > 0) {
+    int rc = grow(ctx, *this, n + extra);
+    if (rc != NEWT_OK) {
+      for (int i : out) free_idx.push_back(i);
+      return rc;
+    }
+    for (int i = 0; i < extra; ++i) out.push_back(n + i);
+    n += extra;
+  }
+  return NEWT_OK;
+}
+
+void HostGroup::release_index(newt_gpu_ctx* ctx, int idx) {
+  int lrow = kind == GK_TREE ? ri_live : lay.live;
+  I(lrow, idx) = 0;
+  slot_of[idx] = -1;
+  free_idx.push_back(idx);
+  // mark the live flag on the device immediately (stream-ordered)
+  int zero = 0;
+  int* dst = kind == GK_TREE ? dI + (size_t)lrow * cap + idx : dI + (size_t)idx * irows + lrow;
+  cudaMemcpyAsync(dst, &zero, sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
+}
+
+// ---------------------------------------------------------------------------
+// model staging
+// ---------------------------------------------------------------------------
+void HostGroup::write_model(newt_gpu_ctx*, int w, const HostModel& m) {
+  if (kind == GK_TREE) {
+    const int L = size;
+    if (topo.empty()) {
+      topo.assign(4 * L, 0);
+      int qo = 0, vo = 0;
+      for (int i = 0; i < L; ++i) {
+        int jt = m.links[i].joint;
+        topo[4 * i] = m.links[i].parent; topo[4 * i + 1] = jt; topo[4 * i + 2] = qo; topo[4 * i + 3] = vo;
+        qo += jt == NEWT_JOINT_FREE ? 7 : (jt == NEWT_JOINT_FIXED ? 0 : 1);
+        vo += jt == NEWT_JOINT_FREE ? 6 : (jt == NEWT_JOINT_FIXED ? 0 : 1);
+      }
+    }
+    for (int i = 0; i < L; ++i) {
+      const newt_link_desc& l = m.links[i];
+      for (int k = 0; k < 3; ++k) { F(r_axis + 3 * i + k, w) = l.axis[k]; F(r_jp + 3 * i + k, w) = l.jp_pos[k]; F(r_jc + 3 * i + k, w) = l.jc_pos[k]; }
+      F(r_mass + i, w) = l.mass;
+      float s6[6]; sym6(l.inertia, s6);
+      for (int k = 0; k < 6; ++k) F(r_inert + 6 * i + k, w) = s6[k];
+      F(r_damp + i, w) = i == 0 ? l.free_damping : l.damping;
+      F(r_arm + i, w) = l.armature;
+    }
+    for (int k = 0; k < 4; ++k) F(r_rootq + k, w) = m.links[0].jp_quat[k];
+    F(r_dtg, w) = m.dt; F(r_dtg + 1, w) = m.g[0]; F(r_dtg + 2, w) = m.g[1]; F(r_dtg + 3, w) = m.g[2];
+    // default state: root pose from jp for a free root, zeros elsewhere
+    for (int k = 0; k < nq; ++k) F(r_q + k, w) = 0.f;
+    for (int k = 0; k < nv; ++k) { F(r_qd + k, w) = 0.f; F(r_qfrc + k, w) = 0.f; F(r_qacc + k, w) = 0.f; }
+    if (m.links[0].joint == NEWT_JOINT_FREE) {
+      for (int k = 0; k < 3; ++k) F(r_q + k, w) = m.links[0].jp_pos[k];
+      for (int k = 0; k < 4; ++k) F(r_q + 3 + k, w) = m.links[0].jp_quat[k];
+    }
+    I(ri_solver, w) = m.solver != 0;
+    I(ri_live, w) = 1;
+    I(ri_status, w) = 0;
+  } else if (kind == GK_PILE) {
+    const int nb = size, ng = nb + np;
+    const PileLayout& l = lay;
+    std::vector<int> ent_of_geom(ng);
+    int pi = 0;
+    for (int k = 0; k < m.n_geoms; ++k) {
+      const newt_geom_desc& G = m.geoms[k];
+      int e = G.body >= 0 ? G.body : nb + (pi++);
+      ent_of_geom[k] = e;
+      I(l.gent + k, w) = e;
+      F(l.fric + e, w) = G.friction;
+      F(l.margin + e, w) = G.margin;
+      if (G.body >= 0) {
+        I(l.shape + e, w) = G.shape;
+        for (int a = 0; a < 3; ++a) { F(l.size + 3 * e + a, w) = G.size[a]; F(l.gpos + 3 * e + a, w) = G.local_pos[a]; }
+        for (int a = 0; a < 4; ++a) F(l.gquat + 4 * e + a, w) = G.local_quat[a];
+      } else {
+        int p = e - nb;
+        for (int a = 0; a < 3; ++a) F(l.plane + 7 * p + a, w) = G.local_pos[a];
+        for (int a = 0; a < 4; ++a) F(l.plane + 7 * p + 3 + a, w) = G.local_quat[a];
+      }
+    }
+    // solref/solimp: the GPU pile path assumes one soft-constraint setting per world
+    const newt_geom_desc& G0 = m.geoms[0];
+    F(l.soft, w) = G0.solref[0]; F(l.soft + 1, w) = G0.solref[1];
+    for (int a = 0; a < 5; ++a) F(l.soft + 2 + a, w) = G0.solimp[a];
+    for (int b = 0; b < nb; ++b) {
+      const newt_body_desc& B = m.bodies[b];
+      F(l.mass + b, w) = B.mass;
+      float s6[6], i6[6]; sym6(B.inertia, s6); inv6(B.inertia, i6);
+      for (int k = 0; k < 6; ++k) { F(l.inert + 6 * b + k, w) = s6[k]; F(l.iinv + 6 * b + k, w) = i6[k]; }
+      for (int a = 0; a < 3; ++a) { F(l.pos + 3 * b + a, w) = 0.f; F(l.vel + 3 * b + a, w) = 0.f; F(l.omg + 3 * b + a, w) = 0.f; }
+      F(l.quat + 4 * b, w) = 0.f; F(l.quat + 4 * b + 1, w) = 0.f; F(l.quat + 4 * b + 2, w) = 0.f; F(l.quat + 4 * b + 3, w) = 1.f;
+    }
+    F(l.dtg, w) = m.dt; F(l.dtg + 1, w) = m.g[0]; F(l.dtg + 2, w) = m.g[1]; F(l.dtg + 3, w) = m.g[2];
+    I(l.iters, w) = m.iterations;
+    I(l.status, w) = 0; I(l.ncon, w) = 0; I(l.live, w) = 1;
+  }
+  model_dirty = true;
+  pending.push_back(w);
+}
+
+int HostGroup::flush_model(newt_gpu_ctx* ctx) {
+  if (kind == GK_TREE && !dtopo && !topo.empty()) {
+    CKG(cudaMalloc(&dtopo, topo.size() * sizeof(int)));
+    CKG(cudaMemcpy(dtopo, topo.data(), topo.size() * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  if (!model_dirty) return NEWT_OK;
+  // upload only the newly written worlds: other worlds of the group may be
+  // mid-rollout on the device, with a stale host mirror
+  std::sort(pending.begin(), pending.end());
+  size_t i = 0;
+  while (i < pending.size()) {
+    size_t j = i + 1;
+    while (j < pending.size() && pending[j] == pending[j - 1] + 1) ++j;
+    const size_t a = pending[i], k = j - i;
+    if (kind == GK_TREE) {
+      CKG(cudaMemcpy2DAsync(dF + a, cap * sizeof(float), hF.data() + a, cap * sizeof(float), k * sizeof(float), frows,
+                            cudaMemcpyHostToDevice, ctx->stream));
+      CKG(cudaMemcpy2DAsync(dI + a, cap * sizeof(int), hI.data() + a, cap * sizeof(int), k * sizeof(int), irows,
+                            cudaMemcpyHostToDevice, ctx->stream));
+    } else {
+      CKG(cudaMemcpyAsync(dF + a * frows, hF.data() + a * frows, k * frows * sizeof(float), cudaMemcpyHostToDevice,
+                          ctx->stream));
+      CKG(cudaMemcpyAsync(dI + a * irows, hI.data() + a * irows, k * irows * sizeof(int), cudaMemcpyHostToDevice,
+                          ctx->stream));
+    }
+    i = j;
+  }
+  CKG(cudaStreamSynchronize(ctx->stream));
+  pending.clear();
+  model_dirty = false;
+  return NEWT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// state staging (MuJoCo layout in, newt layout on the device)
+// ---------------------------------------------------------------------------
+static void state_range(const HostGroup& g, size_t* lo, size_t* cnt) {
+  if (g.kind == GK_TREE) { *lo = g.r_q; *cnt = (size_t)g.nq + g.nv; }
+  else { *lo = g.lay.pos; *cnt = (size_t)(g.lay.omg + 3 * g.size - g.lay.pos); }
+}
+
+void HostGroup::stage_state(int w, const HostModel& m, const float* qpos, const float* qvel) {
+  if (kind == GK_TREE) {
+    int c = 0, v = 0;
+    for (int i = 0; i < size; ++i) {
+      int jt = topo[4 * i + 1], qo = topo[4 * i + 2], vo = topo[4 * i + 3];
+      if (jt == NEWT_JOINT_FREE) {
+        float q4[4] = {qpos[c + 4], qpos[c + 5], qpos[c + 6], qpos[c + 3]};
+        q_norm(q4);
+        for (int k = 0; k < 3; ++k) F(r_q + qo + k, w) = qpos[c + k];
+        for (int k = 0; k < 4; ++k) F(r_q + qo + 3 + k, w) = q4[k];
+        float vb[3];
+        q_rotT(q4, qvel + v, vb);
+        for (int k = 0; k < 3; ++k) { F(r_qd + vo + k, w) = qvel[v + 3 + k]; F(r_qd + vo + 3 + k, w) = vb[k]; }
+        c += 7; v += 6;
+      } else if (jt == NEWT_JOINT_HINGE || jt == NEWT_JOINT_SLIDE) {
+        F(r_q + qo, w) = qpos[c]; F(r_qd + vo, w) = qvel[v];
+        c += 1; v += 1;
+      }
+    }
+  } else if (kind == GK_PILE) {
+    for (int b = 0; b < size; ++b) {
+      const float* p = qpos + 7 * b;
+      const float* vv = qvel + 6 * b;
+      float q4[4] = {p[4], p[5], p[6], p[3]};
+      q_norm(q4);
+      for (int k = 0; k < 3; ++k) { F(lay.pos + 3 * b + k, w) = p[k]; F(lay.vel + 3 * b + k, w) = vv[k]; F(lay.omg + 3 * b + k, w) = vv[3 + k]; }
+      for (int k = 0; k < 4; ++k) F(lay.quat + 4 * b + k, w) = q4[k];
+    }
+  }
+  (void)m;
+  state_dirty = true;
+}
+
+void HostGroup::stage_qfrc(int w, const HostModel& m, const float* qfrc) {
+  if (kind == GK_TREE) for (int k = 0; k < nv; ++k) F(r_qfrc + k, w) = qfrc[k];
+  (void)m;
+  qfrc_dirty = true;
+}
+
+int HostGroup::flush_state(newt_gpu_ctx* ctx) {
+  if (!state_dirty) return NEWT_OK;
+  size_t lo, cnt;
+  state_range(*this, &lo, &cnt);
+  if (kind == GK_TREE) {
+    CKG(cudaMemcpyAsync(dF + lo * cap, hF.data() + lo * cap, cnt * cap * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  } else {
+    CKG(cudaMemcpy2DAsync(dF + lo, frows * sizeof(float), hF.data() + lo, frows * sizeof(float), cnt * sizeof(float),
+                          n, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  CKG(cudaStreamSynchronize(ctx->stream));
+  state_dirty = false;
+  return NEWT_OK;
+}
+
+int HostGroup::flush_qfrc(newt_gpu_ctx* ctx) {
+  if (!qfrc_dirty) return NEWT_OK;
+  if (kind == GK_TREE) {
+    CKG(cudaMemcpyAsync(dF + (size_t)r_qfrc * cap, hF.data() + (size_t)r_qfrc * cap, (size_t)nv * cap * sizeof(float),
+                        cudaMemcpyHostToDevice, ctx->stream));
+    CKG(cudaStreamSynchronize(ctx->stream));
+  }
+  qfrc_dirty = false;
+  return NEWT_OK;
+}
+
+int HostGroup::fetch_state(newt_gpu_ctx* ctx) {
+  if (n == 0) return NEWT_OK;
+  if (kind == GK_TREE) {
+    size_t lo = r_q, cnt = (size_t)nq + 3 * (size_t)nv;  // q qd qfrc qacc
+    CKG(cudaMemcpyAsync(hF.data() + lo * cap, dF + lo * cap, cnt * cap * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  } else {
+    size_t lo, cnt;
+    state_range(*this, &lo, &cnt);
+    CKG(cudaMemcpy2DAsync(hF.data() + lo, frows * sizeof(float), dF + lo, frows * sizeof(float), cnt * sizeof(float), n,
+                          cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CKG(cudaStreamSynchronize(ctx->stream));
+  device_newer = false;
+  return NEWT_OK;
+}
+
+void HostGroup::read_state(int w, const HostModel& m, float* qpos, float* qvel) const {
+  if (kind == GK_TREE) {
+    int c = 0, v = 0;
+    for (int i = 0; i < size; ++i) {
+      int jt = topo[4 * i + 1], qo = topo[4 * i + 2], vo = topo[4 * i + 3];
+      if (jt == NEWT_JOINT_FREE) {
+        float q4[4] = {Fc(r_q + qo + 3, w), Fc(r_q + qo + 4, w), Fc(r_q + qo + 5, w), Fc(r_q + qo + 6, w)};
+        for (int k = 0; k < 3; ++k) qpos[c + k] = Fc(r_q + qo + k, w);
+        qpos[c + 3] = q4[3]; qpos[c + 4] = q4[0]; qpos[c + 5] = q4[1]; qpos[c + 6] = q4[2];
+        float vb[3] = {Fc(r_qd + vo + 3, w), Fc(r_qd + vo + 4, w), Fc(r_qd + vo + 5, w)}, vw[3];
+        q_rot(q4, vb, vw);
+        for (int k = 0; k < 3; ++k) { qvel[v + k] = vw[k]; qvel[v + 3 + k] = Fc(r_qd + vo + k, w); }
+        c += 7; v += 6;
+      } else if (jt == NEWT_JOINT_HINGE || jt == NEWT_JOINT_SLIDE) {
+        qpos[c] = Fc(r_q + qo, w); qvel[v] = Fc(r_qd + vo, w);
+        c += 1; v += 1;
+      }
+    }
+  } else if (kind == GK_PILE) {
+    for (int b = 0; b < size; ++b) {
+      float* p = qpos + 7 * b;
+      float* vv = qvel + 6 * b;
+      for (int k = 0; k < 3; ++k) { p[k] = Fc(lay.pos + 3 * b + k, w); vv[k] = Fc(lay.vel + 3 * b + k, w); vv[3 + k] = Fc(lay.omg + 3 * b + k, w); }
+      p[3] = Fc(lay.quat + 4 * b + 3, w); p[4] = Fc(lay.quat + 4 * b, w); p[5] = Fc(lay.quat + 4 * b + 1, w); p[6] = Fc(lay.quat + 4 * b + 2, w);
+    }
+  }
+  (void)m;
+}
+
+void HostGroup::read_qacc(int w, const HostModel& m, float* qacc) const {
+  if (kind == GK_TREE) for (int k = 0; k < nv; ++k) qacc[k] = Fc(r_qacc + k, w);
+  else for (int k = 0; k < m.nv; ++k) qacc[k] = 0.f;
+}
+
+int HostGroup::fetch_status(newt_gpu_ctx* ctx) {
+  if (n == 0) return NEWT_OK;
+  if (kind == GK_TREE) {
+    CKG(cudaMemcpy(hI.data() + (size_t)ri_status * cap, dI + (size_t)ri_status * cap, (size_t)cap * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int w = 0; w < n; ++w) status_host[w] = (uint32_t)hI[(size_t)ri_status * cap + w];
+  } else {
+    CKG(cudaMemcpy2D(hI.data() + lay.status, irows * sizeof(int), dI + lay.status, irows * sizeof(int), sizeof(int), n,
+                     cudaMemcpyDeviceToHost));
+    for (int w = 0; w < n; ++w) status_host[w] = (uint32_t)hI[(size_t)w * irows + lay.status];
+  }
+  return NEWT_OK;
+}
+
+int HostGroup::clear_status(newt_gpu_ctx* ctx) {
+  if (n == 0) return NEWT_OK;
+  if (kind == GK_TREE) {
+    CKG(cudaMemsetAsync(dI + (size_t)ri_status * cap, 0, (size_t)cap * sizeof(int), ctx->stream));
+  } else {
+    CKG(cudaMemset2DAsync(dI + lay.status, irows * sizeof(int), 0, sizeof(int), n, ctx->stream));
+  }
+  CKG(cudaStreamSynchronize(ctx->stream));
+  return NEWT_OK;
+}
+
+int HostGroup::read_contacts(newt_gpu_ctx* ctx, int w, int cap_out, int* n_out, int* pairs, float* data) {
+  if (kind != GK_PILE && kind != GK_TREE_CONTACT) { *n_out = 0; return NEWT_OK; }
+  if (kind == GK_TREE_CONTACT) return NEWT_E_INVALID;
+  std::vector<int> rec(irows);
+  std::vector<float> frec(frows);
+  CKG(cudaStreamSynchronize(ctx->stream));
+  CKG(cudaMemcpy(rec.data(), dI + (size_t)w * irows, irows * sizeof(int), cudaMemcpyDeviceToHost));
+  CKG(cudaMemcpy(frec.data(), dF + (size_t)w * frows, frows * sizeof(float), cudaMemcpyDeviceToHost));
+  int nc = rec[lay.ncon];
+  *n_out = nc;
+  for (int i = 0; i < nc && i < cap_out && i < maxc; ++i) {
+    if (pairs) { pairs[2 * i] = rec[lay.cpair + 2 * i]; pairs[2 * i + 1] = rec[lay.cpair + 2 * i + 1]; }
+    if (data) for (int k = 0; k < 7; ++k) data[7 * i + k] = frec[lay.cdata + 7 * i + k];
+  }
+  return NEWT_OK;
+}
+
+int HostGroup::read_impulses(newt_gpu_ctx* ctx, int w, int cap_out, int* n_out, float* imp) {
+  if (kind != GK_PILE) { *n_out = 0; return NEWT_OK; }
+  std::vector<int> rec(irows);
+  std::vector<float> frec(frows);
+  CKG(cudaStreamSynchronize(ctx->stream));
+  CKG(cudaMemcpy(rec.data(), dI + (size_t)w * irows, irows * sizeof(int), cudaMemcpyDeviceToHost));
+  CKG(cudaMemcpy(frec.data(), dF + (size_t)w * frows, frows * sizeof(float), cudaMemcpyDeviceToHost));
+  int nc = std::min(rec[lay.ncon], maxc);
+  int nr = 4 * nc;
+  *n_out = nr;
+  for (int i = 0; i < nr && i < cap_out; ++i) imp[i] = frec[lay.imp + i];
+  return NEWT_OK;
+}
+
+void HostGroup::release() {
+  if (dF) cudaFree(dF);
+  if (dI) cudaFree(dI);
+  if (dtopo) cudaFree(dtopo);
+  if (plain_scratch) cudaFree(plain_scratch);
+  dF = nullptr; dI = nullptr; dtopo = nullptr; plain_scratch = nullptr;
+}
+
+TreeGroupDev HostGroup::tree_dev() const {
+  TreeGroupDev d;
+  d.n = n; d.cap = cap; d.L = size; d.nq = nq; d.nv = nv;
+  d.topo = dtopo;
+  auto row = [&](int r) { return dF + (size_t)r * cap; };
+  d.axis = row(r_axis); d.jp = row(r_jp); d.jc = row(r_jc); d.rootq = row(r_rootq); d.mass = row(r_mass);
+  d.inert = row(r_inert); d.damp = row(r_damp); d.arm = row(r_arm); d.dtg = row(r_dtg);
+  d.solver = dI + (size_t)ri_solver * cap;
+  d.live = dI + (size_t)ri_live * cap;
+  d.q = row(r_q); d.qd = row(r_qd); d.qfrc = row(r_qfrc); d.qacc = row(r_qacc);
+  d.status = (uint32_t*)(dI + (size_t)ri_status * cap);
+  return d;
+}
+
+PileGroupDev HostGroup::pile_dev() const {
+  PileGroupDev d;
+  d.n = n; d.cap = cap; d.nb = size; d.np = np; d.maxc = maxc; d.lay = lay;
+  d.F = dF; d.I = dI;
+  return d;
+}

@@ -1,0 +1,65 @@
+// Device-side layout of world groups (shared by the kernels and the host
+// runtime).  A group holds worlds of one class and one size.
+//
+//   * Tree groups are structure-of-arrays across worlds (one world per
+//     thread): element k of a per-world field lives at  f[k * cap + w], so a
+//     warp of 32 consecutive worlds reads 128 contiguous bytes.
+//   * Pile groups are world-major (one world per warp): world w's record is
+//     the contiguous range F[w * fstride, (w+1) * fstride), which the warp
+//     stages into shared memory with coalesced loads.
+#pragma once
+#include <stdint.h>
+
+#define NEWT_MAX_LINKS 65
+#define NEWT_MAX_BODIES 64
+#define NEWT_MAX_PLANES 4
+
+enum GroupKind { GK_TREE = 0, GK_PILE = 1, GK_TREE_CONTACT = 2 };
+
+// Kinematic tree without contact (config 0 chains, config 3 chains).
+struct TreeGroupDev {
+  int n;        // worlds stepped (indices 0..n-1; freed indices are masked by `live`)
+  int cap;      // SoA stride
+  int L, nq, nv;
+  const int* topo;  // [4*L]: parent, joint type, q offset, v offset (same for all worlds)
+  // per-world model (SoA)
+  const float* axis;   // 3L
+  const float* jp;     // 3L   joint_offset_in_parent position
+  const float* jc;     // 3L   joint_offset_in_child position
+  const float* rootq;  // 4    root orientation (x y z w) for a fixed root
+  const float* mass;   // L
+  const float* inert;  // 6L   xx yy zz xy xz yz
+  const float* damp;   // L    hinge/slide damping (link 0: free_damping)
+  const float* arm;    // L    armature
+  const float* dtg;    // 4    dt, gx, gy, gz
+  const int* solver;   // 1    nonzero enables free-root qfrc (newt/src/forces.rs:16-31)
+  const int* live;     // 1    nonzero for allocated worlds
+  // per-world state (SoA)
+  float* q;     // nq  (newt layout: free root p xyz, quat xyzw; hinge angle)
+  float* qd;    // nv  (free root: omega_body, v_body; hinge rate)
+  float* qfrc;  // nv
+  float* qacc;  // nv  (last step)
+  uint32_t* status;
+};
+
+// Field offsets (in floats / ints) inside one pile world's record.
+struct PileLayout {
+  int fstride, istride;
+  // float fields
+  int mass, inert, iinv, size, gpos, gquat, fric, margin, soft, plane, dtg;
+  int pos, quat, vel, omg;
+  int cdata, imp;
+  // int fields
+  int shape, gent, iters, status, ncon, cpair, live;
+};
+
+// Free bodies with one geom each plus static planes (config 1 piles).
+struct PileGroupDev {
+  int n, cap;
+  int nb;        // bodies per world
+  int np;        // static planes per world
+  int maxc;      // contact capacity per world
+  PileLayout lay;
+  float* F;      // world-major float records
+  int* I;        // world-major int records
+};

@@ -1,0 +1,408 @@
+// Host runtime behind the C ABI (include/newt_gpu.h): context, model upload
+// and classification, world slots grouped by class and size, MuJoCo-layout
+// state conversion, step dispatch (plain vs batched), diagnostics.
+//
+// The boundary mirrors newt's World API (newt/src/world.rs:325 `World::new`,
+// :950-981 `add_*`, :519-623 `apply_mujoco_qpos/qvel`, :1459 `step`); errors
+// that newt raises as panics come back as status codes.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/newt_gpu.h"
+#include "groups.h"
+#include "runtime.h"
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+static int fail(newt_gpu_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+#define CK(call)                                                                   \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess) return fail(ctx, NEWT_E_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+static void quat_conj_rot(const float q[4], const float v[3], float out[3]) {  // R(q)^T v
+  float qx = -q[0], qy = -q[1], qz = -q[2], qw = q[3];
+  float tx = 2.f * (qy * v[2] - qz * v[1]), ty = 2.f * (qz * v[0] - qx * v[2]), tz = 2.f * (qx * v[1] - qy * v[0]);
+  out[0] = v[0] + qw * tx + (qy * tz - qz * ty);
+  out[1] = v[1] + qw * ty + (qz * tx - qx * tz);
+  out[2] = v[2] + qw * tz + (qx * ty - qy * tx);
+}
+static void quat_rot(const float q[4], const float v[3], float out[3]) {
+  float qc[4] = {-q[0], -q[1], -q[2], q[3]};
+  quat_conj_rot(qc, v, out);
+}
+static void renorm(float q[4]) {
+  float n = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  if (n == 0.f) { q[0] = q[1] = q[2] = 0.f; q[3] = 1.f; return; }
+  for (int k = 0; k < 4; ++k) q[k] /= n;
+}
+static bool inv_sym(const float m9[9], float out6[6]) {
+  // m9 column-major; output (xx yy zz xy xz yz) of the inverse
+  double a = m9[0], b = m9[3], c = m9[6], d = m9[1], e = m9[4], f = m9[7], g = m9[2], h = m9[5], i = m9[8];
+  double det = a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
+  if (det == 0.0 || !std::isfinite(det)) return false;
+  double inv = 1.0 / det;
+  double r00 = (e * i - f * h) * inv, r01 = (c * h - b * i) * inv, r02 = (b * f - c * e) * inv;
+  double r11 = (a * i - c * g) * inv, r12 = (c * d - a * f) * inv, r22 = (a * e - b * d) * inv;
+  out6[0] = (float)r00; out6[1] = (float)r11; out6[2] = (float)r22;
+  out6[3] = (float)r01; out6[4] = (float)r02; out6[5] = (float)r12;
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// model upload / classification
+// ---------------------------------------------------------------------------
+static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
+  m.n_links = d.n_links; m.n_bodies = d.n_bodies; m.n_geoms = d.n_geoms;
+  m.links.assign(d.links, d.links + d.n_links);
+  m.bodies.assign(d.bodies, d.bodies + d.n_bodies);
+  m.geoms.assign(d.geoms, d.geoms + d.n_geoms);
+  m.dt = d.dt; for (int k = 0; k < 3; ++k) m.g[k] = d.gravity[k];
+  m.solver = d.solver; m.iterations = d.iterations; m.self_coll = d.tree_self_collision;
+  if (!(d.dt > 0.f)) return fail(ctx, NEWT_E_INVALID, "dt must be > 0");
+  if (d.solver != 0 && d.solver != NEWT_SOLVER_PGS && d.solver != NEWT_SOLVER_NEWTON)
+    return fail(ctx, NEWT_E_INVALID, "unknown solver mode");
+  if ((d.solver == NEWT_SOLVER_PGS || d.solver == NEWT_SOLVER_NEWTON) && d.iterations < 1)
+    return fail(ctx, NEWT_E_INVALID, "solver iterations must be >= 1 (newt/src/solver.rs:127-129)");
+  int nq = 7 * d.n_bodies, nv = 6 * d.n_bodies;
+  for (int i = 0; i < d.n_links; ++i) {
+    const newt_link_desc& L = d.links[i];
+    if (i == 0 && L.parent != -1) return fail(ctx, NEWT_E_INVALID, "link 0 must be the root");
+    if (i > 0 && (L.parent < 0 || L.parent >= i)) return fail(ctx, NEWT_E_INVALID, "links must be topologically sorted");
+    if (i == 0 && L.joint != NEWT_JOINT_FREE && L.joint != NEWT_JOINT_FIXED)
+      return fail(ctx, NEWT_E_INVALID, "root joint must be free or fixed");
+    if (i > 0 && L.joint != NEWT_JOINT_HINGE && L.joint != NEWT_JOINT_SLIDE && L.joint != NEWT_JOINT_FIXED)
+      return fail(ctx, NEWT_E_INVALID, "GPU path supports hinge, slide and fixed child joints");
+    if (i > 0 && !(L.jp_quat[3] == 1.f && L.jc_quat[3] == 1.f))
+      return fail(ctx, NEWT_E_INVALID, "child joint frames must have identity orientation (newt v0 convention)");
+    if (i == 0 && L.jc_quat[3] != 1.f) return fail(ctx, NEWT_E_INVALID, "root joint_offset_in_child must be identity");
+    if (!(L.mass > 0.f)) return fail(ctx, NEWT_E_INVALID, "link mass must be > 0");
+    nq += L.joint == NEWT_JOINT_FREE ? 7 : (L.joint == NEWT_JOINT_FIXED ? 0 : 1);
+    nv += L.joint == NEWT_JOINT_FREE ? 6 : (L.joint == NEWT_JOINT_FIXED ? 0 : 1);
+  }
+  m.nq = nq; m.nv = nv;
+  if (d.n_links > NEWT_MAX_LINKS) return fail(ctx, NEWT_E_INVALID, "too many links");
+  if (d.n_bodies > NEWT_MAX_BODIES) return fail(ctx, NEWT_E_INVALID, "too many bodies");
+  // classify
+  if (d.n_links > 0 && d.n_bodies == 0 && d.n_geoms == 0) { m.kind = GK_TREE; m.size = d.n_links; return NEWT_OK; }
+  if (d.n_links == 0 && d.n_bodies > 0) {
+    // piles: one geom per body (sphere/box) plus static planes
+    std::vector<int> per_body(d.n_bodies, 0);
+    int np = 0;
+    for (int k = 0; k < d.n_geoms; ++k) {
+      const newt_geom_desc& G = d.geoms[k];
+      if (G.link >= 0) return fail(ctx, NEWT_E_INVALID, "link geom in a tree-less world");
+      if (G.body >= 0) {
+        if (G.body >= d.n_bodies) return fail(ctx, NEWT_E_INVALID, "geom body out of range");
+        if (G.shape != NEWT_SHAPE_SPHERE && G.shape != NEWT_SHAPE_BOX)
+          return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "free-body geoms must be spheres or boxes on the GPU path");
+        per_body[G.body]++;
+      } else {
+        if (G.shape != NEWT_SHAPE_PLANE) return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "static geoms must be planes");
+        ++np;
+      }
+      if (G.condim != 3 && G.condim != 1) return fail(ctx, NEWT_E_INVALID, "condim must be 1 or 3");
+    }
+    for (int b = 0; b < d.n_bodies; ++b)
+      if (per_body[b] != 1) return fail(ctx, NEWT_E_INVALID, "GPU piles need exactly one geom per body");
+    if (np > NEWT_MAX_PLANES) return fail(ctx, NEWT_E_INVALID, "too many planes");
+    if (d.solver != NEWT_SOLVER_PGS) return fail(ctx, NEWT_E_INVALID, "GPU piles use the PGS solver");
+    m.kind = GK_PILE; m.size = d.n_bodies; m.np = np;
+    return NEWT_OK;
+  }
+  if (d.n_links > 0 && d.n_bodies == 0 && d.n_geoms > 0) {
+    m.kind = GK_TREE_CONTACT; m.size = d.n_links;
+    return NEWT_OK;
+  }
+  return fail(ctx, NEWT_E_INVALID, "unsupported world class (mixed trees and free bodies)");
+}
+
+// ---------------------------------------------------------------------------
+// groups
+// ---------------------------------------------------------------------------
+HostGroup* find_or_make_group(newt_gpu_ctx* ctx, const HostModel& m) {
+  for (auto& g : ctx->groups)
+    if (g->kind == m.kind && g->size == m.size && g->np == m.np && g->topo_key == m.topo_key()) return g.get();
+  auto g = std::make_unique<HostGroup>();
+  g->kind = m.kind; g->size = m.size; g->np = m.np; g->topo_key = m.topo_key();
+  g->nq = m.nq; g->nv = m.nv;
+  g->id = (int)ctx->groups.size();
+  ctx->groups.push_back(std::move(g));
+  return ctx->groups.back().get();
+}
+
+extern "C" {
+
+int newt_gpu_create(const newt_gpu_opts* opts, newt_gpu_ctx** out) {
+  if (!out) return NEWT_E_INVALID;
+  *out = nullptr;
+  auto* ctx = new newt_gpu_ctx();
+  ctx->device = opts ? opts->device : 0;
+  ctx->max_worlds = opts && opts->max_worlds > 0 ? opts->max_worlds : (1 << 20);
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) { delete ctx; return NEWT_E_CUDA; }
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return NEWT_E_CUDA; }
+  cudaEventCreate(&ctx->ev[0]);
+  cudaEventCreate(&ctx->ev[1]);
+  size_t fr = 0, tot = 0;
+  cudaMemGetInfo(&fr, &tot);
+  uint64_t reserve = (uint64_t)2 << 30;
+  ctx->budget = opts && opts->hbm_budget_bytes ? opts->hbm_budget_bytes : (fr > reserve ? fr - reserve : fr / 2);
+  *out = ctx;
+  return NEWT_OK;
+}
+
+int newt_gpu_destroy(newt_gpu_ctx* ctx) {
+  if (!ctx) return NEWT_E_INVALID;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& g : ctx->groups) g->release();
+  if (ctx->l2buf) cudaFree(ctx->l2buf);
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  for (void* p : ctx->plan_bufs) cudaFree(p);
+  cudaEventDestroy(ctx->ev[0]);
+  cudaEventDestroy(ctx->ev[1]);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return NEWT_OK;
+}
+
+const char* newt_gpu_last_error(const newt_gpu_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int newt_gpu_upload_models(newt_gpu_ctx* ctx, const newt_model_desc* models, int32_t n, int32_t* ids) {
+  if (!ctx || !models || n < 0) return NEWT_E_INVALID;
+  for (int i = 0; i < n; ++i) {
+    HostModel m;
+    int rc = classify(ctx, models[i], m);
+    if (rc != NEWT_OK) return rc;
+    ctx->models.push_back(std::move(m));
+    if (ids) ids[i] = (int32_t)ctx->models.size() - 1;
+  }
+  return NEWT_OK;
+}
+
+int newt_gpu_model_dims(const newt_gpu_ctx* ctx, int32_t id, int32_t* nq, int32_t* nv) {
+  if (!ctx || id < 0 || id >= (int)ctx->models.size()) return NEWT_E_INVALID;
+  if (nq) *nq = ctx->models[id].nq;
+  if (nv) *nv = ctx->models[id].nv;
+  return NEWT_OK;
+}
+
+int newt_gpu_alloc_worlds(newt_gpu_ctx* ctx, const int32_t* model_ids, int32_t n, int32_t* slots_out) {
+  if (!ctx || !model_ids || n < 0) return NEWT_E_INVALID;
+  cudaSetDevice(ctx->device);
+  // group the request so each group grows at most once
+  std::map<int, std::vector<int>> by_group;
+  for (int i = 0; i < n; ++i) {
+    int id = model_ids[i];
+    if (id < 0 || id >= (int)ctx->models.size()) return fail(ctx, NEWT_E_INVALID, "bad model id");
+    HostGroup* g = find_or_make_group(ctx, ctx->models[id]);
+    by_group[g->id].push_back(i);
+  }
+  for (auto& kv : by_group) {
+    HostGroup* g = ctx->groups[kv.first].get();
+    std::vector<int> idx;
+    int rc = g->reserve_indices(ctx, (int)kv.second.size(), idx);
+    if (rc != NEWT_OK) return rc;
+    for (size_t k = 0; k < kv.second.size(); ++k) {
+      int req = kv.second[k];
+      int slot = (int)ctx->slots.size();
+      if (!ctx->free_slots.empty()) { slot = ctx->free_slots.back(); ctx->free_slots.pop_back(); }
+      else ctx->slots.push_back(SlotRef{});
+      ctx->slots[slot] = SlotRef{g->id, idx[k], model_ids[req], true};
+      g->write_model(ctx, idx[k], ctx->models[model_ids[req]]);
+      g->slot_of[idx[k]] = slot;
+      if (slots_out) slots_out[req] = slot;
+    }
+    rc = g->flush_model(ctx);
+    if (rc != NEWT_OK) return rc;
+  }
+  ctx->graph_dirty = true;
+  return NEWT_OK;
+}
+
+int newt_gpu_free_worlds(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n) {
+  if (!ctx) return NEWT_E_INVALID;
+  for (int i = 0; i < n; ++i) {
+    int s = slots[i];
+    if (s < 0 || s >= (int)ctx->slots.size() || !ctx->slots[s].live) return fail(ctx, NEWT_E_INVALID, "bad slot");
+    SlotRef& r = ctx->slots[s];
+    ctx->groups[r.group]->release_index(ctx, r.index);
+    r.live = false;
+    ctx->free_slots.push_back(s);
+  }
+  ctx->graph_dirty = true;
+  return NEWT_OK;
+}
+
+int newt_gpu_set_state(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, const float* qpos, const float* qvel) {
+  if (!ctx || (n > 0 && (!slots || !qpos || !qvel))) return NEWT_E_INVALID;
+  cudaSetDevice(ctx->device);
+  // worlds not named here must keep their device state: refresh the host
+  // mirror of any group that stepped since its last fetch and is only
+  // partially overwritten by this call
+  std::vector<int> touched(ctx->groups.size(), 0);
+  for (int i = 0; i < n; ++i) {
+    int s = slots[i];
+    if (s < 0 || s >= (int)ctx->slots.size() || !ctx->slots[s].live) return fail(ctx, NEWT_E_INVALID, "bad slot");
+    touched[ctx->slots[s].group]++;
+  }
+  for (size_t gi = 0; gi < ctx->groups.size(); ++gi) {
+    HostGroup* g = ctx->groups[gi].get();
+    int live = g->n - (int)g->free_idx.size();
+    if (touched[gi] > 0 && g->device_newer && touched[gi] < live) {
+      int rc = g->fetch_state(ctx);
+      if (rc != NEWT_OK) return rc;
+    }
+  }
+  long qo = 0, vo = 0;
+  for (int i = 0; i < n; ++i) {
+    int s = slots[i];
+    const SlotRef& r = ctx->slots[s];
+    const HostModel& m = ctx->models[r.model];
+    ctx->groups[r.group]->stage_state(r.index, m, qpos + qo, qvel + vo);
+    qo += m.nq; vo += m.nv;
+  }
+  for (auto& g : ctx->groups) { int rc = g->flush_state(ctx); if (rc != NEWT_OK) return rc; }
+  return NEWT_OK;
+}
+
+int newt_gpu_get_state(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, float* qpos, float* qvel) {
+  if (!ctx || (n > 0 && (!slots || !qpos || !qvel))) return NEWT_E_INVALID;
+  cudaSetDevice(ctx->device);
+  for (auto& g : ctx->groups) { int rc = g->fetch_state(ctx); if (rc != NEWT_OK) return rc; }
+  long qo = 0, vo = 0;
+  for (int i = 0; i < n; ++i) {
+    int s = slots[i];
+    if (s < 0 || s >= (int)ctx->slots.size() || !ctx->slots[s].live) return fail(ctx, NEWT_E_INVALID, "bad slot");
+    const SlotRef& r = ctx->slots[s];
+    const HostModel& m = ctx->models[r.model];
+    ctx->groups[r.group]->read_state(r.index, m, qpos + qo, qvel + vo);
+    qo += m.nq; vo += m.nv;
+  }
+  return NEWT_OK;
+}
+
+int newt_gpu_set_qfrc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, const float* qfrc) {
+  if (!ctx || (n > 0 && (!slots || !qfrc))) return NEWT_E_INVALID;
+  cudaSetDevice(ctx->device);
+  long vo = 0;
+  for (int i = 0; i < n; ++i) {
+    int s = slots[i];
+    if (s < 0 || s >= (int)ctx->slots.size() || !ctx->slots[s].live) return fail(ctx, NEWT_E_INVALID, "bad slot");
+    const SlotRef& r = ctx->slots[s];
+    const HostModel& m = ctx->models[r.model];
+    ctx->groups[r.group]->stage_qfrc(r.index, m, qfrc + vo);
+    vo += m.nv;
+  }
+  for (auto& g : ctx->groups) { int rc = g->flush_qfrc(ctx); if (rc != NEWT_OK) return rc; }
+  return NEWT_OK;
+}
+
+int newt_gpu_step(newt_gpu_ctx* ctx, int32_t n_steps, int32_t mode) {
+  if (!ctx || n_steps < 0) return NEWT_E_INVALID;
+  if (n_steps == 0) return NEWT_OK;
+  cudaSetDevice(ctx->device);
+  int rc = mode == NEWT_STEP_PLAIN ? step_plain(ctx, n_steps) : step_batched(ctx, n_steps);
+  if (rc != NEWT_OK) return rc;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(ctx, NEWT_E_CUDA, std::string("launch: ") + cudaGetErrorString(e));
+  return NEWT_OK;
+}
+
+int newt_gpu_sync(newt_gpu_ctx* ctx, int32_t timeout_ms) {
+  if (!ctx) return NEWT_E_INVALID;
+  cudaSetDevice(ctx->device);
+  auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    cudaError_t e = cudaStreamQuery(ctx->stream);
+    if (e == cudaSuccess) return NEWT_OK;
+    if (e != cudaErrorNotReady) return fail(ctx, NEWT_E_CUDA, cudaGetErrorString(e));
+    double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (timeout_ms >= 0 && ms > timeout_ms) return fail(ctx, NEWT_E_TIMEOUT, "stream did not drain in time");
+    std::this_thread::yield();
+  }
+}
+
+int newt_gpu_world_status(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, uint32_t* status, int32_t clear) {
+  if (!ctx || (n > 0 && (!slots || !status))) return NEWT_E_INVALID;
+  cudaSetDevice(ctx->device);
+  for (auto& g : ctx->groups) { int rc = g->fetch_status(ctx); if (rc != NEWT_OK) return rc; }
+  for (int i = 0; i < n; ++i) {
+    int s = slots[i];
+    if (s < 0 || s >= (int)ctx->slots.size() || !ctx->slots[s].live) return fail(ctx, NEWT_E_INVALID, "bad slot");
+    status[i] = ctx->groups[ctx->slots[s].group]->status_host[ctx->slots[s].index];
+  }
+  if (clear) for (auto& g : ctx->groups) { int rc = g->clear_status(ctx); if (rc != NEWT_OK) return rc; }
+  return NEWT_OK;
+}
+
+int newt_gpu_get_qacc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, float* qacc) {
+  if (!ctx || (n > 0 && (!slots || !qacc))) return NEWT_E_INVALID;
+  cudaSetDevice(ctx->device);
+  for (auto& g : ctx->groups) { int rc = g->fetch_state(ctx); if (rc != NEWT_OK) return rc; }
+  long vo = 0;
+  for (int i = 0; i < n; ++i) {
+    int s = slots[i];
+    if (s < 0 || s >= (int)ctx->slots.size() || !ctx->slots[s].live) return fail(ctx, NEWT_E_INVALID, "bad slot");
+    const SlotRef& r = ctx->slots[s];
+    const HostModel& m = ctx->models[r.model];
+    ctx->groups[r.group]->read_qacc(r.index, m, qacc + vo);
+    vo += m.nv;
+  }
+  return NEWT_OK;
+}
+
+int newt_gpu_get_contacts(newt_gpu_ctx* ctx, int32_t slot, int32_t cap, int32_t* n_out, int32_t* pairs, float* data) {
+  if (!ctx || slot < 0 || slot >= (int)ctx->slots.size() || !ctx->slots[slot].live || !n_out) return NEWT_E_INVALID;
+  cudaSetDevice(ctx->device);
+  const SlotRef& r = ctx->slots[slot];
+  return ctx->groups[r.group]->read_contacts(ctx, r.index, cap, n_out, pairs, data);
+}
+
+int newt_gpu_get_impulses(newt_gpu_ctx* ctx, int32_t slot, int32_t cap, int32_t* n_out, float* imp) {
+  if (!ctx || slot < 0 || slot >= (int)ctx->slots.size() || !ctx->slots[slot].live || !n_out) return NEWT_E_INVALID;
+  cudaSetDevice(ctx->device);
+  const SlotRef& r = ctx->slots[slot];
+  return ctx->groups[r.group]->read_impulses(ctx, r.index, cap, n_out, imp);
+}
+
+int newt_gpu_event_record(newt_gpu_ctx* ctx, int32_t which) {
+  if (!ctx || which < 0 || which > 1) return NEWT_E_INVALID;
+  cudaSetDevice(ctx->device);
+  CK(cudaEventRecord(ctx->ev[which], ctx->stream));
+  return NEWT_OK;
+}
+
+int newt_gpu_event_elapsed_ms(newt_gpu_ctx* ctx, float* ms) {
+  if (!ctx || !ms) return NEWT_E_INVALID;
+  cudaSetDevice(ctx->device);
+  CK(cudaEventSynchronize(ctx->ev[1]));
+  CK(cudaEventElapsedTime(ms, ctx->ev[0], ctx->ev[1]));
+  return NEWT_OK;
+}
+
+int newt_gpu_flush_l2(newt_gpu_ctx* ctx) {
+  if (!ctx) return NEWT_E_INVALID;
+  cudaSetDevice(ctx->device);
+  const size_t bytes = (size_t)256 << 20;  // 256 MiB > 129 MB L2
+  if (!ctx->l2buf) CK(cudaMalloc(&ctx->l2buf, bytes));
+  CK(cudaMemsetAsync(ctx->l2buf, ctx->l2flip++ & 1, bytes, ctx->stream));
+  return NEWT_OK;
+}
+
+int64_t newt_gpu_launch_count(const newt_gpu_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+}  // extern "C"

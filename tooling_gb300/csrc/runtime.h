@@ -1,0 +1,136 @@
+// Host-side runtime structures (internal to the library).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <memory>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/newt_gpu.h"
+#include "groups.h"
+
+
+struct HostModel {
+  int kind = -1, size = 0, np = 0;
+  int n_links = 0, n_bodies = 0, n_geoms = 0;
+  int nq = 0, nv = 0;
+  std::vector<newt_link_desc> links;
+  std::vector<newt_body_desc> bodies;
+  std::vector<newt_geom_desc> geoms;
+  float dt = 0.005f, g[3] = {0, 0, -9.81f};
+  int solver = 1, iterations = 20, self_coll = 0;
+  // topology key: trees in one group must share parent/joint layout
+  std::string topo_key() const {
+    std::string k;
+    for (auto& l : links) { k += std::to_string(l.parent); k += ':'; k += std::to_string(l.joint); k += ','; }
+    if (kind == GK_TREE_CONTACT) {
+      for (auto& gd : geoms) { k += 'g'; k += std::to_string(gd.shape); k += '@'; k += std::to_string(gd.link); }
+    }
+    if (kind == GK_PILE) {
+      // geom order fixes the pair order; shapes may differ per world
+      k += "np"; k += std::to_string(np);
+    }
+    return k;
+  }
+};
+
+struct SlotRef {
+  int group = -1, index = -1, model = -1;
+  bool live = false;
+};
+
+struct newt_gpu_ctx;
+
+struct HostGroup {
+  int id = 0, kind = 0, size = 0, np = 0;
+  std::string topo_key;
+  int nq = 0, nv = 0;
+  int cap = 0, n = 0;  // capacity and high-water mark
+  std::vector<int> free_idx, slot_of;
+  // float rows x cap (tree: SoA) or cap x fstride (pile: world-major)
+  size_t frows = 0, irows = 0;
+  float* dF = nullptr;
+  int* dI = nullptr;
+  int* dtopo = nullptr;
+  std::vector<float> hF;  // host mirror of all float fields
+  std::vector<int> hI;    // host mirror of all int fields
+  std::vector<int> topo;
+  std::vector<uint32_t> status_host;
+  bool model_dirty = false, state_dirty = false, qfrc_dirty = false;
+  bool device_newer = false;  // kernels advanced the state after the last fetch
+  std::vector<int> pending;  // indices whose model record awaits upload
+  // tree layout rows
+  int r_axis = 0, r_jp = 0, r_jc = 0, r_rootq = 0, r_mass = 0, r_inert = 0, r_damp = 0, r_arm = 0, r_dtg = 0;
+  int r_q = 0, r_qd = 0, r_qfrc = 0, r_qacc = 0;
+  int ri_solver = 0, ri_live = 0, ri_status = 0;
+  // pile layout
+  PileLayout lay{};
+  int maxc = 0;
+  // tree-contact data (see tc_layout in newton_kernels.cu)
+  void* tc = nullptr;
+  void* plain_scratch = nullptr;
+  size_t plain_scratch_bytes = 0;
+
+  int reserve_indices(newt_gpu_ctx* ctx, int k, std::vector<int>& out);
+  void release_index(newt_gpu_ctx* ctx, int idx);
+  void write_model(newt_gpu_ctx* ctx, int idx, const HostModel& m);
+  int flush_model(newt_gpu_ctx* ctx);
+  void stage_state(int idx, const HostModel& m, const float* qpos, const float* qvel);
+  void stage_qfrc(int idx, const HostModel& m, const float* qfrc);
+  int flush_state(newt_gpu_ctx* ctx);
+  int flush_qfrc(newt_gpu_ctx* ctx);
+  int fetch_state(newt_gpu_ctx* ctx);
+  void read_state(int idx, const HostModel& m, float* qpos, float* qvel) const;
+  void read_qacc(int idx, const HostModel& m, float* qacc) const;
+  int fetch_status(newt_gpu_ctx* ctx);
+  int clear_status(newt_gpu_ctx* ctx);
+  int read_contacts(newt_gpu_ctx* ctx, int idx, int cap, int* n_out, int* pairs, float* data);
+  int read_impulses(newt_gpu_ctx* ctx, int idx, int cap, int* n_out, float* imp);
+  void release();
+  // kernel argument builders
+  TreeGroupDev tree_dev() const;
+  PileGroupDev pile_dev() const;
+  size_t bytes_per_world() const;
+  // float/int element accessors (host mirror)
+  float& F(size_t row, size_t w) { return kind == GK_TREE ? hF[row * cap + w] : hF[w * frows + row]; }
+  int& I(size_t row, size_t w) { return kind == GK_TREE ? hI[row * cap + w] : hI[w * irows + row]; }
+  float Fc(size_t row, size_t w) const { return kind == GK_TREE ? hF[row * cap + w] : hF[w * frows + row]; }
+  int Ic(size_t row, size_t w) const { return kind == GK_TREE ? hI[row * cap + w] : hI[w * irows + row]; }
+};
+
+struct newt_gpu_ctx {
+  int device = 0;
+  int max_worlds = 0;
+  uint64_t budget = 0, used = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  std::string err;
+  std::vector<HostModel> models;
+  std::vector<std::unique_ptr<HostGroup>> groups;
+  std::vector<SlotRef> slots;
+  std::vector<int> free_slots;
+  void* l2buf = nullptr;
+  unsigned l2flip = 0;
+  int64_t launches = 0;
+  // batched path
+  cudaGraphExec_t graph_exec = nullptr;
+  int graph_steps = -1;
+  bool graph_dirty = true;
+  std::vector<void*> plan_bufs;  // device queues / group tables the graph reads
+  int queue_items = 0;
+  size_t queue_cap = 0;
+};
+
+HostGroup* find_or_make_group(newt_gpu_ctx* ctx, const HostModel& m);
+int step_plain(newt_gpu_ctx* ctx, int n_steps);
+int step_batched(newt_gpu_ctx* ctx, int n_steps);
+
+// kernel launchers (defined in the .cu kernel files)
+extern "C" int newt_tree_bucket(int L);
+extern "C" void newt_launch_tree_fused(const TreeGroupDev& g, int base, int count, int n_steps, cudaStream_t st);
+extern "C" void newt_launch_tree_plain(const TreeGroupDev& g, cudaStream_t st);
+extern "C" void newt_launch_pile_fused(const PileGroupDev& g, int base, int count, int n_steps, cudaStream_t st);
+extern "C" void newt_launch_pile_plain(const PileGroupDev& g, void* scratch, cudaStream_t st, int* launches);
+extern "C" size_t newt_pile_plain_scratch_bytes(const PileGroupDev& g);

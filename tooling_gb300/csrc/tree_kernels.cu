@@ -1,0 +1,314 @@
+// Kinematic-tree stepping kernels: forward kinematics, the articulated-body
+// algorithm with the Euler implicit-damping fold, and semi-implicit Euler
+// integration, one world per thread.
+//
+// Restates, for FP32 on sm_103a:
+//   newt/src/tree.rs:771-858    forward_kinematics_into (only the orientations
+//                               are needed without contact: gravity enters ABA
+//                               as a body-frame force m*R^T g)
+//   newt/src/tree.rs:1021-1116  aba_with_velocity_implicit_workspace
+//   newt/src/forces.rs:6-85     assemble_joint_forces (qfrc_applied - damping*qdot)
+//   newt/src/aba.rs:803-1102    aba::run
+//   newt/src/tree.rs:1393-1475  euler_step_with_workspace / integrate_tree_positions
+//
+// Two forms:
+//   * fused  (`tree_fused_kernel`): the whole horizon in one launch; each
+//     thread keeps its world's state in registers/local memory and reads its
+//     model parameters (L1/L2-resident) every step.  Used by the batched path.
+//   * plain  (`tree_fk_kernel`, `tree_aba_kernel`, `tree_integrate_kernel`):
+//     one launch per stage per step with state round-tripping through HBM.
+#include "common.cuh"
+#include "groups.h"
+
+namespace {
+
+enum { JF = 0, JX = 1, JH = 2, JS = 3 };
+
+struct LinkScratch {
+  PX X;
+  SM6 S, v, c;
+  SF6 U, pA;
+  ABI IA;
+  float D, u;
+};
+
+// Per-world ABA (forward dynamics).  q/qd/qfrc are the world's state in newt
+// layout; writes qdd.  `scr` is MAXL entries of per-link scratch.
+template <int MAXL>
+__device__ bool tree_aba(const TreeGroupDev& g, int w, const float* q, const float* qd, const float* qfrc,
+                         float* qdd, LinkScratch* scr) {
+  const int L = g.L, cap = g.cap;
+  const float dt = g.dtg[w];
+  const V3 grav = v3(g.dtg[cap + w], g.dtg[2 * cap + w], g.dtg[3 * cap + w]);
+  V3 gb[MAXL];  // gravity in each link frame
+  // ---- pass 1 (root -> leaves): transforms, velocities, bias ----
+  for (int i = 0; i < L; ++i) {
+    const int parent = g.topo[4 * i], jt = g.topo[4 * i + 1], qo = g.topo[4 * i + 2], vo = g.topo[4 * i + 3];
+    LinkScratch& s = scr[i];
+    const float m = g.mass[i * cap + w];
+    S3 I{g.inert[(6 * i) * cap + w], g.inert[(6 * i + 1) * cap + w], g.inert[(6 * i + 2) * cap + w],
+         g.inert[(6 * i + 3) * cap + w], g.inert[(6 * i + 4) * cap + w], g.inert[(6 * i + 5) * cap + w]};
+    if (i == 0) {
+      Q4 ori;
+      if (jt == JF) {
+        ori = Q4{q[qo + 3], q[qo + 4], q[qo + 5], q[qo + 6]};
+        s.v = SM6{v3(qd[vo], qd[vo + 1], qd[vo + 2]), v3(qd[vo + 3], qd[vo + 4], qd[vo + 5])};
+      } else {
+        ori = Q4{g.rootq[w], g.rootq[cap + w], g.rootq[2 * cap + w], g.rootq[3 * cap + w]};
+        s.v = SM6{v3(0.f, 0.f, 0.f), v3(0.f, 0.f, 0.f)};
+      }
+      gb[0] = qrot_inv(ori, grav);
+      s.c = SM6{v3(0.f, 0.f, 0.f), v3(0.f, 0.f, 0.f)};
+    } else {
+      const V3 jp = v3(g.jp[(3 * i) * cap + w], g.jp[(3 * i + 1) * cap + w], g.jp[(3 * i + 2) * cap + w]);
+      const V3 jc = v3(g.jc[(3 * i) * cap + w], g.jc[(3 * i + 1) * cap + w], g.jc[(3 * i + 2) * cap + w]);
+      const V3 ax = v3(g.axis[(3 * i) * cap + w], g.axis[(3 * i + 1) * cap + w], g.axis[(3 * i + 2) * cap + w]);
+      const LinkScratch& p = scr[parent];
+      if (jt == JH) {
+        float an = sqrtf(len2(ax));
+        V3 axn = an > 0.f ? ax * (1.f / an) : ax;
+        float sn, cs;
+        sincosf(-0.5f * q[qo], &sn, &cs);
+        s.X.E = quat_mat(Q4{axn.x * sn, axn.y * sn, axn.z * sn, cs});
+        s.X.t = jc - mv(s.X.E, jp);
+        s.S = SM6{ax, cross(jc, ax)};
+      } else if (jt == JS) {
+        s.X.E = quat_mat(Q4{0.f, 0.f, 0.f, 1.f});
+        s.X.t = (jc - jp) - ax * q[qo];
+        s.S = SM6{v3(0.f, 0.f, 0.f), ax};
+      } else {  // fixed (identity joint frames)
+        s.X.E = quat_mat(Q4{0.f, 0.f, 0.f, 1.f});
+        s.X.t = jc - jp;
+        s.S = SM6{v3(0.f, 0.f, 0.f), v3(0.f, 0.f, 0.f)};
+      }
+      gb[i] = mv(s.X.E, gb[parent]);
+      SM6 vp = px_motion(s.X, p.v);
+      if (jt == JX) {
+        s.v = vp;
+        s.c = SM6{v3(0.f, 0.f, 0.f), v3(0.f, 0.f, 0.f)};
+      } else {
+        SM6 sq = smscale(s.S, qd[vo]);
+        s.v = smadd(vp, sq);
+        s.c = crm(s.v, sq);
+      }
+    }
+    s.IA.A = I;
+    for (int r = 0; r < 3; ++r) for (int c = 0; c < 3; ++c) s.IA.B.m[r][c] = 0.f;
+    s.IA.C = S3{m, m, m, 0.f, 0.f, 0.f};
+    SF6 Iv = abi_mul(s.IA, s.v);
+    SF6 ext{v3(0.f, 0.f, 0.f), gb[i] * m};
+    s.pA = sfsub(crf(s.v, Iv), ext);
+  }
+  // ---- pass 2 (leaves -> root): articulated inertias and biases ----
+  for (int i = L - 1; i >= 1; --i) {
+    const int parent = g.topo[4 * i], jt = g.topo[4 * i + 1], vo = g.topo[4 * i + 3];
+    LinkScratch& s = scr[i];
+    LinkScratch& p = scr[parent];
+    SF6 ps = sfadd(s.pA, abi_mul(s.IA, s.c));
+    if (jt == JX) {
+      abi_add(p.IA, abi_pull_back(s.IA, s.X));
+      p.pA = sfadd(p.pA, px_force_T(s.X, ps));
+      continue;
+    }
+    const float damp = g.damp[i * cap + w], arm = g.arm[i * cap + w];
+    SF6 U = abi_mul(s.IA, s.S);
+    float D = sdot6(s.S, U) + arm + dt * damp;
+    float tau = qfrc[vo] - damp * qd[vo];
+    float u = tau - sdot6(s.S, ps);
+    float invD = 1.f / D;
+    SF6 pfull = sfadd(ps, sfscale(U, u * invD));
+    ABI Ia = s.IA;
+    abi_rank1_sub(Ia, U, invD);
+    s.U = U; s.D = D; s.u = u;
+    abi_add(p.IA, abi_pull_back(Ia, s.X));
+    p.pA = sfadd(p.pA, px_force_T(s.X, pfull));
+  }
+  // ---- root ----
+  SM6 a0{v3(0.f, 0.f, 0.f), v3(0.f, 0.f, 0.f)};
+  bool ok = true;
+  const int jt0 = g.topo[1];
+  if (jt0 == JF) {
+    const int vo = g.topo[3];
+    SF6 fr{v3(0.f, 0.f, 0.f), v3(0.f, 0.f, 0.f)};
+    if (g.solver[w] != 0) fr = SF6{v3(qfrc[vo], qfrc[vo + 1], qfrc[vo + 2]), v3(qfrc[vo + 3], qfrc[vo + 4], qfrc[vo + 5])};
+    SF6 rhs = sfsub(fr, scr[0].pA);
+    const float fd = g.damp[w];
+    ABI I0 = scr[0].IA;
+    if (fd != 0.f) {
+      rhs = sfsub(rhs, SF6{v3(qd[vo], qd[vo + 1], qd[vo + 2]) * fd, v3(qd[vo + 3], qd[vo + 4], qd[vo + 5]) * fd});
+      float dm = dt * fd;
+      I0.A.xx += dm; I0.A.yy += dm; I0.A.zz += dm; I0.C.xx += dm; I0.C.yy += dm; I0.C.zz += dm;
+    }
+    ok = abi_solve(I0, rhs, &a0);
+    qdd[vo] = a0.w.x; qdd[vo + 1] = a0.w.y; qdd[vo + 2] = a0.w.z;
+    qdd[vo + 3] = a0.v.x; qdd[vo + 4] = a0.v.y; qdd[vo + 5] = a0.v.z;
+  }
+  // ---- pass 3 (root -> leaves): accelerations ----
+  SM6 acc[MAXL];
+  acc[0] = a0;
+  for (int i = 1; i < L; ++i) {
+    const int parent = g.topo[4 * i], jt = g.topo[4 * i + 1], vo = g.topo[4 * i + 3];
+    const LinkScratch& s = scr[i];
+    SM6 xa = px_motion(s.X, acc[parent]);
+    if (jt == JX) { acc[i] = smadd(xa, s.c); continue; }
+    float qa = (s.u - sdot6(xa, s.U)) / s.D;
+    qdd[vo] = qa;
+    acc[i] = smadd(smadd(xa, s.c), smscale(s.S, qa));
+  }
+  return ok;
+}
+
+template <int MAXL>
+__device__ void tree_integrate(const TreeGroupDev& g, int w, float* q, float* qd, const float* qdd) {
+  const float dt = g.dtg[w];
+  for (int k = 0; k < g.nv; ++k) qd[k] += qdd[k] * dt;
+  for (int i = 0; i < g.L; ++i) {
+    const int jt = g.topo[4 * i + 1], qo = g.topo[4 * i + 2], vo = g.topo[4 * i + 3];
+    if (jt == JF) {
+      Q4 ori{q[qo + 3], q[qo + 4], q[qo + 5], q[qo + 6]};
+      V3 om = v3(qd[vo], qd[vo + 1], qd[vo + 2]);
+      V3 dp = qrot(ori, v3(qd[vo + 3], qd[vo + 4], qd[vo + 5])) * dt;
+      q[qo] += dp.x; q[qo + 1] += dp.y; q[qo + 2] += dp.z;
+      Q4 nx = q_integrate(ori, om, dt);
+      q[qo + 3] = nx.x; q[qo + 4] = nx.y; q[qo + 5] = nx.z; q[qo + 6] = nx.w;
+    } else if (jt == JH || jt == JS) {
+      q[qo] += qd[vo] * dt;
+    }
+  }
+}
+
+__device__ __forceinline__ bool finite_all(const float* a, int n) {
+  bool ok = true;
+  for (int k = 0; k < n; ++k) ok = ok && isfinite(a[k]);
+  return ok;
+}
+
+}  // namespace
+
+// One world's whole horizon with its state kept on-chip.
+template <int MAXL>
+__device__ __forceinline__ void tree_world_steps(const TreeGroupDev& g, int w, int n_steps) {
+  const int cap = g.cap, nq = g.nq, nv = g.nv;
+  float q[MAXL + 6], qd[MAXL + 5], qf[MAXL + 5], qdd[MAXL + 5];
+  for (int k = 0; k < nq; ++k) q[k] = g.q[k * cap + w];
+  for (int k = 0; k < nv; ++k) { qd[k] = g.qd[k * cap + w]; qf[k] = g.qfrc[k * cap + w]; qdd[k] = 0.f; }
+  LinkScratch scr[MAXL];
+  uint32_t st = 0;
+  for (int s = 0; s < n_steps; ++s) {
+    if (!tree_aba<MAXL>(g, w, q, qd, qf, qdd, scr)) st |= NEWT_WS_NOT_PD;
+    tree_integrate<MAXL>(g, w, q, qd, qdd);
+  }
+  if (!finite_all(q, nq) || !finite_all(qd, nv)) st |= NEWT_WS_NONFINITE;
+  for (int k = 0; k < nq; ++k) g.q[k * cap + w] = q[k];
+  for (int k = 0; k < nv; ++k) { g.qd[k * cap + w] = qd[k]; g.qacc[k * cap + w] = qdd[k]; }
+  if (st) g.status[w] |= st;
+}
+
+// Whole horizon in one launch over a contiguous range of one group.
+template <int MAXL>
+__global__ void __launch_bounds__(64) tree_fused_kernel(TreeGroupDev g, int base, int count, int n_steps) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int w = base + t;
+  if (w >= g.n || !g.live[w]) return;
+  tree_world_steps<MAXL>(g, w, n_steps);
+}
+
+// Persistent form: blocks pull (group, base, count) items from a queue
+// sorted by size class (largest first) until it is drained.
+template <int MAXL>
+__global__ void __launch_bounds__(64) tree_persistent_kernel(const TreeGroupDev* groups, const int* queue,
+                                                             int* counter, int n_items, int n_steps) {
+  __shared__ int item;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int it = item;
+    if (it >= n_items) return;
+    const int gi = queue[3 * it], base = queue[3 * it + 1], count = queue[3 * it + 2];
+    const TreeGroupDev g = groups[gi];
+    const int w = base + (int)threadIdx.x;
+    if ((int)threadIdx.x < count && w < g.n && g.live[w]) tree_world_steps<MAXL>(g, w, n_steps);
+  }
+}
+
+// Plain form, stage 1+2: forward dynamics from HBM state into HBM qacc.
+template <int MAXL>
+__global__ void __launch_bounds__(128) tree_aba_kernel(TreeGroupDev g) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= g.n || !g.live[w]) return;
+  const int cap = g.cap, nq = g.nq, nv = g.nv;
+  float q[MAXL + 6], qd[MAXL + 5], qf[MAXL + 5], qdd[MAXL + 5];
+  for (int k = 0; k < nq; ++k) q[k] = g.q[k * cap + w];
+  for (int k = 0; k < nv; ++k) { qd[k] = g.qd[k * cap + w]; qf[k] = g.qfrc[k * cap + w]; qdd[k] = 0.f; }
+  LinkScratch scr[MAXL];
+  if (!tree_aba<MAXL>(g, w, q, qd, qf, qdd, scr)) g.status[w] |= NEWT_WS_NOT_PD;
+  for (int k = 0; k < nv; ++k) g.qacc[k * cap + w] = qdd[k];
+}
+
+// Plain form, stage 3: Euler integration from HBM qacc.
+template <int MAXL>
+__global__ void __launch_bounds__(128) tree_integrate_kernel(TreeGroupDev g) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= g.n || !g.live[w]) return;
+  const int cap = g.cap, nq = g.nq, nv = g.nv;
+  float q[MAXL + 6], qd[MAXL + 5], qdd[MAXL + 5];
+  for (int k = 0; k < nq; ++k) q[k] = g.q[k * cap + w];
+  for (int k = 0; k < nv; ++k) { qd[k] = g.qd[k * cap + w]; qdd[k] = g.qacc[k * cap + w]; }
+  tree_integrate<MAXL>(g, w, q, qd, qdd);
+  if (!finite_all(q, nq) || !finite_all(qd, nv)) g.status[w] |= NEWT_WS_NONFINITE;
+  for (int k = 0; k < nq; ++k) g.q[k * cap + w] = q[k];
+  for (int k = 0; k < nv; ++k) g.qd[k * cap + w] = qd[k];
+}
+
+// Host-side launchers (MAXL buckets 8, 16, 32, 65).
+#define NEWT_TREE_BUCKETS(X) X(8) X(16) X(32) X(65)
+
+extern "C" int newt_tree_bucket(int L) { return L <= 8 ? 8 : L <= 16 ? 16 : L <= 32 ? 32 : 65; }
+
+extern "C" void newt_launch_tree_fused(const TreeGroupDev& g, int base, int count, int n_steps, cudaStream_t st) {
+  const int B = 64;
+  int grid = (count + B - 1) / B;
+  if (grid == 0) return;
+  switch (newt_tree_bucket(g.L)) {
+#define X(M) case M: tree_fused_kernel<M><<<grid, B, 0, st>>>(g, base, count, n_steps); break;
+    NEWT_TREE_BUCKETS(X)
+#undef X
+  }
+}
+
+extern "C" void newt_launch_tree_persistent(const TreeGroupDev* dgroups, const int* dqueue, int* dcounter, int n_items,
+                                            int bucket, int n_steps, int grid, cudaStream_t st) {
+  if (grid <= 0 || n_items <= 0) return;
+  switch (bucket) {
+#define X(M) case M: tree_persistent_kernel<M><<<grid, 64, 0, st>>>(dgroups, dqueue, dcounter, n_items, n_steps); break;
+    NEWT_TREE_BUCKETS(X)
+#undef X
+  }
+}
+
+extern "C" int newt_tree_persistent_blocks_per_sm(int bucket) {
+  int nb = 1;
+  switch (bucket) {
+#define X(M) case M: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, tree_persistent_kernel<M>, 64, 0); break;
+    NEWT_TREE_BUCKETS(X)
+#undef X
+  }
+  return nb < 1 ? 1 : nb;
+}
+
+extern "C" void newt_launch_tree_plain(const TreeGroupDev& g, cudaStream_t st) {
+  const int B = 128;
+  int grid = (g.n + B - 1) / B;
+  if (grid == 0) return;
+  switch (newt_tree_bucket(g.L)) {
+#define X(M)                                            \
+  case M:                                               \
+    tree_aba_kernel<M><<<grid, B, 0, st>>>(g);          \
+    tree_integrate_kernel<M><<<grid, B, 0, st>>>(g);    \
+    break;
+    NEWT_TREE_BUCKETS(X)
+#undef X
+  }
+}

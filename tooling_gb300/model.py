@@ -214,3 +214,92 @@ def static_plane(point=(0.0, 0.0, 0.0), normal=(0.0, 0.0, 1.0), friction: float 
     else:
         raise ValueError("only +Z planes are used by this package's scenes")
     return Geom(shape=SHAPE_PLANE, local_pos=tuple(point), local_quat=quat, friction=friction)
+
+
+def _np_dtype(struct):
+    """numpy structured dtype with the exact layout of a ctypes Structure."""
+    names, formats, offsets = [], [], []
+    for name, ctype in struct._fields_:
+        f = getattr(struct, name)
+        names.append(name)
+        offsets.append(f.offset)
+        if hasattr(ctype, "_length_"):
+            base = ctype._type_
+            formats.append((np.dtype(base), (ctype._length_,)))
+        else:
+            formats.append(np.dtype(ctype))
+    return np.dtype({"names": names, "formats": formats, "offsets": offsets, "itemsize": C.sizeof(struct)})
+
+
+LINK_DT = _np_dtype(LinkDesc)
+BODY_DT = _np_dtype(BodyDesc)
+GEOM_DT = _np_dtype(GeomDesc)
+
+
+class Batch:
+    """Many worlds described by flat numpy arrays (vectorised scene building).
+
+    ``links``/``bodies``/``geoms`` are structured arrays with the C layout;
+    world ``w`` owns ``links[link_off[w]:link_off[w]+n_links[w]]`` and so on.
+    ``descs`` is a ctypes ``ModelDesc`` array pointing into those buffers: one
+    model per world.  ``qpos``/``qvel``/``qfrc`` are MuJoCo-layout state blocks
+    concatenated in world order.
+    """
+
+    def __init__(self, links, n_links, bodies, n_bodies, geoms, n_geoms, dt, gravity, solver, iterations,
+                 self_coll=0):
+        self.links = np.ascontiguousarray(links)
+        self.bodies = np.ascontiguousarray(bodies)
+        self.geoms = np.ascontiguousarray(geoms)
+        W = len(n_links)
+        self.n_worlds = W
+        self.n_links = np.asarray(n_links, np.int64)
+        self.n_bodies = np.asarray(n_bodies, np.int64)
+        self.n_geoms = np.asarray(n_geoms, np.int64)
+        self.link_off = np.concatenate([[0], np.cumsum(self.n_links)[:-1]]).astype(np.int64)
+        self.body_off = np.concatenate([[0], np.cumsum(self.n_bodies)[:-1]]).astype(np.int64)
+        self.geom_off = np.concatenate([[0], np.cumsum(self.n_geoms)[:-1]]).astype(np.int64)
+        nq = 7 * self.n_bodies.copy()
+        nv = 6 * self.n_bodies.copy()
+        if len(self.links):
+            jt = self.links["joint"]
+            jq = np.select([jt == JOINT_FREE, jt == JOINT_FIXED, jt == JOINT_BALL], [7, 0, 4], 1)
+            jv = np.select([jt == JOINT_FREE, jt == JOINT_FIXED, jt == JOINT_BALL], [6, 0, 3], 1)
+            cq = np.concatenate([[0], np.cumsum(jq)])
+            cv = np.concatenate([[0], np.cumsum(jv)])
+            nq += cq[self.link_off + self.n_links] - cq[self.link_off]
+            nv += cv[self.link_off + self.n_links] - cv[self.link_off]
+        self.nq = nq
+        self.nv = nv
+        self.q_off = np.concatenate([[0], np.cumsum(nq)[:-1]]).astype(np.int64)
+        self.v_off = np.concatenate([[0], np.cumsum(nv)[:-1]]).astype(np.int64)
+        self.descs = (ModelDesc * W)()
+        lp = self.links.ctypes.data if len(self.links) else 0
+        bp = self.bodies.ctypes.data if len(self.bodies) else 0
+        gp = self.geoms.ctypes.data if len(self.geoms) else 0
+        dt = np.broadcast_to(np.asarray(dt, np.float32), (W,))
+        iters = np.broadcast_to(np.asarray(iterations, np.int32), (W,))
+        solver = np.broadcast_to(np.asarray(solver, np.int32), (W,))
+        for w in range(W):
+            d = self.descs[w]
+            d.n_links, d.n_bodies, d.n_geoms = int(self.n_links[w]), int(self.n_bodies[w]), int(self.n_geoms[w])
+            d.links = C.cast(lp + int(self.link_off[w]) * LINK_DT.itemsize, C.POINTER(LinkDesc))
+            d.bodies = C.cast(bp + int(self.body_off[w]) * BODY_DT.itemsize, C.POINTER(BodyDesc))
+            d.geoms = C.cast(gp + int(self.geom_off[w]) * GEOM_DT.itemsize, C.POINTER(GeomDesc))
+            d.dt = float(dt[w])
+            d.gravity[0], d.gravity[1], d.gravity[2] = gravity
+            d.solver, d.iterations, d.tree_self_collision = int(solver[w]), int(iters[w]), int(self_coll)
+        self.qpos = np.zeros(int(nq.sum()), np.float32)
+        self.qvel = np.zeros(int(nv.sum()), np.float32)
+        self.qfrc = np.zeros(int(nv.sum()), np.float32)
+
+    def __len__(self) -> int:
+        return self.n_worlds
+
+    def subset(self, idx):
+        """Views of the state blocks for a list of worlds (for oracle calls)."""
+        idx = np.asarray(idx)
+        qp = np.concatenate([self.qpos[self.q_off[w]:self.q_off[w] + self.nq[w]] for w in idx])
+        qv = np.concatenate([self.qvel[self.v_off[w]:self.v_off[w] + self.nv[w]] for w in idx])
+        qf = np.concatenate([self.qfrc[self.v_off[w]:self.v_off[w] + self.nv[w]] for w in idx])
+        return qp, qv, qf

@@ -1,0 +1,196 @@
+"""Seeded synthetic worlds for the five benchmark workloads.
+
+No dataset is involved: every world is drawn from a seeded generator with the
+shapes, sizes and distributions the workloads specify.  Seeds:
+``splitmix64(0x6e657774 + config_index)`` per workload and
+``splitmix64(config_seed ^ world_id)`` per world, so any world can be rebuilt
+alone (the serving tests rely on that).
+
+Workloads
+  chain     : 7-link serial hinge pendulum, no contact (dt 1e-3)
+  pile      : 16 free spheres/boxes above a plane, PGS 50 (dt 2e-3)
+  quadruped : floating-base 18-DoF quadruped on a plane, Newton <= 20 (dt 2e-3)
+  uneven    : 50/50 chains and piles, 2..64 bodies (log-uniform), PGS 50
+"""
+from __future__ import annotations
+
+import math
+from typing import Optional
+
+import numpy as np
+
+from . import model as M
+
+MASK64 = (1 << 64) - 1
+DEFAULT_SOLREF = (0.02, 1.0)
+DEFAULT_SOLIMP = (0.9, 0.95, 0.001, 0.5, 2.0)
+
+
+def splitmix64(x: int) -> int:
+    x = (x + 0x9E3779B97F4A7C15) & MASK64
+    z = x
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & MASK64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & MASK64
+    return z ^ (z >> 31)
+
+
+def config_seed(index: int) -> int:
+    return splitmix64(0x6E657774 + index)
+
+
+def world_rng(cfg_seed: int, world_id: int) -> np.random.Generator:
+    return np.random.default_rng(splitmix64(cfg_seed ^ world_id))
+
+
+def _f32(x):
+    return np.float32(x)
+
+
+def _diag9(a, b, c):
+    return np.array([a, 0, 0, 0, b, 0, 0, 0, c], np.float32)
+
+
+def capsule_inertia(mass, radius, half_height):
+    return np.array(M.solid_capsule_inertia(mass, radius, half_height), np.float32)
+
+
+def sphere_inertia(mass, r):
+    return np.array(M.solid_sphere_inertia(mass, r), np.float32)
+
+
+def box_inertia(mass, h):
+    return np.array(M.solid_box_inertia(mass, h), np.float32)
+
+
+def _geom(shape, body=-1, link=-1, size=(0, 0, 0), pos=(0, 0, 0), quat=(0, 0, 0, 1), friction=1.0, condim=3):
+    g = np.zeros((), M.GEOM_DT)
+    g["shape"], g["body"], g["link"] = shape, body, link
+    g["size"] = size
+    g["local_pos"] = pos
+    g["local_quat"] = quat
+    g["friction"] = friction
+    g["solref"] = DEFAULT_SOLREF
+    g["solimp"] = DEFAULT_SOLIMP
+    g["condim"] = condim
+    g["group"] = 0xFFFFFFFF
+    g["mask"] = 0xFFFFFFFF
+    return g
+
+
+def _link(parent, joint, axis=(0, 0, 1), damping=0.0, jp=(0, 0, 0), jpq=(0, 0, 0, 1), jc=(0, 0, 0), mass=1.0,
+          inertia=None):
+    l = np.zeros((), M.LINK_DT)
+    l["parent"], l["joint"] = parent, joint
+    l["axis"] = axis
+    l["damping"] = damping
+    l["jp_pos"] = jp
+    l["jp_quat"] = jpq
+    l["jc_pos"] = jc
+    l["jc_quat"] = (0, 0, 0, 1)
+    l["mass"] = mass
+    l["inertia"] = inertia if inertia is not None else _diag9(1, 1, 1)
+    return l
+
+
+# ---------------------------------------------------------------------------
+# chain: serial hinge pendulum
+# ---------------------------------------------------------------------------
+CHAIN_RADIUS = 0.03
+
+
+def _chain_world(rng: np.random.Generator, n_hinges: int, damping: bool = True):
+    """Fixed root at the origin + n hinge links about x, joint at each capsule's
+    top (joint_offset_in_child = (0,0,L/2), parent offset (0,0,-L_parent/2))."""
+    links = [_link(-1, M.JOINT_FIXED, mass=1.0, inertia=_diag9(1, 1, 1))]
+    masses = rng.uniform(0.5, 2.0, n_hinges)
+    lengths = rng.uniform(0.2, 0.5, n_hinges)
+    damp = rng.uniform(0.0, 0.1, n_hinges) if damping else np.zeros(n_hinges)
+    prev_half = 0.0
+    for i in range(n_hinges):
+        half = float(_f32(lengths[i]) * _f32(0.5))
+        links.append(_link(i, M.JOINT_HINGE, axis=(1.0, 0.0, 0.0), damping=float(damp[i]),
+                           jp=(0.0, 0.0, -prev_half), jc=(0.0, 0.0, half), mass=float(masses[i]),
+                           inertia=capsule_inertia(masses[i], CHAIN_RADIUS, half)))
+        prev_half = half
+    q = rng.uniform(-math.pi, math.pi, n_hinges)
+    qd = rng.normal(0.0, 1.0, n_hinges)
+    tau = rng.normal(0.0, 0.5, n_hinges)
+    return links, q, qd, tau
+
+
+def chain_batch(n_worlds: int = 4096, n_hinges: int = 7, seed_index: int = 0, dt: float = 1e-3,
+                damping: bool = True, torque: bool = True, first_world: int = 0) -> M.Batch:
+    cs = config_seed(seed_index)
+    all_links, qs, qds, taus = [], [], [], []
+    for w in range(first_world, first_world + n_worlds):
+        links, q, qd, tau = _chain_world(world_rng(cs, w), n_hinges, damping)
+        all_links += links
+        qs.append(q); qds.append(qd); taus.append(tau if torque else np.zeros_like(tau))
+    b = M.Batch(np.stack(all_links), [n_hinges + 1] * n_worlds, np.zeros(0, M.BODY_DT), [0] * n_worlds,
+                np.zeros(0, M.GEOM_DT), [0] * n_worlds, dt, (0.0, 0.0, -9.81), M.SOLVER_PGS, 50)
+    b.qpos[:] = np.concatenate(qs)
+    b.qvel[:] = np.concatenate(qds)
+    b.qfrc[:] = np.concatenate(taus)
+    return b
+
+
+# ---------------------------------------------------------------------------
+# pile: free spheres and boxes above a plane
+# ---------------------------------------------------------------------------
+def _random_quat(rng):
+    # uniform unit quaternion (Shoemake); returned as w, x, y, z (MuJoCo order)
+    u1, u2, u3 = rng.random(3)
+    a, b = math.sqrt(1 - u1), math.sqrt(u1)
+    x, y = a * math.sin(2 * math.pi * u2), a * math.cos(2 * math.pi * u2)
+    z, w = b * math.sin(2 * math.pi * u3), b * math.cos(2 * math.pi * u3)
+    return (w, x, y, z)
+
+
+def _pile_world(rng: np.random.Generator, n_bodies: int, box_lo=(-1.0, -1.0, 0.3), box_hi=(1.0, 1.0, 2.3)):
+    """n free bodies: 50% spheres r~U(.05,.2), 50% boxes half-extents~U(.05,.2);
+    density 1000; positions uniform in the box, rejection-sampled so bounding
+    spheres do not overlap; uniform random orientations; zero velocity."""
+    bodies, geoms = [], [_geom(M.SHAPE_PLANE, friction=1.0)]
+    qpos = []
+    centers, radii = [], []
+    for b in range(n_bodies):
+        sphere = rng.random() < 0.5
+        if sphere:
+            r = float(rng.uniform(0.05, 0.2))
+            mass = float(_f32(1000.0) * _f32(4.0 / 3.0 * math.pi * r ** 3))
+            inertia = sphere_inertia(mass, r)
+            size = (r, 0.0, 0.0)
+            bound = r
+        else:
+            h = rng.uniform(0.05, 0.2, 3)
+            mass = float(_f32(1000.0 * 8.0 * h[0] * h[1] * h[2]))
+            inertia = box_inertia(mass, h)
+            size = tuple(float(v) for v in h)
+            bound = float(np.linalg.norm(h))
+        mu = float(rng.uniform(0.3, 1.0))
+        for _ in range(1000):
+            p = rng.uniform(box_lo, box_hi)
+            if all(np.linalg.norm(p - c) > bound + rc for c, rc in zip(centers, radii)):
+                break
+        centers.append(p)
+        radii.append(bound)
+        bd = np.zeros((), M.BODY_DT)
+        bd["mass"] = mass
+        bd["inertia"] = inertia
+        bodies.append(bd)
+        geoms.append(_geom(M.SHAPE_SPHERE if sphere else M.SHAPE_BOX, body=b, size=size, friction=mu))
+        qpos.append(np.concatenate([p, _random_quat(rng)]))
+    return bodies, geoms, np.concatenate(qpos)
+
+
+def pile_batch(n_worlds: int = 8192, n_bodies: int = 16, seed_index: int = 1, dt: float = 2e-3,
+               iterations: int = 50, first_world: int = 0) -> M.Batch:
+    cs = config_seed(seed_index)
+    bodies, geoms, qps = [], [], []
+    for w in range(first_world, first_world + n_worlds):
+        b, g, qp = _pile_world(world_rng(cs, w), n_bodies)
+        bodies += b; geoms += g; qps.append(qp)
+    batch = M.Batch(np.zeros(0, M.LINK_DT), [0] * n_worlds, np.stack(bodies), [n_bodies] * n_worlds,
+                    np.stack(geoms), [n_bodies + 1] * n_worlds, dt, (0.0, 0.0, -9.81), M.SOLVER_PGS, iterations)
+    batch.qpos[:] = np.concatenate(qps)
+    return batch
