@@ -1,0 +1,303 @@
+"""Benchmark: batched GPU stepping of newt worlds on GB300.
+
+Workload (the metric's headline configuration): 8192 independent worlds, each
+16 free bodies (50% spheres, 50% boxes, density 1000) above a plane, pyramidal
+friction, PGS 50 iterations, dt = 2e-3 -- seeded synthetic worlds.
+
+A bench step advances every world by `--substeps` env-steps with one call of
+the C ABI's batched step (persistent kernel, CUDA-graph replay).  Timing:
+  value : device time with CUDA events on the engine's stream, L2 flushed
+          between timed steps, state resident in HBM;
+  e2e   : wall time of set_state (host->device) + step + get_state
+          (device->host) through the C ABI with host buffers, every step.
+The reference arm (`--impl reference`) times newt's algorithm on the host
+cores: the C++ restatement of newt's f32 step (newt itself is Rust and no
+Rust toolchain exists on these machines).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--substeps", type=int, default=25)
+    ap.add_argument("--worlds", type=int, default=8192)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--plain", action="store_true", help="also time the plain (per-stage launch) form")
+    return ap.parse_args()
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return rank, ws, local, dist
+    return rank, ws, local, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def peaks():
+    try:
+        with open(PEAKS_PATH) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait(timeout=10)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1])); smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def pile_algorithmic_bytes(batch, substeps: int) -> float:
+    """Algorithmic HBM bytes of one persistent launch: each world's model and
+    state read once, its state written once (the horizon runs on-chip), and
+    the last step's contact list written out.  Model: mass, 6 inertia, 6
+    inverse inertia, shape, 3 size, 3 geom offset, 4 geom orientation,
+    friction and margin per body; one plane (7), soft params (7), dt+gravity.
+    State: 13 floats per body read and written."""
+    nb = int(batch.n_bodies[0])
+    model = nb * (1 + 6 + 6 + 1 + 3 + 3 + 4 + 2) + 7 + 2 + 7 + 4 + (nb + 1)
+    state = 13 * nb
+    contacts = 11 * 40  # ~40 contacts x (pair ints, pos, normal, pen, 4 impulses) written once
+    return float(len(batch)) * 4.0 * (model + 2 * state + contacts)
+
+
+def run_gpu(args, rank, ws, local, dist):
+    from tooling_gb300 import build as B
+    B.build()
+    from tooling_gb300 import Engine, STEP_BATCHED, STEP_PLAIN, scenes
+    eng = Engine(device=local)
+    W = args.worlds
+    batch = scenes.pile_batch(n_worlds=W, first_world=rank * W)
+    ids = eng.upload(batch)
+    slots = eng.alloc(ids)
+    eng.set_state(slots, batch.qpos, batch.qvel)
+    S = args.substeps
+    # warm-up (also captures the CUDA graph)
+    for _ in range(max(3, args.warmup)):
+        eng.step(S, STEP_BATCHED)
+    eng.sync()
+    start_qpos, start_qvel = eng.get_state(slots, int(batch.nq.sum()), int(batch.nv.sum()))
+    launches0 = eng.launch_count()
+    clocks = Clocks(local)
+    clocks.start()
+    per_step = []
+    barrier(dist)
+    eng.sync()
+    for _ in range(args.steps):
+        eng.flush_l2()
+        eng.event(0)
+        eng.step(S, STEP_BATCHED)
+        eng.event(1)
+        per_step.append(eng.elapsed_ms())
+    eng.sync()
+    barrier(dist)
+    clk = clocks.stop()
+    launches = eng.launch_count() - launches0
+    total_ms = max_over_ranks(dist, float(sum(per_step)))
+    env_steps = W * S * args.steps * ws
+    value = env_steps / (total_ms / 1e3)
+    st = eng.status(slots)
+    # e2e: host buffers in, host buffers out, every step
+    qp = start_qpos.copy()
+    qv = start_qvel.copy()
+    h2d = (qp.nbytes + qv.nbytes)
+    d2h = h2d
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.set_state(slots, qp, qv)
+        eng.step(S, STEP_BATCHED)
+        qp, qv = eng.get_state(slots, int(batch.nq.sum()), int(batch.nv.sum()))
+    eng.sync()
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    e2e = env_steps / e2e_s
+    plain = None
+    if args.plain:
+        # the same timed horizon from the same start state, plain form
+        eng.set_state(slots, start_qpos, start_qvel)
+        eng.step(1, STEP_PLAIN)
+        eng.set_state(slots, start_qpos, start_qvel)
+        eng.sync()
+        pms = 0.0
+        for _ in range(args.steps):
+            eng.flush_l2()
+            eng.event(0)
+            eng.step(S, STEP_PLAIN)
+            eng.event(1)
+            pms += eng.elapsed_ms()
+        plain = W * S * args.steps / (pms / 1e3)
+    hbm, src = peaks()
+    alg = pile_algorithmic_bytes(batch, S)
+    avg_ms = total_ms / args.steps
+    achieved = alg / (avg_ms / 1e3) / 1e9
+    out = {
+        "metric": "env-steps/s", "value": value, "unit": "env-steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": avg_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
+        "config": {"workload": "pile: free spheres/boxes on a plane, PGS 50 iterations, dt 2e-3",
+                   "worlds_per_gpu": W, "bodies_per_world": 16, "env_steps_per_bench_step": S,
+                   "mode": "batched (persistent kernel, CUDA graph)", "l2": "flushed between timed steps",
+                   "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": e2e, "unit": "env-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "peak_source": src,
+                     "note": "FP32/latency-bound contact solve; HBM fraction shown for the persistent launch"},
+        "status_flags": int(np.bitwise_or.reduce(st)) if len(st) else 0,
+    }
+    if plain is not None:
+        out["plain_value"] = plain
+        out["batched_over_plain"] = value / ws / plain
+    eng.close()
+    return out, (batch, start_qpos, start_qvel)
+
+
+def cpu_baseline(batch, qpos, qvel, S, n_worlds=256, steps=500):
+    """The f32 restatement of newt's step on the host cores: one world per
+    thread, static partition, all cores; a sample of the worlds over the same
+    horizon the GPU timed region covers."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+    from tooling_gb300 import model as M
+    cores = os.cpu_count() or 1
+    idx = np.arange(min(n_worlds, len(batch)))
+    qp = np.concatenate([qpos[batch.q_off[w]:batch.q_off[w] + batch.nq[w]] for w in idx])
+    qv = np.concatenate([qvel[batch.v_off[w]:batch.v_off[w] + batch.nv[w]] for w in idx])
+    n_steps = steps or S
+    # a ModelDesc array for just the sampled worlds
+    sub = M.Batch(batch.links, batch.n_links[idx], batch.bodies[:int(batch.n_bodies[idx].sum())], batch.n_bodies[idx],
+                  batch.geoms[:int(batch.n_geoms[idx].sum())], batch.n_geoms[idx], 2e-3, (0.0, 0.0, -9.81),
+                  M.SOLVER_PGS, 50)
+    secs = oracle_py.time_run(sub, np.arange(len(idx)), qp, qv, None, n_steps, cores)
+    return {"value": len(idx) * n_steps / secs, "unit": "env-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{len(idx)} pile worlds x {n_steps} env-steps from the bench's start state, f32 restatement of "
+                      f"newt's step, {cores} host threads"}
+
+
+def run_reference(args, rank, ws, local, dist):
+    if rank != 0:
+        return None
+    from tooling_gb300 import scenes
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+    n = min(args.worlds, 256)
+    batch = scenes.pile_batch(n_worlds=n)
+    cores = os.cpu_count() or 1
+    # advance the sample to the GPU arm's start phase (its warm-up horizon), untimed
+    qo, vo = oracle_py.run(batch, np.arange(n), batch.qpos, batch.qvel, None, max(3, args.warmup) * args.substeps,
+                           precision=0, n_threads=cores)
+    qp, qv = qo.astype(np.float32), vo.astype(np.float32)
+    vals = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        qo, vo = oracle_py.run(batch, np.arange(n), qp, qv, None, args.substeps, precision=0, n_threads=cores)
+        vals.append(n * args.substeps / (time.perf_counter() - t0))
+        qp, qv = qo.astype(np.float32), vo.astype(np.float32)
+    v = statistics.median(vals)
+    r = {"cores": cores, "sample": f"{n} pile worlds x {args.substeps} env-steps per step, advancing from the GPU "
+                                   f"arm's start phase, f32 restatement of newt's step, {cores} host threads"}
+    return {"impl": "reference", "metric": "env-steps/s", "value": v, "unit": "env-steps/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
+            "config": {"workload": "pile: free spheres/boxes on a plane, PGS 50 iterations, dt 2e-3",
+                       "worlds_per_gpu": args.worlds, "bodies_per_world": 16},
+            "cpu_baseline": {"value": v, "unit": "env-steps/s", "cores": r["cores"], "kind": "port",
+                             "sample": r["sample"] + "; newt is Rust and cannot be built here (no cargo), so its "
+                                                     "arithmetic runs through the byte-identical C++ restatement"},
+            "e2e": {"value": v, "unit": "env-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    rank, ws, local, dist = dist_setup()
+    if args.impl == "reference":
+        out = run_reference(args, rank, ws, local, dist)
+        if out is not None:
+            print(json.dumps(out))
+        return
+    out, (batch, qp, qv) = run_gpu(args, rank, ws, local, dist)
+    if rank == 0:
+        if not args.no_cpu and ws == 1:
+            out["cpu_baseline"] = cpu_baseline(batch, qp, qv, args.substeps, steps=args.substeps * args.steps)
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -164,8 +164,15 @@ static int grow(newt_gpu_ctx* ctx, HostGroup& g, int need) {
   CKG(cudaMalloc(&g.dF, nF.size() * sizeof(float)));
   CKG(cudaMalloc(&g.dI, nI.size() * sizeof(int)));
   ctx->used += (uint64_t)ncap * g.bytes_per_world();
+  // the host mirrors are the staging buffers of every state copy: page-lock
+  // them so host<->device transfers run at full link rate
+  if (!g.hF.empty()) cudaHostUnregister(g.hF.data());
+  if (!g.hI.empty()) cudaHostUnregister(g.hI.data());
   g.hF.swap(nF);
   g.hI.swap(nI);
+  cudaHostRegister(g.hF.data(), g.hF.size() * sizeof(float), cudaHostRegisterDefault);
+  cudaHostRegister(g.hI.data(), g.hI.size() * sizeof(int), cudaHostRegisterDefault);
+  cudaGetLastError();  // registration is an optimisation; ignore a refusal
   g.cap = ncap;
   g.slot_of.resize(ncap, -1);
   g.status_host.resize(ncap, 0);
@@ -173,6 +180,7 @@ static int grow(newt_gpu_ctx* ctx, HostGroup& g, int need) {
   CKG(cudaMemcpyAsync(g.dI, g.hI.data(), g.hI.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
   CKG(cudaStreamSynchronize(ctx->stream));
   ctx->graph_dirty = true;
+  ctx->plain_dirty = true;
   return NEWT_OK;
 }
 
@@ -495,6 +503,9 @@ int HostGroup::read_impulses(newt_gpu_ctx* ctx, int w, int cap_out, int* n_out, 
 }
 
 void HostGroup::release() {
+  if (!hF.empty()) cudaHostUnregister(hF.data());
+  if (!hI.empty()) cudaHostUnregister(hI.data());
+  cudaGetLastError();
   if (dF) cudaFree(dF);
   if (dI) cudaFree(dI);
   if (dtopo) cudaFree(dtopo);
@@ -520,5 +531,7 @@ PileGroupDev HostGroup::pile_dev() const {
   PileGroupDev d;
   d.n = n; d.cap = cap; d.nb = size; d.np = np; d.maxc = maxc; d.lay = lay;
   d.F = dF; d.I = dI;
+  d.scr = (float*)plain_scratch;
+  d.sstride = scr_stride;
   return d;
 }

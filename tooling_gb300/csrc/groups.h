@@ -62,4 +62,6 @@ struct PileGroupDev {
   PileLayout lay;
   float* F;      // world-major float records
   int* I;        // world-major int records
+  float* scr;    // per-world solver scratch (world-major)
+  long sstride;  // floats per world in `scr`
 };

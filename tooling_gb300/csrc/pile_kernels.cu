@@ -1,308 +1,49 @@
-// Free-body contact pipeline, one world per warp (config 1 piles and the
-// pile half of config 3): geom poses, sorted-AABB broadphase, narrowphase,
-// soft-constraint row assembly, island-parallel projected Gauss-Seidel, and
-// semi-implicit Euler integration.
+// Free-body contact pipeline, solver half (config 1 piles and the pile half
+// of config 3).  Per env-step, four kernels run over every pile world:
+//
+//   K1 collide+assemble  one warp per world: load state, broadphase and
+//                        narrowphase (pile_collide.cuh), soft-constraint row
+//                        constants, contact islands
+//   K2 pgs_small         one thread per island with one body and <= 4
+//                        contacts (the common resting case): accumulators,
+//                        Jacobians and impulses live in registers for all
+//                        sweeps
+//   K3 pgs_general       one thread per remaining island, accumulators in
+//                        thread-local arrays
+//   K4 integrate         one warp per world: semi-implicit Euler, state and
+//                        diagnostics back to the world record
 //
 // Restates, for FP32 on sm_103a:
-//   newt/src/world.rs:1459-1537      World::step phase order (Euler branch)
-//   newt/src/broadphase.rs:708-756   geom_aabb; the pair set is the sorted,
-//                                    deduplicated (a<b) list that naive
-//                                    all-pairs would give for overlapping
-//                                    boxes (newt/tests/broadphase.rs:96-118)
-//   newt/src/world.rs:2476-2515      collect_contacts_full (pair order, then
-//                                    emission order within a pair)
-//   newt/src/contact.rs:2509-2587    dispatch + swap/relabel rule
-//   newt/src/solver.rs:703-1257      solve_free_bodies_diag_mode (PGS branch)
-//   newt/src/solver.rs:1448-1518     pgs_step_non_negative / pgs_step_pyramidal_pair
-//   newt/src/solver.rs:1892-2036     row_body_diagonal, contact_regularization,
-//                                    row_residual, apply_impulse_delta
-//   newt/src/solver.rs:166-384       impedance, safe_solref, reference_accel
-//   newt/src/world.rs:1790-1817      step_bodies_euler; world.rs:3223-3245 evaluate
+//   newt/src/solver.rs:703-1257   solve_free_bodies_diag_mode (PGS branch)
+//   newt/src/solver.rs:1448-1518  pgs_step_non_negative / pgs_step_pyramidal_pair
+//   newt/src/solver.rs:1892-2036  row_body_diagonal, contact_regularization,
+//                                 row_residual, apply_impulse_delta
+//   newt/src/solver.rs:166-384    impedance, safe_solref, reference_accel
+//   newt/src/solver.rs:3401-3429  pyramidal facet rows n +- mu t
+//   newt/src/world.rs:3104-3112   tangent_basis
+//   newt/src/world.rs:1790-1817   step_bodies_euler; world.rs:3223-3245 evaluate
 //
-// Gauss-Seidel is order dependent.  Rows of disjoint contact islands never
-// touch the same body, so each lane sweeps whole islands in newt's contact
-// order; the result equals the serial sweep.  Velocity accumulators are kept
-// in world frame (newt keeps the angular one in body frame and rotates on
-// every access; the two are equal up to rounding).
-#include "common.cuh"
-#include "groups.h"
-#include "narrowphase.cuh"
+// Gauss-Seidel is order dependent.  Rows of disjoint islands never touch the
+// same body, so sweeping each island in newt's contact order (one thread per
+// island) equals the serial sweep.  A facet row n + s*mu*t has Jacobian
+// Jn + s*mu*Jt, so each contact stores Jn, Jt1, Jt2 per side and every row
+// is formed on the fly.  Velocity accumulators are kept in world frame
+// (newt keeps the angular one in body frame; equal up to rounding).
+#include <algorithm>
+
+#include "pile_collide.cuh"
+
+using namespace pile;
 
 namespace {
 
-constexpr int SH_PLANE = 0, SH_SPHERE = 1, SH_BOX = 2;
-constexpr int CF = 39;  // floats per contact in the scratch record
-constexpr int CI = 4;   // ints per contact
+// solver-record fields (floats inside one SC block)
+enum { S_JA = 0, S_JB = 18, S_MU = 36, S_IDIAG = 37, S_BIAS = 41, S_REG = 45, S_P0 = 46, S_P1 = 50, S_IMP = 54,
+       S_ROWS = 58 };
+// S_ROWS: per facet row r (0..3), 24 floats at S_ROWS + 24 r:
+//   Ja[6] (J for side a), Wa[6] = M_a^-1 Ja^T, Jb[6], Wb[6] (zero for a static side)
+// pair block: h00, h11, h01, inverse determinant (0 when det <= 0)
 
-// Per-world scratch record (shared memory in the fused kernel, global
-// memory in the plain kernels).  Offsets in floats / ints.
-struct WsLay {
-  int nb, np, ng, maxc, pcap, words;
-  // floats
-  int pos, quat, vel, omg, mass, iinvb, inertb, iinvw, dv, dw, size, gpos, gquat, plane, fric, margin, aabb, con;
-  int soft, dtg;
-  int nf;
-  // ints
-  int shape, gent, pairs, bits, ci, perm, lcnt, uf, misc;
-  int ni;
-};
-
-__host__ __device__ inline WsLay ws_layout(int nb, int np, int maxc) {
-  WsLay L;
-  L.nb = nb; L.np = np; L.ng = nb + np; L.maxc = maxc;
-  int all = L.ng * (L.ng - 1) / 2;
-  L.pcap = all < 2 * maxc ? all : 2 * maxc;
-  L.words = (L.ng + 31) / 32;
-  int f = 0;
-  L.pos = f; f += 3 * nb; L.quat = f; f += 4 * nb; L.vel = f; f += 3 * nb; L.omg = f; f += 3 * nb;
-  L.mass = f; f += nb; L.iinvb = f; f += 6 * nb; L.inertb = f; f += 6 * nb; L.iinvw = f; f += 6 * nb;
-  L.dv = f; f += 3 * nb; L.dw = f; f += 3 * nb; L.size = f; f += 3 * nb; L.gpos = f; f += 3 * nb;
-  L.gquat = f; f += 4 * nb; L.plane = f; f += 7 * np; L.fric = f; f += L.ng; L.margin = f; f += L.ng;
-  L.aabb = f; f += 6 * L.ng; L.soft = f; f += 7; L.dtg = f; f += 4;
-  L.con = f; f += CF * maxc;
-  L.nf = (f + 3) / 4 * 4;
-  int i = 0;
-  L.shape = i; i += nb; L.gent = i; i += L.ng; L.pairs = i; i += 2 * L.pcap; L.bits = i; i += L.ng * L.words;
-  L.ci = i; i += CI * maxc; L.perm = i; i += maxc; L.lcnt = i; i += 33; L.uf = i; i += nb; L.misc = i; i += 4;
-  L.ni = (i + 3) / 4 * 4;
-  return L;
-}
-
-// contact float fields (offsets inside one contact's CF block)
-enum { C_POS = 0, C_N = 3, C_PEN = 6, C_MU = 7, C_T1 = 8, C_ARMA = 11, C_ARMB = 14, C_DIAG = 17, C_REG = 21,
-       C_BIAS = 25, C_IMP = 29, C_H01 = 33, C_ACT = 35, C_NR = 36 };
-// contact int fields: ga, gb, ea, eb
-// misc ints: 0 npairs, 1 ncon, 2 overflow
-
-NEWT_D V3 ld3(const float* p) { return v3(p[0], p[1], p[2]); }
-NEWT_D void st3(float* p, V3 v) { p[0] = v.x; p[1] = v.y; p[2] = v.z; }
-NEWT_D Q4 ld4(const float* p) { return Q4{p[0], p[1], p[2], p[3]}; }
-NEWT_D S3 lds(const float* p) { return S3{p[0], p[1], p[2], p[3], p[4], p[5]}; }
-
-// ---------------------------------------------------------------------------
-// load / store between the world record (global) and the scratch record
-// ---------------------------------------------------------------------------
-NEWT_D void ws_load(const PileGroupDev& g, int w, const WsLay& L, float* wf, int* wi, int lane) {
-  const PileLayout& P = g.lay;
-  const float* F = g.F + (size_t)w * P.fstride;
-  const int* I = g.I + (size_t)w * P.istride;
-  const int nb = L.nb, ng = L.ng;
-  for (int k = lane; k < 3 * nb; k += 32) {
-    wf[L.pos + k] = F[P.pos + k]; wf[L.vel + k] = F[P.vel + k]; wf[L.omg + k] = F[P.omg + k];
-    wf[L.size + k] = F[P.size + k]; wf[L.gpos + k] = F[P.gpos + k];
-  }
-  for (int k = lane; k < 4 * nb; k += 32) { wf[L.quat + k] = F[P.quat + k]; wf[L.gquat + k] = F[P.gquat + k]; }
-  for (int k = lane; k < 6 * nb; k += 32) { wf[L.iinvb + k] = F[P.iinv + k]; wf[L.inertb + k] = F[P.inert + k]; }
-  for (int k = lane; k < nb; k += 32) { wf[L.mass + k] = F[P.mass + k]; wi[L.shape + k] = I[P.shape + k]; }
-  for (int k = lane; k < 7 * L.np; k += 32) wf[L.plane + k] = F[P.plane + k];
-  for (int k = lane; k < ng; k += 32) { wf[L.fric + k] = F[P.fric + k]; wf[L.margin + k] = F[P.margin + k]; wi[L.gent + k] = I[P.gent + k]; }
-  if (lane < 7) wf[L.soft + lane] = F[P.soft + lane];
-  if (lane < 4) wf[L.dtg + lane] = F[P.dtg + lane];
-  __syncwarp();
-}
-
-NEWT_D void ws_store_state(const PileGroupDev& g, int w, const WsLay& L, const float* wf, int lane) {
-  const PileLayout& P = g.lay;
-  float* F = g.F + (size_t)w * P.fstride;
-  for (int k = lane; k < 3 * L.nb; k += 32) { F[P.pos + k] = wf[L.pos + k]; F[P.vel + k] = wf[L.vel + k]; F[P.omg + k] = wf[L.omg + k]; }
-  for (int k = lane; k < 4 * L.nb; k += 32) F[P.quat + k] = wf[L.quat + k];
-}
-
-NEWT_D void ws_store_diag(const PileGroupDev& g, int w, const WsLay& L, const float* wf, const int* wi, int lane) {
-  const PileLayout& P = g.lay;
-  float* F = g.F + (size_t)w * P.fstride;
-  int* I = g.I + (size_t)w * P.istride;
-  const int nc = wi[L.misc + 1];
-  for (int c = lane; c < nc; c += 32) {
-    const float* cf = wf + L.con + CF * c;
-    const int* cc = wi + L.ci + CI * c;
-    I[P.cpair + 2 * c] = cc[0]; I[P.cpair + 2 * c + 1] = cc[1];
-    for (int k = 0; k < 7; ++k) F[P.cdata + 7 * c + k] = cf[C_POS + k];
-    for (int k = 0; k < 4; ++k) F[P.imp + 4 * c + k] = cf[C_IMP + k];
-  }
-  if (lane == 0) {
-    I[P.ncon] = nc;
-    if (wi[L.misc + 2]) I[P.status] |= NEWT_WS_CONTACT_OVERFLOW;
-  }
-}
-
-NEWT_D GPose geom_pose(const WsLay& L, const float* wf, int e) {
-  if (e < L.nb) {
-    V3 bp = ld3(wf + L.pos + 3 * e);
-    Q4 bq = ld4(wf + L.quat + 4 * e);
-    return GPose{bp + qrot(bq, ld3(wf + L.gpos + 3 * e)), qmul(bq, ld4(wf + L.gquat + 4 * e))};
-  }
-  const float* p = wf + L.plane + 7 * (e - L.nb);
-  return GPose{ld3(p), ld4(p + 3)};
-}
-
-// ---------------------------------------------------------------------------
-// collision: AABBs, sort-and-sweep pair marking, ordered pair list, narrowphase
-// ---------------------------------------------------------------------------
-NEWT_D void collide(const WsLay& L, float* wf, int* wi, int lane) {
-  const int ng = L.ng, nb = L.nb, W = L.words;
-  // AABBs per geom index (newt/src/broadphase.rs:708-756); planes unbounded
-  for (int k = lane; k < ng; k += 32) {
-    int e = wi[L.gent + k];
-    float* a = wf + L.aabb + 6 * k;
-    if (e >= nb) { a[0] = -INFINITY; a[1] = -INFINITY; a[2] = -INFINITY; a[3] = INFINITY; a[4] = INFINITY; a[5] = INFINITY; continue; }
-    GPose p = geom_pose(L, wf, e);
-    V3 ext;
-    if (wi[L.shape + e] == SH_SPHERE) { float r = wf[L.size + 3 * e]; ext = v3(r, r, r); }
-    else {
-      V3 h = ld3(wf + L.size + 3 * e);
-      M3 R = quat_mat(p.q);
-      ext = v3(fabsf(R.m[0][0]) * h.x + fabsf(R.m[0][1]) * h.y + fabsf(R.m[0][2]) * h.z,
-               fabsf(R.m[1][0]) * h.x + fabsf(R.m[1][1]) * h.y + fabsf(R.m[1][2]) * h.z,
-               fabsf(R.m[2][0]) * h.x + fabsf(R.m[2][1]) * h.y + fabsf(R.m[2][2]) * h.z);
-    }
-    float mg = wf[L.margin + e];
-    ext = ext + v3(mg, mg, mg);
-    a[0] = p.p.x - ext.x; a[1] = p.p.y - ext.y; a[2] = p.p.z - ext.z;
-    a[3] = p.p.x + ext.x; a[4] = p.p.y + ext.y; a[5] = p.p.z + ext.z;
-  }
-  for (int k = lane; k < ng * W; k += 32) wi[L.bits + k] = 0;
-  __syncwarp();
-  // sort geom indices by min.x (odd-even transposition over <= 64 keys held
-  // two per lane), then sweep: each geom scans forward while min.x overlaps
-  {
-    int key0 = lane, key1 = lane + 32;
-    // planes (and unused keys) sort last: only body geoms are swept
-    float v0 = (key0 < ng && wi[L.gent + key0] < nb) ? wf[L.aabb + 6 * key0] : INFINITY;
-    float v1 = (key1 < ng && wi[L.gent + key1] < nb) ? wf[L.aabb + 6 * key1] : INFINITY;
-    int* order = wi + L.perm;  // borrows the permutation buffer (maxc >= 64)
-    // bitonic sort of 64 (value, index) pairs held two per lane
-    for (int size = 2; size <= 64; size <<= 1) {
-      for (int stride = size >> 1; stride > 0; stride >>= 1) {
-        float pv0, pv1; int pk0, pk1;
-        if (stride == 32) { pv0 = v1; pk0 = key1; pv1 = v0; pk1 = key0; }
-        else {
-          pv0 = __shfl_xor_sync(0xffffffffu, v0, stride); pk0 = __shfl_xor_sync(0xffffffffu, key0, stride);
-          pv1 = __shfl_xor_sync(0xffffffffu, v1, stride); pk1 = __shfl_xor_sync(0xffffffffu, key1, stride);
-        }
-        float nv[2]; int nk[2];
-        for (int h = 0; h < 2; ++h) {
-          const int pos = lane + 32 * h;
-          const float v = h ? v1 : v0, pv = h ? pv1 : pv0;
-          const int key = h ? key1 : key0, pk = h ? pk1 : pk0;
-          const bool up = (pos & size) == 0;
-          const bool lower = pos < (pos ^ stride);
-          const bool take_min = (up == lower);
-          const bool less = (pv < v) || (pv == v && pk < key);
-          const bool take_partner = take_min ? less : !less;
-          nv[h] = take_partner ? pv : v;
-          nk[h] = take_partner ? pk : key;
-        }
-        v0 = nv[0]; key0 = nk[0]; v1 = nv[1]; key1 = nk[1];
-      }
-    }
-    order[lane] = key0; order[lane + 32] = key1;
-    __syncwarp();
-    int nsort = 0;
-    for (int k = 0; k < ng; ++k) nsort += (wi[L.gent + k] < nb);  // uniform
-    for (int h = 0; h < 2; ++h) {
-      int i = lane + 32 * h;
-      if (i >= nsort) continue;
-      int ga = order[i];
-      const float* A = wf + L.aabb + 6 * ga;
-      for (int j = i + 1; j < nsort; ++j) {
-        int gb = order[j];
-        const float* B = wf + L.aabb + 6 * gb;
-        if (B[0] > A[3]) break;
-        if (A[1] > B[4] || B[1] > A[4] || A[2] > B[5] || B[2] > A[5]) continue;
-        int lo = ga < gb ? ga : gb, hi = ga < gb ? gb : ga;
-        atomicOr(reinterpret_cast<unsigned*>(wi + L.bits + lo * W + (hi >> 5)), 1u << (hi & 31));
-      }
-    }
-    // every body geom pairs with every plane
-    for (int k = lane; k < ng; k += 32) {
-      if (wi[L.gent + k] < nb) continue;
-      for (int b = 0; b < ng; ++b) {
-        if (b == k || wi[L.gent + b] >= nb) continue;
-        int lo = b < k ? b : k, hi = b < k ? k : b;
-        atomicOr(reinterpret_cast<unsigned*>(wi + L.bits + lo * W + (hi >> 5)), 1u << (hi & 31));
-      }
-    }
-  }
-  __syncwarp();
-  // ordered pair list: rows a in order, bits b > a ascending (warp scan of row counts)
-  int base = 0;
-  for (int r0 = 0; r0 < ng; r0 += 32) {
-    int a = r0 + lane;
-    int cnt = 0;
-    if (a < ng) for (int k = 0; k < W; ++k) cnt += __popc((unsigned)wi[L.bits + a * W + k]);
-    int incl = cnt;
-    for (int o = 1; o < 32; o <<= 1) { int t = __shfl_up_sync(0xffffffffu, incl, o); if (lane >= o) incl += t; }
-    int off = base + incl - cnt;
-    if (a < ng) {
-      for (int k = 0; k < W; ++k) {
-        unsigned m = (unsigned)wi[L.bits + a * W + k];
-        while (m) {
-          int bb = __ffs(m) - 1; m &= m - 1;
-          if (off < L.pcap) { wi[L.pairs + 2 * off] = a; wi[L.pairs + 2 * off + 1] = 32 * k + bb; }
-          ++off;
-        }
-      }
-    }
-    base += __shfl_sync(0xffffffffu, incl, 31);
-  }
-  const int npairs = base < L.pcap ? base : L.pcap;
-  int overflow = base > L.pcap;
-  __syncwarp();
-  // narrowphase: 32 pairs per round, contacts appended in pair order
-  int nc = 0;
-  for (int r0 = 0; r0 < npairs; r0 += 32) {
-    int pi = r0 + lane;
-    CRes res[4];
-    int cnt = 0, ga = 0, gb = 0;
-    bool flip = false;
-    if (pi < npairs) {
-      ga = wi[L.pairs + 2 * pi]; gb = wi[L.pairs + 2 * pi + 1];
-      int ea = wi[L.gent + ga], eb = wi[L.gent + gb];
-      int sa = ea < nb ? wi[L.shape + ea] : SH_PLANE, sb = eb < nb ? wi[L.shape + eb] : SH_PLANE;
-      float margin = fmaxf(wf[L.margin + ea], wf[L.margin + eb]);
-      GPose pa = geom_pose(L, wf, ea), pb = geom_pose(L, wf, eb);
-      // try (A, B); otherwise (B, A) and relabel (newt/src/contact.rs:2561-2586)
-      if (sa == SH_SPHERE && sb == SH_PLANE) cnt = np_sphere_plane(pa, wf[L.size + 3 * ea], margin, pb, res);
-      else if (sa == SH_BOX && sb == SH_PLANE) cnt = np_box_plane(pa, ld3(wf + L.size + 3 * ea), margin, pb, res);
-      else if (sa == SH_SPHERE && sb == SH_SPHERE) cnt = np_sphere_sphere(pa.p, wf[L.size + 3 * ea], pb.p, wf[L.size + 3 * eb], margin, res);
-      else if (sa == SH_BOX && sb == SH_BOX) cnt = np_box_box(pa, ld3(wf + L.size + 3 * ea), pb, ld3(wf + L.size + 3 * eb), margin, res);
-      else if (sa == SH_SPHERE && sb == SH_BOX) cnt = np_sphere_box(pa, wf[L.size + 3 * ea], pb, ld3(wf + L.size + 3 * eb), margin, res);
-      else {
-        flip = true;
-        if (sb == SH_SPHERE && sa == SH_PLANE) cnt = np_sphere_plane(pb, wf[L.size + 3 * eb], margin, pa, res);
-        else if (sb == SH_BOX && sa == SH_PLANE) cnt = np_box_plane(pb, ld3(wf + L.size + 3 * eb), margin, pa, res);
-        else if (sb == SH_SPHERE && sa == SH_BOX) cnt = np_sphere_box(pb, wf[L.size + 3 * eb], pa, ld3(wf + L.size + 3 * ea), margin, res);
-      }
-    }
-    int incl = cnt;
-    for (int o = 1; o < 32; o <<= 1) { int t = __shfl_up_sync(0xffffffffu, incl, o); if (lane >= o) incl += t; }
-    int off = nc + incl - cnt;
-    for (int k = 0; k < cnt; ++k) {
-      int c = off + k;
-      if (c >= L.maxc) { overflow = 1; break; }
-      float* cf = wf + L.con + CF * c;
-      int* cc = wi + L.ci + CI * c;
-      V3 n = flip ? -res[k].n : res[k].n;
-      st3(cf + C_POS, res[k].pos); st3(cf + C_N, n); cf[C_PEN] = res[k].pen;
-      int ea = wi[L.gent + ga], eb = wi[L.gent + gb];
-      cf[C_MU] = fminf(wf[L.fric + ea], wf[L.fric + eb]);
-      cc[0] = ga; cc[1] = gb; cc[2] = ea; cc[3] = eb;
-    }
-    nc += __shfl_sync(0xffffffffu, incl, 31);
-  }
-  overflow = __any_sync(0xffffffffu, overflow);
-  if (lane == 0) {
-    wi[L.misc] = npairs;
-    wi[L.misc + 1] = nc < L.maxc ? nc : L.maxc;
-    wi[L.misc + 2] = overflow;
-  }
-  __syncwarp();
-}
-
-// ---------------------------------------------------------------------------
-// row assembly (newt/src/solver.rs:752-1061)
-// ---------------------------------------------------------------------------
 NEWT_D float impedance(float pos, const float* soft) {
   // effective_solimp + impedance_at_position(pos, 0) (solver.rs:301-326)
   float dmin = fminf(fmaxf(soft[2], 1.0e-4f), 0.9999f), dmax = fminf(fmaxf(soft[3], 1.0e-4f), 0.9999f);
@@ -317,228 +58,667 @@ NEWT_D float impedance(float pos, const float* soft) {
   return dmin + (dmax - dmin) * y;
 }
 
-NEWT_D void assemble(const WsLay& L, float* wf, int* wi, int lane) {
+struct J6 { V3 l, a; };
+NEWT_D float jdot(const J6& j, V3 dv, V3 dw) { return dot(j.l, dv) + dot(j.a, dw); }
+NEWT_D J6 jrow(const J6& n, const J6& t, float s) { return J6{n.l + t.l * s, n.a + t.a * s}; }
+NEWT_D J6 ldj(const float* p) { return J6{v3(p[0], p[1], p[2]), v3(p[3], p[4], p[5])}; }
+NEWT_D void stj(float* p, const J6& j) { p[0] = j.l.x; p[1] = j.l.y; p[2] = j.l.z; p[3] = j.a.x; p[4] = j.a.y; p[5] = j.a.z; }
+
+// ---------------------------------------------------------------------------
+// K1 part 2: row constants and islands (newt/src/solver.rs:752-1061)
+// ---------------------------------------------------------------------------
+// Island work lists: the PGS kernels run over compacted lists, one list per
+// island class so each kernel variant is sized for its islands.
+constexpr int N_ICLASS = 6;  // 1 body x {1, 2, 3-4 contacts}, <= 4 bodies, <= 8 bodies, more
+struct IslandLists {
+  int* items;   // N_ICLASS x cap entries: (world index in the table << 6) | island
+  int* counts;  // N_ICLASS counters, zeroed before each step
+  int cap;
+};
+
+// 0-2: one body with 1, 2, 3-4 contacts (thread per island, registers);
+// 3: up to 4 bodies, 4: up to 8 bodies (thread per island, precomputed rows,
+// registers; at most 32 contacts); 5: the rest (thread-local accumulators)
+NEWT_D int island_class(int nbody, int cnt) {
+  if (nbody == 1 && cnt == 1) return 0;
+  if (nbody == 1 && cnt == 2) return 1;
+  if (nbody == 1 && cnt <= 4) return 2;
+  if (cnt > 32) return 5;
+  return nbody <= 4 ? 3 : (nbody <= 8 ? 4 : 5);
+}
+
+NEWT_D void assemble(const WsLay& L, float* wf, int* wi, int lane, int t_world, const IslandLists& il) {
   const int nb = L.nb, nc = wi[L.misc + 1];
   const float dt = wf[L.dtg];
   const V3 grav = v3(wf[L.dtg + 1], wf[L.dtg + 2], wf[L.dtg + 3]);
   const float* soft = wf + L.soft;
-  // world inverse inertias + zeroed accumulators
   for (int b = lane; b < nb; b += 32) {
     M3 R = quat_mat(ld4(wf + L.quat + 4 * b));
-    S3 ib = lds(wf + L.iinvb + 6 * b);
-    S3 iw = sym_congr(M3{{{R.m[0][0], R.m[1][0], R.m[2][0]}, {R.m[0][1], R.m[1][1], R.m[2][1]}, {R.m[0][2], R.m[1][2], R.m[2][2]}}}, ib);
+    M3 RT{{{R.m[0][0], R.m[1][0], R.m[2][0]}, {R.m[0][1], R.m[1][1], R.m[2][1]}, {R.m[0][2], R.m[1][2], R.m[2][2]}}};
+    S3 iw = sym_congr(RT, lds(wf + L.iinvb + 6 * b));
     float* o = wf + L.iinvw + 6 * b;
     o[0] = iw.xx; o[1] = iw.yy; o[2] = iw.zz; o[3] = iw.xy; o[4] = iw.xz; o[5] = iw.yz;
     st3(wf + L.dv + 3 * b, v3(0.f, 0.f, 0.f));
     st3(wf + L.dw + 3 * b, v3(0.f, 0.f, 0.f));
   }
-  __syncwarp();
-  // soft-constraint reference (solver.rs:331-384): safe_solref, direct vs positive
-  float tc = soft[0], dr = soft[1];
-  const bool direct = tc < 0.f;
-  if (!direct && tc < 2.f * dt) tc = 2.f * dt;
-  const float dmax = fminf(fmaxf(soft[3], 1.0e-4f), 0.9999f);
+  // active contacts (solver.rs:762-769): a dynamic side and penetration beyond the gap (gap = 0)
   for (int c = lane; c < nc; c += 32) {
     float* cf = wf + L.con + CF * c;
     const int* cc = wi + L.ci + CI * c;
+    cf[C_ACT] = ((cc[2] < nb || cc[3] < nb) && cf[C_PEN] > 0.f) ? 1.f : 0.f;
+    for (int k = 0; k < 4; ++k) cf[C_IMP + k] = 0.f;
+  }
+  __syncwarp();
+  // islands: union-find over dynamic-dynamic contacts, islands ordered by
+  // their smallest body, contacts within an island in contact order
+  if (lane == 0) {
+    int* uf = wi + L.uf;
+    for (int b = 0; b < nb; ++b) uf[b] = b;
+    for (int c = 0; c < nc; ++c) {
+      const int* cc = wi + L.ci + CI * c;
+      if (wf[L.con + CF * c + C_ACT] == 0.f || cc[2] >= nb || cc[3] >= nb) continue;
+      int ra = cc[2], rb = cc[3];
+      while (uf[ra] != ra) ra = uf[ra];
+      while (uf[rb] != rb) rb = uf[rb];
+      if (ra != rb) { if (ra < rb) uf[rb] = ra; else uf[ra] = rb; }
+    }
+    for (int b = 0; b < nb; ++b) { int r = b; while (uf[r] != r) r = uf[r]; uf[b] = r; }
+    // island id per root body; count contacts per island
+    int* root_isl = wi + L.blocal;  // temp: root -> island id (rewritten below)
+    for (int b = 0; b < nb; ++b) root_isl[b] = -1;
+    int nisl = 0;
+    for (int c = 0; c < nc; ++c) {
+      const int* cc = wi + L.ci + CI * c;
+      if (wf[L.con + CF * c + C_ACT] == 0.f) continue;
+      int body = cc[2] < nb ? cc[2] : cc[3];
+      int r = uf[body];
+      if (root_isl[r] < 0) root_isl[r] = -2;  // mark: island exists
+    }
+    for (int b = 0; b < nb; ++b) if (root_isl[b] == -2) root_isl[b] = nisl++;
+    int* icount = wi + L.icount;
+    int* istart = wi + L.istart;
+    for (int i = 0; i < nisl; ++i) icount[i] = 0;
+    for (int c = 0; c < nc; ++c) {
+      const int* cc = wi + L.ci + CI * c;
+      if (wf[L.con + CF * c + C_ACT] == 0.f) continue;
+      icount[root_isl[uf[cc[2] < nb ? cc[2] : cc[3]]]]++;
+    }
+    int s = 0;
+    for (int i = 0; i < nisl; ++i) { istart[i] = s; s += icount[i]; }
+    // bodies per island (body order), island-local body index
+    int* inb = wi + L.inb;
+    int* ibstart = wi + L.ibstart;
+    int* ibody = wi + L.ibody;
+    for (int i = 0; i < nisl; ++i) inb[i] = 0;
+    int* bisl = wi + L.perm;  // temp: body -> island (or -1)
+    for (int b = 0; b < nb; ++b) bisl[b] = root_isl[uf[b]];
+    for (int b = 0; b < nb; ++b) if (bisl[b] >= 0) inb[bisl[b]]++;
+    int t = 0;
+    for (int i = 0; i < nisl; ++i) { ibstart[i] = t; t += inb[i]; }
+    int fillb[NEWT_MAX_BODIES];
+    for (int i = 0; i < nisl; ++i) fillb[i] = ibstart[i];
+    int* blocal = wi + L.blocal;  // now: body -> island-local index
+    for (int b = 0; b < nb; ++b) {
+      int i = bisl[b];
+      if (i < 0) { blocal[b] = -1; continue; }
+      blocal[b] = fillb[i] - ibstart[i];
+      ibody[fillb[i]++] = b;
+    }
+    // contact slot in island order
+    int fillc[NEWT_MAX_BODIES];
+    for (int i = 0; i < nisl; ++i) fillc[i] = istart[i];
+    int* sccon = wi + L.sccon;
+    int* scid = wi + L.scid;
+    for (int c = 0; c < nc; ++c) {
+      const int* cc = wi + L.ci + CI * c;
+      if (wf[L.con + CF * c + C_ACT] == 0.f) continue;
+      int i = bisl[cc[2] < nb ? cc[2] : cc[3]];
+      int k = fillc[i]++;
+      sccon[k] = c;
+      scid[2 * k] = cc[2] < nb ? blocal[cc[2]] : -1;
+      scid[2 * k + 1] = cc[3] < nb ? blocal[cc[3]] : -1;
+    }
+    wi[L.misc + 3] = nisl;
+    // append this world's islands to the class work lists
+    int ncls[N_ICLASS] = {0, 0, 0, 0, 0};
+    for (int i = 0; i < nisl; ++i) ncls[island_class(inb[i], icount[i])]++;
+    int base[N_ICLASS];
+    for (int c = 0; c < N_ICLASS; ++c) base[c] = ncls[c] ? atomicAdd(il.counts + c, ncls[c]) : 0;
+    for (int i = 0; i < nisl; ++i) {
+      const int c = island_class(inb[i], icount[i]);
+      const int slot = base[c]++;
+      if (slot < il.cap) il.items[(size_t)c * il.cap + slot] = (t_world << 6) | i;
+    }
+  }
+  __syncwarp();
+  // per active contact: Jacobians, regularisation, bias, pair constants
+  float tc = soft[0], dr = soft[1];
+  const bool direct = tc < 0.f;
+  if (!direct && tc < 2.f * dt) tc = 2.f * dt;  // safe_solref (solver.rs:331-338)
+  const float dmax = fminf(fmaxf(soft[3], 1.0e-4f), 0.9999f);
+  const int nisl = wi[L.misc + 3];
+  const int nact = nisl > 0 ? wi[L.istart + nisl - 1] + wi[L.icount + nisl - 1] : 0;
+  for (int k = lane; k < nact; k += 32) {
+    const int c = wi[L.sccon + k];
+    const float* cf = wf + L.con + CF * c;
+    const int* cc = wi + L.ci + CI * c;
+    float* sc = wf + L.sc + SC * k;
     const int ea = cc[2], eb = cc[3];
     const bool da = ea < nb, db = eb < nb;
-    float pen = cf[C_PEN];
-    // inactive: both static or force-free gap covers the penetration (gap = 0)
-    bool act = (da || db) && pen > 0.f;
-    cf[C_ACT] = act ? 1.f : 0.f;
-    for (int k = 0; k < 4; ++k) cf[C_IMP + k] = 0.f;
-    if (!act) continue;
-    V3 n = ld3(cf + C_N), pos = ld3(cf + C_POS);
-    // tangent_basis (world.rs:3104-3112), t2 = n x t1 (solver.rs:3458-3463)
+    const float pen = cf[C_PEN], mu = cf[C_MU];
+    const V3 n = ld3(cf + C_N), pos = ld3(cf + C_POS);
     V3 ref = fabsf(n.z) < 0.9f ? v3(0.f, 0.f, 1.f) : v3(1.f, 0.f, 0.f);
     V3 t1 = cross(ref, n);
     float tl = sqrtf(len2(t1));
     t1 = tl == 0.f ? v3(0.f, 0.f, 0.f) : t1 * (1.f / tl);
-    V3 t2 = cross(n, t1);
-    st3(cf + C_T1, t1);
-    V3 arma = da ? pos - ld3(wf + L.pos + 3 * ea) : v3(0.f, 0.f, 0.f);
-    V3 armb = db ? pos - ld3(wf + L.pos + 3 * eb) : v3(0.f, 0.f, 0.f);
-    st3(cf + C_ARMA, arma); st3(cf + C_ARMB, armb);
-    const float mu = cf[C_MU];
-    const int nr = 4;  // pyramidal condim 3
-    cf[C_NR] = (float)nr;
+    const V3 t2 = cross(n, t1);
+    const V3 arma = da ? pos - ld3(wf + L.pos + 3 * ea) : v3(0.f, 0.f, 0.f);
+    const V3 armb = db ? pos - ld3(wf + L.pos + 3 * eb) : v3(0.f, 0.f, 0.f);
+    // side Jacobians: a = (d, arm_a x d); b = -(d, arm_b x d); zero when static
+    J6 Ja[3], Jb[3];
+    const V3 ds[3] = {n, t1, t2};
+    for (int q = 0; q < 3; ++q) {
+      Ja[q] = da ? J6{ds[q], cross(arma, ds[q])} : J6{v3(0.f, 0.f, 0.f), v3(0.f, 0.f, 0.f)};
+      Jb[q] = db ? J6{-ds[q], -cross(armb, ds[q])} : J6{v3(0.f, 0.f, 0.f), v3(0.f, 0.f, 0.f)};
+      stj(sc + S_JA + 6 * q, Ja[q]);
+      stj(sc + S_JB + 6 * q, Jb[q]);
+    }
+    sc[S_MU] = mu;
+    const float ima = da ? 1.f / wf[L.mass + ea] : 0.f, imb = db ? 1.f / wf[L.mass + eb] : 0.f;
+    const S3 Ia = da ? lds(wf + L.iinvw + 6 * ea) : S3{0, 0, 0, 0, 0, 0};
+    const S3 Ib = db ? lds(wf + L.iinvw + 6 * eb) : S3{0, 0, 0, 0, 0, 0};
     const float d = impedance(-pen, soft);
-    float tran = 0.f;
-    if (da) tran += 1.f / wf[L.mass + ea];
-    if (db) tran += 1.f / wf[L.mass + eb];
+    const float tran = ima + imb;
     const float reg = d > 0.f ? 2.f * mu * mu * ((1.f - d) / d * (tran * (1.f + mu * mu))) : 0.f;
+    sc[S_REG] = reg;
     float b_, k_;
     if (direct) { b_ = -dr / dmax; k_ = -soft[0] / (dmax * dmax); }
     else { b_ = 2.f / (dmax * tc); k_ = d / (dmax * dmax * tc * tc * dr * dr); }
     V3 va = v3(0.f, 0.f, 0.f), vb = v3(0.f, 0.f, 0.f);
     if (da) va = ld3(wf + L.vel + 3 * ea) + cross(qrot(ld4(wf + L.quat + 4 * ea), ld3(wf + L.omg + 3 * ea)), arma);
     if (db) vb = ld3(wf + L.vel + 3 * eb) + cross(qrot(ld4(wf + L.quat + 4 * eb), ld3(wf + L.omg + 3 * eb)), armb);
-    V3 dirs[4] = {n + t1 * mu, n - t1 * mu, n + t2 * mu, n - t2 * mu};
-    V3 anga[4], angb[4];
-    for (int r = 0; r < nr; ++r) {
-      V3 dir = dirs[r];
+    float diag[4];
+    J6 Ra[4], Rb[4];
+    for (int r = 0; r < 4; ++r) {
+      const int q = r < 2 ? 1 : 2;
+      const float s = (r & 1) ? -mu : mu;
+      Ra[r] = jrow(Ja[0], Ja[q], s);
+      Rb[r] = jrow(Jb[0], Jb[q], s);
+      const V3 dir = n + ds[q] * s;
+      // A_ii (row_body_diagonal) + regulariser
       float aii = 0.f, dvf = 0.f;
-      anga[r] = cross(arma, dir); angb[r] = cross(armb, dir);
-      if (da) { aii += dot(anga[r], smv(lds(wf + L.iinvw + 6 * ea), anga[r])) + 1.f / wf[L.mass + ea]; dvf += dot(grav * dt, dir); }
-      if (db) { aii += dot(angb[r], smv(lds(wf + L.iinvw + 6 * eb), angb[r])) + 1.f / wf[L.mass + eb]; dvf -= dot(grav * dt, dir); }
-      float vcur = dot(va - vb, dir);
-      float aref = -b_ * vcur - k_ * (-pen);
-      cf[C_REG + r] = reg;
-      cf[C_DIAG + r] = aii + reg;
-      cf[C_BIAS + r] = dvf - aref * dt;
+      if (da) { aii += dot(Ra[r].a, smv(Ia, Ra[r].a)) + ima; dvf += dot(grav * dt, dir); }
+      if (db) { aii += dot(Rb[r].a, smv(Ib, Rb[r].a)) + imb; dvf -= dot(grav * dt, dir); }
+      diag[r] = aii + reg;
+      sc[S_IDIAG + r] = 1.f / diag[r];
+      const float vcur = dot(va - vb, dir);
+      const float aref = -b_ * vcur - k_ * (-pen);
+      sc[S_BIAS + r] = dvf - aref * dt;
+      sc[S_IMP + r] = 0.f;
+      float* row = sc + S_ROWS + 24 * r;
+      stj(row, Ra[r]);
+      stj(row + 6, J6{Ra[r].l * ima, smv(Ia, Ra[r].a)});
+      stj(row + 12, Rb[r]);
+      stj(row + 18, J6{Rb[r].l * imb, smv(Ib, Rb[r].a)});
     }
-    // pyramidal pair cross responses h01 (solver.rs:1037-1061)
+    // pyramidal pair blocks (solver.rs:1037-1061, 1476-1518)
     for (int p = 0; p < 2; ++p) {
-      int i0 = 2 * p, i1 = 2 * p + 1;
-      float h = 0.f;
-      if (da) h += dot(dirs[i0], dirs[i1]) / wf[L.mass + ea] + dot(anga[i0], smv(lds(wf + L.iinvw + 6 * ea), anga[i1]));
-      if (db) h += dot(dirs[i0], dirs[i1]) / wf[L.mass + eb] + dot(angb[i0], smv(lds(wf + L.iinvw + 6 * eb), angb[i1]));
-      cf[C_H01 + p] = h;
+      const int i0 = 2 * p, i1 = i0 + 1;
+      float h01 = 0.f;
+      if (da) h01 += dot(Ra[i0].l, Ra[i1].l) * ima + dot(Ra[i0].a, smv(Ia, Ra[i1].a));
+      if (db) h01 += dot(Rb[i0].l, Rb[i1].l) * imb + dot(Rb[i0].a, smv(Ib, Rb[i1].a));
+      const float det = diag[i0] * diag[i1] - h01 * h01;
+      float* pb = sc + (p ? S_P1 : S_P0);
+      pb[0] = diag[i0]; pb[1] = diag[i1]; pb[2] = h01; pb[3] = det > 0.f ? 1.f / det : 0.f;
     }
   }
   __syncwarp();
 }
 
 // ---------------------------------------------------------------------------
-// islands + PGS
+// PGS row steps (newt/src/solver.rs:1448-1518), generic over how the
+// residual is read and the impulse applied.
 // ---------------------------------------------------------------------------
-NEWT_D int uf_find(int* uf, int x) {
-  while (uf[x] != x) { uf[x] = uf[uf[x]]; x = uf[x]; }
-  return x;
+struct RowStep {
+  // returns the new impulse for a half-line (f >= 0) step
+  NEWT_D static float nonneg(float imp, float res, float idiag) {
+    float nf = imp - res * idiag;
+    return nf < 0.f ? 0.f : nf;
+  }
+  // 2x2 pyramidal pair; writes the new impulses
+  NEWT_D static void pair(float ii, float ij, float ri, float rj, const float* pb, float* ni_out, float* nj_out) {
+    const float h00 = pb[0], h11 = pb[1], h01 = pb[2], idet = pb[3];
+    const float di = (-ri * h11 + h01 * rj) * idet;
+    const float dj = (h01 * ri - h00 * rj) * idet;
+    const float ni = ii + di, nj = ij + dj;
+    if (ni >= 0.f && nj >= 0.f) { *ni_out = ni; *nj_out = nj; }
+    else if (ni < 0.f && nj < 0.f) { *ni_out = 0.f; *nj_out = 0.f; }
+    else if (ni < 0.f) { *ni_out = 0.f; *nj_out = fmaxf(ij - rj / h11, 0.f); }
+    else { *ni_out = fmaxf(ii - ri / h00, 0.f); *nj_out = 0.f; }
+  }
+};
+
+struct Loc { const PileGroupDev* g; int w; };
+
+// Map a flat index to (group, index within group) over cumulative segments.
+NEWT_D int find_seg(const int* seg, int ng, int t) {
+  int lo = 0, hi = ng - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (seg[mid] <= t) lo = mid; else hi = mid - 1;
+  }
+  return lo;
 }
 
-NEWT_D void islands(const WsLay& L, float* wf, int* wi, int lane) {
-  const int nb = L.nb, nc = wi[L.misc + 1];
-  if (lane == 0) {
-    int* uf = wi + L.uf;
-    for (int b = 0; b < nb; ++b) uf[b] = b;
-    for (int c = 0; c < nc; ++c) {
-      const float* cf = wf + L.con + CF * c;
-      const int* cc = wi + L.ci + CI * c;
-      if (cf[C_ACT] == 0.f || cc[2] >= nb || cc[3] >= nb) continue;
-      int ra = uf_find(uf, cc[2]), rb = uf_find(uf, cc[3]);
-      if (ra != rb) { if (ra < rb) uf[rb] = ra; else uf[ra] = rb; }
-    }
-    // island rank -> lane (round robin over roots in body order)
-    int* lanemap = wi + L.lcnt;  // reuse as per-lane counters below; roots map kept in uf sign bits
-    int rank = 0;
-    int lane_of_root[NEWT_MAX_BODIES];
-    for (int b = 0; b < nb; ++b) if (uf_find(uf, b) == b) lane_of_root[b] = (rank++) & 31;
-    for (int k = 0; k < 33; ++k) lanemap[k] = 0;
-    int* perm = wi + L.perm;
-    // counting sort of active contacts by lane, stable in contact order
-    for (int c = 0; c < nc; ++c) {
-      const float* cf = wf + L.con + CF * c;
-      const int* cc = wi + L.ci + CI * c;
-      if (cf[C_ACT] == 0.f) continue;
-      int body = cc[2] < nb ? cc[2] : cc[3];
-      lanemap[lane_of_root[uf_find(uf, body)] + 1]++;
-    }
-    for (int k = 0; k < 32; ++k) lanemap[k + 1] += lanemap[k];
-    int fill[32];
-    for (int k = 0; k < 32; ++k) fill[k] = lanemap[k];
-    for (int c = 0; c < nc; ++c) {
-      const float* cf = wf + L.con + CF * c;
-      const int* cc = wi + L.ci + CI * c;
-      if (cf[C_ACT] == 0.f) continue;
-      int body = cc[2] < nb ? cc[2] : cc[3];
-      perm[fill[lane_of_root[uf_find(uf, body)]]++] = c;
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// K1: collide + assemble (one warp per world)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) pile_k_collide(const PileGroupDev* G, const int* wseg, int ng, int total,
+                                                      IslandLists il) {
+  const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (t >= total) return;
+  const int gi = find_seg(wseg, ng, t);
+  const PileGroupDev& g = G[gi];
+  const int w = t - wseg[gi];
+  if (w >= g.n || !g.I[(size_t)w * g.lay.istride + g.lay.live]) return;
+  const WsLay L = ws_layout(g.nb, g.np, g.maxc);
+  float* wf = g.scr + (size_t)w * g.sstride;
+  int* wi = reinterpret_cast<int*>(wf + L.nf);
+  const int lane = threadIdx.x & 31;
+  ws_load(g, w, L, wf, wi, lane);
+  collide(L, wf, wi, lane);
+  assemble(L, wf, wi, lane, t, il);
+}
+
+// Resolve a list item to its world scratch and island.
+struct IslandRef {
+  const PileGroupDev* g;
+  int w, isl;
+  float* wf;
+  const int* wi;
+  WsLay L;
+};
+
+NEWT_D bool island_ref(const PileGroupDev* G, const int* wseg, int ng, int item, IslandRef* r) {
+  const int t = item >> 6;
+  r->isl = item & 63;
+  const int gi = find_seg(wseg, ng, t);
+  r->g = G + gi;
+  r->w = t - wseg[gi];
+  r->L = ws_layout(r->g->nb, r->g->np, r->g->maxc);
+  r->wf = r->g->scr + (size_t)r->w * r->g->sstride;
+  r->wi = reinterpret_cast<const int*>(r->wf + r->L.nf);
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// K2: one-body islands with at most MC contacts; every sweep in registers
+// ---------------------------------------------------------------------------
+template <int MC>
+__global__ void __launch_bounds__(128) pile_k_pgs_small(const PileGroupDev* G, const int* wseg, int ng,
+                                                        const int* items, const int* count, int cls) {
+  const int n_items = count[cls];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_items; t += gridDim.x * blockDim.x) {
+  IslandRef R;
+  island_ref(G, wseg, ng, items[t], &R);
+  const WsLay& L = R.L;
+  float* wf = R.wf;
+  const int* wi = R.wi;
+  const int isl = R.isl;
+  const int cnt = wi[L.icount + isl];
+  const int k0 = wi[L.istart + isl];
+  const int body = wi[L.ibody + wi[L.ibstart + isl]];
+  const int iters = R.g->I[(size_t)R.w * R.g->lay.istride + R.g->lay.iters];
+  const float im = 1.f / wf[L.mass + body];
+  const S3 Iw = lds(wf + L.iinvw + 6 * body);
+  J6 jn[MC], jt1[MC], jt2[MC];
+  float mu[MC], idg[MC][4], bias[MC][4], reg[MC], pb[MC][8], imp[MC][4];
+#pragma unroll
+  for (int c = 0; c < MC; ++c) {
+    if (c < cnt) {
+      const float* sc = wf + L.sc + SC * (k0 + c);
+      const bool sa = wi[L.scid + 2 * (k0 + c)] >= 0;
+      const float* J = sc + (sa ? S_JA : S_JB);
+      jn[c] = ldj(J); jt1[c] = ldj(J + 6); jt2[c] = ldj(J + 12);
+      mu[c] = sc[S_MU]; reg[c] = sc[S_REG];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) { idg[c][r] = sc[S_IDIAG + r]; bias[c][r] = sc[S_BIAS + r]; imp[c][r] = 0.f; }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) pb[c][q] = sc[S_P0 + q];
     }
   }
-  __syncwarp();
-}
-
-struct Side { bool dyn; int b; float im; V3 arm; };
-
-NEWT_D float row_resid(const float* wf, const WsLay& L, const Side& A, const Side& B, V3 dir) {
-  float s = 0.f;
-  if (A.dyn) s += dot(ld3(wf + L.dv + 3 * A.b), dir) + dot(ld3(wf + L.dw + 3 * A.b), cross(A.arm, dir));
-  if (B.dyn) s -= dot(ld3(wf + L.dv + 3 * B.b), dir) + dot(ld3(wf + L.dw + 3 * B.b), cross(B.arm, dir));
-  return s;
-}
-NEWT_D void row_apply(float* wf, const WsLay& L, const Side& A, const Side& B, V3 dir, float df) {
-  if (df == 0.f) return;
-  if (A.dyn) {
-    float* dv = wf + L.dv + 3 * A.b;
-    float* dw = wf + L.dw + 3 * A.b;
-    st3(dv, ld3(dv) + dir * (df * A.im));
-    st3(dw, ld3(dw) + smv(lds(wf + L.iinvw + 6 * A.b), cross(A.arm, dir * df)));
-  }
-  if (B.dyn) {
-    float* dv = wf + L.dv + 3 * B.b;
-    float* dw = wf + L.dw + 3 * B.b;
-    st3(dv, ld3(dv) - dir * (df * B.im));
-    st3(dw, ld3(dw) + smv(lds(wf + L.iinvw + 6 * B.b), cross(B.arm, dir * (-df))));
-  }
-}
-
-NEWT_D void pgs(const WsLay& L, float* wf, int* wi, int lane, int iters) {
-  const int nb = L.nb;
-  const int beg = wi[L.lcnt + lane], end = wi[L.lcnt + lane + 1];
+  V3 dv = v3(0.f, 0.f, 0.f), dw = v3(0.f, 0.f, 0.f);
   for (int it = 0; it < iters; ++it) {
-    for (int k = beg; k < end; ++k) {
-      const int c = wi[L.perm + k];
-      float* cf = wf + L.con + CF * c;
-      const int* cc = wi + L.ci + CI * c;
-      Side A{cc[2] < nb, cc[2], 0.f, ld3(cf + C_ARMA)}, B{cc[3] < nb, cc[3], 0.f, ld3(cf + C_ARMB)};
-      if (A.dyn) A.im = 1.f / wf[L.mass + A.b];
-      if (B.dyn) B.im = 1.f / wf[L.mass + B.b];
-      const V3 n = ld3(cf + C_N), t1 = ld3(cf + C_T1), t2 = cross(n, t1);
-      const float mu = cf[C_MU];
-      const V3 dirs[4] = {n + t1 * mu, n - t1 * mu, n + t2 * mu, n - t2 * mu};
-      float* imp = cf + C_IMP;
-      // normal-facet half-line step on row 0 (solver.rs:1448-1465)
-      {
-        float res = row_resid(wf, L, A, B, dirs[0]) + cf[C_REG] * imp[0] + cf[C_BIAS];
-        float nf = imp[0] - res / cf[C_DIAG];
-        float pr = nf < 0.f ? 0.f : nf;
-        float dl = pr - imp[0];
-        imp[0] = pr;
-        row_apply(wf, L, A, B, dirs[0], dl);
-      }
-      // two opposing-facet pairs as 2x2 blocks (solver.rs:1476-1518)
-      for (int p = 0; p < 2; ++p) {
-        const int i = 2 * p, j = 2 * p + 1;
-        const float h01 = cf[C_H01 + p];
-        float ri = row_resid(wf, L, A, B, dirs[i]) + cf[C_REG + i] * imp[i] + cf[C_BIAS + i];
-        float rj = row_resid(wf, L, A, B, dirs[j]) + cf[C_REG + j] * imp[j] + cf[C_BIAS + j];
-        const float h00 = cf[C_DIAG + i], h11 = cf[C_DIAG + j];
-        const float det = h00 * h11 - h01 * h01;
-        if (det <= 0.f) {
-          for (int q = 0; q < 2; ++q) {
-            int r = q ? j : i;
-            float res = row_resid(wf, L, A, B, dirs[r]) + cf[C_REG + r] * imp[r] + cf[C_BIAS + r];
-            float nf = imp[r] - res / cf[C_DIAG + r];
-            float pr = nf < 0.f ? 0.f : nf;
-            float dl = pr - imp[r];
-            imp[r] = pr;
-            row_apply(wf, L, A, B, dirs[r], dl);
+#pragma unroll
+    for (int c = 0; c < MC; ++c) {
+      if (c < cnt) {
+        {
+          const J6 j = jrow(jn[c], jt1[c], mu[c]);
+          const float res = jdot(j, dv, dw) + reg[c] * imp[c][0] + bias[c][0];
+          const float nf = RowStep::nonneg(imp[c][0], res, idg[c][0]);
+          const float dl = nf - imp[c][0];
+          imp[c][0] = nf;
+          dv = dv + j.l * (dl * im);
+          dw = dw + smv(Iw, j.a * dl);
+        }
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+          const J6& jt = p ? jt2[c] : jt1[c];
+          const J6 ji = jrow(jn[c], jt, mu[c]), jj = jrow(jn[c], jt, -mu[c]);
+          const int i = 2 * p, j = i + 1;
+          const float* P = pb[c] + 4 * p;
+          if (P[3] == 0.f) {  // det <= 0: two half-line steps
+            float res = jdot(ji, dv, dw) + reg[c] * imp[c][i] + bias[c][i];
+            float nf = RowStep::nonneg(imp[c][i], res, idg[c][i]);
+            float dl = nf - imp[c][i];
+            imp[c][i] = nf;
+            dv = dv + ji.l * (dl * im); dw = dw + smv(Iw, ji.a * dl);
+            res = jdot(jj, dv, dw) + reg[c] * imp[c][j] + bias[c][j];
+            nf = RowStep::nonneg(imp[c][j], res, idg[c][j]);
+            dl = nf - imp[c][j];
+            imp[c][j] = nf;
+            dv = dv + jj.l * (dl * im); dw = dw + smv(Iw, jj.a * dl);
+            continue;
           }
+          const float ri = jdot(ji, dv, dw) + reg[c] * imp[c][i] + bias[c][i];
+          const float rj = jdot(jj, dv, dw) + reg[c] * imp[c][j] + bias[c][j];
+          float ni, nj;
+          RowStep::pair(imp[c][i], imp[c][j], ri, rj, P, &ni, &nj);
+          const float ai = ni - imp[c][i], aj = nj - imp[c][j];
+          imp[c][i] = ni; imp[c][j] = nj;
+          dv = dv + ji.l * (ai * im) + jj.l * (aj * im);
+          dw = dw + smv(Iw, ji.a * ai + jj.a * aj);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < MC; ++c)
+    if (c < cnt) {
+      float* cimp = wf + L.con + CF * wi[L.sccon + k0 + c] + C_IMP;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) cimp[r] = imp[c][r];
+    }
+  st3(wf + L.dv + 3 * body, dv);
+  st3(wf + L.dw + 3 * body, dw);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K3: islands with several bodies.  MB > 0: at most MB bodies, accumulators
+// in registers (selected by island-local index); MB == 0: any size,
+// accumulators in a thread-local array.
+// ---------------------------------------------------------------------------
+template <int MB>
+struct Accs {
+  float a[MB > 0 ? MB : NEWT_MAX_BODIES][6];
+  NEWT_D void zero(int nb) {
+#pragma unroll
+    for (int b = 0; b < (MB > 0 ? MB : NEWT_MAX_BODIES); ++b)
+      if (MB > 0 || b < nb)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) a[b][q] = 0.f;
+  }
+  NEWT_D void get(int b, V3* l, V3* w) const {
+    if (MB > 0) {
+      float v[6];
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        float x = a[0][q];
+#pragma unroll
+        for (int k = 1; k < (MB > 0 ? MB : 1); ++k) x = b == k ? a[k][q] : x;
+        v[q] = x;
+      }
+      *l = v3(v[0], v[1], v[2]); *w = v3(v[3], v[4], v[5]);
+    } else {
+      *l = v3(a[b][0], a[b][1], a[b][2]); *w = v3(a[b][3], a[b][4], a[b][5]);
+    }
+  }
+  NEWT_D void add(int b, V3 l, V3 w) {
+    if (MB > 0) {
+      const float v[6] = {l.x, l.y, l.z, w.x, w.y, w.z};
+#pragma unroll
+      for (int k = 0; k < (MB > 0 ? MB : 1); ++k)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) a[k][q] += b == k ? v[q] : 0.f;
+    } else {
+      a[b][0] += l.x; a[b][1] += l.y; a[b][2] += l.z; a[b][3] += w.x; a[b][4] += w.y; a[b][5] += w.z;
+    }
+  }
+};
+
+template <int MB>
+__global__ void __launch_bounds__(128) pile_k_pgs_multi(const PileGroupDev* G, const int* wseg, int ng,
+                                                        const int* items, const int* count, int cls) {
+  const int n_items = count[cls];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_items; t += gridDim.x * blockDim.x) {
+  IslandRef R;
+  island_ref(G, wseg, ng, items[t], &R);
+  const WsLay& L = R.L;
+  float* wf = R.wf;
+  const int* wi = R.wi;
+  const int isl = R.isl;
+  const int nbody = wi[L.inb + isl], cnt = wi[L.icount + isl];
+  const int k0 = wi[L.istart + isl], b0 = wi[L.ibstart + isl];
+  const int iters = R.g->I[(size_t)R.w * R.g->lay.istride + R.g->lay.iters];
+  Accs<MB> acc;
+  acc.zero(nbody);
+  for (int it = 0; it < iters; ++it) {
+    for (int k = k0; k < k0 + cnt; ++k) {
+      float* sc = wf + L.sc + SC * k;
+      const int la = wi[L.scid + 2 * k], lb = wi[L.scid + 2 * k + 1];
+      const float mu = sc[S_MU], reg = sc[S_REG];
+      const J6 an = ldj(sc + S_JA), bn = ldj(sc + S_JB);
+      const J6 at1 = ldj(sc + S_JA + 6), bt1 = ldj(sc + S_JB + 6), at2 = ldj(sc + S_JA + 12), bt2 = ldj(sc + S_JB + 12);
+      float* imp = sc + S_IMP;
+      float ima = 0.f, imb = 0.f;
+      S3 Ia{0, 0, 0, 0, 0, 0}, Ib{0, 0, 0, 0, 0, 0};
+      if (la >= 0) { const int b = wi[L.ibody + b0 + la]; ima = 1.f / wf[L.mass + b]; Ia = lds(wf + L.iinvw + 6 * b); }
+      if (lb >= 0) { const int b = wi[L.ibody + b0 + lb]; imb = 1.f / wf[L.mass + b]; Ib = lds(wf + L.iinvw + 6 * b); }
+      V3 dva = v3(0.f, 0.f, 0.f), dwa = dva, dvb = dva, dwb = dva;
+      if (la >= 0) acc.get(la, &dva, &dwa);
+      if (lb >= 0) acc.get(lb, &dvb, &dwb);
+      float im0 = imp[0], im1 = imp[1], im2 = imp[2], im3 = imp[3];
+      auto apply = [&](const J6& ja, const J6& jb, float dl) {
+        if (la >= 0) { dva = dva + ja.l * (dl * ima); dwa = dwa + smv(Ia, ja.a * dl); }
+        if (lb >= 0) { dvb = dvb + jb.l * (dl * imb); dwb = dwb + smv(Ib, jb.a * dl); }
+      };
+      {
+        const J6 ja = jrow(an, at1, mu), jb = jrow(bn, bt1, mu);
+        const float res = jdot(ja, dva, dwa) + jdot(jb, dvb, dwb) + reg * im0 + sc[S_BIAS];
+        const float nf = RowStep::nonneg(im0, res, sc[S_IDIAG]);
+        const float dl = nf - im0;
+        im0 = nf;
+        apply(ja, jb, dl);
+      }
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {
+        const J6& at = p ? at2 : at1;
+        const J6& bt = p ? bt2 : bt1;
+        const J6 jai = jrow(an, at, mu), jbi = jrow(bn, bt, mu), jaj = jrow(an, at, -mu), jbj = jrow(bn, bt, -mu);
+        const int i = 2 * p, j = i + 1;
+        float& ii = p ? im2 : im0;
+        float& ij = p ? im3 : im1;
+        const float* P = sc + (p ? S_P1 : S_P0);
+        if (P[3] == 0.f) {
+          float res = jdot(jai, dva, dwa) + jdot(jbi, dvb, dwb) + reg * ii + sc[S_BIAS + i];
+          float nf = RowStep::nonneg(ii, res, sc[S_IDIAG + i]);
+          float dl = nf - ii;
+          ii = nf;
+          apply(jai, jbi, dl);
+          res = jdot(jaj, dva, dwa) + jdot(jbj, dvb, dwb) + reg * ij + sc[S_BIAS + j];
+          nf = RowStep::nonneg(ij, res, sc[S_IDIAG + j]);
+          dl = nf - ij;
+          ij = nf;
+          apply(jaj, jbj, dl);
           continue;
         }
-        const float di = (-ri * h11 + h01 * rj) / det;
-        const float dj = (h01 * ri - h00 * rj) / det;
-        const float ni = imp[i] + di, nj = imp[j] + dj;
-        float a, b;
-        if (ni >= 0.f && nj >= 0.f) { a = ni; b = nj; }
-        else if (ni < 0.f && nj < 0.f) { a = 0.f; b = 0.f; }
-        else if (ni < 0.f) { a = 0.f; b = fmaxf(imp[j] - rj / h11, 0.f); }
-        else { a = fmaxf(imp[i] - ri / h00, 0.f); b = 0.f; }
-        const float ai = a - imp[i], aj = b - imp[j];
-        imp[i] = a; imp[j] = b;
-        row_apply(wf, L, A, B, dirs[i], ai);
-        row_apply(wf, L, A, B, dirs[j], aj);
+        const float ri = jdot(jai, dva, dwa) + jdot(jbi, dvb, dwb) + reg * ii + sc[S_BIAS + i];
+        const float rj = jdot(jaj, dva, dwa) + jdot(jbj, dvb, dwb) + reg * ij + sc[S_BIAS + j];
+        float ni, nj;
+        RowStep::pair(ii, ij, ri, rj, P, &ni, &nj);
+        const float ai = ni - ii, aj = nj - ij;
+        ii = ni; ij = nj;
+        apply(jai, jbi, ai);
+        apply(jaj, jbj, aj);
       }
+      imp[0] = im0; imp[1] = im1; imp[2] = im2; imp[3] = im3;
+      // write the two touched accumulators back
+      if (la >= 0) { V3 l0, w0; acc.get(la, &l0, &w0); acc.add(la, dva - l0, dwa - w0); }
+      if (lb >= 0) { V3 l0, w0; acc.get(lb, &l0, &w0); acc.add(lb, dvb - l0, dwb - w0); }
     }
   }
-  __syncwarp();
+  for (int k = k0; k < k0 + cnt; ++k) {
+    const float* sc = wf + L.sc + SC * k;
+    float* cimp = wf + L.con + CF * wi[L.sccon + k] + C_IMP;
+    for (int r = 0; r < 4; ++r) cimp[r] = sc[S_IMP + r];
+  }
+  for (int b = 0; b < nbody; ++b) {
+    const int body = wi[L.ibody + b0 + b];
+    V3 l, w;
+    acc.get(b, &l, &w);
+    st3(wf + L.dv + 3 * body, l);
+    st3(wf + L.dw + 3 * body, w);
+  }
+  }
 }
 
 // ---------------------------------------------------------------------------
-// integration (world.rs:1790-1817, 3223-3245)
+// K3': islands of up to MB bodies, one thread per island (SIMT across 32
+// islands per warp).  Every facet row's J and W = M^-1 J^T come precomputed
+// from the assemble pass (S_ROWS), so a Gauss-Seidel row update is two
+// 6-wide dot products and two 6-wide axpys; each contact's rows are pulled
+// into registers with one batch of loads per sweep, and the island's body
+// accumulators live in registers.
 // ---------------------------------------------------------------------------
-NEWT_D void integrate(const WsLay& L, float* wf, int lane, uint32_t* st) {
+constexpr int MAXC3 = 32;  // contacts of a class-3 island (larger islands take class 4)
+
+NEWT_D float dot6r(const float* j, const float* a) {
+  return j[0] * a[0] + j[1] * a[1] + j[2] * a[2] + j[3] * a[3] + j[4] * a[4] + j[5] * a[5];
+}
+NEWT_D void axpy6r(float* a, const float* w, float s) {
+#pragma unroll
+  for (int q = 0; q < 6; ++q) a[q] += s * w[q];
+}
+
+template <int MB>
+__global__ void __launch_bounds__(128) pile_k_pgs_rows(const PileGroupDev* G, const int* wseg, int ng,
+                                                       const int* items, const int* count, int cls) {
+  const int n_items = count[cls];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_items; t += gridDim.x * blockDim.x) {
+    IslandRef R;
+    island_ref(G, wseg, ng, items[t], &R);
+    const WsLay& L = R.L;
+    float* wf = R.wf;
+    const int* wi = R.wi;
+    const int isl = R.isl;
+    const int nbody = wi[L.inb + isl], cnt = wi[L.icount + isl];
+    const int k0 = wi[L.istart + isl], b0 = wi[L.ibstart + isl];
+    const int iters = R.g->I[(size_t)R.w * R.g->lay.istride + R.g->lay.iters];
+    float impl[MAXC3][4];  // impulses stay thread-local during the sweeps
+    for (int k = 0; k < cnt; ++k) for (int r = 0; r < 4; ++r) impl[k][r] = 0.f;
+    float acc[MB][6];
+#pragma unroll
+    for (int b = 0; b < MB; ++b)
+#pragma unroll
+      for (int q = 0; q < 6; ++q) acc[b][q] = 0.f;
+    for (int it = 0; it < iters; ++it) {
+      for (int k = k0; k < k0 + cnt; ++k) {
+        const float* __restrict__ sc = wf + L.sc + SC * k;
+        const int la = __ldg(wi + L.scid + 2 * k), lb = __ldg(wi + L.scid + 2 * k + 1);
+        float rows[4][24];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+#pragma unroll
+          for (int q = 0; q < 12; ++q) rows[r][q] = la >= 0 ? __ldg(sc + S_ROWS + 24 * r + q) : 0.f;
+#pragma unroll
+          for (int q = 12; q < 24; ++q) rows[r][q] = lb >= 0 ? __ldg(sc + S_ROWS + 24 * r + q) : 0.f;
+        }
+        const float reg = __ldg(sc + S_REG);
+        float idg[4], bias[4], imp[4], P[8];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) { idg[r] = __ldg(sc + S_IDIAG + r); bias[r] = __ldg(sc + S_BIAS + r); imp[r] = impl[k - k0][r]; }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) P[q] = __ldg(sc + S_P0 + q);
+        float aa[6], ab[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+          float xa = 0.f, xb = 0.f;
+#pragma unroll
+          for (int b = 0; b < MB; ++b) { xa = la == b ? acc[b][q] : xa; xb = lb == b ? acc[b][q] : xb; }
+          aa[q] = xa; ab[q] = xb;
+        }
+        auto resid = [&](int r) { return dot6r(rows[r], aa) + dot6r(rows[r] + 12, ab) + reg * imp[r] + bias[r]; };
+        auto apply = [&](int r, float dl) { axpy6r(aa, rows[r] + 6, dl); axpy6r(ab, rows[r] + 18, dl); };
+        {
+          const float nf = RowStep::nonneg(imp[0], resid(0), idg[0]);
+          const float dl = nf - imp[0];
+          imp[0] = nf;
+          apply(0, dl);
+        }
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+          const int i = 2 * p, j = i + 1;
+          const float* Pp = P + 4 * p;
+          if (Pp[3] == 0.f) {
+            float nf = RowStep::nonneg(imp[i], resid(i), idg[i]);
+            float dl = nf - imp[i];
+            imp[i] = nf;
+            apply(i, dl);
+            nf = RowStep::nonneg(imp[j], resid(j), idg[j]);
+            dl = nf - imp[j];
+            imp[j] = nf;
+            apply(j, dl);
+            continue;
+          }
+          const float ri = resid(i), rj = resid(j);
+          float ni, nj;
+          RowStep::pair(imp[i], imp[j], ri, rj, Pp, &ni, &nj);
+          const float ai = ni - imp[i], aj = nj - imp[j];
+          imp[i] = ni; imp[j] = nj;
+          apply(i, ai);
+          apply(j, aj);
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) impl[k - k0][r] = imp[r];
+#pragma unroll
+        for (int b = 0; b < MB; ++b)
+#pragma unroll
+          for (int q = 0; q < 6; ++q) acc[b][q] = la == b ? aa[q] : (lb == b ? ab[q] : acc[b][q]);
+      }
+    }
+    for (int k = k0; k < k0 + cnt; ++k) {
+      float* cimp = wf + L.con + CF * wi[L.sccon + k] + C_IMP;
+      for (int r = 0; r < 4; ++r) cimp[r] = impl[k - k0][r];
+    }
+#pragma unroll
+    for (int b = 0; b < MB; ++b) {
+      if (b < nbody) {
+        const int body = wi[L.ibody + b0 + b];
+        st3(wf + L.dv + 3 * body, v3(acc[b][0], acc[b][1], acc[b][2]));
+        st3(wf + L.dw + 3 * body, v3(acc[b][3], acc[b][4], acc[b][5]));
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K4: integration + write-back (world.rs:1790-1817, 3223-3245)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) pile_k_integrate(const PileGroupDev* G, const int* wseg, int ng, int total,
+                                                        int write_diag) {
+  const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (t >= total) return;
+  const int gi = find_seg(wseg, ng, t);
+  const PileGroupDev& g = G[gi];
+  const int w = t - wseg[gi];
+  if (w >= g.n || !g.I[(size_t)w * g.lay.istride + g.lay.live]) return;
+  const WsLay L = ws_layout(g.nb, g.np, g.maxc);
+  float* wf = g.scr + (size_t)w * g.sstride;
+  const int* wi = reinterpret_cast<const int*>(wf + L.nf);
+  const int lane = threadIdx.x & 31;
   const float dt = wf[L.dtg];
   const V3 grav = v3(wf[L.dtg + 1], wf[L.dtg + 2], wf[L.dtg + 3]);
   bool bad = false;
@@ -557,175 +737,70 @@ NEWT_D void integrate(const WsLay& L, float* wf, int lane, uint32_t* st) {
     bad |= !(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(lv.x) && isfinite(lv.y) && isfinite(lv.z) &&
              isfinite(av.x) && isfinite(av.y) && isfinite(av.z));
   }
-  if (__any_sync(0xffffffffu, bad)) *st |= NEWT_WS_NONFINITE;
+  bad = __any_sync(0xffffffffu, bad);
   __syncwarp();
-}
-
-NEWT_D void world_step(const WsLay& L, float* wf, int* wi, int lane, int iters, uint32_t* st) {
-  collide(L, wf, wi, lane);
-  assemble(L, wf, wi, lane);
-  islands(L, wf, wi, lane);
-  pgs(L, wf, wi, lane, iters);
-  integrate(L, wf, lane, st);
-}
-
-}  // namespace
-
-// ---------------------------------------------------------------------------
-// fused: one warp per world, scratch record in shared memory, whole horizon
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(32) pile_fused_kernel(PileGroupDev g, int base, int count, int n_steps) {
-  extern __shared__ float smem[];
-  const int item = blockIdx.x;
-  if (item >= count) return;
-  const int w = base + item;
-  if (w >= g.n) return;
-  const int* I = g.I + (size_t)w * g.lay.istride;
-  if (!I[g.lay.live]) return;
-  const WsLay L = ws_layout(g.nb, g.np, g.maxc);
-  float* wf = smem;
-  int* wi = reinterpret_cast<int*>(smem + L.nf);
-  const int lane = threadIdx.x;
-  ws_load(g, w, L, wf, wi, lane);
-  const int iters = I[g.lay.iters];
-  uint32_t st = 0;
-  for (int s = 0; s < n_steps; ++s) world_step(L, wf, wi, lane, iters, &st);
   ws_store_state(g, w, L, wf, lane);
-  ws_store_diag(g, w, L, wf, wi, lane);
-  if (lane == 0 && st) atomicOr(reinterpret_cast<unsigned*>(g.I + (size_t)w * g.lay.istride + g.lay.status), st);
-}
-
-// persistent: blocks (one warp each) pull (group, base, count) items
-__global__ void __launch_bounds__(32) pile_persistent_kernel(const PileGroupDev* groups, const int* queue, int* counter,
-                                                             int n_items, int n_steps) {
-  extern __shared__ float smem[];
-  const int lane = threadIdx.x;
-  for (;;) {
-    int it = 0;
-    if (lane == 0) it = atomicAdd(counter, 1);
-    it = __shfl_sync(0xffffffffu, it, 0);
-    if (it >= n_items) return;
-    const PileGroupDev g = groups[queue[3 * it]];
-    const int base = queue[3 * it + 1], count = queue[3 * it + 2];
-    const WsLay L = ws_layout(g.nb, g.np, g.maxc);
-    float* wf = smem;
-    int* wi = reinterpret_cast<int*>(smem + L.nf);
-    for (int k = 0; k < count; ++k) {
-      const int w = base + k;
-      if (w >= g.n) break;
-      const int* I = g.I + (size_t)w * g.lay.istride;
-      if (!I[g.lay.live]) continue;
-      ws_load(g, w, L, wf, wi, lane);
-      const int iters = I[g.lay.iters];
-      uint32_t st = 0;
-      for (int s = 0; s < n_steps; ++s) world_step(L, wf, wi, lane, iters, &st);
-      ws_store_state(g, w, L, wf, lane);
-      ws_store_diag(g, w, L, wf, wi, lane);
-      if (lane == 0 && st) atomicOr(reinterpret_cast<unsigned*>(g.I + (size_t)w * g.lay.istride + g.lay.status), st);
-      __syncwarp();
-    }
-  }
+  if (write_diag) ws_store_diag(g, w, L, wf, wi, lane);
+  else if (lane == 0 && wi[L.misc + 2])
+    atomicOr(reinterpret_cast<unsigned*>(g.I + (size_t)w * g.lay.istride + g.lay.status), NEWT_WS_CONTACT_OVERFLOW);
+  if (lane == 0 && bad)
+    atomicOr(reinterpret_cast<unsigned*>(g.I + (size_t)w * g.lay.istride + g.lay.status), NEWT_WS_NONFINITE);
 }
 
 // ---------------------------------------------------------------------------
-// plain: one launch per stage per step, scratch record in global memory
+// launchers
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ bool plain_world(const PileGroupDev& g, int* w_out) {
-  const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  *w_out = w;
-  if (w >= g.n) return false;
-  return g.I[(size_t)w * g.lay.istride + g.lay.live] != 0;
-}
-
-__global__ void pile_plain_collide(PileGroupDev g, float* scr) {
-  int w;
-  if (!plain_world(g, &w)) return;
-  const WsLay L = ws_layout(g.nb, g.np, g.maxc);
-  float* wf = scr + (size_t)w * (L.nf + L.ni);
-  int* wi = reinterpret_cast<int*>(wf + L.nf);
-  const int lane = threadIdx.x & 31;
-  ws_load(g, w, L, wf, wi, lane);
-  collide(L, wf, wi, lane);
-}
-__global__ void pile_plain_assemble(PileGroupDev g, float* scr) {
-  int w;
-  if (!plain_world(g, &w)) return;
-  const WsLay L = ws_layout(g.nb, g.np, g.maxc);
-  float* wf = scr + (size_t)w * (L.nf + L.ni);
-  int* wi = reinterpret_cast<int*>(wf + L.nf);
-  assemble(L, wf, wi, threadIdx.x & 31);
-}
-__global__ void pile_plain_solve(PileGroupDev g, float* scr) {
-  int w;
-  if (!plain_world(g, &w)) return;
-  const WsLay L = ws_layout(g.nb, g.np, g.maxc);
-  float* wf = scr + (size_t)w * (L.nf + L.ni);
-  int* wi = reinterpret_cast<int*>(wf + L.nf);
-  const int lane = threadIdx.x & 31;
-  islands(L, wf, wi, lane);
-  pgs(L, wf, wi, lane, g.I[(size_t)w * g.lay.istride + g.lay.iters]);
-}
-__global__ void pile_plain_integrate(PileGroupDev g, float* scr) {
-  int w;
-  if (!plain_world(g, &w)) return;
-  const WsLay L = ws_layout(g.nb, g.np, g.maxc);
-  float* wf = scr + (size_t)w * (L.nf + L.ni);
-  int* wi = reinterpret_cast<int*>(wf + L.nf);
-  const int lane = threadIdx.x & 31;
-  uint32_t st = 0;
-  integrate(L, wf, lane, &st);
-  ws_store_state(g, w, L, wf, lane);
-  ws_store_diag(g, w, L, wf, wi, lane);
-  if (lane == 0 && st) atomicOr(reinterpret_cast<unsigned*>(g.I + (size_t)w * g.lay.istride + g.lay.status), st);
-}
-
 extern "C" size_t newt_pile_ws_bytes(int nb, int np, int maxc) {
   WsLay L = ws_layout(nb, np, maxc);
-  return (size_t)(L.nf + L.ni) * 4;
+  size_t words = (size_t)(L.nf + L.ni);
+  return (words + 31) / 32 * 32 * 4;
 }
 
-extern "C" size_t newt_pile_plain_scratch_bytes(const PileGroupDev& g) {
-  return newt_pile_ws_bytes(g.nb, g.np, g.maxc) * (size_t)(g.cap > 0 ? g.cap : 1);
+// Kernel attributes and resident-grid sizes (called outside stream capture).
+static int cap128 = 4096, capw = 4096;
+extern "C" void newt_pile_init() {
+  int dev = 0, sms = 1, b1 = 1, b2 = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, pile_k_pgs_small<4>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, pile_k_pgs_rows<4>, 128, 0);
+  cap128 = sms * (b1 > 0 ? b1 : 1) * 2;
+  capw = sms * (b2 > 0 ? b2 : 1) * 2;
 }
 
-extern "C" void newt_launch_pile_plain(const PileGroupDev& g, void* scratch, cudaStream_t st, int* launches) {
-  const int wpb = 4;  // fixed tile: 4 worlds (warps) per block
-  int grid = (g.n + wpb - 1) / wpb;
-  if (grid == 0) { *launches = 0; return; }
-  float* s = (float*)scratch;
-  pile_plain_collide<<<grid, 32 * wpb, 0, st>>>(g, s);
-  pile_plain_assemble<<<grid, 32 * wpb, 0, st>>>(g, s);
-  pile_plain_solve<<<grid, 32 * wpb, 0, st>>>(g, s);
-  pile_plain_integrate<<<grid, 32 * wpb, 0, st>>>(g, s);
-  *launches = 4;
-}
+// Bytes of the island work lists for `slots` island slots.
+extern "C" size_t newt_pile_list_bytes(int slots) { return ((size_t)N_ICLASS * (size_t)slots + 32) * sizeof(int); }
 
-static void set_smem(size_t bytes) {
-  static size_t done = 0;
-  if (bytes > done) {
-    cudaFuncSetAttribute(pile_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    cudaFuncSetAttribute(pile_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    done = bytes;
+// One env-step of every pile world in the table.  `lists` holds the island
+// work lists (newt_pile_list_bytes); its last 32 ints are the counters.
+// The island classes are independent: they run on three forked streams
+// (`side`, joined back with `ev[1..3]` after `ev[0]` forks them).
+extern "C" int newt_launch_pile_step(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
+                                     int total_slots, int* lists, int write_diag, cudaStream_t st,
+                                     const cudaStream_t* side, cudaEvent_t* ev) {
+  if (total_worlds <= 0) return 0;
+  IslandLists il;
+  il.items = lists;
+  il.cap = total_slots;
+  il.counts = lists + (size_t)N_ICLASS * total_slots;
+  cudaMemsetAsync(il.counts, 0, N_ICLASS * sizeof(int), st);
+  const int wpb = 4;
+  pile_k_collide<<<(total_worlds + wpb - 1) / wpb, 32 * wpb, 0, st>>>(dG, dwseg, ng, total_worlds, il);
+  // list kernels loop over their items: grids sized to the resident capacity
+  const int grid = std::min((total_slots + 127) / 128, cap128);
+  const size_t c = (size_t)total_slots;
+  cudaEventRecord(ev[0], st);
+  for (int k = 0; k < 3; ++k) cudaStreamWaitEvent(side[k], ev[0], 0);
+  pile_k_pgs_rows<4><<<grid, 128, 0, side[0]>>>(dG, dwseg, ng, il.items + 3 * c, il.counts, 3);
+  pile_k_pgs_small<4><<<grid, 128, 0, side[1]>>>(dG, dwseg, ng, il.items + 2 * c, il.counts, 2);
+  pile_k_pgs_small<2><<<grid, 128, 0, side[2]>>>(dG, dwseg, ng, il.items + 1 * c, il.counts, 1);
+  pile_k_pgs_small<1><<<grid, 128, 0, side[2]>>>(dG, dwseg, ng, il.items + 0 * c, il.counts, 0);
+  pile_k_pgs_rows<8><<<grid, 128, 0, st>>>(dG, dwseg, ng, il.items + 4 * c, il.counts, 4);
+  pile_k_pgs_multi<0><<<grid, 128, 0, st>>>(dG, dwseg, ng, il.items + 5 * c, il.counts, 5);
+  for (int k = 0; k < 3; ++k) {
+    cudaEventRecord(ev[1 + k], side[k]);
+    cudaStreamWaitEvent(st, ev[1 + k], 0);
   }
-}
-
-extern "C" void newt_launch_pile_fused(const PileGroupDev& g, int base, int count, int n_steps, cudaStream_t st) {
-  if (count <= 0) return;
-  size_t smem = newt_pile_ws_bytes(g.nb, g.np, g.maxc);
-  set_smem(smem);
-  pile_fused_kernel<<<count, 32, smem, st>>>(g, base, count, n_steps);
-}
-
-extern "C" void newt_launch_pile_persistent(const PileGroupDev* dgroups, const int* dqueue, int* dcounter, int n_items,
-                                            int n_steps, int grid, size_t smem, cudaStream_t st) {
-  if (grid <= 0 || n_items <= 0) return;
-  set_smem(smem);
-  pile_persistent_kernel<<<grid, 32, smem, st>>>(dgroups, dqueue, dcounter, n_items, n_steps);
-}
-
-extern "C" int newt_pile_blocks_per_sm(size_t smem) {
-  set_smem(smem);
-  int nb = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, pile_persistent_kernel, 32, smem);
-  return nb < 1 ? 1 : nb;
+  pile_k_integrate<<<(total_worlds + wpb - 1) / wpb, 32 * wpb, 0, st>>>(dG, dwseg, ng, total_worlds, write_diag);
+  return 8;
 }

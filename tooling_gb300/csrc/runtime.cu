@@ -172,6 +172,10 @@ int newt_gpu_destroy(newt_gpu_ctx* ctx) {
   if (ctx->l2buf) cudaFree(ctx->l2buf);
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
   for (void* p : ctx->plan_bufs) cudaFree(p);
+  for (void* p : ctx->plain_bufs) cudaFree(p);
+  if (ctx->side) cudaStreamDestroy(ctx->side);
+  for (int k = 0; k < 3; ++k) if (ctx->pside[k]) cudaStreamDestroy(ctx->pside[k]);
+  for (int k = 0; k < 4; ++k) if (ctx->pev[k]) cudaEventDestroy(ctx->pev[k]);
   cudaEventDestroy(ctx->ev[0]);
   cudaEventDestroy(ctx->ev[1]);
   cudaStreamDestroy(ctx->stream);
@@ -230,6 +234,7 @@ int newt_gpu_alloc_worlds(newt_gpu_ctx* ctx, const int32_t* model_ids, int32_t n
     if (rc != NEWT_OK) return rc;
   }
   ctx->graph_dirty = true;
+  ctx->plain_dirty = true;
   return NEWT_OK;
 }
 
@@ -244,6 +249,7 @@ int newt_gpu_free_worlds(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n) {
     ctx->free_slots.push_back(s);
   }
   ctx->graph_dirty = true;
+  ctx->plain_dirty = true;
   return NEWT_OK;
 }
 

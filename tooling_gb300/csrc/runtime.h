@@ -70,8 +70,9 @@ struct HostGroup {
   int maxc = 0;
   // tree-contact data (see tc_layout in newton_kernels.cu)
   void* tc = nullptr;
-  void* plain_scratch = nullptr;
+  void* plain_scratch = nullptr;  // pile solver scratch (cap worlds)
   size_t plain_scratch_bytes = 0;
+  long scr_stride = 0;             // floats per world in plain_scratch
 
   int reserve_indices(newt_gpu_ctx* ctx, int k, std::vector<int>& out);
   void release_index(newt_gpu_ctx* ctx, int idx);
@@ -120,6 +121,14 @@ struct newt_gpu_ctx {
   bool graph_dirty = true;
   std::vector<void*> plan_bufs;  // device queues / group tables the graph reads
   int queue_items = 0;
+  cudaStream_t side = nullptr;   // second capture branch (tree persistent kernels)
+  cudaStream_t pside[3] = {nullptr, nullptr, nullptr};  // pile island-class branches
+  cudaEvent_t pev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // plain path: one single-group table per group
+  struct PlainTable { void* dG; int* dseg; int* lists; int ng, worlds, slots; };
+  bool plain_dirty = true;
+  std::vector<PlainTable> plain_tables;
+  std::vector<void*> plain_bufs;
   size_t queue_cap = 0;
 };
 
@@ -131,6 +140,3 @@ int step_batched(newt_gpu_ctx* ctx, int n_steps);
 extern "C" int newt_tree_bucket(int L);
 extern "C" void newt_launch_tree_fused(const TreeGroupDev& g, int base, int count, int n_steps, cudaStream_t st);
 extern "C" void newt_launch_tree_plain(const TreeGroupDev& g, cudaStream_t st);
-extern "C" void newt_launch_pile_fused(const PileGroupDev& g, int base, int count, int n_steps, cudaStream_t st);
-extern "C" void newt_launch_pile_plain(const PileGroupDev& g, void* scratch, cudaStream_t st, int* launches);
-extern "C" size_t newt_pile_plain_scratch_bytes(const PileGroupDev& g);

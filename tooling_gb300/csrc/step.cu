@@ -1,8 +1,12 @@
-// Step dispatch: the plain form (one launch per stage per step, fixed tiles,
-// every group launched separately) and the batched form (one fused launch per
-// kernel family over the whole horizon, work items pulled by persistent
-// blocks from a device queue sorted by size class, captured once in a CUDA
-// graph and replayed).
+// Step dispatch.
+//
+// Plain form (the drop-in baseline): every group is launched separately,
+// one launch per stage per env-step with fixed tiles.
+// Batched form: trees run their whole horizon in one persistent launch per
+// size bucket, pulling work items from a device queue sorted by size class;
+// pile worlds of every size share one launch per stage per env-step over a
+// segment table; the whole call is captured once in a CUDA graph (trees and
+// piles as concurrent branches) and replayed.
 #include <algorithm>
 #include <cstdio>
 #include <vector>
@@ -17,46 +21,123 @@
 
 extern "C" void newt_launch_tree_persistent(const TreeGroupDev* dgroups, const int* dqueue, int* dcounter, int n_items,
                                             int bucket, int n_steps, int grid, cudaStream_t st);
-extern "C" void newt_launch_pile_persistent(const PileGroupDev* dgroups, const int* dqueue, int* dcounter, int n_items,
-                                            int n_steps, int grid, size_t smem, cudaStream_t st);
 extern "C" int newt_tree_persistent_blocks_per_sm(int bucket);
-extern "C" int newt_pile_blocks_per_sm(size_t smem);
 extern "C" size_t newt_pile_ws_bytes(int nb, int np, int maxc);
+extern "C" int newt_launch_pile_step(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
+                                     int total_slots, int* lists, int write_diag, cudaStream_t st,
+                                     const cudaStream_t* side, cudaEvent_t* ev);
+extern "C" void newt_pile_init();
+
+// Streams and events the pile step forks its island classes onto.
+static int ensure_pile_streams(newt_gpu_ctx* ctx) {
+  if (ctx->pside[0]) return NEWT_OK;
+  newt_pile_init();
+  for (int k = 0; k < 3; ++k) CKS(cudaStreamCreateWithFlags(&ctx->pside[k], cudaStreamNonBlocking));
+  for (int k = 0; k < 4; ++k) CKS(cudaEventCreateWithFlags(&ctx->pev[k], cudaEventDisableTiming));
+  return NEWT_OK;
+}
+extern "C" size_t newt_pile_list_bytes(int slots);
+extern "C" int newt_tc_step(newt_gpu_ctx* ctx, HostGroup* g, int n_steps, int fused);
 
 static int sm_count(newt_gpu_ctx* ctx) {
   static int n = 0;
   if (n == 0) { cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, ctx->device); if (n <= 0) n = 1; }
   return n;
 }
-extern "C" int newt_tc_step(newt_gpu_ctx* ctx, HostGroup* g, int n_steps, int fused);
 
 static void mark_stepped(newt_gpu_ctx* ctx) {
   for (auto& g : ctx->groups) if (g->n > 0) g->device_newer = true;
 }
 
+// Per-group solver scratch for pile worlds (world-major, cap worlds).
+static int ensure_pile_scratch(newt_gpu_ctx* ctx, HostGroup* g) {
+  int rs = ensure_pile_streams(ctx);
+  if (rs != NEWT_OK) return rs;
+  size_t per = newt_pile_ws_bytes(g->size, g->np, g->maxc);
+  size_t need = per * (size_t)g->cap;
+  if (g->plain_scratch_bytes < need) {
+    if (g->plain_scratch) cudaFree(g->plain_scratch);
+    g->plain_scratch = nullptr;
+    CKS(cudaMalloc(&g->plain_scratch, need));
+    g->plain_scratch_bytes = need;
+    ctx->graph_dirty = true;
+    ctx->plain_dirty = true;
+  }
+  g->scr_stride = (long)(per / 4);
+  return NEWT_OK;
+}
+
+// A device segment table over a set of pile groups.
+struct PileTable {
+  PileGroupDev* dG = nullptr;
+  int* dseg = nullptr;   // [ng+1] cumulative world counts
+  int* lists = nullptr;  // island work lists + counters
+  int ng = 0, worlds = 0, slots = 0;
+};
+
+static int build_pile_table(newt_gpu_ctx* ctx, const std::vector<HostGroup*>& gs, PileTable& t,
+                            std::vector<void*>& owned) {
+  std::vector<PileGroupDev> hg;
+  std::vector<int> wseg{0}, iseg{0};
+  for (HostGroup* g : gs) {
+    int rc = ensure_pile_scratch(ctx, g);
+    if (rc != NEWT_OK) return rc;
+    hg.push_back(g->pile_dev());
+    wseg.push_back(wseg.back() + g->n);
+    iseg.push_back(iseg.back() + g->n * g->size);
+  }
+  t.ng = (int)hg.size();
+  t.worlds = wseg.back();
+  t.slots = iseg.back();
+  if (t.ng == 0) return NEWT_OK;
+  CKS(cudaMalloc(&t.dG, hg.size() * sizeof(PileGroupDev)));
+  CKS(cudaMalloc(&t.dseg, wseg.size() * sizeof(int)));
+  CKS(cudaMalloc(&t.lists, newt_pile_list_bytes(t.slots)));
+  CKS(cudaMemcpy(t.dG, hg.data(), hg.size() * sizeof(PileGroupDev), cudaMemcpyHostToDevice));
+  CKS(cudaMemcpy(t.dseg, wseg.data(), wseg.size() * sizeof(int), cudaMemcpyHostToDevice));
+  owned.push_back(t.dG);
+  owned.push_back(t.dseg);
+  owned.push_back(t.lists);
+  return NEWT_OK;
+}
+
+static int launch_pile_steps(newt_gpu_ctx* ctx, const PileTable& t, int n_steps, cudaStream_t st) {
+  for (int s = 0; s < n_steps; ++s)
+    ctx->launches += newt_launch_pile_step(t.dG, t.dseg, t.ng, t.worlds, t.slots, t.lists, s == n_steps - 1, st,
+                                           ctx->pside, ctx->pev);
+  return NEWT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// plain
+// ---------------------------------------------------------------------------
 int step_plain(newt_gpu_ctx* ctx, int n_steps) {
-  for (auto& gp : ctx->groups) {
-    HostGroup* g = gp.get();
-    if (g->n == 0 || g->kind != GK_PILE) continue;
-    size_t need = newt_pile_plain_scratch_bytes(g->pile_dev());
-    if (g->plain_scratch_bytes < need) {
-      if (g->plain_scratch) cudaFree(g->plain_scratch);
-      g->plain_scratch = nullptr;
-      CKS(cudaMalloc(&g->plain_scratch, need));
-      g->plain_scratch_bytes = need;
+  // per-group single-entry tables (rebuilt when groups change)
+  if (ctx->plain_dirty) {
+    for (void* p : ctx->plain_bufs) cudaFree(p);
+    ctx->plain_bufs.clear();
+    ctx->plain_tables.clear();
+    for (auto& gp : ctx->groups) {
+      PileTable t;
+      if (gp->kind == GK_PILE && gp->n > 0) {
+        int rc = build_pile_table(ctx, {gp.get()}, t, ctx->plain_bufs);
+        if (rc != NEWT_OK) return rc;
+      }
+      ctx->plain_tables.push_back({t.dG, t.dseg, t.lists, t.ng, t.worlds, t.slots});
     }
+    ctx->plain_dirty = false;
   }
   for (int s = 0; s < n_steps; ++s) {
-    for (auto& gp : ctx->groups) {
-      HostGroup* g = gp.get();
+    for (size_t gi = 0; gi < ctx->groups.size(); ++gi) {
+      HostGroup* g = ctx->groups[gi].get();
       if (g->n == 0) continue;
       if (g->kind == GK_TREE) {
         newt_launch_tree_plain(g->tree_dev(), ctx->stream);
         ctx->launches += 2;
       } else if (g->kind == GK_PILE) {
-        int nl = 0;
-        newt_launch_pile_plain(g->pile_dev(), g->plain_scratch, ctx->stream, &nl);
-        ctx->launches += nl;
+        const auto& T = ctx->plain_tables[gi];
+        ctx->launches += newt_launch_pile_step((const PileGroupDev*)T.dG, T.dseg, T.ng, T.worlds, T.slots, T.lists,
+                                               s == n_steps - 1, ctx->stream, ctx->pside, ctx->pev);
       } else if (g->kind == GK_TREE_CONTACT) {
         int rc = newt_tc_step(ctx, g, 1, 0);
         if (rc != NEWT_OK) return rc;
@@ -68,93 +149,78 @@ int step_plain(newt_gpu_ctx* ctx, int n_steps) {
 }
 
 // ---------------------------------------------------------------------------
-// batched: persistent kernels over a size-class-sorted device queue
+// batched
 // ---------------------------------------------------------------------------
-struct QueueBuild {
-  std::vector<int> items;  // (group slot in dev array, base, count) triples, cost-sorted
-  std::vector<TreeGroupDev> tg;
-  std::vector<PileGroupDev> pg;
-  size_t smem = 0;  // pile scratch record bytes (largest group)
-};
-
-static int build_queue(newt_gpu_ctx* ctx, int bucket_or_pile, QueueBuild& qb) {
-  // Items are chunks of worlds; bigger worlds come first so the tail of the
-  // persistent grid is made of cheap items (longest-processing-time order).
-  struct It { long cost; int g, base, count; };
-  std::vector<It> its;
-  for (auto& gp : ctx->groups) {
-    HostGroup* g = gp.get();
-    if (g->n == 0) continue;
-    if (bucket_or_pile < 0) {
-      if (g->kind != GK_PILE) continue;
-      int gi = (int)qb.pg.size();
-      qb.pg.push_back(g->pile_dev());
-      qb.smem = std::max(qb.smem, newt_pile_ws_bytes(g->size, g->np, g->maxc));
-      const int chunk = 2;  // worlds per item (one warp each)
-      for (int b = 0; b < g->n; b += chunk)
-        its.push_back({(long)g->size * g->size, gi, b, std::min(chunk, g->n - b)});
-    } else {
-      if (g->kind != GK_TREE || newt_tree_bucket(g->size) != bucket_or_pile) continue;
-      int gi = (int)qb.tg.size();
-      qb.tg.push_back(g->tree_dev());
-      const int chunk = 64;  // worlds per item (one thread each)
-      for (int b = 0; b < g->n; b += chunk) its.push_back({(long)g->size, gi, b, std::min(chunk, g->n - b)});
-    }
-  }
-  std::stable_sort(its.begin(), its.end(), [](const It& a, const It& b) { return a.cost > b.cost; });
-  for (auto& i : its) { qb.items.push_back(i.g); qb.items.push_back(i.base); qb.items.push_back(i.count); }
-  return (int)its.size();
-}
-
 static int capture(newt_gpu_ctx* ctx, int n_steps) {
   std::vector<void*> bufs;
-  struct Launch { int kind; int bucket; void* dg; int* dq; int* dc; int items; size_t smem; };
-  std::vector<Launch> launches;
+  // trees: one persistent launch per size bucket over a cost-sorted queue
+  struct TreeLaunch { int bucket; TreeGroupDev* dg; int* dq; int* dc; int items; int grid; };
+  std::vector<TreeLaunch> tls;
   const int buckets[4] = {8, 16, 32, 65};
-  for (int bi = -1; bi < 4; ++bi) {
-    QueueBuild qb;
-    int nitems = build_queue(ctx, bi < 0 ? -1 : buckets[bi], qb);
-    if (nitems == 0) continue;
-    void* dg = nullptr;
-    size_t gbytes = bi < 0 ? qb.pg.size() * sizeof(PileGroupDev) : qb.tg.size() * sizeof(TreeGroupDev);
-    CKS(cudaMalloc(&dg, gbytes));
-    CKS(cudaMemcpy(dg, bi < 0 ? (void*)qb.pg.data() : (void*)qb.tg.data(), gbytes, cudaMemcpyHostToDevice));
-    int* dq = nullptr;
-    CKS(cudaMalloc(&dq, qb.items.size() * sizeof(int)));
-    CKS(cudaMemcpy(dq, qb.items.data(), qb.items.size() * sizeof(int), cudaMemcpyHostToDevice));
-    int* dc = nullptr;
-    CKS(cudaMalloc(&dc, sizeof(int)));
-    bufs.push_back(dg); bufs.push_back(dq); bufs.push_back(dc);
-    launches.push_back({bi < 0 ? GK_PILE : GK_TREE, bi < 0 ? -1 : buckets[bi], dg, dq, dc, nitems, qb.smem});
+  for (int bucket : buckets) {
+    struct It { long cost; int g, base, count; };
+    std::vector<It> its;
+    std::vector<TreeGroupDev> tg;
+    for (auto& gp : ctx->groups) {
+      HostGroup* g = gp.get();
+      if (g->n == 0 || g->kind != GK_TREE || newt_tree_bucket(g->size) != bucket) continue;
+      int gi = (int)tg.size();
+      tg.push_back(g->tree_dev());
+      const int chunk = 64;
+      for (int b = 0; b < g->n; b += chunk) its.push_back({(long)g->size, gi, b, std::min(chunk, g->n - b)});
+    }
+    if (its.empty()) continue;
+    std::stable_sort(its.begin(), its.end(), [](const It& a, const It& b) { return a.cost > b.cost; });
+    std::vector<int> q;
+    for (auto& i : its) { q.push_back(i.g); q.push_back(i.base); q.push_back(i.count); }
+    TreeLaunch L{bucket, nullptr, nullptr, nullptr, (int)its.size(), 0};
+    CKS(cudaMalloc(&L.dg, tg.size() * sizeof(TreeGroupDev)));
+    CKS(cudaMemcpy(L.dg, tg.data(), tg.size() * sizeof(TreeGroupDev), cudaMemcpyHostToDevice));
+    CKS(cudaMalloc(&L.dq, q.size() * sizeof(int)));
+    CKS(cudaMemcpy(L.dq, q.data(), q.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CKS(cudaMalloc(&L.dc, sizeof(int)));
+    bufs.push_back(L.dg); bufs.push_back(L.dq); bufs.push_back(L.dc);
+    L.grid = std::min(L.items, newt_tree_persistent_blocks_per_sm(bucket) * sm_count(ctx));
+    tls.push_back(L);
   }
-  // occupancy queries and function attributes stay outside the capture
-  std::vector<int> grids;
-  for (auto& L : launches) {
-    int per_sm = L.kind == GK_PILE ? newt_pile_blocks_per_sm(L.smem) : newt_tree_persistent_blocks_per_sm(L.bucket);
-    grids.push_back(std::min(L.items, per_sm * sm_count(ctx)));
-  }
+  // piles: one table over every pile group (largest worlds first)
+  std::vector<HostGroup*> piles;
+  for (auto& gp : ctx->groups) if (gp->n > 0 && gp->kind == GK_PILE) piles.push_back(gp.get());
+  std::stable_sort(piles.begin(), piles.end(), [](HostGroup* a, HostGroup* b) { return a->size > b->size; });
+  PileTable pt;
+  int rc = build_pile_table(ctx, piles, pt, bufs);
+  if (rc != NEWT_OK) return rc;
+
+  cudaEvent_t fork = nullptr, join = nullptr;
+  if (!ctx->side) CKS(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+  CKS(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+  CKS(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
   cudaGraph_t graph;
   CKS(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-  for (size_t li = 0; li < launches.size(); ++li) {
-    const auto& L = launches[li];
-    const int grid = grids[li];
-    cudaMemsetAsync(L.dc, 0, sizeof(int), ctx->stream);
-    if (L.kind == GK_PILE)
-      newt_launch_pile_persistent((const PileGroupDev*)L.dg, L.dq, L.dc, L.items, n_steps, grid, L.smem, ctx->stream);
-    else
-      newt_launch_tree_persistent((const TreeGroupDev*)L.dg, L.dq, L.dc, L.items, L.bucket, n_steps, grid, ctx->stream);
+  cudaEventRecord(fork, ctx->stream);
+  cudaStreamWaitEvent(ctx->side, fork, 0);
+  for (auto& L : tls) {
+    cudaMemsetAsync(L.dc, 0, sizeof(int), ctx->side);
+    newt_launch_tree_persistent(L.dg, L.dq, L.dc, L.items, L.bucket, n_steps, L.grid, ctx->side);
   }
+  cudaEventRecord(join, ctx->side);
+  int64_t before = ctx->launches;
+  if (pt.ng > 0) launch_pile_steps(ctx, pt, n_steps, ctx->stream);
+  int pile_launches = (int)(ctx->launches - before);
+  ctx->launches = before;
+  cudaStreamWaitEvent(ctx->stream, join, 0);
   cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+  cudaEventDestroy(fork);
+  cudaEventDestroy(join);
   if (ce != cudaSuccess) { ctx->err = cudaGetErrorString(ce); return NEWT_E_CUDA; }
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
   CKS(cudaGraphInstantiate(&ctx->graph_exec, graph, 0));
   cudaGraphDestroy(graph);
-  // the graph references these buffers: keep them with the context
   for (void* p : ctx->plan_bufs) cudaFree(p);
   ctx->plan_bufs = bufs;
   ctx->graph_steps = n_steps;
   ctx->graph_dirty = false;
-  ctx->queue_items = (int)launches.size();
+  ctx->queue_items = (int)tls.size() + pile_launches;
   return NEWT_OK;
 }
 
