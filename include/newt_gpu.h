@@ -158,6 +158,22 @@ NEWT_API int newt_gpu_set_qfrc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t 
 #define NEWT_STEP_PLAIN 0
 #define NEWT_STEP_BATCHED 1
 NEWT_API int newt_gpu_step(newt_gpu_ctx* ctx, int32_t n_steps, int32_t mode);
+/* Allocation-free plain step.  No counterpart in the reference (newt steps
+ * one world on the host and has no device memory to manage).
+ * Same kernels and results as newt_gpu_step(ctx, n, NEWT_STEP_PLAIN), all on
+ * the context's stream, but the pile solver's scratch, island work lists and
+ * group tables sit in one fixed device array of NEWT_STATIC_SCRATCH_BYTES per
+ * device instead of buffers from cudaMalloc: for callers that must not
+ * allocate or free device memory while they step.  About 131 KB per
+ * 16-body pile world (some 250 such worlds fit); a context that needs more
+ * gets NEWT_E_NOMEM before anything is launched.  Tree worlds need no
+ * scratch; tree-contact worlds are refused (NEWT_E_INVALID).
+ * The first call on a device sets up (symbol lookup, kernel loading): make it
+ * before any stream capture.  There is one array per device, so calls whose
+ * GPU work can overlap (two contexts or threads on one device) race; order
+ * them (newt_gpu_sync between contexts). */
+#define NEWT_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
+NEWT_API int newt_gpu_step_static(newt_gpu_ctx* ctx, int32_t n_steps);
 /* Waits for the context's stream (bounded host wait; NEWT_E_TIMEOUT). */
 NEWT_API int newt_gpu_sync(newt_gpu_ctx* ctx, int32_t timeout_ms);
 

@@ -28,7 +28,7 @@ EXPORTED = [
     "newt_gpu_alloc_worlds", "newt_gpu_free_worlds", "newt_gpu_set_state", "newt_gpu_get_state",
     "newt_gpu_set_qfrc", "newt_gpu_step", "newt_gpu_sync", "newt_gpu_world_status", "newt_gpu_get_qacc",
     "newt_gpu_get_contacts", "newt_gpu_get_impulses", "newt_gpu_event_record", "newt_gpu_event_elapsed_ms",
-    "newt_gpu_flush_l2", "newt_gpu_launch_count",
+    "newt_gpu_flush_l2", "newt_gpu_launch_count", "newt_gpu_step_static",
 ]
 
 
@@ -75,6 +75,7 @@ def load_library(path: str = LIB_PATH):
         "newt_gpu_event_elapsed_ms": ([P, P], C.c_int),
         "newt_gpu_flush_l2": ([P], C.c_int),
         "newt_gpu_launch_count": ([P], C.c_int64),
+        "newt_gpu_step_static": ([P, I32], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -166,6 +167,10 @@ class Engine:
     # -- stepping -------------------------------------------------------------
     def step(self, n_steps: int = 1, mode: int = STEP_BATCHED):
         self._ck(self.L.newt_gpu_step(self.ctx, int(n_steps), int(mode)))
+
+    def step_static(self, n_steps: int = 1):
+        """Plain step whose solver scratch is a fixed device array (no allocation)."""
+        self._ck(self.L.newt_gpu_step_static(self.ctx, int(n_steps)))
 
     def sync(self, timeout_ms: int = 600000):
         self._ck(self.L.newt_gpu_sync(self.ctx, int(timeout_ms)))

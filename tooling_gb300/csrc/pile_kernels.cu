@@ -804,3 +804,45 @@ extern "C" int newt_launch_pile_step(const PileGroupDev* dG, const int* dwseg, i
   pile_k_integrate<<<(total_worlds + wpb - 1) / wpb, 32 * wpb, 0, st>>>(dG, dwseg, ng, total_worlds, write_diag);
   return 8;
 }
+
+// Loads every kernel of the pile step and sizes the list grids, so that the
+// launches that follow create nothing on the device.  Returns the first CUDA
+// error met.
+extern "C" cudaError_t newt_pile_prepare_kernels() {
+  newt_pile_init();
+  cudaFuncAttributes a;
+  const void* fns[] = {(const void*)pile_k_collide,         (const void*)pile_k_pgs_rows<4>,
+                       (const void*)pile_k_pgs_small<4>,    (const void*)pile_k_pgs_small<2>,
+                       (const void*)pile_k_pgs_small<1>,    (const void*)pile_k_pgs_rows<8>,
+                       (const void*)pile_k_pgs_multi<0>,    (const void*)pile_k_integrate};
+  for (const void* f : fns) {
+    cudaError_t e = cudaFuncGetAttributes(&a, f);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// The stages of newt_launch_pile_step issued in order on the one stream `st`
+// (no forked streams, no events).  Results are the same: the island classes
+// touch disjoint islands.
+extern "C" int newt_launch_pile_step_serial(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
+                                            int total_slots, int* lists, int write_diag, cudaStream_t st) {
+  if (total_worlds <= 0) return 0;
+  IslandLists il;
+  il.items = lists;
+  il.cap = total_slots;
+  il.counts = lists + (size_t)N_ICLASS * total_slots;
+  cudaMemsetAsync(il.counts, 0, N_ICLASS * sizeof(int), st);
+  const int wpb = 4;
+  pile_k_collide<<<(total_worlds + wpb - 1) / wpb, 32 * wpb, 0, st>>>(dG, dwseg, ng, total_worlds, il);
+  const int grid = std::min((total_slots + 127) / 128, cap128);
+  const size_t c = (size_t)total_slots;
+  pile_k_pgs_rows<8><<<grid, 128, 0, st>>>(dG, dwseg, ng, il.items + 4 * c, il.counts, 4);
+  pile_k_pgs_multi<0><<<grid, 128, 0, st>>>(dG, dwseg, ng, il.items + 5 * c, il.counts, 5);
+  pile_k_pgs_rows<4><<<grid, 128, 0, st>>>(dG, dwseg, ng, il.items + 3 * c, il.counts, 3);
+  pile_k_pgs_small<4><<<grid, 128, 0, st>>>(dG, dwseg, ng, il.items + 2 * c, il.counts, 2);
+  pile_k_pgs_small<2><<<grid, 128, 0, st>>>(dG, dwseg, ng, il.items + 1 * c, il.counts, 1);
+  pile_k_pgs_small<1><<<grid, 128, 0, st>>>(dG, dwseg, ng, il.items + 0 * c, il.counts, 0);
+  pile_k_integrate<<<(total_worlds + wpb - 1) / wpb, 32 * wpb, 0, st>>>(dG, dwseg, ng, total_worlds, write_diag);
+  return 8;
+}

@@ -298,6 +298,19 @@ extern "C" int newt_tree_persistent_blocks_per_sm(int bucket) {
   return nb < 1 ? 1 : nb;
 }
 
+// Loads the plain-form kernels of every size bucket, so that their first
+// launch creates nothing on the device.  Returns the first CUDA error met.
+extern "C" cudaError_t newt_tree_prepare_kernels() {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaSuccess;
+#define X(M)                                                                             \
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, (const void*)tree_aba_kernel<M>);  \
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, (const void*)tree_integrate_kernel<M>);
+  NEWT_TREE_BUCKETS(X)
+#undef X
+  return e;
+}
+
 extern "C" void newt_launch_tree_plain(const TreeGroupDev& g, cudaStream_t st) {
   const int B = 128;
   int grid = (g.n + B - 1) / B;
