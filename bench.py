@@ -123,18 +123,30 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def pile_algorithmic_bytes(batch, substeps: int) -> float:
-    """Algorithmic HBM bytes of one persistent launch: each world's model and
-    state read once, its state written once (the horizon runs on-chip), and
-    the last step's contact list written out.  Model: mass, 6 inertia, 6
-    inverse inertia, shape, 3 size, 3 geom offset, 4 geom orientation,
-    friction and margin per body; one plane (7), soft params (7), dt+gravity.
-    State: 13 floats per body read and written."""
-    nb = int(batch.n_bodies[0])
-    model = nb * (1 + 6 + 6 + 1 + 3 + 3 + 4 + 2) + 7 + 2 + 7 + 4 + (nb + 1)
-    state = 13 * nb
-    contacts = 11 * 40  # ~40 contacts x (pair ints, pos, normal, pen, 4 impulses) written once
-    return float(len(batch)) * 4.0 * (model + 2 * state + contacts)
+ROW_WORDS = 117  # solver words per active contact: 4 facet rows x (J, M^-1 J^T) x 2 sides + 21 constants
+
+
+def pile_kernel_bytes(kernel: str, n_worlds: int, nb: int, work: dict) -> float:
+    """Algorithmic HBM bytes of one launch (one env-step) of a pile kernel:
+    what the kernel must read and write at least once, from the per-class
+    work of the step (islands, contacts, bodies per island class).
+      collide: each world record read (per body: position, velocity, angular
+        velocity, size, geom offset 3 each; orientation, geom orientation 4
+        each; inverse and body inertia 6 each; mass, shape; per geom friction,
+        margin, filter; plane 7, soft parameters 7, dt and gravity 4) and the
+        solver rows of every active contact written;
+      class-c solver: the rows of its contacts read, 4 impulses per contact
+        and 6 velocity deltas per body written;
+      integrate: 13 state words read and written and 6 deltas read per body."""
+    contacts, bodies = work["contacts"], work["bodies"]
+    if kernel == "pile_k_collide":
+        rec = nb * 37 + 7 + 3 * (nb + 1) + 7 + 4
+        return 4.0 * (n_worlds * rec + int(contacts.sum()) * (ROW_WORDS + 1))
+    if kernel == "pile_k_integrate":
+        return 4.0 * n_worlds * nb * (13 + 6 + 13)
+    from tooling_gb300.api import PILE_KERNELS
+    c = PILE_KERNELS.index(kernel) - 1
+    return 4.0 * (int(contacts[c]) * (ROW_WORDS + 4) + int(bodies[c]) * 6)
 
 
 def run_gpu(args, rank, ws, local, dist):
@@ -148,6 +160,8 @@ def run_gpu(args, rank, ws, local, dist):
     slots = eng.alloc(ids)
     eng.set_state(slots, batch.qpos, batch.qvel)
     S = args.substeps
+    # per-kernel timing events ride in the captured graph (on each kernel's stream)
+    eng.pile_profile(1)
     # warm-up (also captures the CUDA graph)
     for _ in range(max(3, args.warmup)):
         eng.step(S, STEP_BATCHED)
@@ -157,6 +171,8 @@ def run_gpu(args, rank, ws, local, dist):
     clocks = Clocks(local)
     clocks.start()
     per_step = []
+    kernel_ms = {}
+    work = None
     barrier(dist)
     eng.sync()
     for _ in range(args.steps):
@@ -165,6 +181,9 @@ def run_gpu(args, rank, ws, local, dist):
         eng.step(S, STEP_BATCHED)
         eng.event(1)
         per_step.append(eng.elapsed_ms())
+        kms, work = eng.pile_profile()
+        for k, v in kms.items():
+            kernel_ms[k] = kernel_ms.get(k, 0.0) + v
     eng.sync()
     barrier(dist)
     clk = clocks.stop()
@@ -203,23 +222,33 @@ def run_gpu(args, rank, ws, local, dist):
             pms += eng.elapsed_ms()
         plain = W * S * args.steps / (pms / 1e3)
     hbm, src = peaks()
-    alg = pile_algorithmic_bytes(batch, S)
     avg_ms = total_ms / args.steps
-    achieved = alg / (avg_ms / 1e3) / 1e9
+    n_launch = args.steps * S  # launches of each pile kernel in the timed region
+    dom = max(kernel_ms, key=kernel_ms.get)
+    dom_ms = kernel_ms[dom] / n_launch
+    alg = pile_kernel_bytes(dom, W, int(batch.n_bodies[0]), work)
+    achieved = alg / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else None
+    tot_k = sum(kernel_ms.values())
+    kernels = {k: {"ms_per_launch": v / n_launch, "share": v / tot_k if tot_k else None,
+                   "algorithmic_bytes": pile_kernel_bytes(k, W, int(batch.n_bodies[0]), work)}
+               for k, v in kernel_ms.items()}
     out = {
         "metric": "env-steps/s", "value": value, "unit": "env-steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": avg_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
-        "config": {"workload": "pile: free spheres/boxes on a plane, PGS 50 iterations, dt 2e-3",
+        "config": {"workload": "pile: 16 free spheres/boxes on a plane per world, PGS 50 iterations, dt 2e-3",
                    "worlds_per_gpu": W, "bodies_per_world": 16, "env_steps_per_bench_step": S,
-                   "mode": "batched (persistent kernel, CUDA graph)", "l2": "flushed between timed steps",
-                   "parallelism": f"replicas x{ws}"},
+                   "mode": "batched (8 kernels per env-step, island classes on 3 forked streams, CUDA graph)",
+                   "l2": "flushed between timed steps", "parallelism": f"replicas x{ws}"},
         "e2e": {"value": e2e, "unit": "env-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clk,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "peak_source": src,
-                     "note": "FP32/latency-bound contact solve; HBM fraction shown for the persistent launch"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm if achieved else None, "traffic": None, "peak_source": src,
+                     "algorithmic_bytes_per_launch": alg, "ms_per_launch": dom_ms,
+                     "note": "dependent Gauss-Seidel chains (latency-bound); timed live by event pairs "
+                             "on the kernel's stream inside the graph"},
+        "kernels": kernels,
         "status_flags": int(np.bitwise_or.reduce(st)) if len(st) else 0,
     }
     if plain is not None:

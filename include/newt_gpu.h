@@ -202,6 +202,23 @@ NEWT_API int newt_gpu_flush_l2(newt_gpu_ctx* ctx);                              
 /* Kernel launches issued by this context since creation. */
 NEWT_API int64_t newt_gpu_launch_count(const newt_gpu_ctx* ctx);
 
+/* Profiling surface of the free-body contact step (no counterpart in newt,
+ * whose per-phase timing lives in newt/benches/newt_perf.rs).
+ * enable >= 0 sets whether later batched steps bracket every pile kernel with
+ * a pair of timing events on the stream that kernel runs on (two event nodes
+ * per kernel in the captured graph); enable < 0 leaves the setting.
+ * Outputs (each nullable) describe the last newt_gpu_step call, after waiting
+ * for it:
+ *   kernel_ms[NEWT_PILE_KERNELS]  device time of each pile kernel summed over
+ *       that call's env-steps, in launch-table order: collide, the solvers of
+ *       island classes 0..5, integrate (zeros unless timing was on for a
+ *       batched step);
+ *   work[3 * NEWT_PILE_ISLAND_CLASSES]  islands, then contacts, then bodies
+ *       per island class in that call's last env-step. */
+#define NEWT_PILE_KERNELS 9
+#define NEWT_PILE_ISLAND_CLASSES 7
+NEWT_API int newt_gpu_pile_profile(newt_gpu_ctx* ctx, int32_t enable, float* kernel_ms, int32_t* work);
+
 #ifdef __cplusplus
 }
 #endif

@@ -76,6 +76,10 @@ def test_pgs_impulses_match_oracle_at_equal_iterations(eng, settled):
     slots = _load(eng, b)
     eng.step(1, STEP_BATCHED)
     eng.sync()
+    _, work = eng.pile_profile()
+    # the one-body kernels, the short multi-body kernel and the long-island
+    # chain kernel all have islands to solve here
+    assert (work["islands"][[0, 1, 2, 3, 5]] > 0).all(), work["islands"]
     worst = 0.0
     for w in range(len(b)):
         qp = b.qpos[b.q_off[w]:b.q_off[w] + b.nq[w]]

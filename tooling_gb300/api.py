@@ -28,8 +28,12 @@ EXPORTED = [
     "newt_gpu_alloc_worlds", "newt_gpu_free_worlds", "newt_gpu_set_state", "newt_gpu_get_state",
     "newt_gpu_set_qfrc", "newt_gpu_step", "newt_gpu_sync", "newt_gpu_world_status", "newt_gpu_get_qacc",
     "newt_gpu_get_contacts", "newt_gpu_get_impulses", "newt_gpu_event_record", "newt_gpu_event_elapsed_ms",
-    "newt_gpu_flush_l2", "newt_gpu_launch_count", "newt_gpu_step_static",
+    "newt_gpu_flush_l2", "newt_gpu_launch_count", "newt_gpu_step_static", "newt_gpu_pile_profile",
 ]
+PILE_KERNELS = ["pile_k_collide", "pile_k_pgs_small<1>", "pile_k_pgs_small<2>", "pile_k_pgs_small<4>",
+                "pile_k_pgs_lane<4,4>", "pile_k_pgs_lane<5,4>", "pile_k_pgs_lane<33,32>", "pile_k_pgs_multi<0>",
+                "pile_k_integrate"]
+PILE_ISLAND_CLASSES = 7
 
 
 class NewtError(RuntimeError):
@@ -76,6 +80,7 @@ def load_library(path: str = LIB_PATH):
         "newt_gpu_flush_l2": ([P], C.c_int),
         "newt_gpu_launch_count": ([P], C.c_int64),
         "newt_gpu_step_static": ([P, I32], C.c_int),
+        "newt_gpu_pile_profile": ([P, I32, P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -210,3 +215,13 @@ class Engine:
 
     def launch_count(self) -> int:
         return int(self.L.newt_gpu_launch_count(self.ctx))
+
+    def pile_profile(self, enable: int = -1):
+        """(per-kernel ms of the last step call, {islands, contacts, bodies} per
+        island class of its last env-step); enable 1/0 switches kernel timing
+        for later batched steps, -1 leaves it."""
+        ms = np.zeros(len(PILE_KERNELS), np.float32)
+        work = np.zeros(3 * PILE_ISLAND_CLASSES, np.int32)
+        self._ck(self.L.newt_gpu_pile_profile(self.ctx, int(enable), _p(ms), _p(work)))
+        w = work.reshape(3, PILE_ISLAND_CLASSES)
+        return dict(zip(PILE_KERNELS, ms.tolist())), {"islands": w[0], "contacts": w[1], "bodies": w[2]}

@@ -1,17 +1,20 @@
-// Free-body contact pipeline, solver half (config 1 piles and the pile half
-// of config 3).  Per env-step, four kernels run over every pile world:
+// Free-body contact pipeline, solver half (the pile worlds: free spheres and
+// boxes on a plane).  Per env-step, over every pile world:
 //
 //   K1 collide+assemble  one warp per world: load state, broadphase and
 //                        narrowphase (pile_collide.cuh), soft-constraint row
-//                        constants, contact islands
+//                        constants (J and M^-1 J^T of every facet row),
+//                        contact islands, appended to per-class work lists
 //   K2 pgs_small         one thread per island with one body and <= 4
 //                        contacts (the common resting case): accumulators,
 //                        Jacobians and impulses live in registers for all
-//                        sweeps
-//   K3 pgs_general       one thread per remaining island, accumulators in
-//                        thread-local arrays
+//                        sweeps (classes 0-2)
+//   K3a pgs_lane         one thread per multi-body island, one warp per
+//                        block spread over every SM (classes 3-5)
+//   K3b pgs_multi        fallback for islands past K3a's limits (class 6)
 //   K4 integrate         one warp per world: semi-implicit Euler, state and
 //                        diagnostics back to the world record
+// The class kernels touch disjoint islands and run concurrently.
 //
 // Restates, for FP32 on sm_103a:
 //   newt/src/solver.rs:703-1257   solve_free_bodies_diag_mode (PGS branch)
@@ -26,11 +29,13 @@
 // Gauss-Seidel is order dependent.  Rows of disjoint islands never touch the
 // same body, so sweeping each island in newt's contact order (one thread per
 // island) equals the serial sweep.  A facet row n + s*mu*t has Jacobian
-// Jn + s*mu*Jt, so each contact stores Jn, Jt1, Jt2 per side and every row
-// is formed on the fly.  Velocity accumulators are kept in world frame
-// (newt keeps the angular one in body frame; equal up to rounding).
+// Jn + s*mu*Jt; each contact stores Jn, Jt1, Jt2 per side (K2, K3b form the
+// rows on the fly) and the four rows with their M^-1 J^T (K3a).  Velocity
+// accumulators are kept in world frame (newt keeps the angular one in body
+// frame; equal up to rounding).
 #include <algorithm>
 
+#include "../../include/newt_gpu.h"
 #include "pile_collide.cuh"
 
 using namespace pile;
@@ -69,22 +74,31 @@ NEWT_D void stj(float* p, const J6& j) { p[0] = j.l.x; p[1] = j.l.y; p[2] = j.l.
 // ---------------------------------------------------------------------------
 // Island work lists: the PGS kernels run over compacted lists, one list per
 // island class so each kernel variant is sized for its islands.
-constexpr int N_ICLASS = 6;  // 1 body x {1, 2, 3-4 contacts}, <= 4 bodies, <= 8 bodies, more
+// 1 body x {1, 2, 3-4 contacts}; short multi-body islands (<= 4 contacts) with
+// <= 4 or 5 bodies; long islands (5..32 contacts); the rest
+constexpr int N_ICLASS = 7;
+constexpr int CH_MIN = 5;    // contacts of the shortest island in the long-island class
+constexpr int CH_MAXC = 32;  // contacts of the longest island in the long-island class
 struct IslandLists {
   int* items;   // N_ICLASS x cap entries: (world index in the table << 6) | island
-  int* counts;  // N_ICLASS counters, zeroed before each step
+  // zeroed before each step: [0, N_ICLASS) islands per class (the list
+  // lengths), then contacts per class, then bodies per class
+  int* counts;
   int cap;
 };
+constexpr int N_COUNTERS = 3 * N_ICLASS;
 
-// 0-2: one body with 1, 2, 3-4 contacts (thread per island, registers);
-// 3: up to 4 bodies, 4: up to 8 bodies (thread per island, precomputed rows,
-// registers; at most 32 contacts); 5: the rest (thread-local accumulators)
+// 0-2: one body with 1, 2, 3-4 contacts (pile_k_pgs_small: everything in
+// registers); 3, 4: fewer than CH_MIN contacts with up to 4 / 5 bodies, and
+// 5: CH_MIN..CH_MAXC contacts (pile_k_pgs_lane, sized per class); 6: the
+// rest (pile_k_pgs_multi).  An island is connected, so it has at most one
+// body more than contacts.
 NEWT_D int island_class(int nbody, int cnt) {
   if (nbody == 1 && cnt == 1) return 0;
   if (nbody == 1 && cnt == 2) return 1;
   if (nbody == 1 && cnt <= 4) return 2;
-  if (cnt > 32) return 5;
-  return nbody <= 4 ? 3 : (nbody <= 8 ? 4 : 5);
+  if (cnt < CH_MIN) return nbody <= 4 ? 3 : 4;
+  return (cnt <= CH_MAXC && nbody <= CH_MAXC + 1) ? 5 : 6;
 }
 
 NEWT_D void assemble(const WsLay& L, float* wf, int* wi, int lane, int t_world, const IslandLists& il) {
@@ -180,10 +194,21 @@ NEWT_D void assemble(const WsLay& L, float* wf, int* wi, int lane, int t_world, 
     }
     wi[L.misc + 3] = nisl;
     // append this world's islands to the class work lists
-    int ncls[N_ICLASS] = {0, 0, 0, 0, 0};
-    for (int i = 0; i < nisl; ++i) ncls[island_class(inb[i], icount[i])]++;
+    int ncls[N_ICLASS] = {}, ccls[N_ICLASS] = {}, bcls[N_ICLASS] = {};
+    for (int i = 0; i < nisl; ++i) {
+      const int c = island_class(inb[i], icount[i]);
+      ncls[c]++;
+      ccls[c] += icount[i];
+      bcls[c] += inb[i];
+    }
     int base[N_ICLASS];
-    for (int c = 0; c < N_ICLASS; ++c) base[c] = ncls[c] ? atomicAdd(il.counts + c, ncls[c]) : 0;
+    for (int c = 0; c < N_ICLASS; ++c) {
+      base[c] = 0;
+      if (!ncls[c]) continue;
+      base[c] = atomicAdd(il.counts + c, ncls[c]);
+      atomicAdd(il.counts + N_ICLASS + c, ccls[c]);
+      atomicAdd(il.counts + 2 * N_ICLASS + c, bcls[c]);
+    }
     for (int i = 0; i < nisl; ++i) {
       const int c = island_class(inb[i], icount[i]);
       const int slot = base[c]++;
@@ -255,11 +280,13 @@ NEWT_D void assemble(const WsLay& L, float* wf, int* wi, int lane, int t_world, 
       const float aref = -b_ * vcur - k_ * (-pen);
       sc[S_BIAS + r] = dvf - aref * dt;
       sc[S_IMP + r] = 0.f;
+      // a static side's row is stored as zeros, so the solvers need no masks
       float* row = sc + S_ROWS + 24 * r;
-      stj(row, Ra[r]);
-      stj(row + 6, J6{Ra[r].l * ima, smv(Ia, Ra[r].a)});
-      stj(row + 12, Rb[r]);
-      stj(row + 18, J6{Rb[r].l * imb, smv(Ib, Rb[r].a)});
+      const J6 z{v3(0.f, 0.f, 0.f), v3(0.f, 0.f, 0.f)};
+      stj(row, da ? Ra[r] : z);
+      stj(row + 6, da ? J6{Ra[r].l * ima, smv(Ia, Ra[r].a)} : z);
+      stj(row + 12, db ? Rb[r] : z);
+      stj(row + 18, db ? J6{Rb[r].l * imb, smv(Ib, Rb[r].a)} : z);
     }
     // pyramidal pair blocks (solver.rs:1037-1061, 1476-1518)
     for (int p = 0; p < 2; ++p) {
@@ -447,9 +474,11 @@ __global__ void __launch_bounds__(128) pile_k_pgs_small(const PileGroupDev* G, c
 }
 
 // ---------------------------------------------------------------------------
-// K3: islands with several bodies.  MB > 0: at most MB bodies, accumulators
-// in registers (selected by island-local index); MB == 0: any size,
-// accumulators in a thread-local array.
+// K3b: the fallback for islands past the lane kernels' limits (more than
+// CH_MAXC contacts), one thread per island, rows formed on the fly from the
+// contact Jacobians.  MB > 0: at most MB bodies, accumulators in registers
+// (selected by island-local index); MB == 0: any size, accumulators in a
+// thread-local array.
 // ---------------------------------------------------------------------------
 template <int MB>
 struct Accs {
@@ -585,29 +614,27 @@ __global__ void __launch_bounds__(128) pile_k_pgs_multi(const PileGroupDev* G, c
   }
 }
 
-// ---------------------------------------------------------------------------
-// K3': islands of up to MB bodies, one thread per island (SIMT across 32
-// islands per warp).  Every facet row's J and W = M^-1 J^T come precomputed
-// from the assemble pass (S_ROWS), so a Gauss-Seidel row update is two
-// 6-wide dot products and two 6-wide axpys; each contact's rows are pulled
-// into registers with one batch of loads per sweep, and the island's body
-// accumulators live in registers.
-// ---------------------------------------------------------------------------
-constexpr int MAXC3 = 32;  // contacts of a class-3 island (larger islands take class 4)
-
-NEWT_D float dot6r(const float* j, const float* a) {
-  return j[0] * a[0] + j[1] * a[1] + j[2] * a[2] + j[3] * a[3] + j[4] * a[4] + j[5] * a[5];
-}
 NEWT_D void axpy6r(float* a, const float* w, float s) {
 #pragma unroll
   for (int q = 0; q < 6; ++q) a[q] += s * w[q];
 }
+NEWT_D float tdot6(const float* j, const float* a) {
+  return ((j[0] * a[0] + j[1] * a[1]) + (j[2] * a[2] + j[3] * a[3])) + (j[4] * a[4] + j[5] * a[5]);
+}
 
-template <int MB>
-__global__ void __launch_bounds__(128) pile_k_pgs_rows(const PileGroupDev* G, const int* wseg, int ng,
-                                                       const int* items, const int* count, int cls) {
+// ---------------------------------------------------------------------------
+// K3a: multi-body islands, one thread per island, launched one warp per
+// block so that a class's islands spread over every SM and each SM's L1
+// keeps its warps' rows resident through all sweeps (the chain of dependent
+// row updates then waits on L1, not L2).  Body accumulators and impulses sit
+// in thread-local arrays indexed by the contact's island-local body ids; a
+// static side reads and writes a dummy slot (its rows are stored as zeros).
+// ---------------------------------------------------------------------------
+template <int MAXB, int MAXC>
+__global__ void __launch_bounds__(32) pile_k_pgs_lane(const PileGroupDev* G, const int* wseg, int ng,
+                                                      const int* items, const int* count, int cls) {
   const int n_items = count[cls];
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_items; t += gridDim.x * blockDim.x) {
+  for (int t = blockIdx.x * 32 + threadIdx.x; t < n_items; t += gridDim.x * 32) {
     IslandRef R;
     island_ref(G, wseg, ng, items[t], &R);
     const WsLay& L = R.L;
@@ -617,41 +644,33 @@ __global__ void __launch_bounds__(128) pile_k_pgs_rows(const PileGroupDev* G, co
     const int nbody = wi[L.inb + isl], cnt = wi[L.icount + isl];
     const int k0 = wi[L.istart + isl], b0 = wi[L.ibstart + isl];
     const int iters = R.g->I[(size_t)R.w * R.g->lay.istride + R.g->lay.iters];
-    float impl[MAXC3][4];  // impulses stay thread-local during the sweeps
-    for (int k = 0; k < cnt; ++k) for (int r = 0; r < 4; ++r) impl[k][r] = 0.f;
-    float acc[MB][6];
-#pragma unroll
-    for (int b = 0; b < MB; ++b)
-#pragma unroll
+    float acc[MAXB + 1][6];
+    float impl[MAXC][4];
+    for (int b = 0; b <= MAXB; ++b)
       for (int q = 0; q < 6; ++q) acc[b][q] = 0.f;
+    for (int k = 0; k < cnt; ++k)
+      for (int r = 0; r < 4; ++r) impl[k][r] = 0.f;
     for (int it = 0; it < iters; ++it) {
-      for (int k = k0; k < k0 + cnt; ++k) {
-        const float* __restrict__ sc = wf + L.sc + SC * k;
-        const int la = __ldg(wi + L.scid + 2 * k), lb = __ldg(wi + L.scid + 2 * k + 1);
-        float rows[4][24];
+      for (int k = 0; k < cnt; ++k) {
+        const float* __restrict__ sc = wf + L.sc + SC * (k0 + k);
+        const int la = __ldg(wi + L.scid + 2 * (k0 + k)), lb = __ldg(wi + L.scid + 2 * (k0 + k) + 1);
+        const int ia = la >= 0 ? la : MAXB, ib = lb >= 0 ? lb : MAXB;
+        float rows[96];
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
-#pragma unroll
-          for (int q = 0; q < 12; ++q) rows[r][q] = la >= 0 ? __ldg(sc + S_ROWS + 24 * r + q) : 0.f;
-#pragma unroll
-          for (int q = 12; q < 24; ++q) rows[r][q] = lb >= 0 ? __ldg(sc + S_ROWS + 24 * r + q) : 0.f;
-        }
+        for (int q = 0; q < 96; ++q) rows[q] = __ldg(sc + S_ROWS + q);
         const float reg = __ldg(sc + S_REG);
         float idg[4], bias[4], imp[4], P[8];
 #pragma unroll
-        for (int r = 0; r < 4; ++r) { idg[r] = __ldg(sc + S_IDIAG + r); bias[r] = __ldg(sc + S_BIAS + r); imp[r] = impl[k - k0][r]; }
+        for (int r = 0; r < 4; ++r) { idg[r] = __ldg(sc + S_IDIAG + r); bias[r] = __ldg(sc + S_BIAS + r); imp[r] = impl[k][r]; }
 #pragma unroll
         for (int q = 0; q < 8; ++q) P[q] = __ldg(sc + S_P0 + q);
         float aa[6], ab[6];
 #pragma unroll
-        for (int q = 0; q < 6; ++q) {
-          float xa = 0.f, xb = 0.f;
-#pragma unroll
-          for (int b = 0; b < MB; ++b) { xa = la == b ? acc[b][q] : xa; xb = lb == b ? acc[b][q] : xb; }
-          aa[q] = xa; ab[q] = xb;
-        }
-        auto resid = [&](int r) { return dot6r(rows[r], aa) + dot6r(rows[r] + 12, ab) + reg * imp[r] + bias[r]; };
-        auto apply = [&](int r, float dl) { axpy6r(aa, rows[r] + 6, dl); axpy6r(ab, rows[r] + 18, dl); };
+        for (int q = 0; q < 6; ++q) { aa[q] = acc[ia][q]; ab[q] = acc[ib][q]; }
+        auto resid = [&](int r) {
+          return (tdot6(rows + 24 * r, aa) + tdot6(rows + 24 * r + 12, ab)) + (reg * imp[r] + bias[r]);
+        };
+        auto apply = [&](int r, float dl) { axpy6r(aa, rows + 24 * r + 6, dl); axpy6r(ab, rows + 24 * r + 18, dl); };
         {
           const float nf = RowStep::nonneg(imp[0], resid(0), idg[0]);
           const float dl = nf - imp[0];
@@ -682,24 +701,19 @@ __global__ void __launch_bounds__(128) pile_k_pgs_rows(const PileGroupDev* G, co
           apply(j, aj);
         }
 #pragma unroll
-        for (int r = 0; r < 4; ++r) impl[k - k0][r] = imp[r];
+        for (int r = 0; r < 4; ++r) impl[k][r] = imp[r];
 #pragma unroll
-        for (int b = 0; b < MB; ++b)
-#pragma unroll
-          for (int q = 0; q < 6; ++q) acc[b][q] = la == b ? aa[q] : (lb == b ? ab[q] : acc[b][q]);
+        for (int q = 0; q < 6; ++q) { acc[ia][q] = aa[q]; acc[ib][q] = ab[q]; }
       }
     }
-    for (int k = k0; k < k0 + cnt; ++k) {
-      float* cimp = wf + L.con + CF * wi[L.sccon + k] + C_IMP;
-      for (int r = 0; r < 4; ++r) cimp[r] = impl[k - k0][r];
+    for (int k = 0; k < cnt; ++k) {
+      float* cimp = wf + L.con + CF * wi[L.sccon + k0 + k] + C_IMP;
+      for (int r = 0; r < 4; ++r) cimp[r] = impl[k][r];
     }
-#pragma unroll
-    for (int b = 0; b < MB; ++b) {
-      if (b < nbody) {
-        const int body = wi[L.ibody + b0 + b];
-        st3(wf + L.dv + 3 * body, v3(acc[b][0], acc[b][1], acc[b][2]));
-        st3(wf + L.dw + 3 * body, v3(acc[b][3], acc[b][4], acc[b][5]));
-      }
+    for (int b = 0; b < nbody; ++b) {
+      const int body = wi[L.ibody + b0 + b];
+      st3(wf + L.dv + 3 * body, v3(acc[b][0], acc[b][1], acc[b][2]));
+      st3(wf + L.dw + 3 * body, v3(acc[b][3], acc[b][4], acc[b][5]));
     }
   }
 }
@@ -757,52 +771,86 @@ extern "C" size_t newt_pile_ws_bytes(int nb, int np, int maxc) {
 }
 
 // Kernel attributes and resident-grid sizes (called outside stream capture).
-static int cap128 = 4096, capw = 4096;
+static int cap128 = 4096, capl = 2432;
 extern "C" void newt_pile_init() {
-  int dev = 0, sms = 1, b1 = 1, b2 = 1;
+  int dev = 0, sms = 1, b1 = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, pile_k_pgs_small<4>, 128, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, pile_k_pgs_rows<4>, 128, 0);
   cap128 = sms * (b1 > 0 ? b1 : 1) * 2;
-  capw = sms * (b2 > 0 ? b2 : 1) * 2;
+  capl = sms * 16;  // one-warp blocks of the lane kernels, spread over every SM
 }
 
 // Bytes of the island work lists for `slots` island slots.
 extern "C" size_t newt_pile_list_bytes(int slots) { return ((size_t)N_ICLASS * (size_t)slots + 32) * sizeof(int); }
 
+// Launches the solver of island class `cl` on stream `s`; list kernels loop
+// over their items, so their grids are sized to the resident capacity.
+static void launch_class(int cl, const PileGroupDev* dG, const int* dwseg, int ng, const IslandLists& il, int grid,
+                         int gridl, cudaStream_t s) {
+  const int* items = il.items + (size_t)cl * il.cap;
+  switch (cl) {
+    case 0: pile_k_pgs_small<1><<<grid, 128, 0, s>>>(dG, dwseg, ng, items, il.counts, cl); break;
+    case 1: pile_k_pgs_small<2><<<grid, 128, 0, s>>>(dG, dwseg, ng, items, il.counts, cl); break;
+    case 2: pile_k_pgs_small<4><<<grid, 128, 0, s>>>(dG, dwseg, ng, items, il.counts, cl); break;
+    case 3: pile_k_pgs_lane<4, CH_MIN - 1><<<gridl, 32, 0, s>>>(dG, dwseg, ng, items, il.counts, cl); break;
+    case 4: pile_k_pgs_lane<CH_MIN, CH_MIN - 1><<<gridl, 32, 0, s>>>(dG, dwseg, ng, items, il.counts, cl); break;
+    case 5: pile_k_pgs_lane<CH_MAXC + 1, CH_MAXC><<<gridl, 32, 0, s>>>(dG, dwseg, ng, items, il.counts, cl); break;
+    default: pile_k_pgs_multi<0><<<grid, 128, 0, s>>>(dG, dwseg, ng, items, il.counts, cl); break;
+  }
+}
+
+static_assert(N_COUNTERS <= 32, "counters live in the last 32 ints of the lists");
+static_assert(N_ICLASS + 2 == NEWT_PILE_KERNELS && N_ICLASS == NEWT_PILE_ISLAND_CLASSES,
+              "kernel table of the profiling surface");
+
 // One env-step of every pile world in the table.  `lists` holds the island
 // work lists (newt_pile_list_bytes); its last 32 ints are the counters.
 // The island classes are independent: they run on three forked streams
-// (`side`, joined back with `ev[1..3]` after `ev[0]` forks them).
+// (`side`, joined back with `ev[1..3]` after `ev[0]` forks them); the
+// long-island chain, which bounds the step, starts first on `st`.
+// `kev` (nullable): 2 * NEWT_PILE_KERNELS timing events; kernel k of the
+// step (0 collide, 1 + c the solver of island class c, N_ICLASS + 1
+// integrate) is bracketed by kev[2k], kev[2k+1] recorded on the stream it
+// runs on (external event nodes under stream capture).
 extern "C" int newt_launch_pile_step(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
                                      int total_slots, int* lists, int write_diag, cudaStream_t st,
-                                     const cudaStream_t* side, cudaEvent_t* ev) {
+                                     const cudaStream_t* side, cudaEvent_t* ev, cudaEvent_t* kev) {
   if (total_worlds <= 0) return 0;
   IslandLists il;
   il.items = lists;
   il.cap = total_slots;
   il.counts = lists + (size_t)N_ICLASS * total_slots;
-  cudaMemsetAsync(il.counts, 0, N_ICLASS * sizeof(int), st);
+  auto mark = [&](int k, int end, cudaStream_t s) {
+    if (kev) cudaEventRecordWithFlags(kev[2 * k + end], s, cudaEventRecordExternal);
+  };
+  cudaMemsetAsync(il.counts, 0, N_COUNTERS * sizeof(int), st);
   const int wpb = 4;
+  mark(0, 0, st);
   pile_k_collide<<<(total_worlds + wpb - 1) / wpb, 32 * wpb, 0, st>>>(dG, dwseg, ng, total_worlds, il);
+  mark(0, 1, st);
   // list kernels loop over their items: grids sized to the resident capacity
   const int grid = std::min((total_slots + 127) / 128, cap128);
-  const size_t c = (size_t)total_slots;
+  const int gridl = std::min((total_slots + 31) / 32, capl);
   cudaEventRecord(ev[0], st);
   for (int k = 0; k < 3; ++k) cudaStreamWaitEvent(side[k], ev[0], 0);
-  pile_k_pgs_rows<4><<<grid, 128, 0, side[0]>>>(dG, dwseg, ng, il.items + 3 * c, il.counts, 3);
-  pile_k_pgs_small<4><<<grid, 128, 0, side[1]>>>(dG, dwseg, ng, il.items + 2 * c, il.counts, 2);
-  pile_k_pgs_small<2><<<grid, 128, 0, side[2]>>>(dG, dwseg, ng, il.items + 1 * c, il.counts, 1);
-  pile_k_pgs_small<1><<<grid, 128, 0, side[2]>>>(dG, dwseg, ng, il.items + 0 * c, il.counts, 0);
-  pile_k_pgs_rows<8><<<grid, 128, 0, st>>>(dG, dwseg, ng, il.items + 4 * c, il.counts, 4);
-  pile_k_pgs_multi<0><<<grid, 128, 0, st>>>(dG, dwseg, ng, il.items + 5 * c, il.counts, 5);
+  // stream of each island class: the chain class first on `st`
+  const int order[N_ICLASS] = {5, 6, 3, 4, 2, 1, 0};
+  const cudaStream_t on[N_ICLASS] = {st, st, side[0], side[0], side[1], side[2], side[2]};
+  for (int i = 0; i < N_ICLASS; ++i) {
+    const int cl = order[i];
+    mark(1 + cl, 0, on[i]);
+    launch_class(cl, dG, dwseg, ng, il, grid, gridl, on[i]);
+    mark(1 + cl, 1, on[i]);
+  }
   for (int k = 0; k < 3; ++k) {
     cudaEventRecord(ev[1 + k], side[k]);
     cudaStreamWaitEvent(st, ev[1 + k], 0);
   }
+  mark(N_ICLASS + 1, 0, st);
   pile_k_integrate<<<(total_worlds + wpb - 1) / wpb, 32 * wpb, 0, st>>>(dG, dwseg, ng, total_worlds, write_diag);
-  return 8;
+  mark(N_ICLASS + 1, 1, st);
+  return N_ICLASS + 2;
 }
 
 // Loads every kernel of the pile step and sizes the list grids, so that the
@@ -811,9 +859,11 @@ extern "C" int newt_launch_pile_step(const PileGroupDev* dG, const int* dwseg, i
 extern "C" cudaError_t newt_pile_prepare_kernels() {
   newt_pile_init();
   cudaFuncAttributes a;
-  const void* fns[] = {(const void*)pile_k_collide,         (const void*)pile_k_pgs_rows<4>,
+  const void* fns[] = {(const void*)pile_k_collide,
                        (const void*)pile_k_pgs_small<4>,    (const void*)pile_k_pgs_small<2>,
-                       (const void*)pile_k_pgs_small<1>,    (const void*)pile_k_pgs_rows<8>,
+                       (const void*)pile_k_pgs_small<1>,    (const void*)pile_k_pgs_lane<4, CH_MIN - 1>,
+                       (const void*)pile_k_pgs_lane<CH_MIN, CH_MIN - 1>,
+                       (const void*)pile_k_pgs_lane<CH_MAXC + 1, CH_MAXC>,
                        (const void*)pile_k_pgs_multi<0>,    (const void*)pile_k_integrate};
   for (const void* f : fns) {
     cudaError_t e = cudaFuncGetAttributes(&a, f);
@@ -832,17 +882,12 @@ extern "C" int newt_launch_pile_step_serial(const PileGroupDev* dG, const int* d
   il.items = lists;
   il.cap = total_slots;
   il.counts = lists + (size_t)N_ICLASS * total_slots;
-  cudaMemsetAsync(il.counts, 0, N_ICLASS * sizeof(int), st);
+  cudaMemsetAsync(il.counts, 0, N_COUNTERS * sizeof(int), st);
   const int wpb = 4;
   pile_k_collide<<<(total_worlds + wpb - 1) / wpb, 32 * wpb, 0, st>>>(dG, dwseg, ng, total_worlds, il);
   const int grid = std::min((total_slots + 127) / 128, cap128);
-  const size_t c = (size_t)total_slots;
-  pile_k_pgs_rows<8><<<grid, 128, 0, st>>>(dG, dwseg, ng, il.items + 4 * c, il.counts, 4);
-  pile_k_pgs_multi<0><<<grid, 128, 0, st>>>(dG, dwseg, ng, il.items + 5 * c, il.counts, 5);
-  pile_k_pgs_rows<4><<<grid, 128, 0, st>>>(dG, dwseg, ng, il.items + 3 * c, il.counts, 3);
-  pile_k_pgs_small<4><<<grid, 128, 0, st>>>(dG, dwseg, ng, il.items + 2 * c, il.counts, 2);
-  pile_k_pgs_small<2><<<grid, 128, 0, st>>>(dG, dwseg, ng, il.items + 1 * c, il.counts, 1);
-  pile_k_pgs_small<1><<<grid, 128, 0, st>>>(dG, dwseg, ng, il.items + 0 * c, il.counts, 0);
+  const int gridl = std::min((total_slots + 31) / 32, capl);
+  for (int cl = N_ICLASS - 1; cl >= 0; --cl) launch_class(cl, dG, dwseg, ng, il, grid, gridl, st);
   pile_k_integrate<<<(total_worlds + wpb - 1) / wpb, 32 * wpb, 0, st>>>(dG, dwseg, ng, total_worlds, write_diag);
-  return 8;
+  return N_ICLASS + 2;
 }

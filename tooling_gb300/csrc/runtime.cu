@@ -176,6 +176,7 @@ int newt_gpu_destroy(newt_gpu_ctx* ctx) {
   if (ctx->side) cudaStreamDestroy(ctx->side);
   for (int k = 0; k < 3; ++k) if (ctx->pside[k]) cudaStreamDestroy(ctx->pside[k]);
   for (int k = 0; k < 4; ++k) if (ctx->pev[k]) cudaEventDestroy(ctx->pev[k]);
+  for (cudaEvent_t e : ctx->kev) cudaEventDestroy(e);
   cudaEventDestroy(ctx->ev[0]);
   cudaEventDestroy(ctx->ev[1]);
   cudaStreamDestroy(ctx->stream);
@@ -410,5 +411,38 @@ int newt_gpu_flush_l2(newt_gpu_ctx* ctx) {
 }
 
 int64_t newt_gpu_launch_count(const newt_gpu_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+int newt_gpu_pile_profile(newt_gpu_ctx* ctx, int32_t enable, float* kernel_ms, int32_t* work) {
+  if (!ctx) return NEWT_E_INVALID;
+  cudaSetDevice(ctx->device);
+  if (enable >= 0 && (enable != 0) != ctx->profile) {
+    ctx->profile = enable != 0;
+    ctx->graph_dirty = true;  // recapture with (or without) the event nodes
+  }
+  if (!kernel_ms && !work) return NEWT_OK;
+  int rc = newt_gpu_sync(ctx, 600000);
+  if (rc != NEWT_OK) return rc;
+  const int K = NEWT_PILE_KERNELS;
+  if (kernel_ms) {
+    for (int k = 0; k < K; ++k) kernel_ms[k] = 0.f;
+    for (int s = 0; s < ctx->kev_steps; ++s)
+      for (int k = 0; k < K; ++k) {
+        float ms = 0.f;
+        const size_t e = (size_t)2 * (K * s + k);
+        CK(cudaEventElapsedTime(&ms, ctx->kev[e], ctx->kev[e + 1]));
+        kernel_ms[k] += ms;
+      }
+  }
+  if (work) {
+    const int C = NEWT_PILE_ISLAND_CLASSES, n = 3 * C;
+    for (int k = 0; k < n; ++k) work[k] = 0;
+    for (const auto& l : ctx->last_lists) {
+      int32_t h[3 * NEWT_PILE_ISLAND_CLASSES];
+      CK(cudaMemcpy(h, l.first + (size_t)C * l.second, sizeof(h), cudaMemcpyDeviceToHost));
+      for (int k = 0; k < n; ++k) work[k] += h[k];
+    }
+  }
+  return NEWT_OK;
+}
 
 }  // extern "C"

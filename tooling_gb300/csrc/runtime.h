@@ -130,6 +130,14 @@ struct newt_gpu_ctx {
   std::vector<PlainTable> plain_tables;
   std::vector<void*> plain_bufs;
   size_t queue_cap = 0;
+  // profiling: timing events around the pile kernels of batched captures,
+  // and the island work lists (pointer, slots) the last step used
+  bool profile = false;
+  std::vector<cudaEvent_t> kev;
+  int kev_steps = 0;
+  std::vector<std::pair<int*, int>> last_lists;
+  std::vector<std::pair<int*, int>> graph_lists;  // the captured graph's, copied to last_lists per replay
+  int graph_kev_steps = 0;
 };
 
 HostGroup* find_or_make_group(newt_gpu_ctx* ctx, const HostModel& m);

@@ -25,7 +25,7 @@ extern "C" int newt_tree_persistent_blocks_per_sm(int bucket);
 extern "C" size_t newt_pile_ws_bytes(int nb, int np, int maxc);
 extern "C" int newt_launch_pile_step(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
                                      int total_slots, int* lists, int write_diag, cudaStream_t st,
-                                     const cudaStream_t* side, cudaEvent_t* ev);
+                                     const cudaStream_t* side, cudaEvent_t* ev, cudaEvent_t* kev);
 extern "C" void newt_pile_init();
 
 // Streams and events the pile step forks its island classes onto.
@@ -101,10 +101,29 @@ static int build_pile_table(newt_gpu_ctx* ctx, const std::vector<HostGroup*>& gs
   return NEWT_OK;
 }
 
+// Timing events for the pile kernels of a captured horizon (profiling only):
+// NEWT_PILE_KERNELS pairs per env-step.
+static int ensure_kernel_events(newt_gpu_ctx* ctx, int n_steps) {
+  const size_t need = (size_t)2 * NEWT_PILE_KERNELS * n_steps;
+  while (ctx->kev.size() < need) {
+    cudaEvent_t e;
+    CKS(cudaEventCreate(&e));
+    ctx->kev.push_back(e);
+  }
+  return NEWT_OK;
+}
+
 static int launch_pile_steps(newt_gpu_ctx* ctx, const PileTable& t, int n_steps, cudaStream_t st) {
+  const bool timed = ctx->profile;
+  if (timed) {
+    int rc = ensure_kernel_events(ctx, n_steps);
+    if (rc != NEWT_OK) return rc;
+  }
   for (int s = 0; s < n_steps; ++s)
     ctx->launches += newt_launch_pile_step(t.dG, t.dseg, t.ng, t.worlds, t.slots, t.lists, s == n_steps - 1, st,
-                                           ctx->pside, ctx->pev);
+                                           ctx->pside, ctx->pev,
+                                           timed ? ctx->kev.data() + (size_t)2 * NEWT_PILE_KERNELS * s : nullptr);
+  ctx->graph_kev_steps = timed ? n_steps : 0;
   return NEWT_OK;
 }
 
@@ -127,6 +146,10 @@ int step_plain(newt_gpu_ctx* ctx, int n_steps) {
     }
     ctx->plain_dirty = false;
   }
+  ctx->last_lists.clear();
+  for (const auto& T : ctx->plain_tables)
+    if (T.lists) ctx->last_lists.push_back({T.lists, T.slots});
+  ctx->kev_steps = 0;
   for (int s = 0; s < n_steps; ++s) {
     for (size_t gi = 0; gi < ctx->groups.size(); ++gi) {
       HostGroup* g = ctx->groups[gi].get();
@@ -137,7 +160,7 @@ int step_plain(newt_gpu_ctx* ctx, int n_steps) {
       } else if (g->kind == GK_PILE) {
         const auto& T = ctx->plain_tables[gi];
         ctx->launches += newt_launch_pile_step((const PileGroupDev*)T.dG, T.dseg, T.ng, T.worlds, T.slots, T.lists,
-                                               s == n_steps - 1, ctx->stream, ctx->pside, ctx->pev);
+                                               s == n_steps - 1, ctx->stream, ctx->pside, ctx->pev, nullptr);
       } else if (g->kind == GK_TREE_CONTACT) {
         int rc = newt_tc_step(ctx, g, 1, 0);
         if (rc != NEWT_OK) return rc;
@@ -196,6 +219,13 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
   CKS(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
   CKS(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
   cudaGraph_t graph;
+  if (ctx->profile) {
+    int r = ensure_kernel_events(ctx, n_steps);
+    if (r != NEWT_OK) return r;
+  }
+  ctx->graph_lists.clear();
+  if (pt.ng > 0) ctx->graph_lists.push_back({pt.lists, pt.slots});
+  ctx->graph_kev_steps = 0;
   CKS(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
   cudaEventRecord(fork, ctx->stream);
   cudaStreamWaitEvent(ctx->side, fork, 0);
@@ -235,6 +265,8 @@ int step_batched(newt_gpu_ctx* ctx, int n_steps) {
     CKS(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
     ctx->launches += ctx->queue_items;
   }
+  ctx->last_lists = ctx->graph_lists;
+  ctx->kev_steps = ctx->graph_kev_steps;
   if (has_tc) {
     for (auto& gp : ctx->groups)
       if (gp->n > 0 && gp->kind == GK_TREE_CONTACT) {
