@@ -38,7 +38,25 @@ template <class R> void World<R>::step() {
   tree_qfrc.assign(trees.size(), std::vector<R>());
   for (size_t t = 0; t < trees.size(); ++t) tree_qfrc[t].assign(trees[t].nv(), R(0));
   tree_body_wrenches.assign(bodies.size(), Wrench<R>{Vec3<R>(), Vec3<R>()});
-  if (solver) solve_tree_contacts(*this, tree_contacts, solver_mode == M_NEWTON);
+  if (solver) solve_tree_contacts(*this, tree_contacts, solver_mode == M_NEWTON, integrator == 1);
+  if (integrator == 0) {
+    // RK4 (world.rs:1495-1498): step_bodies, then step_trees (world.rs:1826-1945)
+    // with the solver's generalised forces held over the four stages.
+    if (!bodies.empty()) throw std::runtime_error("RK4 free-body stepping is not restated");
+    for (size_t ti = 0; ti < trees.size(); ++ti) {
+      Tree<R>& tree = trees[ti];
+      const bool prior = tree.disable_penalty_limits;
+      if (solver) {
+        for (int s = 0; s < tree.nv(); ++s) tree.qfrc_applied[s] += tree_qfrc[ti][s];
+        tree.disable_penalty_limits = true;
+      }
+      rk4_step_tree(tree, gravity, dt);
+      if (solver)
+        for (int s = 0; s < tree.nv(); ++s) tree.qfrc_applied[s] -= tree_qfrc[ti][s];
+      tree.disable_penalty_limits = prior;
+    }
+    return;
+  }
   // step_trees_euler (world.rs:1952-2051)
   for (size_t ti = 0; ti < trees.size(); ++ti) {
     Tree<R>& tree = trees[ti];

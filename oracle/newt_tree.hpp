@@ -356,6 +356,66 @@ template <class R> void integrate_tree_positions(Tree<R>& t, R dt) {
   }
 }
 
+// tree.rs:1485-1550 (tree_deriv): dq from the stage state, dv = qddot.
+template <class R> void tree_deriv(const Tree<R>& t, const std::vector<R>& qdd, std::vector<R>& dq, std::vector<R>& dv) {
+  dq.assign(t.q.size(), R(0));
+  dv = qdd;
+  for (size_t i = 0; i < t.links.size(); ++i) {
+    const int qo = t.q_off[i], vo = t.v_off[i];
+    switch (t.links[i].type) {
+      case J_FREE: {
+        const Quat<R> ori(t.q[qo + 3], t.q[qo + 4], t.q[qo + 5], t.q[qo + 6]);
+        const Vec3<R> wb(t.qdot[vo], t.qdot[vo + 1], t.qdot[vo + 2]);
+        const Vec3<R> vb(t.qdot[vo + 3], t.qdot[vo + 4], t.qdot[vo + 5]);
+        const Vec3<R> vw = ori.rotate(vb);
+        dq[qo] = vw.x; dq[qo + 1] = vw.y; dq[qo + 2] = vw.z;
+        const Quat<R> d = ori.derivative(wb);
+        dq[qo + 3] = d.x; dq[qo + 4] = d.y; dq[qo + 5] = d.z; dq[qo + 6] = d.w;
+        break;
+      }
+      case J_HINGE: case J_SLIDE: dq[qo] = t.qdot[vo]; break;
+      case J_BALL: {
+        const Quat<R> qb(t.q[qo], t.q[qo + 1], t.q[qo + 2], t.q[qo + 3]);
+        const Quat<R> d = qb.derivative(Vec3<R>(t.qdot[vo], t.qdot[vo + 1], t.qdot[vo + 2]));
+        dq[qo] = d.x; dq[qo + 1] = d.y; dq[qo + 2] = d.z; dq[qo + 3] = d.w;
+        break;
+      }
+      default: break;
+    }
+  }
+}
+
+// tree.rs:1234-1364 (rk4_step_with_workspace): four explicit ABA stages with
+// the external wrenches held at zero (solver mode), then quaternion
+// renormalisation of free and ball joints.  No actuators, no mocap roots.
+template <class R> void rk4_step_tree(Tree<R>& t, Vec3<R> gravity, R dt) {
+  const std::vector<R> q0 = t.q, v0 = t.qdot;
+  const std::vector<Wrench<R>> ext(t.links.size(), Wrench<R>{Vec3<R>(), Vec3<R>()});
+  std::vector<Pose<R>> poses;
+  std::vector<R> qdd, dq[4], dv[4];
+  for (int s = 0; s < 4; ++s) {
+    forward_kinematics(t, poses);
+    aba(t, poses, gravity, ext, R(0), qdd);
+    tree_deriv(t, qdd, dq[s], dv[s]);
+    if (s == 3) break;
+    const R h = s < 2 ? dt * R(0.5) : dt;
+    for (size_t j = 0; j < q0.size(); ++j) t.q[j] = q0[j] + dq[s][j] * h;
+    for (size_t j = 0; j < v0.size(); ++j) t.qdot[j] = v0[j] + dv[s][j] * h;
+  }
+  const R sixth = R(1) / R(6);
+  for (size_t j = 0; j < q0.size(); ++j)
+    t.q[j] = q0[j] + (dq[0][j] + R(2) * dq[1][j] + R(2) * dq[2][j] + dq[3][j]) * (dt * sixth);
+  for (size_t j = 0; j < v0.size(); ++j)
+    t.qdot[j] = v0[j] + (dv[0][j] + R(2) * dv[1][j] + R(2) * dv[2][j] + dv[3][j]) * (dt * sixth);
+  for (size_t i = 0; i < t.links.size(); ++i) {
+    const int type = t.links[i].type;
+    if (!(type == J_FREE && i == 0) && type != J_BALL) continue;
+    const int o = t.q_off[i] + (type == J_FREE ? 3 : 0);
+    const Quat<R> q = Quat<R>(t.q[o], t.q[o + 1], t.q[o + 2], t.q[o + 3]).renormalize();
+    t.q[o] = q.x; t.q[o + 1] = q.y; t.q[o + 2] = q.z; t.q[o + 3] = q.w;
+  }
+}
+
 // tree.rs:1393-1420 (non-implicit-fast Euler; no mocap roots).  Returns the
 // qacc used for the step through `qacc_out` when it is non-null.
 template <class R> void euler_step_tree(Tree<R>& t, Vec3<R> gravity, R dt, std::vector<R>* qacc_out = nullptr) {

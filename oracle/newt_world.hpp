@@ -680,6 +680,7 @@ template <class R> struct World {
   Vec3<R> gravity = Vec3<R>(0, 0, R(-9.81));
   int solver_mode = M_PGS;
   int iterations = 20;
+  int integrator = 1;  // 0: RK4 (newt's default), 1: semi-implicit Euler (world.rs:76-84)
   std::vector<Body<R>> bodies;
   std::vector<Tree<R>> trees;
   std::vector<Geom<R>> geoms;

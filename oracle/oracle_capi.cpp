@@ -192,8 +192,10 @@ template <class R> void set_qfrc(World<R>& w, const float* qfrc) {
 
 template <class R>
 int run_one(const newt_model_desc& d, const float* qpos, const float* qvel, const float* qfrc, int n_steps, int layout,
+            int integrator,
             double* qpos_out, double* qvel_out, double* qacc_out) {
   World<R> w = build_world<R>(d);
+  w.integrator = integrator;
   set_state(w, qpos, qvel, layout);
   set_qfrc(w, qfrc);
   std::vector<R> qacc;
@@ -226,9 +228,11 @@ int oracle_model_dims(const newt_model_desc* d, int* nq, int* nv) { return dims(
 // Steps `n_worlds` worlds independently.  World w uses models[model_of_world[w]]
 // and the w-th qpos/qvel/qfrc block (blocks concatenated).  Outputs are double.
 // n_threads > 1 partitions worlds statically across host threads.
-int oracle_run(const newt_model_desc* models, int n_worlds, const int* model_of_world, const float* qpos,
-               const float* qvel, const float* qfrc, int n_steps, int precision, int layout, double* qpos_out,
-               double* qvel_out, double* qacc_out, int n_threads) {
+// integrator: 1 semi-implicit Euler (the stepped path), 0 RK4 (newt's default,
+// used to replay its RK4 goldens).
+int oracle_run_ex(const newt_model_desc* models, int n_worlds, const int* model_of_world, const float* qpos,
+                  const float* qvel, const float* qfrc, int n_steps, int precision, int layout, double* qpos_out,
+                  double* qvel_out, double* qacc_out, int n_threads, int integrator) {
   std::vector<long> qo(n_worlds + 1, 0), vo(n_worlds + 1, 0);
   for (int w = 0; w < n_worlds; ++w) {
     int nq, nv; dims(models[model_of_world[w]], &nq, &nv);
@@ -240,10 +244,10 @@ int oracle_run(const newt_model_desc* models, int n_worlds, const int* model_of_
       const newt_model_desc& d = models[model_of_world[w]];
       try {
         if (precision == 0)
-          run_one<float>(d, qpos + qo[w], qvel + vo[w], qfrc ? qfrc + vo[w] : nullptr, n_steps, layout,
+          run_one<float>(d, qpos + qo[w], qvel + vo[w], qfrc ? qfrc + vo[w] : nullptr, n_steps, layout, integrator,
                          qpos_out + qo[w], qvel_out + vo[w], qacc_out ? qacc_out + vo[w] : nullptr);
         else
-          run_one<double>(d, qpos + qo[w], qvel + vo[w], qfrc ? qfrc + vo[w] : nullptr, n_steps, layout,
+          run_one<double>(d, qpos + qo[w], qvel + vo[w], qfrc ? qfrc + vo[w] : nullptr, n_steps, layout, integrator,
                           qpos_out + qo[w], qvel_out + vo[w], qacc_out ? qacc_out + vo[w] : nullptr);
       } catch (const std::exception& e) {
         std::fprintf(stderr, "oracle_run world %d: %s\n", w, e.what());
@@ -261,6 +265,49 @@ int oracle_run(const newt_model_desc* models, int n_worlds, const int* model_of_
     for (auto& x : th) x.join();
   }
   return err.load();
+}
+
+int oracle_run(const newt_model_desc* models, int n_worlds, const int* model_of_world, const float* qpos,
+               const float* qvel, const float* qfrc, int n_steps, int precision, int layout, double* qpos_out,
+               double* qvel_out, double* qacc_out, int n_threads) {
+  return oracle_run_ex(models, n_worlds, model_of_world, qpos, qvel, qfrc, n_steps, precision, layout, qpos_out,
+                       qvel_out, qacc_out, n_threads, 1);
+}
+
+// Row impulses of one world's tree-contact solve at its state (MuJoCo
+// layout; the Euler form of the step), in row order: 4 facet rows per
+// pyramidal condim-3 contact, 1 per condim-1 contact.  Also returns the
+// tree's generalised contact forces (nv) when qfrc_out is non-null.
+int oracle_tree_impulses(const newt_model_desc* d, const float* qpos, const float* qvel, const float* qfrc,
+                         int precision, int cap, int* n_out, double* impulses, double* qfrc_out) {
+  int rc = 0;
+  auto go = [&](auto tag) {
+    using R = decltype(tag);
+    World<R> w = build_world<R>(*d);
+    set_state(w, qpos, qvel, 0);
+    set_qfrc(w, qfrc);
+    std::vector<Contact<R>> cs, tc;
+    w.detect_contacts(cs);
+    for (const Contact<R>& c : cs)
+      if (w.geoms[c.ga].att_kind() == 2 || w.geoms[c.gb].att_kind() == 2) tc.push_back(c);
+    w.tree_qfrc.assign(w.trees.size(), std::vector<R>());
+    for (size_t t = 0; t < w.trees.size(); ++t) w.tree_qfrc[t].assign(w.trees[t].nv(), R(0));
+    w.tree_body_wrenches.assign(w.bodies.size(), Wrench<R>{Vec3<R>(), Vec3<R>()});
+    std::vector<R> imp;
+    try {
+      solve_tree_contacts(w, tc, w.solver_mode == M_NEWTON, true, &imp);
+    } catch (const std::exception& e) {
+      std::fprintf(stderr, "oracle_tree_impulses: %s\n", e.what());
+      rc = 1;
+      return;
+    }
+    *n_out = (int)imp.size();
+    for (int i = 0; i < (int)imp.size() && i < cap; ++i) impulses[i] = (double)imp[i];
+    if (qfrc_out && !w.trees.empty())
+      for (int k = 0; k < w.trees[0].nv(); ++k) qfrc_out[k] = (double)w.tree_qfrc[0][k];
+  };
+  if (precision == 0) go(0.0f); else go(0.0);
+  return rc;
 }
 
 // Contacts of one world at its given state (MuJoCo layout), detected exactly

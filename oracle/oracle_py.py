@@ -38,6 +38,10 @@ def lib():
         P = C.c_void_p
         L.oracle_run.argtypes = [P, C.c_int, P, P, P, P, C.c_int, C.c_int, C.c_int, P, P, P, C.c_int]
         L.oracle_run.restype = C.c_int
+        L.oracle_run_ex.argtypes = [P, C.c_int, P, P, P, P, C.c_int, C.c_int, C.c_int, P, P, P, C.c_int, C.c_int]
+        L.oracle_run_ex.restype = C.c_int
+        L.oracle_tree_impulses.argtypes = [P, P, P, P, C.c_int, C.c_int, P, P, P]
+        L.oracle_tree_impulses.restype = C.c_int
         L.oracle_contacts.argtypes = [P, P, P, C.c_int, C.c_int, P, P, P]
         L.oracle_impulses.argtypes = [P, P, P, C.c_int, C.c_int, C.c_int, P, P]
         L.oracle_mass_matrix.argtypes = [P, P, C.c_int, P]
@@ -56,8 +60,10 @@ def _ptr(a: Optional[np.ndarray]):
 
 
 def run(packed, model_of_world: np.ndarray, qpos: np.ndarray, qvel: np.ndarray, qfrc: Optional[np.ndarray],
-        n_steps: int, precision: int = 1, layout: int = 0, want_qacc: bool = False, n_threads: int = 1):
-    """Step worlds on the CPU; returns (qpos, qvel[, qacc]) as float64 arrays."""
+        n_steps: int, precision: int = 1, layout: int = 0, want_qacc: bool = False, n_threads: int = 1,
+        integrator: int = 1):
+    """Step worlds on the CPU; returns (qpos, qvel[, qacc]) as float64 arrays.
+    integrator 1 = semi-implicit Euler (the GPU path), 0 = RK4 (newt's default)."""
     mow = np.ascontiguousarray(model_of_world, dtype=np.int32)
     qpos = np.ascontiguousarray(qpos, dtype=np.float32)
     qvel = np.ascontiguousarray(qvel, dtype=np.float32)
@@ -65,8 +71,9 @@ def run(packed, model_of_world: np.ndarray, qpos: np.ndarray, qvel: np.ndarray, 
     qo = np.zeros(qpos.shape[0], dtype=np.float64)
     vo = np.zeros(qvel.shape[0], dtype=np.float64)
     qa = np.zeros(qvel.shape[0], dtype=np.float64) if want_qacc else None
-    rc = lib().oracle_run(C.cast(packed.descs, C.c_void_p), len(mow), _ptr(mow), _ptr(qpos), _ptr(qvel), _ptr(qf),
-                          int(n_steps), int(precision), int(layout), _ptr(qo), _ptr(vo), _ptr(qa), int(n_threads))
+    rc = lib().oracle_run_ex(C.cast(packed.descs, C.c_void_p), len(mow), _ptr(mow), _ptr(qpos), _ptr(qvel), _ptr(qf),
+                             int(n_steps), int(precision), int(layout), _ptr(qo), _ptr(vo), _ptr(qa), int(n_threads),
+                             int(integrator))
     if rc != 0:
         raise RuntimeError("oracle_run failed")
     return (qo, vo, qa) if want_qacc else (qo, vo)
@@ -93,6 +100,22 @@ def impulses(packed, index: int, qpos: np.ndarray, qvel: np.ndarray, precision: 
     d = C.cast(C.byref(packed.descs[index]), C.c_void_p)
     lib().oracle_impulses(d, _ptr(qpos), _ptr(qvel), precision, iterations, cap, C.byref(n), _ptr(out))
     return out[: min(n.value, cap)]
+
+
+def tree_impulses(packed, index: int, qpos: np.ndarray, qvel: np.ndarray, qfrc: Optional[np.ndarray] = None,
+                  precision: int = 1, cap: int = 4096):
+    """Row impulses and generalised contact forces of one world's tree-contact
+    solve at its state (Euler form); returns (impulses, qfrc_contact)."""
+    qpos = np.ascontiguousarray(qpos, dtype=np.float32)
+    qvel = np.ascontiguousarray(qvel, dtype=np.float32)
+    qf = None if qfrc is None else np.ascontiguousarray(qfrc, dtype=np.float32)
+    n = C.c_int(0)
+    out = np.zeros(cap, dtype=np.float64)
+    qc = np.zeros(qvel.shape[0], dtype=np.float64)
+    d = C.cast(C.byref(packed.descs[index]), C.c_void_p)
+    if lib().oracle_tree_impulses(d, _ptr(qpos), _ptr(qvel), _ptr(qf), precision, cap, C.byref(n), _ptr(out), _ptr(qc)):
+        raise RuntimeError("oracle_tree_impulses failed")
+    return out[: min(n.value, cap)], qc
 
 
 def mass_matrix(packed, index: int, q_native: np.ndarray, nv: int, precision: int = 1) -> np.ndarray:

@@ -125,3 +125,95 @@ def test_double_pendulum_euler_matches_mujoco_capture(precision, qtol, vtol):
         worst_q = max(worst_q, np.abs(qo - ref["qpos"][k]).max())
         worst_v = max(worst_v, np.abs(vo - ref["qvel"][k]).max())
     assert worst_q <= qtol and worst_v <= vtol, (worst_q, worst_v)
+
+
+def _tree_contact_scene(solver):
+    """newt/tests/solver_golden.rs:93-144: a free-root tree with one hinge
+    child, a box on each link, resting on a plane (newt's default RK4)."""
+    w = M.WorldModel(dt=0.005, gravity=(0.0, 0.0, -9.81), solver=solver, iterations=30,
+                     tree_self_collision=1)  # newt collides in-tree pairs by default (world.rs:340)
+    plane = M.static_plane(friction=0.7)
+    plane.solref = (0.05, 1.5)
+    w.add_geom(plane)
+    gold = _read_f32("solver_tree.bin").reshape(4, 15)
+    root_q = [float(x) for x in gold[0, 3:7]]  # Quat::from_axis_angle(normalize(1, 0.4, -0.2), 0.35)
+    w.push_link(M.Link(parent=-1, joint=M.JOINT_FREE, jp_pos=(0.13, -0.07, 0.78), jp_quat=root_q, mass=1.2,
+                       inertia=M._diag9(0.08, 0.09, 0.1)))
+    w.push_link(M.Link(parent=0, joint=M.JOINT_HINGE, axis=(0.0, 1.0, 0.0), jp_pos=(0.0, 0.0, -0.3),
+                       jc_pos=(0.0, 0.0, 0.22), mass=0.75, inertia=M._diag9(0.02, 0.025, 0.018)))
+    w.add_geom(M.Geom(shape=M.SHAPE_BOX, link=0, size=(0.22, 0.17, 0.19), local_pos=(0.08, -0.06, 0.0),
+                      local_quat=quat_from_axis_angle((0.0, 1.0, 0.0), 0.2), friction=0.7))
+    w.add_geom(M.Geom(shape=M.SHAPE_BOX, link=1, size=(0.14, 0.12, 0.24), local_pos=(0.0, 0.0, -0.18),
+                      local_quat=quat_from_axis_angle((1.0, 0.0, 0.0), -0.15), friction=0.7))
+    q0 = np.concatenate([gold[0, :7], [0.37]]).astype(np.float32)
+    v0 = np.array([0, 0, 0, 0, 0, 0, -0.25], np.float32)
+    return w, q0, v0
+
+
+@pytest.mark.parametrize("solver,name", [(M.SOLVER_PGS, "solver_tree.bin"), (M.SOLVER_NEWTON, "solver_newton_tree.bin")])
+def test_tree_contact_solver_golden_is_byte_identical(solver, name):
+    """newt/tests/solver_golden.rs:260-297: q and qdot after 0, 50, 200 and
+    1000 RK4 steps with the joint tree-contact solve held over each step."""
+    w, q0, v0 = _tree_contact_scene(solver)
+    packed = M.PackedModels([w])
+    gold = _read_f32(name).reshape(4, 15)
+    assert np.concatenate([q0, v0]).tobytes() == gold[0].tobytes()
+    got = [np.concatenate([q0, v0])]
+    for n in (50, 200, 1000):
+        qo, vo = oracle_py.run(packed, np.zeros(1, np.int32), q0, v0, None, n, precision=0, layout=1, integrator=0)
+        got.append(np.concatenate([qo, vo]).astype(np.float32))
+    got = np.stack(got)
+    assert got.tobytes() == gold.tobytes(), np.abs(got - gold).max(axis=1)
+
+
+def _joints_chain():
+    """newt/tests/joints_golden.rs:23-60: fixed root and three X hinges."""
+    w = M.WorldModel(dt=0.005, gravity=(0.0, 0.0, -9.81), solver=0)
+    w.push_link(M.Link(parent=-1, joint=M.JOINT_FIXED, mass=1.0, inertia=M._diag9(1.0, 1.0, 1.0)))
+    masses, lengths = [f32(1.1), f32(0.7), f32(1.3)], [f32(0.6), f32(0.4), f32(0.5)]
+    for i in range(3):
+        m, l = masses[i], lengths[i]
+        ip = f32(f32(f32(f32(1.0) / f32(12.0)) * m) * l) * l
+        anchor = (0.0, 0.0, 0.0) if i == 0 else (0.0, 0.0, float(-lengths[i - 1] * f32(0.5)))
+        w.push_link(M.Link(parent=i, joint=M.JOINT_HINGE, axis=(1.0, 0.0, 0.0), jp_pos=anchor,
+                           jc_pos=(0.0, 0.0, float(l * f32(0.5))), mass=float(m),
+                           inertia=M._diag9(float(ip), float(ip), 1e-6)))
+    return w, np.array([0.4, -0.3, 0.2], np.float32), np.array([0.0, 0.5, 0.0], np.float32)
+
+
+def _joints_floating(q0):
+    """newt/tests/joints_golden.rs:62-103: free box with a swinging arm, no gravity."""
+    from f32util import normalize
+    w = M.WorldModel(dt=0.005, gravity=(0.0, 0.0, 0.0), solver=0)
+    hx, hy, hz, m0 = f32(0.3), f32(0.2), f32(0.15), f32(2.0)
+    m3 = m0 / f32(3.0)
+    box_i = M._diag9(float(m3 * (hy * hy + hz * hz)), float(m3 * (hx * hx + hz * hz)), float(m3 * (hx * hx + hy * hy)))
+    w.push_link(M.Link(parent=-1, joint=M.JOINT_FREE, jp_pos=(0.5, -1.0, 4.5), jp_quat=[float(x) for x in q0],
+                       mass=2.0, inertia=box_i))
+    l, m1 = f32(0.8), f32(0.7)
+    ip = f32(f32(f32(f32(1.0) / f32(12.0)) * m1) * l) * l
+    w.push_link(M.Link(parent=0, joint=M.JOINT_HINGE, axis=[float(x) for x in normalize((1.0, 0.3, 0.0))],
+                       jp_pos=(0.0, 0.0, float(-hz)), jc_pos=(0.0, 0.0, float(l * f32(0.5))), mass=float(m1),
+                       inertia=M._diag9(float(ip), float(ip), 1e-4)))
+    return w
+
+
+def test_joints_chain_and_floating_golden_is_byte_identical():
+    """newt/tests/joints_golden.rs:105-170: tree RK4 (explicit ABA) after 0,
+    100 and 1000 steps for a hinge chain and a floating base with an arm."""
+    gold = _read_f32("joints_chain_and_floating.bin").reshape(3, 21)
+    wc, qc, vc = _joints_chain()
+    wf = _joints_floating(gold[0, 9:13])  # Quat::from_axis_angle((1, 0.4, -0.3), 0.6)
+    qf = gold[0, 6:14].copy()
+    vf = np.array([0, 0, 0, 0, 0, 0, 4.0], np.float32)
+    assert np.concatenate([qc, vc, qf, vf]).tobytes() == gold[0].tobytes()
+    got = [gold[0]]
+    for n in (100, 1000):
+        row = []
+        for w, q, v in ((wc, qc, vc), (wf, qf, vf)):
+            qo, vo = oracle_py.run(M.PackedModels([w]), np.zeros(1, np.int32), q, v, None, n, precision=0, layout=1,
+                                   integrator=0)
+            row += [qo, vo]
+        got.append(np.concatenate(row).astype(np.float32))
+    got = np.stack(got)
+    assert got.tobytes() == gold.tobytes(), np.abs(got - gold).max(axis=1)
