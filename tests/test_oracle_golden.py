@@ -217,3 +217,37 @@ def test_joints_chain_and_floating_golden_is_byte_identical():
         got.append(np.concatenate(row).astype(np.float32))
     got = np.stack(got)
     assert got.tobytes() == gold.tobytes(), np.abs(got - gold).max(axis=1)
+
+
+def _tree_chain_contact(solver):
+    """tests/references/tree_chain_contact.xml as newt's MJCF loader builds
+    it: a free root sphere and a hinged sphere below it, falling on a plane
+    (Euler, dt 2e-3, 20 solver iterations)."""
+    w = M.WorldModel(dt=0.002, gravity=(0.0, 0.0, -9.81), solver=solver, iterations=20)
+    w.add_geom(M.static_plane(friction=0.6))
+    w.push_link(M.Link(parent=-1, joint=M.JOINT_FREE, jp_pos=(0.0, 0.0, 1.35), mass=1.1,
+                       inertia=M._diag9(0.08, 0.09, 0.1)))
+    w.push_link(M.Link(parent=0, joint=M.JOINT_HINGE, axis=(0.0, 1.0, 0.0), jp_pos=(0.0, 0.0, -0.25),
+                       jc_pos=(0.0, 0.0, 0.25), mass=0.8, inertia=M._diag9(0.025, 0.03, 0.02)))
+    w.add_geom(M.Geom(shape=M.SHAPE_SPHERE, link=0, size=(0.24, 0.0, 0.0), friction=0.6))
+    w.add_geom(M.Geom(shape=M.SHAPE_SPHERE, link=1, size=(0.19, 0.0, 0.0), friction=0.6))
+    return w
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("solver,name,qtol,vtol", [
+    (M.SOLVER_NEWTON, "tree_chain_contact_newton_euler.bin", 8.0e-2, 1.3),
+    (M.SOLVER_PGS, "tree_chain_contact_pgs_euler.bin", 7.0e-2, 0.7)])
+def test_tree_chain_contact_euler_matches_mujoco_capture(precision, solver, name, qtol, vtol):
+    """Tree-contact rows of newt/tests/differential.rs:1411-1446 (the Euler
+    form of the joint solve), inside newt's own windows against MuJoCo."""
+    ref = read_newtdif(name)
+    packed = M.PackedModels([_tree_chain_contact(solver)])
+    qpos = ref["qpos"][0].astype(np.float32)
+    qvel = ref["qvel"][0].astype(np.float32)
+    worst_q = worst_v = 0.0
+    for k, step in enumerate(ref["steps"]):
+        qo, vo = oracle_py.run(packed, np.zeros(1, np.int32), qpos, qvel, None, step, precision=precision)
+        worst_q = max(worst_q, np.abs(qo - ref["qpos"][k]).max())
+        worst_v = max(worst_v, np.abs(vo - ref["qvel"][k]).max())
+    assert worst_q <= qtol and worst_v <= vtol, (worst_q, worst_v)
