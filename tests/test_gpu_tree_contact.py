@@ -1,0 +1,168 @@
+"""GPU parity for tree-contact worlds (quadrupeds on a plane, Newton or PGS)
+through the C ABI, against the FP64 oracle.
+
+Bars (stated here, checked below):
+  * contact pair lists identical to the oracle's wherever no penetration lies
+    within 1e-6 of the margin;
+  * row impulses within 1e-3 relative (of the world's largest impulse), same
+    solver and iteration cap;
+  * short-horizon trajectories within 2e-3 m / 5e-2 m/s;
+  * the MuJoCo capture of newt's tree-chain contact scene inside newt's own
+    differential windows (qpos 8e-2 / 7e-2, qvel 1.3 / 0.7).
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import oracle_py
+from tooling_gb300 import Engine, STEP_BATCHED, STEP_PLAIN, scenes
+from tooling_gb300 import model as M
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from test_oracle_golden import _tree_chain_contact, read_newtdif  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+IMPULSE_RTOL = 1e-3
+MARGIN_BAND = 1e-6
+
+
+@pytest.fixture(scope="module")
+def eng():
+    from tooling_gb300 import build as B
+    B.build()
+    e = Engine(device=0)
+    yield e
+    e.close()
+
+
+def _settled(solver, n=24, steps=300, first=300):
+    """Quadrupeds advanced by the FP64 oracle until they lie on the plane
+    with 4-12 contacts each."""
+    b = scenes.quadruped_batch(n_worlds=n, first_world=first, solver=solver)
+    rq, rv = oracle_py.run(b, np.arange(len(b)), b.qpos, b.qvel, None, steps, precision=1)
+    b.qpos[:] = rq.astype(np.float32)
+    b.qvel[:] = rv.astype(np.float32)
+    return b
+
+
+@pytest.fixture(scope="module")
+def settled_newton():
+    return _settled(M.SOLVER_NEWTON)
+
+
+@pytest.fixture(scope="module")
+def settled_pgs():
+    return _settled(M.SOLVER_PGS)
+
+
+def _load(eng, b):
+    slots = eng.alloc(eng.upload(b))
+    eng.set_state(slots, b.qpos, b.qvel)
+    if b.qfrc.any():
+        eng.set_qfrc(slots, b.qfrc)
+    return slots
+
+
+def _world(b, w):
+    return (b.qpos[b.q_off[w]:b.q_off[w] + b.nq[w]], b.qvel[b.v_off[w]:b.v_off[w] + b.nv[w]],
+            b.qfrc[b.v_off[w]:b.v_off[w] + b.nv[w]])
+
+
+def test_contact_pair_lists_match_oracle(eng, settled_newton):
+    b = settled_newton
+    slots = _load(eng, b)
+    eng.step(1, STEP_PLAIN)
+    eng.sync()
+    compared = 0
+    for w in range(len(b)):
+        qp, qv, _ = _world(b, w)
+        rp, rd = oracle_py.contacts(b, w, qp, qv)
+        if len(rd) and (np.abs(rd[:, 6]) < MARGIN_BAND).any():
+            continue
+        gp, gd = eng.contacts(int(slots[w]))
+        assert np.array_equal(gp, rp), f"world {w}"
+        if len(rd):
+            assert np.abs(gd[:, 6] - rd[:, 6]).max() < 1e-4
+            assert np.abs(gd[:, :3] - rd[:, :3]).max() < 1e-4
+            assert np.abs(gd[:, 3:6] - rd[:, 3:6]).max() < 1e-5
+        compared += 1
+    assert compared >= len(b) // 2
+    eng.free(slots)
+
+
+@pytest.mark.parametrize("which", ["newton", "pgs"])
+def test_impulses_match_oracle(eng, settled_newton, settled_pgs, which):
+    b = settled_newton if which == "newton" else settled_pgs
+    slots = _load(eng, b)
+    eng.step(1, STEP_PLAIN)
+    eng.sync()
+    worst, rows = 0.0, 0
+    for w in range(len(b)):
+        qp, qv, qf = _world(b, w)
+        rp, rd = oracle_py.contacts(b, w, qp, qv)
+        if len(rd) and (np.abs(rd[:, 6]) < MARGIN_BAND).any():
+            continue
+        ref, _ = oracle_py.tree_impulses(b, w, qp, qv, qf)
+        g = eng.impulses(int(slots[w]))
+        assert len(g) == len(ref), f"world {w}"
+        if len(ref):
+            worst = max(worst, np.abs(g - ref).max() / max(1e-9, np.abs(ref).max()))
+            rows += len(ref)
+    assert rows > 0
+    assert worst <= IMPULSE_RTOL, worst
+    st = eng.status(slots)
+    assert not (st & 0x7).any(), st  # no NaN, no factorisation failure, no overflow
+    eng.free(slots)
+
+
+def test_short_trajectory_tracks_oracle(eng, settled_newton):
+    b = settled_newton
+    b.qfrc[:] = scenes.quadruped_controls(len(b), 0, first_world=300)
+    slots = _load(eng, b)
+    eng.step(10, STEP_PLAIN)
+    qp, qv = eng.get_state(slots, int(b.nq.sum()), int(b.nv.sum()))
+    rq, rv = oracle_py.run(b, np.arange(len(b)), b.qpos, b.qvel, b.qfrc, 10, precision=1)
+    assert np.abs(qp - rq).max() < 2e-3
+    assert np.abs(qv - rv).max() < 5e-2
+    b.qfrc[:] = 0.0
+    eng.free(slots)
+
+
+def test_plain_and_batched_agree(eng, settled_newton):
+    b = settled_newton
+    s1 = _load(eng, b)
+    eng.step(5, STEP_PLAIN)
+    q1, v1 = eng.get_state(s1, int(b.nq.sum()), int(b.nv.sum()))
+    eng.free(s1)
+    s2 = _load(eng, b)
+    eng.step(5, STEP_BATCHED)
+    q2, v2 = eng.get_state(s2, int(b.nq.sum()), int(b.nv.sum()))
+    eng.free(s2)
+    assert np.abs(q1 - q2).max() < 1e-5 and np.abs(v1 - v2).max() < 1e-4
+
+
+@pytest.mark.parametrize("solver,name,qtol,vtol", [
+    (M.SOLVER_NEWTON, "tree_chain_contact_newton_euler.bin", 8.0e-2, 1.3),
+    (M.SOLVER_PGS, "tree_chain_contact_pgs_euler.bin", 7.0e-2, 0.7)])
+def test_tree_chain_contact_within_mujoco_windows(eng, solver, name, qtol, vtol):
+    """The GPU step on newt's tree-chain contact scene stays inside the
+    windows newt's differential tests allow against MuJoCo
+    (newt/tests/differential.rs:1411-1446)."""
+    ref = read_newtdif(name)
+    packed = M.PackedModels([_tree_chain_contact(solver)])
+    slots = eng.alloc(eng.upload(packed))
+    eng.set_state(slots, ref["qpos"][0].astype(np.float32), ref["qvel"][0].astype(np.float32))
+    worst_q = worst_v = 0.0
+    prev = 0
+    for k, step in enumerate(ref["steps"]):
+        if step > prev:
+            eng.step(step - prev, STEP_PLAIN)
+            prev = step
+        qp, qv = eng.get_state(slots, 8, 7)
+        worst_q = max(worst_q, np.abs(qp - ref["qpos"][k]).max())
+        worst_v = max(worst_v, np.abs(qv - ref["qvel"][k]).max())
+    eng.free(slots)
+    assert worst_q <= qtol and worst_v <= vtol, (worst_q, worst_v)

@@ -62,9 +62,14 @@ static void tree_rows(HostGroup& g) {
   g.r_qd = r; r += g.nv;
   g.r_qfrc = r; r += g.nv;
   g.r_qacc = r; r += g.nv;
-  g.frows = r;
   g.ri_solver = 0; g.ri_live = 1; g.ri_status = 2;
   g.irows = 3;
+  if (g.kind == GK_TREE_CONTACT) {  // per-geom model rows (TcGroupDev::geom), solver mode
+    g.r_geom = r; r += 21 * g.ng;
+    g.ri_mode = 3; g.ri_iters = 4;
+    g.irows = 5;
+  }
+  g.frows = r;
 }
 
 static int pile_maxc(int nb, int np) {
@@ -113,14 +118,21 @@ static void pile_rows(HostGroup& g) {
   g.irows = l.istride;
 }
 
-size_t HostGroup::bytes_per_world() const { return frows * sizeof(float) + irows * sizeof(int); }
+// Model and state rows plus the world's solver scratch (counted against the
+// admission budget; the scratch itself is allocated at the first step).
+size_t HostGroup::bytes_per_world() const {
+  size_t b = frows * sizeof(float) + irows * sizeof(int);
+  if (kind == GK_PILE) b += newt_pile_ws_bytes(size, np, maxc);
+  if (kind == GK_TREE_CONTACT) b += newt_tc_ws_bytes(size, nv, ng, maxc);
+  return b;
+}
 
 // ---------------------------------------------------------------------------
 // capacity
 // ---------------------------------------------------------------------------
 static int grow(newt_gpu_ctx* ctx, HostGroup& g, int need) {
   if (g.frows == 0) {
-    if (g.kind == GK_TREE) tree_rows(g);
+    if (g.soa()) tree_rows(g);
     else if (g.kind == GK_PILE) pile_rows(g);
   }
   if (need <= g.cap) return NEWT_OK;
@@ -133,7 +145,7 @@ static int grow(newt_gpu_ctx* ctx, HostGroup& g, int need) {
   }
   std::vector<float> nF(g.frows * (size_t)ncap, 0.f);
   std::vector<int> nI(g.irows * (size_t)ncap, 0);
-  if (g.kind == GK_TREE) {
+  if (g.soa()) {
     for (size_t r = 0; r < g.frows; ++r)
       for (int w = 0; w < g.cap; ++w) nF[r * ncap + w] = g.hF[r * g.cap + w];
     for (size_t r = 0; r < g.irows; ++r)
@@ -149,7 +161,7 @@ static int grow(newt_gpu_ctx* ctx, HostGroup& g, int need) {
     CKG(cudaStreamSynchronize(ctx->stream));
     CKG(cudaMemcpy(cur.data(), g.dF, cur.size() * sizeof(float), cudaMemcpyDeviceToHost));
     CKG(cudaMemcpy(curI.data(), g.dI, curI.size() * sizeof(int), cudaMemcpyDeviceToHost));
-    if (g.kind == GK_TREE) {
+    if (g.soa()) {
       for (size_t r = 0; r < g.frows; ++r)
         for (int w = 0; w < g.cap; ++w) nF[r * ncap + w] = cur[r * g.cap + w];
       for (size_t r = 0; r < g.irows; ++r)
@@ -201,22 +213,50 @@ int HostGroup::reserve_indices(newt_gpu_ctx* ctx, int k, std::vector<int>& out) 
 }
 
 void HostGroup::release_index(newt_gpu_ctx* ctx, int idx) {
-  int lrow = kind == GK_TREE ? ri_live : lay.live;
+  int lrow = soa() ? ri_live : lay.live;
   I(lrow, idx) = 0;
   slot_of[idx] = -1;
   free_idx.push_back(idx);
   // mark the live flag on the device immediately (stream-ordered)
   int zero = 0;
-  int* dst = kind == GK_TREE ? dI + (size_t)lrow * cap + idx : dI + (size_t)idx * irows + lrow;
+  int* dst = soa() ? dI + (size_t)lrow * cap + idx : dI + (size_t)idx * irows + lrow;
   cudaMemcpyAsync(dst, &zero, sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
   cudaStreamSynchronize(ctx->stream);
+}
+
+// Geom topology, candidate pairs and contact capacity of a tree-contact
+// group, fixed by its first model (the topology key makes them uniform).
+void HostGroup::setup_tc(const HostModel& m) {
+  ng = m.n_geoms;
+  // (static, link geom) pairs in newt's auto_pairs order with its filter
+  // (world.rs:1042-1069); link-link pairs are refused at upload
+  gtopo.assign(3 * ng, 0);
+  for (int k = 0; k < ng; ++k) {
+    gtopo[2 * k] = m.geoms[k].shape;
+    gtopo[2 * k + 1] = m.geoms[k].link;
+    gtopo[2 * ng + k] = m.geoms[k].condim;
+  }
+  gpairs.clear();
+  maxc = 0;
+  for (int a = 0; a < ng; ++a)
+    for (int b = a + 1; b < ng; ++b) {
+      const newt_geom_desc &A = m.geoms[a], &B = m.geoms[b];
+      if ((A.link < 0) == (B.link < 0)) continue;
+      if (!((A.group & B.mask) != 0u && (B.group & A.mask) != 0u)) continue;
+      gpairs.push_back(a);
+      gpairs.push_back(b);
+      const int shape = A.link >= 0 ? A.shape : B.shape;
+      maxc += shape == NEWT_SHAPE_BOX ? 4 : (shape == NEWT_SHAPE_CAPSULE ? 2 : 1);
+    }
+  npairs = (int)gpairs.size() / 2;
+  if (maxc < 1) maxc = 1;
 }
 
 // ---------------------------------------------------------------------------
 // model staging
 // ---------------------------------------------------------------------------
 void HostGroup::write_model(newt_gpu_ctx*, int w, const HostModel& m) {
-  if (kind == GK_TREE) {
+  if (soa()) {
     const int L = size;
     if (topo.empty()) {
       topo.assign(4 * L, 0);
@@ -249,6 +289,18 @@ void HostGroup::write_model(newt_gpu_ctx*, int w, const HostModel& m) {
     I(ri_solver, w) = m.solver != 0;
     I(ri_live, w) = 1;
     I(ri_status, w) = 0;
+    if (kind == GK_TREE_CONTACT) {
+      for (int k = 0; k < ng; ++k) {
+        const newt_geom_desc& G = m.geoms[k];
+        float rec[21] = {G.size[0], G.size[1], G.size[2], G.local_pos[0], G.local_pos[1], G.local_pos[2],
+                         G.local_quat[0], G.local_quat[1], G.local_quat[2], G.local_quat[3], G.friction, G.margin,
+                         G.gap, G.solref[0], G.solref[1], G.solimp[0], G.solimp[1], G.solimp[2], G.solimp[3],
+                         G.solimp[4], 0.f};
+        for (int f = 0; f < 21; ++f) F(r_geom + 21 * k + f, w) = rec[f];
+      }
+      I(ri_mode, w) = m.solver;
+      I(ri_iters, w) = m.iterations;
+    }
   } else if (kind == GK_PILE) {
     const int nb = size, ng = nb + np;
     const PileLayout& l = lay;
@@ -292,9 +344,16 @@ void HostGroup::write_model(newt_gpu_ctx*, int w, const HostModel& m) {
 }
 
 int HostGroup::flush_model(newt_gpu_ctx* ctx) {
-  if (kind == GK_TREE && !dtopo && !topo.empty()) {
+  if (soa() && !dtopo && !topo.empty()) {
     CKG(cudaMalloc(&dtopo, topo.size() * sizeof(int)));
     CKG(cudaMemcpy(dtopo, topo.data(), topo.size() * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  if (kind == GK_TREE_CONTACT && !dgtopo && !gtopo.empty()) {
+    CKG(cudaMalloc(&dgtopo, gtopo.size() * sizeof(int)));
+    CKG(cudaMemcpy(dgtopo, gtopo.data(), gtopo.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CKG(cudaMalloc(&dpairs, std::max<size_t>(gpairs.size(), 2) * sizeof(int)));
+    if (!gpairs.empty())
+      CKG(cudaMemcpy(dpairs, gpairs.data(), gpairs.size() * sizeof(int), cudaMemcpyHostToDevice));
   }
   if (!model_dirty) return NEWT_OK;
   // upload only the newly written worlds: other worlds of the group may be
@@ -305,7 +364,7 @@ int HostGroup::flush_model(newt_gpu_ctx* ctx) {
     size_t j = i + 1;
     while (j < pending.size() && pending[j] == pending[j - 1] + 1) ++j;
     const size_t a = pending[i], k = j - i;
-    if (kind == GK_TREE) {
+    if (soa()) {
       CKG(cudaMemcpy2DAsync(dF + a, cap * sizeof(float), hF.data() + a, cap * sizeof(float), k * sizeof(float), frows,
                             cudaMemcpyHostToDevice, ctx->stream));
       CKG(cudaMemcpy2DAsync(dI + a, cap * sizeof(int), hI.data() + a, cap * sizeof(int), k * sizeof(int), irows,
@@ -328,12 +387,12 @@ int HostGroup::flush_model(newt_gpu_ctx* ctx) {
 // state staging (MuJoCo layout in, newt layout on the device)
 // ---------------------------------------------------------------------------
 static void state_range(const HostGroup& g, size_t* lo, size_t* cnt) {
-  if (g.kind == GK_TREE) { *lo = g.r_q; *cnt = (size_t)g.nq + g.nv; }
+  if (g.soa()) { *lo = g.r_q; *cnt = (size_t)g.nq + g.nv; }
   else { *lo = g.lay.pos; *cnt = (size_t)(g.lay.omg + 3 * g.size - g.lay.pos); }
 }
 
 void HostGroup::stage_state(int w, const HostModel& m, const float* qpos, const float* qvel) {
-  if (kind == GK_TREE) {
+  if (soa()) {
     int c = 0, v = 0;
     for (int i = 0; i < size; ++i) {
       int jt = topo[4 * i + 1], qo = topo[4 * i + 2], vo = topo[4 * i + 3];
@@ -366,7 +425,7 @@ void HostGroup::stage_state(int w, const HostModel& m, const float* qpos, const 
 }
 
 void HostGroup::stage_qfrc(int w, const HostModel& m, const float* qfrc) {
-  if (kind == GK_TREE) for (int k = 0; k < nv; ++k) F(r_qfrc + k, w) = qfrc[k];
+  if (soa()) for (int k = 0; k < nv; ++k) F(r_qfrc + k, w) = qfrc[k];
   (void)m;
   qfrc_dirty = true;
 }
@@ -375,7 +434,7 @@ int HostGroup::flush_state(newt_gpu_ctx* ctx) {
   if (!state_dirty) return NEWT_OK;
   size_t lo, cnt;
   state_range(*this, &lo, &cnt);
-  if (kind == GK_TREE) {
+  if (soa()) {
     CKG(cudaMemcpyAsync(dF + lo * cap, hF.data() + lo * cap, cnt * cap * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
   } else {
     CKG(cudaMemcpy2DAsync(dF + lo, frows * sizeof(float), hF.data() + lo, frows * sizeof(float), cnt * sizeof(float),
@@ -388,7 +447,7 @@ int HostGroup::flush_state(newt_gpu_ctx* ctx) {
 
 int HostGroup::flush_qfrc(newt_gpu_ctx* ctx) {
   if (!qfrc_dirty) return NEWT_OK;
-  if (kind == GK_TREE) {
+  if (soa()) {
     CKG(cudaMemcpyAsync(dF + (size_t)r_qfrc * cap, hF.data() + (size_t)r_qfrc * cap, (size_t)nv * cap * sizeof(float),
                         cudaMemcpyHostToDevice, ctx->stream));
     CKG(cudaStreamSynchronize(ctx->stream));
@@ -399,7 +458,7 @@ int HostGroup::flush_qfrc(newt_gpu_ctx* ctx) {
 
 int HostGroup::fetch_state(newt_gpu_ctx* ctx) {
   if (n == 0) return NEWT_OK;
-  if (kind == GK_TREE) {
+  if (soa()) {
     size_t lo = r_q, cnt = (size_t)nq + 3 * (size_t)nv;  // q qd qfrc qacc
     CKG(cudaMemcpyAsync(hF.data() + lo * cap, dF + lo * cap, cnt * cap * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
   } else {
@@ -414,7 +473,7 @@ int HostGroup::fetch_state(newt_gpu_ctx* ctx) {
 }
 
 void HostGroup::read_state(int w, const HostModel& m, float* qpos, float* qvel) const {
-  if (kind == GK_TREE) {
+  if (soa()) {
     int c = 0, v = 0;
     for (int i = 0; i < size; ++i) {
       int jt = topo[4 * i + 1], qo = topo[4 * i + 2], vo = topo[4 * i + 3];
@@ -443,13 +502,13 @@ void HostGroup::read_state(int w, const HostModel& m, float* qpos, float* qvel) 
 }
 
 void HostGroup::read_qacc(int w, const HostModel& m, float* qacc) const {
-  if (kind == GK_TREE) for (int k = 0; k < nv; ++k) qacc[k] = Fc(r_qacc + k, w);
+  if (soa()) for (int k = 0; k < nv; ++k) qacc[k] = Fc(r_qacc + k, w);
   else for (int k = 0; k < m.nv; ++k) qacc[k] = 0.f;
 }
 
 int HostGroup::fetch_status(newt_gpu_ctx* ctx) {
   if (n == 0) return NEWT_OK;
-  if (kind == GK_TREE) {
+  if (soa()) {
     CKG(cudaMemcpy(hI.data() + (size_t)ri_status * cap, dI + (size_t)ri_status * cap, (size_t)cap * sizeof(int), cudaMemcpyDeviceToHost));
     for (int w = 0; w < n; ++w) status_host[w] = (uint32_t)hI[(size_t)ri_status * cap + w];
   } else {
@@ -462,7 +521,7 @@ int HostGroup::fetch_status(newt_gpu_ctx* ctx) {
 
 int HostGroup::clear_status(newt_gpu_ctx* ctx) {
   if (n == 0) return NEWT_OK;
-  if (kind == GK_TREE) {
+  if (soa()) {
     CKG(cudaMemsetAsync(dI + (size_t)ri_status * cap, 0, (size_t)cap * sizeof(int), ctx->stream));
   } else {
     CKG(cudaMemset2DAsync(dI + lay.status, irows * sizeof(int), 0, sizeof(int), n, ctx->stream));
@@ -473,7 +532,27 @@ int HostGroup::clear_status(newt_gpu_ctx* ctx) {
 
 int HostGroup::read_contacts(newt_gpu_ctx* ctx, int w, int cap_out, int* n_out, int* pairs, float* data) {
   if (kind != GK_PILE && kind != GK_TREE_CONTACT) { *n_out = 0; return NEWT_OK; }
-  if (kind == GK_TREE_CONTACT) return NEWT_E_INVALID;
+  if (kind == GK_TREE_CONTACT) {
+    // contact records in the world's solver scratch (see newton_kernels.cu)
+    int o_con, o_imp, o_misc;
+    newt_tc_offsets(size, nv, ng, maxc, &o_con, &o_imp, &o_misc);
+    *n_out = 0;
+    if (!plain_scratch) return NEWT_OK;
+    const float* base = (const float*)plain_scratch + (size_t)w * scr_stride;
+    std::vector<float> recs(24 * (size_t)maxc);
+    int misc[2];
+    CKG(cudaStreamSynchronize(ctx->stream));
+    CKG(cudaMemcpy(misc, base + o_misc, sizeof(misc), cudaMemcpyDeviceToHost));
+    CKG(cudaMemcpy(recs.data(), base + o_con, recs.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    const int nc = std::min(misc[0], maxc);
+    *n_out = nc;
+    for (int i = 0; i < nc && i < cap_out; ++i) {
+      const float* c = recs.data() + 24 * i;
+      if (pairs) { std::memcpy(&pairs[2 * i], &c[0], sizeof(int)); std::memcpy(&pairs[2 * i + 1], &c[1], sizeof(int)); }
+      if (data) { for (int k = 0; k < 6; ++k) data[7 * i + k] = c[4 + k]; data[7 * i + 6] = c[10]; }
+    }
+    return NEWT_OK;
+  }
   std::vector<int> rec(irows);
   std::vector<float> frec(frows);
   CKG(cudaStreamSynchronize(ctx->stream));
@@ -489,6 +568,20 @@ int HostGroup::read_contacts(newt_gpu_ctx* ctx, int w, int cap_out, int* n_out, 
 }
 
 int HostGroup::read_impulses(newt_gpu_ctx* ctx, int w, int cap_out, int* n_out, float* imp) {
+  if (kind == GK_TREE_CONTACT) {
+    int o_con, o_imp, o_misc;
+    newt_tc_offsets(size, nv, ng, maxc, &o_con, &o_imp, &o_misc);
+    *n_out = 0;
+    if (!plain_scratch) return NEWT_OK;
+    const float* base = (const float*)plain_scratch + (size_t)w * scr_stride;
+    int misc[2];
+    CKG(cudaStreamSynchronize(ctx->stream));
+    CKG(cudaMemcpy(misc, base + o_misc, sizeof(misc), cudaMemcpyDeviceToHost));
+    const int nr = std::min(misc[1], 4 * maxc);
+    *n_out = nr;
+    if (nr > 0 && imp) CKG(cudaMemcpy(imp, base + o_imp, std::min(nr, cap_out) * sizeof(float), cudaMemcpyDeviceToHost));
+    return NEWT_OK;
+  }
   if (kind != GK_PILE) { *n_out = 0; return NEWT_OK; }
   std::vector<int> rec(irows);
   std::vector<float> frec(frows);
@@ -509,8 +602,10 @@ void HostGroup::release() {
   if (dF) cudaFree(dF);
   if (dI) cudaFree(dI);
   if (dtopo) cudaFree(dtopo);
+  if (dgtopo) cudaFree(dgtopo);
+  if (dpairs) cudaFree(dpairs);
   if (plain_scratch) cudaFree(plain_scratch);
-  dF = nullptr; dI = nullptr; dtopo = nullptr; plain_scratch = nullptr;
+  dF = nullptr; dI = nullptr; dtopo = nullptr; dgtopo = nullptr; dpairs = nullptr; plain_scratch = nullptr;
 }
 
 TreeGroupDev HostGroup::tree_dev() const {
@@ -531,6 +626,19 @@ PileGroupDev HostGroup::pile_dev() const {
   PileGroupDev d;
   d.n = n; d.cap = cap; d.nb = size; d.np = np; d.maxc = maxc; d.lay = lay;
   d.F = dF; d.I = dI;
+  d.scr = (float*)plain_scratch;
+  d.sstride = scr_stride;
+  return d;
+}
+
+TcGroupDev HostGroup::tc_dev() const {
+  TcGroupDev d;
+  d.t = tree_dev();
+  d.ng = ng; d.npairs = npairs; d.maxc = maxc;
+  d.gtopo = dgtopo; d.pairs = dpairs;
+  d.geom = dF + (size_t)r_geom * cap;
+  d.mode = dI + (size_t)ri_mode * cap;
+  d.iters = dI + (size_t)ri_iters * cap;
   d.scr = (float*)plain_scratch;
   d.sstride = scr_stride;
   return d;

@@ -42,6 +42,23 @@ struct TreeGroupDev {
   uint32_t* status;
 };
 
+// A tree whose link geoms touch static planes (quadruped worlds): the tree
+// group's SoA layout plus per-geom model rows, the solver mode and a
+// world-major solver scratch.
+struct TcGroupDev {
+  TreeGroupDev t;
+  int ng;            // geoms per world (link geoms and static planes, model order)
+  int npairs;        // candidate (static, link geom) pairs, newt's pair order
+  int maxc;          // contact capacity per world
+  const int* gtopo;  // [2*ng] shape, link (-1 static); then [ng] condim
+  const int* pairs;  // [2*npairs] geom indices (a < b)
+  const float* geom; // 21 SoA rows per geom: size3 pos3 quat4 fric margin gap solref2 solimp5
+  const int* mode;   // per world: NEWT_SOLVER_PGS | NEWT_SOLVER_NEWTON
+  const int* iters;  // per world
+  float* scr;        // world-major solver scratch
+  long sstride;      // floats per world in `scr`
+};
+
 // Field offsets (in floats / ints) inside one pile world's record.
 struct PileLayout {
   int fstride, istride;

@@ -1,10 +1,760 @@
-// Tree-contact worlds (floating-base trees on a plane with a Newton or PGS
-// constraint solve).  Placeholder dispatch until the kernel lands: such
-// worlds are rejected at step time with a clear error.
+// Tree-contact step: worlds holding one articulated tree whose link geoms
+// touch static planes (the quadruped workload), stepped with newt's
+// semi-implicit Euler and its joint tree-contact solve.  Per env-step:
+//
+//   tree_aba_kernel        thread per world (tree_kernels.cu): a_free, the
+//                          ABA with the implicit damping fold, into qacc
+//   tc_k_solve             warp per world (this file): forward kinematics,
+//                          link-plane contacts, link COM Jacobians and the
+//                          mass matrix, its Cholesky factors, the Jacobian
+//                          row of every cone facet, A = J M^-1 J^T, the
+//                          regulariser and bias, Newton or PGS, and
+//                          qacc = a_free + M^-1 J^T f / dt
+//   tree_integrate_kernel  thread per world (tree_kernels.cu)
+//
+// Restates, for FP32 on sm_103a:
+//   newt/src/solver.rs:2805-3366  solve_tree_contacts (Euler form:
+//                                 factors of M + dt*B, implicit free ABA)
+//   newt/src/solver.rs:3537-3600  world_jacobian_for_side
+//   newt/src/solver.rs:3719-3797  tree_body_invweight0, tree_contact_diag_approx
+//   newt/src/solver.rs:1960-1974  contact_regularization_from_diag
+//   newt/src/newton.rs:275-620    NewtonSystem::solve, exact_pyramidal_line_search
+//   newt/src/jacobian.rs:38-120   point_jacobian
+//   newt/src/dynamics.rs:474-648  mass_matrix, cholesky; tree.rs:645-684
+//   newt/src/tree.rs:771-858      forward_kinematics
+//   newt/src/contact.rs:269-400   sphere/box/capsule-plane contacts and the
+//                                 (plane, geom) label swap of :2509-2587
+// Changes that only move rounding:
+//   * M = sum_l J_l^T diag(m_l, I_l) J_l from the link COM Jacobians (the CRB
+//     recursion's matrix);
+//   * A = Y^T Y with Y = L^-1 J^T (newt solves M^-1 J^T column by column);
+//   * the line search walks newt's candidate set (the breakpoints where a
+//     non-negative coordinate reaches zero, and each window's minimiser of
+//     the piecewise-quadratic cost) with H p and H s updated one column per
+//     breakpoint instead of re-multiplied per candidate; newt's
+//     finite-difference slope inside a window is the masked direction used
+//     here, and its window minimiser mid - g(mid).s / s.Hs equals -c1/c2;
+//   * qacc adds M^-1 J^T f / dt to a_free instead of re-running the ABA with
+//     the contact forces (the ABA is linear in the applied forces).
+// FP64: when the FP32 Cholesky of the Newton Hessian has a pivot ratio
+// (max L_ii / min L_ii)^2 above 1e6, the factor and the direction solves are
+// redone in FP64 (status bit NEWT_WS_FP64_FALLBACK).
+#include <algorithm>
+
+#include "../../include/newt_gpu.h"
+#include "common.cuh"
+#include "groups.h"
+#include "narrowphase.cuh"
 #include "runtime.h"
 
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int TC_WARPS = 2;  // warps (worlds) per block
+constexpr int CREC = 24;     // floats per contact record
+// contact record fields
+enum { K_GA = 0, K_GB = 1, K_LINK = 2, K_SIGN = 3, K_POS = 4, K_N = 7, K_PEN = 10, K_GAP = 11, K_MU = 12,
+       K_SR = 13, K_SI = 15, K_CONDIM = 20, K_ROW = 21 };
+constexpr int GREC = 21;  // SoA geom model rows: size3 pos3 quat4 fric margin gap solref2 solimp5
+enum { G_SIZE = 0, G_POS = 3, G_QUAT = 6, G_FRIC = 10, G_MARGIN = 11, G_GAP = 12, G_SR = 13, G_SI = 15 };
+enum { JF = 0, JX = 1, JH = 2, JS = 3 };
+
+NEWT_D float warp_sum(float v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  return v;
+}
+NEWT_D double warp_sumd(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  return v;
+}
+
+NEWT_D Q4 q_axis_angle(V3 axis, float angle) {  // math.rs:574-580
+  const float l = sqrtf(len2(axis));
+  const V3 a = l > 0.f ? axis * (1.f / l) : v3(0.f, 0.f, 0.f);
+  float s, c;
+  sincosf(angle * 0.5f, &s, &c);
+  return Q4{a.x * s, a.y * s, a.z * s, c};
+}
+NEWT_D V3 ldv3(const float* p) { return v3(p[0], p[1], p[2]); }
+NEWT_D void stv3(float* p, V3 v) { p[0] = v.x; p[1] = v.y; p[2] = v.z; }
+
+// soft-constraint parameters (solver.rs:166-384)
+struct Soft { float tc, dr, dmin, dmax, width, mid; int power; };
+NEWT_D float clamp_imp(float v) { return v < 1.0e-4f ? 1.0e-4f : (v > 0.9999f ? 0.9999f : v); }
+NEWT_D float impedance_at(float position, const Soft& s) {
+  const float dmin = clamp_imp(s.dmin), dmax = clamp_imp(s.dmax), mid = clamp_imp(s.mid);
+  const float width = s.width > 0.f ? s.width : 0.f;
+  const int power = s.power > 1 ? s.power : 1;
+  float x = position / width;
+  if (x < 0.f) x = -x;
+  float y;
+  if (x <= 0.f) y = 0.f;
+  else if (x >= 1.f) y = 1.f;
+  else if (x < mid) { float r = x / mid, p = 1.f; for (int i = 0; i < power; ++i) p *= r; y = mid * p; }
+  else { float r = (1.f - x) / (1.f - mid), p = 1.f; for (int i = 0; i < power; ++i) p *= r; y = 1.f - (1.f - mid) * p; }
+  return dmin + (dmax - dmin) * y;
+}
+NEWT_D float reference_accel(float position, float velocity, float tc, float dr, const Soft& s, float dt) {
+  const bool direct = tc < 0.f;
+  if (!direct && tc < 2.f * dt) tc = 2.f * dt;  // safe_solref (solver.rs:331-338)
+  const float dmax = clamp_imp(s.dmax);
+  const float d = impedance_at(position, s);
+  float b, k;
+  if (direct) { b = -dr / dmax; k = -tc / (dmax * dmax); }
+  else { b = 2.f / (dmax * tc); k = d / (dmax * dmax * tc * tc * dr * dr); }
+  return -b * velocity - k * position;
+}
+
+// ---------------------------------------------------------------------------
+// per-world scratch (world-major, floats); matrices column-major
+// ---------------------------------------------------------------------------
+struct TcLay {
+  int L, nv, ng, maxc, ld;
+  int pose, jv, jw, iw, M, LM, LD, tw, con, jt, y, H, LH, LHd, imp, misc, words;
+};
+NEWT_HD int up4(int n) { return (n + 3) / 4 * 4; }
+NEWT_HD TcLay tc_layout(int L, int nv, int ng, int maxc) {
+  TcLay t;
+  t.L = L; t.nv = nv; t.ng = ng; t.maxc = maxc;
+  t.ld = up4(4 * maxc);
+  int f = 0;
+  t.pose = f; f += up4(7 * L);
+  t.jv = f; f += up4(3 * nv * L);
+  t.jw = f; f += up4(3 * nv * L);
+  t.iw = f; f += up4(6 * L);
+  t.M = f; f += up4(nv * nv);
+  t.LM = f; f += up4(nv * nv);
+  t.LD = f; f += up4(nv * nv);
+  t.tw = f; f += up4(L);
+  t.con = f; f += up4(CREC * maxc);
+  t.jt = f; f += up4(nv * t.ld);
+  t.y = f; f += up4(nv * t.ld);
+  t.H = f; f += up4(t.ld * t.ld);
+  t.LH = f; f += up4(t.ld * t.ld);
+  t.LHd = f; f += up4(2 * t.ld * t.ld);  // doubles (offset is a multiple of 4 floats)
+  t.imp = f; f += up4(t.ld);
+  t.misc = f; f += 8;  // ncon, nrows, newton iterations
+  t.words = (f + 31) / 32 * 32;
+  return t;
+}
+// per-warp shared vectors (ld floats each) and row maps (ld ints each)
+enum { V_X = 0, V_D, V_G, V_B, V_REG, V_DIAG, V_U, V_V, V_P, V_S, N_VEC };
+NEWT_HD int tc_smem_words(int ld) { return (N_VEC + 2) * ld; }
+
+// In-place lower Cholesky of the n x n column-major matrix A (leading
+// dimension ld).  Right-looking: column k is scaled, then the lanes update
+// the trailing lower triangle, one lane per row.  Returns false (uniformly)
+// when a pivot is not positive; reports the pivot range of L.
+template <class T>
+NEWT_D bool warp_cholesky(T* A, int n, int ld, int lane, T* min_piv, T* max_piv) {
+  T mn = T(1e30), mx = T(0);
+  for (int k = 0; k < n; ++k) {
+    __syncwarp();
+    const T akk = A[(size_t)k * ld + k];
+    if (!(akk > T(0))) return false;
+    const T lkk = sqrt(akk);
+    mn = lkk < mn ? lkk : mn;
+    mx = lkk > mx ? lkk : mx;
+    const T inv = T(1) / lkk;
+    __syncwarp();
+    for (int i = k + 1 + lane; i < n; i += 32) A[(size_t)k * ld + i] *= inv;
+    if (lane == 0) A[(size_t)k * ld + k] = lkk;
+    __syncwarp();
+    for (int j = k + 1; j < n; ++j) {
+      const T ljk = A[(size_t)k * ld + j];
+      for (int i = j + lane; i < n; i += 32) A[(size_t)j * ld + i] -= A[(size_t)k * ld + i] * ljk;
+    }
+  }
+  __syncwarp();
+  *min_piv = mn;
+  *max_piv = mx;
+  return true;
+}
+
+// Solves L L^T z = rhs in place on the shared vector `v` (length n) with the
+// column-major factor L: forward substitution column by column (lanes update
+// the rows below), then backward substitution by row dot products.
+template <class T>
+NEWT_D void warp_llt_solve(const T* Lf, int n, int ld, float* v, int lane) {
+  for (int k = 0; k < n; ++k) {
+    __syncwarp();
+    const T yk = T(v[k]) / Lf[(size_t)k * ld + k];
+    __syncwarp();
+    if (lane == 0) v[k] = (float)yk;
+    for (int i = k + 1 + lane; i < n; i += 32) v[i] = (float)(T(v[i]) - Lf[(size_t)k * ld + i] * yk);
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    __syncwarp();
+    T s = T(0);
+    for (int m = k + 1 + lane; m < n; m += 32) s += Lf[(size_t)k * ld + m] * T(v[m]);
+    if (sizeof(T) == 8) s = (T)warp_sumd((double)s); else s = (T)warp_sum((float)s);
+    const T zk = (T(v[k]) - s) / Lf[(size_t)k * ld + k];
+    __syncwarp();
+    if (lane == 0) v[k] = (float)zk;
+  }
+  __syncwarp();
+}
+
+// out = H x (column-major H, lane per row; x shared).
+NEWT_D void warp_matvec(const float* H, int n, int ld, const float* x, float* out, int lane) {
+  __syncwarp();
+  for (int r = lane; r < n; r += 32) {
+    float s = 0.f;
+    for (int c = 0; c < n; ++c) s += H[(size_t)c * ld + r] * x[c];
+    out[r] = s;
+  }
+  __syncwarp();
+}
+NEWT_D float warp_dot(const float* a, const float* b, int n, int lane) {
+  float s = 0.f;
+  for (int r = lane; r < n; r += 32) s += a[r] * b[r];
+  return warp_sum(s);
+}
+
+}  // namespace
+
+
+// vector length of the per-warp shared vectors: rows and DoF both fit
+NEWT_HD int tc_vl(int nv, int maxc) { int ld = up4(4 * maxc), n = up4(nv); return ld > n ? ld : n; }
+NEWT_HD int tc_warp_words(int nv, int maxc) { return N_VEC * tc_vl(nv, maxc) + 2 * up4(4 * maxc); }
+
+namespace {
+
+// Columns of the world-frame point Jacobian of link `l` at `pt`
+// (jacobian.rs:38-120), walking the chain to the root; `col(k, rot, trans)`
+// receives every DoF column of the chain.
+template <class F>
+NEWT_D void chain_columns(const TreeGroupDev& g, int w, const float* pose, int l, V3 pt, F col) {
+  const int cap = g.cap;
+  for (int i = l; i >= 0; i = g.topo[4 * i]) {
+    const int jt = g.topo[4 * i + 1], vo = g.topo[4 * i + 3];
+    if (jt == JF) {
+      const float* pi = pose + 7 * i;
+      const Q4 o = Q4{pi[3], pi[4], pi[5], pi[6]};
+      const V3 r = pt - ldv3(pi);
+      for (int k = 0; k < 3; ++k) {
+        const V3 aw = qrot(o, v3(k == 0 ? 1.f : 0.f, k == 1 ? 1.f : 0.f, k == 2 ? 1.f : 0.f));
+        col(vo + k, aw, cross(aw, r));
+        col(vo + 3 + k, v3(0.f, 0.f, 0.f), aw);
+      }
+    } else if (jt == JH || jt == JS) {
+      const float* pp = pose + 7 * g.topo[4 * i];
+      const Q4 po = Q4{pp[3], pp[4], pp[5], pp[6]};
+      const V3 ax = v3(g.axis[(3 * i) * cap + w], g.axis[(3 * i + 1) * cap + w], g.axis[(3 * i + 2) * cap + w]);
+      const V3 aw = qrot(po, ax);
+      if (jt == JH) {
+        const V3 jp = v3(g.jp[(3 * i) * cap + w], g.jp[(3 * i + 1) * cap + w], g.jp[(3 * i + 2) * cap + w]);
+        const V3 jw = ldv3(pp) + qrot(po, jp);
+        col(vo, aw, cross(aw, pt - jw));
+      } else {
+        col(vo, v3(0.f, 0.f, 0.f), aw);
+      }
+    }
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// K_B: one warp per world
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
+  extern __shared__ __align__(16) float tcs[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w = blockIdx.x * TC_WARPS + warp;
+  const TreeGroupDev& g = G.t;
+  if (w >= g.n || !g.live[w]) return;  // uniform per warp
+  const int cap = g.cap, L = g.L, nv = g.nv;
+  const TcLay lay = tc_layout(L, nv, G.ng, G.maxc);
+  const int ld = lay.ld, vl = tc_vl(nv, G.maxc);
+  float* wf = G.scr + (size_t)w * G.sstride;
+  float* sv = tcs + (size_t)warp * tc_warp_words(nv, G.maxc);
+  float* vx = sv + V_X * vl; float* vd = sv + V_D * vl; float* vg = sv + V_G * vl; float* vb = sv + V_B * vl;
+  float* vreg = sv + V_REG * vl; float* vdiag = sv + V_DIAG * vl; float* vu = sv + V_U * vl;
+  float* vv = sv + V_V * vl; float* vp = sv + V_P * vl; float* vs = sv + V_S * vl;
+  int* rcon = reinterpret_cast<int*>(sv + N_VEC * vl);
+  int* rfac = rcon + ld;
+  const float dt = g.dtg[w];
+  uint32_t status = 0;
+  const float* gm = G.geom;
+  auto gv = [&](int gi, int f) { return gm[(size_t)(GREC * gi + f) * cap + w]; };
+
+  // ---- forward kinematics (tree.rs:771-858), lane 0 ----
+  float* pose = wf + lay.pose;
+  if (lane == 0) {
+    for (int i = 0; i < L; ++i) {
+      const int parent = g.topo[4 * i], jt = g.topo[4 * i + 1], qo = g.topo[4 * i + 2];
+      const V3 jp = v3(g.jp[(3 * i) * cap + w], g.jp[(3 * i + 1) * cap + w], g.jp[(3 * i + 2) * cap + w]);
+      const V3 jc = v3(g.jc[(3 * i) * cap + w], g.jc[(3 * i + 1) * cap + w], g.jc[(3 * i + 2) * cap + w]);
+      V3 p;
+      Q4 o;
+      if (i == 0) {
+        if (jt == JF) {
+          p = v3(g.q[qo * cap + w], g.q[(qo + 1) * cap + w], g.q[(qo + 2) * cap + w]);
+          o = Q4{g.q[(qo + 3) * cap + w], g.q[(qo + 4) * cap + w], g.q[(qo + 5) * cap + w], g.q[(qo + 6) * cap + w]};
+        } else {
+          o = Q4{g.rootq[w], g.rootq[cap + w], g.rootq[2 * cap + w], g.rootq[3 * cap + w]};
+          p = jp - qrot(o, jc);
+        }
+      } else {
+        const float* pp = pose + 7 * parent;
+        const Q4 po = Q4{pp[3], pp[4], pp[5], pp[6]};
+        const V3 jpw = ldv3(pp) + qrot(po, jp);
+        const V3 ax = v3(g.axis[(3 * i) * cap + w], g.axis[(3 * i + 1) * cap + w], g.axis[(3 * i + 2) * cap + w]);
+        if (jt == JH) {
+          o = qmul(po, q_axis_angle(ax, g.q[qo * cap + w]));
+          p = jpw - qrot(o, jc);
+        } else if (jt == JS) {
+          o = po;
+          p = jpw + qrot(po, ax * g.q[qo * cap + w]) - qrot(o, jc);
+        } else {
+          o = po;
+          p = jpw - qrot(o, jc);
+        }
+      }
+      float* d = pose + 7 * i;
+      stv3(d, p);
+      d[3] = o.x; d[4] = o.y; d[5] = o.z; d[6] = o.w;
+    }
+  }
+  __syncwarp();
+
+  // ---- link-plane contacts in newt's pair order, lane 0 ----
+  float* con = wf + lay.con;
+  if (lane == 0) {
+    int ncon = 0;
+    bool overflow = false;
+    for (int pi = 0; pi < G.npairs && !overflow; ++pi) {
+      const int a = G.pairs[2 * pi], b = G.pairs[2 * pi + 1];
+      const bool a_static = G.gtopo[2 * a + 1] < 0;
+      const int gl = a_static ? b : a, gp = a_static ? a : b;  // link geom, plane
+      const int link = G.gtopo[2 * gl + 1], shape = G.gtopo[2 * gl];
+      const float* lp = pose + 7 * link;
+      const Q4 lo = Q4{lp[3], lp[4], lp[5], lp[6]};
+      GPose gpose, ppose;
+      gpose.p = ldv3(lp) + qrot(lo, v3(gv(gl, G_POS), gv(gl, G_POS + 1), gv(gl, G_POS + 2)));
+      gpose.q = qmul(lo, Q4{gv(gl, G_QUAT), gv(gl, G_QUAT + 1), gv(gl, G_QUAT + 2), gv(gl, G_QUAT + 3)});
+      ppose.p = v3(gv(gp, G_POS), gv(gp, G_POS + 1), gv(gp, G_POS + 2));
+      ppose.q = Q4{gv(gp, G_QUAT), gv(gp, G_QUAT + 1), gv(gp, G_QUAT + 2), gv(gp, G_QUAT + 3)};
+      const float margin = fmaxf(gv(a, G_MARGIN), gv(b, G_MARGIN));
+      CRes cr[4];
+      int nc = 0;
+      if (shape == NEWT_SHAPE_SPHERE) {
+        nc = np_sphere_plane(gpose, gv(gl, G_SIZE), margin, ppose, cr);
+      } else if (shape == NEWT_SHAPE_BOX) {
+        nc = np_box_plane(gpose, v3(gv(gl, G_SIZE), gv(gl, G_SIZE + 1), gv(gl, G_SIZE + 2)), margin, ppose, cr);
+      } else if (shape == NEWT_SHAPE_CAPSULE) {  // contact.rs:367-400: both segment ends
+        const V3 n = qrot(ppose.q, v3(0.f, 0.f, 1.f));
+        const V3 ax = qrot(gpose.q, v3(0.f, 0.f, 1.f));
+        const float r = gv(gl, G_SIZE), hh = gv(gl, G_SIZE + 1);
+        for (int k = 0; k < 2; ++k) {
+          const V3 e = k == 0 ? gpose.p + ax * hh : gpose.p - ax * hh;
+          const float raw = dot(e - ppose.p, n) - r;
+          if (raw <= margin) cr[nc++] = CRes{e - n * (r + raw * 0.5f), n, margin - raw};
+        }
+      }
+      for (int k = 0; k < nc; ++k) {
+        if (ncon >= G.maxc) { overflow = true; break; }
+        float* c = con + CREC * ncon;
+        // the narrowphase ran as (geom, plane); a pair listed as (plane, geom)
+        // is relabelled with the normal flipped (contact.rs:2509-2587)
+        c[K_GA] = __int_as_float(a);
+        c[K_GB] = __int_as_float(b);
+        c[K_LINK] = __int_as_float(link);
+        c[K_SIGN] = a_static ? -1.f : 1.f;
+        stv3(c + K_POS, cr[k].pos);
+        stv3(c + K_N, a_static ? -cr[k].n : cr[k].n);
+        c[K_PEN] = cr[k].pen;
+        c[K_GAP] = fmaxf(gv(a, G_GAP), gv(b, G_GAP));
+        c[K_MU] = fminf(gv(a, G_FRIC), gv(b, G_FRIC));
+        // combine_solref (geom.rs:156-185), combine_solimp (solver.rs:242)
+        const float ta = gv(a, G_SR), tb = gv(b, G_SR), da = gv(a, G_SR + 1), db = gv(b, G_SR + 1);
+        const bool dira = ta < 0.f, dirb = tb < 0.f;
+        c[K_SR] = dira != dirb ? (dira ? ta : tb) : fminf(ta, tb);
+        c[K_SR + 1] = dira != dirb ? (dira ? da : db) : fminf(da, db);
+        for (int q = 0; q < 3; ++q) c[K_SI + q] = fminf(gv(a, G_SI + q), gv(b, G_SI + q));
+        c[K_SI + 3] = gv(a, G_SI + 3);
+        c[K_SI + 4] = gv(a, G_SI + 4);
+        c[K_CONDIM] = (float)min(G.gtopo[2 * G.ng + a], G.gtopo[2 * G.ng + b]);
+        ++ncon;
+      }
+    }
+    if (overflow) status |= NEWT_WS_CONTACT_OVERFLOW;
+    // rows of the active contacts, in contact order (solver.rs:2881-2890)
+    int nr = 0;
+    for (int c = 0; c < ncon; ++c) {
+      float* cc = con + CREC * c;
+      const bool act = cc[K_PEN] - cc[K_GAP] > 0.f;
+      const int k = (int)cc[K_CONDIM] == 3 ? 4 : 1;
+      cc[K_ROW] = __int_as_float(act ? nr : -1);
+      if (!act) continue;
+      for (int f = 0; f < k; ++f) { rcon[nr + f] = c; rfac[nr + f] = k == 4 ? f : -1; }
+      nr += k;
+    }
+    wf[lay.misc] = __int_as_float(ncon);
+    wf[lay.misc + 1] = __int_as_float(nr);
+    wf[lay.misc + 2] = __int_as_float(0);
+  }
+  __syncwarp();
+  const int nr = __float_as_int(wf[lay.misc + 1]);
+  if (nr == 0) {  // no active contact: qacc stays a_free
+    if (lane == 0 && status) atomicOr(g.status + w, status);
+    return;
+  }
+
+  // ---- link COM Jacobians and world inertias, lane per link ----
+  for (int l = lane; l < L; l += 32) {
+    float* jv = wf + lay.jv + 3 * nv * l;
+    float* jw = wf + lay.jw + 3 * nv * l;
+    for (int k = 0; k < 3 * nv; ++k) { jv[k] = 0.f; jw[k] = 0.f; }
+    const float* pl = pose + 7 * l;
+    chain_columns(g, w, pose, l, ldv3(pl), [&](int k, V3 rot, V3 tr) { stv3(jw + 3 * k, rot); stv3(jv + 3 * k, tr); });
+    const M3 R = quat_mat(Q4{pl[3], pl[4], pl[5], pl[6]});
+    M3 RT;
+    for (int r = 0; r < 3; ++r) for (int c = 0; c < 3; ++c) RT.m[r][c] = R.m[c][r];
+    const S3 Ib{g.inert[(6 * l) * cap + w], g.inert[(6 * l + 1) * cap + w], g.inert[(6 * l + 2) * cap + w],
+                g.inert[(6 * l + 3) * cap + w], g.inert[(6 * l + 4) * cap + w], g.inert[(6 * l + 5) * cap + w]};
+    const S3 Iw = sym_congr(RT, Ib);  // R I R^T
+    float* iw = wf + lay.iw + 6 * l;
+    iw[0] = Iw.xx; iw[1] = Iw.yy; iw[2] = Iw.zz; iw[3] = Iw.xy; iw[4] = Iw.xz; iw[5] = Iw.yz;
+  }
+  __syncwarp();
+
+  // ---- mass matrix (lower triangle, column-major), lane per entry ----
+  float* Mm = wf + lay.M;
+  {
+    int e = 0;
+    for (int j = 0; j < nv; ++j)
+      for (int i = j; i < nv; ++i, ++e) {
+        if ((e & 31) != lane) continue;
+        float s = 0.f;
+        for (int l = 0; l < L; ++l) {
+          const float* jv = wf + lay.jv + 3 * nv * l;
+          const float* jw = wf + lay.jw + 3 * nv * l;
+          const float* iw = wf + lay.iw + 6 * l;
+          const S3 I{iw[0], iw[1], iw[2], iw[3], iw[4], iw[5]};
+          s += g.mass[l * cap + w] * dot(ldv3(jv + 3 * i), ldv3(jv + 3 * j)) + dot(ldv3(jw + 3 * i), smv(I, ldv3(jw + 3 * j)));
+        }
+        Mm[j * nv + i] = s;
+      }
+  }
+  __syncwarp();
+  // armature (diagonal, child joints) and the implicit damping dt*B (tree.rs:645-684)
+  float* LM = wf + lay.LM;
+  float* LD = wf + lay.LD;
+  for (int k = lane; k < nv * nv; k += 32) { LM[k] = Mm[k]; LD[k] = Mm[k]; }
+  __syncwarp();
+  if (lane == 0) {
+    for (int i = 0; i < L; ++i) {
+      const int jt = g.topo[4 * i + 1], vo = g.topo[4 * i + 3];
+      if (jt == JF) {
+        const float dm = dt * g.damp[i * cap + w];
+        for (int k = 0; k < 6; ++k) LM[(vo + k) * nv + vo + k] += dm;
+      } else if (jt == JH || jt == JS) {
+        const float arm = g.arm[i * cap + w];
+        LD[vo * nv + vo] += arm;
+        LM[vo * nv + vo] += arm + dt * g.damp[i * cap + w];
+      }
+    }
+  }
+  __syncwarp();
+  float mn, mx;
+  if (!warp_cholesky(LM, nv, nv, lane, &mn, &mx) || !warp_cholesky(LD, nv, nv, lane, &mn, &mx)) {
+    if (lane == 0) atomicOr(g.status + w, status | NEWT_WS_NOT_PD);
+    return;
+  }
+
+  // ---- Jacobian rows of the cone facets, velocities, lane per row ----
+  float* Jt = wf + lay.jt;
+  for (int r = lane; r < nr; r += 32) {
+    const float* cc = con + CREC * rcon[r];
+    const int link = __float_as_int(cc[K_LINK]);
+    const float sign = cc[K_SIGN], mu = cc[K_MU];
+    const V3 n = ldv3(cc + K_N), pt = ldv3(cc + K_POS);
+    V3 dir = n;
+    const int f = rfac[r];
+    if (f >= 0) {  // pyramidal facets n +- mu t1, n +- mu t2 (solver.rs:3401-3429)
+      const V3 ref = fabsf(n.z) < 0.9f ? v3(0.f, 0.f, 1.f) : v3(1.f, 0.f, 0.f);  // tangent_basis
+      V3 t1 = cross(ref, n);
+      t1 = t1 * (1.f / sqrtf(len2(t1)));
+      const V3 t = f < 2 ? t1 : cross(n, t1);
+      dir = n + t * ((f & 1) ? -mu : mu);
+    }
+    for (int k = 0; k < nv; ++k) Jt[(size_t)k * ld + r] = 0.f;
+    chain_columns(g, w, pose, link, pt, [&](int k, V3, V3 tr) { Jt[(size_t)k * ld + r] = dot(tr, dir) * sign; });
+    float vel = 0.f, vfree = 0.f;
+    for (int k = 0; k < nv; ++k) {
+      const float jk = Jt[(size_t)k * ld + r];
+      vel += jk * g.qd[k * cap + w];
+      vfree += jk * g.qacc[k * cap + w];
+    }
+    vu[r] = vel;
+    vv[r] = vfree * dt;  // J . (a_free dt): the free-motion velocity change
+  }
+  __syncwarp();
+
+  // ---- Y = L^-1 J^T and A = Y^T Y (solver.rs:3043-3066), lane per row ----
+  float* Y = wf + lay.y;
+  float* H = wf + lay.H;
+  for (int r = lane; r < nr; r += 32) {
+    for (int k = 0; k < nv; ++k) {
+      float s = Jt[(size_t)k * ld + r];
+      for (int m = 0; m < k; ++m) s -= LM[m * nv + k] * Y[(size_t)m * ld + r];
+      Y[(size_t)k * ld + r] = s / LM[k * nv + k];
+    }
+  }
+  __syncwarp();
+  for (int r = lane; r < nr; r += 32)
+    for (int c = 0; c < nr; ++c) {
+      float s = 0.f;
+      for (int k = 0; k < nv; ++k) s += Y[(size_t)k * ld + r] * Y[(size_t)k * ld + c];
+      H[(size_t)c * ld + r] = s;
+    }
+  // ---- mean inverse weight of each link's COM (tree_body_invweight0), lane per link ----
+  for (int l = lane; l < L; l += 32) {
+    const float* jv = wf + lay.jv + 3 * nv * l;
+    float tr = 0.f;
+    for (int axis = 0; axis < 3; ++axis) {
+      // |L_D^-1 jv_axis|^2 = jv_axis^T M^-1 jv_axis (forward substitution only)
+      float y[NEWT_MAX_LINKS + 5];
+      float s2 = 0.f;
+      for (int k = 0; k < nv; ++k) {
+        float s = jv[3 * k + axis];
+        for (int m = 0; m < k; ++m) s -= LD[m * nv + k] * y[m];
+        y[k] = s / LD[k * nv + k];
+        s2 += y[k] * y[k];
+      }
+      tr += s2;
+    }
+    wf[lay.tw + l] = tr / 3.f;
+  }
+  __syncwarp();
+
+  // ---- regulariser, diagonal and bias per row (solver.rs:3068-3121) ----
+  for (int r = lane; r < nr; r += 32) {
+    const float* cc = con + CREC * rcon[r];
+    const float pen = cc[K_PEN] - cc[K_GAP], mu = cc[K_MU];
+    const Soft s{cc[K_SR], cc[K_SR + 1], cc[K_SI], cc[K_SI + 1], cc[K_SI + 2], cc[K_SI + 3], (int)cc[K_SI + 4]};
+    const float d = impedance_at(-pen, s);
+    const bool pyr = rfac[r] >= 0;
+    const float tw = wf[lay.tw + __float_as_int(cc[K_LINK])];
+    const float base = (1.f - d) / d * (pyr ? tw * (1.f + mu * mu) : tw);
+    const float reg = pyr ? 2.f * mu * mu * base : base;
+    vreg[r] = reg;
+    vdiag[r] = H[(size_t)r * ld + r] + reg;
+    vb[r] = vv[r] - reference_accel(-pen, vu[r], s.tc, s.dr, s, dt) * dt;
+    vx[r] = 0.f;
+  }
+  __syncwarp();
+
+  const int mode = G.mode[w];
+  const int iters = G.iters[w];
+  int done_it = 0;
+  if (mode == NEWT_SOLVER_PGS) {
+    // dense Gauss-Seidel, four non-negative facet steps per pyramidal block
+    // (world_pgs_non_negative, solver.rs:3851-3862)
+    for (int it = 0; it < iters; ++it)
+      for (int r = 0; r < nr; ++r) {
+        float s = 0.f;
+        for (int c = lane; c < nr; c += 32) s += H[(size_t)r * ld + c] * vx[c];
+        s = warp_sum(s);
+        const float res = (vb[r] + s) + vreg[r] * vx[r];
+        const float p = vx[r] - res / vdiag[r];
+        __syncwarp();
+        if (lane == 0) vx[r] = p < 0.f ? 0.f : p;
+        __syncwarp();
+      }
+    done_it = iters;
+  } else {
+    // ---- Newton (newton.rs:275-339) on H = A + diag(R) ----
+    for (int r = lane; r < nr; r += 32) H[(size_t)r * ld + r] += vreg[r];
+    __syncwarp();
+    float* LH = wf + lay.LH;
+    double* LHd = reinterpret_cast<double*>(wf + lay.LHd);
+    auto copy_h = [&]() {
+      __syncwarp();
+      for (int c = 0; c < nr; ++c)
+        for (int r = lane; r < nr; r += 32) LH[(size_t)c * ld + r] = H[(size_t)c * ld + r];
+      __syncwarp();
+    };
+    copy_h();
+    bool ok = warp_cholesky(LH, nr, ld, lane, &mn, &mx);
+    if (!ok) {
+      // zero-friction facets duplicate rows: a solver-only pivot (solver.rs:3215-3232)
+      bool zero_mu = false;
+      for (int r = lane; r < nr; r += 32) zero_mu = zero_mu || (rfac[r] >= 0 && con[CREC * rcon[r] + K_MU] == 0.f);
+      if (__any_sync(FULL, zero_mu)) {
+        float sc = 0.f;
+        for (int c = 0; c < nr; ++c)
+          for (int r = lane; r < nr; r += 32) sc = fmaxf(sc, fabsf(H[(size_t)c * ld + r]));
+        for (int o = 16; o > 0; o >>= 1) sc = fmaxf(sc, __shfl_xor_sync(FULL, sc, o));
+        const float piv = fmaxf(sc * 1.0e-6f, 1.0e-7f);
+        __syncwarp();
+        for (int r = lane; r < nr; r += 32) H[(size_t)r * ld + r] += piv;
+        copy_h();
+        ok = warp_cholesky(LH, nr, ld, lane, &mn, &mx);
+      }
+    }
+    bool use64 = !ok || (mx / mn) * (mx / mn) > 1.0e6f;
+    if (use64) {
+      __syncwarp();
+      for (int c = 0; c < nr; ++c)
+        for (int r = lane; r < nr; r += 32) LHd[(size_t)c * ld + r] = (double)H[(size_t)c * ld + r];
+      double mnd, mxd;
+      ok = warp_cholesky(LHd, nr, ld, lane, &mnd, &mxd);
+      status |= NEWT_WS_FP64_FALLBACK;
+    }
+    if (!ok) {
+      status |= NEWT_WS_NOT_PD;
+      for (int r = lane; r < nr; r += 32) vx[r] = 0.f;
+    } else {
+      float cur = 0.f;  // cost at x = 0
+      const int max_it = iters > 1 ? iters : 1;
+      for (int it = 0; it < max_it; ++it) {
+        // gradient g = H x + b, direction d = -(L L^T)^-1 g
+        warp_matvec(H, nr, ld, vx, vg, lane);
+        for (int r = lane; r < nr; r += 32) { vg[r] += vb[r]; vd[r] = -vg[r]; }
+        __syncwarp();
+        if (use64) warp_llt_solve(LHd, nr, ld, vd, lane);
+        else warp_llt_solve(LH, nr, ld, vd, lane);
+        if (warp_dot(vg, vd, nr, lane) >= 0.f) break;
+        // ---- exact line search over the projected path (newton.rs:435-556) ----
+        for (int r = lane; r < nr; r += 32) {
+          const float x = vx[r], d = vd[r];
+          const bool fr = x > 0.f || (x == 0.f && d > 0.f);
+          vp[r] = fr ? x : 0.f;
+          vs[r] = fr ? d : 0.f;
+          const float a = (x > 0.f && d < 0.f) ? -x / d : 2.f;  // where x + a d reaches zero
+          vreg[r] = (a > 0.f && a < 1.f) ? a : 2.f;
+        }
+        warp_matvec(H, nr, ld, vp, vu, lane);
+        warp_matvec(H, nr, ld, vs, vv, lane);
+        float best_a = 0.f, best_c = cur, lo = 0.f;
+        for (int guard = 0; guard <= nr; ++guard) {
+          // cost on the window: c0 + c1 a + c2 a^2 / 2 with p = P + a S
+          const float Pu = warp_dot(vp, vu, nr, lane), Pv = warp_dot(vp, vv, nr, lane);
+          const float Sv = warp_dot(vs, vv, nr, lane), bP = warp_dot(vb, vp, nr, lane), bS = warp_dot(vb, vs, nr, lane);
+          // next breakpoint (warp argmin)
+          float bm = 2.f;
+          int bi = -1;
+          for (int r = lane; r < nr; r += 32) if (vreg[r] < bm) { bm = vreg[r]; bi = r; }
+          for (int o = 16; o > 0; o >>= 1) {
+            const float om = __shfl_xor_sync(FULL, bm, o);
+            const int oi = __shfl_xor_sync(FULL, bi, o);
+            if (om < bm || (om == bm && oi >= 0 && (bi < 0 || oi < bi))) { bm = om; bi = oi; }
+          }
+          const float hi = bm < 1.f ? bm : 1.f;
+          if (hi - lo > 1.0e-7f) {
+            const float c0 = 0.5f * Pu + bP, c1 = Pv + bS, c2 = Sv;
+            const float opt = c2 > 0.f ? fminf(fmaxf(-c1 / c2, lo), hi) : 0.5f * (lo + hi);
+            const float cand[3] = {lo, hi, opt};
+            for (int k = 0; k < 3; ++k) {
+              const float a = cand[k];
+              const float cost = c0 + c1 * a + 0.5f * c2 * a * a;
+              if (cost < best_c) { best_c = cost; best_a = a; }
+            }
+          }
+          if (bi < 0) break;
+          // coordinate bi leaves the free set: P, S lose it, H P and H S a column
+          const float xj = vp[bi], dj = vs[bi];
+          __syncwarp();
+          for (int r = lane; r < nr; r += 32) {
+            const float hc = H[(size_t)bi * ld + r];
+            vu[r] -= xj * hc;
+            vv[r] -= dj * hc;
+          }
+          if (lane == 0) { vp[bi] = 0.f; vs[bi] = 0.f; vreg[bi] = 2.f; }
+          __syncwarp();
+          lo = hi;
+        }
+        if (best_a <= 0.f || cur - best_c <= 1.0e-7f * (1.f + fabsf(cur))) break;
+        for (int r = lane; r < nr; r += 32) {
+          const float x = vx[r] + best_a * vd[r];
+          vx[r] = x < 0.f ? 0.f : x;
+        }
+        __syncwarp();
+        cur = best_c;
+        done_it = it + 1;
+      }
+      if (done_it == max_it) status |= NEWT_WS_ITER_CAP;
+    }
+  }
+  __syncwarp();
+
+  // ---- outputs: impulses, J^T f / dt, qacc = a_free + (M + dt B)^-1 J^T f / dt ----
+  for (int r = lane; r < nr; r += 32) wf[lay.imp + r] = vx[r];
+  for (int k = lane; k < nv; k += 32) {
+    float s = 0.f;
+    for (int r = 0; r < nr; ++r) s += Jt[(size_t)k * ld + r] * vx[r];
+    vg[k] = s / dt;
+  }
+  __syncwarp();
+  warp_llt_solve(LM, nv, nv, vg, lane);
+  for (int k = lane; k < nv; k += 32) g.qacc[k * cap + w] += vg[k];
+  if (lane == 0) {
+    wf[lay.misc + 2] = __int_as_float(done_it);
+    if (status) atomicOr(g.status + w, status);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+extern "C" size_t newt_tc_ws_bytes(int L, int nv, int ng, int maxc) {
+  return (size_t)tc_layout(L, nv, ng, maxc).words * sizeof(float);
+}
+extern "C" size_t newt_tc_smem_bytes(int nv, int maxc) {
+  return (size_t)TC_WARPS * tc_warp_words(nv, maxc) * sizeof(float);
+}
+// Kernel attribute for the dynamic shared memory (outside stream capture).
+extern "C" cudaError_t newt_tc_init(int nv, int maxc) {
+  return cudaFuncSetAttribute(tc_k_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)newt_tc_smem_bytes(nv, maxc));
+}
+extern "C" void newt_launch_tc_solve(const TcGroupDev& G, cudaStream_t st) {
+  const int grid = (G.t.n + TC_WARPS - 1) / TC_WARPS;
+  if (grid == 0) return;
+  tc_k_solve<<<grid, 32 * TC_WARPS, newt_tc_smem_bytes(G.t.nv, G.maxc), st>>>(G);
+}
+extern "C" void newt_tc_offsets(int L, int nv, int ng, int maxc, int* con, int* imp, int* misc) {
+  const TcLay t = tc_layout(L, nv, ng, maxc);
+  *con = t.con;
+  *imp = t.imp;
+  *misc = t.misc;
+}
+
+extern "C" void newt_launch_tree_aba(const TreeGroupDev& g, cudaStream_t st);
+extern "C" void newt_launch_tree_integrate(const TreeGroupDev& g, cudaStream_t st);
+
+#define CKT(call)                                                               \
+  do {                                                                          \
+    cudaError_t e_ = (call);                                                    \
+    if (e_ != cudaSuccess) { ctx->err = std::string(#call ": ") + cudaGetErrorString(e_); return NEWT_E_CUDA; } \
+  } while (0)
+
+// n_steps env-steps of one tree-contact group: a_free, the contact solve and
+// the integration, three launches per env-step on the context's stream.
 extern "C" int newt_tc_step(newt_gpu_ctx* ctx, HostGroup* g, int n_steps, int fused) {
-  (void)g; (void)n_steps; (void)fused;
-  ctx->err = "tree-contact worlds are not supported by this build";
-  return NEWT_E_INVALID;
+  (void)fused;
+  if (g->n == 0) return NEWT_OK;
+  const size_t per = newt_tc_ws_bytes(g->size, g->nv, g->ng, g->maxc);
+  const size_t need = per * (size_t)g->cap;
+  if (g->plain_scratch_bytes < need) {
+    if (g->plain_scratch) cudaFree(g->plain_scratch);
+    g->plain_scratch = nullptr;
+    g->plain_scratch_bytes = 0;
+    CKT(cudaMalloc(&g->plain_scratch, need));
+    CKT(cudaMemset(g->plain_scratch, 0, need));
+    g->plain_scratch_bytes = need;
+  }
+  g->scr_stride = (long)(per / sizeof(float));
+  CKT(newt_tc_init(g->nv, g->maxc));
+  const TcGroupDev d = g->tc_dev();
+  for (int s = 0; s < n_steps; ++s) {
+    newt_launch_tree_aba(d.t, ctx->stream);
+    newt_launch_tc_solve(d, ctx->stream);
+    newt_launch_tree_integrate(d.t, ctx->stream);
+    ctx->launches += 3;
+  }
+  return NEWT_OK;
 }

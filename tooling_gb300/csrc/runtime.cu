@@ -123,6 +123,25 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
     return NEWT_OK;
   }
   if (d.n_links > 0 && d.n_bodies == 0 && d.n_geoms > 0) {
+    // one tree whose link geoms (spheres, boxes, capsules) touch static planes
+    int nlink_geoms = 0;
+    for (int k = 0; k < d.n_geoms; ++k) {
+      const newt_geom_desc& G = d.geoms[k];
+      if (G.body >= 0) return fail(ctx, NEWT_E_INVALID, "body geom in a world without free bodies");
+      if (G.link >= d.n_links) return fail(ctx, NEWT_E_INVALID, "geom link out of range");
+      if (G.link >= 0) {
+        if (G.shape != NEWT_SHAPE_SPHERE && G.shape != NEWT_SHAPE_BOX && G.shape != NEWT_SHAPE_CAPSULE)
+          return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "link geoms must be spheres, boxes or capsules on the GPU path");
+        ++nlink_geoms;
+      } else if (G.shape != NEWT_SHAPE_PLANE) {
+        return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "static geoms must be planes");
+      }
+      if (G.condim != 3 && G.condim != 1) return fail(ctx, NEWT_E_INVALID, "condim must be 1 or 3");
+    }
+    if (d.tree_self_collision && nlink_geoms > 1)
+      return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "in-tree geom pairs are not on the GPU path (disable tree self-collision)");
+    if (d.solver != NEWT_SOLVER_PGS && d.solver != NEWT_SOLVER_NEWTON)
+      return fail(ctx, NEWT_E_INVALID, "tree-contact worlds need the PGS or Newton solver");
     m.kind = GK_TREE_CONTACT; m.size = d.n_links;
     return NEWT_OK;
   }
@@ -138,6 +157,7 @@ HostGroup* find_or_make_group(newt_gpu_ctx* ctx, const HostModel& m) {
   auto g = std::make_unique<HostGroup>();
   g->kind = m.kind; g->size = m.size; g->np = m.np; g->topo_key = m.topo_key();
   g->nq = m.nq; g->nv = m.nv;
+  if (m.kind == GK_TREE_CONTACT) g->setup_tc(m);
   g->id = (int)ctx->groups.size();
   ctx->groups.push_back(std::move(g));
   return ctx->groups.back().get();

@@ -26,7 +26,12 @@ struct HostModel {
     std::string k;
     for (auto& l : links) { k += std::to_string(l.parent); k += ':'; k += std::to_string(l.joint); k += ','; }
     if (kind == GK_TREE_CONTACT) {
-      for (auto& gd : geoms) { k += 'g'; k += std::to_string(gd.shape); k += '@'; k += std::to_string(gd.link); }
+      // shapes, attachments, condim and filters fix the pair list and the rows
+      for (auto& gd : geoms) {
+        k += 'g'; k += std::to_string(gd.shape); k += '@'; k += std::to_string(gd.link);
+        k += 'c'; k += std::to_string(gd.condim); k += 'f'; k += std::to_string(gd.group); k += '/';
+        k += std::to_string(gd.mask);
+      }
     }
     if (kind == GK_PILE) {
       // geom order fixes the pair order; shapes may differ per world
@@ -68,8 +73,15 @@ struct HostGroup {
   // pile layout
   PileLayout lay{};
   int maxc = 0;
-  // tree-contact data (see tc_layout in newton_kernels.cu)
-  void* tc = nullptr;
+  // tree-contact groups: per-geom model rows, geom topology, candidate pairs
+  int ng = 0, npairs = 0;
+  int r_geom = 0, ri_mode = 0, ri_iters = 0;
+  std::vector<int> gtopo, gpairs;
+  int* dgtopo = nullptr;
+  int* dpairs = nullptr;
+  bool soa() const { return kind == GK_TREE || kind == GK_TREE_CONTACT; }
+  TcGroupDev tc_dev() const;
+  void setup_tc(const HostModel& m);
   void* plain_scratch = nullptr;  // pile solver scratch (cap worlds)
   size_t plain_scratch_bytes = 0;
   long scr_stride = 0;             // floats per world in plain_scratch
@@ -95,10 +107,10 @@ struct HostGroup {
   PileGroupDev pile_dev() const;
   size_t bytes_per_world() const;
   // float/int element accessors (host mirror)
-  float& F(size_t row, size_t w) { return kind == GK_TREE ? hF[row * cap + w] : hF[w * frows + row]; }
-  int& I(size_t row, size_t w) { return kind == GK_TREE ? hI[row * cap + w] : hI[w * irows + row]; }
-  float Fc(size_t row, size_t w) const { return kind == GK_TREE ? hF[row * cap + w] : hF[w * frows + row]; }
-  int Ic(size_t row, size_t w) const { return kind == GK_TREE ? hI[row * cap + w] : hI[w * irows + row]; }
+  float& F(size_t row, size_t w) { return soa() ? hF[row * cap + w] : hF[w * frows + row]; }
+  int& I(size_t row, size_t w) { return soa() ? hI[row * cap + w] : hI[w * irows + row]; }
+  float Fc(size_t row, size_t w) const { return soa() ? hF[row * cap + w] : hF[w * frows + row]; }
+  int Ic(size_t row, size_t w) const { return soa() ? hI[row * cap + w] : hI[w * irows + row]; }
 };
 
 struct newt_gpu_ctx {
@@ -148,3 +160,6 @@ int step_batched(newt_gpu_ctx* ctx, int n_steps);
 extern "C" int newt_tree_bucket(int L);
 extern "C" void newt_launch_tree_fused(const TreeGroupDev& g, int base, int count, int n_steps, cudaStream_t st);
 extern "C" void newt_launch_tree_plain(const TreeGroupDev& g, cudaStream_t st);
+extern "C" void newt_tc_offsets(int L, int nv, int ng, int maxc, int* con, int* imp, int* misc);
+extern "C" size_t newt_tc_ws_bytes(int L, int nv, int ng, int maxc);
+extern "C" size_t newt_pile_ws_bytes(int nb, int np, int maxc);

@@ -311,6 +311,29 @@ extern "C" cudaError_t newt_tree_prepare_kernels() {
   return e;
 }
 
+// The two plain stages on their own (the tree-contact step runs its contact
+// solve between them).
+extern "C" void newt_launch_tree_aba(const TreeGroupDev& g, cudaStream_t st) {
+  const int B = 128;
+  const int grid = (g.n + B - 1) / B;
+  if (grid == 0) return;
+  switch (newt_tree_bucket(g.L)) {
+#define X(M) case M: tree_aba_kernel<M><<<grid, B, 0, st>>>(g); break;
+    NEWT_TREE_BUCKETS(X)
+#undef X
+  }
+}
+extern "C" void newt_launch_tree_integrate(const TreeGroupDev& g, cudaStream_t st) {
+  const int B = 128;
+  const int grid = (g.n + B - 1) / B;
+  if (grid == 0) return;
+  switch (newt_tree_bucket(g.L)) {
+#define X(M) case M: tree_integrate_kernel<M><<<grid, B, 0, st>>>(g); break;
+    NEWT_TREE_BUCKETS(X)
+#undef X
+  }
+}
+
 extern "C" void newt_launch_tree_plain(const TreeGroupDev& g, cudaStream_t st) {
   const int B = 128;
   int grid = (g.n + B - 1) / B;

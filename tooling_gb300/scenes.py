@@ -194,3 +194,108 @@ def pile_batch(n_worlds: int = 8192, n_bodies: int = 16, seed_index: int = 1, dt
                     np.stack(geoms), [n_bodies + 1] * n_worlds, dt, (0.0, 0.0, -9.81), M.SOLVER_PGS, iterations)
     batch.qpos[:] = np.concatenate(qps)
     return batch
+
+
+# ---------------------------------------------------------------------------
+# quadruped: floating-base torso with 4 x 3 revolute legs on a plane
+# ---------------------------------------------------------------------------
+QUAD_TORSO_HALF = (0.2, 0.1, 0.05)  # 0.4 x 0.2 x 0.1 m box
+QUAD_TORSO_MASS = 5.0
+QUAD_LINK_HALF = 0.1                # capsule links 0.2 m long
+QUAD_LINK_RADIUS = 0.02
+QUAD_LINK_MASS = 0.5
+QUAD_MU = 0.8
+QUAD_CROUCH = (0.0, 0.9, -1.8)      # hip-ab, hip-flex, knee nominal angles
+QUAD_HIPS = ((0.15, 1.0), (0.15, -1.0), (-0.15, 1.0), (-0.15, -1.0))  # (x, side)
+
+
+def _rot(axis, a):
+    c, s = math.cos(a), math.sin(a)
+    if axis == 0:
+        return np.array([[1, 0, 0], [0, c, -s], [0, s, c]])
+    return np.array([[c, 0, s], [0, 1, 0], [-s, 0, c]])
+
+
+def _quad_lowest_point(base_z, q):
+    """Lowest point of the legs' capsules (forward kinematics with the torso
+    level at height base_z; used to reject initial penetration)."""
+    low = np.inf
+    for leg, (hx, side) in enumerate(QUAD_HIPS):
+        ab, flex, knee = q[3 * leg:3 * leg + 3]
+        # link 1: hinge about x at the torso side, capsule along y, outward
+        R1 = _rot(0, ab)
+        j1 = np.array([hx, side * QUAD_TORSO_HALF[1], base_z])
+        p1 = j1 + R1 @ np.array([0.0, side * QUAD_LINK_HALF, 0.0])
+        e1 = [p1 + R1 @ np.array([0.0, s * QUAD_LINK_HALF, 0.0]) for s in (1, -1)]
+        # link 2: hip flexion about y at link 1's outer end, hanging down
+        j2 = p1 + R1 @ np.array([0.0, side * QUAD_LINK_HALF, 0.0])
+        R2 = R1 @ _rot(1, flex)
+        p2 = j2 - R2 @ np.array([0.0, 0.0, QUAD_LINK_HALF])
+        j3 = p2 - R2 @ np.array([0.0, 0.0, QUAD_LINK_HALF])
+        R3 = R2 @ _rot(1, knee)
+        p3 = j3 - R3 @ np.array([0.0, 0.0, QUAD_LINK_HALF])
+        ends = e1 + [p2 + R2 @ np.array([0, 0, s * QUAD_LINK_HALF]) for s in (1, -1)]
+        ends += [p3 + R3 @ np.array([0, 0, s * QUAD_LINK_HALF]) for s in (1, -1)]
+        low = min(low, min(e[2] for e in ends) - QUAD_LINK_RADIUS)
+    return low
+
+
+def _quad_world(rng: np.random.Generator, max_tries: int = 100):
+    """Torso box (5 kg) with a free joint; per leg a hip-ab link (hinge x, a
+    lateral capsule), a thigh (hinge y) and a shank (hinge y), capsules 0.2 m
+    x r 0.02 m, 0.5 kg.  Base height U(0.3, 0.5); joint angles = nominal crouch
+    + N(0, 0.2), resampled until no capsule starts below the plane (straight
+    0.6 m legs cannot stand under a 0.3-0.5 m base)."""
+    cap_i = capsule_inertia(QUAD_LINK_MASS, QUAD_LINK_RADIUS, QUAD_LINK_HALF)
+    # a capsule along the link's y axis: its z axis turned onto y
+    lat_q = (-math.sin(math.pi / 4), 0.0, 0.0, math.cos(math.pi / 4))
+    links = [_link(-1, M.JOINT_FREE, mass=QUAD_TORSO_MASS, inertia=box_inertia(QUAD_TORSO_MASS, QUAD_TORSO_HALF))]
+    geoms = [_geom(M.SHAPE_PLANE, friction=QUAD_MU),
+             _geom(M.SHAPE_BOX, link=0, size=QUAD_TORSO_HALF, friction=QUAD_MU)]
+    for leg, (hx, side) in enumerate(QUAD_HIPS):
+        l1, l2, l3 = 1 + 3 * leg, 2 + 3 * leg, 3 + 3 * leg
+        links.append(_link(0, M.JOINT_HINGE, axis=(1.0, 0.0, 0.0), jp=(hx, side * QUAD_TORSO_HALF[1], 0.0),
+                           jc=(0.0, -side * QUAD_LINK_HALF, 0.0), mass=QUAD_LINK_MASS, inertia=cap_i))
+        links.append(_link(l1, M.JOINT_HINGE, axis=(0.0, 1.0, 0.0), jp=(0.0, side * QUAD_LINK_HALF, 0.0),
+                           jc=(0.0, 0.0, QUAD_LINK_HALF), mass=QUAD_LINK_MASS, inertia=cap_i))
+        links.append(_link(l2, M.JOINT_HINGE, axis=(0.0, 1.0, 0.0), jp=(0.0, 0.0, -QUAD_LINK_HALF),
+                           jc=(0.0, 0.0, QUAD_LINK_HALF), mass=QUAD_LINK_MASS, inertia=cap_i))
+        geoms.append(_geom(M.SHAPE_CAPSULE, link=l1, size=(QUAD_LINK_RADIUS, QUAD_LINK_HALF, 0.0), quat=lat_q,
+                           friction=QUAD_MU))
+        for l in (l2, l3):
+            geoms.append(_geom(M.SHAPE_CAPSULE, link=l, size=(QUAD_LINK_RADIUS, QUAD_LINK_HALF, 0.0),
+                               friction=QUAD_MU))
+    base = float(rng.uniform(0.3, 0.5))
+    nominal = np.tile(QUAD_CROUCH, 4)
+    for _ in range(max_tries):
+        q = nominal + rng.normal(0.0, 0.2, 12)
+        if _quad_lowest_point(base, q) > 1e-3:
+            break
+    else:
+        q = nominal
+    qpos = np.concatenate([[0.0, 0.0, base, 1.0, 0.0, 0.0, 0.0], q])
+    return links, geoms, qpos
+
+
+def quadruped_batch(n_worlds: int = 16384, seed_index: int = 2, dt: float = 2e-3, iterations: int = 20,
+                    solver: int = M.SOLVER_NEWTON, first_world: int = 0) -> M.Batch:
+    cs = config_seed(seed_index)
+    links, geoms, qps = [], [], []
+    for w in range(first_world, first_world + n_worlds):
+        l, g, qp = _quad_world(world_rng(cs, w))
+        links += l; geoms += g; qps.append(qp)
+    b = M.Batch(np.stack(links), [13] * n_worlds, np.zeros(0, M.BODY_DT), [0] * n_worlds, np.stack(geoms),
+                [14] * n_worlds, dt, (0.0, 0.0, -9.81), solver, iterations)
+    b.qpos[:] = np.concatenate(qps)
+    return b
+
+
+def quadruped_controls(n_worlds: int, block: int, seed_index: int = 2, first_world: int = 0) -> np.ndarray:
+    """Joint torques tau ~ N(0, 2) for the 12 actuated DoF of every world,
+    for control block `block` (the controls are resampled every 20 steps);
+    MuJoCo qvel order (6 free-root entries of zero first)."""
+    cs = config_seed(seed_index)
+    out = np.zeros((n_worlds, 18), np.float32)
+    for i, w in enumerate(range(first_world, first_world + n_worlds)):
+        out[i, 6:] = world_rng(cs ^ (0x9E3779B9 * (block + 1)), w).normal(0.0, 2.0, 12)
+    return out.reshape(-1)
