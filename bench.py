@@ -43,6 +43,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--plain", action="store_true", help="also time the plain (per-stage launch) form")
+    ap.add_argument("--workload", default="pile", choices=["pile", "quadruped"],
+                    help="pile: 16 free bodies on a plane (default); quadruped: Newton tree contact")
     return ap.parse_args()
 
 
@@ -258,6 +260,136 @@ def run_gpu(args, rank, ws, local, dist):
     return out, (batch, start_qpos, start_qvel)
 
 
+def tc_kernel_bytes(kernel: str, n_worlds: int, batch, contacts_per_world: float) -> float:
+    """Algorithmic HBM bytes of one launch (one env-step) of a tree-contact
+    kernel for quadruped worlds (13 links, 14 geoms, nq 19, nv 18).
+      tree_aba_kernel: per link model (axis, joint offsets, mass, inertia,
+        damping, armature: 18 words), q, qdot and qfrc read, qacc written;
+      tc_k_solve: the same model plus 20 words per geom, q, qdot and a_free
+        read, qacc written, and per contact its 24-word record and 4 impulses
+        written;
+      tree_integrate_kernel: q, qdot, qacc read, q and qdot written."""
+    L, G, nq, nv = int(batch.n_links[0]), int(batch.n_geoms[0]), int(batch.nq[0]), int(batch.nv[0])
+    if kernel == "tree_aba_kernel":
+        words = 18 * L + nq + 2 * nv + nv
+    elif kernel == "tc_k_solve":
+        words = 18 * L + 20 * G + nq + 2 * nv + nv + contacts_per_world * 28
+    else:
+        words = nq + 2 * nv + nq + nv
+    return 4.0 * n_worlds * words
+
+
+def run_gpu_quadruped(args, rank, ws, local, dist):
+    """Quadrupeds on a plane, Newton <= 20 iterations, dt 2e-3: one bench
+    step is one control block of 20 env-steps (the torques are resampled
+    every 20 steps and uploaded before the block)."""
+    from tooling_gb300 import build as B
+    B.build()
+    from tooling_gb300 import Engine, STEP_BATCHED, scenes
+    eng = Engine(device=local)
+    W = args.worlds
+    batch = scenes.quadruped_batch(n_worlds=W, first_world=rank * W)
+    slots = eng.alloc(eng.upload(batch))
+    eng.set_state(slots, batch.qpos, batch.qvel)
+    S = 20
+    n_blocks = max(3, args.warmup) + 2 * args.steps
+    ctrl = [scenes.quadruped_controls(W, k, first_world=rank * W) for k in range(n_blocks)]
+    eng.pile_profile(1)
+    blk = 0
+    for _ in range(max(3, args.warmup)):
+        eng.set_qfrc(slots, ctrl[blk]); blk += 1
+        eng.step(S, STEP_BATCHED)
+    eng.sync()
+    start_qpos, start_qvel = eng.get_state(slots, int(batch.nq.sum()), int(batch.nv.sum()))
+    launches0 = eng.launch_count()
+    clocks = Clocks(local)
+    clocks.start()
+    per_step, kernel_ms = [], {}
+    barrier(dist)
+    eng.sync()
+    for _ in range(args.steps):
+        eng.set_qfrc(slots, ctrl[blk]); blk += 1  # the control block, uploaded before the timed step
+        eng.flush_l2()
+        eng.event(0)
+        eng.step(S, STEP_BATCHED)
+        eng.event(1)
+        per_step.append(eng.elapsed_ms())
+        for k, v in eng.tc_profile().items():
+            kernel_ms[k] = kernel_ms.get(k, 0.0) + v
+    eng.sync()
+    barrier(dist)
+    clk = clocks.stop()
+    launches = eng.launch_count() - launches0
+    total_ms = max_over_ranks(dist, float(sum(per_step)))
+    value = W * S * args.steps * ws / (total_ms / 1e3)
+    st = eng.status(slots)
+    sample = slots[:: max(1, W // 64)]
+    contacts = float(np.mean([len(eng.contacts(int(s))[0]) for s in sample]))
+    # e2e: host state and controls in, host state out, every bench step
+    qp, qv = start_qpos.copy(), start_qvel.copy()
+    h2d = qp.nbytes + qv.nbytes + ctrl[0].nbytes
+    d2h = qp.nbytes + qv.nbytes
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.set_state(slots, qp, qv)
+        eng.set_qfrc(slots, ctrl[blk]); blk += 1
+        eng.step(S, STEP_BATCHED)
+        qp, qv = eng.get_state(slots, int(batch.nq.sum()), int(batch.nv.sum()))
+    eng.sync()
+    e2e = W * S * args.steps * ws / max_over_ranks(dist, time.perf_counter() - t0)
+    hbm, src = peaks()
+    n_launch = args.steps * S
+    dom = max(kernel_ms, key=kernel_ms.get)
+    dom_ms = kernel_ms[dom] / n_launch
+    alg = tc_kernel_bytes(dom, W, batch, contacts)
+    achieved = alg / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else None
+    tot_k = sum(kernel_ms.values())
+    avg_ms = total_ms / args.steps
+    out = {
+        "metric": "env-steps/s", "value": value, "unit": "env-steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": avg_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
+        "config": {"workload": "quadruped: floating torso + 4x3 revolute legs on a plane, Newton <= 20 iterations, "
+                               "dt 2e-3, tau ~ N(0,2) resampled every 20 steps",
+                   "worlds_per_gpu": W, "dof": int(batch.nv[0]), "env_steps_per_bench_step": S,
+                   "mode": "3 kernels per env-step (ABA, warp-per-world contact solve, integrate)",
+                   "l2": "flushed between timed steps (working set also exceeds L2)",
+                   "parallelism": f"replicas x{ws}", "contacts_per_world_end": contacts},
+        "e2e": {"value": e2e, "unit": "env-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm if achieved else None, "traffic": None, "peak_source": src,
+                     "algorithmic_bytes_per_launch": alg, "ms_per_launch": dom_ms,
+                     "note": "dense per-world Newton solves, latency-bound; timed live by event pairs on the "
+                             "launching stream"},
+        "kernels": {k: {"ms_per_launch": v / n_launch, "share": v / tot_k if tot_k else None,
+                        "algorithmic_bytes": tc_kernel_bytes(k, W, batch, contacts)} for k, v in kernel_ms.items()},
+        "status_flags": int(np.bitwise_or.reduce(st)) if len(st) else 0,
+    }
+    eng.close()
+    return out, (batch, start_qpos, start_qvel, ctrl[0])
+
+
+def cpu_baseline_quadruped(batch, qpos, qvel, qfrc, n_worlds=256, steps=40):
+    """The f32 restatement of newt's step (Newton tree-contact solve) on all
+    host cores, on a sample of the quadrupeds from the timed region's start."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+    from tooling_gb300 import scenes
+    cores = os.cpu_count() or 1
+    n = min(n_worlds, len(batch))
+    sub = scenes.quadruped_batch(n_worlds=n)
+    qp = qpos[: int(sub.nq.sum())]
+    qv = qvel[: int(sub.nv.sum())]
+    qf = qfrc[: int(sub.nv.sum())]
+    secs = oracle_py.time_run(sub, np.arange(n), qp, qv, qf, steps, cores)
+    return {"value": n * steps / secs, "unit": "env-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{n} quadruped worlds x {steps} env-steps from the bench's start state, f32 restatement of "
+                      f"newt's step (Newton tree-contact solve), {cores} host threads"}
+
+
 def cpu_baseline(batch, qpos, qvel, S, n_worlds=256, steps=500):
     """The f32 restatement of newt's step on the host cores: one world per
     thread, static partition, all cores; a sample of the worlds over the same
@@ -319,6 +451,15 @@ def main():
     if args.impl == "reference":
         out = run_reference(args, rank, ws, local, dist)
         if out is not None:
+            print(json.dumps(out))
+        return
+    if args.workload == "quadruped":
+        if args.worlds == 8192 and "--worlds" not in sys.argv:
+            args.worlds = 16384
+        out, (batch, qp, qv, qf) = run_gpu_quadruped(args, rank, ws, local, dist)
+        if rank == 0:
+            if not args.no_cpu and ws == 1:
+                out["cpu_baseline"] = cpu_baseline_quadruped(batch, qp, qv, qf)
             print(json.dumps(out))
         return
     out, (batch, qp, qv) = run_gpu(args, rank, ws, local, dist)

@@ -219,6 +219,15 @@ NEWT_API int64_t newt_gpu_launch_count(const newt_gpu_ctx* ctx);
 #define NEWT_PILE_ISLAND_CLASSES 7
 NEWT_API int newt_gpu_pile_profile(newt_gpu_ctx* ctx, int32_t enable, float* kernel_ms, int32_t* work);
 
+/* Profiling surface of the tree-contact step (quadruped worlds).  With
+ * timing on (newt_gpu_pile_profile's `enable`), every tree-contact env-step
+ * brackets its kernels with timing events on the context's stream; this
+ * returns, after waiting for the last newt_gpu_step call, each kernel's
+ * device time summed over that call: unconstrained ABA, contact solve,
+ * integration (NEWT_TC_KERNELS entries). */
+#define NEWT_TC_KERNELS 3
+NEWT_API int newt_gpu_tc_profile(newt_gpu_ctx* ctx, float* kernel_ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -29,7 +29,9 @@ EXPORTED = [
     "newt_gpu_set_qfrc", "newt_gpu_step", "newt_gpu_sync", "newt_gpu_world_status", "newt_gpu_get_qacc",
     "newt_gpu_get_contacts", "newt_gpu_get_impulses", "newt_gpu_event_record", "newt_gpu_event_elapsed_ms",
     "newt_gpu_flush_l2", "newt_gpu_launch_count", "newt_gpu_step_static", "newt_gpu_pile_profile",
+    "newt_gpu_tc_profile",
 ]
+TC_KERNELS = ["tree_aba_kernel", "tc_k_solve", "tree_integrate_kernel"]
 PILE_KERNELS = ["pile_k_collide", "pile_k_pgs_small<1>", "pile_k_pgs_small<2>", "pile_k_pgs_small<4>",
                 "pile_k_pgs_lane<4,4>", "pile_k_pgs_lane<5,4>", "pile_k_pgs_lane<33,32>", "pile_k_pgs_multi<0>",
                 "pile_k_integrate"]
@@ -81,6 +83,7 @@ def load_library(path: str = LIB_PATH):
         "newt_gpu_launch_count": ([P], C.c_int64),
         "newt_gpu_step_static": ([P, I32], C.c_int),
         "newt_gpu_pile_profile": ([P, I32, P, P], C.c_int),
+        "newt_gpu_tc_profile": ([P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -215,6 +218,13 @@ class Engine:
 
     def launch_count(self) -> int:
         return int(self.L.newt_gpu_launch_count(self.ctx))
+
+    def tc_profile(self) -> dict:
+        """Per-kernel ms of the last step call's tree-contact env-steps
+        (timing is switched on with pile_profile(1))."""
+        ms = np.zeros(len(TC_KERNELS), np.float32)
+        self._ck(self.L.newt_gpu_tc_profile(self.ctx, _p(ms)))
+        return dict(zip(TC_KERNELS, ms.tolist()))
 
     def pile_profile(self, enable: int = -1):
         """(per-kernel ms of the last step call, {islands, contacts, bodies} per

@@ -50,7 +50,7 @@
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
-constexpr int TC_WARPS = 2;  // warps (worlds) per block
+constexpr int TC_WARPS = 1;  // warps (worlds) per block
 constexpr int CREC = 24;     // floats per contact record
 // contact record fields
 enum { K_GA = 0, K_GB = 1, K_LINK = 2, K_SIGN = 3, K_POS = 4, K_N = 7, K_PEN = 10, K_GAP = 11, K_MU = 12,
@@ -110,7 +110,7 @@ NEWT_D float reference_accel(float position, float velocity, float tc, float dr,
 // ---------------------------------------------------------------------------
 struct TcLay {
   int L, nv, ng, maxc, ld;
-  int pose, jv, jw, iw, M, LM, LD, tw, con, jt, y, H, LH, LHd, imp, misc, words;
+  int jv, jw, iw, con, jt, H, LH, LHd, imp, misc, words;
 };
 NEWT_HD int up4(int n) { return (n + 3) / 4 * 4; }
 NEWT_HD TcLay tc_layout(int L, int nv, int ng, int maxc) {
@@ -118,28 +118,45 @@ NEWT_HD TcLay tc_layout(int L, int nv, int ng, int maxc) {
   t.L = L; t.nv = nv; t.ng = ng; t.maxc = maxc;
   t.ld = up4(4 * maxc);
   int f = 0;
-  t.pose = f; f += up4(7 * L);
   t.jv = f; f += up4(3 * nv * L);
   t.jw = f; f += up4(3 * nv * L);
-  t.iw = f; f += up4(6 * L);
-  t.M = f; f += up4(nv * nv);
-  t.LM = f; f += up4(nv * nv);
-  t.LD = f; f += up4(nv * nv);
-  t.tw = f; f += up4(L);
+  t.iw = f; f += up4(7 * L);  // world inertias (6 per link), then link masses
   t.con = f; f += up4(CREC * maxc);
-  t.jt = f; f += up4(nv * t.ld);
-  t.y = f; f += up4(nv * t.ld);
+  t.jt = f; f += up4(nv * t.ld);  // J^T, then Y in place, when the rows exceed the shared tile
   t.H = f; f += up4(t.ld * t.ld);
-  t.LH = f; f += up4(t.ld * t.ld);
-  t.LHd = f; f += up4(2 * t.ld * t.ld);  // doubles (offset is a multiple of 4 floats)
+  t.LH = f; f += up4(t.ld * t.ld);       // factor of H when it exceeds the shared tile
+  t.LHd = f; f += up4(2 * t.ld * t.ld);  // FP64 factor (offset is a multiple of 4 floats)
   t.imp = f; f += up4(t.ld);
   t.misc = f; f += 8;  // ncon, nrows, newton iterations
   t.words = (f + 31) / 32 * 32;
   return t;
 }
-// per-warp shared vectors (ld floats each) and row maps (ld ints each)
+// Per-world shared working set: solver vectors, row maps, link poses, the
+// two mass-matrix factors, link inverse weights, a tile that first holds the
+// link COM Jacobians and inertias and later the Newton factor, and the
+// Jacobian rows (overwritten in place by Y = L^-1 J^T).  The tile and the rows
+// live here when the active rows fit NRS (sequential Cholesky and
+// triangular-solve steps then wait on shared memory instead of L2).
 enum { V_X = 0, V_D, V_G, V_B, V_REG, V_DIAG, V_U, V_V, V_P, V_S, N_VEC };
-NEWT_HD int tc_smem_words(int ld) { return (N_VEC + 2) * ld; }
+constexpr int NRS = 48;
+struct TcSmem { int vl, ldr, nrs, vec, rmap, pose, lm, ldf, tw, lh, jy, words; };
+NEWT_HD TcSmem tc_smem(int L, int nv, int maxc) {
+  TcSmem m;
+  m.ldr = up4(4 * maxc);
+  m.vl = m.ldr > up4(nv) ? m.ldr : up4(nv);
+  m.nrs = m.ldr < NRS ? m.ldr : NRS;
+  int f = 0;
+  m.vec = f; f += N_VEC * m.vl;
+  m.rmap = f; f += 2 * m.ldr;
+  m.pose = f; f += up4(7 * L);
+  m.lm = f; f += up4(nv * nv);
+  m.ldf = f; f += up4(nv * nv);
+  m.tw = f; f += up4(L);
+  m.lh = f; f += m.nrs * m.nrs;
+  m.jy = f; f += up4(nv * m.nrs);
+  m.words = f;
+  return m;
+}
 
 // In-place lower Cholesky of the n x n column-major matrix A (leading
 // dimension ld).  Right-looking: column k is scaled, then the lanes update
@@ -195,6 +212,21 @@ NEWT_D void warp_llt_solve(const T* Lf, int n, int ld, float* v, int lane) {
   __syncwarp();
 }
 
+// Solves L^T z = rhs in place on the shared vector `v` (backward
+// substitution by row dot products of the column-major factor L).
+NEWT_D void warp_lt_solve(const float* Lf, int n, int ld, float* v, int lane) {
+  for (int k = n - 1; k >= 0; --k) {
+    __syncwarp();
+    float s = 0.f;
+    for (int m = k + 1 + lane; m < n; m += 32) s += Lf[(size_t)k * ld + m] * v[m];
+    s = warp_sum(s);
+    const float zk = (v[k] - s) / Lf[(size_t)k * ld + k];
+    __syncwarp();
+    if (lane == 0) v[k] = zk;
+  }
+  __syncwarp();
+}
+
 // out = H x (column-major H, lane per row; x shared).
 NEWT_D void warp_matvec(const float* H, int n, int ld, const float* x, float* out, int lane) {
   __syncwarp();
@@ -213,10 +245,6 @@ NEWT_D float warp_dot(const float* a, const float* b, int n, int lane) {
 
 }  // namespace
 
-
-// vector length of the per-warp shared vectors: rows and DoF both fit
-NEWT_HD int tc_vl(int nv, int maxc) { int ld = up4(4 * maxc), n = up4(nv); return ld > n ? ld : n; }
-NEWT_HD int tc_warp_words(int nv, int maxc) { return N_VEC * tc_vl(nv, maxc) + 2 * up4(4 * maxc); }
 
 namespace {
 
@@ -266,26 +294,45 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   if (w >= g.n || !g.live[w]) return;  // uniform per warp
   const int cap = g.cap, L = g.L, nv = g.nv;
   const TcLay lay = tc_layout(L, nv, G.ng, G.maxc);
-  const int ld = lay.ld, vl = tc_vl(nv, G.maxc);
+  const TcSmem sm = tc_smem(L, nv, G.maxc);
+  const int ld = lay.ld, vl = sm.vl;
   float* wf = G.scr + (size_t)w * G.sstride;
-  float* sv = tcs + (size_t)warp * tc_warp_words(nv, G.maxc);
+  float* sv = tcs + (size_t)warp * sm.words;
   float* vx = sv + V_X * vl; float* vd = sv + V_D * vl; float* vg = sv + V_G * vl; float* vb = sv + V_B * vl;
   float* vreg = sv + V_REG * vl; float* vdiag = sv + V_DIAG * vl; float* vu = sv + V_U * vl;
   float* vv = sv + V_V * vl; float* vp = sv + V_P * vl; float* vs = sv + V_S * vl;
-  int* rcon = reinterpret_cast<int*>(sv + N_VEC * vl);
-  int* rfac = rcon + ld;
+  int* rcon = reinterpret_cast<int*>(sv + sm.rmap);
+  int* rfac = rcon + sm.ldr;
   const float dt = g.dtg[w];
   uint32_t status = 0;
   const float* gm = G.geom;
   auto gv = [&](int gi, int f) { return gm[(size_t)(GREC * gi + f) * cap + w]; };
 
-  // ---- forward kinematics (tree.rs:771-858), lane 0 ----
-  float* pose = wf + lay.pose;
-  if (lane == 0) {
-    for (int i = 0; i < L; ++i) {
+  // ---- forward kinematics (tree.rs:771-858) ----
+  // Each lane loads one link's joint parameters; the chain is then walked in
+  // link order by every lane (parameters arrive by shuffle), lane 0 storing
+  // the poses.
+  float* pose = sv + sm.pose;
+  for (int base = 0; base < L; base += 32) {
+    const int li = base + lane;
+    float pj[3] = {0.f, 0.f, 0.f}, pc[3] = {0.f, 0.f, 0.f}, pa[3] = {0.f, 0.f, 0.f}, pq = 0.f;
+    if (li < L) {
+      for (int k = 0; k < 3; ++k) {
+        pj[k] = g.jp[(3 * li + k) * cap + w];
+        pc[k] = g.jc[(3 * li + k) * cap + w];
+        pa[k] = g.axis[(3 * li + k) * cap + w];
+      }
+      const int jt = g.topo[4 * li + 1], qo = g.topo[4 * li + 2];
+      if (jt == JH || jt == JS) pq = g.q[qo * cap + w];
+    }
+    const int nl = L - base < 32 ? L - base : 32;
+    for (int k = 0; k < nl; ++k) {
+      const int i = base + k;
+      const V3 jp = v3(__shfl_sync(FULL, pj[0], k), __shfl_sync(FULL, pj[1], k), __shfl_sync(FULL, pj[2], k));
+      const V3 jc = v3(__shfl_sync(FULL, pc[0], k), __shfl_sync(FULL, pc[1], k), __shfl_sync(FULL, pc[2], k));
+      const V3 ax = v3(__shfl_sync(FULL, pa[0], k), __shfl_sync(FULL, pa[1], k), __shfl_sync(FULL, pa[2], k));
+      const float qa = __shfl_sync(FULL, pq, k);
       const int parent = g.topo[4 * i], jt = g.topo[4 * i + 1], qo = g.topo[4 * i + 2];
-      const V3 jp = v3(g.jp[(3 * i) * cap + w], g.jp[(3 * i + 1) * cap + w], g.jp[(3 * i + 2) * cap + w]);
-      const V3 jc = v3(g.jc[(3 * i) * cap + w], g.jc[(3 * i + 1) * cap + w], g.jc[(3 * i + 2) * cap + w]);
       V3 p;
       Q4 o;
       if (i == 0) {
@@ -297,38 +344,48 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
           p = jp - qrot(o, jc);
         }
       } else {
+        __syncwarp();
         const float* pp = pose + 7 * parent;
         const Q4 po = Q4{pp[3], pp[4], pp[5], pp[6]};
         const V3 jpw = ldv3(pp) + qrot(po, jp);
-        const V3 ax = v3(g.axis[(3 * i) * cap + w], g.axis[(3 * i + 1) * cap + w], g.axis[(3 * i + 2) * cap + w]);
         if (jt == JH) {
-          o = qmul(po, q_axis_angle(ax, g.q[qo * cap + w]));
+          o = qmul(po, q_axis_angle(ax, qa));
           p = jpw - qrot(o, jc);
         } else if (jt == JS) {
           o = po;
-          p = jpw + qrot(po, ax * g.q[qo * cap + w]) - qrot(o, jc);
+          p = jpw + qrot(po, ax * qa) - qrot(o, jc);
         } else {
           o = po;
           p = jpw - qrot(o, jc);
         }
       }
-      float* d = pose + 7 * i;
-      stv3(d, p);
-      d[3] = o.x; d[4] = o.y; d[5] = o.z; d[6] = o.w;
+      __syncwarp();
+      if (lane == 0) {
+        float* d = pose + 7 * i;
+        stv3(d, p);
+        d[3] = o.x; d[4] = o.y; d[5] = o.z; d[6] = o.w;
+      }
     }
   }
   __syncwarp();
 
-  // ---- link-plane contacts in newt's pair order, lane 0 ----
+  // ---- link-plane contacts in newt's pair order: lane per pair, a warp scan
+  //      places each pair's contacts ----
   float* con = wf + lay.con;
-  if (lane == 0) {
-    int ncon = 0;
-    bool overflow = false;
-    for (int pi = 0; pi < G.npairs && !overflow; ++pi) {
-      const int a = G.pairs[2 * pi], b = G.pairs[2 * pi + 1];
-      const bool a_static = G.gtopo[2 * a + 1] < 0;
+  int ncon = 0;
+  bool overflow = false;
+  for (int base = 0; base < G.npairs; base += 32) {
+    const int pi = base + lane;
+    CRes cr[4];
+    int nc = 0, a = 0, b = 0, link = 0;
+    bool a_static = false;
+    if (pi < G.npairs) {
+      a = G.pairs[2 * pi];
+      b = G.pairs[2 * pi + 1];
+      a_static = G.gtopo[2 * a + 1] < 0;
       const int gl = a_static ? b : a, gp = a_static ? a : b;  // link geom, plane
-      const int link = G.gtopo[2 * gl + 1], shape = G.gtopo[2 * gl];
+      link = G.gtopo[2 * gl + 1];
+      const int shape = G.gtopo[2 * gl];
       const float* lp = pose + 7 * link;
       const Q4 lo = Q4{lp[3], lp[4], lp[5], lp[6]};
       GPose gpose, ppose;
@@ -337,8 +394,6 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
       ppose.p = v3(gv(gp, G_POS), gv(gp, G_POS + 1), gv(gp, G_POS + 2));
       ppose.q = Q4{gv(gp, G_QUAT), gv(gp, G_QUAT + 1), gv(gp, G_QUAT + 2), gv(gp, G_QUAT + 3)};
       const float margin = fmaxf(gv(a, G_MARGIN), gv(b, G_MARGIN));
-      CRes cr[4];
-      int nc = 0;
       if (shape == NEWT_SHAPE_SPHERE) {
         nc = np_sphere_plane(gpose, gv(gl, G_SIZE), margin, ppose, cr);
       } else if (shape == NEWT_SHAPE_BOX) {
@@ -353,59 +408,84 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
           if (raw <= margin) cr[nc++] = CRes{e - n * (r + raw * 0.5f), n, margin - raw};
         }
       }
-      for (int k = 0; k < nc; ++k) {
-        if (ncon >= G.maxc) { overflow = true; break; }
-        float* c = con + CREC * ncon;
-        // the narrowphase ran as (geom, plane); a pair listed as (plane, geom)
-        // is relabelled with the normal flipped (contact.rs:2509-2587)
-        c[K_GA] = __int_as_float(a);
-        c[K_GB] = __int_as_float(b);
-        c[K_LINK] = __int_as_float(link);
-        c[K_SIGN] = a_static ? -1.f : 1.f;
-        stv3(c + K_POS, cr[k].pos);
-        stv3(c + K_N, a_static ? -cr[k].n : cr[k].n);
-        c[K_PEN] = cr[k].pen;
-        c[K_GAP] = fmaxf(gv(a, G_GAP), gv(b, G_GAP));
-        c[K_MU] = fminf(gv(a, G_FRIC), gv(b, G_FRIC));
-        // combine_solref (geom.rs:156-185), combine_solimp (solver.rs:242)
-        const float ta = gv(a, G_SR), tb = gv(b, G_SR), da = gv(a, G_SR + 1), db = gv(b, G_SR + 1);
-        const bool dira = ta < 0.f, dirb = tb < 0.f;
-        c[K_SR] = dira != dirb ? (dira ? ta : tb) : fminf(ta, tb);
-        c[K_SR + 1] = dira != dirb ? (dira ? da : db) : fminf(da, db);
-        for (int q = 0; q < 3; ++q) c[K_SI + q] = fminf(gv(a, G_SI + q), gv(b, G_SI + q));
-        c[K_SI + 3] = gv(a, G_SI + 3);
-        c[K_SI + 4] = gv(a, G_SI + 4);
-        c[K_CONDIM] = (float)min(G.gtopo[2 * G.ng + a], G.gtopo[2 * G.ng + b]);
-        ++ncon;
-      }
     }
-    if (overflow) status |= NEWT_WS_CONTACT_OVERFLOW;
-    // rows of the active contacts, in contact order (solver.rs:2881-2890)
-    int nr = 0;
-    for (int c = 0; c < ncon; ++c) {
-      float* cc = con + CREC * c;
-      const bool act = cc[K_PEN] - cc[K_GAP] > 0.f;
-      const int k = (int)cc[K_CONDIM] == 3 ? 4 : 1;
-      cc[K_ROW] = __int_as_float(act ? nr : -1);
-      if (!act) continue;
-      for (int f = 0; f < k; ++f) { rcon[nr + f] = c; rfac[nr + f] = k == 4 ? f : -1; }
-      nr += k;
+    int incl = nc;  // inclusive scan of the per-pair counts
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += t;
     }
+    const int total = __shfl_sync(FULL, incl, 31);
+    const int off = ncon + incl - nc;
+    for (int k = 0; k < nc; ++k) {
+      if (off + k >= G.maxc) { overflow = true; break; }
+      float* c = con + CREC * (off + k);
+      // the narrowphase ran as (geom, plane); a pair listed as (plane, geom)
+      // is relabelled with the normal flipped (contact.rs:2509-2587)
+      c[K_GA] = __int_as_float(a);
+      c[K_GB] = __int_as_float(b);
+      c[K_LINK] = __int_as_float(link);
+      c[K_SIGN] = a_static ? -1.f : 1.f;
+      stv3(c + K_POS, cr[k].pos);
+      stv3(c + K_N, a_static ? -cr[k].n : cr[k].n);
+      c[K_PEN] = cr[k].pen;
+      c[K_GAP] = fmaxf(gv(a, G_GAP), gv(b, G_GAP));
+      c[K_MU] = fminf(gv(a, G_FRIC), gv(b, G_FRIC));
+      // combine_solref (geom.rs:156-185), combine_solimp (solver.rs:242)
+      const float ta = gv(a, G_SR), tb = gv(b, G_SR), da = gv(a, G_SR + 1), db = gv(b, G_SR + 1);
+      const bool dira = ta < 0.f, dirb = tb < 0.f;
+      c[K_SR] = dira != dirb ? (dira ? ta : tb) : fminf(ta, tb);
+      c[K_SR + 1] = dira != dirb ? (dira ? da : db) : fminf(da, db);
+      for (int q = 0; q < 3; ++q) c[K_SI + q] = fminf(gv(a, G_SI + q), gv(b, G_SI + q));
+      c[K_SI + 3] = gv(a, G_SI + 3);
+      c[K_SI + 4] = gv(a, G_SI + 4);
+      c[K_CONDIM] = (float)min(G.gtopo[2 * G.ng + a], G.gtopo[2 * G.ng + b]);
+    }
+    ncon = ncon + total < G.maxc ? ncon + total : G.maxc;
+  }
+  if (__any_sync(FULL, overflow)) status |= NEWT_WS_CONTACT_OVERFLOW;
+  __syncwarp();
+  // rows of the active contacts, in contact order (solver.rs:2881-2890):
+  // lane per contact, a warp scan assigns the row ranges
+  int nrows = 0;
+  for (int base = 0; base < ncon; base += 32) {
+    const int c = base + lane;
+    int k = 0;
+    if (c < ncon) {
+      const float* cc = con + CREC * c;
+      if (cc[K_PEN] - cc[K_GAP] > 0.f) k = (int)cc[K_CONDIM] == 3 ? 4 : 1;
+    }
+    int incl = k;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const int start = nrows + incl - k;
+    if (c < ncon) {
+      con[CREC * c + K_ROW] = __int_as_float(k > 0 ? start : -1);
+      for (int f = 0; f < k; ++f) { rcon[start + f] = c; rfac[start + f] = k == 4 ? f : -1; }
+    }
+    nrows += __shfl_sync(FULL, incl, 31);
+  }
+  if (lane == 0) {
     wf[lay.misc] = __int_as_float(ncon);
-    wf[lay.misc + 1] = __int_as_float(nr);
+    wf[lay.misc + 1] = __int_as_float(nrows);
     wf[lay.misc + 2] = __int_as_float(0);
   }
-  __syncwarp();
-  const int nr = __float_as_int(wf[lay.misc + 1]);
+  const int nr = nrows;
   if (nr == 0) {  // no active contact: qacc stays a_free
     if (lane == 0 && status) atomicOr(g.status + w, status);
     return;
   }
 
-  // ---- link COM Jacobians and world inertias, lane per link ----
+  // ---- link COM Jacobians, world inertias and masses, lane per link ----
+  const bool jac_shared = 6 * nv * L + 7 * L <= sm.nrs * sm.nrs;
+  float* JV = jac_shared ? sv + sm.lh : wf + lay.jv;
+  float* JW = jac_shared ? JV + 3 * nv * L : wf + lay.jw;
+  float* IW = jac_shared ? JW + 3 * nv * L : wf + lay.iw;  // 6 per link, then the link masses
+  float* MS = IW + 6 * L;
   for (int l = lane; l < L; l += 32) {
-    float* jv = wf + lay.jv + 3 * nv * l;
-    float* jw = wf + lay.jw + 3 * nv * l;
+    float* jv = JV + 3 * nv * l;
+    float* jw = JW + 3 * nv * l;
     for (int k = 0; k < 3 * nv; ++k) { jv[k] = 0.f; jw[k] = 0.f; }
     const float* pl = pose + 7 * l;
     chain_columns(g, w, pose, l, ldv3(pl), [&](int k, V3 rot, V3 tr) { stv3(jw + 3 * k, rot); stv3(jv + 3 * k, tr); });
@@ -415,34 +495,31 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
     const S3 Ib{g.inert[(6 * l) * cap + w], g.inert[(6 * l + 1) * cap + w], g.inert[(6 * l + 2) * cap + w],
                 g.inert[(6 * l + 3) * cap + w], g.inert[(6 * l + 4) * cap + w], g.inert[(6 * l + 5) * cap + w]};
     const S3 Iw = sym_congr(RT, Ib);  // R I R^T
-    float* iw = wf + lay.iw + 6 * l;
+    float* iw = IW + 6 * l;
     iw[0] = Iw.xx; iw[1] = Iw.yy; iw[2] = Iw.zz; iw[3] = Iw.xy; iw[4] = Iw.xz; iw[5] = Iw.yz;
+    MS[l] = g.mass[l * cap + w];
   }
   __syncwarp();
 
   // ---- mass matrix (lower triangle, column-major), lane per entry ----
-  float* Mm = wf + lay.M;
-  {
-    int e = 0;
-    for (int j = 0; j < nv; ++j)
-      for (int i = j; i < nv; ++i, ++e) {
-        if ((e & 31) != lane) continue;
-        float s = 0.f;
-        for (int l = 0; l < L; ++l) {
-          const float* jv = wf + lay.jv + 3 * nv * l;
-          const float* jw = wf + lay.jw + 3 * nv * l;
-          const float* iw = wf + lay.iw + 6 * l;
-          const S3 I{iw[0], iw[1], iw[2], iw[3], iw[4], iw[5]};
-          s += g.mass[l * cap + w] * dot(ldv3(jv + 3 * i), ldv3(jv + 3 * j)) + dot(ldv3(jw + 3 * i), smv(I, ldv3(jw + 3 * j)));
-        }
-        Mm[j * nv + i] = s;
-      }
+  float* LM = sv + sm.lm;   // factor of M + dt B (response, qacc)
+  float* LD = sv + sm.ldf;  // factor of M (diagApprox)
+  for (int e = lane; e < nv * nv; e += 32) {
+    const int i = e % nv, j = e / nv;
+    if (i < j) continue;
+    float s = 0.f;
+    for (int l = 0; l < L; ++l) {
+      const float* jv = JV + 3 * nv * l;
+      const float* jw = JW + 3 * nv * l;
+      const float* iw = IW + 6 * l;
+      const S3 I{iw[0], iw[1], iw[2], iw[3], iw[4], iw[5]};
+      s += MS[l] * dot(ldv3(jv + 3 * i), ldv3(jv + 3 * j)) + dot(ldv3(jw + 3 * i), smv(I, ldv3(jw + 3 * j)));
+    }
+    LD[j * nv + i] = s;
   }
   __syncwarp();
   // armature (diagonal, child joints) and the implicit damping dt*B (tree.rs:645-684)
-  float* LM = wf + lay.LM;
-  float* LD = wf + lay.LD;
-  for (int k = lane; k < nv * nv; k += 32) { LM[k] = Mm[k]; LD[k] = Mm[k]; }
+  for (int k = lane; k < nv * nv; k += 32) LM[k] = LD[k];
   __syncwarp();
   if (lane == 0) {
     for (int i = 0; i < L; ++i) {
@@ -465,10 +542,16 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   }
 
   // ---- Jacobian rows of the cone facets, velocities, lane per row ----
-  float* Jt = wf + lay.jt;
+  const bool rows_shared = nr <= sm.nrs;
+  float* Jt = rows_shared ? sv + sm.jy : wf + lay.jt;  // J^T, column-major; becomes Y
+  const int ldj = rows_shared ? sm.nrs : ld;
+  float* tw = sv + sm.tw;  // 1 marks a link that owns rows; then its inverse weight
+  for (int l = lane; l < L; l += 32) tw[l] = 0.f;
+  __syncwarp();
   for (int r = lane; r < nr; r += 32) {
     const float* cc = con + CREC * rcon[r];
     const int link = __float_as_int(cc[K_LINK]);
+    tw[link] = 1.f;
     const float sign = cc[K_SIGN], mu = cc[K_MU];
     const V3 n = ldv3(cc + K_N), pt = ldv3(cc + K_POS);
     V3 dir = n;
@@ -480,11 +563,11 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
       const V3 t = f < 2 ? t1 : cross(n, t1);
       dir = n + t * ((f & 1) ? -mu : mu);
     }
-    for (int k = 0; k < nv; ++k) Jt[(size_t)k * ld + r] = 0.f;
-    chain_columns(g, w, pose, link, pt, [&](int k, V3, V3 tr) { Jt[(size_t)k * ld + r] = dot(tr, dir) * sign; });
+    for (int k = 0; k < nv; ++k) Jt[(size_t)k * ldj + r] = 0.f;
+    chain_columns(g, w, pose, link, pt, [&](int k, V3, V3 tr) { Jt[(size_t)k * ldj + r] = dot(tr, dir) * sign; });
     float vel = 0.f, vfree = 0.f;
     for (int k = 0; k < nv; ++k) {
-      const float jk = Jt[(size_t)k * ld + r];
+      const float jk = Jt[(size_t)k * ldj + r];
       vel += jk * g.qd[k * cap + w];
       vfree += jk * g.qacc[k * cap + w];
     }
@@ -494,25 +577,28 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   __syncwarp();
 
   // ---- Y = L^-1 J^T and A = Y^T Y (solver.rs:3043-3066), lane per row ----
-  float* Y = wf + lay.y;
+  float* Y = Jt;  // forward substitution in place, one row per lane
   float* H = wf + lay.H;
   for (int r = lane; r < nr; r += 32) {
+    float y[NEWT_MAX_LINKS + 5];
     for (int k = 0; k < nv; ++k) {
-      float s = Jt[(size_t)k * ld + r];
-      for (int m = 0; m < k; ++m) s -= LM[m * nv + k] * Y[(size_t)m * ld + r];
-      Y[(size_t)k * ld + r] = s / LM[k * nv + k];
+      float s = Jt[(size_t)k * ldj + r];
+      for (int m = 0; m < k; ++m) s -= LM[m * nv + k] * y[m];
+      y[k] = s / LM[k * nv + k];
+      Y[(size_t)k * ldj + r] = y[k];
     }
   }
   __syncwarp();
   for (int r = lane; r < nr; r += 32)
     for (int c = 0; c < nr; ++c) {
       float s = 0.f;
-      for (int k = 0; k < nv; ++k) s += Y[(size_t)k * ld + r] * Y[(size_t)k * ld + c];
+      for (int k = 0; k < nv; ++k) s += Y[(size_t)k * ldj + r] * Y[(size_t)k * ldj + c];
       H[(size_t)c * ld + r] = s;
     }
   // ---- mean inverse weight of each link's COM (tree_body_invweight0), lane per link ----
   for (int l = lane; l < L; l += 32) {
-    const float* jv = wf + lay.jv + 3 * nv * l;
+    if (tw[l] == 0.f) continue;  // no rows on this link
+    const float* jv = JV + 3 * nv * l;
     float tr = 0.f;
     for (int axis = 0; axis < 3; ++axis) {
       // |L_D^-1 jv_axis|^2 = jv_axis^T M^-1 jv_axis (forward substitution only)
@@ -526,7 +612,7 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
       }
       tr += s2;
     }
-    wf[lay.tw + l] = tr / 3.f;
+    tw[l] = tr / 3.f;
   }
   __syncwarp();
 
@@ -537,8 +623,8 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
     const Soft s{cc[K_SR], cc[K_SR + 1], cc[K_SI], cc[K_SI + 1], cc[K_SI + 2], cc[K_SI + 3], (int)cc[K_SI + 4]};
     const float d = impedance_at(-pen, s);
     const bool pyr = rfac[r] >= 0;
-    const float tw = wf[lay.tw + __float_as_int(cc[K_LINK])];
-    const float base = (1.f - d) / d * (pyr ? tw * (1.f + mu * mu) : tw);
+    const float twl = tw[__float_as_int(cc[K_LINK])];
+    const float base = (1.f - d) / d * (pyr ? twl * (1.f + mu * mu) : twl);
     const float reg = pyr ? 2.f * mu * mu * base : base;
     vreg[r] = reg;
     vdiag[r] = H[(size_t)r * ld + r] + reg;
@@ -569,16 +655,19 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
     // ---- Newton (newton.rs:275-339) on H = A + diag(R) ----
     for (int r = lane; r < nr; r += 32) H[(size_t)r * ld + r] += vreg[r];
     __syncwarp();
-    float* LH = wf + lay.LH;
+    // the factor lives in the shared tile when the rows fit, else in HBM
+    const bool lh_shared = nr <= sm.nrs;
+    float* LH = lh_shared ? sv + sm.lh : wf + lay.LH;
+    const int ldh = lh_shared ? sm.nrs : ld;
     double* LHd = reinterpret_cast<double*>(wf + lay.LHd);
     auto copy_h = [&]() {
       __syncwarp();
       for (int c = 0; c < nr; ++c)
-        for (int r = lane; r < nr; r += 32) LH[(size_t)c * ld + r] = H[(size_t)c * ld + r];
+        for (int r = lane; r < nr; r += 32) LH[(size_t)c * ldh + r] = H[(size_t)c * ld + r];
       __syncwarp();
     };
     copy_h();
-    bool ok = warp_cholesky(LH, nr, ld, lane, &mn, &mx);
+    bool ok = warp_cholesky(LH, nr, ldh, lane, &mn, &mx);
     if (!ok) {
       // zero-friction facets duplicate rows: a solver-only pivot (solver.rs:3215-3232)
       bool zero_mu = false;
@@ -592,7 +681,7 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
         __syncwarp();
         for (int r = lane; r < nr; r += 32) H[(size_t)r * ld + r] += piv;
         copy_h();
-        ok = warp_cholesky(LH, nr, ld, lane, &mn, &mx);
+        ok = warp_cholesky(LH, nr, ldh, lane, &mn, &mx);
       }
     }
     bool use64 = !ok || (mx / mn) * (mx / mn) > 1.0e6f;
@@ -616,7 +705,7 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
         for (int r = lane; r < nr; r += 32) { vg[r] += vb[r]; vd[r] = -vg[r]; }
         __syncwarp();
         if (use64) warp_llt_solve(LHd, nr, ld, vd, lane);
-        else warp_llt_solve(LH, nr, ld, vd, lane);
+        else warp_llt_solve(LH, nr, ldh, vd, lane);
         if (warp_dot(vg, vd, nr, lane) >= 0.f) break;
         // ---- exact line search over the projected path (newton.rs:435-556) ----
         for (int r = lane; r < nr; r += 32) {
@@ -630,10 +719,11 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
         warp_matvec(H, nr, ld, vp, vu, lane);
         warp_matvec(H, nr, ld, vs, vv, lane);
         float best_a = 0.f, best_c = cur, lo = 0.f;
+        // cost on a window: c0 + c1 a + c2 a^2 / 2 with p = P + a S; the five
+        // products are updated in O(1) when a coordinate leaves the free set
+        float Pu = warp_dot(vp, vu, nr, lane), Pv = warp_dot(vp, vv, nr, lane);
+        float Sv = warp_dot(vs, vv, nr, lane), bP = warp_dot(vb, vp, nr, lane), bS = warp_dot(vb, vs, nr, lane);
         for (int guard = 0; guard <= nr; ++guard) {
-          // cost on the window: c0 + c1 a + c2 a^2 / 2 with p = P + a S
-          const float Pu = warp_dot(vp, vu, nr, lane), Pv = warp_dot(vp, vv, nr, lane);
-          const float Sv = warp_dot(vs, vv, nr, lane), bP = warp_dot(vb, vp, nr, lane), bS = warp_dot(vb, vs, nr, lane);
           // next breakpoint (warp argmin)
           float bm = 2.f;
           int bi = -1;
@@ -656,7 +746,13 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
           }
           if (bi < 0) break;
           // coordinate bi leaves the free set: P, S lose it, H P and H S a column
-          const float xj = vp[bi], dj = vs[bi];
+          const float xj = vp[bi], dj = vs[bi], uj = vu[bi], vj = vv[bi], bj = vb[bi];
+          const float hjj = H[(size_t)bi * ld + bi];
+          Pu += (xj * hjj - 2.f * uj) * xj;
+          Pv += xj * dj * hjj - xj * vj - dj * uj;
+          Sv += (dj * hjj - 2.f * vj) * dj;
+          bP -= bj * xj;
+          bS -= bj * dj;
           __syncwarp();
           for (int r = lane; r < nr; r += 32) {
             const float hc = H[(size_t)bi * ld + r];
@@ -682,14 +778,15 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   __syncwarp();
 
   // ---- outputs: impulses, J^T f / dt, qacc = a_free + (M + dt B)^-1 J^T f / dt ----
+  // J^T = L Y, so (L L^T)^-1 J^T f / dt = L^-T (Y f) / dt: one back substitution
   for (int r = lane; r < nr; r += 32) wf[lay.imp + r] = vx[r];
   for (int k = lane; k < nv; k += 32) {
     float s = 0.f;
-    for (int r = 0; r < nr; ++r) s += Jt[(size_t)k * ld + r] * vx[r];
+    for (int r = 0; r < nr; ++r) s += Y[(size_t)k * ldj + r] * vx[r];
     vg[k] = s / dt;
   }
   __syncwarp();
-  warp_llt_solve(LM, nv, nv, vg, lane);
+  warp_lt_solve(LM, nv, nv, vg, lane);
   for (int k = lane; k < nv; k += 32) g.qacc[k * cap + w] += vg[k];
   if (lane == 0) {
     wf[lay.misc + 2] = __int_as_float(done_it);
@@ -703,18 +800,18 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
 extern "C" size_t newt_tc_ws_bytes(int L, int nv, int ng, int maxc) {
   return (size_t)tc_layout(L, nv, ng, maxc).words * sizeof(float);
 }
-extern "C" size_t newt_tc_smem_bytes(int nv, int maxc) {
-  return (size_t)TC_WARPS * tc_warp_words(nv, maxc) * sizeof(float);
+extern "C" size_t newt_tc_smem_bytes(int L, int nv, int maxc) {
+  return (size_t)TC_WARPS * tc_smem(L, nv, maxc).words * sizeof(float);
 }
 // Kernel attribute for the dynamic shared memory (outside stream capture).
-extern "C" cudaError_t newt_tc_init(int nv, int maxc) {
+extern "C" cudaError_t newt_tc_init(int L, int nv, int maxc) {
   return cudaFuncSetAttribute(tc_k_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)newt_tc_smem_bytes(nv, maxc));
+                              (int)newt_tc_smem_bytes(L, nv, maxc));
 }
 extern "C" void newt_launch_tc_solve(const TcGroupDev& G, cudaStream_t st) {
   const int grid = (G.t.n + TC_WARPS - 1) / TC_WARPS;
   if (grid == 0) return;
-  tc_k_solve<<<grid, 32 * TC_WARPS, newt_tc_smem_bytes(G.t.nv, G.maxc), st>>>(G);
+  tc_k_solve<<<grid, 32 * TC_WARPS, newt_tc_smem_bytes(G.t.L, G.t.nv, G.maxc), st>>>(G);
 }
 extern "C" void newt_tc_offsets(int L, int nv, int ng, int maxc, int* con, int* imp, int* misc) {
   const TcLay t = tc_layout(L, nv, ng, maxc);
@@ -748,13 +845,29 @@ extern "C" int newt_tc_step(newt_gpu_ctx* ctx, HostGroup* g, int n_steps, int fu
     g->plain_scratch_bytes = need;
   }
   g->scr_stride = (long)(per / sizeof(float));
-  CKT(newt_tc_init(g->nv, g->maxc));
+  CKT(newt_tc_init(g->size, g->nv, g->maxc));
   const TcGroupDev d = g->tc_dev();
+  const bool timed = ctx->profile;
+  if (timed) {
+    while (ctx->tcev.size() < (size_t)6 * n_steps) {
+      cudaEvent_t e;
+      CKT(cudaEventCreate(&e));
+      ctx->tcev.push_back(e);
+    }
+  }
+  auto mark = [&](int s, int k) { if (timed) cudaEventRecord(ctx->tcev[(size_t)6 * s + k], ctx->stream); };
   for (int s = 0; s < n_steps; ++s) {
+    mark(s, 0);
     newt_launch_tree_aba(d.t, ctx->stream);
+    mark(s, 1);
+    mark(s, 2);
     newt_launch_tc_solve(d, ctx->stream);
+    mark(s, 3);
+    mark(s, 4);
     newt_launch_tree_integrate(d.t, ctx->stream);
+    mark(s, 5);
     ctx->launches += 3;
   }
+  ctx->tcev_steps = timed ? n_steps : 0;
   return NEWT_OK;
 }

@@ -197,6 +197,7 @@ int newt_gpu_destroy(newt_gpu_ctx* ctx) {
   for (int k = 0; k < 3; ++k) if (ctx->pside[k]) cudaStreamDestroy(ctx->pside[k]);
   for (int k = 0; k < 4; ++k) if (ctx->pev[k]) cudaEventDestroy(ctx->pev[k]);
   for (cudaEvent_t e : ctx->kev) cudaEventDestroy(e);
+  for (cudaEvent_t e : ctx->tcev) cudaEventDestroy(e);
   cudaEventDestroy(ctx->ev[0]);
   cudaEventDestroy(ctx->ev[1]);
   cudaStreamDestroy(ctx->stream);
@@ -431,6 +432,21 @@ int newt_gpu_flush_l2(newt_gpu_ctx* ctx) {
 }
 
 int64_t newt_gpu_launch_count(const newt_gpu_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+int newt_gpu_tc_profile(newt_gpu_ctx* ctx, float* kernel_ms) {
+  if (!ctx || !kernel_ms) return NEWT_E_INVALID;
+  cudaSetDevice(ctx->device);
+  int rc = newt_gpu_sync(ctx, 600000);
+  if (rc != NEWT_OK) return rc;
+  for (int k = 0; k < NEWT_TC_KERNELS; ++k) kernel_ms[k] = 0.f;
+  for (int s = 0; s < ctx->tcev_steps; ++s)
+    for (int k = 0; k < NEWT_TC_KERNELS; ++k) {
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, ctx->tcev[(size_t)6 * s + 2 * k], ctx->tcev[(size_t)6 * s + 2 * k + 1]));
+      kernel_ms[k] += ms;
+    }
+  return NEWT_OK;
+}
 
 int newt_gpu_pile_profile(newt_gpu_ctx* ctx, int32_t enable, float* kernel_ms, int32_t* work) {
   if (!ctx) return NEWT_E_INVALID;

@@ -150,6 +150,10 @@ struct newt_gpu_ctx {
   std::vector<std::pair<int*, int>> last_lists;
   std::vector<std::pair<int*, int>> graph_lists;  // the captured graph's, copied to last_lists per replay
   int graph_kev_steps = 0;
+  // tree-contact step timing: 3 kernels x (start, end) per env-step of the
+  // last tree-contact step call, recorded when `profile` is on
+  std::vector<cudaEvent_t> tcev;
+  int tcev_steps = 0;
 };
 
 HostGroup* find_or_make_group(newt_gpu_ctx* ctx, const HostModel& m);

@@ -292,10 +292,11 @@ def quadruped_batch(n_worlds: int = 16384, seed_index: int = 2, dt: float = 2e-3
 
 def quadruped_controls(n_worlds: int, block: int, seed_index: int = 2, first_world: int = 0) -> np.ndarray:
     """Joint torques tau ~ N(0, 2) for the 12 actuated DoF of every world,
-    for control block `block` (the controls are resampled every 20 steps);
-    MuJoCo qvel order (6 free-root entries of zero first)."""
+    for control block `block` (controls are resampled every 20 steps);
+    MuJoCo qvel order, the 6 free-root entries zero.  One generator per
+    (workload, block, first world) draws the whole block."""
     cs = config_seed(seed_index)
+    rng = np.random.default_rng([cs, block, first_world])
     out = np.zeros((n_worlds, 18), np.float32)
-    for i, w in enumerate(range(first_world, first_world + n_worlds)):
-        out[i, 6:] = world_rng(cs ^ (0x9E3779B9 * (block + 1)), w).normal(0.0, 2.0, 12)
+    out[:, 6:] = rng.normal(0.0, 2.0, (n_worlds, 12))
     return out.reshape(-1)
