@@ -43,8 +43,9 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--plain", action="store_true", help="also time the plain (per-stage launch) form")
-    ap.add_argument("--workload", default="pile", choices=["pile", "quadruped"],
-                    help="pile: 16 free bodies on a plane (default); quadruped: Newton tree contact")
+    ap.add_argument("--workload", default="pile", choices=["pile", "quadruped", "uneven"],
+                    help="pile: 16 free bodies on a plane (default); quadruped: Newton tree contact; "
+                         "uneven: chains and piles of 2..64 bodies, batched vs plain")
     return ap.parse_args()
 
 
@@ -372,6 +373,110 @@ def run_gpu_quadruped(args, rank, ws, local, dist):
     return out, (batch, start_qpos, start_qvel, ctrl[0])
 
 
+def run_gpu_uneven(args, rank, ws, local, dist):
+    """Uneven batch: chains and piles with 2..64 bodies (log-uniform), PGS 50,
+    dt 2e-3.  The batched form (tree persistent kernels per size bucket plus
+    one pile table over every size, captured in a CUDA graph) is timed beside
+    the plain form (one launch per stage per size group) on the same worlds
+    from the same start state."""
+    from tooling_gb300 import build as B
+    B.build()
+    from tooling_gb300 import scenes
+    batch = scenes.uneven_batch(n_worlds=args.worlds, first_world=rank * args.worlds)  # before the first GPU call
+    from tooling_gb300 import Engine, STEP_BATCHED, STEP_PLAIN
+    eng = Engine(device=local)
+    W = args.worlds
+    slots = eng.alloc(eng.upload(batch))
+    eng.set_state(slots, batch.qpos, batch.qvel)
+    eng.set_qfrc(slots, batch.qfrc)
+    S = args.substeps
+    eng.pile_profile(1)
+    for _ in range(max(3, args.warmup)):
+        eng.step(S, STEP_BATCHED)
+    eng.sync()
+    nq, nv = int(batch.nq.sum()), int(batch.nv.sum())
+    start_qpos, start_qvel = eng.get_state(slots, nq, nv)
+    launches0 = eng.launch_count()
+    clocks = Clocks(local)
+    clocks.start()
+    per_step, kernel_ms, work = [], {}, None
+    barrier(dist)
+    eng.sync()
+    for _ in range(args.steps):
+        eng.flush_l2()
+        eng.event(0)
+        eng.step(S, STEP_BATCHED)
+        eng.event(1)
+        per_step.append(eng.elapsed_ms())
+        kms, work = eng.pile_profile()
+        for k, v in kms.items():
+            kernel_ms[k] = kernel_ms.get(k, 0.0) + v
+    eng.sync()
+    barrier(dist)
+    clk = clocks.stop()
+    launches = eng.launch_count() - launches0
+    total_ms = max_over_ranks(dist, float(sum(per_step)))
+    value = W * S * args.steps * ws / (total_ms / 1e3)
+    st = eng.status(slots)
+    # plain form, same worlds, same start state
+    eng.set_state(slots, start_qpos, start_qvel)
+    eng.step(1, STEP_PLAIN)  # builds the per-group tables (allocation outside the timed region)
+    eng.set_state(slots, start_qpos, start_qvel)
+    eng.sync()
+    plain_launch0 = eng.launch_count()
+    pms = 0.0
+    for _ in range(args.steps):
+        eng.flush_l2()
+        eng.event(0)
+        eng.step(S, STEP_PLAIN)
+        eng.event(1)
+        pms += eng.elapsed_ms()
+    plain_launches = eng.launch_count() - plain_launch0
+    plain = W * S * args.steps / (max_over_ranks(dist, pms) / 1e3)
+    # e2e through the C ABI with host buffers, batched form
+    qp, qv = start_qpos.copy(), start_qvel.copy()
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.set_state(slots, qp, qv)
+        eng.step(S, STEP_BATCHED)
+        qp, qv = eng.get_state(slots, nq, nv)
+    eng.sync()
+    e2e = W * S * args.steps * ws / max_over_ranks(dist, time.perf_counter() - t0)
+    hbm, src = peaks()
+    n_launch = args.steps * S
+    dom = max(kernel_ms, key=kernel_ms.get)
+    dom_ms = kernel_ms[dom] / n_launch
+    n_piles = int((batch.n_bodies > 0).sum())
+    # pile kernels see the pile worlds only; 16-body rows stand in for the mean body count
+    mean_nb = int(round(float(batch.n_bodies[batch.n_bodies > 0].mean()))) if n_piles else 0
+    alg = pile_kernel_bytes(dom, n_piles, mean_nb, work)
+    achieved = alg / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else None
+    out = {
+        "metric": "env-steps/s", "value": value, "unit": "env-steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
+        "config": {"workload": "uneven: 50/50 chains and piles, 2..64 bodies log-uniform, PGS 50, dt 2e-3",
+                   "worlds_per_gpu": W, "chains": W - n_piles, "piles": n_piles, "env_steps_per_bench_step": S,
+                   "mode": "batched: tree persistent kernels per size bucket + one pile table, CUDA graph",
+                   "l2": "flushed between timed steps", "parallelism": f"replicas x{ws}"},
+        "plain_value": plain, "batched_over_plain": value / ws / plain,
+        "plain_launches_per_bench_step": plain_launches / args.steps,
+        "e2e": {"value": e2e, "unit": "env-steps/s", "h2d_bytes_per_step": qp.nbytes + qv.nbytes,
+                "d2h_bytes_per_step": qp.nbytes + qv.nbytes},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm if achieved else None, "traffic": None, "peak_source": src,
+                     "algorithmic_bytes_per_launch": alg, "ms_per_launch": dom_ms,
+                     "note": "pile kernels timed live inside the graph; the tree persistent kernels run "
+                             "concurrently on a second branch"},
+        "status_flags": int(np.bitwise_or.reduce(st)) if len(st) else 0,
+    }
+    eng.close()
+    return out
+
+
 def cpu_baseline_quadruped(batch, qpos, qvel, qfrc, n_worlds=256, steps=40):
     """The f32 restatement of newt's step (Newton tree-contact solve) on all
     host cores, on a sample of the quadrupeds from the timed region's start."""
@@ -451,6 +556,15 @@ def main():
     if args.impl == "reference":
         out = run_reference(args, rank, ws, local, dist)
         if out is not None:
+            print(json.dumps(out))
+        return
+    if args.workload == "uneven":
+        if args.worlds == 8192 and "--worlds" not in sys.argv:
+            args.worlds = 32768
+        if args.steps == 20 and "--steps" not in sys.argv:
+            args.steps = 4
+        out = run_gpu_uneven(args, rank, ws, local, dist)
+        if rank == 0:
             print(json.dumps(out))
         return
     if args.workload == "quadruped":

@@ -508,14 +508,18 @@ void HostGroup::read_qacc(int w, const HostModel& m, float* qacc) const {
 
 int HostGroup::fetch_status(newt_gpu_ctx* ctx) {
   if (n == 0) return NEWT_OK;
+  // copies on the context's stream: the steps that set the status words run
+  // there, and a plain cudaMemcpy does not wait for a non-blocking stream
   if (soa()) {
-    CKG(cudaMemcpy(hI.data() + (size_t)ri_status * cap, dI + (size_t)ri_status * cap, (size_t)cap * sizeof(int), cudaMemcpyDeviceToHost));
-    for (int w = 0; w < n; ++w) status_host[w] = (uint32_t)hI[(size_t)ri_status * cap + w];
+    CKG(cudaMemcpyAsync(hI.data() + (size_t)ri_status * cap, dI + (size_t)ri_status * cap, (size_t)cap * sizeof(int),
+                        cudaMemcpyDeviceToHost, ctx->stream));
   } else {
-    CKG(cudaMemcpy2D(hI.data() + lay.status, irows * sizeof(int), dI + lay.status, irows * sizeof(int), sizeof(int), n,
-                     cudaMemcpyDeviceToHost));
-    for (int w = 0; w < n; ++w) status_host[w] = (uint32_t)hI[(size_t)w * irows + lay.status];
+    CKG(cudaMemcpy2DAsync(hI.data() + lay.status, irows * sizeof(int), dI + lay.status, irows * sizeof(int),
+                          sizeof(int), n, cudaMemcpyDeviceToHost, ctx->stream));
   }
+  CKG(cudaStreamSynchronize(ctx->stream));
+  for (int w = 0; w < n; ++w)
+    status_host[w] = soa() ? (uint32_t)hI[(size_t)ri_status * cap + w] : (uint32_t)hI[(size_t)w * irows + lay.status];
   return NEWT_OK;
 }
 

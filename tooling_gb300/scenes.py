@@ -168,9 +168,11 @@ def _pile_world(rng: np.random.Generator, n_bodies: int, box_lo=(-1.0, -1.0, 0.3
             size = tuple(float(v) for v in h)
             bound = float(np.linalg.norm(h))
         mu = float(rng.uniform(0.3, 1.0))
+        C_arr = np.asarray(centers).reshape(-1, 3)
+        R_arr = np.asarray(radii)
         for _ in range(1000):
             p = rng.uniform(box_lo, box_hi)
-            if all(np.linalg.norm(p - c) > bound + rc for c, rc in zip(centers, radii)):
+            if not len(C_arr) or np.all(np.sqrt(((C_arr - p) ** 2).sum(axis=1)) > bound + R_arr):
                 break
         centers.append(p)
         radii.append(bound)
@@ -300,3 +302,75 @@ def quadruped_controls(n_worlds: int, block: int, seed_index: int = 2, first_wor
     out = np.zeros((n_worlds, 18), np.float32)
     out[:, 6:] = rng.normal(0.0, 2.0, (n_worlds, 12))
     return out.reshape(-1)
+
+
+# ---------------------------------------------------------------------------
+# uneven: a mixed batch of chains and piles with 2..64 bodies
+# ---------------------------------------------------------------------------
+def uneven_sizes(n_worlds: int, seed_index: int = 3, first_world: int = 0):
+    """(kind, n) per world: n = floor(exp(U(ln 2, ln 65))) in [2, 64], kind
+    'chain' or 'pile' with probability 1/2 each."""
+    cs = config_seed(seed_index)
+    out = []
+    for w in range(first_world, first_world + n_worlds):
+        rng = world_rng(cs, w)
+        n = int(math.floor(math.exp(rng.uniform(math.log(2.0), math.log(65.0)))))
+        out.append(("chain" if rng.random() < 0.5 else "pile", min(max(n, 2), 64)))
+    return out
+
+
+def _pack(items, dtype):
+    out = np.empty(len(items), dtype)
+    for i, x in enumerate(items):
+        out[i] = x
+    return out
+
+
+def _uneven_chunk(args):
+    """Worlds [first, first + count) of the uneven workload as packed arrays."""
+    seed_index, first, count = args
+    cs = config_seed(seed_index)
+    links, bodies, geoms, nl, nb, ng, qps, qvs, taus = [], [], [], [], [], [], [], [], []
+    for w in range(first, first + count):
+        rng = world_rng(cs, w)
+        n = int(math.floor(math.exp(rng.uniform(math.log(2.0), math.log(65.0)))))
+        n = min(max(n, 2), 64)
+        if rng.random() < 0.5:
+            l, q, qd, tau = _chain_world(rng, n)
+            links += l; nl.append(len(l)); nb.append(0); ng.append(0)
+            qps.append(q); qvs.append(qd); taus.append(tau)
+        else:
+            b, g, qp = _pile_world(rng, n)
+            bodies += b; geoms += g; nl.append(0); nb.append(n); ng.append(len(g))
+            qps.append(qp); qvs.append(np.zeros(6 * n)); taus.append(np.zeros(6 * n))
+    return (_pack(links, M.LINK_DT), nl, _pack(bodies, M.BODY_DT), nb, _pack(geoms, M.GEOM_DT), ng,
+            np.concatenate(qps), np.concatenate(qvs), np.concatenate(taus))
+
+
+def uneven_batch(n_worlds: int = 32768, seed_index: int = 3, dt: float = 2e-3, iterations: int = 50,
+                 first_world: int = 0, workers: int = 0) -> M.Batch:
+    """Chains (the chain generator with n hinges) and piles (the pile
+    generator with n bodies) mixed in one batch, PGS 50, dt 2e-3; every
+    world is rebuilt from its own seed.  Large batches are generated in
+    chunks by a spawn-started process pool (`workers` 0 = all cores)."""
+    chunk = 1024
+    jobs = [(seed_index, f, min(chunk, first_world + n_worlds - f))
+            for f in range(first_world, first_world + n_worlds, chunk)]
+    if len(jobs) > 1:
+        import concurrent.futures as cf
+        import multiprocessing as mp
+        import os
+        nw = workers or min(len(jobs), os.cpu_count() or 1)
+        with cf.ProcessPoolExecutor(max_workers=nw, mp_context=mp.get_context("spawn")) as ex:
+            parts = list(ex.map(_uneven_chunk, jobs))
+    else:
+        parts = [_uneven_chunk(j) for j in jobs]
+    cat = lambda k: np.concatenate([p[k] for p in parts])
+    nl = sum((list(p[1]) for p in parts), [])
+    nb = sum((list(p[3]) for p in parts), [])
+    ng = sum((list(p[5]) for p in parts), [])
+    batch = M.Batch(cat(0), nl, cat(2), nb, cat(4), ng, dt, (0.0, 0.0, -9.81), M.SOLVER_PGS, iterations)
+    batch.qpos[:] = cat(6)
+    batch.qvel[:] = cat(7)
+    batch.qfrc[:] = cat(8)
+    return batch
