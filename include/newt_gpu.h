@@ -201,6 +201,51 @@ NEWT_API int newt_gpu_event_elapsed_ms(newt_gpu_ctx* ctx, float* ms);
 NEWT_API int newt_gpu_flush_l2(newt_gpu_ctx* ctx);                              /* writes a buffer > L2 */
 /* Kernel launches issued by this context since creation. */
 NEWT_API int64_t newt_gpu_launch_count(const newt_gpu_ctx* ctx);
+/* Device bytes the world groups hold (capacity x bytes per world: model,
+ * state, contact and solver buffers) and the admission budget they are
+ * checked against. */
+NEWT_API int newt_gpu_memory(const newt_gpu_ctx* ctx, uint64_t* used, uint64_t* budget);
+
+/* ---- served rollouts ------------------------------------------------------
+ * No counterpart in newt, whose callers (newt/examples/*.rs,
+ * sandbox/src/main.rs:601) own one World and call World::step in their own
+ * loop.  newt_gpu_serve is that loop for many requests at once: a request
+ * (model, initial state, control sequence, horizon) is admitted into a free
+ * world slot once it has arrived and the device budget allows
+ * (newt_gpu_alloc_worlds answers NEWT_E_NOMEM past it; the request then
+ * waits), its state stays on the device, every admitted world advances by
+ * one env-step per tick through one step call (requests join and leave
+ * between ticks), row t of its controls is applied as qfrc at its step t,
+ * and its final state is read back when its horizon completes (a horizon of
+ * 0 returns the initial state without admission).  Latency = completion -
+ * arrival (completion - call start when real_time is 0). */
+typedef struct newt_serve_request {
+  int32_t model_id;        /* an uploaded model */
+  int32_t horizon;         /* env-steps */
+  double arrival_s;        /* seconds after the call starts */
+  const float* qpos;       /* initial state, MuJoCo layout (nq, nv) */
+  const float* qvel;
+  const float* ctrl;       /* horizon x nv generalised forces, row t at step t; NULL = none */
+  float* qpos_out;         /* final state written at completion (nullable) */
+  float* qvel_out;
+  double admit_s;          /* out: admission time */
+  double done_s;           /* out: completion time */
+} newt_serve_request;
+typedef struct newt_serve_opts {
+  int32_t max_active;      /* cap on admitted requests (0: the device budget only) */
+  int32_t real_time;       /* 1: arrivals follow the wall clock; 0: all present at start */
+  int32_t step_mode;       /* NEWT_STEP_BATCHED or NEWT_STEP_PLAIN */
+} newt_serve_opts;
+typedef struct newt_serve_stats {
+  int32_t completed, peak_active;
+  int64_t ticks;
+  double wall_s;           /* call start to last completion */
+  double env_steps;        /* sum of the completed horizons */
+  double mean_active;      /* admitted requests per tick, averaged */
+  double p50_ms, p99_ms, max_ms, mean_ms;  /* latency */
+} newt_serve_stats;
+NEWT_API int newt_gpu_serve(newt_gpu_ctx* ctx, newt_serve_request* reqs, int32_t n, const newt_serve_opts* opts,
+                            newt_serve_stats* stats);
 
 /* Profiling surface of the free-body contact step (no counterpart in newt,
  * whose per-phase timing lives in newt/benches/newt_perf.rs).

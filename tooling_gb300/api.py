@@ -29,7 +29,7 @@ EXPORTED = [
     "newt_gpu_set_qfrc", "newt_gpu_step", "newt_gpu_sync", "newt_gpu_world_status", "newt_gpu_get_qacc",
     "newt_gpu_get_contacts", "newt_gpu_get_impulses", "newt_gpu_event_record", "newt_gpu_event_elapsed_ms",
     "newt_gpu_flush_l2", "newt_gpu_launch_count", "newt_gpu_step_static", "newt_gpu_pile_profile",
-    "newt_gpu_tc_profile",
+    "newt_gpu_tc_profile", "newt_gpu_serve", "newt_gpu_memory",
 ]
 TC_KERNELS = ["tree_aba_kernel", "tc_k_solve", "tree_integrate_kernel"]
 PILE_KERNELS = ["pile_k_collide", "pile_k_pgs_small<1>", "pile_k_pgs_small<2>", "pile_k_pgs_small<4>",
@@ -46,6 +46,29 @@ class NewtError(RuntimeError):
 
 class Opts(C.Structure):
     _fields_ = [("device", C.c_int32), ("max_worlds", C.c_int32), ("hbm_budget_bytes", C.c_uint64)]
+
+
+class ServeRequest(C.Structure):
+    _fields_ = [("model_id", C.c_int32), ("horizon", C.c_int32), ("arrival_s", C.c_double),
+                ("qpos", C.c_void_p), ("qvel", C.c_void_p), ("ctrl", C.c_void_p),
+                ("qpos_out", C.c_void_p), ("qvel_out", C.c_void_p), ("admit_s", C.c_double), ("done_s", C.c_double)]
+
+
+class ServeOpts(C.Structure):
+    _fields_ = [("max_active", C.c_int32), ("real_time", C.c_int32), ("step_mode", C.c_int32)]
+
+
+# newt_serve_request as a numpy record (same layout), so request tables are
+# built without a Python loop
+SERVE_DTYPE = np.dtype([("model_id", "<i4"), ("horizon", "<i4"), ("arrival_s", "<f8"), ("qpos", "<u8"),
+                        ("qvel", "<u8"), ("ctrl", "<u8"), ("qpos_out", "<u8"), ("qvel_out", "<u8"),
+                        ("admit_s", "<f8"), ("done_s", "<f8")], align=True)
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("completed", C.c_int32), ("peak_active", C.c_int32), ("ticks", C.c_int64), ("wall_s", C.c_double),
+                ("env_steps", C.c_double), ("mean_active", C.c_double), ("p50_ms", C.c_double),
+                ("p99_ms", C.c_double), ("max_ms", C.c_double), ("mean_ms", C.c_double)]
 
 
 _lib = None
@@ -84,6 +107,8 @@ def load_library(path: str = LIB_PATH):
         "newt_gpu_step_static": ([P, I32], C.c_int),
         "newt_gpu_pile_profile": ([P, I32, P, P], C.c_int),
         "newt_gpu_tc_profile": ([P, P], C.c_int),
+        "newt_gpu_serve": ([P, P, I32, P, P], C.c_int),
+        "newt_gpu_memory": ([P, P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -189,6 +214,47 @@ class Engine:
         self._ck(self.L.newt_gpu_world_status(self.ctx, _p(s), len(s), _p(out), int(clear)))
         return out
 
+    # -- served rollouts -------------------------------------------------------
+    def serve(self, model_ids, horizons, arrivals_s, qpos: np.ndarray, qvel: np.ndarray,
+              ctrl: Optional[np.ndarray] = None, ctrl_off=None, max_active: int = 0,
+              real_time: bool = True, mode: int = STEP_BATCHED):
+        """Serve rollout requests through the native loop (newt_gpu_serve).
+
+        qpos / qvel: the requests' initial states concatenated in request
+        order (MuJoCo layout).  ctrl: one flat float32 array; request i reads
+        horizon_i x nv_i values from element ctrl_off[i] (-1: no controls).
+        Returns (final qpos, final qvel) concatenated like the inputs, a
+        stats dict, and the admission and completion times (s)."""
+        n = len(model_ids)
+        ids = np.ascontiguousarray(model_ids, np.int32)
+        hz = np.ascontiguousarray(horizons, np.int32)
+        dims = np.array([self.dims(int(m)) for m in ids], np.int64).reshape(n, 2)
+        qoff = np.concatenate([[0], np.cumsum(dims[:, 0])])
+        voff = np.concatenate([[0], np.cumsum(dims[:, 1])])
+        qp = np.ascontiguousarray(qpos, np.float32)
+        qv = np.ascontiguousarray(qvel, np.float32)
+        if qp.size != qoff[-1] or qv.size != voff[-1]:
+            raise ValueError("qpos/qvel sizes do not match the requests' models")
+        oq, ov = np.zeros(qoff[-1], np.float32), np.zeros(voff[-1], np.float32)
+        r = np.zeros(n, SERVE_DTYPE)
+        r["model_id"], r["horizon"], r["arrival_s"] = ids, hz, np.asarray(arrivals_s, np.float64)
+        r["qpos"] = qp.ctypes.data + 4 * qoff[:-1]
+        r["qvel"] = qv.ctypes.data + 4 * voff[:-1]
+        r["qpos_out"] = oq.ctypes.data + 4 * qoff[:-1]
+        r["qvel_out"] = ov.ctypes.data + 4 * voff[:-1]
+        if ctrl is not None:
+            c = np.ascontiguousarray(ctrl, np.float32)
+            co = np.asarray(ctrl_off, np.int64)
+            need = co + hz.astype(np.int64) * dims[:, 1]
+            if np.any((co >= 0) & (need > c.size)):
+                raise ValueError("a control window runs past the end of ctrl")
+            r["ctrl"] = np.where(co >= 0, c.ctypes.data + 4 * np.maximum(co, 0), 0).astype(np.uint64)
+        opts = ServeOpts(int(max_active), int(bool(real_time)), int(mode))
+        st = ServeStats()
+        self._ck(self.L.newt_gpu_serve(self.ctx, r.ctypes.data, n, C.byref(opts), C.byref(st)))
+        stats = {k: getattr(st, k) for k, _ in ServeStats._fields_}
+        return oq, ov, stats, r["admit_s"].copy(), r["done_s"].copy()
+
     # -- diagnostics ----------------------------------------------------------
     def contacts(self, slot: int, cap: int = 1024):
         n = C.c_int32()
@@ -215,6 +281,12 @@ class Engine:
 
     def flush_l2(self):
         self._ck(self.L.newt_gpu_flush_l2(self.ctx))
+
+    def memory(self):
+        """(device bytes held by the world groups, admission budget)."""
+        u, b = C.c_uint64(), C.c_uint64()
+        self._ck(self.L.newt_gpu_memory(self.ctx, C.byref(u), C.byref(b)))
+        return u.value, b.value
 
     def launch_count(self) -> int:
         return int(self.L.newt_gpu_launch_count(self.ctx))

@@ -17,7 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnewt_gpu.so")
 SOURCES = ["runtime.cu", "groups.cu", "step.cu", "tree_kernels.cu", "pile_kernels.cu", "newton_kernels.cu",
-           "static_step.cu"]
+           "static_step.cu",
+           "world_io.cu", "serve.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -50,7 +51,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
                     "--expt-relaxed-constexpr", "-I", os.path.join(HERE, "..", "include")]
 
     def comp(src):
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         cmd = [nvcc] + flags + ["-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

@@ -138,10 +138,15 @@ static int grow(newt_gpu_ctx* ctx, HostGroup& g, int need) {
   if (need <= g.cap) return NEWT_OK;
   int ncap = std::max(need, std::max(64, g.cap * 2));
   if (ncap > ctx->max_worlds) ncap = std::max(need, ctx->max_worlds);
-  uint64_t add = (uint64_t)(ncap - g.cap) * g.bytes_per_world();
-  if (ctx->used + add > ctx->budget) {
-    ctx->err = "HBM admission budget exhausted";
-    return NEWT_E_NOMEM;
+  const uint64_t bpw = g.bytes_per_world();
+  if (ctx->used + (uint64_t)(ncap - g.cap) * bpw > ctx->budget) {
+    // short of the doubling: take what the rest of the budget holds
+    const uint64_t room = ctx->budget > ctx->used ? (ctx->budget - ctx->used) / bpw : 0;
+    ncap = (int)std::min<uint64_t>((uint64_t)ncap, (uint64_t)g.cap + room);
+    if (ncap < need) {
+      ctx->err = "HBM admission budget exhausted";
+      return NEWT_E_NOMEM;
+    }
   }
   std::vector<float> nF(g.frows * (size_t)ncap, 0.f);
   std::vector<int> nI(g.irows * (size_t)ncap, 0);
@@ -212,16 +217,12 @@ int HostGroup::reserve_indices(newt_gpu_ctx* ctx, int k, std::vector<int>& out) 
   return NEWT_OK;
 }
 
-void HostGroup::release_index(newt_gpu_ctx* ctx, int idx) {
+int* HostGroup::release_index(int idx) {
   int lrow = soa() ? ri_live : lay.live;
   I(lrow, idx) = 0;
   slot_of[idx] = -1;
   free_idx.push_back(idx);
-  // mark the live flag on the device immediately (stream-ordered)
-  int zero = 0;
-  int* dst = soa() ? dI + (size_t)lrow * cap + idx : dI + (size_t)idx * irows + lrow;
-  cudaMemcpyAsync(dst, &zero, sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
-  cudaStreamSynchronize(ctx->stream);
+  return soa() ? dI + (size_t)lrow * cap + idx : dI + (size_t)idx * irows + lrow;  // the device live flag
 }
 
 // Geom topology, candidate pairs and contact capacity of a tree-contact
@@ -386,9 +387,9 @@ int HostGroup::flush_model(newt_gpu_ctx* ctx) {
 // ---------------------------------------------------------------------------
 // state staging (MuJoCo layout in, newt layout on the device)
 // ---------------------------------------------------------------------------
-static void state_range(const HostGroup& g, size_t* lo, size_t* cnt) {
-  if (g.soa()) { *lo = g.r_q; *cnt = (size_t)g.nq + g.nv; }
-  else { *lo = g.lay.pos; *cnt = (size_t)(g.lay.omg + 3 * g.size - g.lay.pos); }
+void HostGroup::state_rows(size_t* lo, size_t* cnt) const {
+  if (soa()) { *lo = r_q; *cnt = (size_t)nq + nv; }  // q then qd
+  else { *lo = lay.pos; *cnt = (size_t)(lay.omg + 3 * size - lay.pos); }
 }
 
 void HostGroup::stage_state(int w, const HostModel& m, const float* qpos, const float* qvel) {
@@ -421,55 +422,11 @@ void HostGroup::stage_state(int w, const HostModel& m, const float* qpos, const 
     }
   }
   (void)m;
-  state_dirty = true;
 }
 
 void HostGroup::stage_qfrc(int w, const HostModel& m, const float* qfrc) {
   if (soa()) for (int k = 0; k < nv; ++k) F(r_qfrc + k, w) = qfrc[k];
   (void)m;
-  qfrc_dirty = true;
-}
-
-int HostGroup::flush_state(newt_gpu_ctx* ctx) {
-  if (!state_dirty) return NEWT_OK;
-  size_t lo, cnt;
-  state_range(*this, &lo, &cnt);
-  if (soa()) {
-    CKG(cudaMemcpyAsync(dF + lo * cap, hF.data() + lo * cap, cnt * cap * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
-  } else {
-    CKG(cudaMemcpy2DAsync(dF + lo, frows * sizeof(float), hF.data() + lo, frows * sizeof(float), cnt * sizeof(float),
-                          n, cudaMemcpyHostToDevice, ctx->stream));
-  }
-  CKG(cudaStreamSynchronize(ctx->stream));
-  state_dirty = false;
-  return NEWT_OK;
-}
-
-int HostGroup::flush_qfrc(newt_gpu_ctx* ctx) {
-  if (!qfrc_dirty) return NEWT_OK;
-  if (soa()) {
-    CKG(cudaMemcpyAsync(dF + (size_t)r_qfrc * cap, hF.data() + (size_t)r_qfrc * cap, (size_t)nv * cap * sizeof(float),
-                        cudaMemcpyHostToDevice, ctx->stream));
-    CKG(cudaStreamSynchronize(ctx->stream));
-  }
-  qfrc_dirty = false;
-  return NEWT_OK;
-}
-
-int HostGroup::fetch_state(newt_gpu_ctx* ctx) {
-  if (n == 0) return NEWT_OK;
-  if (soa()) {
-    size_t lo = r_q, cnt = (size_t)nq + 3 * (size_t)nv;  // q qd qfrc qacc
-    CKG(cudaMemcpyAsync(hF.data() + lo * cap, dF + lo * cap, cnt * cap * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
-  } else {
-    size_t lo, cnt;
-    state_range(*this, &lo, &cnt);
-    CKG(cudaMemcpy2DAsync(hF.data() + lo, frows * sizeof(float), dF + lo, frows * sizeof(float), cnt * sizeof(float), n,
-                          cudaMemcpyDeviceToHost, ctx->stream));
-  }
-  CKG(cudaStreamSynchronize(ctx->stream));
-  device_newer = false;
-  return NEWT_OK;
 }
 
 void HostGroup::read_state(int w, const HostModel& m, float* qpos, float* qvel) const {

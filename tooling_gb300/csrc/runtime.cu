@@ -32,35 +32,6 @@ static int fail(newt_gpu_ctx* c, int code, const std::string& msg) {
     if (e_ != cudaSuccess) return fail(ctx, NEWT_E_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
   } while (0)
 
-static void quat_conj_rot(const float q[4], const float v[3], float out[3]) {  // R(q)^T v
-  float qx = -q[0], qy = -q[1], qz = -q[2], qw = q[3];
-  float tx = 2.f * (qy * v[2] - qz * v[1]), ty = 2.f * (qz * v[0] - qx * v[2]), tz = 2.f * (qx * v[1] - qy * v[0]);
-  out[0] = v[0] + qw * tx + (qy * tz - qz * ty);
-  out[1] = v[1] + qw * ty + (qz * tx - qx * tz);
-  out[2] = v[2] + qw * tz + (qx * ty - qy * tx);
-}
-static void quat_rot(const float q[4], const float v[3], float out[3]) {
-  float qc[4] = {-q[0], -q[1], -q[2], q[3]};
-  quat_conj_rot(qc, v, out);
-}
-static void renorm(float q[4]) {
-  float n = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
-  if (n == 0.f) { q[0] = q[1] = q[2] = 0.f; q[3] = 1.f; return; }
-  for (int k = 0; k < 4; ++k) q[k] /= n;
-}
-static bool inv_sym(const float m9[9], float out6[6]) {
-  // m9 column-major; output (xx yy zz xy xz yz) of the inverse
-  double a = m9[0], b = m9[3], c = m9[6], d = m9[1], e = m9[4], f = m9[7], g = m9[2], h = m9[5], i = m9[8];
-  double det = a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
-  if (det == 0.0 || !std::isfinite(det)) return false;
-  double inv = 1.0 / det;
-  double r00 = (e * i - f * h) * inv, r01 = (c * h - b * i) * inv, r02 = (b * f - c * e) * inv;
-  double r11 = (a * i - c * g) * inv, r12 = (c * d - a * f) * inv, r22 = (a * e - b * d) * inv;
-  out6[0] = (float)r00; out6[1] = (float)r11; out6[2] = (float)r22;
-  out6[3] = (float)r01; out6[4] = (float)r02; out6[5] = (float)r12;
-  return true;
-}
-
 // ---------------------------------------------------------------------------
 // model upload / classification
 // ---------------------------------------------------------------------------
@@ -198,6 +169,8 @@ int newt_gpu_destroy(newt_gpu_ctx* ctx) {
   for (int k = 0; k < 4; ++k) if (ctx->pev[k]) cudaEventDestroy(ctx->pev[k]);
   for (cudaEvent_t e : ctx->kev) cudaEventDestroy(e);
   for (cudaEvent_t e : ctx->tcev) cudaEventDestroy(e);
+  if (ctx->io_h) cudaFreeHost(ctx->io_h);
+  if (ctx->io_d) cudaFree(ctx->io_d);
   cudaEventDestroy(ctx->ev[0]);
   cudaEventDestroy(ctx->ev[1]);
   cudaStreamDestroy(ctx->stream);
@@ -226,9 +199,29 @@ int newt_gpu_model_dims(const newt_gpu_ctx* ctx, int32_t id, int32_t* nq, int32_
   return NEWT_OK;
 }
 
+// Returns live slots to the free lists and clears their worlds' live flags
+// on the device (one launch for the whole list).
+static int release_slots(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n) {
+  std::vector<int*> flags;
+  flags.reserve(n);
+  for (int i = 0; i < n; ++i) {
+    SlotRef& r = ctx->slots[slots[i]];
+    flags.push_back(ctx->groups[r.group]->release_index(r.index));
+    r.live = false;
+    ctx->free_slots.push_back(slots[i]);
+  }
+  return io_clear_flags(ctx, flags);
+}
+
 int newt_gpu_alloc_worlds(newt_gpu_ctx* ctx, const int32_t* model_ids, int32_t n, int32_t* slots_out) {
   if (!ctx || !model_ids || n < 0) return NEWT_E_INVALID;
   cudaSetDevice(ctx->device);
+  // a captured step graph covers every group up to its high-water mark and
+  // skips worlds that are not live, so it stays valid unless a group is
+  // created or grows
+  const size_t groups_before = ctx->groups.size();
+  std::vector<std::pair<int, int>> extent;
+  for (auto& g : ctx->groups) extent.push_back({g->n, g->cap});
   // group the request so each group grows at most once
   std::map<int, std::vector<int>> by_group;
   for (int i = 0; i < n; ++i) {
@@ -237,11 +230,28 @@ int newt_gpu_alloc_worlds(newt_gpu_ctx* ctx, const int32_t* model_ids, int32_t n
     HostGroup* g = find_or_make_group(ctx, ctx->models[id]);
     by_group[g->id].push_back(i);
   }
+  // all or nothing: a group that cannot grow undoes the worlds this call
+  // already placed in other groups
+  std::vector<int32_t> placed;
+  auto finish = [&](int rc) {
+    bool grew = ctx->groups.size() != groups_before;
+    for (size_t k = 0; k < extent.size() && !grew; ++k)
+      grew = ctx->groups[k]->n != extent[k].first || ctx->groups[k]->cap != extent[k].second;
+    if (grew) {
+      ctx->graph_dirty = true;
+      ctx->plain_dirty = true;
+    }
+    return rc;
+  };
+  auto undo = [&](int rc) {
+    int rc2 = release_slots(ctx, placed.data(), (int32_t)placed.size());
+    return finish(rc != NEWT_OK ? rc : rc2);
+  };
   for (auto& kv : by_group) {
     HostGroup* g = ctx->groups[kv.first].get();
     std::vector<int> idx;
     int rc = g->reserve_indices(ctx, (int)kv.second.size(), idx);
-    if (rc != NEWT_OK) return rc;
+    if (rc != NEWT_OK) return undo(rc);
     for (size_t k = 0; k < kv.second.size(); ++k) {
       int req = kv.second[k];
       int slot = (int)ctx->slots.size();
@@ -251,71 +261,84 @@ int newt_gpu_alloc_worlds(newt_gpu_ctx* ctx, const int32_t* model_ids, int32_t n
       g->write_model(ctx, idx[k], ctx->models[model_ids[req]]);
       g->slot_of[idx[k]] = slot;
       if (slots_out) slots_out[req] = slot;
+      placed.push_back(slot);
     }
     rc = g->flush_model(ctx);
-    if (rc != NEWT_OK) return rc;
+    if (rc != NEWT_OK) return undo(rc);
   }
-  ctx->graph_dirty = true;
-  ctx->plain_dirty = true;
-  return NEWT_OK;
+  return finish(NEWT_OK);
 }
 
 int newt_gpu_free_worlds(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n) {
-  if (!ctx) return NEWT_E_INVALID;
+  if (!ctx || (n > 0 && !slots)) return NEWT_E_INVALID;
+  cudaSetDevice(ctx->device);
   for (int i = 0; i < n; ++i) {
     int s = slots[i];
     if (s < 0 || s >= (int)ctx->slots.size() || !ctx->slots[s].live) return fail(ctx, NEWT_E_INVALID, "bad slot");
-    SlotRef& r = ctx->slots[s];
-    ctx->groups[r.group]->release_index(ctx, r.index);
-    r.live = false;
-    ctx->free_slots.push_back(s);
+    for (int j = 0; j < i; ++j)
+      if (slots[j] == s) return fail(ctx, NEWT_E_INVALID, "slot named twice");
   }
-  ctx->graph_dirty = true;
-  ctx->plain_dirty = true;
+  // the freed worlds' live flags are cleared on the device; captured graphs
+  // and plain tables skip them, so neither needs rebuilding
+  return release_slots(ctx, slots, n);
+}
+
+// Collects, per group, the worlds a call names (in call order), checking
+// every slot first.
+static int group_worlds(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, std::vector<std::vector<int>>& by_group) {
+  by_group.assign(ctx->groups.size(), {});
+  for (int i = 0; i < n; ++i) {
+    int s = slots[i];
+    if (s < 0 || s >= (int)ctx->slots.size() || !ctx->slots[s].live) return fail(ctx, NEWT_E_INVALID, "bad slot");
+    by_group[ctx->slots[s].group].push_back(ctx->slots[s].index);
+  }
   return NEWT_OK;
+}
+
+enum RowSet { ROWS_STATE, ROWS_QFRC, ROWS_QACC };
+
+static std::vector<RowMove> moves_for(newt_gpu_ctx* ctx, std::vector<std::vector<int>>& by_group, RowSet set) {
+  std::vector<RowMove> mv;
+  for (size_t gi = 0; gi < by_group.size(); ++gi) {
+    if (by_group[gi].empty()) continue;
+    HostGroup* g = ctx->groups[gi].get();
+    size_t lo = 0, cnt = 0;
+    if (set == ROWS_STATE) g->state_rows(&lo, &cnt);
+    else if (!g->soa()) continue;  // free-body piles carry no generalised force or acceleration rows
+    else { lo = set == ROWS_QFRC ? g->r_qfrc : g->r_qacc; cnt = g->nv; }
+    mv.push_back(RowMove{g, std::move(by_group[gi]), lo, cnt});
+  }
+  return mv;
 }
 
 int newt_gpu_set_state(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, const float* qpos, const float* qvel) {
   if (!ctx || (n > 0 && (!slots || !qpos || !qvel))) return NEWT_E_INVALID;
   cudaSetDevice(ctx->device);
-  // worlds not named here must keep their device state: refresh the host
-  // mirror of any group that stepped since its last fetch and is only
-  // partially overwritten by this call
-  std::vector<int> touched(ctx->groups.size(), 0);
-  for (int i = 0; i < n; ++i) {
-    int s = slots[i];
-    if (s < 0 || s >= (int)ctx->slots.size() || !ctx->slots[s].live) return fail(ctx, NEWT_E_INVALID, "bad slot");
-    touched[ctx->slots[s].group]++;
-  }
-  for (size_t gi = 0; gi < ctx->groups.size(); ++gi) {
-    HostGroup* g = ctx->groups[gi].get();
-    int live = g->n - (int)g->free_idx.size();
-    if (touched[gi] > 0 && g->device_newer && touched[gi] < live) {
-      int rc = g->fetch_state(ctx);
-      if (rc != NEWT_OK) return rc;
-    }
-  }
+  std::vector<std::vector<int>> by_group;
+  int rc = group_worlds(ctx, slots, n, by_group);
+  if (rc != NEWT_OK) return rc;
   long qo = 0, vo = 0;
   for (int i = 0; i < n; ++i) {
-    int s = slots[i];
-    const SlotRef& r = ctx->slots[s];
+    const SlotRef& r = ctx->slots[slots[i]];
     const HostModel& m = ctx->models[r.model];
     ctx->groups[r.group]->stage_state(r.index, m, qpos + qo, qvel + vo);
     qo += m.nq; vo += m.nv;
   }
-  for (auto& g : ctx->groups) { int rc = g->flush_state(ctx); if (rc != NEWT_OK) return rc; }
-  return NEWT_OK;
+  // only the named worlds' rows move: the others keep their device state
+  return io_scatter(ctx, moves_for(ctx, by_group, ROWS_STATE));
 }
 
 int newt_gpu_get_state(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, float* qpos, float* qvel) {
   if (!ctx || (n > 0 && (!slots || !qpos || !qvel))) return NEWT_E_INVALID;
   cudaSetDevice(ctx->device);
-  for (auto& g : ctx->groups) { int rc = g->fetch_state(ctx); if (rc != NEWT_OK) return rc; }
+  std::vector<std::vector<int>> by_group;
+  int rc = group_worlds(ctx, slots, n, by_group);
+  if (rc != NEWT_OK) return rc;
+  rc = io_gather(ctx, moves_for(ctx, by_group, ROWS_STATE));
+  if (rc != NEWT_OK) return rc;
   long qo = 0, vo = 0;
   for (int i = 0; i < n; ++i) {
-    int s = slots[i];
-    if (s < 0 || s >= (int)ctx->slots.size() || !ctx->slots[s].live) return fail(ctx, NEWT_E_INVALID, "bad slot");
-    const SlotRef& r = ctx->slots[s];
+    const SlotRef& r = ctx->slots[slots[i]];
     const HostModel& m = ctx->models[r.model];
     ctx->groups[r.group]->read_state(r.index, m, qpos + qo, qvel + vo);
     qo += m.nq; vo += m.nv;
@@ -326,17 +349,17 @@ int newt_gpu_get_state(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, float
 int newt_gpu_set_qfrc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, const float* qfrc) {
   if (!ctx || (n > 0 && (!slots || !qfrc))) return NEWT_E_INVALID;
   cudaSetDevice(ctx->device);
+  std::vector<std::vector<int>> by_group;
+  int rc = group_worlds(ctx, slots, n, by_group);
+  if (rc != NEWT_OK) return rc;
   long vo = 0;
   for (int i = 0; i < n; ++i) {
-    int s = slots[i];
-    if (s < 0 || s >= (int)ctx->slots.size() || !ctx->slots[s].live) return fail(ctx, NEWT_E_INVALID, "bad slot");
-    const SlotRef& r = ctx->slots[s];
+    const SlotRef& r = ctx->slots[slots[i]];
     const HostModel& m = ctx->models[r.model];
     ctx->groups[r.group]->stage_qfrc(r.index, m, qfrc + vo);
     vo += m.nv;
   }
-  for (auto& g : ctx->groups) { int rc = g->flush_qfrc(ctx); if (rc != NEWT_OK) return rc; }
-  return NEWT_OK;
+  return io_scatter(ctx, moves_for(ctx, by_group, ROWS_QFRC));
 }
 
 int newt_gpu_step(newt_gpu_ctx* ctx, int32_t n_steps, int32_t mode) {
@@ -380,12 +403,14 @@ int newt_gpu_world_status(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, ui
 int newt_gpu_get_qacc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, float* qacc) {
   if (!ctx || (n > 0 && (!slots || !qacc))) return NEWT_E_INVALID;
   cudaSetDevice(ctx->device);
-  for (auto& g : ctx->groups) { int rc = g->fetch_state(ctx); if (rc != NEWT_OK) return rc; }
+  std::vector<std::vector<int>> by_group;
+  int rc = group_worlds(ctx, slots, n, by_group);
+  if (rc != NEWT_OK) return rc;
+  rc = io_gather(ctx, moves_for(ctx, by_group, ROWS_QACC));
+  if (rc != NEWT_OK) return rc;
   long vo = 0;
   for (int i = 0; i < n; ++i) {
-    int s = slots[i];
-    if (s < 0 || s >= (int)ctx->slots.size() || !ctx->slots[s].live) return fail(ctx, NEWT_E_INVALID, "bad slot");
-    const SlotRef& r = ctx->slots[s];
+    const SlotRef& r = ctx->slots[slots[i]];
     const HostModel& m = ctx->models[r.model];
     ctx->groups[r.group]->read_qacc(r.index, m, qacc + vo);
     vo += m.nv;
@@ -432,6 +457,13 @@ int newt_gpu_flush_l2(newt_gpu_ctx* ctx) {
 }
 
 int64_t newt_gpu_launch_count(const newt_gpu_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+int newt_gpu_memory(const newt_gpu_ctx* ctx, uint64_t* used, uint64_t* budget) {
+  if (!ctx) return NEWT_E_INVALID;
+  if (used) *used = ctx->used;
+  if (budget) *budget = ctx->budget;
+  return NEWT_OK;
+}
 
 int newt_gpu_tc_profile(newt_gpu_ctx* ctx, float* kernel_ms) {
   if (!ctx || !kernel_ms) return NEWT_E_INVALID;

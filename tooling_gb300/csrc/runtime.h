@@ -63,8 +63,7 @@ struct HostGroup {
   std::vector<int> hI;    // host mirror of all int fields
   std::vector<int> topo;
   std::vector<uint32_t> status_host;
-  bool model_dirty = false, state_dirty = false, qfrc_dirty = false;
-  bool device_newer = false;  // kernels advanced the state after the last fetch
+  bool model_dirty = false;
   std::vector<int> pending;  // indices whose model record awaits upload
   // tree layout rows
   int r_axis = 0, r_jp = 0, r_jc = 0, r_rootq = 0, r_mass = 0, r_inert = 0, r_damp = 0, r_arm = 0, r_dtg = 0;
@@ -87,14 +86,15 @@ struct HostGroup {
   long scr_stride = 0;             // floats per world in plain_scratch
 
   int reserve_indices(newt_gpu_ctx* ctx, int k, std::vector<int>& out);
-  void release_index(newt_gpu_ctx* ctx, int idx);
+  int* release_index(int idx);  // host side; returns the world's device live flag
   void write_model(newt_gpu_ctx* ctx, int idx, const HostModel& m);
   int flush_model(newt_gpu_ctx* ctx);
+  // state in the host mirror for one world; moved to and from the device
+  // per world by io_scatter / io_gather over state_rows (q, qd) or the
+  // qfrc / qacc rows
   void stage_state(int idx, const HostModel& m, const float* qpos, const float* qvel);
   void stage_qfrc(int idx, const HostModel& m, const float* qfrc);
-  int flush_state(newt_gpu_ctx* ctx);
-  int flush_qfrc(newt_gpu_ctx* ctx);
-  int fetch_state(newt_gpu_ctx* ctx);
+  void state_rows(size_t* lo, size_t* cnt) const;
   void read_state(int idx, const HostModel& m, float* qpos, float* qvel) const;
   void read_qacc(int idx, const HostModel& m, float* qacc) const;
   int fetch_status(newt_gpu_ctx* ctx);
@@ -154,7 +154,21 @@ struct newt_gpu_ctx {
   // last tree-contact step call, recorded when `profile` is on
   std::vector<cudaEvent_t> tcev;
   int tcev_steps = 0;
+  // per-world state I/O staging (pinned host + device, same size)
+  void* io_h = nullptr;
+  void* io_d = nullptr;
+  size_t io_bytes = 0;
 };
+
+// rows [lo, lo + cnt) of the worlds `idx` of one group
+struct RowMove {
+  HostGroup* g;
+  std::vector<int> idx;
+  size_t lo, cnt;
+};
+int io_scatter(newt_gpu_ctx* ctx, const std::vector<RowMove>& mv);  // host mirror -> device
+int io_gather(newt_gpu_ctx* ctx, const std::vector<RowMove>& mv);   // device -> host mirror
+int io_clear_flags(newt_gpu_ctx* ctx, const std::vector<int*>& flags);  // *flag = 0 on the device
 
 HostGroup* find_or_make_group(newt_gpu_ctx* ctx, const HostModel& m);
 int step_plain(newt_gpu_ctx* ctx, int n_steps);

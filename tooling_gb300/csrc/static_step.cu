@@ -140,7 +140,6 @@ extern "C" NEWT_API int newt_gpu_step_static(newt_gpu_ctx* ctx, int32_t n_steps)
     if (ng > 0)
       ctx->launches += newt_launch_pile_step_serial(dG, dseg, ng, seg[ng], slots, lists, s == n_steps - 1, ctx->stream);
   }
-  for (auto& g : ctx->groups) if (g->n > 0) g->device_newer = true;
   e = cudaGetLastError();
   if (e != cudaSuccess) return fail(ctx, NEWT_E_CUDA, std::string("launch: ") + cudaGetErrorString(e));
   return NEWT_OK;

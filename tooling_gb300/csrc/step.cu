@@ -45,10 +45,6 @@ static int sm_count(newt_gpu_ctx* ctx) {
   return n;
 }
 
-static void mark_stepped(newt_gpu_ctx* ctx) {
-  for (auto& g : ctx->groups) if (g->n > 0) g->device_newer = true;
-}
-
 // Per-group solver scratch for pile worlds (world-major, cap worlds).
 static int ensure_pile_scratch(newt_gpu_ctx* ctx, HostGroup* g) {
   int rs = ensure_pile_streams(ctx);
@@ -167,7 +163,6 @@ int step_plain(newt_gpu_ctx* ctx, int n_steps) {
       }
     }
   }
-  mark_stepped(ctx);
   return NEWT_OK;
 }
 
@@ -274,6 +269,5 @@ int step_batched(newt_gpu_ctx* ctx, int n_steps) {
         if (rc != NEWT_OK) return rc;
       }
   }
-  mark_stepped(ctx);
   return NEWT_OK;
 }

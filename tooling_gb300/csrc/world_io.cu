@@ -1,0 +1,222 @@
+// Per-world state I/O: moves chosen rows of the named worlds between the
+// host mirror and the device, so a call that touches k worlds moves k worlds'
+// rows (what newt's World::apply_mujoco_qpos/qvel, newt/src/world.rs:519-623,
+// touches for one world) instead of whole groups.
+//
+// One call packs every group's segment into one pinned staging buffer, makes
+// one copy and one scatter (or gather) launch per group, then synchronises
+// once; a group whose named worlds are consecutive indices skips the packing
+// and moves by one strided copy.  The packed order follows the device layout so both sides of each
+// launch are coalesced: tree groups keep fields as rows x cap (packed as
+// rows x k), pile groups keep worlds contiguous (packed as k x rows).
+#include <algorithm>
+
+#include "runtime.h"
+
+#define CKW(call)                                                               \
+  do {                                                                          \
+    cudaError_t e_ = (call);                                                    \
+    if (e_ != cudaSuccess) { ctx->err = std::string(#call ": ") + cudaGetErrorString(e_); return NEWT_E_CUDA; } \
+  } while (0)
+
+namespace {
+
+__global__ void rows_scatter(float* __restrict__ dF, int soa, int cap, int frows, int lo, int cnt,
+                             const int* __restrict__ idx, int k, const float* __restrict__ src) {
+  const long total = (long)k * cnt;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    if (soa) {
+      const int r = (int)(t / k), j = (int)(t % k);
+      dF[(size_t)(lo + r) * cap + idx[j]] = src[t];
+    } else {
+      const int j = (int)(t / cnt), r = (int)(t % cnt);
+      dF[(size_t)idx[j] * frows + lo + r] = src[t];
+    }
+  }
+}
+
+__global__ void rows_gather(const float* __restrict__ dF, int soa, int cap, int frows, int lo, int cnt,
+                            const int* __restrict__ idx, int k, float* __restrict__ dst) {
+  const long total = (long)k * cnt;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    if (soa) {
+      const int r = (int)(t / k), j = (int)(t % k);
+      dst[t] = dF[(size_t)(lo + r) * cap + idx[j]];
+    } else {
+      const int j = (int)(t / cnt), r = (int)(t % cnt);
+      dst[t] = dF[(size_t)idx[j] * frows + lo + r];
+    }
+  }
+}
+
+__global__ void flags_clear(int* const* __restrict__ flags, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) *flags[i] = 0;
+}
+
+int grid_for(long total) {
+  const long b = (total + 255) / 256;
+  return (int)std::max<long>(1, std::min<long>(b, 152L * 16));
+}
+
+// staging: [idx ints | floats], both for every segment of the call
+int ensure_staging(newt_gpu_ctx* ctx, size_t n_idx, size_t n_f) {
+  const size_t bytes = ((n_idx * sizeof(int) + 255) & ~(size_t)255) + n_f * sizeof(float);
+  if (bytes <= ctx->io_bytes) return NEWT_OK;
+  size_t want = std::max<size_t>(bytes, 2 * ctx->io_bytes);
+  want = std::max<size_t>(want, 1 << 20);
+  if (ctx->io_h) cudaFreeHost(ctx->io_h);
+  if (ctx->io_d) cudaFree(ctx->io_d);
+  ctx->io_h = nullptr;
+  ctx->io_d = nullptr;
+  ctx->io_bytes = 0;
+  CKW(cudaMallocHost(&ctx->io_h, want));
+  CKW(cudaMalloc(&ctx->io_d, want));
+  ctx->io_bytes = want;
+  return NEWT_OK;
+}
+
+struct Layout {
+  size_t idx_bytes;
+  std::vector<size_t> ioff, foff;
+  size_t n_idx = 0, n_f = 0;
+};
+
+Layout layout(const std::vector<RowMove>& mv) {
+  Layout L;
+  for (const RowMove& m : mv) {
+    L.ioff.push_back(L.n_idx);
+    L.foff.push_back(L.n_f);
+    L.n_idx += m.idx.size();
+    L.n_f += m.idx.size() * m.cnt;
+  }
+  L.idx_bytes = (L.n_idx * sizeof(int) + 255) & ~(size_t)255;
+  return L;
+}
+
+// A world list that is one run of consecutive indices moves as one strided
+// copy straight between the host mirror and the device, with no packing.
+bool consecutive(const std::vector<int>& idx) {
+  for (size_t j = 1; j < idx.size(); ++j)
+    if (idx[j] != idx[0] + (int)j) return false;
+  return !idx.empty();
+}
+
+cudaError_t copy_run(const RowMove& m, cudaStream_t st, bool to_device) {
+  HostGroup& g = *m.g;
+  const size_t a = (size_t)m.idx[0], k = m.idx.size();
+  float* h = g.hF.data();
+  float* d = g.dF;
+  if (g.soa()) {  // cnt rows of k consecutive worlds, row pitch cap
+    const size_t off = m.lo * g.cap + a, pitch = g.cap * sizeof(float);
+    return to_device ? cudaMemcpy2DAsync(d + off, pitch, h + off, pitch, k * sizeof(float), m.cnt,
+                                         cudaMemcpyHostToDevice, st)
+                     : cudaMemcpy2DAsync(h + off, pitch, d + off, pitch, k * sizeof(float), m.cnt,
+                                         cudaMemcpyDeviceToHost, st);
+  }
+  const size_t off = a * g.frows + m.lo, pitch = g.frows * sizeof(float);  // k worlds of cnt values
+  return to_device ? cudaMemcpy2DAsync(d + off, pitch, h + off, pitch, m.cnt * sizeof(float), k,
+                                       cudaMemcpyHostToDevice, st)
+                   : cudaMemcpy2DAsync(h + off, pitch, d + off, pitch, m.cnt * sizeof(float), k,
+                                       cudaMemcpyDeviceToHost, st);
+}
+
+}  // namespace
+
+int io_scatter(newt_gpu_ctx* ctx, const std::vector<RowMove>& all) {
+  std::vector<RowMove> mv;
+  for (const RowMove& m : all) {
+    if (consecutive(m.idx)) CKW(copy_run(m, ctx->stream, true));
+    else mv.push_back(m);
+  }
+  if (mv.empty()) {
+    CKW(cudaStreamSynchronize(ctx->stream));
+    return NEWT_OK;
+  }
+  const Layout L = layout(mv);
+  int rc = ensure_staging(ctx, L.n_idx, L.n_f);
+  if (rc != NEWT_OK) return rc;
+  int* hi = (int*)ctx->io_h;
+  float* hf = (float*)((char*)ctx->io_h + L.idx_bytes);
+  for (size_t s = 0; s < mv.size(); ++s) {
+    const RowMove& m = mv[s];
+    const HostGroup& g = *m.g;
+    const size_t k = m.idx.size();
+    std::copy(m.idx.begin(), m.idx.end(), hi + L.ioff[s]);
+    float* out = hf + L.foff[s];
+    for (size_t j = 0; j < k; ++j)
+      for (size_t r = 0; r < m.cnt; ++r) {
+        const float v = g.Fc(m.lo + r, m.idx[j]);
+        if (g.soa()) out[r * k + j] = v; else out[j * m.cnt + r] = v;
+      }
+  }
+  CKW(cudaMemcpyAsync(ctx->io_d, ctx->io_h, L.idx_bytes + L.n_f * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  const int* di = (const int*)ctx->io_d;
+  const float* df = (const float*)((char*)ctx->io_d + L.idx_bytes);
+  for (size_t s = 0; s < mv.size(); ++s) {
+    const RowMove& m = mv[s];
+    const long total = (long)m.idx.size() * m.cnt;
+    if (total == 0) continue;
+    rows_scatter<<<grid_for(total), 256, 0, ctx->stream>>>(m.g->dF, m.g->soa() ? 1 : 0, m.g->cap, (int)m.g->frows,
+                                                            (int)m.lo, (int)m.cnt, di + L.ioff[s], (int)m.idx.size(),
+                                                            df + L.foff[s]);
+    ctx->launches++;
+  }
+  CKW(cudaGetLastError());
+  CKW(cudaStreamSynchronize(ctx->stream));  // the pinned staging is reused by the next call
+  return NEWT_OK;
+}
+
+int io_gather(newt_gpu_ctx* ctx, const std::vector<RowMove>& all) {
+  std::vector<RowMove> mv;
+  for (const RowMove& m : all) {
+    if (consecutive(m.idx)) CKW(copy_run(m, ctx->stream, false));
+    else mv.push_back(m);
+  }
+  if (mv.empty()) {
+    CKW(cudaStreamSynchronize(ctx->stream));
+    return NEWT_OK;
+  }
+  const Layout L = layout(mv);
+  int rc = ensure_staging(ctx, L.n_idx, L.n_f);
+  if (rc != NEWT_OK) return rc;
+  int* hi = (int*)ctx->io_h;
+  for (size_t s = 0; s < mv.size(); ++s) std::copy(mv[s].idx.begin(), mv[s].idx.end(), hi + L.ioff[s]);
+  CKW(cudaMemcpyAsync(ctx->io_d, ctx->io_h, L.n_idx * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  const int* di = (const int*)ctx->io_d;
+  float* df = (float*)((char*)ctx->io_d + L.idx_bytes);
+  for (size_t s = 0; s < mv.size(); ++s) {
+    const RowMove& m = mv[s];
+    const long total = (long)m.idx.size() * m.cnt;
+    if (total == 0) continue;
+    rows_gather<<<grid_for(total), 256, 0, ctx->stream>>>(m.g->dF, m.g->soa() ? 1 : 0, m.g->cap, (int)m.g->frows,
+                                                           (int)m.lo, (int)m.cnt, di + L.ioff[s], (int)m.idx.size(),
+                                                           df + L.foff[s]);
+    ctx->launches++;
+  }
+  CKW(cudaGetLastError());
+  float* hf = (float*)((char*)ctx->io_h + L.idx_bytes);
+  CKW(cudaMemcpyAsync(hf, df, L.n_f * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  CKW(cudaStreamSynchronize(ctx->stream));
+  for (size_t s = 0; s < mv.size(); ++s) {
+    const RowMove& m = mv[s];
+    HostGroup& g = *m.g;
+    const size_t k = m.idx.size();
+    const float* in = hf + L.foff[s];
+    for (size_t j = 0; j < k; ++j)
+      for (size_t r = 0; r < m.cnt; ++r) g.F(m.lo + r, m.idx[j]) = g.soa() ? in[r * k + j] : in[j * m.cnt + r];
+  }
+  return NEWT_OK;
+}
+
+int io_clear_flags(newt_gpu_ctx* ctx, const std::vector<int*>& flags) {
+  if (flags.empty()) return NEWT_OK;
+  int rc = ensure_staging(ctx, 0, 2 * flags.size());  // one pointer = two floats' room
+  if (rc != NEWT_OK) return rc;
+  std::copy(flags.begin(), flags.end(), (int**)ctx->io_h);
+  CKW(cudaMemcpyAsync(ctx->io_d, ctx->io_h, flags.size() * sizeof(int*), cudaMemcpyHostToDevice, ctx->stream));
+  flags_clear<<<grid_for((long)flags.size()), 256, 0, ctx->stream>>>((int* const*)ctx->io_d, (int)flags.size());
+  ctx->launches++;
+  CKW(cudaGetLastError());
+  CKW(cudaStreamSynchronize(ctx->stream));
+  return NEWT_OK;
+}
