@@ -243,6 +243,10 @@ typedef struct newt_serve_stats {
   double env_steps;        /* sum of the completed horizons */
   double mean_active;      /* admitted requests per tick, averaged */
   double p50_ms, p99_ms, max_ms, mean_ms;  /* latency */
+  /* host wall time per phase, summed over ticks: admission (alloc + state
+   * upload), controls (qfrc upload), step (launch to completion), and
+   * completion (state read-back + release) */
+  double admit_s, ctrl_s, step_s, complete_s;
 } newt_serve_stats;
 NEWT_API int newt_gpu_serve(newt_gpu_ctx* ctx, newt_serve_request* reqs, int32_t n, const newt_serve_opts* opts,
                             newt_serve_stats* stats);

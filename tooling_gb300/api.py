@@ -33,7 +33,7 @@ EXPORTED = [
 ]
 TC_KERNELS = ["tree_aba_kernel", "tc_k_solve", "tree_integrate_kernel"]
 PILE_KERNELS = ["pile_k_collide", "pile_k_pgs_small<1>", "pile_k_pgs_small<2>", "pile_k_pgs_small<4>",
-                "pile_k_pgs_lane<4,4>", "pile_k_pgs_lane<5,4>", "pile_k_pgs_lane<33,32>", "pile_k_pgs_multi<0>",
+                "pile_k_pgs_quad[3]", "pile_k_pgs_quad[4]", "pile_k_pgs_quad[5]", "pile_k_pgs_quad[6]",
                 "pile_k_integrate"]
 PILE_ISLAND_CLASSES = 7
 
@@ -68,7 +68,8 @@ SERVE_DTYPE = np.dtype([("model_id", "<i4"), ("horizon", "<i4"), ("arrival_s", "
 class ServeStats(C.Structure):
     _fields_ = [("completed", C.c_int32), ("peak_active", C.c_int32), ("ticks", C.c_int64), ("wall_s", C.c_double),
                 ("env_steps", C.c_double), ("mean_active", C.c_double), ("p50_ms", C.c_double),
-                ("p99_ms", C.c_double), ("max_ms", C.c_double), ("mean_ms", C.c_double)]
+                ("p99_ms", C.c_double), ("max_ms", C.c_double), ("mean_ms", C.c_double), ("admit_s", C.c_double),
+                ("ctrl_s", C.c_double), ("step_s", C.c_double), ("complete_s", C.c_double)]
 
 
 _lib = None

@@ -27,7 +27,7 @@ namespace pile {
 constexpr int SH_PLANE = 0, SH_SPHERE = 1, SH_BOX = 2;
 constexpr int CF = 39;  // floats per contact in the scratch record
 constexpr int CI = 4;   // ints per contact
-constexpr int SC = 154;  // floats per active contact in the solver record
+constexpr int SC = 188;  // floats per active contact in the solver record (a multiple of 4)
 
 // Per-world scratch record in global memory (L1/L2 resident while a world
 // is being stepped).  Offsets in floats / ints.
@@ -56,6 +56,7 @@ __host__ __device__ inline WsLay ws_layout(int nb, int np, int maxc) {
   L.gquat = f; f += 4 * nb; L.plane = f; f += 7 * np; L.fric = f; f += L.ng; L.margin = f; f += L.ng;
   L.aabb = f; f += 6 * L.ng; L.soft = f; f += 7; L.dtg = f; f += 4;
   L.con = f; f += CF * maxc;
+  f = (f + 3) / 4 * 4;  // 16-byte aligned solver records
   L.sc = f; f += SC * maxc;
   L.nf = (f + 3) / 4 * 4;
   int i = 0;

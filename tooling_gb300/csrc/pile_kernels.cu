@@ -9,9 +9,9 @@
 //                        contacts (the common resting case): accumulators,
 //                        Jacobians and impulses live in registers for all
 //                        sweeps (classes 0-2)
-//   K3a pgs_lane         one thread per multi-body island, one warp per
-//                        block spread over every SM (classes 3-5)
-//   K3b pgs_multi        fallback for islands past K3a's limits (class 6)
+//   K3 pgs_quad          multi-body islands (classes 3-6): four lanes per
+//                        island, eight islands per warp; the contact sweep
+//                        serial, each contact's rows spread over the lanes
 //   K4 integrate         one warp per world: semi-implicit Euler, state and
 //                        diagnostics back to the world record
 // The class kernels touch disjoint islands and run concurrently.
@@ -29,8 +29,8 @@
 // Gauss-Seidel is order dependent.  Rows of disjoint islands never touch the
 // same body, so sweeping each island in newt's contact order (one thread per
 // island) equals the serial sweep.  A facet row n + s*mu*t has Jacobian
-// Jn + s*mu*Jt; each contact stores Jn, Jt1, Jt2 per side (K2, K3b form the
-// rows on the fly) and the four rows with their M^-1 J^T (K3a).  Velocity
+// Jn + s*mu*Jt; each contact stores Jn, Jt1, Jt2 per side (K2 forms the rows
+// on the fly) and the four rows with their M^-1 J^T (K3).  Velocity
 // accumulators are kept in world frame (newt keeps the angular one in body
 // frame; equal up to rounding).
 #include <algorithm>
@@ -43,11 +43,14 @@ using namespace pile;
 namespace {
 
 // solver-record fields (floats inside one SC block)
-enum { S_JA = 0, S_JB = 18, S_MU = 36, S_IDIAG = 37, S_BIAS = 41, S_REG = 45, S_P0 = 46, S_P1 = 50, S_IMP = 54,
-       S_ROWS = 58 };
-// S_ROWS: per facet row r (0..3), 24 floats at S_ROWS + 24 r:
-//   Ja[6] (J for side a), Wa[6] = M_a^-1 Ja^T, Jb[6], Wb[6] (zero for a static side)
+// (16-byte aligned: the multi-body solver reads them as float4)
+enum { S_JA = 0, S_JB = 18, S_IDIAG = 36, S_BIAS = 40, S_P0 = 44, S_P1 = 48, S_REG = 52, S_MU = 53, S_IMP = 56,
+       S_ROWS = 60 };
+// S_ROWS: per facet row r (0..3), 32 floats at S_ROWS + 32 r: J then
+//   M^-1 J^T, each as four float4 triples (side a linear, side a angular,
+//   side b linear, side b angular; w = 0), zero for a static side
 // pair block: h00, h11, h01, inverse determinant (0 when det <= 0)
+static_assert(S_ROWS + 4 * 32 == SC, "solver record size");
 
 NEWT_D float impedance(float pos, const float* soft) {
   // effective_solimp + impedance_at_position(pos, 0) (solver.rs:301-326)
@@ -89,10 +92,9 @@ struct IslandLists {
 constexpr int N_COUNTERS = 3 * N_ICLASS;
 
 // 0-2: one body with 1, 2, 3-4 contacts (pile_k_pgs_small: everything in
-// registers); 3, 4: fewer than CH_MIN contacts with up to 4 / 5 bodies, and
-// 5: CH_MIN..CH_MAXC contacts (pile_k_pgs_lane, sized per class); 6: the
-// rest (pile_k_pgs_multi).  An island is connected, so it has at most one
-// body more than contacts.
+// registers); 3, 4: fewer than CH_MIN contacts with up to 4 / 5 bodies; 5:
+// CH_MIN..CH_MAXC contacts; 6: the rest (pile_k_pgs_quad, sized per class).
+// An island is connected, so it has at most one body more than contacts.
 NEWT_D int island_class(int nbody, int cnt) {
   if (nbody == 1 && cnt == 1) return 0;
   if (nbody == 1 && cnt == 2) return 1;
@@ -281,12 +283,14 @@ NEWT_D void assemble(const WsLay& L, float* wf, int* wi, int lane, int t_world, 
       sc[S_BIAS + r] = dvf - aref * dt;
       sc[S_IMP + r] = 0.f;
       // a static side's row is stored as zeros, so the solvers need no masks
-      float* row = sc + S_ROWS + 24 * r;
-      const J6 z{v3(0.f, 0.f, 0.f), v3(0.f, 0.f, 0.f)};
-      stj(row, da ? Ra[r] : z);
-      stj(row + 6, da ? J6{Ra[r].l * ima, smv(Ia, Ra[r].a)} : z);
-      stj(row + 12, db ? Rb[r] : z);
-      stj(row + 18, db ? J6{Rb[r].l * imb, smv(Ib, Rb[r].a)} : z);
+      float* row = sc + S_ROWS + 32 * r;
+      const V3 z = v3(0.f, 0.f, 0.f);
+      const V3 trip[8] = {da ? Ra[r].l : z, da ? Ra[r].a : z, db ? Rb[r].l : z, db ? Rb[r].a : z,
+                          da ? Ra[r].l * ima : z, da ? smv(Ia, Ra[r].a) : z,
+                          db ? Rb[r].l * imb : z, db ? smv(Ib, Rb[r].a) : z};
+      for (int e = 0; e < 8; ++e) {
+        row[4 * e] = trip[e].x; row[4 * e + 1] = trip[e].y; row[4 * e + 2] = trip[e].z; row[4 * e + 3] = 0.f;
+      }
     }
     // pyramidal pair blocks (solver.rs:1037-1061, 1476-1518)
     for (int p = 0; p < 2; ++p) {
@@ -474,247 +478,178 @@ __global__ void __launch_bounds__(128) pile_k_pgs_small(const PileGroupDev* G, c
 }
 
 // ---------------------------------------------------------------------------
-// K3b: the fallback for islands past the lane kernels' limits (more than
-// CH_MAXC contacts), one thread per island, rows formed on the fly from the
-// contact Jacobians.  MB > 0: at most MB bodies, accumulators in registers
-// (selected by island-local index); MB == 0: any size, accumulators in a
-// thread-local array.
+// K3: multi-body islands (classes 3-6), four lanes per island and eight
+// islands per warp.  The contact sweep of an island stays serial (Gauss-
+// Seidel order); inside one contact, lane l of the island's four holds one
+// float4 triple of the 12 velocity-accumulator entries the contact touches
+// (side a linear, side a angular, side b linear, side b angular) and the
+// matching triples of the facet rows' J and M^-1 J^T.  A facet residual is
+// a triple dot product summed over the four lanes (two shuffles; a 2x2 pair
+// sums both rows at once), every lane takes the same scalar step and updates
+// its own triple.  Body accumulators live in shared memory (island-local
+// ids, a dummy slot for a static side), impulses in the solver record.  The
+// warp runs until its longest island is done; finished islands idle.
 // ---------------------------------------------------------------------------
-template <int MB>
-struct Accs {
-  float a[MB > 0 ? MB : NEWT_MAX_BODIES][6];
-  NEWT_D void zero(int nb) {
-#pragma unroll
-    for (int b = 0; b < (MB > 0 ? MB : NEWT_MAX_BODIES); ++b)
-      if (MB > 0 || b < nb)
-#pragma unroll
-        for (int q = 0; q < 6; ++q) a[b][q] = 0.f;
-  }
-  NEWT_D void get(int b, V3* l, V3* w) const {
-    if (MB > 0) {
-      float v[6];
-#pragma unroll
-      for (int q = 0; q < 6; ++q) {
-        float x = a[0][q];
-#pragma unroll
-        for (int k = 1; k < (MB > 0 ? MB : 1); ++k) x = b == k ? a[k][q] : x;
-        v[q] = x;
-      }
-      *l = v3(v[0], v[1], v[2]); *w = v3(v[3], v[4], v[5]);
-    } else {
-      *l = v3(a[b][0], a[b][1], a[b][2]); *w = v3(a[b][3], a[b][4], a[b][5]);
-    }
-  }
-  NEWT_D void add(int b, V3 l, V3 w) {
-    if (MB > 0) {
-      const float v[6] = {l.x, l.y, l.z, w.x, w.y, w.z};
-#pragma unroll
-      for (int k = 0; k < (MB > 0 ? MB : 1); ++k)
-#pragma unroll
-        for (int q = 0; q < 6; ++q) a[k][q] += b == k ? v[q] : 0.f;
-    } else {
-      a[b][0] += l.x; a[b][1] += l.y; a[b][2] += l.z; a[b][3] += w.x; a[b][4] += w.y; a[b][5] += w.z;
-    }
-  }
+NEWT_D float dot3(const float* j, const float* a) { return (j[0] * a[0] + j[1] * a[1]) + j[2] * a[2]; }
+NEWT_D float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+
+// One lane's share of one contact: its triple of each facet row's J and
+// M^-1 J^T, the row scalars, the impulses and its side's body slot.
+struct QuadContact {
+  float J[4][3], W[4][3];
+  float idg[4], bias[4], P[8], imp[4], reg;
+  int body;
 };
 
-template <int MB>
-__global__ void __launch_bounds__(128) pile_k_pgs_multi(const PileGroupDev* G, const int* wseg, int ng,
-                                                        const int* items, const int* count, int cls) {
+NEWT_D void quad_load(const float* sc, const int* ids, int side, int l, int dummy, QuadContact& c) {
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const float4 j = ldg4(sc + S_ROWS + 32 * r + 4 * l), w = ldg4(sc + S_ROWS + 32 * r + 16 + 4 * l);
+    c.J[r][0] = j.x; c.J[r][1] = j.y; c.J[r][2] = j.z;
+    c.W[r][0] = w.x; c.W[r][1] = w.y; c.W[r][2] = w.z;
+  }
+  const float4 d = ldg4(sc + S_IDIAG), b = ldg4(sc + S_BIAS), p0 = ldg4(sc + S_P0), p1 = ldg4(sc + S_P1);
+  c.idg[0] = d.x; c.idg[1] = d.y; c.idg[2] = d.z; c.idg[3] = d.w;
+  c.bias[0] = b.x; c.bias[1] = b.y; c.bias[2] = b.z; c.bias[3] = b.w;
+  c.P[0] = p0.x; c.P[1] = p0.y; c.P[2] = p0.z; c.P[3] = p0.w;
+  c.P[4] = p1.x; c.P[5] = p1.y; c.P[6] = p1.z; c.P[7] = p1.w;
+  c.reg = __ldg(sc + S_REG);
+  const float4 m = *reinterpret_cast<const float4*>(sc + S_IMP);  // written by this kernel in the previous sweep
+  c.imp[0] = m.x; c.imp[1] = m.y; c.imp[2] = m.z; c.imp[3] = m.w;
+  const int id = __ldg(ids + side);
+  c.body = id >= 0 ? id : dummy;
+}
+
+NEWT_D void quad_zero(int dummy, QuadContact& c) {
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+#pragma unroll
+    for (int e = 0; e < 3; ++e) c.J[r][e] = c.W[r][e] = 0.f;
+    c.idg[r] = c.bias[r] = c.imp[r] = 0.f;
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) c.P[i] = 0.f;
+  c.reg = 0.f;
+  c.body = dummy;
+}
+
+template <int MAXB, int WPB>
+__global__ void __launch_bounds__(32 * WPB) pile_k_pgs_quad(const PileGroupDev* G, const int* wseg, int ng,
+                                                            const int* items, const int* count, int cls) {
+  __shared__ float acc_s[WPB][8][MAXB + 1][6];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int slot = lane >> 2, l = lane & 3, side = l >> 1, part = l & 1;
+  const unsigned gm = 0xFu << (lane & ~3);  // this island's four lanes
+  float(*acc)[6] = acc_s[wib][slot];
   const int n_items = count[cls];
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_items; t += gridDim.x * blockDim.x) {
-  IslandRef R;
-  island_ref(G, wseg, ng, items[t], &R);
-  const WsLay& L = R.L;
-  float* wf = R.wf;
-  const int* wi = R.wi;
-  const int isl = R.isl;
-  const int nbody = wi[L.inb + isl], cnt = wi[L.icount + isl];
-  const int k0 = wi[L.istart + isl], b0 = wi[L.ibstart + isl];
-  const int iters = R.g->I[(size_t)R.w * R.g->lay.istride + R.g->lay.iters];
-  Accs<MB> acc;
-  acc.zero(nbody);
-  for (int it = 0; it < iters; ++it) {
-    for (int k = k0; k < k0 + cnt; ++k) {
-      float* sc = wf + L.sc + SC * k;
-      const int la = wi[L.scid + 2 * k], lb = wi[L.scid + 2 * k + 1];
-      const float mu = sc[S_MU], reg = sc[S_REG];
-      const J6 an = ldj(sc + S_JA), bn = ldj(sc + S_JB);
-      const J6 at1 = ldj(sc + S_JA + 6), bt1 = ldj(sc + S_JB + 6), at2 = ldj(sc + S_JA + 12), bt2 = ldj(sc + S_JB + 12);
-      float* imp = sc + S_IMP;
-      float ima = 0.f, imb = 0.f;
-      S3 Ia{0, 0, 0, 0, 0, 0}, Ib{0, 0, 0, 0, 0, 0};
-      if (la >= 0) { const int b = wi[L.ibody + b0 + la]; ima = 1.f / wf[L.mass + b]; Ia = lds(wf + L.iinvw + 6 * b); }
-      if (lb >= 0) { const int b = wi[L.ibody + b0 + lb]; imb = 1.f / wf[L.mass + b]; Ib = lds(wf + L.iinvw + 6 * b); }
-      V3 dva = v3(0.f, 0.f, 0.f), dwa = dva, dvb = dva, dwb = dva;
-      if (la >= 0) acc.get(la, &dva, &dwa);
-      if (lb >= 0) acc.get(lb, &dvb, &dwb);
-      float im0 = imp[0], im1 = imp[1], im2 = imp[2], im3 = imp[3];
-      auto apply = [&](const J6& ja, const J6& jb, float dl) {
-        if (la >= 0) { dva = dva + ja.l * (dl * ima); dwa = dwa + smv(Ia, ja.a * dl); }
-        if (lb >= 0) { dvb = dvb + jb.l * (dl * imb); dwb = dwb + smv(Ib, jb.a * dl); }
+  const int stride = gridDim.x * WPB * 8;
+  for (int base = (blockIdx.x * WPB + wib) * 8; base < n_items; base += stride) {
+    const int t = base + slot;
+    int nbody = 0, cnt = 0, k0 = 0, b0 = 0, iters = 0;
+    float* wf = nullptr;
+    const int* wi = nullptr;
+    WsLay L{};
+    if (t < n_items) {
+      IslandRef R;
+      island_ref(G, wseg, ng, items[t], &R);
+      L = R.L;
+      wf = R.wf;
+      wi = R.wi;
+      nbody = wi[L.inb + R.isl];
+      cnt = wi[L.icount + R.isl];
+      k0 = wi[L.istart + R.isl];
+      b0 = wi[L.ibstart + R.isl];
+      iters = R.g->I[(size_t)R.w * R.g->lay.istride + R.g->lay.iters];
+    }
+    float* const sc0 = t < n_items ? wf + L.sc + SC * k0 : nullptr;
+    const int* const id0 = t < n_items ? wi + L.scid + 2 * k0 : nullptr;
+    for (int i = l; i < 6 * (nbody + 1); i += 4) (&acc[0][0])[i] = 0.f;
+    const int total = iters * cnt;
+    int tmax = total;
+#pragma unroll
+    for (int o = 4; o < 32; o <<= 1) tmax = max(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
+    __syncwarp();
+    QuadContact cur, nxt;
+    if (total > 0) quad_load(sc0, id0, side, l, nbody, cur);
+    else quad_zero(nbody, cur);
+    int k = 0;
+    for (int step = 0; step < tmax; ++step) {
+      const bool on = step < total;
+      // the next contact's values are fetched while this one is solved
+      const int kn = k + 1 == cnt ? 0 : k + 1;
+      if (step + 1 < total) quad_load(sc0 + (size_t)SC * kn, id0 + 2 * kn, side, l, nbody, nxt);
+      else quad_zero(nbody, nxt);
+      float a[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) a[c] = on ? acc[cur.body][3 * part + c] : 0.f;
+      float im[4] = {cur.imp[0], cur.imp[1], cur.imp[2], cur.imp[3]};
+      auto single = [&](int r) {
+        float d = dot3(cur.J[r], a);
+        d += __shfl_xor_sync(gm, d, 1);
+        d += __shfl_xor_sync(gm, d, 2);
+        const float res = d + (cur.reg * im[r] + cur.bias[r]);
+        const float nf = RowStep::nonneg(im[r], res, cur.idg[r]);
+        const float dl = nf - im[r];
+        im[r] = nf;
+        a[0] += cur.W[r][0] * dl;
+        a[1] += cur.W[r][1] * dl;
+        a[2] += cur.W[r][2] * dl;
       };
-      {
-        const J6 ja = jrow(an, at1, mu), jb = jrow(bn, bt1, mu);
-        const float res = jdot(ja, dva, dwa) + jdot(jb, dvb, dwb) + reg * im0 + sc[S_BIAS];
-        const float nf = RowStep::nonneg(im0, res, sc[S_IDIAG]);
-        const float dl = nf - im0;
-        im0 = nf;
-        apply(ja, jb, dl);
-      }
+      single(0);
 #pragma unroll
       for (int p = 0; p < 2; ++p) {
-        const J6& at = p ? at2 : at1;
-        const J6& bt = p ? bt2 : bt1;
-        const J6 jai = jrow(an, at, mu), jbi = jrow(bn, bt, mu), jaj = jrow(an, at, -mu), jbj = jrow(bn, bt, -mu);
         const int i = 2 * p, j = i + 1;
-        float& ii = p ? im2 : im0;
-        float& ij = p ? im3 : im1;
-        const float* P = sc + (p ? S_P1 : S_P0);
-        if (P[3] == 0.f) {
-          float res = jdot(jai, dva, dwa) + jdot(jbi, dvb, dwb) + reg * ii + sc[S_BIAS + i];
-          float nf = RowStep::nonneg(ii, res, sc[S_IDIAG + i]);
-          float dl = nf - ii;
-          ii = nf;
-          apply(jai, jbi, dl);
-          res = jdot(jaj, dva, dwa) + jdot(jbj, dvb, dwb) + reg * ij + sc[S_BIAS + j];
-          nf = RowStep::nonneg(ij, res, sc[S_IDIAG + j]);
-          dl = nf - ij;
-          ij = nf;
-          apply(jaj, jbj, dl);
+        const float* Pp = cur.P + 4 * p;
+        if (Pp[3] == 0.f) {  // uniform over the island's lanes
+          single(i);
+          single(j);
           continue;
         }
-        const float ri = jdot(jai, dva, dwa) + jdot(jbi, dvb, dwb) + reg * ii + sc[S_BIAS + i];
-        const float rj = jdot(jaj, dva, dwa) + jdot(jbj, dvb, dwb) + reg * ij + sc[S_BIAS + j];
+        float di = dot3(cur.J[i], a), dj = dot3(cur.J[j], a);
+        di += __shfl_xor_sync(gm, di, 1);
+        dj += __shfl_xor_sync(gm, dj, 1);
+        di += __shfl_xor_sync(gm, di, 2);
+        dj += __shfl_xor_sync(gm, dj, 2);
+        const float ri = di + (cur.reg * im[i] + cur.bias[i]);
+        const float rj = dj + (cur.reg * im[j] + cur.bias[j]);
         float ni, nj;
-        RowStep::pair(ii, ij, ri, rj, P, &ni, &nj);
-        const float ai = ni - ii, aj = nj - ij;
-        ii = ni; ij = nj;
-        apply(jai, jbi, ai);
-        apply(jaj, jbj, aj);
+        RowStep::pair(im[i], im[j], ri, rj, Pp, &ni, &nj);
+        const float ai = ni - im[i], aj = nj - im[j];
+        im[i] = ni;
+        im[j] = nj;
+        a[0] += cur.W[i][0] * ai;
+        a[1] += cur.W[i][1] * ai;
+        a[2] += cur.W[i][2] * ai;
+        a[0] += cur.W[j][0] * aj;
+        a[1] += cur.W[j][1] * aj;
+        a[2] += cur.W[j][2] * aj;
       }
-      imp[0] = im0; imp[1] = im1; imp[2] = im2; imp[3] = im3;
-      // write the two touched accumulators back
-      if (la >= 0) { V3 l0, w0; acc.get(la, &l0, &w0); acc.add(la, dva - l0, dwa - w0); }
-      if (lb >= 0) { V3 l0, w0; acc.get(lb, &l0, &w0); acc.add(lb, dvb - l0, dwb - w0); }
+      if (on) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) acc[cur.body][3 * part + c] = a[c];
+        if (l == 0) *reinterpret_cast<float4*>(sc0 + (size_t)SC * k + S_IMP) = make_float4(im[0], im[1], im[2], im[3]);
+        if (kn == k) {  // a one-contact island reads its own update back
+#pragma unroll
+          for (int r = 0; r < 4; ++r) nxt.imp[r] = im[r];
+        }
+        k = kn;
+      }
+      __syncwarp();
+      cur = nxt;
     }
-  }
-  for (int k = k0; k < k0 + cnt; ++k) {
-    const float* sc = wf + L.sc + SC * k;
-    float* cimp = wf + L.con + CF * wi[L.sccon + k] + C_IMP;
-    for (int r = 0; r < 4; ++r) cimp[r] = sc[S_IMP + r];
-  }
-  for (int b = 0; b < nbody; ++b) {
-    const int body = wi[L.ibody + b0 + b];
-    V3 l, w;
-    acc.get(b, &l, &w);
-    st3(wf + L.dv + 3 * body, l);
-    st3(wf + L.dw + 3 * body, w);
-  }
-  }
-}
-
-NEWT_D void axpy6r(float* a, const float* w, float s) {
-#pragma unroll
-  for (int q = 0; q < 6; ++q) a[q] += s * w[q];
-}
-NEWT_D float tdot6(const float* j, const float* a) {
-  return ((j[0] * a[0] + j[1] * a[1]) + (j[2] * a[2] + j[3] * a[3])) + (j[4] * a[4] + j[5] * a[5]);
-}
-
-// ---------------------------------------------------------------------------
-// K3a: multi-body islands, one thread per island, launched one warp per
-// block so that a class's islands spread over every SM and each SM's L1
-// keeps its warps' rows resident through all sweeps (the chain of dependent
-// row updates then waits on L1, not L2).  Body accumulators and impulses sit
-// in thread-local arrays indexed by the contact's island-local body ids; a
-// static side reads and writes a dummy slot (its rows are stored as zeros).
-// ---------------------------------------------------------------------------
-template <int MAXB, int MAXC>
-__global__ void __launch_bounds__(32) pile_k_pgs_lane(const PileGroupDev* G, const int* wseg, int ng,
-                                                      const int* items, const int* count, int cls) {
-  const int n_items = count[cls];
-  for (int t = blockIdx.x * 32 + threadIdx.x; t < n_items; t += gridDim.x * 32) {
-    IslandRef R;
-    island_ref(G, wseg, ng, items[t], &R);
-    const WsLay& L = R.L;
-    float* wf = R.wf;
-    const int* wi = R.wi;
-    const int isl = R.isl;
-    const int nbody = wi[L.inb + isl], cnt = wi[L.icount + isl];
-    const int k0 = wi[L.istart + isl], b0 = wi[L.ibstart + isl];
-    const int iters = R.g->I[(size_t)R.w * R.g->lay.istride + R.g->lay.iters];
-    float acc[MAXB + 1][6];
-    float impl[MAXC][4];
-    for (int b = 0; b <= MAXB; ++b)
-      for (int q = 0; q < 6; ++q) acc[b][q] = 0.f;
-    for (int k = 0; k < cnt; ++k)
-      for (int r = 0; r < 4; ++r) impl[k][r] = 0.f;
-    for (int it = 0; it < iters; ++it) {
-      for (int k = 0; k < cnt; ++k) {
-        const float* __restrict__ sc = wf + L.sc + SC * (k0 + k);
-        const int la = __ldg(wi + L.scid + 2 * (k0 + k)), lb = __ldg(wi + L.scid + 2 * (k0 + k) + 1);
-        const int ia = la >= 0 ? la : MAXB, ib = lb >= 0 ? lb : MAXB;
-        float rows[96];
-#pragma unroll
-        for (int q = 0; q < 96; ++q) rows[q] = __ldg(sc + S_ROWS + q);
-        const float reg = __ldg(sc + S_REG);
-        float idg[4], bias[4], imp[4], P[8];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) { idg[r] = __ldg(sc + S_IDIAG + r); bias[r] = __ldg(sc + S_BIAS + r); imp[r] = impl[k][r]; }
-#pragma unroll
-        for (int q = 0; q < 8; ++q) P[q] = __ldg(sc + S_P0 + q);
-        float aa[6], ab[6];
-#pragma unroll
-        for (int q = 0; q < 6; ++q) { aa[q] = acc[ia][q]; ab[q] = acc[ib][q]; }
-        auto resid = [&](int r) {
-          return (tdot6(rows + 24 * r, aa) + tdot6(rows + 24 * r + 12, ab)) + (reg * imp[r] + bias[r]);
-        };
-        auto apply = [&](int r, float dl) { axpy6r(aa, rows + 24 * r + 6, dl); axpy6r(ab, rows + 24 * r + 18, dl); };
-        {
-          const float nf = RowStep::nonneg(imp[0], resid(0), idg[0]);
-          const float dl = nf - imp[0];
-          imp[0] = nf;
-          apply(0, dl);
-        }
-#pragma unroll
-        for (int p = 0; p < 2; ++p) {
-          const int i = 2 * p, j = i + 1;
-          const float* Pp = P + 4 * p;
-          if (Pp[3] == 0.f) {
-            float nf = RowStep::nonneg(imp[i], resid(i), idg[i]);
-            float dl = nf - imp[i];
-            imp[i] = nf;
-            apply(i, dl);
-            nf = RowStep::nonneg(imp[j], resid(j), idg[j]);
-            dl = nf - imp[j];
-            imp[j] = nf;
-            apply(j, dl);
-            continue;
-          }
-          const float ri = resid(i), rj = resid(j);
-          float ni, nj;
-          RowStep::pair(imp[i], imp[j], ri, rj, Pp, &ni, &nj);
-          const float ai = ni - imp[i], aj = nj - imp[j];
-          imp[i] = ni; imp[j] = nj;
-          apply(i, ai);
-          apply(j, aj);
-        }
-#pragma unroll
-        for (int r = 0; r < 4; ++r) impl[k][r] = imp[r];
-#pragma unroll
-        for (int q = 0; q < 6; ++q) { acc[ia][q] = aa[q]; acc[ib][q] = ab[q]; }
+    if (t < n_items) {
+      for (int kk = l; kk < cnt; kk += 4) {
+        const float* s2 = sc0 + (size_t)SC * kk;
+        float* cimp = wf + L.con + CF * wi[L.sccon + k0 + kk] + C_IMP;
+        for (int r = 0; r < 4; ++r) cimp[r] = s2[S_IMP + r];
+      }
+      for (int b = l; b < nbody; b += 4) {
+        const int bd = wi[L.ibody + b0 + b];
+        st3(wf + L.dv + 3 * bd, v3(acc[b][0], acc[b][1], acc[b][2]));
+        st3(wf + L.dw + 3 * bd, v3(acc[b][3], acc[b][4], acc[b][5]));
       }
     }
-    for (int k = 0; k < cnt; ++k) {
-      float* cimp = wf + L.con + CF * wi[L.sccon + k0 + k] + C_IMP;
-      for (int r = 0; r < 4; ++r) cimp[r] = impl[k][r];
-    }
-    for (int b = 0; b < nbody; ++b) {
-      const int body = wi[L.ibody + b0 + b];
-      st3(wf + L.dv + 3 * body, v3(acc[b][0], acc[b][1], acc[b][2]));
-      st3(wf + L.dw + 3 * body, v3(acc[b][3], acc[b][4], acc[b][5]));
-    }
+    __syncwarp();
   }
 }
 
@@ -771,14 +706,25 @@ extern "C" size_t newt_pile_ws_bytes(int nb, int np, int maxc) {
 }
 
 // Kernel attributes and resident-grid sizes (called outside stream capture).
-static int cap128 = 4096, capl = 2432;
+static int cap128 = 4096, capq[4] = {1216, 1216, 1216, 304};
+
+// the multi-body island kernels of classes 3-6: bodies per island, warps per block
+#define NEWT_QUAD_KERNELS(X) X(3, 4, 4) X(4, CH_MIN, 4) X(5, CH_MAXC + 1, 4) X(6, NEWT_MAX_BODIES, 2)
+
 extern "C" void newt_pile_init() {
   int dev = 0, sms = 1, b1 = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, pile_k_pgs_small<4>, 128, 0);
   cap128 = sms * (b1 > 0 ? b1 : 1) * 2;
-  capl = sms * 16;  // one-warp blocks of the lane kernels, spread over every SM
+#define OCC(cl, mb, wpb)                                                                  \
+  {                                                                                       \
+    int b = 1;                                                                            \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pile_k_pgs_quad<mb, wpb>, 32 * wpb, 0); \
+    capq[cl - 3] = sms * (b > 0 ? b : 1);                                                 \
+  }
+  NEWT_QUAD_KERNELS(OCC)
+#undef OCC
 }
 
 // Bytes of the island work lists for `slots` island slots.
@@ -787,16 +733,20 @@ extern "C" size_t newt_pile_list_bytes(int slots) { return ((size_t)N_ICLASS * (
 // Launches the solver of island class `cl` on stream `s`; list kernels loop
 // over their items, so their grids are sized to the resident capacity.
 static void launch_class(int cl, const PileGroupDev* dG, const int* dwseg, int ng, const IslandLists& il, int grid,
-                         int gridl, cudaStream_t s) {
+                         cudaStream_t s) {
   const int* items = il.items + (size_t)cl * il.cap;
   switch (cl) {
     case 0: pile_k_pgs_small<1><<<grid, 128, 0, s>>>(dG, dwseg, ng, items, il.counts, cl); break;
     case 1: pile_k_pgs_small<2><<<grid, 128, 0, s>>>(dG, dwseg, ng, items, il.counts, cl); break;
     case 2: pile_k_pgs_small<4><<<grid, 128, 0, s>>>(dG, dwseg, ng, items, il.counts, cl); break;
-    case 3: pile_k_pgs_lane<4, CH_MIN - 1><<<gridl, 32, 0, s>>>(dG, dwseg, ng, items, il.counts, cl); break;
-    case 4: pile_k_pgs_lane<CH_MIN, CH_MIN - 1><<<gridl, 32, 0, s>>>(dG, dwseg, ng, items, il.counts, cl); break;
-    case 5: pile_k_pgs_lane<CH_MAXC + 1, CH_MAXC><<<gridl, 32, 0, s>>>(dG, dwseg, ng, items, il.counts, cl); break;
-    default: pile_k_pgs_multi<0><<<grid, 128, 0, s>>>(dG, dwseg, ng, items, il.counts, cl); break;
+#define LAUNCH(c, mb, wpb)                                                                                   \
+  case c:                                                                                                    \
+    pile_k_pgs_quad<mb, wpb><<<std::min((il.cap + 8 * wpb - 1) / (8 * wpb), capq[c - 3]), 32 * wpb, 0, s>>>( \
+        dG, dwseg, ng, items, il.counts, cl);                                                                \
+    break;
+    NEWT_QUAD_KERNELS(LAUNCH)
+#undef LAUNCH
+    default: break;
   }
 }
 
@@ -831,16 +781,15 @@ extern "C" int newt_launch_pile_step(const PileGroupDev* dG, const int* dwseg, i
   mark(0, 1, st);
   // list kernels loop over their items: grids sized to the resident capacity
   const int grid = std::min((total_slots + 127) / 128, cap128);
-  const int gridl = std::min((total_slots + 31) / 32, capl);
   cudaEventRecord(ev[0], st);
   for (int k = 0; k < 3; ++k) cudaStreamWaitEvent(side[k], ev[0], 0);
   // stream of each island class: the chain class first on `st`
   const int order[N_ICLASS] = {5, 6, 3, 4, 2, 1, 0};
-  const cudaStream_t on[N_ICLASS] = {st, st, side[0], side[0], side[1], side[2], side[2]};
+  const cudaStream_t on[N_ICLASS] = {st, side[1], side[0], side[0], side[1], side[2], side[2]};
   for (int i = 0; i < N_ICLASS; ++i) {
     const int cl = order[i];
     mark(1 + cl, 0, on[i]);
-    launch_class(cl, dG, dwseg, ng, il, grid, gridl, on[i]);
+    launch_class(cl, dG, dwseg, ng, il, grid, on[i]);
     mark(1 + cl, 1, on[i]);
   }
   for (int k = 0; k < 3; ++k) {
@@ -859,12 +808,11 @@ extern "C" int newt_launch_pile_step(const PileGroupDev* dG, const int* dwseg, i
 extern "C" cudaError_t newt_pile_prepare_kernels() {
   newt_pile_init();
   cudaFuncAttributes a;
-  const void* fns[] = {(const void*)pile_k_collide,
-                       (const void*)pile_k_pgs_small<4>,    (const void*)pile_k_pgs_small<2>,
-                       (const void*)pile_k_pgs_small<1>,    (const void*)pile_k_pgs_lane<4, CH_MIN - 1>,
-                       (const void*)pile_k_pgs_lane<CH_MIN, CH_MIN - 1>,
-                       (const void*)pile_k_pgs_lane<CH_MAXC + 1, CH_MAXC>,
-                       (const void*)pile_k_pgs_multi<0>,    (const void*)pile_k_integrate};
+  const void* fns[] = {(const void*)pile_k_collide,       (const void*)pile_k_pgs_small<4>,
+                       (const void*)pile_k_pgs_small<2>,    (const void*)pile_k_pgs_small<1>,
+                       (const void*)pile_k_pgs_quad<4, 4>,  (const void*)pile_k_pgs_quad<CH_MIN, 4>,
+                       (const void*)pile_k_pgs_quad<CH_MAXC + 1, 4>, (const void*)pile_k_pgs_quad<NEWT_MAX_BODIES, 2>,
+                       (const void*)pile_k_integrate};
   for (const void* f : fns) {
     cudaError_t e = cudaFuncGetAttributes(&a, f);
     if (e != cudaSuccess) return e;
@@ -886,8 +834,7 @@ extern "C" int newt_launch_pile_step_serial(const PileGroupDev* dG, const int* d
   const int wpb = 4;
   pile_k_collide<<<(total_worlds + wpb - 1) / wpb, 32 * wpb, 0, st>>>(dG, dwseg, ng, total_worlds, il);
   const int grid = std::min((total_slots + 127) / 128, cap128);
-  const int gridl = std::min((total_slots + 31) / 32, capl);
-  for (int cl = N_ICLASS - 1; cl >= 0; --cl) launch_class(cl, dG, dwseg, ng, il, grid, gridl, st);
+  for (int cl = N_ICLASS - 1; cl >= 0; --cl) launch_class(cl, dG, dwseg, ng, il, grid, st);
   pile_k_integrate<<<(total_worlds + wpb - 1) / wpb, 32 * wpb, 0, st>>>(dG, dwseg, ng, total_worlds, write_diag);
   return N_ICLASS + 2;
 }

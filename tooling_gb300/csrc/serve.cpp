@@ -138,6 +138,7 @@ extern "C" NEWT_API int newt_gpu_serve(newt_gpu_ctx* ctx, newt_serve_request* re
         if (rc2 != NEWT_OK) return bail(rc2);
       }
     }
+    stats->admit_s += now() - tn;
     if (active.empty()) {
       if (next < order.size() && real_time) {  // idle until the next arrival
         const double wait = reqs[order[next]].arrival_s - now();
@@ -146,6 +147,7 @@ extern "C" NEWT_API int newt_gpu_serve(newt_gpu_ctx* ctx, newt_serve_request* re
       continue;
     }
     // ---- tick: controls for the active requests, then one env-step ----
+    const double tc = now();
     slots.clear();
     qf.clear();
     for (const Active& a : active) {
@@ -158,8 +160,13 @@ extern "C" NEWT_API int newt_gpu_serve(newt_gpu_ctx* ctx, newt_serve_request* re
       int rc = newt_gpu_set_qfrc(ctx, slots.data(), (int32_t)slots.size(), qf.data());
       if (rc != NEWT_OK) return bail(rc);
     }
+    const double ts = now();
+    stats->ctrl_s += ts - tc;
     int rc = newt_gpu_step(ctx, 1, mode);
+    if (rc == NEWT_OK) rc = newt_gpu_sync(ctx, 600000);
     if (rc != NEWT_OK) return bail(rc);
+    const double te = now();
+    stats->step_s += te - ts;
     stats->ticks += 1;
     active_sum += (double)active.size();
     stats->peak_active = std::max<int32_t>(stats->peak_active, (int32_t)active.size());
@@ -170,6 +177,7 @@ extern "C" NEWT_API int newt_gpu_serve(newt_gpu_ctx* ctx, newt_serve_request* re
       if (active[k].t >= reqs[active[k].req].horizon) fin.push_back(k);
     }
     if (fin.empty()) continue;
+    const double tf = now();
     slots.clear();
     int32_t tq = 0, tv = 0;
     for (size_t k : fin) { slots.push_back(active[k].slot); tq += active[k].nq; tv += active[k].nv; }
@@ -200,6 +208,7 @@ extern "C" NEWT_API int newt_gpu_serve(newt_gpu_ctx* ctx, newt_serve_request* re
       keep.push_back(active[k]);
     }
     active.swap(keep);
+    stats->complete_s += now() - tf;
   }
   stats->completed = done;
   stats->wall_s = now();
