@@ -251,3 +251,54 @@ def test_tree_chain_contact_euler_matches_mujoco_capture(precision, solver, name
         worst_q = max(worst_q, np.abs(qo - ref["qpos"][k]).max())
         worst_v = max(worst_v, np.abs(vo - ref["qvel"][k]).max())
     assert worst_q <= qtol and worst_v <= vtol, (worst_q, worst_v)
+
+
+def _free_body_scene(name):
+    """The free-body differential scenes as newt's MJCF loader builds them:
+    a free-jointed top-level body without children becomes a World body
+    (newt/src/mjcf.rs:889-1010), geoms at the body origin, default solref
+    and solimp, margin 0, condim 3; initial state from scenarios.json.
+    Returns (model, qpos0, qvel0) in MuJoCo layout."""
+    if name == "ballistic":  # tests/references/ballistic.xml
+        w = M.WorldModel(dt=0.005, gravity=(0.0, 0.0, -9.81), solver=M.SOLVER_PGS, iterations=20)
+        w.add_body(1.0, M._diag9(0.05, 0.06, 0.07))
+        return w, [0.1, -0.2, 3.0, 1.0, 0.0, 0.0, 0.0], [3.0, -1.5, 5.0, 0.0, 0.0, 0.0]
+    w = M.WorldModel(dt=0.002, gravity=(0.0, 0.0, -9.81), solver=M.SOLVER_PGS, iterations=20)
+    if name == "sphere_drop":  # tests/references/sphere_drop.xml
+        w.add_geom(M.static_plane(friction=0.8))
+        b = w.add_body(0.5, M._diag9(0.002, 0.002, 0.002))
+        w.add_geom(M.Geom(shape=M.SHAPE_SPHERE, body=b, size=(0.1, 0.0, 0.0), friction=0.8))
+        return w, [0.0, 0.0, 0.6, 1.0, 0.0, 0.0, 0.0], [0.0] * 6
+    assert name == "box_stack"  # tests/references/box_stack.xml
+    w.add_geom(M.static_plane(friction=0.6))
+    qpos = []
+    for mass, inert, pos in ((1.2, 0.098, (0.0, 0.0, 0.5)), (0.9, 0.0735, (0.02, 0.0, 1.25)),
+                             (1.5, 0.1225, (0.0, 0.0, 2.0))):
+        b = w.add_body(mass, M._diag9(inert, inert, inert))
+        w.add_geom(M.Geom(shape=M.SHAPE_BOX, body=b, size=(0.35, 0.35, 0.35), friction=0.6))
+        qpos += list(pos) + [1.0, 0.0, 0.0, 0.0]
+    return w, qpos, [0.0] * 18
+
+
+# matched-Euler windows against MuJoCo 3.11.0 (newt/tests/differential.rs:1272-1295)
+FREE_BODY_WINDOWS = [("ballistic", 3.0e-5, 8.0e-5), ("sphere_drop", 1.5e-2, 9.0e-1), ("box_stack", 2.0e-2, 5.0e-1)]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("name,qtol,vtol", FREE_BODY_WINDOWS)
+def test_free_body_euler_matches_mujoco_capture(precision, name, qtol, vtol):
+    """Free-body rows of newt's matched-Euler differential test
+    (differential.rs:1593-1599): the pile path's integrator, contacts and PGS
+    stay inside newt's own windows against the MuJoCo captures."""
+    ref = read_newtdif(f"{name}_euler.bin")
+    w, q0, v0 = _free_body_scene(name)
+    packed = M.PackedModels([w])
+    qpos = np.array(q0, np.float32)
+    qvel = np.array(v0, np.float32)
+    assert np.abs(qpos - ref["qpos"][0]).max() < 1e-7 and np.abs(qvel - ref["qvel"][0]).max() == 0
+    worst_q = worst_v = 0.0
+    for k, step in enumerate(ref["steps"]):
+        qo, vo = oracle_py.run(packed, np.zeros(1, np.int32), qpos, qvel, None, step, precision=precision)
+        worst_q = max(worst_q, np.abs(qo - ref["qpos"][k]).max())
+        worst_v = max(worst_v, np.abs(vo - ref["qvel"][k]).max())
+    assert worst_q <= qtol and worst_v <= vtol, (worst_q, worst_v)

@@ -569,19 +569,17 @@ __global__ void __launch_bounds__(32 * WPB) pile_k_pgs_quad(const PileGroupDev* 
 #pragma unroll
     for (int o = 4; o < 32; o <<= 1) tmax = max(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
     __syncwarp();
-    QuadContact cur, nxt;
-    if (total > 0) quad_load(sc0, id0, side, l, nbody, cur);
-    else quad_zero(nbody, cur);
     int k = 0;
-    for (int step = 0; step < tmax; ++step) {
+    // one contact of the sweep; the next contact's values are fetched into
+    // `nxt` while `cur` is solved (the loop below alternates the two)
+    auto contact = [&](int step, QuadContact& cur, QuadContact& nxt) {
       const bool on = step < total;
-      // the next contact's values are fetched while this one is solved
       const int kn = k + 1 == cnt ? 0 : k + 1;
       if (step + 1 < total) quad_load(sc0 + (size_t)SC * kn, id0 + 2 * kn, side, l, nbody, nxt);
-      else quad_zero(nbody, nxt);
+      const int body = on ? cur.body : 0;
       float a[3];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) a[c] = on ? acc[cur.body][3 * part + c] : 0.f;
+      for (int c = 0; c < 3; ++c) a[c] = on ? acc[body][3 * part + c] : 0.f;
       float im[4] = {cur.imp[0], cur.imp[1], cur.imp[2], cur.imp[3]};
       auto single = [&](int r) {
         float d = dot3(cur.J[r], a);
@@ -626,7 +624,7 @@ __global__ void __launch_bounds__(32 * WPB) pile_k_pgs_quad(const PileGroupDev* 
       }
       if (on) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) acc[cur.body][3 * part + c] = a[c];
+        for (int c = 0; c < 3; ++c) acc[body][3 * part + c] = a[c];
         if (l == 0) *reinterpret_cast<float4*>(sc0 + (size_t)SC * k + S_IMP) = make_float4(im[0], im[1], im[2], im[3]);
         if (kn == k) {  // a one-contact island reads its own update back
 #pragma unroll
@@ -635,7 +633,14 @@ __global__ void __launch_bounds__(32 * WPB) pile_k_pgs_quad(const PileGroupDev* 
         k = kn;
       }
       __syncwarp();
-      cur = nxt;
+    };
+    QuadContact c0, c1;
+    if (total > 0) quad_load(sc0, id0, side, l, nbody, c0);
+    else quad_zero(nbody, c0);
+    quad_zero(nbody, c1);
+    for (int step = 0; step < tmax; step += 2) {
+      contact(step, c0, c1);
+      if (step + 1 < tmax) contact(step + 1, c1, c0);
     }
     if (t < n_items) {
       for (int kk = l; kk < cnt; kk += 4) {
