@@ -629,41 +629,67 @@ def cpu_baseline(batch, qpos, qvel, S, n_worlds=256, steps=500):
 
 
 def run_reference(args, rank, ws, local, dist):
+    """newt's algorithm on the host cores for the chosen workload: the float
+    restatement (newt is Rust and cannot be built here), all host threads, a
+    bounded sample of the workload's worlds advancing `substeps` env-steps per
+    bench step from the GPU arm's start phase."""
     if rank != 0:
         return None
     from tooling_gb300 import scenes
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py
-    n = min(args.worlds, 256)
-    batch = scenes.pile_batch(n_worlds=n)
     cores = os.cpu_count() or 1
+    line = {"impl": "reference", "metric": "env-steps/s", "unit": "env-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator)"}
+    if args.workload == "serve":
+        line["unavailable"] = ("newt has no serving loop; its per-world step on the host cores is timed by "
+                               "--impl reference --workload uneven")
+        return line
+    S, qfrc = args.substeps, None
+    if args.workload == "quadruped":
+        n, S = min(args.worlds, 64), 20
+        batch = scenes.quadruped_batch(n_worlds=n)
+        qfrc = scenes.quadruped_controls(n, 0)
+        config = {"workload": "quadruped: 13-link trees on a plane, Newton <= 20, dt 2e-3",
+                  "worlds_per_gpu": args.worlds}
+    elif args.workload == "uneven":
+        n = min(args.worlds, 256)
+        batch = scenes.uneven_batch(n_worlds=n)
+        qfrc = batch.qfrc
+        config = {"workload": "uneven: 50/50 chains and piles, 2..64 bodies log-uniform, PGS 50, dt 2e-3",
+                  "worlds_per_gpu": args.worlds}
+    else:
+        n = min(args.worlds, 256)
+        batch = scenes.pile_batch(n_worlds=n)
+        config = {"workload": "pile: free spheres/boxes on a plane, PGS 50 iterations, dt 2e-3",
+                  "worlds_per_gpu": args.worlds, "bodies_per_world": 16}
+    idx = np.arange(n)
     # advance the sample to the GPU arm's start phase (its warm-up horizon), untimed
-    qo, vo = oracle_py.run(batch, np.arange(n), batch.qpos, batch.qvel, None, max(3, args.warmup) * args.substeps,
-                           precision=0, n_threads=cores)
+    qo, vo = oracle_py.run(batch, idx, batch.qpos, batch.qvel, qfrc, max(3, args.warmup) * S, precision=0,
+                           n_threads=cores)
     qp, qv = qo.astype(np.float32), vo.astype(np.float32)
     vals = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        qo, vo = oracle_py.run(batch, np.arange(n), qp, qv, None, args.substeps, precision=0, n_threads=cores)
-        vals.append(n * args.substeps / (time.perf_counter() - t0))
+        qo, vo = oracle_py.run(batch, idx, qp, qv, qfrc, S, precision=0, n_threads=cores)
+        vals.append(n * S / (time.perf_counter() - t0))
         qp, qv = qo.astype(np.float32), vo.astype(np.float32)
     v = statistics.median(vals)
-    r = {"cores": cores, "sample": f"{n} pile worlds x {args.substeps} env-steps per step, advancing from the GPU "
-                                   f"arm's start phase, f32 restatement of newt's step, {cores} host threads"}
-    return {"impl": "reference", "metric": "env-steps/s", "value": v, "unit": "env-steps/s", "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
-            "config": {"workload": "pile: free spheres/boxes on a plane, PGS 50 iterations, dt 2e-3",
-                       "worlds_per_gpu": args.worlds, "bodies_per_world": 16},
-            "cpu_baseline": {"value": v, "unit": "env-steps/s", "cores": r["cores"], "kind": "port",
-                             "sample": r["sample"] + "; newt is Rust and cannot be built here (no cargo), so its "
-                                                     "arithmetic runs through the byte-identical C++ restatement"},
-            "e2e": {"value": v, "unit": "env-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    sample = (f"{n} worlds x {S} env-steps per step, advancing from the GPU arm's start phase, f32 restatement of "
+              f"newt's step, {cores} host threads; newt is Rust and cannot be built here (no cargo), so its "
+              f"arithmetic runs through the byte-identical C++ restatement")
+    line.update({"value": v, "config": config,
+                 "cpu_baseline": {"value": v, "unit": "env-steps/s", "cores": cores, "kind": "port", "sample": sample},
+                 "e2e": {"value": v, "unit": "env-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+    return line
 
 
 def main():
     args = parse()
     rank, ws, local, dist = dist_setup()
+    if "--worlds" not in sys.argv:  # each workload's configured world count
+        args.worlds = {"uneven": 32768, "quadruped": 16384}.get(args.workload, args.worlds)
     if args.impl == "reference":
         out = run_reference(args, rank, ws, local, dist)
         if out is not None:
@@ -675,15 +701,11 @@ def main():
             print(json.dumps(out))
         return
     if args.workload == "uneven":
-        if args.worlds == 8192 and "--worlds" not in sys.argv:
-            args.worlds = 32768
         out = run_gpu_uneven(args, rank, ws, local, dist)
         if rank == 0:
             print(json.dumps(out))
         return
     if args.workload == "quadruped":
-        if args.worlds == 8192 and "--worlds" not in sys.argv:
-            args.worlds = 16384
         out, (batch, qp, qv, qf) = run_gpu_quadruped(args, rank, ws, local, dist)
         if rank == 0:
             if not args.no_cpu and ws == 1:

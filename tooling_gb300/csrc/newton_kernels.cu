@@ -136,9 +136,13 @@ NEWT_HD TcLay tc_layout(int L, int nv, int ng, int maxc) {
 // link COM Jacobians and inertias and later the Newton factor, and the
 // Jacobian rows (overwritten in place by Y = L^-1 J^T).  The tile and the rows
 // live here when the active rows fit NRS (sequential Cholesky and
-// triangular-solve steps then wait on shared memory instead of L2).
+// triangular-solve steps then wait on shared memory instead of L2).  NRS
+// trades the tile against residency: 20 rows (five contacts; a standing
+// quadruped has about two) keep the block at ~12 KB, 18 warps per SM; a
+// sweep of 48/32/24/20/16 rows on 16384 quadrupeds gave 7.2/7.1/8.0/8.2/8.1M
+// env-steps/s.
 enum { V_X = 0, V_D, V_G, V_B, V_REG, V_DIAG, V_U, V_V, V_P, V_S, N_VEC };
-constexpr int NRS = 48;
+constexpr int NRS = 20;
 struct TcSmem { int vl, ldr, nrs, vec, rmap, pose, lm, ldf, tw, lh, jy, words; };
 NEWT_HD TcSmem tc_smem(int L, int nv, int maxc) {
   TcSmem m;
