@@ -179,6 +179,7 @@ def run_gpu(args, rank, ws, local, dist):
     per_step = []
     kernel_ms = {}
     work = None
+    n_launch = 0  # launches of each pile kernel in the timed region
     barrier(dist)
     eng.sync()
     for _ in range(args.steps):
@@ -188,6 +189,7 @@ def run_gpu(args, rank, ws, local, dist):
         eng.event(1)
         per_step.append(eng.elapsed_ms())
         kms, work = eng.pile_profile()
+        n_launch += work["launches"]
         for k, v in kms.items():
             kernel_ms[k] = kernel_ms.get(k, 0.0) + v
     eng.sync()
@@ -229,14 +231,14 @@ def run_gpu(args, rank, ws, local, dist):
         plain = W * S * args.steps / (pms / 1e3)
     hbm, src = peaks()
     avg_ms = total_ms / args.steps
-    n_launch = args.steps * S  # launches of each pile kernel in the timed region
+    branches = n_launch / (args.steps * S)  # world-range branches per env-step
     dom = max(kernel_ms, key=kernel_ms.get)
     dom_ms = kernel_ms[dom] / n_launch
-    alg = pile_kernel_bytes(dom, W, int(batch.n_bodies[0]), work)
+    alg = pile_kernel_bytes(dom, W, int(batch.n_bodies[0]), work) / branches
     achieved = alg / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else None
     tot_k = sum(kernel_ms.values())
     kernels = {k: {"ms_per_launch": v / n_launch, "share": v / tot_k if tot_k else None,
-                   "algorithmic_bytes": pile_kernel_bytes(k, W, int(batch.n_bodies[0]), work)}
+                   "algorithmic_bytes": pile_kernel_bytes(k, W, int(batch.n_bodies[0]), work) / branches}
                for k, v in kernel_ms.items()}
     out = {
         "metric": "env-steps/s", "value": value, "unit": "env-steps/s", "n_gpus": ws, "steps": args.steps,
@@ -244,7 +246,8 @@ def run_gpu(args, rank, ws, local, dist):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
         "config": {"workload": "pile: 16 free spheres/boxes on a plane per world, PGS 50 iterations, dt 2e-3",
                    "worlds_per_gpu": W, "bodies_per_world": 16, "env_steps_per_bench_step": S,
-                   "mode": "batched (8 kernels per env-step, island classes on 3 forked streams, CUDA graph)",
+                   "mode": "batched: 9 kernels per env-step and world-range branch, branches and island classes "
+                           "on forked streams, CUDA graph",
                    "l2": "flushed between timed steps", "parallelism": f"replicas x{ws}"},
         "e2e": {"value": e2e, "unit": "env-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
@@ -406,7 +409,7 @@ def run_gpu_uneven(args, rank, ws, local, dist):
     launches0 = eng.launch_count()
     clocks = Clocks(local)
     clocks.start()
-    per_step, kernel_ms, work = [], {}, None
+    per_step, kernel_ms, work, n_launch = [], {}, None, 0
     barrier(dist)
     eng.sync()
     for _ in range(args.steps):
@@ -416,6 +419,7 @@ def run_gpu_uneven(args, rank, ws, local, dist):
         eng.event(1)
         per_step.append(eng.elapsed_ms())
         kms, work = eng.pile_profile()
+        n_launch += work["launches"]
         for k, v in kms.items():
             kernel_ms[k] = kernel_ms.get(k, 0.0) + v
     eng.sync()
@@ -451,13 +455,13 @@ def run_gpu_uneven(args, rank, ws, local, dist):
     eng.sync()
     e2e = W * S * args.steps * ws / max_over_ranks(dist, time.perf_counter() - t0)
     hbm, src = peaks()
-    n_launch = args.steps * S
+    branches = n_launch / (args.steps * S) if n_launch else 1.0
     dom = max(kernel_ms, key=kernel_ms.get)
-    dom_ms = kernel_ms[dom] / n_launch
+    dom_ms = kernel_ms[dom] / max(n_launch, 1)
     n_piles = int((batch.n_bodies > 0).sum())
-    # pile kernels see the pile worlds only; 16-body rows stand in for the mean body count
+    # pile kernels see the pile worlds only; the mean body count stands in for every world's
     mean_nb = int(round(float(batch.n_bodies[batch.n_bodies > 0].mean()))) if n_piles else 0
-    alg = pile_kernel_bytes(dom, n_piles, mean_nb, work)
+    alg = pile_kernel_bytes(dom, n_piles, mean_nb, work) / branches
     achieved = alg / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else None
     out = {
         "metric": "env-steps/s", "value": value, "unit": "env-steps/s", "n_gpus": ws, "steps": args.steps,

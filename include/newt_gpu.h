@@ -259,14 +259,17 @@ NEWT_API int newt_gpu_serve(newt_gpu_ctx* ctx, newt_serve_request* reqs, int32_t
  * Outputs (each nullable) describe the last newt_gpu_step call, after waiting
  * for it:
  *   kernel_ms[NEWT_PILE_KERNELS]  device time of each pile kernel summed over
- *       that call's env-steps, in launch-table order: collide, the solvers of
- *       island classes 0..5, integrate (zeros unless timing was on for a
+ *       that call's launches, in launch-table order: collide, the solvers of
+ *       island classes 0..6, integrate (zeros unless timing was on for a
  *       batched step);
  *   work[3 * NEWT_PILE_ISLAND_CLASSES]  islands, then contacts, then bodies
- *       per island class in that call's last env-step. */
+ *       per island class in that call's last env-step;
+ *   launches  launches of each kernel summed in kernel_ms (env-steps times
+ *       the world-range branches of the batched form). */
 #define NEWT_PILE_KERNELS 9
 #define NEWT_PILE_ISLAND_CLASSES 7
-NEWT_API int newt_gpu_pile_profile(newt_gpu_ctx* ctx, int32_t enable, float* kernel_ms, int32_t* work);
+NEWT_API int newt_gpu_pile_profile(newt_gpu_ctx* ctx, int32_t enable, float* kernel_ms, int32_t* work,
+                                   int32_t* launches);
 
 /* Profiling surface of the tree-contact step (quadruped worlds).  With
  * timing on (newt_gpu_pile_profile's `enable`), every tree-contact env-step

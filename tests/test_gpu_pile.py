@@ -150,3 +150,20 @@ def test_free_body_scenes_within_mujoco_windows(eng, name, qtol, vtol, mode):
         worst_v = max(worst_v, np.abs(v - ref["qvel"][k]).max())
     eng.free(slots)
     assert worst_q <= qtol and worst_v <= vtol, (worst_q, worst_v)
+
+
+def test_world_range_branches_match_plain(eng):
+    """Past 4096 pile worlds the batched form splits every group into
+    world-range branches on their own streams; each world's arithmetic is
+    unchanged, so batched and plain agree bit for bit."""
+    b = scenes.pile_batch(n_worlds=8300, first_world=9000)
+    slots = _load(eng, b)
+    nq, nv = int(b.nq.sum()), int(b.nv.sum())
+    eng.step(30, STEP_BATCHED)
+    qb, vb = eng.get_state(slots, nq, nv)
+    eng.set_state(slots, b.qpos, b.qvel)
+    eng.step(30, STEP_PLAIN)
+    qp, vp = eng.get_state(slots, nq, nv)
+    eng.free(slots)
+    np.testing.assert_array_equal(qb, qp)
+    np.testing.assert_array_equal(vb, vp)

@@ -106,7 +106,7 @@ def load_library(path: str = LIB_PATH):
         "newt_gpu_flush_l2": ([P], C.c_int),
         "newt_gpu_launch_count": ([P], C.c_int64),
         "newt_gpu_step_static": ([P, I32], C.c_int),
-        "newt_gpu_pile_profile": ([P, I32, P, P], C.c_int),
+        "newt_gpu_pile_profile": ([P, I32, P, P, P], C.c_int),
         "newt_gpu_tc_profile": ([P, P], C.c_int),
         "newt_gpu_serve": ([P, P, I32, P, P], C.c_int),
         "newt_gpu_memory": ([P, P, P], C.c_int),
@@ -300,11 +300,14 @@ class Engine:
         return dict(zip(TC_KERNELS, ms.tolist()))
 
     def pile_profile(self, enable: int = -1):
-        """(per-kernel ms of the last step call, {islands, contacts, bodies} per
-        island class of its last env-step); enable 1/0 switches kernel timing
-        for later batched steps, -1 leaves it."""
+        """(per-kernel ms summed over the last step call's launches, {islands,
+        contacts, bodies per island class of its last env-step, launches per
+        kernel}); enable 1/0 switches kernel timing for later batched steps,
+        -1 leaves it."""
         ms = np.zeros(len(PILE_KERNELS), np.float32)
         work = np.zeros(3 * PILE_ISLAND_CLASSES, np.int32)
-        self._ck(self.L.newt_gpu_pile_profile(self.ctx, int(enable), _p(ms), _p(work)))
+        n = C.c_int32()
+        self._ck(self.L.newt_gpu_pile_profile(self.ctx, int(enable), _p(ms), _p(work), C.byref(n)))
         w = work.reshape(3, PILE_ISLAND_CLASSES)
-        return dict(zip(PILE_KERNELS, ms.tolist())), {"islands": w[0], "contacts": w[1], "bodies": w[2]}
+        return dict(zip(PILE_KERNELS, ms.tolist())), {"islands": w[0], "contacts": w[1], "bodies": w[2],
+                                                      "launches": n.value}

@@ -487,8 +487,9 @@ __global__ void __launch_bounds__(128) pile_k_pgs_small(const PileGroupDev* G, c
 // a triple dot product summed over the four lanes (two shuffles; a 2x2 pair
 // sums both rows at once), every lane takes the same scalar step and updates
 // its own triple.  Body accumulators live in shared memory (island-local
-// ids, a dummy slot for a static side), impulses in the solver record.  The
-// warp runs until its longest island is done; finished islands idle.
+// ids, a dummy slot for a static side), and so do the impulses of islands
+// within the class's contact bound (the solver record holds them otherwise).
+// The warp runs until its longest island is done; finished islands idle.
 // ---------------------------------------------------------------------------
 NEWT_D float dot3(const float* j, const float* a) { return (j[0] * a[0] + j[1] * a[1]) + j[2] * a[2]; }
 NEWT_D float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
@@ -501,7 +502,8 @@ struct QuadContact {
   int body;
 };
 
-NEWT_D void quad_load(const float* sc, const int* ids, int side, int l, int dummy, QuadContact& c) {
+NEWT_D void quad_load(const float* sc, const float4* imp, const int* ids, int side, int l, int dummy,
+                      QuadContact& c) {
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     const float4 j = ldg4(sc + S_ROWS + 32 * r + 4 * l), w = ldg4(sc + S_ROWS + 32 * r + 16 + 4 * l);
@@ -514,7 +516,7 @@ NEWT_D void quad_load(const float* sc, const int* ids, int side, int l, int dumm
   c.P[0] = p0.x; c.P[1] = p0.y; c.P[2] = p0.z; c.P[3] = p0.w;
   c.P[4] = p1.x; c.P[5] = p1.y; c.P[6] = p1.z; c.P[7] = p1.w;
   c.reg = __ldg(sc + S_REG);
-  const float4 m = *reinterpret_cast<const float4*>(sc + S_IMP);  // written by this kernel in the previous sweep
+  const float4 m = *imp;  // written by this kernel in the previous sweep
   c.imp[0] = m.x; c.imp[1] = m.y; c.imp[2] = m.z; c.imp[3] = m.w;
   const int id = __ldg(ids + side);
   c.body = id >= 0 ? id : dummy;
@@ -533,10 +535,13 @@ NEWT_D void quad_zero(int dummy, QuadContact& c) {
   c.body = dummy;
 }
 
-template <int MAXB, int WPB>
+// MAXB: bodies per island; MAXC > 0: contacts per island, whose impulses are
+// then kept in shared memory (0: in the solver record); WPB: warps per block.
+template <int MAXB, int MAXC, int WPB>
 __global__ void __launch_bounds__(32 * WPB) pile_k_pgs_quad(const PileGroupDev* G, const int* wseg, int ng,
                                                             const int* items, const int* count, int cls) {
   __shared__ float acc_s[WPB][8][MAXB + 1][6];
+  __shared__ float4 imp_s[WPB][8][MAXC > 0 ? MAXC : 1];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int slot = lane >> 2, l = lane & 3, side = l >> 1, part = l & 1;
   const unsigned gm = 0xFu << (lane & ~3);  // this island's four lanes
@@ -563,7 +568,14 @@ __global__ void __launch_bounds__(32 * WPB) pile_k_pgs_quad(const PileGroupDev* 
     }
     float* const sc0 = t < n_items ? wf + L.sc + SC * k0 : nullptr;
     const int* const id0 = t < n_items ? wi + L.scid + 2 * k0 : nullptr;
+    float4* const imps = imp_s[wib][slot];
+    // impulse of contact k: shared memory, or the solver record
+    auto impk = [&](int k) -> float4* {
+      return MAXC > 0 ? imps + k : reinterpret_cast<float4*>(sc0 + (size_t)SC * k + S_IMP);
+    };
     for (int i = l; i < 6 * (nbody + 1); i += 4) (&acc[0][0])[i] = 0.f;
+    if (MAXC > 0)
+      for (int i = l; i < cnt; i += 4) imps[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     const int total = iters * cnt;
     int tmax = total;
 #pragma unroll
@@ -575,7 +587,7 @@ __global__ void __launch_bounds__(32 * WPB) pile_k_pgs_quad(const PileGroupDev* 
     auto contact = [&](int step, QuadContact& cur, QuadContact& nxt) {
       const bool on = step < total;
       const int kn = k + 1 == cnt ? 0 : k + 1;
-      if (step + 1 < total) quad_load(sc0 + (size_t)SC * kn, id0 + 2 * kn, side, l, nbody, nxt);
+      if (step + 1 < total) quad_load(sc0 + (size_t)SC * kn, impk(kn), id0 + 2 * kn, side, l, nbody, nxt);
       const int body = on ? cur.body : 0;
       float a[3];
 #pragma unroll
@@ -625,7 +637,7 @@ __global__ void __launch_bounds__(32 * WPB) pile_k_pgs_quad(const PileGroupDev* 
       if (on) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) acc[body][3 * part + c] = a[c];
-        if (l == 0) *reinterpret_cast<float4*>(sc0 + (size_t)SC * k + S_IMP) = make_float4(im[0], im[1], im[2], im[3]);
+        if (l == 0) *impk(k) = make_float4(im[0], im[1], im[2], im[3]);
         if (kn == k) {  // a one-contact island reads its own update back
 #pragma unroll
           for (int r = 0; r < 4; ++r) nxt.imp[r] = im[r];
@@ -635,7 +647,7 @@ __global__ void __launch_bounds__(32 * WPB) pile_k_pgs_quad(const PileGroupDev* 
       __syncwarp();
     };
     QuadContact c0, c1;
-    if (total > 0) quad_load(sc0, id0, side, l, nbody, c0);
+    if (total > 0) quad_load(sc0, impk(0), id0, side, l, nbody, c0);
     else quad_zero(nbody, c0);
     quad_zero(nbody, c1);
     for (int step = 0; step < tmax; step += 2) {
@@ -644,9 +656,9 @@ __global__ void __launch_bounds__(32 * WPB) pile_k_pgs_quad(const PileGroupDev* 
     }
     if (t < n_items) {
       for (int kk = l; kk < cnt; kk += 4) {
-        const float* s2 = sc0 + (size_t)SC * kk;
+        const float4 m = *impk(kk);
         float* cimp = wf + L.con + CF * wi[L.sccon + k0 + kk] + C_IMP;
-        for (int r = 0; r < 4; ++r) cimp[r] = s2[S_IMP + r];
+        cimp[0] = m.x; cimp[1] = m.y; cimp[2] = m.z; cimp[3] = m.w;
       }
       for (int b = l; b < nbody; b += 4) {
         const int bd = wi[L.ibody + b0 + b];
@@ -713,8 +725,10 @@ extern "C" size_t newt_pile_ws_bytes(int nb, int np, int maxc) {
 // Kernel attributes and resident-grid sizes (called outside stream capture).
 static int cap128 = 4096, capq[4] = {1216, 1216, 1216, 304};
 
-// the multi-body island kernels of classes 3-6: bodies per island, warps per block
-#define NEWT_QUAD_KERNELS(X) X(3, 4, 4) X(4, CH_MIN, 4) X(5, CH_MAXC + 1, 4) X(6, NEWT_MAX_BODIES, 2)
+// the multi-body island kernels of classes 3-6: bodies and staged contacts
+// per island, warps per block
+#define NEWT_QUAD_KERNELS(X) \
+  X(3, 4, CH_MIN - 1, 4) X(4, CH_MIN, CH_MIN - 1, 4) X(5, CH_MAXC + 1, CH_MAXC, 4) X(6, NEWT_MAX_BODIES, 0, 2)
 
 extern "C" void newt_pile_init() {
   int dev = 0, sms = 1, b1 = 1;
@@ -722,11 +736,11 @@ extern "C" void newt_pile_init() {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, pile_k_pgs_small<4>, 128, 0);
   cap128 = sms * (b1 > 0 ? b1 : 1) * 2;
-#define OCC(cl, mb, wpb)                                                                  \
-  {                                                                                       \
-    int b = 1;                                                                            \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pile_k_pgs_quad<mb, wpb>, 32 * wpb, 0); \
-    capq[cl - 3] = sms * (b > 0 ? b : 1);                                                 \
+#define OCC(cl, mb, mc, wpb)                                                                  \
+  {                                                                                           \
+    int b = 1;                                                                                \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pile_k_pgs_quad<mb, mc, wpb>, 32 * wpb, 0); \
+    capq[cl - 3] = sms * (b > 0 ? b : 1);                                                     \
   }
   NEWT_QUAD_KERNELS(OCC)
 #undef OCC
@@ -744,10 +758,10 @@ static void launch_class(int cl, const PileGroupDev* dG, const int* dwseg, int n
     case 0: pile_k_pgs_small<1><<<grid, 128, 0, s>>>(dG, dwseg, ng, items, il.counts, cl); break;
     case 1: pile_k_pgs_small<2><<<grid, 128, 0, s>>>(dG, dwseg, ng, items, il.counts, cl); break;
     case 2: pile_k_pgs_small<4><<<grid, 128, 0, s>>>(dG, dwseg, ng, items, il.counts, cl); break;
-#define LAUNCH(c, mb, wpb)                                                                                   \
-  case c:                                                                                                    \
-    pile_k_pgs_quad<mb, wpb><<<std::min((il.cap + 8 * wpb - 1) / (8 * wpb), capq[c - 3]), 32 * wpb, 0, s>>>( \
-        dG, dwseg, ng, items, il.counts, cl);                                                                \
+#define LAUNCH(c, mb, mc, wpb)                                                                                    \
+  case c:                                                                                                         \
+    pile_k_pgs_quad<mb, mc, wpb><<<std::min((il.cap + 8 * wpb - 1) / (8 * wpb), capq[c - 3]), 32 * wpb, 0, s>>>( \
+        dG, dwseg, ng, items, il.counts, cl);                                                                     \
     break;
     NEWT_QUAD_KERNELS(LAUNCH)
 #undef LAUNCH
@@ -815,8 +829,10 @@ extern "C" cudaError_t newt_pile_prepare_kernels() {
   cudaFuncAttributes a;
   const void* fns[] = {(const void*)pile_k_collide,       (const void*)pile_k_pgs_small<4>,
                        (const void*)pile_k_pgs_small<2>,    (const void*)pile_k_pgs_small<1>,
-                       (const void*)pile_k_pgs_quad<4, 4>,  (const void*)pile_k_pgs_quad<CH_MIN, 4>,
-                       (const void*)pile_k_pgs_quad<CH_MAXC + 1, 4>, (const void*)pile_k_pgs_quad<NEWT_MAX_BODIES, 2>,
+                       (const void*)pile_k_pgs_quad<4, CH_MIN - 1, 4>,
+                       (const void*)pile_k_pgs_quad<CH_MIN, CH_MIN - 1, 4>,
+                       (const void*)pile_k_pgs_quad<CH_MAXC + 1, CH_MAXC, 4>,
+                       (const void*)pile_k_pgs_quad<NEWT_MAX_BODIES, 0, 2>,
                        (const void*)pile_k_integrate};
   for (const void* f : fns) {
     cudaError_t e = cudaFuncGetAttributes(&a, f);

@@ -167,6 +167,10 @@ int newt_gpu_destroy(newt_gpu_ctx* ctx) {
   if (ctx->side) cudaStreamDestroy(ctx->side);
   for (int k = 0; k < 3; ++k) if (ctx->pside[k]) cudaStreamDestroy(ctx->pside[k]);
   for (int k = 0; k < 4; ++k) if (ctx->pev[k]) cudaEventDestroy(ctx->pev[k]);
+  for (int b = 0; b < newt_gpu_ctx::PILE_BRANCHES; ++b) {
+    for (int k = 0; k < 4; ++k) if (ctx->pbs[b][k]) cudaStreamDestroy(ctx->pbs[b][k]);
+    for (int k = 0; k < 5; ++k) if (ctx->pbe[b][k]) cudaEventDestroy(ctx->pbe[b][k]);
+  }
   for (cudaEvent_t e : ctx->kev) cudaEventDestroy(e);
   for (cudaEvent_t e : ctx->tcev) cudaEventDestroy(e);
   if (ctx->io_h) cudaFreeHost(ctx->io_h);
@@ -480,20 +484,21 @@ int newt_gpu_tc_profile(newt_gpu_ctx* ctx, float* kernel_ms) {
   return NEWT_OK;
 }
 
-int newt_gpu_pile_profile(newt_gpu_ctx* ctx, int32_t enable, float* kernel_ms, int32_t* work) {
+int newt_gpu_pile_profile(newt_gpu_ctx* ctx, int32_t enable, float* kernel_ms, int32_t* work, int32_t* launches) {
   if (!ctx) return NEWT_E_INVALID;
   cudaSetDevice(ctx->device);
   if (enable >= 0 && (enable != 0) != ctx->profile) {
     ctx->profile = enable != 0;
     ctx->graph_dirty = true;  // recapture with (or without) the event nodes
   }
+  if (launches) *launches = ctx->kev_steps * ctx->kev_branches;
   if (!kernel_ms && !work) return NEWT_OK;
   int rc = newt_gpu_sync(ctx, 600000);
   if (rc != NEWT_OK) return rc;
   const int K = NEWT_PILE_KERNELS;
   if (kernel_ms) {
     for (int k = 0; k < K; ++k) kernel_ms[k] = 0.f;
-    for (int s = 0; s < ctx->kev_steps; ++s)
+    for (int s = 0; s < ctx->kev_steps * ctx->kev_branches; ++s)
       for (int k = 0; k < K; ++k) {
         float ms = 0.f;
         const size_t e = (size_t)2 * (K * s + k);

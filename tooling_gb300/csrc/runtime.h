@@ -136,6 +136,11 @@ struct newt_gpu_ctx {
   cudaStream_t side = nullptr;   // second capture branch (tree persistent kernels)
   cudaStream_t pside[3] = {nullptr, nullptr, nullptr};  // pile island-class branches
   cudaEvent_t pev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // batched piles: world-range branches, each with its own main stream, three
+  // island-class streams and four fork/join events
+  static constexpr int PILE_BRANCHES = 2;
+  cudaStream_t pbs[PILE_BRANCHES][4] = {};
+  cudaEvent_t pbe[PILE_BRANCHES][5] = {};
   // plain path: one single-group table per group
   struct PlainTable { void* dG; int* dseg; int* lists; int ng, worlds, slots; };
   bool plain_dirty = true;
@@ -145,11 +150,11 @@ struct newt_gpu_ctx {
   // profiling: timing events around the pile kernels of batched captures,
   // and the island work lists (pointer, slots) the last step used
   bool profile = false;
-  std::vector<cudaEvent_t> kev;
-  int kev_steps = 0;
+  std::vector<cudaEvent_t> kev;  // [branch][env-step][kernel][start, end]
+  int kev_steps = 0, kev_branches = 1;
   std::vector<std::pair<int*, int>> last_lists;
   std::vector<std::pair<int*, int>> graph_lists;  // the captured graph's, copied to last_lists per replay
-  int graph_kev_steps = 0;
+  int graph_kev_steps = 0, graph_kev_branches = 1;
   // tree-contact step timing: 3 kernels x (start, end) per env-step of the
   // last tree-contact step call, recorded when `profile` is on
   std::vector<cudaEvent_t> tcev;

@@ -71,16 +71,26 @@ struct PileTable {
   int ng = 0, worlds = 0, slots = 0;
 };
 
+// Branch `part` of `parts` covers worlds [n*part/parts, n*(part+1)/parts) of
+// every group: a view of the group with its record, int and scratch pointers
+// moved to the range (pile records are world-major).
 static int build_pile_table(newt_gpu_ctx* ctx, const std::vector<HostGroup*>& gs, PileTable& t,
-                            std::vector<void*>& owned) {
+                            std::vector<void*>& owned, int part = 0, int parts = 1) {
   std::vector<PileGroupDev> hg;
   std::vector<int> wseg{0}, iseg{0};
   for (HostGroup* g : gs) {
     int rc = ensure_pile_scratch(ctx, g);
     if (rc != NEWT_OK) return rc;
-    hg.push_back(g->pile_dev());
-    wseg.push_back(wseg.back() + g->n);
-    iseg.push_back(iseg.back() + g->n * g->size);
+    const int a = (int)((long)g->n * part / parts), b = (int)((long)g->n * (part + 1) / parts);
+    if (b <= a) continue;
+    PileGroupDev d = g->pile_dev();
+    d.n = b - a;
+    d.F += (size_t)a * d.lay.fstride;
+    d.I += (size_t)a * d.lay.istride;
+    d.scr += (size_t)a * d.sstride;
+    hg.push_back(d);
+    wseg.push_back(wseg.back() + d.n);
+    iseg.push_back(iseg.back() + d.n * g->size);
   }
   t.ng = (int)hg.size();
   t.worlds = wseg.back();
@@ -98,9 +108,9 @@ static int build_pile_table(newt_gpu_ctx* ctx, const std::vector<HostGroup*>& gs
 }
 
 // Timing events for the pile kernels of a captured horizon (profiling only):
-// NEWT_PILE_KERNELS pairs per env-step.
-static int ensure_kernel_events(newt_gpu_ctx* ctx, int n_steps) {
-  const size_t need = (size_t)2 * NEWT_PILE_KERNELS * n_steps;
+// NEWT_PILE_KERNELS pairs per env-step and branch.
+static int ensure_kernel_events(newt_gpu_ctx* ctx, int n_steps, int branches = 1) {
+  const size_t need = (size_t)2 * NEWT_PILE_KERNELS * n_steps * branches;
   while (ctx->kev.size() < need) {
     cudaEvent_t e;
     CKS(cudaEventCreate(&e));
@@ -109,17 +119,26 @@ static int ensure_kernel_events(newt_gpu_ctx* ctx, int n_steps) {
   return NEWT_OK;
 }
 
-static int launch_pile_steps(newt_gpu_ctx* ctx, const PileTable& t, int n_steps, cudaStream_t st) {
-  const bool timed = ctx->profile;
-  if (timed) {
-    int rc = ensure_kernel_events(ctx, n_steps);
-    if (rc != NEWT_OK) return rc;
-  }
-  for (int s = 0; s < n_steps; ++s)
+// `n_steps` env-steps of one table on stream `st` (island classes forked to
+// `side`, joined with `ev`); timing events of branch `branch` when profiling.
+static void launch_pile_steps(newt_gpu_ctx* ctx, const PileTable& t, int n_steps, cudaStream_t st,
+                              const cudaStream_t* side, cudaEvent_t* ev, int branch) {
+  for (int s = 0; s < n_steps; ++s) {
+    cudaEvent_t* kev = ctx->profile
+                           ? ctx->kev.data() + (size_t)2 * NEWT_PILE_KERNELS * ((size_t)branch * n_steps + s)
+                           : nullptr;
     ctx->launches += newt_launch_pile_step(t.dG, t.dseg, t.ng, t.worlds, t.slots, t.lists, s == n_steps - 1, st,
-                                           ctx->pside, ctx->pev,
-                                           timed ? ctx->kev.data() + (size_t)2 * NEWT_PILE_KERNELS * s : nullptr);
-  ctx->graph_kev_steps = timed ? n_steps : 0;
+                                           side, ev, kev);
+  }
+}
+
+// Streams and events of the batched form's world-range branches.
+static int ensure_pile_branches(newt_gpu_ctx* ctx) {
+  if (ctx->pbs[0][0]) return NEWT_OK;
+  for (int b = 0; b < newt_gpu_ctx::PILE_BRANCHES; ++b) {
+    for (int k = 0; k < 4; ++k) CKS(cudaStreamCreateWithFlags(&ctx->pbs[b][k], cudaStreamNonBlocking));
+    for (int k = 0; k < 5; ++k) CKS(cudaEventCreateWithFlags(&ctx->pbe[b][k], cudaEventDisableTiming));
+  }
   return NEWT_OK;
 }
 
@@ -146,6 +165,7 @@ int step_plain(newt_gpu_ctx* ctx, int n_steps) {
   for (const auto& T : ctx->plain_tables)
     if (T.lists) ctx->last_lists.push_back({T.lists, T.slots});
   ctx->kev_steps = 0;
+  ctx->kev_branches = 1;
   for (int s = 0; s < n_steps; ++s) {
     for (size_t gi = 0; gi < ctx->groups.size(); ++gi) {
       HostGroup* g = ctx->groups[gi].get();
@@ -201,13 +221,24 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
     L.grid = std::min(L.items, newt_tree_persistent_blocks_per_sm(bucket) * sm_count(ctx));
     tls.push_back(L);
   }
-  // piles: one table over every pile group (largest worlds first)
+  // piles: tables over every pile group (largest worlds first), one per
+  // world-range branch; the branches run on their own streams, so one
+  // branch's long-island tail overlaps the others' collide and solve
   std::vector<HostGroup*> piles;
-  for (auto& gp : ctx->groups) if (gp->n > 0 && gp->kind == GK_PILE) piles.push_back(gp.get());
+  long pile_worlds = 0;
+  for (auto& gp : ctx->groups)
+    if (gp->n > 0 && gp->kind == GK_PILE) { piles.push_back(gp.get()); pile_worlds += gp->n; }
   std::stable_sort(piles.begin(), piles.end(), [](HostGroup* a, HostGroup* b) { return a->size > b->size; });
-  PileTable pt;
-  int rc = build_pile_table(ctx, piles, pt, bufs);
-  if (rc != NEWT_OK) return rc;
+  const int nbr = (int)std::max<long>(1, std::min<long>(newt_gpu_ctx::PILE_BRANCHES, pile_worlds / 4096));
+  std::vector<PileTable> pts(nbr);
+  for (int b = 0; b < nbr; ++b) {
+    int rc = build_pile_table(ctx, piles, pts[b], bufs, b, nbr);
+    if (rc != NEWT_OK) return rc;
+  }
+  if (pile_worlds > 0) {
+    int rc = ensure_pile_branches(ctx);
+    if (rc != NEWT_OK) return rc;
+  }
 
   cudaEvent_t fork = nullptr, join = nullptr;
   if (!ctx->side) CKS(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
@@ -215,12 +246,12 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
   CKS(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
   cudaGraph_t graph;
   if (ctx->profile) {
-    int r = ensure_kernel_events(ctx, n_steps);
+    int r = ensure_kernel_events(ctx, n_steps, nbr);
     if (r != NEWT_OK) return r;
   }
   ctx->graph_lists.clear();
-  if (pt.ng > 0) ctx->graph_lists.push_back({pt.lists, pt.slots});
-  ctx->graph_kev_steps = 0;
+  for (const PileTable& t : pts)
+    if (t.ng > 0) ctx->graph_lists.push_back({t.lists, t.slots});
   CKS(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
   cudaEventRecord(fork, ctx->stream);
   cudaStreamWaitEvent(ctx->side, fork, 0);
@@ -230,9 +261,18 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
   }
   cudaEventRecord(join, ctx->side);
   int64_t before = ctx->launches;
-  if (pt.ng > 0) launch_pile_steps(ctx, pt, n_steps, ctx->stream);
+  for (int b = 0; b < nbr; ++b) {
+    if (pts[b].ng == 0) continue;
+    cudaStream_t* bs = ctx->pbs[b];
+    cudaStreamWaitEvent(bs[0], fork, 0);
+    launch_pile_steps(ctx, pts[b], n_steps, bs[0], bs + 1, ctx->pbe[b], b);
+    cudaEventRecord(ctx->pbe[b][4], bs[0]);
+    cudaStreamWaitEvent(ctx->stream, ctx->pbe[b][4], 0);
+  }
   int pile_launches = (int)(ctx->launches - before);
   ctx->launches = before;
+  ctx->graph_kev_steps = ctx->profile && pile_worlds > 0 ? n_steps : 0;
+  ctx->graph_kev_branches = nbr;
   cudaStreamWaitEvent(ctx->stream, join, 0);
   cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
   cudaEventDestroy(fork);
@@ -262,6 +302,7 @@ int step_batched(newt_gpu_ctx* ctx, int n_steps) {
   }
   ctx->last_lists = ctx->graph_lists;
   ctx->kev_steps = ctx->graph_kev_steps;
+  ctx->kev_branches = ctx->graph_kev_branches;
   if (has_tc) {
     for (auto& gp : ctx->groups)
       if (gp->n > 0 && gp->kind == GK_TREE_CONTACT) {
