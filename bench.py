@@ -168,9 +168,11 @@ def run_gpu(args, rank, ws, local, dist):
     S = args.substeps
     # per-kernel timing events ride in the captured graph (on each kernel's stream)
     eng.pile_profile(1)
-    # warm-up (also captures the CUDA graph)
+    # warm-up (also captures the CUDA graph), then the launch-choice autotuner
+    # (it leaves the worlds' state as it found it)
     for _ in range(max(3, args.warmup)):
         eng.step(S, STEP_BATCHED)
+    tuned = eng.autotune(S)
     eng.sync()
     start_qpos, start_qvel = eng.get_state(slots, int(batch.nq.sum()), int(batch.nv.sum()))
     launches0 = eng.launch_count()
@@ -247,7 +249,7 @@ def run_gpu(args, rank, ws, local, dist):
         "config": {"workload": "pile: 16 free spheres/boxes on a plane per world, PGS 50 iterations, dt 2e-3",
                    "worlds_per_gpu": W, "bodies_per_world": 16, "env_steps_per_bench_step": S,
                    "mode": "batched: 9 kernels per env-step and world-range branch, branches and island classes "
-                           "on forked streams, CUDA graph",
+                           "on forked streams, CUDA graph", "autotuned": tuned,
                    "l2": "flushed between timed steps", "parallelism": f"replicas x{ws}"},
         "e2e": {"value": e2e, "unit": "env-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
@@ -397,10 +399,13 @@ def run_gpu_uneven(args, rank, ws, local, dist):
     eng.set_qfrc(slots, batch.qfrc)
     S = args.substeps
     eng.pile_profile(1)
-    # warm-up (graph capture, first-touch), then back to the start state: the
-    # timed steps cover env-steps 0 .. steps x substeps of every world
+    # warm-up (graph capture, first-touch) and the launch-choice autotuner,
+    # then back to the start state: the timed steps cover env-steps
+    # 0 .. steps x substeps of every world
     for _ in range(max(3, args.warmup)):
         eng.step(S, STEP_BATCHED)
+    tuned = eng.autotune(S)
+    eng.step(S, STEP_BATCHED)
     eng.sync()
     nq, nv = int(batch.nq.sum()), int(batch.nv.sum())
     start_qpos, start_qvel = batch.qpos.copy(), batch.qvel.copy()
@@ -470,6 +475,7 @@ def run_gpu_uneven(args, rank, ws, local, dist):
         "config": {"workload": "uneven: 50/50 chains and piles, 2..64 bodies log-uniform, PGS 50, dt 2e-3",
                    "worlds_per_gpu": W, "chains": W - n_piles, "piles": n_piles, "env_steps_per_bench_step": S,
                    "horizon": f"env-steps 0..{S * args.steps} from the start state (piles fall and settle)",
+                   "autotuned": tuned,
                    "mode": "batched: tree persistent kernels per size bucket + one pile table, CUDA graph",
                    "l2": "flushed between timed steps", "parallelism": f"replicas x{ws}"},
         "plain_value": plain, "batched_over_plain": value / ws / plain,

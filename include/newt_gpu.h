@@ -201,6 +201,13 @@ NEWT_API int newt_gpu_event_elapsed_ms(newt_gpu_ctx* ctx, float* ms);
 NEWT_API int newt_gpu_flush_l2(newt_gpu_ctx* ctx);                              /* writes a buffer > L2 */
 /* Kernel launches issued by this context since creation. */
 NEWT_API int64_t newt_gpu_launch_count(const newt_gpu_ctx* ctx);
+/* Times the batched step's launch choices on the live worlds (world-range
+ * branches of the pile step: 1, 2 or 3; tree persistent grid at full or half
+ * residency), `n_steps` env-steps per trial from one snapshot of every
+ * world, keeps the fastest for later NEWT_STEP_BATCHED calls and leaves every
+ * world's state as it was.  `choice` (nullable, 3 ints): branches, tree grid
+ * percent, and the winner's time in microseconds.  No counterpart in newt. */
+NEWT_API int newt_gpu_autotune(newt_gpu_ctx* ctx, int32_t n_steps, int32_t* choice);
 /* Device bytes the world groups hold (capacity x bytes per world: model,
  * state, contact and solver buffers) and the admission budget they are
  * checked against. */

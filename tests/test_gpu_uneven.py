@@ -74,3 +74,26 @@ def test_status_reports_blow_up_right_after_the_step(eng, mode):
         eng.step(25, mode)
     assert int(eng.status(slots)[0]) & 0x1
     eng.free(slots)
+
+
+def test_autotune_keeps_state_and_results(eng, batch):
+    """newt_gpu_autotune times the batched form's launch choices on the live
+    worlds from one snapshot: the worlds end where they began, and the chosen
+    form still agrees with the plain one."""
+    slots = eng.alloc(eng.upload(batch))
+    eng.set_state(slots, batch.qpos, batch.qvel)
+    eng.set_qfrc(slots, batch.qfrc)
+    nq, nv = int(batch.nq.sum()), int(batch.nv.sum())
+    q0, v0 = eng.get_state(slots, nq, nv)
+    choice = eng.autotune(5)
+    q1, v1 = eng.get_state(slots, nq, nv)
+    np.testing.assert_array_equal(q0, q1)
+    np.testing.assert_array_equal(v0, v1)
+    assert choice["pile_branches"] in (1, 2, 3) and choice["tree_grid_pct"] in (50, 100)
+    eng.step(10, STEP_BATCHED)
+    qb, vb = eng.get_state(slots, nq, nv)
+    eng.set_state(slots, q0, v0)
+    eng.step(10, STEP_PLAIN)
+    qp, vp = eng.get_state(slots, nq, nv)
+    eng.free(slots)
+    assert np.abs(qb - qp).max() < 1e-5 and np.abs(vb - vp).max() < 1e-4

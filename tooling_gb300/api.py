@@ -29,7 +29,7 @@ EXPORTED = [
     "newt_gpu_set_qfrc", "newt_gpu_step", "newt_gpu_sync", "newt_gpu_world_status", "newt_gpu_get_qacc",
     "newt_gpu_get_contacts", "newt_gpu_get_impulses", "newt_gpu_event_record", "newt_gpu_event_elapsed_ms",
     "newt_gpu_flush_l2", "newt_gpu_launch_count", "newt_gpu_step_static", "newt_gpu_pile_profile",
-    "newt_gpu_tc_profile", "newt_gpu_serve", "newt_gpu_memory",
+    "newt_gpu_tc_profile", "newt_gpu_serve", "newt_gpu_memory", "newt_gpu_autotune",
 ]
 TC_KERNELS = ["tree_aba_kernel", "tc_k_solve", "tree_integrate_kernel"]
 PILE_KERNELS = ["pile_k_collide", "pile_k_pgs_small<1>", "pile_k_pgs_small<2>", "pile_k_pgs_small<4>",
@@ -110,6 +110,7 @@ def load_library(path: str = LIB_PATH):
         "newt_gpu_tc_profile": ([P, P], C.c_int),
         "newt_gpu_serve": ([P, P, I32, P, P], C.c_int),
         "newt_gpu_memory": ([P, P, P], C.c_int),
+        "newt_gpu_autotune": ([P, I32, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -282,6 +283,13 @@ class Engine:
 
     def flush_l2(self):
         self._ck(self.L.newt_gpu_flush_l2(self.ctx))
+
+    def autotune(self, n_steps: int = 25) -> dict:
+        """Pick the batched step's launch choices by timing them on the live
+        worlds (their state is left unchanged)."""
+        c = np.zeros(3, np.int32)
+        self._ck(self.L.newt_gpu_autotune(self.ctx, int(n_steps), _p(c)))
+        return {"pile_branches": int(c[0]), "tree_grid_pct": int(c[1]), "best_ms": c[2] / 1000.0}
 
     def memory(self):
         """(device bytes held by the world groups, admission budget)."""

@@ -138,7 +138,10 @@ struct newt_gpu_ctx {
   cudaEvent_t pev[4] = {nullptr, nullptr, nullptr, nullptr};
   // batched piles: world-range branches, each with its own main stream, three
   // island-class streams and four fork/join events
-  static constexpr int PILE_BRANCHES = 2;
+  static constexpr int PILE_BRANCHES = 3;
+  // launch choices of the batched form (newt_gpu_autotune): pile branches
+  // (0: by world count), tree persistent grid in percent of full residency
+  int tune_branches = 0, tune_tree_grid_pct = 100;
   cudaStream_t pbs[PILE_BRANCHES][4] = {};
   cudaEvent_t pbe[PILE_BRANCHES][5] = {};
   // plain path: one single-group table per group
@@ -178,6 +181,7 @@ int io_clear_flags(newt_gpu_ctx* ctx, const std::vector<int*>& flags);  // *flag
 HostGroup* find_or_make_group(newt_gpu_ctx* ctx, const HostModel& m);
 int step_plain(newt_gpu_ctx* ctx, int n_steps);
 int step_batched(newt_gpu_ctx* ctx, int n_steps);
+int autotune_batched(newt_gpu_ctx* ctx, int n_steps, int32_t* choice);
 
 // kernel launchers (defined in the .cu kernel files)
 extern "C" int newt_tree_bucket(int L);

@@ -218,7 +218,8 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
     CKS(cudaMemcpy(L.dq, q.data(), q.size() * sizeof(int), cudaMemcpyHostToDevice));
     CKS(cudaMalloc(&L.dc, sizeof(int)));
     bufs.push_back(L.dg); bufs.push_back(L.dq); bufs.push_back(L.dc);
-    L.grid = std::min(L.items, newt_tree_persistent_blocks_per_sm(bucket) * sm_count(ctx));
+    const int full = newt_tree_persistent_blocks_per_sm(bucket) * sm_count(ctx);
+    L.grid = std::min(L.items, std::max(1, full * ctx->tune_tree_grid_pct / 100));
     tls.push_back(L);
   }
   // piles: tables over every pile group (largest worlds first), one per
@@ -229,7 +230,9 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
   for (auto& gp : ctx->groups)
     if (gp->n > 0 && gp->kind == GK_PILE) { piles.push_back(gp.get()); pile_worlds += gp->n; }
   std::stable_sort(piles.begin(), piles.end(), [](HostGroup* a, HostGroup* b) { return a->size > b->size; });
-  const int nbr = (int)std::max<long>(1, std::min<long>(newt_gpu_ctx::PILE_BRANCHES, pile_worlds / 4096));
+  const int nbr = ctx->tune_branches > 0
+                      ? std::min(ctx->tune_branches, newt_gpu_ctx::PILE_BRANCHES)
+                      : (int)std::max<long>(1, std::min<long>(2, pile_worlds / 4096));
   std::vector<PileTable> pts(nbr);
   for (int b = 0; b < nbr; ++b) {
     int rc = build_pile_table(ctx, piles, pts[b], bufs, b, nbr);
@@ -311,4 +314,67 @@ int step_batched(newt_gpu_ctx* ctx, int n_steps) {
       }
   }
   return NEWT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// autotuning of the batched form's launch choices
+// ---------------------------------------------------------------------------
+// Every trial steps the live worlds from the same snapshot of every group's
+// records (model, state, status: the whole step state; solver scratch is
+// rebuilt each env-step), so the worlds end where they began.
+int autotune_batched(newt_gpu_ctx* ctx, int n_steps, int32_t* choice) {
+  if (n_steps <= 0) return NEWT_E_INVALID;
+  std::vector<std::pair<void*, size_t>> snap;  // (copy, bytes) per group block
+  auto blocks = [&](std::vector<std::pair<void*, size_t>>& out) {
+    for (auto& gp : ctx->groups) {
+      HostGroup* g = gp.get();
+      if (g->n == 0) continue;
+      out.push_back({g->dF, g->frows * (size_t)g->cap * sizeof(float)});
+      out.push_back({g->dI, g->irows * (size_t)g->cap * sizeof(int)});
+    }
+  };
+  std::vector<std::pair<void*, size_t>> live;
+  blocks(live);
+  int rc = NEWT_OK;
+  for (auto& b : live) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, b.second) != cudaSuccess) { rc = NEWT_E_NOMEM; break; }
+    snap.push_back({p, b.second});
+    CKS(cudaMemcpyAsync(p, b.first, b.second, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  auto restore = [&]() -> int {
+    for (size_t i = 0; i < snap.size(); ++i)
+      CKS(cudaMemcpyAsync(live[i].first, snap[i].first, live[i].second, cudaMemcpyDeviceToDevice, ctx->stream));
+    return NEWT_OK;
+  };
+  struct Cand { int branches, grid_pct; };
+  const Cand cands[] = {{1, 100}, {2, 100}, {3, 100}, {1, 50}, {2, 50}};
+  Cand best{ctx->tune_branches, ctx->tune_tree_grid_pct};
+  float best_ms = -1.f;
+  for (const Cand& c : cands) {
+    if (rc != NEWT_OK) break;
+    ctx->tune_branches = c.branches;
+    ctx->tune_tree_grid_pct = c.grid_pct;
+    ctx->graph_dirty = true;
+    // first call captures (and warms up); the second is timed
+    for (int rep = 0; rep < 2 && rc == NEWT_OK; ++rep) {
+      if ((rc = restore()) != NEWT_OK) break;
+      cudaEventRecord(ctx->ev[0], ctx->stream);
+      rc = step_batched(ctx, n_steps);
+      cudaEventRecord(ctx->ev[1], ctx->stream);
+    }
+    if (rc != NEWT_OK) break;
+    if (cudaEventSynchronize(ctx->ev[1]) != cudaSuccess) { rc = NEWT_E_CUDA; break; }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+    if (best_ms < 0.f || ms < best_ms) { best_ms = ms; best = c; }
+  }
+  if (rc == NEWT_OK) rc = restore();
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& b : snap) cudaFree(b.first);
+  ctx->tune_branches = best.branches;
+  ctx->tune_tree_grid_pct = best.grid_pct;
+  ctx->graph_dirty = true;
+  if (choice) { choice[0] = best.branches; choice[1] = best.grid_pct; choice[2] = (int32_t)(best_ms * 1000.f); }
+  return rc;
 }
