@@ -5,7 +5,11 @@ Workload (the metric's headline configuration): 8192 independent worlds, each
 friction, PGS 50 iterations, dt = 2e-3 -- seeded synthetic worlds.
 
 A bench step advances every world by `--substeps` env-steps with one call of
-the C ABI's batched step (persistent kernel, CUDA-graph replay).  Timing:
+the C ABI's batched step (one CUDA-graph replay: per env-step and world-range
+branch, collide, the island-class solvers on forked streams, integrate).
+Other workloads: --workload quadruped (16384 quadrupeds, Newton), uneven
+(32768 chains and piles of 2..64 bodies, batched vs plain), serve (Poisson
+request streams through the served-rollout loop).  Timing:
   value : device time with CUDA events on the engine's stream, L2 flushed
           between timed steps, state resident in HBM;
   e2e   : wall time of set_state (host->device) + step + get_state

@@ -153,8 +153,11 @@ NEWT_API int newt_gpu_set_qfrc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t 
 
 /* Replaces `World::step()` (newt/src/world.rs:1459) for every live world.
  * mode NEWT_STEP_PLAIN: one launch per stage per step, fixed tiles.
- * mode NEWT_STEP_BATCHED: fused persistent launch over the whole horizon,
- *   worlds pulled from a size-class-sorted queue, captured in a CUDA graph. */
+ * mode NEWT_STEP_BATCHED: the whole call captured in one CUDA graph and
+ *   replayed: trees run the horizon in one persistent launch per size bucket
+ *   over a cost-sorted queue; pile worlds of every size share one table per
+ *   world-range branch (collide, island-class solvers on forked streams,
+ *   integrate per env-step); tree-contact worlds follow per env-step. */
 #define NEWT_STEP_PLAIN 0
 #define NEWT_STEP_BATCHED 1
 NEWT_API int newt_gpu_step(newt_gpu_ctx* ctx, int32_t n_steps, int32_t mode);

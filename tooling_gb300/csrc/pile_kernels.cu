@@ -125,75 +125,141 @@ NEWT_D void assemble(const WsLay& L, float* wf, int* wi, int lane, int t_world, 
     for (int k = 0; k < 4; ++k) cf[C_IMP + k] = 0.f;
   }
   __syncwarp();
-  // islands: union-find over dynamic-dynamic contacts, islands ordered by
-  // their smallest body, contacts within an island in contact order
-  if (lane == 0) {
-    int* uf = wi + L.uf;
-    for (int b = 0; b < nb; ++b) uf[b] = b;
-    for (int c = 0; c < nc; ++c) {
-      const int* cc = wi + L.ci + CI * c;
-      if (wf[L.con + CF * c + C_ACT] == 0.f || cc[2] >= nb || cc[3] >= nb) continue;
-      int ra = cc[2], rb = cc[3];
-      while (uf[ra] != ra) ra = uf[ra];
-      while (uf[rb] != rb) rb = uf[rb];
-      if (ra != rb) { if (ra < rb) uf[rb] = ra; else uf[ra] = rb; }
+  // islands, warp-parallel: each body's component as a 64-bit body mask
+  // (bodies joined by active dynamic-dynamic contacts), closed by pointer
+  // jumping (after r rounds a mask reaches every body within 2^r contacts);
+  // an island is named by its smallest body and islands are numbered in that
+  // order; bodies keep body order and contacts contact order inside an island
+  // (the sweep order of newt's solver)
+  unsigned* clo = reinterpret_cast<unsigned*>(wi + L.perm);  // component mask, low word (maxc >= 2 nb)
+  unsigned* chi = clo + nb;                                   // high word
+  auto comp = [&](int b) { return ((unsigned long long)chi[b] << 32) | clo[b]; };
+  auto active = [&](int c) { return wf[L.con + CF * c + C_ACT] != 0.f; };
+  for (int b = lane; b < nb; b += 32) {
+    clo[b] = b < 32 ? 1u << b : 0u;
+    chi[b] = b >= 32 ? 1u << (b - 32) : 0u;
+  }
+  __syncwarp();
+  for (int c = lane; c < nc; c += 32) {
+    const int* cc = wi + L.ci + CI * c;
+    if (!active(c) || cc[2] >= nb || cc[3] >= nb) continue;
+    const int x = cc[2], y = cc[3];
+    atomicOr(clo + x, y < 32 ? 1u << y : 0u);
+    atomicOr(chi + x, y >= 32 ? 1u << (y - 32) : 0u);
+    atomicOr(clo + y, x < 32 ? 1u << x : 0u);
+    atomicOr(chi + y, x >= 32 ? 1u << (x - 32) : 0u);
+  }
+  __syncwarp();
+  for (int round = 0; round < 7; ++round) {  // 2^6 >= the longest path in 64 bodies
+    unsigned long long nw[2] = {0ull, 0ull};
+    bool changed = false;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int b = lane + 32 * j;
+      if (b >= nb) continue;
+      const unsigned long long m = comp(b);
+      unsigned long long acc = m;
+      for (unsigned long long r = m; r; r &= r - 1) acc |= comp(__ffsll((long long)r) - 1);
+      nw[j] = acc;
+      changed |= acc != m;
     }
-    for (int b = 0; b < nb; ++b) { int r = b; while (uf[r] != r) r = uf[r]; uf[b] = r; }
-    // island id per root body; count contacts per island
-    int* root_isl = wi + L.blocal;  // temp: root -> island id (rewritten below)
-    for (int b = 0; b < nb; ++b) root_isl[b] = -1;
-    int nisl = 0;
-    for (int c = 0; c < nc; ++c) {
-      const int* cc = wi + L.ci + CI * c;
-      if (wf[L.con + CF * c + C_ACT] == 0.f) continue;
-      int body = cc[2] < nb ? cc[2] : cc[3];
-      int r = uf[body];
-      if (root_isl[r] < 0) root_isl[r] = -2;  // mark: island exists
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int b = lane + 32 * j;
+      if (b < nb) { clo[b] = (unsigned)nw[j]; chi[b] = (unsigned)(nw[j] >> 32); }
     }
-    for (int b = 0; b < nb; ++b) if (root_isl[b] == -2) root_isl[b] = nisl++;
-    int* icount = wi + L.icount;
-    int* istart = wi + L.istart;
-    for (int i = 0; i < nisl; ++i) icount[i] = 0;
-    for (int c = 0; c < nc; ++c) {
-      const int* cc = wi + L.ci + CI * c;
-      if (wf[L.con + CF * c + C_ACT] == 0.f) continue;
-      icount[root_isl[uf[cc[2] < nb ? cc[2] : cc[3]]]]++;
+    __syncwarp();
+    if (!__any_sync(0xffffffffu, changed)) break;
+  }
+  // islands exist where an active contact touches a component
+  unsigned long long has = 0ull;
+  for (int c = lane; c < nc; c += 32) {
+    if (!active(c)) continue;
+    const int* cc = wi + L.ci + CI * c;
+    has |= 1ull << (__ffsll((long long)comp(cc[2] < nb ? cc[2] : cc[3])) - 1);
+  }
+  const unsigned long long isl_mask =
+      ((unsigned long long)__reduce_or_sync(0xffffffffu, (unsigned)(has >> 32)) << 32) |
+      __reduce_or_sync(0xffffffffu, (unsigned)has);
+  const int nisl = __popcll((long long)isl_mask);
+  auto island_of_root = [&](int r) { return __popcll((long long)(isl_mask & ((1ull << r) - 1ull))); };
+  auto island_of_body = [&](int b) { return island_of_root(__ffsll((long long)comp(b)) - 1); };
+  int* icount = wi + L.icount;
+  int* istart = wi + L.istart;
+  int* inb = wi + L.inb;
+  int* ibstart = wi + L.ibstart;
+  int* ibody = wi + L.ibody;
+  int* blocal = wi + L.blocal;
+  int* fill = wi + L.uf;  // running contact slot per island
+  for (int i = lane; i < nisl; i += 32) {
+    const unsigned lo = (unsigned)isl_mask, hi = (unsigned)(isl_mask >> 32);
+    const int nlo = __popc(lo);
+    const int r = i < nlo ? (int)__fns(lo, 0, i + 1) : 32 + (int)__fns(hi, 0, i + 1 - nlo);  // the island's root
+    inb[i] = __popcll((long long)comp(r));
+    icount[i] = 0;
+  }
+  __syncwarp();
+  for (int c = lane; c < nc; c += 32) {
+    if (!active(c)) continue;
+    const int* cc = wi + L.ci + CI * c;
+    atomicAdd(icount + island_of_body(cc[2] < nb ? cc[2] : cc[3]), 1);
+  }
+  __syncwarp();
+  // exclusive prefix sums over islands (at most 64: two rounds of 32)
+  {
+    int cbase = 0, bbase = 0;
+    for (int i0 = 0; i0 < nisl; i0 += 32) {
+      const int i = i0 + lane;
+      const int vc = i < nisl ? icount[i] : 0, vb = i < nisl ? inb[i] : 0;
+      int sc = vc, sb = vb;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int tc = __shfl_up_sync(0xffffffffu, sc, o), tb = __shfl_up_sync(0xffffffffu, sb, o);
+        if (lane >= o) { sc += tc; sb += tb; }
+      }
+      if (i < nisl) {
+        istart[i] = cbase + sc - vc;
+        fill[i] = cbase + sc - vc;
+        ibstart[i] = bbase + sb - vb;
+      }
+      cbase += __shfl_sync(0xffffffffu, sc, 31);
+      bbase += __shfl_sync(0xffffffffu, sb, 31);
     }
-    int s = 0;
-    for (int i = 0; i < nisl; ++i) { istart[i] = s; s += icount[i]; }
-    // bodies per island (body order), island-local body index
-    int* inb = wi + L.inb;
-    int* ibstart = wi + L.ibstart;
-    int* ibody = wi + L.ibody;
-    for (int i = 0; i < nisl; ++i) inb[i] = 0;
-    int* bisl = wi + L.perm;  // temp: body -> island (or -1)
-    for (int b = 0; b < nb; ++b) bisl[b] = root_isl[uf[b]];
-    for (int b = 0; b < nb; ++b) if (bisl[b] >= 0) inb[bisl[b]]++;
-    int t = 0;
-    for (int i = 0; i < nisl; ++i) { ibstart[i] = t; t += inb[i]; }
-    int fillb[NEWT_MAX_BODIES];
-    for (int i = 0; i < nisl; ++i) fillb[i] = ibstart[i];
-    int* blocal = wi + L.blocal;  // now: body -> island-local index
-    for (int b = 0; b < nb; ++b) {
-      int i = bisl[b];
-      if (i < 0) { blocal[b] = -1; continue; }
-      blocal[b] = fillb[i] - ibstart[i];
-      ibody[fillb[i]++] = b;
-    }
-    // contact slot in island order
-    int fillc[NEWT_MAX_BODIES];
-    for (int i = 0; i < nisl; ++i) fillc[i] = istart[i];
-    int* sccon = wi + L.sccon;
-    int* scid = wi + L.scid;
-    for (int c = 0; c < nc; ++c) {
-      const int* cc = wi + L.ci + CI * c;
-      if (wf[L.con + CF * c + C_ACT] == 0.f) continue;
-      int i = bisl[cc[2] < nb ? cc[2] : cc[3]];
-      int k = fillc[i]++;
+  }
+  __syncwarp();
+  // bodies: island-local index = rank in the component mask
+  for (int b = lane; b < nb; b += 32) {
+    const unsigned long long m = comp(b);
+    const int r = __ffsll((long long)m) - 1;
+    if (!((isl_mask >> r) & 1ull)) { blocal[b] = -1; continue; }
+    const int loc = __popcll((long long)(m & ((1ull << b) - 1ull)));
+    blocal[b] = loc;
+    ibody[ibstart[island_of_root(r)] + loc] = b;
+  }
+  __syncwarp();
+  // contacts: slots in island order, contact order inside an island
+  int* sccon = wi + L.sccon;
+  int* scid = wi + L.scid;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int c0 = 0; c0 < nc; c0 += 32) {
+    const int c = c0 + lane;
+    const bool act = c < nc && active(c);
+    const int* cc = wi + L.ci + CI * (act ? c : 0);
+    const int isl = act ? island_of_body(cc[2] < nb ? cc[2] : cc[3]) : -1;
+    const unsigned grp = __match_any_sync(0xffffffffu, isl);
+    const int base = act ? fill[isl] : 0;
+    __syncwarp();
+    if (act) {
+      const int k = base + __popc(grp & lt);
       sccon[k] = c;
       scid[2 * k] = cc[2] < nb ? blocal[cc[2]] : -1;
       scid[2 * k + 1] = cc[3] < nb ? blocal[cc[3]] : -1;
+      if ((grp & lt) == 0u) fill[isl] = base + __popc(grp);
     }
+    __syncwarp();
+  }
+  if (lane == 0) {
     wi[L.misc + 3] = nisl;
     // append this world's islands to the class work lists
     int ncls[N_ICLASS] = {}, ccls[N_ICLASS] = {}, bcls[N_ICLASS] = {};
@@ -223,7 +289,6 @@ NEWT_D void assemble(const WsLay& L, float* wf, int* wi, int lane, int t_world, 
   const bool direct = tc < 0.f;
   if (!direct && tc < 2.f * dt) tc = 2.f * dt;  // safe_solref (solver.rs:331-338)
   const float dmax = fminf(fmaxf(soft[3], 1.0e-4f), 0.9999f);
-  const int nisl = wi[L.misc + 3];
   const int nact = nisl > 0 ? wi[L.istart + nisl - 1] + wi[L.icount + nisl - 1] : 0;
   for (int k = lane; k < nact; k += 32) {
     const int c = wi[L.sccon + k];

@@ -81,7 +81,7 @@ struct HostGroup {
   bool soa() const { return kind == GK_TREE || kind == GK_TREE_CONTACT; }
   TcGroupDev tc_dev() const;
   void setup_tc(const HostModel& m);
-  void* plain_scratch = nullptr;  // pile solver scratch (cap worlds)
+  void* plain_scratch = nullptr;  // pile solver scratch, cap worlds (both step forms)
   size_t plain_scratch_bytes = 0;
   long scr_stride = 0;             // floats per world in plain_scratch
 
