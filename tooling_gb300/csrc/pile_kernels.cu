@@ -85,9 +85,12 @@ constexpr int CH_MAXC = 32;  // contacts of the longest island in the long-islan
 struct IslandLists {
   int* items;   // N_ICLASS x cap entries: (world index in the table << 6) | island
   // zeroed before each step: [0, N_ICLASS) islands per class (the list
-  // lengths), then contacts per class, then bodies per class
+  // lengths), then contacts per class, then bodies per class (those two only
+  // when `stats` is set: the last env-step of a call, for the profiling
+  // surface; every world adding to the same counters costs contended atomics)
   int* counts;
   int cap;
+  int stats;
 };
 constexpr int N_COUNTERS = 3 * N_ICLASS;
 
@@ -274,8 +277,10 @@ NEWT_D void assemble(const WsLay& L, float* wf, int* wi, int lane, int t_world, 
       base[c] = 0;
       if (!ncls[c]) continue;
       base[c] = atomicAdd(il.counts + c, ncls[c]);
-      atomicAdd(il.counts + N_ICLASS + c, ccls[c]);
-      atomicAdd(il.counts + 2 * N_ICLASS + c, bcls[c]);
+      if (il.stats) {
+        atomicAdd(il.counts + N_ICLASS + c, ccls[c]);
+        atomicAdd(il.counts + 2 * N_ICLASS + c, bcls[c]);
+      }
     }
     for (int i = 0; i < nisl; ++i) {
       const int c = island_class(inb[i], icount[i]);
@@ -854,6 +859,7 @@ extern "C" int newt_launch_pile_step(const PileGroupDev* dG, const int* dwseg, i
   IslandLists il;
   il.items = lists;
   il.cap = total_slots;
+  il.stats = write_diag;
   il.counts = lists + (size_t)N_ICLASS * total_slots;
   auto mark = [&](int k, int end, cudaStream_t s) {
     if (kev) cudaEventRecordWithFlags(kev[2 * k + end], s, cudaEventRecordExternal);
@@ -915,6 +921,7 @@ extern "C" int newt_launch_pile_step_serial(const PileGroupDev* dG, const int* d
   IslandLists il;
   il.items = lists;
   il.cap = total_slots;
+  il.stats = write_diag;
   il.counts = lists + (size_t)N_ICLASS * total_slots;
   cudaMemsetAsync(il.counts, 0, N_COUNTERS * sizeof(int), st);
   const int wpb = 4;
