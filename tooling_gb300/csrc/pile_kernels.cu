@@ -9,9 +9,11 @@
 //                        contacts (the common resting case): accumulators,
 //                        Jacobians and impulses live in registers for all
 //                        sweeps (classes 0-2)
-//   K3 pgs_quad          multi-body islands (classes 3-6): four lanes per
+//   K3 pgs_quad          multi-body islands (classes 3-5): four lanes per
 //                        island, eight islands per warp; the contact sweep
 //                        serial, each contact's rows spread over the lanes
+//   K3c pgs_levels       long islands (class 6): one warp per island, the
+//                        contacts of one dependency level solved at once
 //   K4 integrate         one warp per world: semi-implicit Euler, state and
 //                        diagnostics back to the world record
 // The class kernels touch disjoint islands and run concurrently.
@@ -81,7 +83,7 @@ NEWT_D void stj(float* p, const J6& j) { p[0] = j.l.x; p[1] = j.l.y; p[2] = j.l.
 // <= 4 or 5 bodies; long islands (5..32 contacts); the rest
 constexpr int N_ICLASS = 7;
 constexpr int CH_MIN = 5;    // contacts of the shortest island in the long-island class
-constexpr int CH_MAXC = 32;  // contacts of the longest island in the long-island class
+constexpr int CH_MAXC = 12;  // contacts of the longest island solved by K3 (longer: K3c, by level)
 struct IslandLists {
   int* items;   // N_ICLASS x cap entries: (world index in the table << 6) | island
   // zeroed before each step: [0, N_ICLASS) islands per class (the list
@@ -96,7 +98,8 @@ constexpr int N_COUNTERS = 3 * N_ICLASS;
 
 // 0-2: one body with 1, 2, 3-4 contacts (pile_k_pgs_small: everything in
 // registers); 3, 4: fewer than CH_MIN contacts with up to 4 / 5 bodies; 5:
-// CH_MIN..CH_MAXC contacts; 6: the rest (pile_k_pgs_quad, sized per class).
+// CH_MIN..CH_MAXC contacts (pile_k_pgs_quad, sized per class); 6: the rest
+// (pile_k_pgs_levels).
 // An island is connected, so it has at most one body more than contacts.
 NEWT_D int island_class(int nbody, int cnt) {
   if (nbody == 1 && cnt == 1) return 0;
@@ -548,7 +551,7 @@ __global__ void __launch_bounds__(128) pile_k_pgs_small(const PileGroupDev* G, c
 }
 
 // ---------------------------------------------------------------------------
-// K3: multi-body islands (classes 3-6), four lanes per island and eight
+// K3: multi-body islands (classes 3-5), four lanes per island and eight
 // islands per warp.  The contact sweep of an island stays serial (Gauss-
 // Seidel order); inside one contact, lane l of the island's four holds one
 // float4 triple of the 12 velocity-accumulator entries the contact touches
@@ -741,6 +744,151 @@ __global__ void __launch_bounds__(32 * WPB) pile_k_pgs_quad(const PileGroupDev* 
 }
 
 // ---------------------------------------------------------------------------
+// K3c: long islands (class 6), one warp per island, contacts solved by
+// dependency level.  In newt's sweep order a contact must see the updates of
+// every earlier contact that shares one of its bodies and nothing else, so
+// contact k sits at level 1 + max(level of the last earlier contact on each
+// of its bodies).  Contacts of one level touch disjoint bodies: the eight
+// four-lane groups of the warp solve them at once (each contact exactly as
+// in K3), and the levels run in order, so every body sees its contacts'
+// updates in sweep order and the result equals the serial sweep.
+// ---------------------------------------------------------------------------
+constexpr int PL_WARPS = 4;
+constexpr int PL_MAXC = 512;  // the largest contact capacity of a pile world
+
+__global__ void __launch_bounds__(32 * PL_WARPS) pile_k_pgs_levels(const PileGroupDev* G, const int* wseg, int ng,
+                                                                   const int* items, const int* count, int cls) {
+  __shared__ float acc_s[PL_WARPS][NEWT_MAX_BODIES + 1][6];
+  __shared__ short perm_s[PL_WARPS][PL_MAXC];      // contacts by (level, sweep order)
+  __shared__ short loff_s[PL_WARPS][PL_MAXC + 1];  // level start offsets
+  __shared__ short lev_s[PL_WARPS][PL_MAXC];
+  __shared__ short last_s[PL_WARPS][NEWT_MAX_BODIES + 1];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int slot = lane >> 2, l = lane & 3, side = l >> 1, part = l & 1;
+  const unsigned gm = 0xFu << (lane & ~3);
+  float(*acc)[6] = acc_s[wib];
+  short* perm = perm_s[wib];
+  short* loff = loff_s[wib];
+  short* lev = lev_s[wib];
+  short* last = last_s[wib];
+  const int n_items = count[cls];
+  for (int t = blockIdx.x * PL_WARPS + wib; t < n_items; t += gridDim.x * PL_WARPS) {
+    IslandRef R;
+    island_ref(G, wseg, ng, items[t], &R);
+    const WsLay& L = R.L;
+    float* wf = R.wf;
+    const int* wi = R.wi;
+    const int nbody = wi[L.inb + R.isl], cnt = min(wi[L.icount + R.isl], PL_MAXC);
+    const int k0 = wi[L.istart + R.isl], b0 = wi[L.ibstart + R.isl];
+    const int iters = R.g->I[(size_t)R.w * R.g->lay.istride + R.g->lay.iters];
+    float* const sc0 = wf + L.sc + SC * k0;
+    const int* const id0 = wi + L.scid + 2 * k0;
+    for (int i = lane; i < 6 * (nbody + 1); i += 32) (&acc[0][0])[i] = 0.f;
+    // the level schedule: levels (lane 0), then a counting sort by level
+    int nlev = 0;
+    if (lane == 0) {
+      for (int b = 0; b <= nbody; ++b) last[b] = 0;
+      for (int k = 0; k < cnt; ++k) {
+        const int la = id0[2 * k], lb = id0[2 * k + 1];
+        const int lv = 1 + max(la >= 0 ? (int)last[la] : 0, lb >= 0 ? (int)last[lb] : 0);
+        if (la >= 0) last[la] = (short)lv;
+        if (lb >= 0) last[lb] = (short)lv;
+        lev[k] = (short)lv;
+        nlev = max(nlev, lv);
+      }
+      for (int v = 0; v <= nlev; ++v) loff[v] = 0;
+      for (int k = 0; k < cnt; ++k) loff[lev[k]]++;
+      int run = 0;
+      for (int v = 1; v <= nlev; ++v) { const int c = loff[v]; loff[v - 1] = (short)run; run += c; }
+      loff[nlev] = (short)run;
+      for (int k = 0; k < cnt; ++k) perm[loff[lev[k] - 1]++] = (short)k;
+      for (int v = nlev; v > 0; --v) loff[v] = loff[v - 1];  // back to level starts
+      loff[0] = 0;
+    }
+    nlev = __shfl_sync(0xffffffffu, nlev, 0);
+    __syncwarp();
+    for (int it = 0; it < iters; ++it) {
+      for (int v = 0; v < nlev; ++v) {
+        const int s = loff[v], e = loff[v + 1];
+        for (int base = s; base < e; base += 8) {
+          const int idx = base + slot;
+          const bool on = idx < e;
+          const int k = on ? perm[idx] : 0;
+          QuadContact cur;
+          if (on) quad_load(sc0 + (size_t)SC * k, reinterpret_cast<const float4*>(sc0 + (size_t)SC * k + S_IMP),
+                            id0 + 2 * k, side, l, nbody, cur);
+          else quad_zero(nbody, cur);
+          const int body = on ? cur.body : 0;
+          float a[3];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) a[c] = on ? acc[body][3 * part + c] : 0.f;
+          float im[4] = {cur.imp[0], cur.imp[1], cur.imp[2], cur.imp[3]};
+          auto single = [&](int r) {
+            float d = dot3(cur.J[r], a);
+            d += __shfl_xor_sync(gm, d, 1);
+            d += __shfl_xor_sync(gm, d, 2);
+            const float res = d + (cur.reg * im[r] + cur.bias[r]);
+            const float nf = RowStep::nonneg(im[r], res, cur.idg[r]);
+            const float dl = nf - im[r];
+            im[r] = nf;
+            a[0] += cur.W[r][0] * dl;
+            a[1] += cur.W[r][1] * dl;
+            a[2] += cur.W[r][2] * dl;
+          };
+          single(0);
+#pragma unroll
+          for (int p = 0; p < 2; ++p) {
+            const int i = 2 * p, j = i + 1;
+            const float* Pp = cur.P + 4 * p;
+            if (Pp[3] == 0.f) {  // uniform over the contact's lanes
+              single(i);
+              single(j);
+              continue;
+            }
+            float di = dot3(cur.J[i], a), dj = dot3(cur.J[j], a);
+            di += __shfl_xor_sync(gm, di, 1);
+            dj += __shfl_xor_sync(gm, dj, 1);
+            di += __shfl_xor_sync(gm, di, 2);
+            dj += __shfl_xor_sync(gm, dj, 2);
+            const float ri = di + (cur.reg * im[i] + cur.bias[i]);
+            const float rj = dj + (cur.reg * im[j] + cur.bias[j]);
+            float ni, nj;
+            RowStep::pair(im[i], im[j], ri, rj, Pp, &ni, &nj);
+            const float ai = ni - im[i], aj = nj - im[j];
+            im[i] = ni;
+            im[j] = nj;
+            a[0] += cur.W[i][0] * ai;
+            a[1] += cur.W[i][1] * ai;
+            a[2] += cur.W[i][2] * ai;
+            a[0] += cur.W[j][0] * aj;
+            a[1] += cur.W[j][1] * aj;
+            a[2] += cur.W[j][2] * aj;
+          }
+          if (on) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) acc[body][3 * part + c] = a[c];
+            if (l == 0)
+              *reinterpret_cast<float4*>(sc0 + (size_t)SC * k + S_IMP) = make_float4(im[0], im[1], im[2], im[3]);
+          }
+          __syncwarp();
+        }
+      }
+    }
+    for (int kk = lane; kk < cnt; kk += 32) {
+      const float* s2 = sc0 + (size_t)SC * kk;
+      float* cimp = wf + L.con + CF * wi[L.sccon + k0 + kk] + C_IMP;
+      for (int r = 0; r < 4; ++r) cimp[r] = s2[S_IMP + r];
+    }
+    for (int b = lane; b < nbody; b += 32) {
+      const int bd = wi[L.ibody + b0 + b];
+      st3(wf + L.dv + 3 * bd, v3(acc[b][0], acc[b][1], acc[b][2]));
+      st3(wf + L.dw + 3 * bd, v3(acc[b][3], acc[b][4], acc[b][5]));
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
 // K4: integration + write-back (world.rs:1790-1817, 3223-3245)
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) pile_k_integrate(const PileGroupDev* G, const int* wseg, int ng, int total,
@@ -793,12 +941,11 @@ extern "C" size_t newt_pile_ws_bytes(int nb, int np, int maxc) {
 }
 
 // Kernel attributes and resident-grid sizes (called outside stream capture).
-static int cap128 = 4096, capq[4] = {1216, 1216, 1216, 304};
+static int cap128 = 4096, capq[3] = {1216, 1216, 1216}, capv = 608;
 
 // the multi-body island kernels of classes 3-6: bodies and staged contacts
 // per island, warps per block
-#define NEWT_QUAD_KERNELS(X) \
-  X(3, 4, CH_MIN - 1, 4) X(4, CH_MIN, CH_MIN - 1, 4) X(5, CH_MAXC + 1, CH_MAXC, 4) X(6, NEWT_MAX_BODIES, 0, 2)
+#define NEWT_QUAD_KERNELS(X) X(3, 4, CH_MIN - 1, 4) X(4, CH_MIN, CH_MIN - 1, 4) X(5, CH_MAXC + 1, CH_MAXC, 4)
 
 extern "C" void newt_pile_init() {
   int dev = 0, sms = 1, b1 = 1;
@@ -814,6 +961,9 @@ extern "C" void newt_pile_init() {
   }
   NEWT_QUAD_KERNELS(OCC)
 #undef OCC
+  int bv = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bv, pile_k_pgs_levels, 32 * PL_WARPS, 0);
+  capv = sms * (bv > 0 ? bv : 1);
 }
 
 // Bytes of the island work lists for `slots` island slots.
@@ -835,7 +985,10 @@ static void launch_class(int cl, const PileGroupDev* dG, const int* dwseg, int n
     break;
     NEWT_QUAD_KERNELS(LAUNCH)
 #undef LAUNCH
-    default: break;
+    default:
+      pile_k_pgs_levels<<<std::min((il.cap + PL_WARPS - 1) / PL_WARPS, capv), 32 * PL_WARPS, 0, s>>>(
+          dG, dwseg, ng, items, il.counts, cl);
+      break;
   }
 }
 
@@ -903,7 +1056,7 @@ extern "C" cudaError_t newt_pile_prepare_kernels() {
                        (const void*)pile_k_pgs_quad<4, CH_MIN - 1, 4>,
                        (const void*)pile_k_pgs_quad<CH_MIN, CH_MIN - 1, 4>,
                        (const void*)pile_k_pgs_quad<CH_MAXC + 1, CH_MAXC, 4>,
-                       (const void*)pile_k_pgs_quad<NEWT_MAX_BODIES, 0, 2>,
+                       (const void*)pile_k_pgs_levels,
                        (const void*)pile_k_integrate};
   for (const void* f : fns) {
     cudaError_t e = cudaFuncGetAttributes(&a, f);
