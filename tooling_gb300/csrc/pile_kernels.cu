@@ -83,7 +83,7 @@ NEWT_D void stj(float* p, const J6& j) { p[0] = j.l.x; p[1] = j.l.y; p[2] = j.l.
 // <= 4 or 5 bodies; long islands (5..32 contacts); the rest
 constexpr int N_ICLASS = 7;
 constexpr int CH_MIN = 5;    // contacts of the shortest island in the long-island class
-constexpr int CH_MAXC = 12;  // contacts of the longest island solved by K3 (longer: K3c, by level)
+constexpr int CH_MAXC = 8;  // contacts of the longest island solved by K3 (longer: K3c, by level)
 struct IslandLists {
   int* items;   // N_ICLASS x cap entries: (world index in the table << 6) | island
   // zeroed before each step: [0, N_ICLASS) islands per class (the list
