@@ -33,7 +33,7 @@ EXPORTED = [
 ]
 TC_KERNELS = ["tree_aba_kernel", "tc_k_solve", "tree_integrate_kernel"]
 PILE_KERNELS = ["pile_k_collide", "pile_k_pgs_small<1>", "pile_k_pgs_small<2>", "pile_k_pgs_small<4>",
-                "pile_k_pgs_quad[3]", "pile_k_pgs_quad[4]", "pile_k_pgs_quad[5]", "pile_k_pgs_quad[6]",
+                "pile_k_pgs_quad[3]", "pile_k_pgs_quad[4]", "pile_k_pgs_quad[5]", "pile_k_pgs_levels[6]",
                 "pile_k_integrate"]
 PILE_ISLAND_CLASSES = 7
 
