@@ -216,6 +216,18 @@ NEWT_API int newt_gpu_autotune(newt_gpu_ctx* ctx, int32_t n_steps, int32_t* choi
  * checked against. */
 NEWT_API int newt_gpu_memory(const newt_gpu_ctx* ctx, uint64_t* used, uint64_t* budget);
 
+/* Control streams.  A world's whole control sequence (horizon x nv
+ * generalised forces, `Tree::qfrc_applied`, newt/src/tree.rs:207) is
+ * uploaded once and kept on the device; each newt_gpu_apply_ctrl call writes
+ * the next row of every stream into its world's qfrc and advances the
+ * stream's cursor (past the horizon qfrc keeps its last row).  `ctrl` holds
+ * the worlds' sequences concatenated in `slots` order.  Worlds without
+ * generalised forces (free-body piles) are skipped; a new stream replaces a
+ * world's old one, and freeing the world ends it. */
+NEWT_API int newt_gpu_set_ctrl_stream(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, const float* ctrl,
+                                      const int32_t* horizons);
+NEWT_API int newt_gpu_apply_ctrl(newt_gpu_ctx* ctx);
+
 /* ---- served rollouts ------------------------------------------------------
  * No counterpart in newt, whose callers (newt/examples/*.rs,
  * sandbox/src/main.rs:601) own one World and call World::step in their own

@@ -190,3 +190,35 @@ def test_poisson_arrivals_on_the_wall_clock(eng, worlds):
     assert 0 < st["p50_ms"] <= st["p99_ms"] <= st["max_ms"]
     assert st["wall_s"] >= arrivals[-1]
     _check_alone(e, mids, hz, init, pool, coff, nv, _split(e, mids, oq, ov), range(0, n, 40))
+
+
+def test_control_streams_survive_group_growth(worlds):
+    """Control streams live on the device and point into their worlds' qfrc
+    rows; a group that grows (and moves) between calls must not lose them:
+    each env-step's qfrc equals the stream's next row, as with set_qfrc."""
+    _, q = worlds
+    e = Engine(device=0)
+    try:
+        ids = e.upload(q)
+        init = _states(q)
+        rng = np.random.default_rng(21)
+        h = 12
+        nv = q.nv[0]
+        ctrl = rng.standard_normal((4, h * nv)).astype(np.float32)
+        s = e.alloc(ids[:4])
+        e.set_state(s, np.concatenate([init[i][0] for i in range(4)]), np.concatenate([init[i][1] for i in range(4)]))
+        e.set_ctrl_stream(s, ctrl.reshape(-1), [h] * 4)
+        for t in range(h):
+            if t == 5:  # more worlds of the same group: it grows past its first capacity
+                extra = e.alloc(np.repeat(ids[4:], 12))
+            e.apply_ctrl()
+            e.step(1, STEP_BATCHED)
+        got = e.get_state(s, int(q.nq[:4].sum()), int(q.nv[:4].sum()))
+        e.free(extra)
+        e.free(s)
+        for i in range(4):
+            q0, v0 = _alone(e, ids[i], h, init[i][0], init[i][1], ctrl[i])
+            np.testing.assert_array_equal(got[0][i * q.nq[0]:(i + 1) * q.nq[0]], q0)
+            np.testing.assert_array_equal(got[1][i * nv:(i + 1) * nv], v0)
+    finally:
+        e.close()

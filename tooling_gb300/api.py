@@ -30,6 +30,7 @@ EXPORTED = [
     "newt_gpu_get_contacts", "newt_gpu_get_impulses", "newt_gpu_event_record", "newt_gpu_event_elapsed_ms",
     "newt_gpu_flush_l2", "newt_gpu_launch_count", "newt_gpu_step_static", "newt_gpu_pile_profile",
     "newt_gpu_tc_profile", "newt_gpu_serve", "newt_gpu_memory", "newt_gpu_autotune",
+    "newt_gpu_set_ctrl_stream", "newt_gpu_apply_ctrl",
 ]
 TC_KERNELS = ["tree_aba_kernel", "tc_k_solve", "tree_integrate_kernel"]
 PILE_KERNELS = ["pile_k_collide", "pile_k_pgs_small<1>", "pile_k_pgs_small<2>", "pile_k_pgs_small<4>",
@@ -111,6 +112,8 @@ def load_library(path: str = LIB_PATH):
         "newt_gpu_serve": ([P, P, I32, P, P], C.c_int),
         "newt_gpu_memory": ([P, P, P], C.c_int),
         "newt_gpu_autotune": ([P, I32, P], C.c_int),
+        "newt_gpu_set_ctrl_stream": ([P, P, I32, P, P], C.c_int),
+        "newt_gpu_apply_ctrl": ([P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -192,6 +195,17 @@ class Engine:
         s = np.ascontiguousarray(slots, np.int32)
         q = np.ascontiguousarray(qfrc, np.float32)
         self._ck(self.L.newt_gpu_set_qfrc(self.ctx, _p(s), len(s), _p(q)))
+
+    def set_ctrl_stream(self, slots, ctrl: np.ndarray, horizons):
+        """Upload each world's horizon x nv control sequence (concatenated in
+        slot order) to the device; apply_ctrl writes the next row into qfrc."""
+        s = np.ascontiguousarray(slots, np.int32)
+        h = np.ascontiguousarray(horizons, np.int32)
+        c = np.ascontiguousarray(ctrl, np.float32)
+        self._ck(self.L.newt_gpu_set_ctrl_stream(self.ctx, _p(s), len(s), _p(c), _p(h)))
+
+    def apply_ctrl(self):
+        self._ck(self.L.newt_gpu_apply_ctrl(self.ctx))
 
     def get_qacc(self, slots, nv_total: int) -> np.ndarray:
         s = np.ascontiguousarray(slots, np.int32)

@@ -175,6 +175,8 @@ int newt_gpu_destroy(newt_gpu_ctx* ctx) {
   for (cudaEvent_t e : ctx->tcev) cudaEventDestroy(e);
   if (ctx->io_h) cudaFreeHost(ctx->io_h);
   if (ctx->io_d) cudaFree(ctx->io_d);
+  if (ctx->ctrl_arena) cudaFree(ctx->ctrl_arena);
+  if (ctx->ctrl_dev) cudaFree(ctx->ctrl_dev);
   cudaEventDestroy(ctx->ev[0]);
   cudaEventDestroy(ctx->ev[1]);
   cudaStreamDestroy(ctx->stream);
@@ -213,6 +215,7 @@ static int release_slots(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n) {
     flags.push_back(ctx->groups[r.group]->release_index(r.index));
     r.live = false;
     ctx->free_slots.push_back(slots[i]);
+    ctrl_release_slot(ctx, slots[i]);
   }
   return io_clear_flags(ctx, flags);
 }
@@ -244,6 +247,7 @@ int newt_gpu_alloc_worlds(newt_gpu_ctx* ctx, const int32_t* model_ids, int32_t n
     if (grew) {
       ctx->graph_dirty = true;
       ctx->plain_dirty = true;
+      ctx->ctrl_dirty = true;  // control streams point into the groups' rows
     }
     return rc;
   };

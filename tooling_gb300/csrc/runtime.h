@@ -166,6 +166,17 @@ struct newt_gpu_ctx {
   void* io_h = nullptr;
   void* io_d = nullptr;
   size_t io_bytes = 0;
+  // control streams: per world a horizon x nv block of the device arena and
+  // a cursor; `ctrl_of_slot` maps a slot to its entry (-1: none)
+  struct CtrlEntry { int slot, nv, h, t; size_t off; };
+  float* ctrl_arena = nullptr;
+  size_t ctrl_cap = 0;                               // floats
+  std::vector<std::pair<size_t, size_t>> ctrl_free;  // (offset, floats), sorted
+  std::vector<CtrlEntry> ctrl;
+  std::vector<int> ctrl_of_slot;
+  void* ctrl_dev = nullptr;  // device copy of the entries, rebuilt when `ctrl_dirty`
+  size_t ctrl_dev_cap = 0;
+  bool ctrl_dirty = false;
 };
 
 // rows [lo, lo + cnt) of the worlds `idx` of one group
@@ -177,6 +188,7 @@ struct RowMove {
 int io_scatter(newt_gpu_ctx* ctx, const std::vector<RowMove>& mv);  // host mirror -> device
 int io_gather(newt_gpu_ctx* ctx, const std::vector<RowMove>& mv);   // device -> host mirror
 int io_clear_flags(newt_gpu_ctx* ctx, const std::vector<int*>& flags);  // *flag = 0 on the device
+void ctrl_release_slot(newt_gpu_ctx* ctx, int slot);                     // ends the slot's control stream
 
 HostGroup* find_or_make_group(newt_gpu_ctx* ctx, const HostModel& m);
 int step_plain(newt_gpu_ctx* ctx, int n_steps);

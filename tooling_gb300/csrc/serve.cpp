@@ -8,9 +8,11 @@
 //               finds room in the device budget (NEWT_E_NOMEM: the request
 //               waits for completions); freed world slots are reused, so the
 //               captured step graph stays valid while no group grows
-//   tick        row t of each active request's controls goes to its qfrc,
-//               then one step call of one env-step advances every admitted
-//               world together (continuous batching)
+//   tick        the next row of each admitted request's control stream
+//               (uploaded once at admission, newt_gpu_set_ctrl_stream) goes
+//               to its qfrc on the device, then one step call of one
+//               env-step advances every admitted world together (continuous
+//               batching)
 //   completion  a request whose horizon is reached has its final state read
 //               back and its slot freed; latency = completion - arrival
 #include <algorithm>
@@ -136,6 +138,20 @@ extern "C" NEWT_API int newt_gpu_serve(newt_gpu_ctx* ctx, newt_serve_request* re
       if (!admit.empty()) {
         int rc2 = newt_gpu_set_state(ctx, slots.data(), (int32_t)slots.size(), qp.data(), qv.data());
         if (rc2 != NEWT_OK) return bail(rc2);
+        // the admitted requests' whole control sequences go to the device once
+        std::vector<int32_t> cs, hz;
+        qf.clear();
+        for (size_t k = 0; k < admit.size(); ++k) {
+          const newt_serve_request& r = reqs[admit[k]];
+          if (!r.ctrl || r.horizon == 0) continue;
+          cs.push_back(slots[k]);
+          hz.push_back(r.horizon);
+          qf.insert(qf.end(), r.ctrl, r.ctrl + (size_t)r.horizon * active[active.size() - admit.size() + k].nv);
+        }
+        if (!cs.empty()) {
+          rc2 = newt_gpu_set_ctrl_stream(ctx, cs.data(), (int32_t)cs.size(), qf.data(), hz.data());
+          if (rc2 != NEWT_OK) return bail(rc2);
+        }
       }
     }
     stats->admit_s += now() - tn;
@@ -146,18 +162,10 @@ extern "C" NEWT_API int newt_gpu_serve(newt_gpu_ctx* ctx, newt_serve_request* re
       }
       continue;
     }
-    // ---- tick: controls for the active requests, then one env-step ----
+    // ---- tick: the next control row of every stream, then one env-step ----
     const double tc = now();
-    slots.clear();
-    qf.clear();
-    for (const Active& a : active) {
-      const newt_serve_request& r = reqs[a.req];
-      if (!r.ctrl || a.t >= r.horizon) continue;
-      slots.push_back(a.slot);
-      qf.insert(qf.end(), r.ctrl + (size_t)a.t * a.nv, r.ctrl + (size_t)(a.t + 1) * a.nv);
-    }
-    if (!slots.empty()) {
-      int rc = newt_gpu_set_qfrc(ctx, slots.data(), (int32_t)slots.size(), qf.data());
+    {
+      int rc = newt_gpu_apply_ctrl(ctx);
       if (rc != NEWT_OK) return bail(rc);
     }
     const double ts = now();
