@@ -112,26 +112,34 @@ int newt_gpu_set_ctrl_stream(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n,
   }
   if (total > 0 && !ctrl) return NEWT_E_INVALID;
   if (ctx->ctrl_of_slot.size() < ctx->slots.size()) ctx->ctrl_of_slot.resize(ctx->slots.size(), -1);
+  // the trees' sequences (piles carry no generalised forces) packed into one
+  // block of the arena with one copy; each stream frees its own part later
+  std::vector<float> packed;
+  std::vector<std::pair<int, size_t>> parts;  // (call index, offset in the block)
   size_t src = 0;
   for (int i = 0; i < n; ++i) {
-    const int s = slots[i];
-    const SlotRef& r = ctx->slots[s];
-    const int nv = ctx->models[r.model].nv;
-    const size_t cnt = (size_t)horizons[i] * nv;
-    ctrl_release_slot(ctx, s);
-    if (ctx->groups[r.group]->soa() && cnt > 0) {  // trees only: piles carry no generalised forces
-      size_t off = 0;
-      int rc = arena_alloc(ctx, cnt, &off);
-      if (rc != NEWT_OK) return rc;
-      CKC(cudaMemcpyAsync(ctx->ctrl_arena + off, ctrl + src, cnt * sizeof(float), cudaMemcpyHostToDevice,
-                          ctx->stream));
-      ctx->ctrl_of_slot[s] = (int)ctx->ctrl.size();
-      ctx->ctrl.push_back({s, nv, horizons[i], 0, off});
-      ctx->ctrl_dirty = true;
+    const SlotRef& r = ctx->slots[slots[i]];
+    const size_t cnt = (size_t)horizons[i] * ctx->models[r.model].nv;
+    ctrl_release_slot(ctx, slots[i]);
+    if (ctx->groups[r.group]->soa() && cnt > 0) {
+      parts.push_back({i, packed.size()});
+      packed.insert(packed.end(), ctrl + src, ctrl + src + cnt);
     }
     src += cnt;
   }
-  CKC(cudaStreamSynchronize(ctx->stream));
+  if (parts.empty()) return NEWT_OK;
+  size_t base = 0;
+  int rc = arena_alloc(ctx, packed.size(), &base);
+  if (rc != NEWT_OK) return rc;
+  CKC(cudaMemcpyAsync(ctx->ctrl_arena + base, packed.data(), packed.size() * sizeof(float), cudaMemcpyHostToDevice,
+                      ctx->stream));
+  for (const auto& p : parts) {
+    const int s = slots[p.first];
+    ctx->ctrl_of_slot[s] = (int)ctx->ctrl.size();
+    ctx->ctrl.push_back({s, ctx->models[ctx->slots[s].model].nv, horizons[p.first], 0, base + p.second});
+  }
+  ctx->ctrl_dirty = true;
+  CKC(cudaStreamSynchronize(ctx->stream));  // `packed` is pageable and local
   return NEWT_OK;
 }
 

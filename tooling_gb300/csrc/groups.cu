@@ -357,28 +357,16 @@ int HostGroup::flush_model(newt_gpu_ctx* ctx) {
       CKG(cudaMemcpy(dpairs, gpairs.data(), gpairs.size() * sizeof(int), cudaMemcpyHostToDevice));
   }
   if (!model_dirty) return NEWT_OK;
-  // upload only the newly written worlds: other worlds of the group may be
-  // mid-rollout on the device, with a stale host mirror
+  // upload only the newly written worlds (their whole records): other worlds
+  // of the group may be mid-rollout on the device, with a stale host mirror;
+  // one packed copy and one scatter launch per block, or one strided copy
+  // when the worlds are consecutive
   std::sort(pending.begin(), pending.end());
-  size_t i = 0;
-  while (i < pending.size()) {
-    size_t j = i + 1;
-    while (j < pending.size() && pending[j] == pending[j - 1] + 1) ++j;
-    const size_t a = pending[i], k = j - i;
-    if (soa()) {
-      CKG(cudaMemcpy2DAsync(dF + a, cap * sizeof(float), hF.data() + a, cap * sizeof(float), k * sizeof(float), frows,
-                            cudaMemcpyHostToDevice, ctx->stream));
-      CKG(cudaMemcpy2DAsync(dI + a, cap * sizeof(int), hI.data() + a, cap * sizeof(int), k * sizeof(int), irows,
-                            cudaMemcpyHostToDevice, ctx->stream));
-    } else {
-      CKG(cudaMemcpyAsync(dF + a * frows, hF.data() + a * frows, k * frows * sizeof(float), cudaMemcpyHostToDevice,
-                          ctx->stream));
-      CKG(cudaMemcpyAsync(dI + a * irows, hI.data() + a * irows, k * irows * sizeof(int), cudaMemcpyHostToDevice,
-                          ctx->stream));
-    }
-    i = j;
-  }
-  CKG(cudaStreamSynchronize(ctx->stream));
+  std::vector<RowMove> mv;
+  mv.push_back(RowMove{this, pending, 0, frows, false});
+  mv.push_back(RowMove{this, pending, 0, irows, true});
+  const int rc = io_scatter(ctx, mv);
+  if (rc != NEWT_OK) return rc;
   pending.clear();
   model_dirty = false;
   return NEWT_OK;

@@ -122,14 +122,20 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
 // ---------------------------------------------------------------------------
 // groups
 // ---------------------------------------------------------------------------
-HostGroup* find_or_make_group(newt_gpu_ctx* ctx, const HostModel& m) {
+HostGroup* find_or_make_group(newt_gpu_ctx* ctx, HostModel& m) {
+  if (m.group >= 0) return ctx->groups[m.group].get();
+  if (m.key.empty()) m.key = m.topo_key();
   for (auto& g : ctx->groups)
-    if (g->kind == m.kind && g->size == m.size && g->np == m.np && g->topo_key == m.topo_key()) return g.get();
+    if (g->kind == m.kind && g->size == m.size && g->np == m.np && g->topo_key == m.key) {
+      m.group = g->id;
+      return g.get();
+    }
   auto g = std::make_unique<HostGroup>();
-  g->kind = m.kind; g->size = m.size; g->np = m.np; g->topo_key = m.topo_key();
+  g->kind = m.kind; g->size = m.size; g->np = m.np; g->topo_key = m.key;
   g->nq = m.nq; g->nv = m.nv;
   if (m.kind == GK_TREE_CONTACT) g->setup_tc(m);
   g->id = (int)ctx->groups.size();
+  m.group = g->id;
   ctx->groups.push_back(std::move(g));
   return ctx->groups.back().get();
 }

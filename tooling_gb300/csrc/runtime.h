@@ -21,6 +21,8 @@ struct HostModel {
   std::vector<newt_geom_desc> geoms;
   float dt = 0.005f, g[3] = {0, 0, -9.81f};
   int solver = 1, iterations = 20, self_coll = 0;
+  std::string key;  // topo_key(), computed once at upload
+  int group = -1;   // the group its worlds live in, once one exists
   // topology key: trees in one group must share parent/joint layout
   std::string topo_key() const {
     std::string k;
@@ -179,18 +181,20 @@ struct newt_gpu_ctx {
   bool ctrl_dirty = false;
 };
 
-// rows [lo, lo + cnt) of the worlds `idx` of one group
+// rows [lo, lo + cnt) of the worlds `idx` of one group (of its int block
+// when `ints`, moved as raw 32-bit words)
 struct RowMove {
   HostGroup* g;
   std::vector<int> idx;
   size_t lo, cnt;
+  bool ints = false;
 };
 int io_scatter(newt_gpu_ctx* ctx, const std::vector<RowMove>& mv);  // host mirror -> device
 int io_gather(newt_gpu_ctx* ctx, const std::vector<RowMove>& mv);   // device -> host mirror
 int io_clear_flags(newt_gpu_ctx* ctx, const std::vector<int*>& flags);  // *flag = 0 on the device
 void ctrl_release_slot(newt_gpu_ctx* ctx, int slot);                     // ends the slot's control stream
 
-HostGroup* find_or_make_group(newt_gpu_ctx* ctx, const HostModel& m);
+HostGroup* find_or_make_group(newt_gpu_ctx* ctx, HostModel& m);
 int step_plain(newt_gpu_ctx* ctx, int n_steps);
 int step_batched(newt_gpu_ctx* ctx, int n_steps);
 int autotune_batched(newt_gpu_ctx* ctx, int n_steps, int32_t* choice);

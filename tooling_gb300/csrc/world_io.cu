@@ -10,6 +10,7 @@
 // launch are coalesced: tree groups keep fields as rows x cap (packed as
 // rows x k), pile groups keep worlds contiguous (packed as k x rows).
 #include <algorithm>
+#include <cstring>
 
 #include "runtime.h"
 
@@ -104,8 +105,9 @@ bool consecutive(const std::vector<int>& idx) {
 cudaError_t copy_run(const RowMove& m, cudaStream_t st, bool to_device) {
   HostGroup& g = *m.g;
   const size_t a = (size_t)m.idx[0], k = m.idx.size();
-  float* h = g.hF.data();
-  float* d = g.dF;
+  float* h = m.ints ? reinterpret_cast<float*>(g.hI.data()) : g.hF.data();
+  float* d = m.ints ? reinterpret_cast<float*>(g.dI) : g.dF;
+  const size_t rows = m.ints ? g.irows : g.frows;
   if (g.soa()) {  // cnt rows of k consecutive worlds, row pitch cap
     const size_t off = m.lo * g.cap + a, pitch = g.cap * sizeof(float);
     return to_device ? cudaMemcpy2DAsync(d + off, pitch, h + off, pitch, k * sizeof(float), m.cnt,
@@ -113,7 +115,7 @@ cudaError_t copy_run(const RowMove& m, cudaStream_t st, bool to_device) {
                      : cudaMemcpy2DAsync(h + off, pitch, d + off, pitch, k * sizeof(float), m.cnt,
                                          cudaMemcpyDeviceToHost, st);
   }
-  const size_t off = a * g.frows + m.lo, pitch = g.frows * sizeof(float);  // k worlds of cnt values
+  const size_t off = a * rows + m.lo, pitch = rows * sizeof(float);  // k worlds of cnt values
   return to_device ? cudaMemcpy2DAsync(d + off, pitch, h + off, pitch, m.cnt * sizeof(float), k,
                                        cudaMemcpyHostToDevice, st)
                    : cudaMemcpy2DAsync(h + off, pitch, d + off, pitch, m.cnt * sizeof(float), k,
@@ -145,7 +147,9 @@ int io_scatter(newt_gpu_ctx* ctx, const std::vector<RowMove>& all) {
     float* out = hf + L.foff[s];
     for (size_t j = 0; j < k; ++j)
       for (size_t r = 0; r < m.cnt; ++r) {
-        const float v = g.Fc(m.lo + r, m.idx[j]);
+        float v;
+        if (m.ints) { const int iv = g.Ic(m.lo + r, m.idx[j]); std::memcpy(&v, &iv, sizeof(v)); }
+        else v = g.Fc(m.lo + r, m.idx[j]);
         if (g.soa()) out[r * k + j] = v; else out[j * m.cnt + r] = v;
       }
   }
@@ -156,7 +160,9 @@ int io_scatter(newt_gpu_ctx* ctx, const std::vector<RowMove>& all) {
     const RowMove& m = mv[s];
     const long total = (long)m.idx.size() * m.cnt;
     if (total == 0) continue;
-    rows_scatter<<<grid_for(total), 256, 0, ctx->stream>>>(m.g->dF, m.g->soa() ? 1 : 0, m.g->cap, (int)m.g->frows,
+    rows_scatter<<<grid_for(total), 256, 0, ctx->stream>>>(m.ints ? reinterpret_cast<float*>(m.g->dI) : m.g->dF,
+                                                            m.g->soa() ? 1 : 0, m.g->cap,
+                                                            (int)(m.ints ? m.g->irows : m.g->frows),
                                                             (int)m.lo, (int)m.cnt, di + L.ioff[s], (int)m.idx.size(),
                                                             df + L.foff[s]);
     ctx->launches++;
@@ -188,7 +194,9 @@ int io_gather(newt_gpu_ctx* ctx, const std::vector<RowMove>& all) {
     const RowMove& m = mv[s];
     const long total = (long)m.idx.size() * m.cnt;
     if (total == 0) continue;
-    rows_gather<<<grid_for(total), 256, 0, ctx->stream>>>(m.g->dF, m.g->soa() ? 1 : 0, m.g->cap, (int)m.g->frows,
+    rows_gather<<<grid_for(total), 256, 0, ctx->stream>>>(m.ints ? reinterpret_cast<const float*>(m.g->dI) : m.g->dF,
+                                                           m.g->soa() ? 1 : 0, m.g->cap,
+                                                           (int)(m.ints ? m.g->irows : m.g->frows),
                                                            (int)m.lo, (int)m.cnt, di + L.ioff[s], (int)m.idx.size(),
                                                            df + L.foff[s]);
     ctx->launches++;
@@ -203,7 +211,11 @@ int io_gather(newt_gpu_ctx* ctx, const std::vector<RowMove>& all) {
     const size_t k = m.idx.size();
     const float* in = hf + L.foff[s];
     for (size_t j = 0; j < k; ++j)
-      for (size_t r = 0; r < m.cnt; ++r) g.F(m.lo + r, m.idx[j]) = g.soa() ? in[r * k + j] : in[j * m.cnt + r];
+      for (size_t r = 0; r < m.cnt; ++r) {
+        const float v = g.soa() ? in[r * k + j] : in[j * m.cnt + r];
+        if (m.ints) std::memcpy(&g.I(m.lo + r, m.idx[j]), &v, sizeof(v));
+        else g.F(m.lo + r, m.idx[j]) = v;
+      }
   }
   return NEWT_OK;
 }
