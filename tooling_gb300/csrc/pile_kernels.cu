@@ -419,7 +419,9 @@ NEWT_D int find_seg(const int* seg, int ng, int t) {
 // ---------------------------------------------------------------------------
 // K1: collide + assemble (one warp per world)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) pile_k_collide(const PileGroupDev* G, const int* wseg, int ng, int total,
+// Six blocks per SM (80 registers, a few spills) measured 2.6% faster on the
+// 8192-world pile step than four (128 registers).
+__global__ void __launch_bounds__(128, 6) pile_k_collide(const PileGroupDev* G, const int* wseg, int ng, int total,
                                                       IslandLists il) {
   const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (t >= total) return;
