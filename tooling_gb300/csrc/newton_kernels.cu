@@ -192,6 +192,38 @@ NEWT_D bool warp_cholesky(T* A, int n, int ld, int lane, T* min_piv, T* max_piv)
   return true;
 }
 
+// Two independent n x n factorisations (same order) in one pass, so the
+// lanes' dependent update chains of the two matrices overlap.  Returns false
+// when either has a non-positive pivot.
+NEWT_D bool warp_cholesky2(float* A, float* B, int n, int ld, int lane) {
+  for (int k = 0; k < n; ++k) {
+    __syncwarp();
+    const float akk = A[(size_t)k * ld + k], bkk = B[(size_t)k * ld + k];
+    if (!(akk > 0.f) || !(bkk > 0.f)) return false;
+    const float la = sqrtf(akk), lb = sqrtf(bkk);
+    const float ia = 1.f / la, ib = 1.f / lb;
+    __syncwarp();
+    for (int i = k + 1 + lane; i < n; i += 32) {
+      A[(size_t)k * ld + i] *= ia;
+      B[(size_t)k * ld + i] *= ib;
+    }
+    if (lane == 0) {
+      A[(size_t)k * ld + k] = la;
+      B[(size_t)k * ld + k] = lb;
+    }
+    __syncwarp();
+    for (int j = k + 1; j < n; ++j) {
+      const float ajk = A[(size_t)k * ld + j], bjk = B[(size_t)k * ld + j];
+      for (int i = j + lane; i < n; i += 32) {
+        A[(size_t)j * ld + i] -= A[(size_t)k * ld + i] * ajk;
+        B[(size_t)j * ld + i] -= B[(size_t)k * ld + i] * bjk;
+      }
+    }
+  }
+  __syncwarp();
+  return true;
+}
+
 // Solves L L^T z = rhs in place on the shared vector `v` (length n) with the
 // column-major factor L: forward substitution column by column (lanes update
 // the rows below), then backward substitution by row dot products.
@@ -540,7 +572,7 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   }
   __syncwarp();
   float mn, mx;
-  if (!warp_cholesky(LM, nv, nv, lane, &mn, &mx) || !warp_cholesky(LD, nv, nv, lane, &mn, &mx)) {
+  if (!warp_cholesky2(LM, LD, nv, nv, lane)) {
     if (lane == 0) atomicOr(g.status + w, status | NEWT_WS_NOT_PD);
     return;
   }
@@ -599,26 +631,27 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
       for (int k = 0; k < nv; ++k) s += Y[(size_t)k * ldj + r] * Y[(size_t)k * ldj + c];
       H[(size_t)c * ld + r] = s;
     }
-  // ---- mean inverse weight of each link's COM (tree_body_invweight0), lane per link ----
-  for (int l = lane; l < L; l += 32) {
-    if (tw[l] == 0.f) continue;  // no rows on this link
-    const float* jv = JV + 3 * nv * l;
-    float tr = 0.f;
-    for (int axis = 0; axis < 3; ++axis) {
+  // ---- mean inverse weight of each link's COM (tree_body_invweight0): three
+  // lanes per link, one per axis, ten links per round ----
+  for (int l0 = 0; l0 < L; l0 += 10) {
+    const int l = l0 + lane / 3, axis = lane % 3;
+    float s2 = 0.f;
+    if (lane < 30 && l < L && tw[l] != 0.f) {  // links that own rows
       // |L_D^-1 jv_axis|^2 = jv_axis^T M^-1 jv_axis (forward substitution only)
+      const float* jv = JV + 3 * nv * l;
       float y[NEWT_MAX_LINKS + 5];
-      float s2 = 0.f;
       for (int k = 0; k < nv; ++k) {
         float s = jv[3 * k + axis];
         for (int m = 0; m < k; ++m) s -= LD[m * nv + k] * y[m];
         y[k] = s / LD[k * nv + k];
         s2 += y[k] * y[k];
       }
-      tr += s2;
     }
-    tw[l] = tr / 3.f;
+    const float s2y = __shfl_down_sync(0xffffffffu, s2, 1), s2z = __shfl_down_sync(0xffffffffu, s2, 2);
+    __syncwarp();
+    if (lane < 30 && axis == 0 && l < L && tw[l] != 0.f) tw[l] = ((s2 + s2y) + s2z) / 3.f;
+    __syncwarp();
   }
-  __syncwarp();
 
   // ---- regulariser, diagonal and bias per row (solver.rs:3068-3121) ----
   for (int r = lane; r < nr; r += 32) {
