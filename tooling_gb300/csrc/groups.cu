@@ -251,6 +251,23 @@ void HostGroup::setup_tc(const HostModel& m) {
     }
   npairs = (int)gpairs.size() / 2;
   if (maxc < 1) maxc = 1;
+  // tree structure for the mass matrix: per link its subtree (itself and its
+  // descendants) as a 64-bit mask (two ints), then the link of every DoF
+  const int L = m.n_links;
+  std::vector<unsigned long long> desc(L, 0ull);
+  for (int l = L - 1; l >= 0; --l) {
+    desc[l] |= 1ull << l;
+    if (m.links[l].parent >= 0) desc[m.links[l].parent] |= desc[l];
+  }
+  for (int l = 0; l < L; ++l) {
+    gtopo.push_back((int)(unsigned)(desc[l] & 0xffffffffull));
+    gtopo.push_back((int)(unsigned)(desc[l] >> 32));
+  }
+  for (int l = 0; l < L; ++l) {
+    const int jt = m.links[l].joint;
+    const int nd = jt == NEWT_JOINT_FREE ? 6 : (jt == NEWT_JOINT_FIXED ? 0 : 1);
+    for (int k = 0; k < nd; ++k) gtopo.push_back(l);
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -50,7 +50,8 @@ struct TcGroupDev {
   int ng;            // geoms per world (link geoms and static planes, model order)
   int npairs;        // candidate (static, link geom) pairs, newt's pair order
   int maxc;          // contact capacity per world
-  const int* gtopo;  // [2*ng] shape, link (-1 static); then [ng] condim
+  const int* gtopo;  // [2*ng] shape, link (-1 static); [ng] condim; [2*L] subtree masks (lo, hi);
+                     // [nv] the link of each DoF
   const int* pairs;  // [2*npairs] geom indices (a < b)
   const float* geom; // 21 SoA rows per geom: size3 pos3 quat4 fric margin gap solref2 solimp5
   const int* mode;   // per world: NEWT_SOLVER_PGS | NEWT_SOLVER_NEWTON

@@ -540,17 +540,29 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   // ---- mass matrix (lower triangle, column-major), lane per entry ----
   float* LM = sv + sm.lm;   // factor of M + dt B (response, qacc)
   float* LD = sv + sm.ldf;  // factor of M (diagApprox)
+  // Only links below both DoFs' joints contribute (the others' Jacobian
+  // columns are zero): entry (i, j), i >= j, sums the subtree of DoF i's link
+  // when DoF j's link is an ancestor of it and is zero otherwise, in link
+  // order like the full sum.
+  const int* dmask = G.gtopo + 3 * G.ng;  // subtree masks (lo, hi) per link
+  const int* dlink = dmask + 2 * L;      // link of each DoF
+  auto subtree = [&](int a) {
+    return ((unsigned long long)(unsigned)dmask[2 * a + 1] << 32) | (unsigned)dmask[2 * a];
+  };
   for (int e = lane; e < nv * nv; e += 32) {
     const int i = e % nv, j = e / nv;
     if (i < j) continue;
+    const int ai = dlink[i], aj = dlink[j];
     float s = 0.f;
-    for (int l = 0; l < L; ++l) {
-      const float* jv = JV + 3 * nv * l;
-      const float* jw = JW + 3 * nv * l;
-      const float* iw = IW + 6 * l;
-      const S3 I{iw[0], iw[1], iw[2], iw[3], iw[4], iw[5]};
-      s += MS[l] * dot(ldv3(jv + 3 * i), ldv3(jv + 3 * j)) + dot(ldv3(jw + 3 * i), smv(I, ldv3(jw + 3 * j)));
-    }
+    if ((subtree(aj) >> ai) & 1ull)
+      for (unsigned long long m = subtree(ai); m; m &= m - 1ull) {
+        const int l = __ffsll((long long)m) - 1;
+        const float* jv = JV + 3 * nv * l;
+        const float* jw = JW + 3 * nv * l;
+        const float* iw = IW + 6 * l;
+        const S3 I{iw[0], iw[1], iw[2], iw[3], iw[4], iw[5]};
+        s += MS[l] * dot(ldv3(jv + 3 * i), ldv3(jv + 3 * j)) + dot(ldv3(jw + 3 * i), smv(I, ldv3(jw + 3 * j)));
+      }
     LD[j * nv + i] = s;
   }
   __syncwarp();

@@ -95,6 +95,7 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
   }
   if (d.n_links > 0 && d.n_bodies == 0 && d.n_geoms > 0) {
     // one tree whose link geoms (spheres, boxes, capsules) touch static planes
+    if (d.n_links > 64) return fail(ctx, NEWT_E_INVALID, "tree-contact worlds have at most 64 links");
     int nlink_geoms = 0;
     for (int k = 0; k < d.n_geoms; ++k) {
       const newt_geom_desc& G = d.geoms[k];
