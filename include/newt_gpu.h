@@ -229,7 +229,7 @@ NEWT_API int newt_gpu_set_ctrl_stream(newt_gpu_ctx* ctx, const int32_t* slots, i
 NEWT_API int newt_gpu_apply_ctrl(newt_gpu_ctx* ctx);
 
 /* ---- served rollouts ------------------------------------------------------
- * No counterpart in newt, whose callers (newt/examples/*.rs,
+ * No counterpart in newt, whose callers (the examples in newt/examples,
  * sandbox/src/main.rs:601) own one World and call World::step in their own
  * loop.  newt_gpu_serve is that loop for many requests at once: a request
  * (model, initial state, control sequence, horizon) is admitted into a free

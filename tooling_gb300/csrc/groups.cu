@@ -348,7 +348,9 @@ void HostGroup::write_model(newt_gpu_ctx*, int w, const HostModel& m) {
     for (int b = 0; b < nb; ++b) {
       const newt_body_desc& B = m.bodies[b];
       F(l.mass + b, w) = B.mass;
-      float s6[6], i6[6]; sym6(B.inertia, s6); inv6(B.inertia, i6);
+      float s6[6], i6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      sym6(B.inertia, s6);
+      inv6(B.inertia, i6);  // invertible: checked at upload
       for (int k = 0; k < 6; ++k) { F(l.inert + 6 * b + k, w) = s6[k]; F(l.iinv + 6 * b + k, w) = i6[k]; }
       for (int a = 0; a < 3; ++a) { F(l.pos + 3 * b + a, w) = 0.f; F(l.vel + 3 * b + a, w) = 0.f; F(l.omg + 3 * b + a, w) = 0.f; }
       F(l.quat + 4 * b, w) = 0.f; F(l.quat + 4 * b + 1, w) = 0.f; F(l.quat + 4 * b + 2, w) = 0.f; F(l.quat + 4 * b + 3, w) = 1.f;

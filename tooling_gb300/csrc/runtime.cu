@@ -86,8 +86,15 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
       }
       if (G.condim != 3 && G.condim != 1) return fail(ctx, NEWT_E_INVALID, "condim must be 1 or 3");
     }
-    for (int b = 0; b < d.n_bodies; ++b)
+    for (int b = 0; b < d.n_bodies; ++b) {
       if (per_body[b] != 1) return fail(ctx, NEWT_E_INVALID, "GPU piles need exactly one geom per body");
+      const float* I = d.bodies[b].inertia;  // column-major; Body::new inverts it (newt/src/body.rs)
+      const double det = (double)I[0] * ((double)I[4] * I[8] - (double)I[7] * I[5]) -
+                         (double)I[3] * ((double)I[1] * I[8] - (double)I[7] * I[2]) +
+                         (double)I[6] * ((double)I[1] * I[5] - (double)I[4] * I[2]);
+      if (!(d.bodies[b].mass > 0.f) || !(det > 0.0))
+        return fail(ctx, NEWT_E_INVALID, "free bodies need a positive mass and an invertible inertia");
+    }
     if (np > NEWT_MAX_PLANES) return fail(ctx, NEWT_E_INVALID, "too many planes");
     if (d.solver != NEWT_SOLVER_PGS) return fail(ctx, NEWT_E_INVALID, "GPU piles use the PGS solver");
     m.kind = GK_PILE; m.size = d.n_bodies; m.np = np;
