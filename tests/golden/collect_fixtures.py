@@ -31,6 +31,15 @@ FILES = [
     "references/tree_chain_contact_newton_euler.bin",
     "references/tree_chain_contact_pgs_euler.bin",
     "references/box_plane_mujoco_anchors.json",
+    "references/ballistic.xml",
+    "references/sphere_drop.xml",
+    "references/sphere_drop_stiff.xml",
+    "references/sphere_drop_soft.xml",
+    "references/sphere_drop_stiff_euler.bin",
+    "references/sphere_drop_soft_euler.bin",
+    "references/box_stack.xml",
+    "references/double_pendulum.xml",
+    "references/tree_chain_contact.xml",
     "references/constraint_factor_diagnostics.json",
 ]
 
