@@ -71,6 +71,13 @@ extern "C" {
 #define NEWT_SOLVER_PGS 1
 #define NEWT_SOLVER_NEWTON 2
 
+/* Semi-implicit Euler (the configs' integrator, implicit joint damping) or
+ * classic RK4 (newt's default: four explicit ABA stages, root quaternion
+ * renormalised after the step, newt/src/tree.rs:1234-1364); RK4 is taken for
+ * trees without geoms, and their qacc is the first stage's. */
+#define NEWT_INTEGRATOR_EULER 0
+#define NEWT_INTEGRATOR_RK4 1
+
 typedef struct newt_link_desc {      /* newt::tree::Link */
   int32_t parent;                    /* -1 for the root (link 0) */
   int32_t joint;                     /* NEWT_JOINT_* */
@@ -113,6 +120,7 @@ typedef struct newt_model_desc {     /* one world's model: at most one tree */
   int32_t solver;                    /* NEWT_SOLVER_PGS | NEWT_SOLVER_NEWTON */
   int32_t iterations;                /* PGS sweeps / Newton iteration cap */
   int32_t tree_self_collision;       /* 0: in-tree geom pairs are skipped */
+  int32_t integrator;                /* NEWT_INTEGRATOR_*: World::integrator (newt/src/world.rs:76-84) */
 } newt_model_desc;
 
 /* ---- context ------------------------------------------------------------ */

@@ -64,6 +64,10 @@ static void tree_rows(HostGroup& g) {
   g.r_qacc = r; r += g.nv;
   g.ri_solver = 0; g.ri_live = 1; g.ri_status = 2;
   g.irows = 3;
+  if (g.kind == GK_TREE) {  // integrator per world
+    g.ri_integ = 3;
+    g.irows = 4;
+  }
   if (g.kind == GK_TREE_CONTACT) {  // per-geom model rows (TcGroupDev::geom), solver mode
     g.r_geom = r; r += 21 * g.ng;
     g.ri_mode = 3; g.ri_iters = 4;
@@ -307,6 +311,7 @@ void HostGroup::write_model(newt_gpu_ctx*, int w, const HostModel& m) {
     I(ri_solver, w) = m.solver != 0;
     I(ri_live, w) = 1;
     I(ri_status, w) = 0;
+    if (ri_integ >= 0) I(ri_integ, w) = m.integrator;
     if (kind == GK_TREE_CONTACT) {
       for (int k = 0; k < ng; ++k) {
         const newt_geom_desc& G = m.geoms[k];
@@ -585,6 +590,7 @@ TreeGroupDev HostGroup::tree_dev() const {
   d.inert = row(r_inert); d.damp = row(r_damp); d.arm = row(r_arm); d.dtg = row(r_dtg);
   d.solver = dI + (size_t)ri_solver * cap;
   d.live = dI + (size_t)ri_live * cap;
+  d.integ = ri_integ >= 0 ? dI + (size_t)ri_integ * cap : nullptr;
   d.q = row(r_q); d.qd = row(r_qd); d.qfrc = row(r_qfrc); d.qacc = row(r_qacc);
   d.status = (uint32_t*)(dI + (size_t)ri_status * cap);
   return d;

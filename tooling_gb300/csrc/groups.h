@@ -34,6 +34,7 @@ struct TreeGroupDev {
   const float* dtg;    // 4    dt, gx, gy, gz
   const int* solver;   // 1    nonzero enables free-root qfrc (newt/src/forces.rs:16-31)
   const int* live;     // 1    nonzero for allocated worlds
+  const int* integ;    // 1    NEWT_INTEGRATOR_* (null: Euler for every world)
   // per-world state (SoA)
   float* q;     // nq  (newt layout: free root p xyz, quat xyzw; hinge angle)
   float* qd;    // nv  (free root: omega_body, v_body; hinge rate)

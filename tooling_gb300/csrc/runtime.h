@@ -20,7 +20,7 @@ struct HostModel {
   std::vector<newt_body_desc> bodies;
   std::vector<newt_geom_desc> geoms;
   float dt = 0.005f, g[3] = {0, 0, -9.81f};
-  int solver = 1, iterations = 20, self_coll = 0;
+  int solver = 1, iterations = 20, self_coll = 0, integrator = NEWT_INTEGRATOR_EULER;
   std::string key;  // topo_key(), computed once at upload
   int group = -1;   // the group its worlds live in, once one exists
   // topology key: trees in one group must share parent/joint layout
@@ -70,7 +70,7 @@ struct HostGroup {
   // tree layout rows
   int r_axis = 0, r_jp = 0, r_jc = 0, r_rootq = 0, r_mass = 0, r_inert = 0, r_damp = 0, r_arm = 0, r_dtg = 0;
   int r_q = 0, r_qd = 0, r_qfrc = 0, r_qacc = 0;
-  int ri_solver = 0, ri_live = 0, ri_status = 0;
+  int ri_solver = 0, ri_live = 0, ri_status = 0, ri_integ = -1;
   // pile layout
   PileLayout lay{};
   int maxc = 0;

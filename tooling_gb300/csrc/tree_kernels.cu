@@ -19,6 +19,7 @@
 //     one launch per stage per step with state round-tripping through HBM.
 #include "common.cuh"
 #include "groups.h"
+#include "../../include/newt_gpu.h"
 
 namespace {
 
@@ -34,11 +35,13 @@ struct LinkScratch {
 
 // Per-world ABA (forward dynamics).  q/qd/qfrc are the world's state in newt
 // layout; writes qdd.  `scr` is MAXL entries of per-link scratch.
+// `idt`: the step folded into the joint damping (dt for semi-implicit Euler,
+// 0 for the explicit RK4 stages).
 template <int MAXL>
 __device__ bool tree_aba(const TreeGroupDev& g, int w, const float* q, const float* qd, const float* qfrc,
-                         float* qdd, LinkScratch* scr) {
+                         float* qdd, LinkScratch* scr, float idt) {
   const int L = g.L, cap = g.cap;
-  const float dt = g.dtg[w];
+  const float dt = idt;
   const V3 grav = v3(g.dtg[cap + w], g.dtg[2 * cap + w], g.dtg[3 * cap + w]);
   V3 gb[MAXL];  // gravity in each link frame
   // ---- pass 1 (root -> leaves): transforms, velocities, bias ----
@@ -177,6 +180,66 @@ __device__ void tree_integrate(const TreeGroupDev& g, int w, float* q, float* qd
   }
 }
 
+// One classic RK4 step (newt/src/tree.rs:1234-1364, derivative of a stage
+// state tree.rs:1485-1550): four explicit ABA stages, stage states
+// q0 + h dq, the weighted sum (dq1 + 2 dq2 + 2 dq3 + dq4) dt/6, then the free
+// root's quaternion renormalised by division (Quat::renormalize).  `qdd`
+// receives the first stage's acceleration.
+template <int MAXL>
+__device__ bool tree_rk4(const TreeGroupDev& g, int w, float* q, float* qd, const float* qf, float* qdd,
+                         LinkScratch* scr) {
+  const int L = g.L, nq = g.nq, nv = g.nv;
+  const float dt = g.dtg[w];
+  float q0[MAXL + 6], v0[MAXL + 5], aq[MAXL + 6], av[MAXL + 5], dq[MAXL + 6], a[MAXL + 5];
+  for (int k = 0; k < nq; ++k) q0[k] = q[k];
+  for (int k = 0; k < nv; ++k) v0[k] = qd[k];
+  bool ok = true;
+  for (int s = 0; s < 4; ++s) {
+    ok = tree_aba<MAXL>(g, w, q, qd, qf, a, scr, 0.f) && ok;
+    if (s == 0)
+      for (int k = 0; k < nv; ++k) qdd[k] = a[k];
+    for (int k = 0; k < nq; ++k) dq[k] = 0.f;
+    for (int i = 0; i < L; ++i) {
+      const int jt = g.topo[4 * i + 1], qo = g.topo[4 * i + 2], vo = g.topo[4 * i + 3];
+      if (jt == JF) {
+        const Q4 ori{q[qo + 3], q[qo + 4], q[qo + 5], q[qo + 6]};
+        const V3 vw = qrot(ori, v3(qd[vo + 3], qd[vo + 4], qd[vo + 5]));
+        dq[qo] = vw.x; dq[qo + 1] = vw.y; dq[qo + 2] = vw.z;
+        const Q4 d = qmul(ori, Q4{qd[vo], qd[vo + 1], qd[vo + 2], 0.f});
+        dq[qo + 3] = d.x * 0.5f; dq[qo + 4] = d.y * 0.5f; dq[qo + 5] = d.z * 0.5f; dq[qo + 6] = d.w * 0.5f;
+      } else if (jt == JH || jt == JS) {
+        dq[qo] = qd[vo];
+      }
+    }
+    if (s == 0) {
+      for (int k = 0; k < nq; ++k) aq[k] = dq[k];
+      for (int k = 0; k < nv; ++k) av[k] = a[k];
+    } else {
+      const float wgt = s == 3 ? 1.f : 2.f;
+      for (int k = 0; k < nq; ++k) aq[k] += wgt * dq[k];
+      for (int k = 0; k < nv; ++k) av[k] += wgt * a[k];
+    }
+    if (s == 3) break;
+    const float h = s < 2 ? dt * 0.5f : dt;
+    for (int k = 0; k < nq; ++k) q[k] = q0[k] + dq[k] * h;
+    for (int k = 0; k < nv; ++k) qd[k] = v0[k] + a[k] * h;
+  }
+  const float c = dt * (1.f / 6.f);
+  for (int k = 0; k < nq; ++k) q[k] = q0[k] + aq[k] * c;
+  for (int k = 0; k < nv; ++k) qd[k] = v0[k] + av[k] * c;
+  if (g.topo[1] == JF) {
+    const int o = g.topo[2] + 3;
+    const float n = sqrtf(q[o] * q[o] + q[o + 1] * q[o + 1] + q[o + 2] * q[o + 2] + q[o + 3] * q[o + 3]);
+    if (n == 0.f) { q[o] = 0.f; q[o + 1] = 0.f; q[o + 2] = 0.f; q[o + 3] = 1.f; }
+    else { q[o] /= n; q[o + 1] /= n; q[o + 2] /= n; q[o + 3] /= n; }
+  }
+  return ok;
+}
+
+__device__ __forceinline__ bool is_rk4(const TreeGroupDev& g, int w) {
+  return g.integ && g.integ[w] == NEWT_INTEGRATOR_RK4;
+}
+
 __device__ __forceinline__ bool finite_all(const float* a, int n) {
   bool ok = true;
   for (int k = 0; k < n; ++k) ok = ok && isfinite(a[k]);
@@ -194,8 +257,13 @@ __device__ __forceinline__ void tree_world_steps(const TreeGroupDev& g, int w, i
   for (int k = 0; k < nv; ++k) { qd[k] = g.qd[k * cap + w]; qf[k] = g.qfrc[k * cap + w]; qdd[k] = 0.f; }
   LinkScratch scr[MAXL];
   uint32_t st = 0;
+  const bool rk4 = is_rk4(g, w);
   for (int s = 0; s < n_steps; ++s) {
-    if (!tree_aba<MAXL>(g, w, q, qd, qf, qdd, scr)) st |= NEWT_WS_NOT_PD;
+    if (rk4) {
+      if (!tree_rk4<MAXL>(g, w, q, qd, qf, qdd, scr)) st |= NEWT_WS_NOT_PD;
+      continue;
+    }
+    if (!tree_aba<MAXL>(g, w, q, qd, qf, qdd, scr, g.dtg[w])) st |= NEWT_WS_NOT_PD;
     tree_integrate<MAXL>(g, w, q, qd, qdd);
   }
   if (!finite_all(q, nq) || !finite_all(qd, nv)) st |= NEWT_WS_NONFINITE;
@@ -243,7 +311,15 @@ __global__ void __launch_bounds__(128) tree_aba_kernel(TreeGroupDev g) {
   for (int k = 0; k < nq; ++k) q[k] = g.q[k * cap + w];
   for (int k = 0; k < nv; ++k) { qd[k] = g.qd[k * cap + w]; qf[k] = g.qfrc[k * cap + w]; qdd[k] = 0.f; }
   LinkScratch scr[MAXL];
-  if (!tree_aba<MAXL>(g, w, q, qd, qf, qdd, scr)) g.status[w] |= NEWT_WS_NOT_PD;
+  if (is_rk4(g, w)) {  // the whole RK4 step here; the integrate stage skips the world
+    uint32_t st = tree_rk4<MAXL>(g, w, q, qd, qf, qdd, scr) ? 0u : NEWT_WS_NOT_PD;
+    if (!finite_all(q, nq) || !finite_all(qd, nv)) st |= NEWT_WS_NONFINITE;
+    for (int k = 0; k < nq; ++k) g.q[k * cap + w] = q[k];
+    for (int k = 0; k < nv; ++k) { g.qd[k * cap + w] = qd[k]; g.qacc[k * cap + w] = qdd[k]; }
+    if (st) g.status[w] |= st;
+    return;
+  }
+  if (!tree_aba<MAXL>(g, w, q, qd, qf, qdd, scr, g.dtg[w])) g.status[w] |= NEWT_WS_NOT_PD;
   for (int k = 0; k < nv; ++k) g.qacc[k * cap + w] = qdd[k];
 }
 
@@ -251,7 +327,7 @@ __global__ void __launch_bounds__(128) tree_aba_kernel(TreeGroupDev g) {
 template <int MAXL>
 __global__ void __launch_bounds__(128) tree_integrate_kernel(TreeGroupDev g) {
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= g.n || !g.live[w]) return;
+  if (w >= g.n || !g.live[w] || is_rk4(g, w)) return;
   const int cap = g.cap, nq = g.nq, nv = g.nv;
   float q[MAXL + 6], qd[MAXL + 5], qdd[MAXL + 5];
   for (int k = 0; k < nq; ++k) q[k] = g.q[k * cap + w];

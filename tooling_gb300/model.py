@@ -19,6 +19,7 @@ import numpy as np
 JOINT_FREE, JOINT_FIXED, JOINT_HINGE, JOINT_SLIDE, JOINT_BALL = 0, 1, 2, 3, 4
 SHAPE_PLANE, SHAPE_SPHERE, SHAPE_BOX, SHAPE_CAPSULE = 0, 1, 2, 3
 SOLVER_PGS, SOLVER_NEWTON = 1, 2
+INTEGRATOR_EULER, INTEGRATOR_RK4 = 0, 1
 JOINT_NQ = {JOINT_FREE: 7, JOINT_FIXED: 0, JOINT_HINGE: 1, JOINT_SLIDE: 1, JOINT_BALL: 4}
 JOINT_NV = {JOINT_FREE: 6, JOINT_FIXED: 0, JOINT_HINGE: 1, JOINT_SLIDE: 1, JOINT_BALL: 3}
 
@@ -51,7 +52,7 @@ class ModelDesc(C.Structure):
         ("n_links", C.c_int32), ("n_bodies", C.c_int32), ("n_geoms", C.c_int32),
         ("links", C.POINTER(LinkDesc)), ("bodies", C.POINTER(BodyDesc)), ("geoms", C.POINTER(GeomDesc)),
         ("dt", C.c_float), ("gravity", C.c_float * 3), ("solver", C.c_int32), ("iterations", C.c_int32),
-        ("tree_self_collision", C.c_int32),
+        ("tree_self_collision", C.c_int32), ("integrator", C.c_int32),
     ]
 
 
@@ -133,6 +134,7 @@ class WorldModel:
     solver: int = SOLVER_PGS
     iterations: int = 20
     tree_self_collision: int = 0
+    integrator: int = 0  # INTEGRATOR_EULER or INTEGRATOR_RK4 (trees without geoms)
     links: List[Link] = field(default_factory=list)
     bodies: List[tuple] = field(default_factory=list)  # (mass, inertia9)
     geoms: List[Geom] = field(default_factory=list)
@@ -200,6 +202,7 @@ class PackedModels:
             md.gravity[:] = list(m.gravity)
             md.solver, md.iterations = m.solver, m.iterations
             md.tree_self_collision = m.tree_self_collision
+            md.integrator = m.integrator
 
     def __len__(self) -> int:
         return len(self.descs)
@@ -247,7 +250,7 @@ class Batch:
     """
 
     def __init__(self, links, n_links, bodies, n_bodies, geoms, n_geoms, dt, gravity, solver, iterations,
-                 self_coll=0):
+                 self_coll=0, integrator=INTEGRATOR_EULER):
         self.links = np.ascontiguousarray(links)
         self.bodies = np.ascontiguousarray(bodies)
         self.geoms = np.ascontiguousarray(geoms)
@@ -289,6 +292,7 @@ class Batch:
             d.dt = float(dt[w])
             d.gravity[0], d.gravity[1], d.gravity[2] = gravity
             d.solver, d.iterations, d.tree_self_collision = int(solver[w]), int(iters[w]), int(self_coll)
+            d.integrator = int(integrator)
         self.qpos = np.zeros(int(nq.sum()), np.float32)
         self.qvel = np.zeros(int(nv.sum()), np.float32)
         self.qfrc = np.zeros(int(nv.sum()), np.float32)
