@@ -74,7 +74,9 @@ extern "C" {
 /* Semi-implicit Euler (the configs' integrator, implicit joint damping) or
  * classic RK4 (newt's default: four explicit ABA stages, root quaternion
  * renormalised after the step, newt/src/tree.rs:1234-1364); RK4 is taken for
- * trees without geoms, and their qacc is the first stage's. */
+ * trees without geoms, whose qacc is the first stage's, and for free-body
+ * piles, whose contact wrenches are solved once at the start of the step and
+ * held over the four stages (newt/src/world.rs:1705-1788). */
 #define NEWT_INTEGRATOR_EULER 0
 #define NEWT_INTEGRATOR_RK4 1
 

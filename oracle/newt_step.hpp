@@ -4,6 +4,8 @@
 //
 // Sources (paths inside hwang2409/tooling):
 //   newt/src/world.rs:1459-1537  World::step
+//   newt/src/world.rs:1705-1788  step_bodies (RK4, solver wrenches held)
+//   newt/src/world.rs:3258-3271  advance_all
 //   newt/src/world.rs:1790-1817  step_bodies_euler
 //   newt/src/world.rs:1952-2051  step_trees_euler
 //   newt/src/world.rs:2097-2152  compute_solver_wrenches
@@ -25,6 +27,48 @@ template <class R> Deriv<R> evaluate(const Body<R>& s, Vec3<R> g, Vec3<R> f, Vec
   return {dlin, dang};
 }
 
+// step_bodies (world.rs:1705-1788): the solver wrenches are computed once at
+// the start state and held over the four stages; stage states start from s0
+// (advance_all, world.rs:3258-3271) and keep their orientations unnormalised.
+template <class R> void World<R>::step_bodies_rk4(bool solver, const std::vector<Contact<R>>& free_contacts) {
+  const size_t n = bodies.size();
+  std::vector<Wrench<R>> ext(n, Wrench<R>{Vec3<R>(), Vec3<R>()});
+  if (solver) {
+    solve_free_bodies_pgs(bodies, geoms, free_contacts, gravity, dt, iterations, ext);
+    for (size_t i = 0; i < n; ++i) { ext[i].f += tree_body_wrenches[i].f; ext[i].t += tree_body_wrenches[i].t; }
+  }
+  struct K { Vec3<R> dp, dv; Quat<R> dq; Vec3<R> dw; };
+  auto eval = [&](const Body<R>& s, size_t i) {
+    Deriv<R> d = evaluate(s, gravity, ext[i].f, ext[i].t);
+    return K{s.vel, d.dlin, s.ori.derivative(s.omega_body), d.dang};
+  };
+  auto advance = [&](const Body<R>& o, const K& k, R h) {
+    Body<R> b = o;
+    b.pos = o.pos + k.dp * h;
+    b.vel = o.vel + k.dv * h;
+    b.ori = o.ori + k.dq * h;
+    b.omega_body = o.omega_body + k.dw * h;
+    return b;
+  };
+  const std::vector<Body<R>> s0 = bodies;
+  for (size_t i = 0; i < n; ++i) {
+    K k1 = eval(s0[i], i);
+    K k2 = eval(advance(s0[i], k1, dt * R(0.5)), i);
+    K k3 = eval(advance(s0[i], k2, dt * R(0.5)), i);
+    K k4 = eval(advance(s0[i], k3, dt), i);
+    const R sixth = R(1.0) / R(6.0);
+    Vec3<R> dp = (k1.dp + k2.dp * R(2.0) + k3.dp * R(2.0) + k4.dp) * sixth;
+    Vec3<R> dv = (k1.dv + k2.dv * R(2.0) + k3.dv * R(2.0) + k4.dv) * sixth;
+    Quat<R> dq = (k1.dq + k2.dq * R(2.0) + k3.dq * R(2.0) + k4.dq) * sixth;
+    Vec3<R> dw = (k1.dw + k2.dw * R(2.0) + k3.dw * R(2.0) + k4.dw) * sixth;
+    Body<R>& b = bodies[i];
+    b.pos = s0[i].pos + dp * dt;
+    b.vel = s0[i].vel + dv * dt;
+    b.ori = (s0[i].ori + dq * dt).renormalize();
+    b.omega_body = s0[i].omega_body + dw * dt;
+  }
+}
+
 template <class R> void World<R>::step() {
   const bool solver = solver_mode == M_PGS || solver_mode == M_NEWTON;
   std::vector<Contact<R>> contacts;
@@ -42,7 +86,7 @@ template <class R> void World<R>::step() {
   if (integrator == 0) {
     // RK4 (world.rs:1495-1498): step_bodies, then step_trees (world.rs:1826-1945)
     // with the solver's generalised forces held over the four stages.
-    if (!bodies.empty()) throw std::runtime_error("RK4 free-body stepping is not restated");
+    if (!bodies.empty()) step_bodies_rk4(solver, free_contacts);
     for (size_t ti = 0; ti < trees.size(); ++ti) {
       Tree<R>& tree = trees[ti];
       const bool prior = tree.disable_penalty_limits;

@@ -733,6 +733,7 @@ template <class R> struct World {
   std::vector<Wrench<R>> tree_body_wrenches;    // per free body
 
   void step();  // defined after the tree-contact solver
+  void step_bodies_rk4(bool solver, const std::vector<Contact<R>>& free_contacts);
 };
 
 }  // namespace oracle

@@ -19,6 +19,7 @@ FILES = [
     "goldens/dynamics_mass_bias.bin",
     "goldens/joints_chain_and_floating.bin",
     "goldens/solver_stack.bin",
+    "goldens/solver_incline.bin",
     "goldens/solver_newton_stack.bin",
     "goldens/solver_tree.bin",
     "goldens/solver_newton_tree.bin",

@@ -1,9 +1,14 @@
-"""RK4 (newt's default integrator) for trees without geoms on the GPU.
+"""RK4 (newt's default integrator) on the GPU: trees without geoms, and
+free-body piles with the PGS wrench held over the stages.
 
 Pinned to newt's own output: the joints golden (newt/tests/joints_golden.rs:
-a fixed-root hinge chain and a floating box with an arm, RK4, f32) after 100
-and 1000 steps; and tracked against the FP64 oracle's RK4 on the 7-link
-chains.  Worlds with geoms stay on Euler (their contacts use it)."""
+a fixed-root hinge chain and a floating box with an arm) after 100 and 1000
+steps; the free-body integrator golden (integrators_golden.rs); the PGS
+solver goldens (solver_golden.rs: a three-box stack and a box on an incline,
+solved once per step and held over the RK4 stages).  The stack is chaotic (the
+FP64 oracle and newt's f32 run drift 2 cm apart by step 200), so it is held
+to one-step parity from newt's own snapshots and to that FP64 window over 1000
+steps.  Trees with geoms stay on Euler."""
 import numpy as np
 import pytest
 
@@ -83,9 +88,106 @@ def test_rk4_chains_track_fp64_oracle(eng):
     assert np.abs(q - eq).max() > 10 * np.abs(q - rq).max()
 
 
-def test_rk4_refused_for_worlds_with_geoms(eng):
-    p = scenes.pile_batch(n_worlds=1)
-    rk = M.Batch(p.links, p.n_links, p.bodies, p.n_bodies, p.geoms, p.n_geoms, 2e-3, (0.0, 0.0, -9.81),
-                 M.SOLVER_PGS, 50, integrator=M.INTEGRATOR_RK4)
+def test_rk4_refused_for_tree_contact_worlds(eng):
+    from test_oracle_golden import _tree_chain_contact
+    w = _tree_chain_contact(M.SOLVER_PGS)
+    w.integrator = M.INTEGRATOR_RK4
     with pytest.raises(NewtError):
-        eng.upload(rk)
+        eng.upload(M.PackedModels([w]))
+
+
+def _mj(q_newt, nb):
+    """newt free-body layout (pos, quat xyzw) to MuJoCo's (pos, quat wxyz);
+    the velocity layouts (v_world, omega_body) agree."""
+    q = np.asarray(q_newt, np.float32).reshape(nb, 7)
+    return np.concatenate([q[:, :3], q[:, 6:7], q[:, 3:6]], axis=1).reshape(-1)
+
+
+def _pile_world(name):
+    from test_oracle_golden import _integrator_scene, _solver_box_scene
+    if name == "integrator":
+        w, q, v = _integrator_scene()
+        # the pile path wants one geom per body: a sphere with nothing to touch
+        w.add_geom(M.Geom(shape=M.SHAPE_SPHERE, body=0, size=(0.05, 0.0, 0.0)))
+        w.solver, w.iterations = M.SOLVER_PGS, 1  # no contacts: a zero wrench, as in newt's penalty mode
+        gold = _read_f32("integrator_rk4.bin").reshape(3, 1, 13)
+        return w, q, v, gold, (20, 100)
+    w, q, v = _solver_box_scene(name)
+    gold = _read_f32(f"solver_{name}.bin").reshape(4, len(w.bodies), 13)
+    return w, q, v, gold, (50, 200, 1000)
+
+
+def _track(eng, name, mode):
+    w, q, v, gold, marks = _pile_world(name)
+    w.integrator = M.INTEGRATOR_RK4
+    nb = len(w.bodies)
+    slots = eng.alloc(eng.upload(M.PackedModels([w])))
+    eng.set_state(slots, _mj(q, nb), v)
+    done, errs = 0, []
+    for row, n in enumerate(marks, start=1):
+        eng.step(n - done, mode)
+        done = n
+        gq, gv = eng.get_state(slots, 7 * nb, 6 * nb)
+        errs.append((n, float(np.abs(gq - _mj(gold[row][:, :7], nb)).max()),
+                     float(np.abs(gv - gold[row][:, 7:].reshape(-1)).max())))
+    assert not (eng.status(slots) & 0x5).any()
+    eng.free(slots)
+    return errs
+
+
+@pytest.mark.parametrize("mode", [STEP_PLAIN, STEP_BATCHED])
+@pytest.mark.parametrize("name,qtol,vtol", [("integrator", 2e-6, 2e-6), ("incline", 5e-4, 5e-3)])
+def test_pile_rk4_tracks_newt_goldens(eng, name, qtol, vtol, mode):
+    errs = _track(eng, name, mode)
+    assert all(dq < qtol and dv < vtol for _, dq, dv in errs), errs
+
+
+@pytest.mark.parametrize("mode", [STEP_PLAIN, STEP_BATCHED])
+def test_pile_rk4_stack_stays_in_newts_envelope(eng, mode):
+    """Twelve f32 runs of newt's stack from start positions nudged by 1e-7 m
+    land up to 4.1 cm and 0.29 m/s from newt's snapshot at step 1000 (and
+    0.13 m/s at step 50, in the transient).  The GPU run must stay within
+    5 cm of newt's positions at every snapshot and within 0.3 m/s of its
+    velocities once the stack has settled (step 1000)."""
+    errs = _track(eng, "stack", mode)
+    assert all(dq < 5e-2 for _, dq, _ in errs) and errs[-1][2] < 0.3, errs
+
+
+def test_pile_rk4_one_step_from_newt_snapshots(eng):
+    """From each of newt's stack snapshots, one GPU RK4 step against one step
+    of the f32 oracle (itself byte-identical to newt over 1000 steps)."""
+    from test_oracle_golden import _solver_box_scene
+    w, _, _ = _solver_box_scene("stack")
+    w.integrator = M.INTEGRATOR_RK4
+    gold = _read_f32("solver_stack.bin").reshape(4, 3, 13)
+    packed = M.PackedModels([w])
+    ids = eng.upload(packed)
+    for row in range(4):
+        q = np.ascontiguousarray(gold[row][:, :7]).reshape(-1)
+        v = np.ascontiguousarray(gold[row][:, 7:]).reshape(-1)
+        slots = eng.alloc(ids)
+        eng.set_state(slots, _mj(q, 3), v)
+        eng.step(1, STEP_BATCHED)
+        gq, gv = eng.get_state(slots, 21, 18)
+        eng.free(slots)
+        rq, rv = oracle_py.run(packed, np.zeros(1, np.int32), q, v, None, 1, precision=0, layout=1, integrator=0)
+        assert np.abs(gq - _mj(rq, 3)).max() < 2e-6 and np.abs(gv - rv).max() < 2e-4, row
+
+
+def test_pile_rk4_batch_tracks_fp64_oracle(eng):
+    """A settled 48-world pile batch stepped 20 times with RK4: within
+    1e-3 m / 1e-2 m/s of the FP64 oracle's RK4."""
+    b = scenes.pile_batch(n_worlds=48, first_world=500)
+    rq, rv = oracle_py.run(b, np.arange(len(b)), b.qpos, b.qvel, None, 300, precision=1)
+    rk = M.Batch(b.links, b.n_links, b.bodies, b.n_bodies, b.geoms, b.n_geoms, 2e-3, (0.0, 0.0, -9.81),
+                 M.SOLVER_PGS, 50, integrator=M.INTEGRATOR_RK4)
+    rk.qpos[:], rk.qvel[:] = rq.astype(np.float32), rv.astype(np.float32)
+    slots = eng.alloc(eng.upload(rk))
+    eng.set_state(slots, rk.qpos, rk.qvel)
+    eng.step(20, STEP_BATCHED)
+    gq, gv = eng.get_state(slots, int(rk.nq.sum()), int(rk.nv.sum()))
+    eng.free(slots)
+    oq, ov = oracle_py.run(rk, np.arange(len(rk)), rk.qpos, rk.qvel, None, 20, precision=1, integrator=0)
+    assert np.abs(gq - oq).max() < 1e-3 and np.abs(gv - ov).max() < 1e-2
+    eq, _ = oracle_py.run(rk, np.arange(len(rk)), rk.qpos, rk.qvel, None, 20, precision=1, integrator=1)
+    assert np.abs(oq - eq).max() > 0  # the two integrators differ on this state

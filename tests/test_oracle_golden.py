@@ -42,6 +42,66 @@ def test_integrator_euler_golden_is_byte_identical():
     assert got.tobytes() == gold.tobytes(), np.abs(got - gold).max()
 
 
+def test_integrator_rk4_golden_is_byte_identical():
+    """newt/tests/integrators_golden.rs:84-91 (RK4, newt's default): the
+    free-body RK4 of world.rs:1705-1788 with no contacts."""
+    w, qpos, qvel = _integrator_scene()
+    packed = M.PackedModels([w])
+    gold = _read_f32("integrator_rk4.bin").reshape(3, 13)
+    got = [np.concatenate([qpos, qvel])]
+    for n in (20, 100):
+        qo, vo = oracle_py.run(packed, np.zeros(1, np.int32), qpos, qvel, None, n, precision=0, layout=1, integrator=0)
+        got.append(np.concatenate([qo, vo]).astype(np.float32))
+    got = np.stack(got)
+    assert got.tobytes() == gold.tobytes(), np.abs(got - gold).max()
+
+
+def _solver_box_scene(name):
+    """newt/tests/solver_golden.rs:27-79: the PGS stack (three unit boxes with
+    1 cm x offsets) and the incline (one asymmetric box under tilted gravity),
+    World::new() defaults (RK4, pyramidal cone), solref (0.05, 1.5) on every
+    geom.  Returns (model, qpos, qvel) in newt's layout."""
+    sr = (0.05, 1.5)
+    if name == "stack":
+        w = M.WorldModel(dt=0.005, gravity=(0.0, 0.0, -9.81), solver=M.SOLVER_PGS, iterations=30)
+        fric, halves = 0.8, [(0.25, 0.25, 0.25)] * 3
+        poses = [(f32(0.01) * f32(k), 0.0, f32(0.25) + f32(0.5) * f32(k)) for k in range(3)]
+    else:
+        L = oracle_py.lib()
+        ang = f32(f32(32.0) * f32(np.pi)) / f32(180.0)
+        g = f32(9.81)
+        gz = -(g * f32(L.oracle_newt_cos(float(ang))))
+        w = M.WorldModel(dt=0.005, gravity=(float(g * f32(L.oracle_newt_sin(float(ang)))), 0.0, float(gz)),
+                         solver=M.SOLVER_PGS, iterations=30)
+        fric, halves, poses = 0.5, [(0.2, 0.21, 0.19)], [(0.01, 0.0, 0.2)]
+    plane = M.static_plane(friction=fric)
+    plane.solref = sr
+    w.add_geom(plane)
+    qpos, qvel = [], []
+    for h, p in zip(halves, poses):
+        b = w.add_body(1.0, M.solid_box_inertia(1.0, h))
+        w.add_geom(M.Geom(shape=M.SHAPE_BOX, body=b, size=h, friction=fric, solref=sr))
+        qpos += [float(x) for x in p] + [0.0, 0.0, 0.0, 1.0]
+        qvel += [0.0] * 6
+    return w, np.array(qpos, np.float32), np.array(qvel, np.float32)
+
+
+@pytest.mark.parametrize("name", ["stack", "incline"])
+def test_solver_rk4_zoh_goldens_are_byte_identical(name):
+    """newt/tests/solver_golden.rs:164-244: free-body PGS solved once per step
+    and held over the RK4 stages, snapshots after 0, 50, 200 and 1000 steps."""
+    w, qpos, qvel = _solver_box_scene(name)
+    nb = len(w.bodies)
+    gold = _read_f32(f"solver_{name}.bin").reshape(4, nb, 13)
+    got = [np.concatenate([qpos.reshape(nb, 7), qvel.reshape(nb, 6)], axis=1)]
+    packed = M.PackedModels([w])
+    for n in (50, 200, 1000):
+        qo, vo = oracle_py.run(packed, np.zeros(1, np.int32), qpos, qvel, None, n, precision=0, layout=1, integrator=0)
+        got.append(np.concatenate([qo.reshape(nb, 7), vo.reshape(nb, 6)], axis=1).astype(np.float32))
+    got = np.stack(got)
+    assert got.tobytes() == gold.tobytes(), np.abs(got - gold).max(axis=(1, 2))
+
+
 def _renormalize(q):
     n = np.sqrt(f32(f32(f32(q[0] * q[0] + q[1] * q[1]) + q[2] * q[2]) + q[3] * q[3]))
     return [x / n for x in q]

@@ -24,6 +24,7 @@ NEWT_HD V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
 NEWT_HD V3 operator-(V3 a) { return v3(-a.x, -a.y, -a.z); }
 NEWT_HD V3 operator*(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
 NEWT_HD V3 operator*(float s, V3 a) { return v3(a.x * s, a.y * s, a.z * s); }
+NEWT_HD V3 operator/(V3 a, float s) { return v3(a.x / s, a.y / s, a.z / s); }
 NEWT_HD V3& operator+=(V3& a, V3 b) { a = a + b; return a; }
 NEWT_HD V3& operator-=(V3& a, V3 b) { a = a - b; return a; }
 NEWT_HD float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }

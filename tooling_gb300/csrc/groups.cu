@@ -115,6 +115,7 @@ static void pile_rows(HostGroup& g) {
   l.status = q; q += 1;
   l.ncon = q; q += 1;
   l.live = q; q += 1;
+  l.integ = q; q += 1;
   l.cpair = q; q += 2 * g.maxc;
   q = (q + 31) / 32 * 32;
   l.istride = q;
@@ -363,6 +364,7 @@ void HostGroup::write_model(newt_gpu_ctx*, int w, const HostModel& m) {
     F(l.dtg, w) = m.dt; F(l.dtg + 1, w) = m.g[0]; F(l.dtg + 2, w) = m.g[1]; F(l.dtg + 3, w) = m.g[2];
     I(l.iters, w) = m.iterations;
     I(l.status, w) = 0; I(l.ncon, w) = 0; I(l.live, w) = 1;
+    I(l.integ, w) = m.integrator;
   }
   model_dirty = true;
   pending.push_back(w);

@@ -69,7 +69,7 @@ struct PileLayout {
   int pos, quat, vel, omg;
   int cdata, imp;
   // int fields
-  int shape, gent, iters, status, ncon, cpair, live;
+  int shape, gent, iters, status, ncon, cpair, live, integ;
 };
 
 // Free bodies with one geom each plus static planes (config 1 piles).

@@ -14,7 +14,8 @@
 //                        serial, each contact's rows spread over the lanes
 //   K3c pgs_levels       long islands (class 6): one warp per island, the
 //                        contacts of one dependency level solved at once
-//   K4 integrate         one warp per world: semi-implicit Euler, state and
+//   K4 integrate         one warp per world: semi-implicit Euler (or RK4 under
+//                        the solver's wrench held over the stages), state and
 //                        diagnostics back to the world record
 // The class kernels touch disjoint islands and run concurrently.
 //
@@ -893,6 +894,61 @@ __global__ void __launch_bounds__(32 * PL_WARPS) pile_k_pgs_levels(const PileGro
 // ---------------------------------------------------------------------------
 // K4: integration + write-back (world.rs:1790-1817, 3223-3245)
 // ---------------------------------------------------------------------------
+// One body's RK4 step under the solver's wrench held constant over the four
+// stages (newt/src/world.rs:1705-1788, stage derivative world.rs:3223-3245,
+// stage states world.rs:3258-3271).  The wrench comes back from the velocity
+// changes the sweeps left: force / mass = dv / dt, world torque =
+// R0 Ib R0^T dw / dt.  Stage orientations are not renormalised; the final one
+// is, by division (newt/src/math.rs:591-598).  Returns true on a non-finite
+// result.
+__device__ __forceinline__ bool pile_rk4_body(float* wf, const WsLay& L, int b, float dt, V3 grav) {
+  const V3 p0 = ld3(wf + L.pos + 3 * b), v0 = ld3(wf + L.vel + 3 * b), w0 = ld3(wf + L.omg + 3 * b);
+  const Q4 q0 = ld4(wf + L.quat + 4 * b);
+  const S3 Ib = lds(wf + L.inertb + 6 * b), Ibi = lds(wf + L.iinvb + 6 * b);
+  const V3 alin = grav + ld3(wf + L.dv + 3 * b) / dt;
+  const V3 tau = qrot(q0, smv(Ib, qrot_inv(q0, ld3(wf + L.dw + 3 * b)))) / dt;
+  auto dang_at = [&](Q4 q, V3 om) {
+    const V3 gyro = -cross(om, smv(Ib, om));
+    return smv(Ibi, qrot_inv(q, tau) + gyro);
+  };
+  auto dori_at = [&](Q4 q, V3 om) {
+    const Q4 d = qmul(q, Q4{om.x, om.y, om.z, 0.f});
+    return Q4{d.x * 0.5f, d.y * 0.5f, d.z * 0.5f, d.w * 0.5f};
+  };
+  auto qstep = [](Q4 a, Q4 d, float h) { return Q4{a.x + d.x * h, a.y + d.y * h, a.z + d.z * h, a.w + d.w * h}; };
+  // k1 at s0
+  const V3 dp1 = v0, dw1 = dang_at(q0, w0);
+  const Q4 dq1 = dori_at(q0, w0);
+  const float h = dt * 0.5f;
+  // k2 at s0 + k1 dt/2
+  V3 vs = v0 + alin * h, ws = w0 + dw1 * h;
+  Q4 qs = qstep(q0, dq1, h);
+  const V3 dp2 = vs, dw2 = dang_at(qs, ws);
+  const Q4 dq2 = dori_at(qs, ws);
+  // k3 at s0 + k2 dt/2
+  vs = v0 + alin * h; ws = w0 + dw2 * h; qs = qstep(q0, dq2, h);
+  const V3 dp3 = vs, dw3 = dang_at(qs, ws);
+  const Q4 dq3 = dori_at(qs, ws);
+  // k4 at s0 + k3 dt
+  vs = v0 + alin * dt; ws = w0 + dw3 * dt; qs = qstep(q0, dq3, dt);
+  const V3 dp4 = vs, dw4 = dang_at(qs, ws);
+  const Q4 dq4 = dori_at(qs, ws);
+  const float sixth = 1.0f / 6.0f;
+  const V3 dp = (dp1 + dp2 * 2.f + dp3 * 2.f + dp4) * sixth;
+  const V3 dv = (alin + alin * 2.f + alin * 2.f + alin) * sixth;
+  const V3 dw = (dw1 + dw2 * 2.f + dw3 * 2.f + dw4) * sixth;
+  const Q4 dq{(dq1.x + dq2.x * 2.f + dq3.x * 2.f + dq4.x) * sixth, (dq1.y + dq2.y * 2.f + dq3.y * 2.f + dq4.y) * sixth,
+              (dq1.z + dq2.z * 2.f + dq3.z * 2.f + dq4.z) * sixth, (dq1.w + dq2.w * 2.f + dq3.w * 2.f + dq4.w) * sixth};
+  const V3 p = p0 + dp * dt, lv = v0 + dv * dt, av = w0 + dw * dt;
+  Q4 nq = qstep(q0, dq, dt);
+  const float n = sqrtf(nq.x * nq.x + nq.y * nq.y + nq.z * nq.z + nq.w * nq.w);
+  nq = n == 0.f ? Q4{0.f, 0.f, 0.f, 1.f} : Q4{nq.x / n, nq.y / n, nq.z / n, nq.w / n};
+  st3(wf + L.pos + 3 * b, p); st3(wf + L.vel + 3 * b, lv); st3(wf + L.omg + 3 * b, av);
+  wf[L.quat + 4 * b] = nq.x; wf[L.quat + 4 * b + 1] = nq.y; wf[L.quat + 4 * b + 2] = nq.z; wf[L.quat + 4 * b + 3] = nq.w;
+  return !(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(lv.x) && isfinite(lv.y) && isfinite(lv.z) &&
+           isfinite(av.x) && isfinite(av.y) && isfinite(av.z) && isfinite(nq.w));
+}
+
 __global__ void __launch_bounds__(128) pile_k_integrate(const PileGroupDev* G, const int* wseg, int ng, int total,
                                                         int write_diag) {
   const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -907,8 +963,13 @@ __global__ void __launch_bounds__(128) pile_k_integrate(const PileGroupDev* G, c
   const int lane = threadIdx.x & 31;
   const float dt = wf[L.dtg];
   const V3 grav = v3(wf[L.dtg + 1], wf[L.dtg + 2], wf[L.dtg + 3]);
+  const bool rk4 = g.I[(size_t)w * g.lay.istride + g.lay.integ] == NEWT_INTEGRATOR_RK4;
   bool bad = false;
   for (int b = lane; b < L.nb; b += 32) {
+    if (rk4) {
+      bad |= pile_rk4_body(wf, L, b, dt, grav);
+      continue;
+    }
     Q4 q = ld4(wf + L.quat + 4 * b);
     V3 om = ld3(wf + L.omg + 3 * b);
     V3 iw = smv(lds(wf + L.inertb + 6 * b), om);
