@@ -73,10 +73,13 @@ extern "C" {
 
 /* Semi-implicit Euler (the configs' integrator, implicit joint damping) or
  * classic RK4 (newt's default: four explicit ABA stages, root quaternion
- * renormalised after the step, newt/src/tree.rs:1234-1364); RK4 is taken for
- * trees without geoms, whose qacc is the first stage's, and for free-body
- * piles, whose contact wrenches are solved once at the start of the step and
- * held over the four stages (newt/src/world.rs:1705-1788). */
+ * renormalised after the step, newt/src/tree.rs:1234-1364).  Under RK4 the
+ * contact solve runs once at the start of the step and its result is held over
+ * the four stages: per-body wrenches for free-body piles
+ * (newt/src/world.rs:1705-1788), J^T f / dt added to qfrc for tree-contact
+ * worlds, whose solve then factors M and uses the explicit free ABA
+ * (world.rs:1826-1945, solver.rs:2852-2855,3602-3622).  A tree's qacc is the
+ * first stage's. */
 #define NEWT_INTEGRATOR_EULER 0
 #define NEWT_INTEGRATOR_RK4 1
 

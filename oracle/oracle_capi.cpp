@@ -278,8 +278,10 @@ int oracle_run(const newt_model_desc* models, int n_worlds, const int* model_of_
 // layout; the Euler form of the step), in row order: 4 facet rows per
 // pyramidal condim-3 contact, 1 per condim-1 contact.  Also returns the
 // tree's generalised contact forces (nv) when qfrc_out is non-null.
-int oracle_tree_impulses(const newt_model_desc* d, const float* qpos, const float* qvel, const float* qfrc,
-                         int precision, int cap, int* n_out, double* impulses, double* qfrc_out) {
+// integrator: 1 the Euler form of the solve (factors of M + dt B, implicit
+// free ABA), 0 the RK4 form (factors of M, explicit free ABA).
+int oracle_tree_impulses_ex(const newt_model_desc* d, const float* qpos, const float* qvel, const float* qfrc,
+                            int precision, int cap, int* n_out, double* impulses, double* qfrc_out, int integrator) {
   int rc = 0;
   auto go = [&](auto tag) {
     using R = decltype(tag);
@@ -295,7 +297,7 @@ int oracle_tree_impulses(const newt_model_desc* d, const float* qpos, const floa
     w.tree_body_wrenches.assign(w.bodies.size(), Wrench<R>{Vec3<R>(), Vec3<R>()});
     std::vector<R> imp;
     try {
-      solve_tree_contacts(w, tc, w.solver_mode == M_NEWTON, true, &imp);
+      solve_tree_contacts(w, tc, w.solver_mode == M_NEWTON, integrator == 1, &imp);
     } catch (const std::exception& e) {
       std::fprintf(stderr, "oracle_tree_impulses: %s\n", e.what());
       rc = 1;
@@ -308,6 +310,10 @@ int oracle_tree_impulses(const newt_model_desc* d, const float* qpos, const floa
   };
   if (precision == 0) go(0.0f); else go(0.0);
   return rc;
+}
+int oracle_tree_impulses(const newt_model_desc* d, const float* qpos, const float* qvel, const float* qfrc,
+                         int precision, int cap, int* n_out, double* impulses, double* qfrc_out) {
+  return oracle_tree_impulses_ex(d, qpos, qvel, qfrc, precision, cap, n_out, impulses, qfrc_out, 1);
 }
 
 // Contacts of one world at its given state (MuJoCo layout), detected exactly

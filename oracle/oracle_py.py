@@ -42,6 +42,8 @@ def lib():
         L.oracle_run_ex.restype = C.c_int
         L.oracle_tree_impulses.argtypes = [P, P, P, P, C.c_int, C.c_int, P, P, P]
         L.oracle_tree_impulses.restype = C.c_int
+        L.oracle_tree_impulses_ex.argtypes = [P, P, P, P, C.c_int, C.c_int, P, P, P, C.c_int]
+        L.oracle_tree_impulses_ex.restype = C.c_int
         L.oracle_contacts.argtypes = [P, P, P, C.c_int, C.c_int, P, P, P]
         L.oracle_impulses.argtypes = [P, P, P, C.c_int, C.c_int, C.c_int, P, P]
         L.oracle_mass_matrix.argtypes = [P, P, C.c_int, P]
@@ -103,9 +105,10 @@ def impulses(packed, index: int, qpos: np.ndarray, qvel: np.ndarray, precision: 
 
 
 def tree_impulses(packed, index: int, qpos: np.ndarray, qvel: np.ndarray, qfrc: Optional[np.ndarray] = None,
-                  precision: int = 1, cap: int = 4096):
+                  precision: int = 1, cap: int = 4096, integrator: int = 1):
     """Row impulses and generalised contact forces of one world's tree-contact
-    solve at its state (Euler form); returns (impulses, qfrc_contact)."""
+    solve at its state (integrator 1: the Euler form, 0: the RK4 form);
+    returns (impulses, qfrc_contact)."""
     qpos = np.ascontiguousarray(qpos, dtype=np.float32)
     qvel = np.ascontiguousarray(qvel, dtype=np.float32)
     qf = None if qfrc is None else np.ascontiguousarray(qfrc, dtype=np.float32)
@@ -113,7 +116,8 @@ def tree_impulses(packed, index: int, qpos: np.ndarray, qvel: np.ndarray, qfrc: 
     out = np.zeros(cap, dtype=np.float64)
     qc = np.zeros(qvel.shape[0], dtype=np.float64)
     d = C.cast(C.byref(packed.descs[index]), C.c_void_p)
-    if lib().oracle_tree_impulses(d, _ptr(qpos), _ptr(qvel), _ptr(qf), precision, cap, C.byref(n), _ptr(out), _ptr(qc)):
+    if lib().oracle_tree_impulses_ex(d, _ptr(qpos), _ptr(qvel), _ptr(qf), precision, cap, C.byref(n), _ptr(out),
+                                     _ptr(qc), int(integrator)):
         raise RuntimeError("oracle_tree_impulses failed")
     return out[: min(n.value, cap)], qc
 

@@ -8,13 +8,16 @@ solver goldens (solver_golden.rs: a three-box stack and a box on an incline,
 solved once per step and held over the RK4 stages).  The stack is chaotic (the
 FP64 oracle and newt's f32 run drift 2 cm apart by step 200), so it is held
 to one-step parity from newt's own snapshots and to that FP64 window over 1000
-steps.  Trees with geoms stay on Euler."""
+steps.  Tree-contact worlds hold the joint solve's generalised force over
+the stages; newt's own tree-contact goldens (solver_tree.bin) need in-tree
+box pairs, which the GPU path does not collide, so those run against the FP64
+oracle's RK4, itself byte-identical to newt on them."""
 import numpy as np
 import pytest
 
 import oracle_py
 from test_oracle_golden import _joints_chain, _joints_floating, _read_f32
-from tooling_gb300 import Engine, NewtError, STEP_BATCHED, STEP_PLAIN, scenes
+from tooling_gb300 import Engine, STEP_BATCHED, STEP_PLAIN, scenes
 from tooling_gb300 import model as M
 
 pytestmark = pytest.mark.gpu
@@ -88,12 +91,86 @@ def test_rk4_chains_track_fp64_oracle(eng):
     assert np.abs(q - eq).max() > 10 * np.abs(q - rq).max()
 
 
-def test_rk4_refused_for_tree_contact_worlds(eng):
+def _damped_chain_contact(solver):
+    """newt's tree-chain contact scene with joint damping (hinge 0.4, free
+    root 0.2), so that the RK4 form of the joint solve (factors of M, the
+    explicit free ABA) differs from the Euler form (M + dt B, the implicit
+    one)."""
     from test_oracle_golden import _tree_chain_contact
-    w = _tree_chain_contact(M.SOLVER_PGS)
+    w = _tree_chain_contact(solver)
+    w.links[1].damping = 0.4
+    w.links[0].free_damping = 0.2
     w.integrator = M.INTEGRATOR_RK4
-    with pytest.raises(NewtError):
-        eng.upload(M.PackedModels([w]))
+    return w
+
+
+@pytest.mark.parametrize("mode", [STEP_PLAIN, STEP_BATCHED])
+@pytest.mark.parametrize("solver", [M.SOLVER_NEWTON, M.SOLVER_PGS])
+def test_tree_contact_rk4_tracks_fp64_oracle(eng, solver, mode):
+    """The contact solve once per step, its J^T f / dt held over the RK4
+    stages (newt/src/world.rs:1826-1945): within 1e-3 m / 1e-2 m/s of the
+    FP64 oracle over 800 steps of falling, landing and rolling (the f32 and
+    FP64 oracles agree to 2e-6 here; Euler lands 7e-3 to 5e-2 m away)."""
+    w = _damped_chain_contact(solver)
+    P = M.PackedModels([w])
+    q0 = np.array([0.0, 0.0, 1.35, 1.0, 0.0, 0.0, 0.0, 0.0], np.float32)
+    v0 = np.array([0.3, 0.0, 0.0, 0.0, 0.5, 0.0, 2.0], np.float32)
+    slots = eng.alloc(eng.upload(P))
+    eng.set_state(slots, q0, v0)
+    done, errs = 0, []
+    for n in (300, 500, 800):
+        eng.step(n - done, mode)
+        done = n
+        gq, gv = eng.get_state(slots, 8, 7)
+        rq, rv = oracle_py.run(P, np.zeros(1, np.int32), q0, v0, None, n, precision=1, integrator=0)
+        eq, _ = oracle_py.run(P, np.zeros(1, np.int32), q0, v0, None, n, precision=1, integrator=1)
+        errs.append((n, float(np.abs(gq - rq).max()), float(np.abs(gv - rv).max()), float(np.abs(eq - rq).max())))
+    assert not (eng.status(slots) & 0x7).any()
+    eng.free(slots)
+    assert all(dq < 1e-3 and dv < 1e-2 for _, dq, dv, _ in errs), errs
+    assert max(e for *_, e in errs) > 5e-3, errs  # the oracle's two integrators do differ here
+
+
+@pytest.mark.parametrize("solver", [M.SOLVER_NEWTON, M.SOLVER_PGS])
+def test_tree_contact_rk4_impulses_match_oracle(eng, solver):
+    """One RK4 step from a resting state with eight contacts: row impulses
+    within 1e-3 relative of the oracle's RK4-form solve."""
+    w = _damped_chain_contact(solver)
+    P = M.PackedModels([w])
+    q0 = np.array([0.0, 0.0, 1.35, 1.0, 0.0, 0.0, 0.0, 0.0], np.float32)
+    v0 = np.array([0.3, 0.0, 0.0, 0.0, 0.5, 0.0, 2.0], np.float32)
+    rq, rv = oracle_py.run(P, np.zeros(1, np.int32), q0, v0, None, 800, precision=1, integrator=0)
+    q, v = rq.astype(np.float32), rv.astype(np.float32)
+    slots = eng.alloc(eng.upload(P))
+    eng.set_state(slots, q, v)
+    eng.step(1, STEP_PLAIN)
+    eng.sync()
+    g = eng.impulses(int(slots[0]))
+    eng.free(slots)
+    ref, _ = oracle_py.tree_impulses(P, 0, q, v, None, integrator=0)
+    assert len(ref) >= 8 and len(g) == len(ref)
+    assert np.abs(g - ref).max() / np.abs(ref).max() < 1e-3
+
+
+@pytest.mark.parametrize("solver", [M.SOLVER_NEWTON, M.SOLVER_PGS])
+def test_quadrupeds_rk4_short_trajectory(eng, solver):
+    """Settled quadrupeds with controls, ten RK4 steps: within 2e-3 m /
+    5e-2 m/s of the FP64 oracle (the tree-contact Euler bar)."""
+    b = scenes.quadruped_batch(n_worlds=16, first_world=300, solver=solver)
+    rq, rv = oracle_py.run(b, np.arange(len(b)), b.qpos, b.qvel, None, 300, precision=1)
+    b.qpos[:], b.qvel[:] = rq.astype(np.float32), rv.astype(np.float32)
+    b.qfrc[:] = scenes.quadruped_controls(len(b), 0, first_world=300)
+    for i in range(len(b)):
+        b.descs[i].integrator = M.INTEGRATOR_RK4
+    slots = eng.alloc(eng.upload(b))
+    eng.set_state(slots, b.qpos, b.qvel)
+    eng.set_qfrc(slots, b.qfrc)
+    eng.step(10, STEP_BATCHED)
+    gq, gv = eng.get_state(slots, int(b.nq.sum()), int(b.nv.sum()))
+    assert not (eng.status(slots) & 0x7).any()
+    eng.free(slots)
+    oq, ov = oracle_py.run(b, np.arange(len(b)), b.qpos, b.qvel, b.qfrc, 10, precision=1, integrator=0)
+    assert np.abs(gq - oq).max() < 2e-3 and np.abs(gv - ov).max() < 5e-2
 
 
 def _mj(q_newt, nb):

@@ -64,14 +64,14 @@ static void tree_rows(HostGroup& g) {
   g.r_qacc = r; r += g.nv;
   g.ri_solver = 0; g.ri_live = 1; g.ri_status = 2;
   g.irows = 3;
-  if (g.kind == GK_TREE) {  // integrator per world
+  if (g.kind == GK_TREE) {  // integrator per world (tree-contact groups: row 5)
     g.ri_integ = 3;
     g.irows = 4;
   }
   if (g.kind == GK_TREE_CONTACT) {  // per-geom model rows (TcGroupDev::geom), solver mode
     g.r_geom = r; r += 21 * g.ng;
-    g.ri_mode = 3; g.ri_iters = 4;
-    g.irows = 5;
+    g.ri_mode = 3; g.ri_iters = 4; g.ri_integ = 5;
+    g.irows = 6;
   }
   g.frows = r;
 }
@@ -593,6 +593,7 @@ TreeGroupDev HostGroup::tree_dev() const {
   d.solver = dI + (size_t)ri_solver * cap;
   d.live = dI + (size_t)ri_live * cap;
   d.integ = ri_integ >= 0 ? dI + (size_t)ri_integ * cap : nullptr;
+  d.cfrc = nullptr; d.cstride = 0;
   d.q = row(r_q); d.qd = row(r_qd); d.qfrc = row(r_qfrc); d.qacc = row(r_qacc);
   d.status = (uint32_t*)(dI + (size_t)ri_status * cap);
   return d;

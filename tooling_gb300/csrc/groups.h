@@ -35,6 +35,8 @@ struct TreeGroupDev {
   const int* solver;   // 1    nonzero enables free-root qfrc (newt/src/forces.rs:16-31)
   const int* live;     // 1    nonzero for allocated worlds
   const int* integ;    // 1    NEWT_INTEGRATOR_* (null: Euler for every world)
+  float* cfrc;         // tree-contact groups: the contact solve's J^T f / dt (nv per world, stride
+  long cstride;        // `cstride` floats, in the solver scratch); null for trees without geoms
   // per-world state (SoA)
   float* q;     // nq  (newt layout: free root p xyz, quat xyzw; hinge angle)
   float* qd;    // nv  (free root: omega_body, v_body; hinge rate)

@@ -11,6 +11,9 @@
 //                          regulariser and bias, Newton or PGS, and
 //                          qacc = a_free + M^-1 J^T f / dt
 //   tree_integrate_kernel  thread per world (tree_kernels.cu)
+// Under RK4 (per world) a_free is the explicit ABA, the solve factors M
+// without the damping term, J^T f / dt goes to the world's scratch, and the
+// integrate stage runs the RK4 step with it added to qfrc.
 //
 // Restates, for FP32 on sm_103a:
 //   newt/src/solver.rs:2805-3366  solve_tree_contacts (Euler form:
@@ -110,7 +113,7 @@ NEWT_D float reference_accel(float position, float velocity, float tc, float dr,
 // ---------------------------------------------------------------------------
 struct TcLay {
   int L, nv, ng, maxc, ld;
-  int jv, jw, iw, con, jt, H, LH, LHd, imp, misc, words;
+  int jv, jw, iw, con, jt, H, LH, LHd, imp, misc, qfc, words;
 };
 NEWT_HD int up4(int n) { return (n + 3) / 4 * 4; }
 NEWT_HD TcLay tc_layout(int L, int nv, int ng, int maxc) {
@@ -128,6 +131,7 @@ NEWT_HD TcLay tc_layout(int L, int nv, int ng, int maxc) {
   t.LHd = f; f += up4(2 * t.ld * t.ld);  // FP64 factor (offset is a multiple of 4 floats)
   t.imp = f; f += up4(t.ld);
   t.misc = f; f += 8;  // ncon, nrows, newton iterations
+  t.qfc = f; f += up4(nv);  // RK4 worlds: J^T f / dt, held over the integrator's stages
   t.words = (f + 31) / 32 * 32;
   return t;
 }
@@ -340,6 +344,7 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   int* rcon = reinterpret_cast<int*>(sv + sm.rmap);
   int* rfac = rcon + sm.ldr;
   const float dt = g.dtg[w];
+  const bool rk4 = g.integ && g.integ[w] == NEWT_INTEGRATOR_RK4;
   uint32_t status = 0;
   const float* gm = G.geom;
   auto gv = [&](int gi, int f) { return gm[(size_t)(GREC * gi + f) * cap + w]; };
@@ -566,19 +571,20 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
     LD[j * nv + i] = s;
   }
   __syncwarp();
-  // armature (diagonal, child joints) and the implicit damping dt*B (tree.rs:645-684)
+  // armature (diagonal, child joints) and, under Euler, the implicit damping
+  // dt*B (tree.rs:645-684); RK4 factors M itself (solver.rs:2852-2855)
   for (int k = lane; k < nv * nv; k += 32) LM[k] = LD[k];
   __syncwarp();
   if (lane == 0) {
     for (int i = 0; i < L; ++i) {
       const int jt = g.topo[4 * i + 1], vo = g.topo[4 * i + 3];
       if (jt == JF) {
-        const float dm = dt * g.damp[i * cap + w];
+        const float dm = rk4 ? 0.f : dt * g.damp[i * cap + w];
         for (int k = 0; k < 6; ++k) LM[(vo + k) * nv + vo + k] += dm;
       } else if (jt == JH || jt == JS) {
         const float arm = g.arm[i * cap + w];
         LD[vo * nv + vo] += arm;
-        LM[vo * nv + vo] += arm + dt * g.damp[i * cap + w];
+        LM[vo * nv + vo] += arm + (rk4 ? 0.f : dt * g.damp[i * cap + w]);
       }
     }
   }
@@ -835,6 +841,13 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
     vg[k] = s / dt;
   }
   __syncwarp();
+  if (rk4)  // the generalised force itself, J^T f / dt = L (Y f) / dt (L column-major lower)
+    for (int i = lane; i < nv; i += 32) {
+      float s = 0.f;
+      for (int k = 0; k <= i; ++k) s += LM[(size_t)k * nv + i] * vg[k];
+      g.cfrc[(size_t)w * g.cstride + i] = s;
+    }
+  __syncwarp();
   warp_lt_solve(LM, nv, nv, vg, lane);
   for (int k = lane; k < nv; k += 32) g.qacc[k * cap + w] += vg[k];
   if (lane == 0) {
@@ -895,7 +908,9 @@ extern "C" int newt_tc_step(newt_gpu_ctx* ctx, HostGroup* g, int n_steps, int fu
   }
   g->scr_stride = (long)(per / sizeof(float));
   CKT(newt_tc_init(g->size, g->nv, g->maxc));
-  const TcGroupDev d = g->tc_dev();
+  TcGroupDev d = g->tc_dev();
+  d.t.cfrc = d.scr + tc_layout(g->size, g->nv, g->ng, g->maxc).qfc;
+  d.t.cstride = d.sstride;
   const bool timed = ctx->profile;
   if (timed) {
     while (ctx->tcev.size() < (size_t)6 * n_steps) {

@@ -46,9 +46,6 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
   if (!(d.dt > 0.f)) return fail(ctx, NEWT_E_INVALID, "dt must be > 0");
   if (d.integrator != NEWT_INTEGRATOR_EULER && d.integrator != NEWT_INTEGRATOR_RK4)
     return fail(ctx, NEWT_E_INVALID, "unknown integrator");
-  if (d.integrator == NEWT_INTEGRATOR_RK4 && !(d.n_links > 0 && d.n_bodies == 0 && d.n_geoms == 0) &&
-      !(d.n_links == 0 && d.n_bodies > 0))
-    return fail(ctx, NEWT_E_INVALID, "RK4 runs on trees without geoms and on free-body piles (tree contacts step with Euler)");
   if (d.solver != 0 && d.solver != NEWT_SOLVER_PGS && d.solver != NEWT_SOLVER_NEWTON)
     return fail(ctx, NEWT_E_INVALID, "unknown solver mode");
   if ((d.solver == NEWT_SOLVER_PGS || d.solver == NEWT_SOLVER_NEWTON) && d.iterations < 1)

@@ -311,7 +311,8 @@ __global__ void __launch_bounds__(128) tree_aba_kernel(TreeGroupDev g) {
   for (int k = 0; k < nq; ++k) q[k] = g.q[k * cap + w];
   for (int k = 0; k < nv; ++k) { qd[k] = g.qd[k * cap + w]; qf[k] = g.qfrc[k * cap + w]; qdd[k] = 0.f; }
   LinkScratch scr[MAXL];
-  if (is_rk4(g, w)) {  // the whole RK4 step here; the integrate stage skips the world
+  const bool rk4 = is_rk4(g, w);
+  if (rk4 && !g.cfrc) {  // no contacts: the whole RK4 step here; the integrate stage skips the world
     uint32_t st = tree_rk4<MAXL>(g, w, q, qd, qf, qdd, scr) ? 0u : NEWT_WS_NOT_PD;
     if (!finite_all(q, nq) || !finite_all(qd, nv)) st |= NEWT_WS_NONFINITE;
     for (int k = 0; k < nq; ++k) g.q[k * cap + w] = q[k];
@@ -319,16 +320,37 @@ __global__ void __launch_bounds__(128) tree_aba_kernel(TreeGroupDev g) {
     if (st) g.status[w] |= st;
     return;
   }
-  if (!tree_aba<MAXL>(g, w, q, qd, qf, qdd, scr, g.dtg[w])) g.status[w] |= NEWT_WS_NOT_PD;
+  // a_free for the contact solve: with the implicit damping fold under Euler,
+  // the explicit ABA under RK4 (newt/src/solver.rs:3602-3622)
+  if (!tree_aba<MAXL>(g, w, q, qd, qf, qdd, scr, rk4 ? 0.f : g.dtg[w])) g.status[w] |= NEWT_WS_NOT_PD;
   for (int k = 0; k < nv; ++k) g.qacc[k * cap + w] = qdd[k];
+  if (rk4)  // the solve adds J^T f / dt here when the world has contacts
+    for (int k = 0; k < nv; ++k) g.cfrc[(size_t)w * g.cstride + k] = 0.f;
 }
 
-// Plain form, stage 3: Euler integration from HBM qacc.
+// Plain form, stage 3: Euler integration from HBM qacc; for RK4 worlds of a
+// tree-contact group, the RK4 step with the contact solve's generalised force
+// added to qfrc and held over the four stages (newt/src/world.rs:1826-1945).
 template <int MAXL>
 __global__ void __launch_bounds__(128) tree_integrate_kernel(TreeGroupDev g) {
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= g.n || !g.live[w] || is_rk4(g, w)) return;
+  if (w >= g.n || !g.live[w]) return;
+  const bool rk4 = is_rk4(g, w);
+  if (rk4 && !g.cfrc) return;  // stepped whole by the ABA stage
   const int cap = g.cap, nq = g.nq, nv = g.nv;
+  if (rk4) {
+    float q[MAXL + 6], qd[MAXL + 5], qf[MAXL + 5], qdd[MAXL + 5];
+    const float* cf = g.cfrc + (size_t)w * g.cstride;
+    for (int k = 0; k < nq; ++k) q[k] = g.q[k * cap + w];
+    for (int k = 0; k < nv; ++k) { qd[k] = g.qd[k * cap + w]; qf[k] = g.qfrc[k * cap + w] + cf[k]; qdd[k] = 0.f; }
+    LinkScratch scr[MAXL];
+    uint32_t st = tree_rk4<MAXL>(g, w, q, qd, qf, qdd, scr) ? 0u : NEWT_WS_NOT_PD;
+    if (!finite_all(q, nq) || !finite_all(qd, nv)) st |= NEWT_WS_NONFINITE;
+    for (int k = 0; k < nq; ++k) g.q[k * cap + w] = q[k];
+    for (int k = 0; k < nv; ++k) { g.qd[k * cap + w] = qd[k]; g.qacc[k * cap + w] = qdd[k]; }
+    if (st) g.status[w] |= st;
+    return;
+  }
   float q[MAXL + 6], qd[MAXL + 5], qdd[MAXL + 5];
   for (int k = 0; k < nq; ++k) q[k] = g.q[k * cap + w];
   for (int k = 0; k < nv; ++k) { qd[k] = g.qd[k * cap + w]; qdd[k] = g.qacc[k * cap + w]; }
