@@ -8,7 +8,8 @@
 //   newt/src/contact.rs:82-214       Contact, ContactBuf (cap 4)
 //   newt/src/contact.rs:269-470      sphere_plane, box_plane, capsule_plane, sphere_sphere
 //   newt/src/contact.rs:569-1247     box_box_full_manifold (SAT + face clipping)
-//   newt/src/contact.rs:2342-2387    closest_points_on_segments
+//   newt/src/contact.rs:473-505      sphere_capsule; :1249-1272 capsule_capsule
+//   newt/src/contact.rs:2313-2387    closest_point_on_segment, closest_points_on_segments
 //   newt/src/contact.rs:2509-2587    dispatch / swap rule
 //   newt/src/world.rs:1042-1069      auto_pairs (naive pair set; broadphase-independent contacts)
 //   newt/src/world.rs:2476-2515      collect_contacts_full
@@ -239,6 +240,31 @@ template <class R> void closest_points_on_segments(Vec3<R> a0, Vec3<R> a1, Vec3<
   *pa = a0 + d1 * sf; *pb = b0 + d2 * t;
 }
 
+// contact.rs:2313-2321 closest_point_on_segment
+template <class R> Vec3<R> closest_point_on_segment(Vec3<R> p, Vec3<R> a, Vec3<R> b) {
+  Vec3<R> ab = b - a;
+  R denom = ab.length_squared();
+  if (denom == R(0)) return a;
+  return a + ab * clamp01((p - a).dot(ab) / denom);
+}
+
+// contact.rs:473-505 sphere_capsule: sphere vs the sphere at the capsule
+// axis point closest to the sphere centre (segment from -h to +h along local z)
+template <class R> CBuf<R> sphere_capsule(int is, const Pose<R>& sp, R rs, int ic, const Pose<R>& cp_, R rc, R hh, R fr, R margin, R gap) {
+  Vec3<R> ax = cp_.o.rotate(Vec3<R>(0, 0, 1));
+  Vec3<R> closest = closest_point_on_segment(sp.p, cp_.p - ax * hh, cp_.p + ax * hh);
+  return sphere_sphere(is, sp.p, rs, ic, closest, rc, fr, margin, gap);
+}
+
+// contact.rs:1249-1272 capsule_capsule: closest points of the two axis
+// segments, then sphere vs sphere there
+template <class R> CBuf<R> capsule_capsule(int ia, const Pose<R>& pa, R ra, R ha, int ib, const Pose<R>& pb, R rb, R hb, R fr, R margin, R gap) {
+  Vec3<R> ax = pa.o.rotate(Vec3<R>(0, 0, 1)), bx = pb.o.rotate(Vec3<R>(0, 0, 1));
+  Vec3<R> ca, cb;
+  closest_points_on_segments(pa.p - ax * ha, pa.p + ax * ha, pb.p - bx * hb, pb.p + bx * hb, &ca, &cb);
+  return sphere_sphere(ia, ca, ra, ib, cb, rb, fr, margin, gap);
+}
+
 template <class R> struct FV { R u, v, depth; };
 
 template <class R> int sh_clip(const FV<R>* subject, R hu, R hv, FV<R>* outp) {  // contact.rs:1087-1139
@@ -392,6 +418,14 @@ template <class R> bool try_np(int ia, const Geom<R>& a, const Pose<R>& pa, int 
   if (a.shape == S_SPHERE && b.shape == S_SPHERE) { *out = sphere_sphere(ia, pa.p, a.size[0], ib, pb.p, b.size[0], fr, margin, gap); return true; }
   if (a.shape == S_BOX && b.shape == S_BOX) {
     *out = box_box(ia, pa, Vec3<R>(a.size[0], a.size[1], a.size[2]), ib, pb, Vec3<R>(b.size[0], b.size[1], b.size[2]), fr, margin, gap);
+    return true;
+  }
+  if (a.shape == S_SPHERE && b.shape == S_CAPSULE) {
+    *out = sphere_capsule(ia, pa, a.size[0], ib, pb, b.size[0], b.size[1], fr, margin, gap);
+    return true;
+  }
+  if (a.shape == S_CAPSULE && b.shape == S_CAPSULE) {
+    *out = capsule_capsule(ia, pa, a.size[0], a.size[1], ib, pb, b.size[0], b.size[1], fr, margin, gap);
     return true;
   }
   if (a.shape == S_SPHERE && b.shape == S_BOX) {

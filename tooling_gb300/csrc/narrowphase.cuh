@@ -8,6 +8,9 @@
 //   sphere_sphere  newt/src/contact.rs:407-470
 //   box_box        newt/src/contact.rs:569-1053 (15-axis SAT, face clipping,
 //                  edge-edge closest points)
+//   capsule_plane  newt/src/contact.rs:367-400
+//   sphere_capsule newt/src/contact.rs:473-505
+//   capsule_capsule newt/src/contact.rs:1249-1272
 //   sphere_box     extension (newt defers this pair, contact.rs:236-257):
 //                  closed-form closest point on the oriented box
 #pragma once
@@ -104,6 +107,41 @@ NEWT_D void seg_closest(V3 a0, V3 a1, V3 b0, V3 b1, V3* pa, V3* pb) {  // contac
   else if (tn > e) { t = 1.f; sf = clamp01f((b_ - c) / a); }
   else { t = tn / e; sf = s; }
   *pa = a0 + d1 * sf; *pb = b0 + d2 * t;
+}
+
+// Capsule (A, axis local z, segment -h..+h) vs plane (B): one contact per
+// segment end within the margin (newt/src/contact.rs:367-400).
+NEWT_D int np_capsule_plane(const GPose& c, float r, float hh, float margin, const GPose& pl, CRes* out) {
+  const V3 n = qrot(pl.q, v3(0.f, 0.f, 1.f));
+  const V3 ax = qrot(c.q, v3(0.f, 0.f, 1.f));
+  int k = 0;
+  for (int e = 0; e < 2; ++e) {
+    const V3 p = e == 0 ? c.p + ax * hh : c.p - ax * hh;
+    const float raw = dot(p - pl.p, n) - r;
+    if (raw <= margin) out[k++] = CRes{p - n * (r + raw * 0.5f), n, margin - raw};
+  }
+  return k;
+}
+
+// Sphere (A) vs capsule (B): the sphere against the sphere at the axis point
+// closest to its centre (contact.rs:473-505, closest_point_on_segment
+// contact.rs:2313-2321).
+NEWT_D int np_sphere_capsule(V3 cs, float rs, const GPose& c, float rc, float hh, float margin, CRes* out) {
+  const V3 ax = qrot(c.q, v3(0.f, 0.f, 1.f));
+  const V3 a = c.p - ax * hh, ab = (c.p + ax * hh) - a;
+  const float den = len2(ab);
+  const V3 q = den == 0.f ? a : a + ab * clamp01f(dot(cs - a, ab) / den);
+  return np_sphere_sphere(cs, rs, q, rc, margin, out);
+}
+
+// Capsule (A) vs capsule (B): closest points of the two axis segments, then
+// sphere vs sphere there (contact.rs:1249-1272).
+NEWT_D int np_capsule_capsule(const GPose& A, float ra, float ha, const GPose& B, float rb, float hb, float margin,
+                              CRes* out) {
+  const V3 ax = qrot(A.q, v3(0.f, 0.f, 1.f)), bx = qrot(B.q, v3(0.f, 0.f, 1.f));
+  V3 pa, pb;
+  seg_closest(A.p - ax * ha, A.p + ax * ha, B.p - bx * hb, B.p + bx * hb, &pa, &pb);
+  return np_sphere_sphere(pa, ra, pb, rb, margin, out);
 }
 
 struct FV2 { float u, v, d; };

@@ -439,15 +439,8 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
         nc = np_sphere_plane(gpose, gv(gl, G_SIZE), margin, ppose, cr);
       } else if (shape == NEWT_SHAPE_BOX) {
         nc = np_box_plane(gpose, v3(gv(gl, G_SIZE), gv(gl, G_SIZE + 1), gv(gl, G_SIZE + 2)), margin, ppose, cr);
-      } else if (shape == NEWT_SHAPE_CAPSULE) {  // contact.rs:367-400: both segment ends
-        const V3 n = qrot(ppose.q, v3(0.f, 0.f, 1.f));
-        const V3 ax = qrot(gpose.q, v3(0.f, 0.f, 1.f));
-        const float r = gv(gl, G_SIZE), hh = gv(gl, G_SIZE + 1);
-        for (int k = 0; k < 2; ++k) {
-          const V3 e = k == 0 ? gpose.p + ax * hh : gpose.p - ax * hh;
-          const float raw = dot(e - ppose.p, n) - r;
-          if (raw <= margin) cr[nc++] = CRes{e - n * (r + raw * 0.5f), n, margin - raw};
-        }
+      } else if (shape == NEWT_SHAPE_CAPSULE) {
+        nc = np_capsule_plane(gpose, gv(gl, G_SIZE), gv(gl, G_SIZE + 1), margin, ppose, cr);
       }
     }
     int incl = nc;  // inclusive scan of the per-pair counts

@@ -24,7 +24,7 @@
 
 namespace pile {
 
-constexpr int SH_PLANE = 0, SH_SPHERE = 1, SH_BOX = 2;
+constexpr int SH_PLANE = 0, SH_SPHERE = 1, SH_BOX = 2, SH_CAPSULE = 3;  // NEWT_SHAPE_*
 constexpr int CF = 39;  // floats per contact in the scratch record
 constexpr int CI = 4;   // ints per contact
 constexpr int SC = 188;  // floats per active contact in the solver record (a multiple of 4)
@@ -148,8 +148,13 @@ NEWT_D void collide(const WsLay& L, float* wf, int* wi, int lane) {
     if (e >= nb) { a[0] = -INFINITY; a[1] = -INFINITY; a[2] = -INFINITY; a[3] = INFINITY; a[4] = INFINITY; a[5] = INFINITY; continue; }
     GPose p = geom_pose(L, wf, e);
     V3 ext;
-    if (wi[L.shape + e] == SH_SPHERE) { float r = wf[L.size + 3 * e]; ext = v3(r, r, r); }
-    else {
+    const int sh = wi[L.shape + e];
+    if (sh == SH_SPHERE) { float r = wf[L.size + 3 * e]; ext = v3(r, r, r); }
+    else if (sh == SH_CAPSULE) {  // |axis| h + r per component (broadphase.rs:720-729)
+      const V3 ax = qrot(p.q, v3(0.f, 0.f, 1.f));
+      const float r = wf[L.size + 3 * e], hh = wf[L.size + 3 * e + 1];
+      ext = v3(fabsf(ax.x) * hh + r, fabsf(ax.y) * hh + r, fabsf(ax.z) * hh + r);
+    } else {
       V3 h = ld3(wf + L.size + 3 * e);
       M3 R = quat_mat(p.q);
       ext = v3(fabsf(R.m[0][0]) * h.x + fabsf(R.m[0][1]) * h.y + fabsf(R.m[0][2]) * h.z,
@@ -268,11 +273,22 @@ NEWT_D void collide(const WsLay& L, float* wf, int* wi, int lane) {
       else if (sa == SH_SPHERE && sb == SH_SPHERE) cnt = np_sphere_sphere(pa.p, wf[L.size + 3 * ea], pb.p, wf[L.size + 3 * eb], margin, res);
       else if (sa == SH_BOX && sb == SH_BOX) cnt = np_box_box(pa, ld3(wf + L.size + 3 * ea), pb, ld3(wf + L.size + 3 * eb), margin, res);
       else if (sa == SH_SPHERE && sb == SH_BOX) cnt = np_sphere_box(pa, wf[L.size + 3 * ea], pb, ld3(wf + L.size + 3 * eb), margin, res);
+      else if (sa == SH_CAPSULE && sb == SH_PLANE)
+        cnt = np_capsule_plane(pa, wf[L.size + 3 * ea], wf[L.size + 3 * ea + 1], margin, pb, res);
+      else if (sa == SH_SPHERE && sb == SH_CAPSULE)
+        cnt = np_sphere_capsule(pa.p, wf[L.size + 3 * ea], pb, wf[L.size + 3 * eb], wf[L.size + 3 * eb + 1], margin, res);
+      else if (sa == SH_CAPSULE && sb == SH_CAPSULE)
+        cnt = np_capsule_capsule(pa, wf[L.size + 3 * ea], wf[L.size + 3 * ea + 1], pb, wf[L.size + 3 * eb],
+                                 wf[L.size + 3 * eb + 1], margin, res);
       else {
         flip = true;
         if (sb == SH_SPHERE && sa == SH_PLANE) cnt = np_sphere_plane(pb, wf[L.size + 3 * eb], margin, pa, res);
         else if (sb == SH_BOX && sa == SH_PLANE) cnt = np_box_plane(pb, ld3(wf + L.size + 3 * eb), margin, pa, res);
         else if (sb == SH_SPHERE && sa == SH_BOX) cnt = np_sphere_box(pb, wf[L.size + 3 * eb], pa, ld3(wf + L.size + 3 * ea), margin, res);
+        else if (sb == SH_CAPSULE && sa == SH_PLANE)
+          cnt = np_capsule_plane(pb, wf[L.size + 3 * eb], wf[L.size + 3 * eb + 1], margin, pa, res);
+        else if (sb == SH_SPHERE && sa == SH_CAPSULE)
+          cnt = np_sphere_capsule(pb.p, wf[L.size + 3 * eb], pa, wf[L.size + 3 * ea], wf[L.size + 3 * ea + 1], margin, res);
       }
     }
     int incl = cnt;

@@ -80,8 +80,10 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
       if (G.link >= 0) return fail(ctx, NEWT_E_INVALID, "link geom in a tree-less world");
       if (G.body >= 0) {
         if (G.body >= d.n_bodies) return fail(ctx, NEWT_E_INVALID, "geom body out of range");
-        if (G.shape != NEWT_SHAPE_SPHERE && G.shape != NEWT_SHAPE_BOX)
-          return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "free-body geoms must be spheres or boxes on the GPU path");
+        if (G.shape != NEWT_SHAPE_SPHERE && G.shape != NEWT_SHAPE_BOX && G.shape != NEWT_SHAPE_CAPSULE)
+          return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "free-body geoms must be spheres, boxes or capsules on the GPU path");
+        if (G.shape == NEWT_SHAPE_CAPSULE && !(G.size[0] > 0.f && G.size[1] >= 0.f))
+          return fail(ctx, NEWT_E_INVALID, "capsule needs radius > 0 and half_height >= 0");
         per_body[G.body]++;
       } else {
         if (G.shape != NEWT_SHAPE_PLANE) return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "static geoms must be planes");
@@ -89,6 +91,17 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
       }
       if (G.condim != 3 && G.condim != 1) return fail(ctx, NEWT_E_INVALID, "condim must be 1 or 3");
     }
+    // newt has no capsule-box primitive (newt/src/contact.rs:232-257) and
+    // panics when such a pair is active; the pair is refused here instead
+    for (int i = 0; i < d.n_geoms; ++i)
+      for (int j = i + 1; j < d.n_geoms; ++j) {
+        const newt_geom_desc &A = d.geoms[i], &B = d.geoms[j];
+        if (A.body < 0 || B.body < 0) continue;
+        const bool cb = (A.shape == NEWT_SHAPE_CAPSULE && B.shape == NEWT_SHAPE_BOX) ||
+                        (A.shape == NEWT_SHAPE_BOX && B.shape == NEWT_SHAPE_CAPSULE);
+        if (cb && (A.group & B.mask) != 0u && (B.group & A.mask) != 0u)
+          return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "capsule-box pairs are not supported (newt/src/contact.rs:232-257)");
+      }
     for (int b = 0; b < d.n_bodies; ++b) {
       if (per_body[b] != 1) return fail(ctx, NEWT_E_INVALID, "GPU piles need exactly one geom per body");
       const float* I = d.bodies[b].inertia;  // column-major; Body::new inverts it (newt/src/body.rs)

@@ -185,6 +185,54 @@ def _pile_world(rng: np.random.Generator, n_bodies: int, box_lo=(-1.0, -1.0, 0.3
     return bodies, geoms, np.concatenate(qpos)
 
 
+def _capsule_pile_world(rng: np.random.Generator, n_bodies: int, box_lo=(-0.8, -0.8, 0.3), box_hi=(0.8, 0.8, 2.0)):
+    """n free bodies: 50% spheres r~U(.05,.2), 50% capsules r~U(.04,.12),
+    half-height~U(.05,.2) along local z; density 1000; placed like the box
+    piles (non-overlapping bounding spheres, random orientations, at rest)."""
+    bodies, geoms = [], [_geom(M.SHAPE_PLANE, friction=1.0)]
+    qpos, centers, radii = [], [], []
+    for b in range(n_bodies):
+        sphere = rng.random() < 0.5
+        if sphere:
+            r = float(rng.uniform(0.05, 0.2))
+            mass = float(_f32(1000.0) * _f32(4.0 / 3.0 * math.pi * r ** 3))
+            inertia, size, bound = sphere_inertia(mass, r), (r, 0.0, 0.0), r
+        else:
+            r, hh = float(rng.uniform(0.04, 0.12)), float(rng.uniform(0.05, 0.2))
+            mass = float(_f32(1000.0 * (math.pi * r * r * 2.0 * hh + 4.0 / 3.0 * math.pi * r ** 3)))
+            inertia = np.array(M.solid_capsule_inertia(mass, r, hh), np.float32)
+            size, bound = (r, hh, 0.0), r + hh
+        mu = float(rng.uniform(0.3, 1.0))
+        C_arr, R_arr = np.asarray(centers).reshape(-1, 3), np.asarray(radii)
+        for _ in range(1000):
+            p = rng.uniform(box_lo, box_hi)
+            if not len(C_arr) or np.all(np.sqrt(((C_arr - p) ** 2).sum(axis=1)) > bound + R_arr):
+                break
+        centers.append(p)
+        radii.append(bound)
+        bd = np.zeros((), M.BODY_DT)
+        bd["mass"], bd["inertia"] = mass, inertia
+        bodies.append(bd)
+        geoms.append(_geom(M.SHAPE_SPHERE if sphere else M.SHAPE_CAPSULE, body=b, size=size, friction=mu))
+        qpos.append(np.concatenate([p, _random_quat(rng)]))
+    return bodies, geoms, np.concatenate(qpos)
+
+
+def capsule_pile_batch(n_worlds: int = 1024, n_bodies: int = 12, seed_index: int = 5, dt: float = 2e-3,
+                       iterations: int = 50, first_world: int = 0) -> M.Batch:
+    """Piles of free spheres and capsules on a plane (sphere-capsule,
+    capsule-capsule and capsule-plane contacts), PGS."""
+    cs = config_seed(seed_index)
+    bodies, geoms, qps = [], [], []
+    for w in range(first_world, first_world + n_worlds):
+        b, g, qp = _capsule_pile_world(world_rng(cs, w), n_bodies)
+        bodies += b; geoms += g; qps.append(qp)
+    batch = M.Batch(np.zeros(0, M.LINK_DT), [0] * n_worlds, np.stack(bodies), [n_bodies] * n_worlds,
+                    np.stack(geoms), [n_bodies + 1] * n_worlds, dt, (0.0, 0.0, -9.81), M.SOLVER_PGS, iterations)
+    batch.qpos[:] = np.concatenate(qps)
+    return batch
+
+
 def pile_batch(n_worlds: int = 8192, n_bodies: int = 16, seed_index: int = 1, dt: float = 2e-3,
                iterations: int = 50, first_world: int = 0) -> M.Batch:
     cs = config_seed(seed_index)
