@@ -66,7 +66,9 @@ extern "C" {
 #define NEWT_SHAPE_PLANE 0
 #define NEWT_SHAPE_SPHERE 1
 #define NEWT_SHAPE_BOX 2
-#define NEWT_SHAPE_CAPSULE 3
+#define NEWT_SHAPE_CAPSULE 3   /* size: radius, half height along local z */
+#define NEWT_SHAPE_CYLINDER 4  /* size: radius, half height along local z */
+#define NEWT_SHAPE_ELLIPSOID 5 /* size: semi-axes */
 
 #define NEWT_SOLVER_PGS 1
 #define NEWT_SOLVER_NEWTON 2

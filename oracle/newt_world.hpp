@@ -9,6 +9,7 @@
 //   newt/src/contact.rs:269-470      sphere_plane, box_plane, capsule_plane, sphere_sphere
 //   newt/src/contact.rs:569-1247     box_box_full_manifold (SAT + face clipping)
 //   newt/src/contact.rs:473-505      sphere_capsule; :1249-1272 capsule_capsule
+//   newt/src/contact.rs:1296-1426    cylinder_plane, ellipsoid_plane
 //   newt/src/contact.rs:2313-2387    closest_point_on_segment, closest_points_on_segments
 //   newt/src/contact.rs:2509-2587    dispatch / swap rule
 //   newt/src/world.rs:1042-1069      auto_pairs (naive pair set; broadphase-independent contacts)
@@ -72,7 +73,7 @@ template <class R> Mat3<R> solid_capsule_inertia(R mass, R radius, R half_height
   return Mat3<R>::diag(i_xx, i_xx, i_zz);
 }
 
-enum Shape { S_PLANE = 0, S_SPHERE = 1, S_BOX = 2, S_CAPSULE = 3 };
+enum Shape { S_PLANE = 0, S_SPHERE = 1, S_BOX = 2, S_CAPSULE = 3, S_CYLINDER = 4, S_ELLIPSOID = 5 };
 
 template <class R> struct SolImp { R dmin = R(0.9), dmax = R(0.95), width = R(0.001), midpoint = R(0.5); int power = 2; };
 template <class R> struct SolRef { R timeconst = R(0.02), dampratio = R(1); bool direct() const { return timeconst < R(0); } };
@@ -238,6 +239,53 @@ template <class R> void closest_points_on_segments(Vec3<R> a0, Vec3<R> a1, Vec3<
   else if (tn > e) { t = R(1); sf = clamp01((b_ - c) / a); }
   else { t = tn / e; sf = s; }
   *pa = a0 + d1 * sf; *pb = b0 + d2 * t;
+}
+
+// contact.rs:1296-1373 cylinder_plane: 18 samples (both cap centres, then
+// the top and bottom rim points at 0, 45, ..., 315 degrees, interleaved), the
+// up to four deepest with penetration > 0, deepest first (ties keep sample
+// order), each projected onto the plane
+template <class R> CBuf<R> cylinder_plane(int ic, const Pose<R>& cp_, R radius, R hh, R fr, R margin, R gap, int ip, const Pose<R>& pp) {
+  Vec3<R> n = pp.o.rotate(Vec3<R>(0, 0, 1)), p0 = pp.p;
+  Vec3<R> ax = cp_.o.rotate(Vec3<R>(0, 0, 1)), xl = cp_.o.rotate(Vec3<R>(1, 0, 0)), yl = cp_.o.rotate(Vec3<R>(0, 1, 0));
+  Vec3<R> top = cp_.p + ax * hh, bot = cp_.p - ax * hh;
+  const R s = R(0.70710677f);
+  Vec3<R> rim[8] = {xl, xl * s + yl * s, yl, -xl * s + yl * s, -xl, -xl * s + -yl * s, -yl, xl * s + -yl * s};
+  Vec3<R> smp[18];
+  smp[0] = top; smp[1] = bot;
+  for (int i = 0; i < 8; ++i) { smp[2 + 2 * i] = top + rim[i] * radius; smp[3 + 2 * i] = bot + rim[i] * radius; }
+  R pen[18];
+  int order[18], cnt = 0;
+  for (int i = 0; i < 18; ++i) {
+    pen[i] = margin - (smp[i] - p0).dot(n);
+    if (pen[i] > R(0)) order[cnt++] = i;
+  }
+  for (int i = 1; i < cnt; ++i)
+    for (int j = i; j > 0 && pen[order[j]] > pen[order[j - 1]]; --j) std::swap(order[j - 1], order[j]);
+  CBuf<R> out;
+  for (int k = 0; k < (cnt > 4 ? 4 : cnt); ++k) {
+    int i = order[k];
+    out.push({ic, ip, smp[i] - n * (margin - pen[i]), n, pen[i], fr, gap});
+  }
+  return out;
+}
+
+// contact.rs:1381-1426 ellipsoid_plane: the support point along -n,
+// p = (a^2 d.x, b^2 d.y, c^2 d.z) / |(a d.x, b d.y, c d.z)| with d = -n in
+// the ellipsoid frame; one contact when margin - distance >= 0
+template <class R> CBuf<R> ellipsoid_plane(int ie, const Pose<R>& ep, Vec3<R> ax, R fr, R margin, R gap, int ip, const Pose<R>& pp) {
+  CBuf<R> out;
+  Vec3<R> n = pp.o.rotate(Vec3<R>(0, 0, 1)), p0 = pp.p;
+  Vec3<R> d = ep.o.inverse_rotate(-n);
+  R dsq = (ax.x * d.x) * (ax.x * d.x) + (ax.y * d.y) * (ax.y * d.y) + (ax.z * d.z) * (ax.z * d.z);
+  if (dsq <= R(0)) return out;
+  R den = Sc<R>::sqrt(dsq);
+  Vec3<R> pl = Vec3<R>(ax.x * ax.x * d.x, ax.y * ax.y * d.y, ax.z * ax.z * d.z) / den;
+  Vec3<R> sw = ep.p + ep.o.rotate(pl);
+  R sg = (sw - p0).dot(n);
+  R pen = margin - sg;
+  if (pen >= R(0)) out.push({ie, ip, sw - n * (sg * R(0.5)), n, pen, fr, gap});
+  return out;
 }
 
 // contact.rs:2313-2321 closest_point_on_segment
@@ -418,6 +466,11 @@ template <class R> bool try_np(int ia, const Geom<R>& a, const Pose<R>& pa, int 
   if (a.shape == S_SPHERE && b.shape == S_SPHERE) { *out = sphere_sphere(ia, pa.p, a.size[0], ib, pb.p, b.size[0], fr, margin, gap); return true; }
   if (a.shape == S_BOX && b.shape == S_BOX) {
     *out = box_box(ia, pa, Vec3<R>(a.size[0], a.size[1], a.size[2]), ib, pb, Vec3<R>(b.size[0], b.size[1], b.size[2]), fr, margin, gap);
+    return true;
+  }
+  if (a.shape == S_CYLINDER && b.shape == S_PLANE) { *out = cylinder_plane(ia, pa, a.size[0], a.size[1], fr, margin, gap, ib, pb); return true; }
+  if (a.shape == S_ELLIPSOID && b.shape == S_PLANE) {
+    *out = ellipsoid_plane(ia, pa, Vec3<R>(a.size[0], a.size[1], a.size[2]), fr, margin, gap, ib, pb);
     return true;
   }
   if (a.shape == S_SPHERE && b.shape == S_CAPSULE) {

@@ -252,7 +252,7 @@ void HostGroup::setup_tc(const HostModel& m) {
       gpairs.push_back(a);
       gpairs.push_back(b);
       const int shape = A.link >= 0 ? A.shape : B.shape;
-      maxc += shape == NEWT_SHAPE_BOX ? 4 : (shape == NEWT_SHAPE_CAPSULE ? 2 : 1);
+      maxc += (shape == NEWT_SHAPE_BOX || shape == NEWT_SHAPE_CYLINDER) ? 4 : (shape == NEWT_SHAPE_CAPSULE ? 2 : 1);
     }
   npairs = (int)gpairs.size() / 2;
   if (maxc < 1) maxc = 1;

@@ -11,6 +11,8 @@
 //   capsule_plane  newt/src/contact.rs:367-400
 //   sphere_capsule newt/src/contact.rs:473-505
 //   capsule_capsule newt/src/contact.rs:1249-1272
+//   cylinder_plane newt/src/contact.rs:1296-1373
+//   ellipsoid_plane newt/src/contact.rs:1381-1426
 //   sphere_box     extension (newt defers this pair, contact.rs:236-257):
 //                  closed-form closest point on the oriented box
 #pragma once
@@ -142,6 +144,74 @@ NEWT_D int np_capsule_capsule(const GPose& A, float ra, float ha, const GPose& B
   V3 pa, pb;
   seg_closest(A.p - ax * ha, A.p + ax * ha, B.p - bx * hb, B.p + bx * hb, &pa, &pb);
   return np_sphere_sphere(pa, ra, pb, rb, margin, out);
+}
+
+// Cylinder (A, axis local z) vs plane (B): 18 samples (the two cap centres,
+// then top and bottom rim points at 0, 45, ..., 315 degrees, interleaved),
+// the up to four deepest with penetration > 0, deepest first with ties in
+// sample order, each projected onto the plane (contact.rs:1296-1373).
+NEWT_D int np_cylinder_plane(const GPose& c, float r, float hh, float margin, const GPose& pl, CRes* out) {
+  const V3 n = qrot(pl.q, v3(0.f, 0.f, 1.f));
+  const V3 ax = qrot(c.q, v3(0.f, 0.f, 1.f)), xl = qrot(c.q, v3(1.f, 0.f, 0.f)), yl = qrot(c.q, v3(0.f, 1.f, 0.f));
+  const V3 top = c.p + ax * hh, bot = c.p - ax * hh;
+  const float s = 0.70710677f;
+  float best_pen[4];
+  int best_i[4], nb = 0;
+  for (int i = 0; i < 18; ++i) {
+    V3 p;
+    if (i < 2) {
+      p = i == 0 ? top : bot;
+    } else {
+      const int k = (i - 2) >> 1;
+      const float cx = (k == 0 || k == 1 || k == 7) ? 1.f : ((k == 3 || k == 4 || k == 5) ? -1.f : 0.f);
+      const float cy = (k == 1 || k == 2 || k == 3) ? 1.f : ((k == 5 || k == 6 || k == 7) ? -1.f : 0.f);
+      const V3 d = (k & 1) ? xl * (cx * s) + yl * (cy * s) : xl * cx + yl * cy;
+      p = ((i - 2) & 1 ? bot : top) + d * r;
+    }
+    const float pen = margin - dot(p - pl.p, n);
+    if (!(pen > 0.f)) continue;
+    // keep the four deepest; a later sample displaces only a strictly shallower one
+    int at = nb < 4 ? nb : 4;
+    while (at > 0 && pen > best_pen[at - 1]) --at;
+    if (at >= 4) continue;
+    for (int j = (nb < 4 ? nb : 3); j > at; --j) { best_pen[j] = best_pen[j - 1]; best_i[j] = best_i[j - 1]; }
+    best_pen[at] = pen;
+    best_i[at] = i;
+    if (nb < 4) ++nb;
+  }
+  for (int k = 0; k < nb; ++k) {
+    const int i = best_i[k];
+    V3 p;
+    if (i < 2) {
+      p = i == 0 ? top : bot;
+    } else {
+      const int q = (i - 2) >> 1;
+      const float cx = (q == 0 || q == 1 || q == 7) ? 1.f : ((q == 3 || q == 4 || q == 5) ? -1.f : 0.f);
+      const float cy = (q == 1 || q == 2 || q == 3) ? 1.f : ((q == 5 || q == 6 || q == 7) ? -1.f : 0.f);
+      const V3 d = (q & 1) ? xl * (cx * s) + yl * (cy * s) : xl * cx + yl * cy;
+      p = ((i - 2) & 1 ? bot : top) + d * r;
+    }
+    out[k] = CRes{p - n * (margin - best_pen[k]), n, best_pen[k]};
+  }
+  return nb;
+}
+
+// Ellipsoid (A, semi-axes e) vs plane (B): the support point along -n in the
+// ellipsoid frame, (e.x^2 d.x, e.y^2 d.y, e.z^2 d.z) / |(e.x d.x, e.y d.y,
+// e.z d.z)|; one contact when margin - distance >= 0 (contact.rs:1381-1426).
+NEWT_D int np_ellipsoid_plane(const GPose& e, V3 ax, float margin, const GPose& pl, CRes* out) {
+  const V3 n = qrot(pl.q, v3(0.f, 0.f, 1.f));
+  const V3 d = qrot_inv(e.q, -n);
+  const float dsq = (ax.x * d.x) * (ax.x * d.x) + (ax.y * d.y) * (ax.y * d.y) + (ax.z * d.z) * (ax.z * d.z);
+  if (!(dsq > 0.f)) return 0;
+  const float den = sqrtf(dsq);
+  const V3 pl_ = v3(ax.x * ax.x * d.x, ax.y * ax.y * d.y, ax.z * ax.z * d.z) / den;
+  const V3 sw = e.p + qrot(e.q, pl_);
+  const float sg = dot(sw - pl.p, n);
+  const float pen = margin - sg;
+  if (!(pen >= 0.f)) return 0;
+  out[0] = CRes{sw - n * (sg * 0.5f), n, pen};
+  return 1;
 }
 
 struct FV2 { float u, v, d; };

@@ -441,6 +441,10 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
         nc = np_box_plane(gpose, v3(gv(gl, G_SIZE), gv(gl, G_SIZE + 1), gv(gl, G_SIZE + 2)), margin, ppose, cr);
       } else if (shape == NEWT_SHAPE_CAPSULE) {
         nc = np_capsule_plane(gpose, gv(gl, G_SIZE), gv(gl, G_SIZE + 1), margin, ppose, cr);
+      } else if (shape == NEWT_SHAPE_CYLINDER) {
+        nc = np_cylinder_plane(gpose, gv(gl, G_SIZE), gv(gl, G_SIZE + 1), margin, ppose, cr);
+      } else if (shape == NEWT_SHAPE_ELLIPSOID) {
+        nc = np_ellipsoid_plane(gpose, v3(gv(gl, G_SIZE), gv(gl, G_SIZE + 1), gv(gl, G_SIZE + 2)), margin, ppose, cr);
       }
     }
     int incl = nc;  // inclusive scan of the per-pair counts

@@ -24,7 +24,7 @@
 
 namespace pile {
 
-constexpr int SH_PLANE = 0, SH_SPHERE = 1, SH_BOX = 2, SH_CAPSULE = 3;  // NEWT_SHAPE_*
+constexpr int SH_PLANE = 0, SH_SPHERE = 1, SH_BOX = 2, SH_CAPSULE = 3, SH_CYLINDER = 4, SH_ELLIPSOID = 5;  // NEWT_SHAPE_*
 constexpr int CF = 39;  // floats per contact in the scratch record
 constexpr int CI = 4;   // ints per contact
 constexpr int SC = 188;  // floats per active contact in the solver record (a multiple of 4)
@@ -154,7 +154,12 @@ NEWT_D void collide(const WsLay& L, float* wf, int* wi, int lane) {
       const V3 ax = qrot(p.q, v3(0.f, 0.f, 1.f));
       const float r = wf[L.size + 3 * e], hh = wf[L.size + 3 * e + 1];
       ext = v3(fabsf(ax.x) * hh + r, fabsf(ax.y) * hh + r, fabsf(ax.z) * hh + r);
-    } else {
+    } else if (sh == SH_CYLINDER) {  // (|x| + |y|) r + |z| h (broadphase.rs:731-739)
+      const V3 xa = qrot(p.q, v3(1.f, 0.f, 0.f)), ya = qrot(p.q, v3(0.f, 1.f, 0.f)), za = qrot(p.q, v3(0.f, 0.f, 1.f));
+      const float r = wf[L.size + 3 * e], hh = wf[L.size + 3 * e + 1];
+      ext = v3((fabsf(xa.x) + fabsf(ya.x)) * r + fabsf(za.x) * hh, (fabsf(xa.y) + fabsf(ya.y)) * r + fabsf(za.y) * hh,
+               (fabsf(xa.z) + fabsf(ya.z)) * r + fabsf(za.z) * hh);
+    } else {  // boxes and ellipsoids: oriented extents of the half sizes
       V3 h = ld3(wf + L.size + 3 * e);
       M3 R = quat_mat(p.q);
       ext = v3(fabsf(R.m[0][0]) * h.x + fabsf(R.m[0][1]) * h.y + fabsf(R.m[0][2]) * h.z,
@@ -275,6 +280,9 @@ NEWT_D void collide(const WsLay& L, float* wf, int* wi, int lane) {
       else if (sa == SH_SPHERE && sb == SH_BOX) cnt = np_sphere_box(pa, wf[L.size + 3 * ea], pb, ld3(wf + L.size + 3 * eb), margin, res);
       else if (sa == SH_CAPSULE && sb == SH_PLANE)
         cnt = np_capsule_plane(pa, wf[L.size + 3 * ea], wf[L.size + 3 * ea + 1], margin, pb, res);
+      else if (sa == SH_CYLINDER && sb == SH_PLANE)
+        cnt = np_cylinder_plane(pa, wf[L.size + 3 * ea], wf[L.size + 3 * ea + 1], margin, pb, res);
+      else if (sa == SH_ELLIPSOID && sb == SH_PLANE) cnt = np_ellipsoid_plane(pa, ld3(wf + L.size + 3 * ea), margin, pb, res);
       else if (sa == SH_SPHERE && sb == SH_CAPSULE)
         cnt = np_sphere_capsule(pa.p, wf[L.size + 3 * ea], pb, wf[L.size + 3 * eb], wf[L.size + 3 * eb + 1], margin, res);
       else if (sa == SH_CAPSULE && sb == SH_CAPSULE)
@@ -287,6 +295,9 @@ NEWT_D void collide(const WsLay& L, float* wf, int* wi, int lane) {
         else if (sb == SH_SPHERE && sa == SH_BOX) cnt = np_sphere_box(pb, wf[L.size + 3 * eb], pa, ld3(wf + L.size + 3 * ea), margin, res);
         else if (sb == SH_CAPSULE && sa == SH_PLANE)
           cnt = np_capsule_plane(pb, wf[L.size + 3 * eb], wf[L.size + 3 * eb + 1], margin, pa, res);
+        else if (sb == SH_CYLINDER && sa == SH_PLANE)
+          cnt = np_cylinder_plane(pb, wf[L.size + 3 * eb], wf[L.size + 3 * eb + 1], margin, pa, res);
+        else if (sb == SH_ELLIPSOID && sa == SH_PLANE) cnt = np_ellipsoid_plane(pb, ld3(wf + L.size + 3 * eb), margin, pa, res);
         else if (sb == SH_SPHERE && sa == SH_CAPSULE)
           cnt = np_sphere_capsule(pb.p, wf[L.size + 3 * eb], pa, wf[L.size + 3 * ea], wf[L.size + 3 * ea + 1], margin, res);
       }

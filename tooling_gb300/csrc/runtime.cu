@@ -69,10 +69,24 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
   m.nq = nq; m.nv = nv;
   if (d.n_links > NEWT_MAX_LINKS) return fail(ctx, NEWT_E_INVALID, "too many links");
   if (d.n_bodies > NEWT_MAX_BODIES) return fail(ctx, NEWT_E_INVALID, "too many bodies");
+  // shape sizes (newt's geom constructors and loaders refuse the rest)
+  for (int k = 0; k < d.n_geoms; ++k) {
+    const newt_geom_desc& G = d.geoms[k];
+    const float a = G.size[0], b = G.size[1], c = G.size[2];
+    bool ok = true;
+    switch (G.shape) {
+      case NEWT_SHAPE_SPHERE: ok = a > 0.f; break;
+      case NEWT_SHAPE_BOX: case NEWT_SHAPE_ELLIPSOID: ok = a > 0.f && b > 0.f && c > 0.f; break;
+      case NEWT_SHAPE_CAPSULE: ok = a > 0.f && b >= 0.f; break;
+      case NEWT_SHAPE_CYLINDER: ok = a > 0.f && b > 0.f; break;
+      default: break;
+    }
+    if (!ok) return fail(ctx, NEWT_E_INVALID, "geom size out of range for its shape");
+  }
   // classify
   if (d.n_links > 0 && d.n_bodies == 0 && d.n_geoms == 0) { m.kind = GK_TREE; m.size = d.n_links; return NEWT_OK; }
   if (d.n_links == 0 && d.n_bodies > 0) {
-    // piles: one geom per body (sphere/box) plus static planes
+    // piles: one geom per body plus static planes
     std::vector<int> per_body(d.n_bodies, 0);
     int np = 0;
     for (int k = 0; k < d.n_geoms; ++k) {
@@ -80,10 +94,9 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
       if (G.link >= 0) return fail(ctx, NEWT_E_INVALID, "link geom in a tree-less world");
       if (G.body >= 0) {
         if (G.body >= d.n_bodies) return fail(ctx, NEWT_E_INVALID, "geom body out of range");
-        if (G.shape != NEWT_SHAPE_SPHERE && G.shape != NEWT_SHAPE_BOX && G.shape != NEWT_SHAPE_CAPSULE)
-          return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "free-body geoms must be spheres, boxes or capsules on the GPU path");
-        if (G.shape == NEWT_SHAPE_CAPSULE && !(G.size[0] > 0.f && G.size[1] >= 0.f))
-          return fail(ctx, NEWT_E_INVALID, "capsule needs radius > 0 and half_height >= 0");
+        if (G.shape < NEWT_SHAPE_SPHERE || G.shape > NEWT_SHAPE_ELLIPSOID)
+          return fail(ctx, NEWT_E_UNSUPPORTED_PAIR,
+                      "free-body geoms must be spheres, boxes, capsules, cylinders or ellipsoids on the GPU path");
         per_body[G.body]++;
       } else {
         if (G.shape != NEWT_SHAPE_PLANE) return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "static geoms must be planes");
@@ -99,8 +112,14 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
         if (A.body < 0 || B.body < 0) continue;
         const bool cb = (A.shape == NEWT_SHAPE_CAPSULE && B.shape == NEWT_SHAPE_BOX) ||
                         (A.shape == NEWT_SHAPE_BOX && B.shape == NEWT_SHAPE_CAPSULE);
-        if (cb && (A.group & B.mask) != 0u && (B.group & A.mask) != 0u)
-          return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "capsule-box pairs are not supported (newt/src/contact.rs:232-257)");
+        const bool round = A.shape == NEWT_SHAPE_CYLINDER || A.shape == NEWT_SHAPE_ELLIPSOID ||
+                           B.shape == NEWT_SHAPE_CYLINDER || B.shape == NEWT_SHAPE_ELLIPSOID;
+        if (!(cb || round) || !((A.group & B.mask) != 0u && (B.group & A.mask) != 0u)) continue;
+        if (cb) return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "capsule-box pairs are not supported (newt/src/contact.rs:232-257)");
+        // cylinders and ellipsoids touch planes only here; newt's sphere-cylinder
+        // and sphere-ellipsoid routes (contact.rs:1519-1725) are not on the GPU path
+        return fail(ctx, NEWT_E_UNSUPPORTED_PAIR,
+                    "a cylinder or ellipsoid body may only collide with planes on the GPU path (filter its body pairs)");
       }
     for (int b = 0; b < d.n_bodies; ++b) {
       if (per_body[b] != 1) return fail(ctx, NEWT_E_INVALID, "GPU piles need exactly one geom per body");
@@ -125,8 +144,9 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
       if (G.body >= 0) return fail(ctx, NEWT_E_INVALID, "body geom in a world without free bodies");
       if (G.link >= d.n_links) return fail(ctx, NEWT_E_INVALID, "geom link out of range");
       if (G.link >= 0) {
-        if (G.shape != NEWT_SHAPE_SPHERE && G.shape != NEWT_SHAPE_BOX && G.shape != NEWT_SHAPE_CAPSULE)
-          return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "link geoms must be spheres, boxes or capsules on the GPU path");
+        if (G.shape < NEWT_SHAPE_SPHERE || G.shape > NEWT_SHAPE_ELLIPSOID)
+          return fail(ctx, NEWT_E_UNSUPPORTED_PAIR,
+                      "link geoms must be spheres, boxes, capsules, cylinders or ellipsoids on the GPU path");
         ++nlink_geoms;
       } else if (G.shape != NEWT_SHAPE_PLANE) {
         return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "static geoms must be planes");

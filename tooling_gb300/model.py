@@ -17,7 +17,7 @@ from typing import List, Optional, Sequence
 import numpy as np
 
 JOINT_FREE, JOINT_FIXED, JOINT_HINGE, JOINT_SLIDE, JOINT_BALL = 0, 1, 2, 3, 4
-SHAPE_PLANE, SHAPE_SPHERE, SHAPE_BOX, SHAPE_CAPSULE = 0, 1, 2, 3
+SHAPE_PLANE, SHAPE_SPHERE, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_CYLINDER, SHAPE_ELLIPSOID = 0, 1, 2, 3, 4, 5
 SOLVER_PGS, SOLVER_NEWTON = 1, 2
 INTEGRATOR_EULER, INTEGRATOR_RK4 = 0, 1
 JOINT_NQ = {JOINT_FREE: 7, JOINT_FIXED: 0, JOINT_HINGE: 1, JOINT_SLIDE: 1, JOINT_BALL: 4}
@@ -73,6 +73,24 @@ def solid_box_inertia(mass: float, h: Sequence[float]) -> List[float]:
     hx2, hy2, hz2 = f(h[0]) * f(h[0]), f(h[1]) * f(h[1]), f(h[2]) * f(h[2])
     m3 = f(mass) / f(3.0)
     return _diag9(m3 * (hy2 + hz2), m3 * (hx2 + hz2), m3 * (hx2 + hy2))
+
+
+def solid_cylinder_inertia(mass: float, radius: float, half_height: float) -> List[float]:
+    """newt/src/geom.rs:993-999 (evaluated in f32)."""
+    f = np.float32
+    m, r2, h2 = f(mass), f(radius) * f(radius), f(half_height) * f(half_height)
+    i_zz = f(0.5) * m * r2
+    i_xx = (f(1.0) / f(12.0)) * m * (f(3.0) * r2 + f(4.0) * h2)
+    return _diag9(i_xx, i_xx, i_zz)
+
+
+def solid_ellipsoid_inertia(mass: float, semi_axes: Sequence[float]) -> List[float]:
+    """newt/src/geom.rs:1009-1017 (evaluated in f32)."""
+    f = np.float32
+    m = f(mass)
+    a2, b2, c2 = (f(x) * f(x) for x in semi_axes)
+    k = f(1.0) / f(5.0)
+    return _diag9(k * m * (b2 + c2), k * m * (a2 + c2), k * m * (a2 + b2))
 
 
 def solid_capsule_inertia(mass: float, radius: float, half_height: float) -> List[float]:
@@ -134,7 +152,7 @@ class WorldModel:
     solver: int = SOLVER_PGS
     iterations: int = 20
     tree_self_collision: int = 0
-    integrator: int = 0  # INTEGRATOR_EULER or INTEGRATOR_RK4 (trees without geoms)
+    integrator: int = 0  # INTEGRATOR_EULER or INTEGRATOR_RK4
     links: List[Link] = field(default_factory=list)
     bodies: List[tuple] = field(default_factory=list)  # (mass, inertia9)
     geoms: List[Geom] = field(default_factory=list)
