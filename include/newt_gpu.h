@@ -204,6 +204,42 @@ NEWT_API int newt_gpu_world_status(newt_gpu_ctx* ctx, const int32_t* slots, int3
  * world.  Mirrors the qacc that `euler_step_with_workspace` integrates
  * (newt/src/tree.rs:1406-1417). */
 NEWT_API int newt_gpu_get_qacc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, float* qacc);
+/* Post-step sensors that read the state alone (newt/src/sensor.rs:153-196,
+ * evaluated as World::evaluate_sensors does after a step, sensor.rs:446-700).
+ * A site frame is (local_pos, local_quat x y z w) in its parent: free body
+ * `index` (on_link 0) or link `index` of the world's tree (on_link 1).
+ *   JOINTPOS / JOINTVEL  hinge or slide coordinate and rate of link `index` (1)
+ *   FRAMEPOS             site position, world (3)
+ *   FRAMEQUAT            site orientation x y z w, world (4)
+ *   GYRO                 parent's body-frame angular velocity in the site frame (3)
+ *   VELOCIMETER          site linear velocity in the site frame (3)
+ *   FRAMELINVEL          site linear velocity, world (3)
+ *   FRAMEANGVEL          parent's angular velocity, world (3)
+ *   SUBTREECOM           mass-weighted centre of link `index` and its descendants (3)
+ * Touch, accelerometer, force and torque readings need newt's post-step
+ * contact re-solve and are not provided. */
+#define NEWT_SENSOR_JOINTPOS 0
+#define NEWT_SENSOR_JOINTVEL 1
+#define NEWT_SENSOR_FRAMEPOS 2
+#define NEWT_SENSOR_FRAMEQUAT 3
+#define NEWT_SENSOR_GYRO 4
+#define NEWT_SENSOR_VELOCIMETER 5
+#define NEWT_SENSOR_FRAMELINVEL 6
+#define NEWT_SENSOR_FRAMEANGVEL 7
+#define NEWT_SENSOR_SUBTREECOM 8
+typedef struct newt_sensor_desc {
+  int32_t kind;        /* NEWT_SENSOR_* */
+  int32_t on_link;     /* 1: `index` is a link of the world's tree, 0: a free body */
+  int32_t index;
+  float local_pos[3];
+  float local_quat[4]; /* x y z w */
+} newt_sensor_desc;
+/* Evaluates `n_sensors` sensors on each of `n` worlds at their current state,
+ * on the device; `out` receives n rows of the sensors' values concatenated in
+ * order (the layout of newt's SensorBank::data, sensor.rs:370-400). */
+NEWT_API int newt_gpu_read_sensors(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, const newt_sensor_desc* sensors,
+                                   int32_t n_sensors, float* out);
+
 /* Contacts detected at the start of the last step for one world:
  * per contact (geom_a, geom_b) pairs into `pairs` (2*cap ints) and
  * pos xyz, normal xyz, penetration into `data` (7*cap floats). */

@@ -338,6 +338,91 @@ int oracle_contacts(const newt_model_desc* d, const float* qpos, const float* qv
   return 0;
 }
 
+// Post-step sensors of one world at its state (MuJoCo layout), restating
+// newt/src/sensor.rs:560-700 for the kinds that read the state alone, with
+// site_world_pose (sensor.rs:794-806), parent_body_velocities (:812-828),
+// site_velocity (:705-726), subtree_com (:728-757) and the link velocities of
+// compute_link_va (:834-900) at zero acceleration.  `sensors` holds per sensor
+// (kind, on_link, index) ints in `si` and (local_pos xyz, local_quat xyzw) in
+// `sf`; `out` receives the concatenated values.
+int oracle_sensors(const newt_model_desc* d, const float* qpos, const float* qvel, int precision, int ns,
+                   const int* si, const float* sf, double* out) {
+  auto go = [&](auto tag) {
+    using R = decltype(tag);
+    World<R> w = build_world<R>(*d);
+    set_state(w, qpos, qvel, 0);
+    std::vector<Pose<R>> poses;
+    std::vector<GMotion<R>> v;
+    if (!w.trees.empty()) {
+      const Tree<R>& t = w.trees[0];
+      forward_kinematics(t, poses);
+      const int n = (int)t.links.size();
+      v.assign(n, GMotion<R>{Vec3<R>(), Vec3<R>()});
+      for (int i = 0; i < n; ++i) {
+        const Link<R>& L = t.links[i];
+        if (L.type == J_FREE) {
+          const int o = t.v_off[i];
+          v[i] = {Vec3<R>(t.qdot[o], t.qdot[o + 1], t.qdot[o + 2]), Vec3<R>(t.qdot[o + 3], t.qdot[o + 4], t.qdot[o + 5])};
+        } else if (L.type == J_FIXED) {
+          v[i] = xup_fixed(L).motion(L.parent >= 0 ? v[L.parent] : GMotion<R>{Vec3<R>(), Vec3<R>()});
+        } else {
+          const GMotion<R> S = L.type == J_HINGE ? GMotion<R>{L.axis, L.jc_pos.cross(L.axis)} : GMotion<R>{Vec3<R>(), L.axis};
+          v[i] = xup_joint(L, t.q[t.q_off[i]]).motion(v[L.parent]).add(S.scale(t.qdot[t.v_off[i]]));
+        }
+      }
+    }
+    int o = 0;
+    for (int k = 0; k < ns; ++k) {
+      const int kind = si[3 * k], on_link = si[3 * k + 1], idx = si[3 * k + 2];
+      const Vec3<R> lp(sf[7 * k], sf[7 * k + 1], sf[7 * k + 2]);
+      const Quat<R> lq(sf[7 * k + 3], sf[7 * k + 4], sf[7 * k + 5], sf[7 * k + 6]);
+      auto put3 = [&](Vec3<R> x) { out[o++] = (double)x.x; out[o++] = (double)x.y; out[o++] = (double)x.z; };
+      if (kind == 0 || kind == 1) {  // JointPos / JointVel
+        const Tree<R>& t = w.trees[0];
+        out[o++] = (double)(kind == 0 ? t.q[t.q_off[idx]] : t.qdot[t.v_off[idx]]);
+        continue;
+      }
+      if (kind == 8) {  // SubtreeCom
+        const Tree<R>& t = w.trees[0];
+        Vec3<R> acc;
+        R m = R(0);
+        for (int j = 0; j < (int)t.links.size(); ++j) {
+          int c = j;
+          bool inc = false;
+          while (c >= 0) { if (c == idx) { inc = true; break; } c = t.links[c].parent; }
+          if (inc) { acc = acc + poses[j].p * t.links[j].mass; m = m + t.links[j].mass; }
+        }
+        put3(m == R(0) ? Vec3<R>() : acc / m);
+        continue;
+      }
+      Vec3<R> pp, wb, lin, ang;
+      Quat<R> po;
+      if (on_link) {
+        pp = poses[idx].p; po = poses[idx].o;
+        wb = v[idx].ang;
+        ang = po.rotate(v[idx].ang);
+        lin = po.rotate(v[idx].lin + v[idx].ang.cross(lp));
+      } else {
+        const Body<R>& b = w.bodies[idx];
+        pp = b.pos; po = b.ori; wb = b.omega_body;
+        ang = b.ori.rotate(b.omega_body);
+        lin = b.vel + ang.cross(b.ori.rotate(lp));
+      }
+      const Quat<R> so = po * lq;
+      switch (kind) {
+        case 2: put3(pp + po.rotate(lp)); break;
+        case 3: out[o++] = (double)so.x; out[o++] = (double)so.y; out[o++] = (double)so.z; out[o++] = (double)so.w; break;
+        case 4: put3(lq.inverse_rotate(wb)); break;
+        case 5: put3(so.inverse_rotate(lin)); break;
+        case 6: put3(lin); break;
+        default: put3(ang); break;
+      }
+    }
+  };
+  if (precision == 0) go(0.0f); else go(0.0);
+  return 0;
+}
+
 // PGS row impulses of one free-body world at its state (one step's solve).
 int oracle_impulses(const newt_model_desc* d, const float* qpos, const float* qvel, int precision, int iterations,
                     int cap, int* n_out, double* impulses) {

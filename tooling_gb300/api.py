@@ -30,8 +30,24 @@ EXPORTED = [
     "newt_gpu_get_contacts", "newt_gpu_get_impulses", "newt_gpu_event_record", "newt_gpu_event_elapsed_ms",
     "newt_gpu_flush_l2", "newt_gpu_launch_count", "newt_gpu_step_static", "newt_gpu_pile_profile",
     "newt_gpu_tc_profile", "newt_gpu_serve", "newt_gpu_memory", "newt_gpu_autotune",
-    "newt_gpu_set_ctrl_stream", "newt_gpu_apply_ctrl",
+    "newt_gpu_set_ctrl_stream", "newt_gpu_apply_ctrl", "newt_gpu_read_sensors",
 ]
+# newt_sensor_desc (include/newt_gpu.h)
+SENSOR_DTYPE = np.dtype([("kind", np.int32), ("on_link", np.int32), ("index", np.int32),
+                         ("local_pos", np.float32, 3), ("local_quat", np.float32, 4)])
+SENSOR_JOINTPOS, SENSOR_JOINTVEL, SENSOR_FRAMEPOS, SENSOR_FRAMEQUAT, SENSOR_GYRO = 0, 1, 2, 3, 4
+SENSOR_VELOCIMETER, SENSOR_FRAMELINVEL, SENSOR_FRAMEANGVEL, SENSOR_SUBTREECOM = 5, 6, 7, 8
+SENSOR_DIM = {SENSOR_JOINTPOS: 1, SENSOR_JOINTVEL: 1, SENSOR_FRAMEQUAT: 4}
+
+
+def sensors(*specs) -> np.ndarray:
+    """Sensor descriptors from (kind, on_link, index[, local_pos[, local_quat xyzw]]) tuples."""
+    out = np.zeros(len(specs), SENSOR_DTYPE)
+    for i, sp in enumerate(specs):
+        out[i]["kind"], out[i]["on_link"], out[i]["index"] = sp[0], sp[1], sp[2]
+        out[i]["local_pos"] = sp[3] if len(sp) > 3 else (0.0, 0.0, 0.0)
+        out[i]["local_quat"] = sp[4] if len(sp) > 4 else (0.0, 0.0, 0.0, 1.0)
+    return out
 TC_KERNELS = ["tree_aba_kernel", "tc_k_solve", "tree_integrate_kernel"]
 PILE_KERNELS = ["pile_k_collide", "pile_k_pgs_small<1>", "pile_k_pgs_small<2>", "pile_k_pgs_small<4>",
                 "pile_k_pgs_quad[3]", "pile_k_pgs_quad[4]", "pile_k_pgs_quad[5]", "pile_k_pgs_levels[6]",
@@ -211,6 +227,16 @@ class Engine:
         s = np.ascontiguousarray(slots, np.int32)
         out = np.zeros(nv_total, np.float32)
         self._ck(self.L.newt_gpu_get_qacc(self.ctx, _p(s), len(s), _p(out)))
+        return out
+
+    def read_sensors(self, slots, sens: np.ndarray) -> np.ndarray:
+        """Evaluate `sens` (a SENSOR_DTYPE array) on each world at its current
+        state, on the device; returns (len(slots), total sensor dim)."""
+        s = np.ascontiguousarray(slots, np.int32)
+        sens = np.ascontiguousarray(sens, SENSOR_DTYPE)
+        D = sum(SENSOR_DIM.get(int(k), 3) for k in sens["kind"])
+        out = np.zeros((len(s), D), np.float32)
+        self._ck(self.L.newt_gpu_read_sensors(self.ctx, _p(s), len(s), _p(sens), len(sens), _p(out)))
         return out
 
     # -- stepping -------------------------------------------------------------

@@ -18,7 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnewt_gpu.so")
 SOURCES = ["runtime.cu", "groups.cu", "step.cu", "tree_kernels.cu", "pile_kernels.cu", "newton_kernels.cu",
            "static_step.cu",
-           "world_io.cu", "serve.cpp", "ctrl_stream.cu"]
+           "world_io.cu", "serve.cpp", "ctrl_stream.cu", "sensors.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

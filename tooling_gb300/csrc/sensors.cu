@@ -1,0 +1,265 @@
+// Post-step sensors that read the state alone: one thread per world walks the
+// tree (forward kinematics and link velocities) or reads the free bodies, then
+// writes every requested sensor's values into the world's output row.
+//
+// Restates, for FP32 on sm_103a:
+//   newt/src/sensor.rs:560-700   evaluate (JointPos, JointVel, FramePos,
+//                                FrameQuat, Gyro, Velocimeter, SubtreeCom,
+//                                FrameLinVel, FrameAngVel)
+//   newt/src/sensor.rs:705-757   site_velocity, subtree_com
+//   newt/src/sensor.rs:794-828   site_world_pose, parent_body_velocities
+//   newt/src/tree.rs:771-858     forward_kinematics (link poses)
+// Link velocities are propagated in the world frame (angular rate and the link
+// origin's velocity) and rotated into the link frame at the end; newt
+// propagates the body-frame spatial velocity (sensor.rs:834-900).  Both give
+// the same vectors up to rounding.
+#include <vector>
+
+#include "../../include/newt_gpu.h"
+#include "common.cuh"
+#include "groups.h"
+#include "runtime.h"
+
+namespace {
+
+enum { JF = 0, JX = 1, JH = 2, JS = 3 };
+
+__host__ __device__ int sensor_dim(int kind) {
+  return kind <= NEWT_SENSOR_JOINTVEL ? 1 : (kind == NEWT_SENSOR_FRAMEQUAT ? 4 : 3);
+}
+
+NEWT_D Q4 axis_angle(V3 axis, float angle) {  // newt/src/math.rs:574-580
+  const float l = sqrtf(len2(axis));
+  const V3 a = l > 0.f ? axis * (1.f / l) : v3(0.f, 0.f, 0.f);
+  float s, c;
+  sincosf(angle * 0.5f, &s, &c);
+  return Q4{a.x * s, a.y * s, a.z * s, c};
+}
+
+// The site's parent frame: pose, world angular velocity, the velocity of its
+// origin (the body's or link's centre of mass), and the body-frame angular
+// velocity.
+struct Frame { V3 p; Q4 o; V3 w_world, v_world, w_body; };
+
+NEWT_D void write_sensors(const newt_sensor_desc* S, int ns, const Frame* frames, const float* q, const float* qd,
+                          const int* qoff, const int* voff, float* row, const V3* subtree_com) {
+  int o = 0;
+  for (int k = 0; k < ns; ++k) {
+    const newt_sensor_desc& s = S[k];
+    const int kind = s.kind;
+    if (kind == NEWT_SENSOR_JOINTPOS) { row[o++] = q[qoff[s.index]]; continue; }
+    if (kind == NEWT_SENSOR_JOINTVEL) { row[o++] = qd[voff[s.index]]; continue; }
+    if (kind == NEWT_SENSOR_SUBTREECOM) {
+      const V3 c = subtree_com[k];
+      row[o++] = c.x; row[o++] = c.y; row[o++] = c.z;
+      continue;
+    }
+    const Frame& f = frames[k];
+    const V3 lp = v3(s.local_pos[0], s.local_pos[1], s.local_pos[2]);
+    const Q4 lq{s.local_quat[0], s.local_quat[1], s.local_quat[2], s.local_quat[3]};
+    V3 r;
+    switch (kind) {
+      case NEWT_SENSOR_FRAMEPOS: r = f.p + qrot(f.o, lp); break;
+      case NEWT_SENSOR_FRAMEQUAT: {
+        const Q4 so = qmul(f.o, lq);
+        row[o++] = so.x; row[o++] = so.y; row[o++] = so.z; row[o++] = so.w;
+        continue;
+      }
+      case NEWT_SENSOR_GYRO: r = qrot_inv(lq, f.w_body); break;
+      case NEWT_SENSOR_FRAMEANGVEL: r = f.w_world; break;
+      default: {  // site linear velocity: origin velocity plus w x (R lp)
+        const V3 lin = f.v_world + cross(f.w_world, qrot(f.o, lp));
+        r = kind == NEWT_SENSOR_VELOCIMETER ? qrot_inv(qmul(f.o, lq), lin) : lin;
+      }
+    }
+    row[o++] = r.x; row[o++] = r.y; row[o++] = r.z;
+  }
+}
+
+// Tree worlds (trees without geoms and tree-contact worlds): newt layout q/qd
+// in the group's SoA rows.  Frames for link sensors and subtree centres are
+// collected per sensor as the links are walked.
+template <int MAXL>
+__global__ void __launch_bounds__(64) tree_sensors_kernel(TreeGroupDev g, const int* idx, int n,
+                                                         const newt_sensor_desc* S, int ns, float* out, int D) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int w = idx[t], cap = g.cap, L = g.L;
+  float q[MAXL + 6], qd[MAXL + 5];
+  for (int k = 0; k < g.nq; ++k) q[k] = g.q[k * cap + w];
+  for (int k = 0; k < g.nv; ++k) qd[k] = g.qd[k * cap + w];
+  V3 P[MAXL], Wn[MAXL], Vn[MAXL];
+  Q4 O[MAXL];
+  int qoff[MAXL], voff[MAXL];
+  for (int i = 0; i < L; ++i) {
+    const int parent = g.topo[4 * i], jt = g.topo[4 * i + 1], qo = g.topo[4 * i + 2], vo = g.topo[4 * i + 3];
+    qoff[i] = qo; voff[i] = vo;
+    const V3 jp = v3(g.jp[(3 * i) * cap + w], g.jp[(3 * i + 1) * cap + w], g.jp[(3 * i + 2) * cap + w]);
+    const V3 jc = v3(g.jc[(3 * i) * cap + w], g.jc[(3 * i + 1) * cap + w], g.jc[(3 * i + 2) * cap + w]);
+    if (i == 0) {
+      if (jt == JF) {
+        P[0] = v3(q[qo], q[qo + 1], q[qo + 2]);
+        O[0] = Q4{q[qo + 3], q[qo + 4], q[qo + 5], q[qo + 6]};
+        Wn[0] = qrot(O[0], v3(qd[vo], qd[vo + 1], qd[vo + 2]));
+        Vn[0] = qrot(O[0], v3(qd[vo + 3], qd[vo + 4], qd[vo + 5]));
+      } else {
+        O[0] = Q4{g.rootq[w], g.rootq[cap + w], g.rootq[2 * cap + w], g.rootq[3 * cap + w]};
+        P[0] = jp - qrot(O[0], jc);
+        Wn[0] = v3(0.f, 0.f, 0.f);
+        Vn[0] = v3(0.f, 0.f, 0.f);
+      }
+      continue;
+    }
+    const V3 ax = v3(g.axis[(3 * i) * cap + w], g.axis[(3 * i + 1) * cap + w], g.axis[(3 * i + 2) * cap + w]);
+    const Q4 po = O[parent];
+    const V3 anchor = P[parent] + qrot(po, jp);
+    V3 wrel = v3(0.f, 0.f, 0.f), vrel = v3(0.f, 0.f, 0.f);
+    if (jt == JH) {
+      O[i] = qmul(po, axis_angle(ax, q[qo]));
+      P[i] = anchor - qrot(O[i], jc);
+      wrel = qrot(po, ax) * qd[vo];
+      vrel = cross(wrel, P[i] - anchor);
+    } else if (jt == JS) {
+      O[i] = po;
+      P[i] = anchor + qrot(po, ax * q[qo]) - qrot(O[i], jc);
+      vrel = qrot(po, ax) * qd[vo];
+    } else {
+      O[i] = po;
+      P[i] = anchor - qrot(O[i], jc);
+    }
+    Wn[i] = Wn[parent] + wrel;
+    Vn[i] = Vn[parent] + cross(Wn[parent], P[i] - P[parent]) + vrel;
+  }
+  Frame fr[16];
+  V3 com[16];
+  for (int k = 0; k < ns && k < 16; ++k) {
+    const newt_sensor_desc& s = S[k];
+    const int l = s.index;
+    if (s.kind == NEWT_SENSOR_SUBTREECOM) {  // sensor.rs:728-757: links whose parent chain reaches l
+      V3 acc = v3(0.f, 0.f, 0.f);
+      float m = 0.f;
+      for (int j = 0; j < L; ++j) {
+        int c = j;
+        while (c > l) c = g.topo[4 * c];
+        if (c != l) continue;
+        const float mj = g.mass[j * cap + w];
+        acc = acc + P[j] * mj;
+        m += mj;
+      }
+      com[k] = m == 0.f ? v3(0.f, 0.f, 0.f) : acc / m;
+      continue;
+    }
+    if (s.kind <= NEWT_SENSOR_JOINTVEL) continue;
+    fr[k] = Frame{P[l], O[l], Wn[l], Vn[l], qrot_inv(O[l], Wn[l])};
+  }
+  write_sensors(S, ns, fr, q, qd, qoff, voff, out + (size_t)t * D, com);
+}
+
+// Pile worlds: free-body poses and velocities from the world-major record.
+__global__ void __launch_bounds__(64) pile_sensors_kernel(PileGroupDev g, const int* idx, int n,
+                                                         const newt_sensor_desc* S, int ns, float* out, int D) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const float* F = g.F + (size_t)idx[t] * g.lay.fstride;
+  Frame fr[16];
+  for (int k = 0; k < ns && k < 16; ++k) {
+    const int b = S[k].index;
+    const Q4 o{F[g.lay.quat + 4 * b], F[g.lay.quat + 4 * b + 1], F[g.lay.quat + 4 * b + 2], F[g.lay.quat + 4 * b + 3]};
+    const V3 wb = v3(F[g.lay.omg + 3 * b], F[g.lay.omg + 3 * b + 1], F[g.lay.omg + 3 * b + 2]);
+    fr[k] = Frame{v3(F[g.lay.pos + 3 * b], F[g.lay.pos + 3 * b + 1], F[g.lay.pos + 3 * b + 2]), o, qrot(o, wb),
+                  v3(F[g.lay.vel + 3 * b], F[g.lay.vel + 3 * b + 1], F[g.lay.vel + 3 * b + 2]), wb};
+  }
+  write_sensors(S, ns, fr, nullptr, nullptr, nullptr, nullptr, out + (size_t)t * D, nullptr);
+}
+
+int bad(newt_gpu_ctx* ctx, const char* msg) {
+  ctx->err = msg;
+  return NEWT_E_INVALID;
+}
+
+}  // namespace
+
+extern "C" int newt_tree_bucket(int L);
+
+int newt_gpu_read_sensors(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, const newt_sensor_desc* sensors,
+                          int32_t n_sensors, float* out) {
+  if (!ctx || n < 0 || n_sensors < 0 || (n > 0 && (!slots || !out)) || (n_sensors > 0 && !sensors))
+    return NEWT_E_INVALID;
+  if (n_sensors > 16) return bad(ctx, "at most 16 sensors per call");
+  if (n == 0 || n_sensors == 0) return NEWT_OK;
+  cudaSetDevice(ctx->device);
+  int D = 0;
+  for (int k = 0; k < n_sensors; ++k) {
+    if (sensors[k].kind < NEWT_SENSOR_JOINTPOS || sensors[k].kind > NEWT_SENSOR_SUBTREECOM)
+      return bad(ctx, "unknown sensor kind");
+    D += sensor_dim(sensors[k].kind);
+  }
+  // validate every world against every sensor, and group the worlds
+  std::vector<std::vector<int>> idx(ctx->groups.size()), rows(ctx->groups.size());
+  for (int i = 0; i < n; ++i) {
+    const int s = slots[i];
+    if (s < 0 || s >= (int)ctx->slots.size() || !ctx->slots[s].live) return bad(ctx, "bad slot");
+    const SlotRef& r = ctx->slots[s];
+    const HostModel& m = ctx->models[r.model];
+    const bool tree = m.kind != GK_PILE;
+    for (int k = 0; k < n_sensors; ++k) {
+      const newt_sensor_desc& d = sensors[k];
+      const bool link_only = d.kind <= NEWT_SENSOR_JOINTVEL || d.kind == NEWT_SENSOR_SUBTREECOM;
+      if ((d.on_link != 0) != tree || (link_only && !d.on_link))
+        return bad(ctx, "sensor attachment does not match the world (links for trees, bodies for piles)");
+      if (d.index < 0 || d.index >= (tree ? m.n_links : m.n_bodies)) return bad(ctx, "sensor index out of range");
+      if (d.kind <= NEWT_SENSOR_JOINTVEL && m.links[d.index].joint != NEWT_JOINT_HINGE &&
+          m.links[d.index].joint != NEWT_JOINT_SLIDE)
+        return bad(ctx, "joint sensors read hinge or slide links");
+    }
+    idx[r.group].push_back(r.index);
+    rows[r.group].push_back(i);
+  }
+  cudaStream_t st = ctx->stream;
+  newt_sensor_desc* dS = nullptr;
+  int* dI = nullptr;
+  float* dO = nullptr;
+  cudaError_t e = cudaMallocAsync(&dS, sizeof(newt_sensor_desc) * n_sensors, st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&dI, sizeof(int) * n, st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&dO, sizeof(float) * (size_t)n * D, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dS, sensors, sizeof(newt_sensor_desc) * n_sensors, cudaMemcpyHostToDevice, st);
+  std::vector<int> order;  // the device rows' order: grouped
+  std::vector<float> host((size_t)n * D);
+  size_t base = 0;
+  for (size_t gi = 0; gi < idx.size() && e == cudaSuccess; ++gi) {
+    const int cnt = (int)idx[gi].size();
+    if (cnt == 0) continue;
+    e = cudaMemcpyAsync(dI + base, idx[gi].data(), sizeof(int) * cnt, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) break;
+    HostGroup* g = ctx->groups[gi].get();
+    const int grid = (cnt + 63) / 64;
+    float* o = dO + base * D;
+    if (g->kind == GK_PILE) {
+      pile_sensors_kernel<<<grid, 64, 0, st>>>(g->pile_dev(), dI + base, cnt, dS, n_sensors, o, D);
+    } else {
+      const TreeGroupDev td = g->tree_dev();
+      switch (newt_tree_bucket(td.L)) {
+        case 8: tree_sensors_kernel<8><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D); break;
+        case 16: tree_sensors_kernel<16><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D); break;
+        case 32: tree_sensors_kernel<32><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D); break;
+        default: tree_sensors_kernel<65><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D); break;
+      }
+    }
+    e = cudaGetLastError();
+    ctx->launches += 1;
+    order.insert(order.end(), rows[gi].begin(), rows[gi].end());
+    base += cnt;
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(host.data(), dO, sizeof(float) * host.size(), cudaMemcpyDeviceToHost, st);
+  if (dS) cudaFreeAsync(dS, st);
+  if (dI) cudaFreeAsync(dI, st);
+  if (dO) cudaFreeAsync(dO, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    ctx->err = std::string("read_sensors: ") + cudaGetErrorString(e);
+    return NEWT_E_CUDA;
+  }
+  for (size_t j = 0; j < order.size(); ++j)
+    std::copy(host.begin() + j * D, host.begin() + (j + 1) * D, out + (size_t)order[j] * D);
+  return NEWT_OK;
+}
