@@ -23,6 +23,7 @@ def eng():
 
 
 def _run(eng, model, ref, mode):
+    model.integrator = M.INTEGRATOR_EULER  # newt's matched rows step Euler (differential.rs:1272-1295)
     slots = eng.alloc(eng.upload(M.PackedModels([model])))
     eng.set_state(slots, ref["qpos"][0].astype(np.float32), ref["qvel"][0].astype(np.float32))
     worst_q = worst_v = 0.0

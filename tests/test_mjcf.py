@@ -94,6 +94,17 @@ def test_loaded_scenes_within_mujoco_windows(name, qtol, vtol):
     assert worst_q <= qtol and worst_v <= vtol, (worst_q, worst_v)
 
 
+def test_integrator_option_reaches_the_model():
+    """mjcf.rs:727-742: RK4 (also when no option is given) or Euler; the
+    GPU path has no implicitfast."""
+    base = '<mujoco><compiler angle="radian"/>{}<worldbody/></mujoco>'
+    assert load_mjcf(base.format("")).model.integrator == M.INTEGRATOR_RK4
+    assert load_mjcf(base.format('<option integrator="RK4"/>')).model.integrator == M.INTEGRATOR_RK4
+    assert load_mjcf(base.format('<option integrator="Euler"/>')).model.integrator == M.INTEGRATOR_EULER
+    with pytest.raises(MjcfUnsupported):
+        load_mjcf(base.format('<option integrator="implicitfast"/>'))
+
+
 def test_outside_the_subset_is_refused():
     with pytest.raises(MjcfUnsupported):
         load_mjcf('<mujoco><compiler angle="radian"/><worldbody><body name="b"><freejoint/>'

@@ -43,7 +43,7 @@ class MjcfScene:
     model: M.WorldModel
     qpos0: np.ndarray        # MuJoCo layout, from the body poses
     qvel0: np.ndarray
-    integrator: str = "RK4"  # MuJoCo's default; the GPU path steps Euler
+    integrator: str = "RK4"  # the XML's option (MuJoCo's default RK4); also set on `model`
     body_names: List[str] = field(default_factory=list)
     link_names: List[str] = field(default_factory=list)
 
@@ -125,7 +125,9 @@ class _Loader:
     def __init__(self, root: ET.Element):
         self.root = root
         self.defaults = _Defaults(root)
-        self.scene = MjcfScene(M.WorldModel(), np.zeros(0, np.float32), np.zeros(0, np.float32))
+        # World::new() steps RK4 unless <option integrator> says otherwise
+        self.scene = MjcfScene(M.WorldModel(integrator=M.INTEGRATOR_RK4), np.zeros(0, np.float32),
+                               np.zeros(0, np.float32))
         self.qpos: List[float] = []
         self.qvel: List[float] = []
         self.tree_qpos: List[float] = []
@@ -150,7 +152,14 @@ class _Loader:
         w.solver = M.SOLVER_PGS if solver == "PGS" else M.SOLVER_NEWTON
         if a.get("cone", "pyramidal") != "pyramidal":
             raise MjcfUnsupported("only the pyramidal cone is on the GPU path")
-        self.scene.integrator = a.get("integrator", "RK4")
+        # mjcf.rs:727-742; implicitfast is not on the GPU path
+        name = a.get("integrator", "RK4")
+        if name in ("RK4", "rk4"):
+            self.scene.integrator, w.integrator = "RK4", M.INTEGRATOR_RK4
+        elif name in ("Euler", "euler"):
+            self.scene.integrator, w.integrator = "Euler", M.INTEGRATOR_EULER
+        else:
+            raise MjcfUnsupported(f"option integrator={name!r}: RK4 or Euler on the GPU path")
 
     # -- geoms -----------------------------------------------------------------
     def geom(self, e: ET.Element, cls: str, body: int = -1, link: int = -1) -> M.Geom:
