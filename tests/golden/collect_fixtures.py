@@ -4,7 +4,8 @@ Runs only where the reference checkout is mounted (never on the GPU machine).
 The files are byte goldens written by newt's test suite (f32 little-endian
 state snapshots, newt/tests/goldens/*.bin) and MuJoCo 3.11.0 FP64 captures in
 newt's NEWTDIF1 format (newt/tests/references/*.bin), plus the scene files
-those captures were made from.  They are data, copied verbatim.
+those captures were made from and newt's packaged JSON models
+(newt/models/*.json).  They are data, copied verbatim.
 """
 import os
 import shutil
@@ -14,6 +15,10 @@ REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/newt/tests"
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 FILES = [
+    "../models/stack.json",
+    "../models/pendulum.json",
+    "../models/arm.json",
+    "../models/pile.json",
     "goldens/integrator_euler.bin",
     "goldens/integrator_rk4.bin",
     "goldens/dynamics_mass_bias.bin",
