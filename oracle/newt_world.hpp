@@ -9,7 +9,7 @@
 //   newt/src/contact.rs:269-470      sphere_plane, box_plane, capsule_plane, sphere_sphere
 //   newt/src/contact.rs:569-1247     box_box_full_manifold (SAT + face clipping)
 //   newt/src/contact.rs:473-505      sphere_capsule; :1249-1272 capsule_capsule
-//   newt/src/contact.rs:1296-1426    cylinder_plane, ellipsoid_plane
+//   newt/src/contact.rs:1296-1426    cylinder_plane, ellipsoid_plane; :1519-1628 sphere_cylinder
 //   newt/src/contact.rs:2313-2387    closest_point_on_segment, closest_points_on_segments
 //   newt/src/contact.rs:2509-2587    dispatch / swap rule
 //   newt/src/world.rs:1042-1069      auto_pairs (naive pair set; broadphase-independent contacts)
@@ -288,6 +288,36 @@ template <class R> CBuf<R> ellipsoid_plane(int ie, const Pose<R>& ep, Vec3<R> ax
   return out;
 }
 
+// contact.rs:1519-1628 sphere_cylinder: the closest point of the solid
+// cylinder to the sphere centre in the cylinder frame; a centre inside is
+// pushed out through the nearer of cap and side (cap on ties)
+template <class R> CBuf<R> sphere_cylinder(int is, const Pose<R>& sp, R rs, int ic, const Pose<R>& cp_, R rc, R hh, R fr, R margin, R gap) {
+  Vec3<R> pl = cp_.o.inverse_rotate(sp.p - cp_.p);
+  R z = pl.z;
+  Vec3<R> pr(pl.x, pl.y, R(0));
+  R dr = pr.length();
+  bool in_ax = rabs(z) <= hh, in_rad = dr <= rc, inside = false;
+  Vec3<R> cl;
+  if (in_ax && in_rad) {
+    inside = true;
+    if (hh - rabs(z) <= rc - dr) cl = Vec3<R>(pl.x, pl.y, (z >= R(0) ? R(1) : R(-1)) * hh);
+    else { Vec3<R> rd = dr > R(0) ? pr / dr : Vec3<R>(1, 0, 0); cl = Vec3<R>(rd.x * rc, rd.y * rc, z); }
+  } else {
+    R zc = z > hh ? hh : (z < -hh ? -hh : z);
+    Vec3<R> rd = dr > R(0) ? pr / dr : Vec3<R>(1, 0, 0);
+    R rcl = dr > rc ? rc : dr;
+    cl = Vec3<R>(rd.x * rcl, rd.y * rcl, zc);
+  }
+  Vec3<R> dl = pl - cl;
+  R dist = Sc<R>::sqrt(dl.length_squared());
+  R pen = (inside ? rs + dist : rs - dist) + margin;
+  CBuf<R> out;
+  if (pen <= R(0)) return out;
+  Vec3<R> nl = dist > R(1.0e-9) ? (inside ? -dl / dist : dl / dist) : Vec3<R>(0, 0, 1);
+  out.push({is, ic, cp_.p + cp_.o.rotate(cl), cp_.o.rotate(nl), pen, fr, gap});
+  return out;
+}
+
 // contact.rs:2313-2321 closest_point_on_segment
 template <class R> Vec3<R> closest_point_on_segment(Vec3<R> p, Vec3<R> a, Vec3<R> b) {
   Vec3<R> ab = b - a;
@@ -471,6 +501,10 @@ template <class R> bool try_np(int ia, const Geom<R>& a, const Pose<R>& pa, int 
   if (a.shape == S_CYLINDER && b.shape == S_PLANE) { *out = cylinder_plane(ia, pa, a.size[0], a.size[1], fr, margin, gap, ib, pb); return true; }
   if (a.shape == S_ELLIPSOID && b.shape == S_PLANE) {
     *out = ellipsoid_plane(ia, pa, Vec3<R>(a.size[0], a.size[1], a.size[2]), fr, margin, gap, ib, pb);
+    return true;
+  }
+  if (a.shape == S_SPHERE && b.shape == S_CYLINDER) {
+    *out = sphere_cylinder(ia, pa, a.size[0], ib, pb, b.size[0], b.size[1], fr, margin, gap);
     return true;
   }
   if (a.shape == S_SPHERE && b.shape == S_CAPSULE) {

@@ -131,12 +131,80 @@ def test_tree_with_cylinder_and_ellipsoid_links(eng, solver):
     assert np.abs(gq - oq).max() < 1e-3 and np.abs(gv - ov).max() < 1e-2
 
 
+def _sphere_cylinder_pile(seed, n=10):
+    """spheres and cylinders on a plane; cylinder pairs filtered (cylinder
+    geoms group 2 / mask 5, spheres group 1, plane group 4)."""
+    rng = np.random.default_rng(seed)
+    w = M.WorldModel(dt=2e-3, gravity=(0.0, 0.0, -9.81), solver=M.SOLVER_PGS, iterations=50)
+    plane = M.static_plane(friction=0.8)
+    plane.group, plane.mask = 4, 0xFF
+    w.add_geom(plane)
+    qpos = []
+    for k in range(n):
+        if k % 2 == 0:
+            r, h = rng.uniform(0.08, 0.2), rng.uniform(0.05, 0.2)
+            m = float(np.float32(1000.0 * np.pi * r * r * 2 * h))
+            b = w.add_body(m, M.solid_cylinder_inertia(m, r, h))
+            g = M.Geom(shape=M.SHAPE_CYLINDER, body=b, size=(r, h, 0.0), friction=0.7)
+            g.group, g.mask = 2, 5
+        else:
+            r = rng.uniform(0.05, 0.15)
+            m = float(np.float32(1000.0 * 4.0 / 3.0 * np.pi * r ** 3))
+            b = w.add_body(m, M.solid_sphere_inertia(m, r))
+            g = M.Geom(shape=M.SHAPE_SPHERE, body=b, size=(r, 0.0, 0.0), friction=0.7)
+            g.group, g.mask = 1, 0xFF
+        w.add_geom(g)
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        qpos += [float(rng.uniform(-0.5, 0.5)), float(rng.uniform(-0.5, 0.5)), float(0.3 + 0.35 * k)] + list(q)
+    return w, np.array(qpos, np.float32), np.zeros(6 * n, np.float32)
+
+
+def test_sphere_cylinder_pile_matches_oracle(eng):
+    """contact.rs:1519-1628 on the pile path: 300 oracle steps of spheres
+    falling onto cylinders, then contact lists and 20 GPU steps against the
+    oracle."""
+    worlds, qs, vs = [], [], []
+    for s in range(12):
+        w, q, v = _sphere_cylinder_pile(200 + s)
+        rq, rv = oracle_py.run(M.PackedModels([w]), np.zeros(1, np.int32), q, v, None, 300, precision=1)
+        worlds.append(w)
+        qs.append(rq.astype(np.float32))
+        vs.append(rv.astype(np.float32))
+    P, q, v = M.PackedModels(worlds), np.concatenate(qs), np.concatenate(vs)
+    slots = eng.alloc(eng.upload(P))
+    eng.set_state(slots, q, v)
+    eng.step(1, STEP_BATCHED)
+    eng.sync()
+    nq, nv, kinds = 70, 60, 0
+    for w in range(len(worlds)):
+        qp, qv = q[w * nq:(w + 1) * nq], v[w * nv:(w + 1) * nv]
+        rp, rd = oracle_py.contacts(P, w, qp, qv)
+        if len(rd) and (np.abs(rd[:, 6]) < MARGIN_BAND).any():
+            continue
+        gp, gd = eng.contacts(int(slots[w]))
+        assert gp.tolist() == rp.tolist(), f"world {w}"
+        if len(rd):
+            assert np.abs(gd[:, 0:7] - rd[:, 0:7]).max() < 1e-4
+        kinds += sum(1 for a, b in rp if {worlds[w].geoms[a].shape, worlds[w].geoms[b].shape}
+                     == {M.SHAPE_SPHERE, M.SHAPE_CYLINDER})
+    eng.free(slots)
+    assert kinds > 5
+    slots = eng.alloc(eng.upload(P))
+    eng.set_state(slots, q, v)
+    eng.step(20, STEP_BATCHED)
+    gq, gv = eng.get_state(slots, len(q), len(v))
+    eng.free(slots)
+    rq, rv = oracle_py.run(P, np.arange(len(worlds)), q, v, None, 20, precision=1)
+    assert np.abs(gq - rq).max() < 1e-3 and np.abs(gv - rv).max() < 1e-2
+
+
 def test_unfiltered_cylinder_body_pair_is_refused(eng):
     w = M.WorldModel(dt=2e-3, gravity=(0.0, 0.0, -9.81), solver=M.SOLVER_PGS, iterations=20)
     w.add_geom(M.static_plane())
     a = w.add_body(1.0, M._diag9(0.01, 0.01, 0.01))
     c = w.add_body(1.0, M._diag9(0.01, 0.01, 0.01))
-    w.add_geom(M.Geom(shape=M.SHAPE_SPHERE, body=a, size=(0.1, 0.0, 0.0)))
+    w.add_geom(M.Geom(shape=M.SHAPE_BOX, body=a, size=(0.1, 0.1, 0.1)))
     w.add_geom(M.Geom(shape=M.SHAPE_CYLINDER, body=c, size=(0.05, 0.1, 0.0)))
     with pytest.raises(NewtError):
         eng.upload(M.PackedModels([w]))

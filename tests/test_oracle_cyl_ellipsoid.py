@@ -108,3 +108,43 @@ def test_ellipsoid_depth_matches_surface_search():
         mid[2] *= 0.5
         assert np.abs(data[0, 0:3] - mid).max() < 2e-2 * a32.max()
     assert hits > 15
+
+
+def test_sphere_cylinder_matches_signed_distance():
+    """contact.rs:1519-1628 against the signed distance of the sphere centre
+    to the solid cylinder: outside, |(max(r_xy - R, 0), max(|z| - h, 0))|;
+    inside, -min(R - r_xy, h - |z|); penetration = r_s - signed distance."""
+    rng = np.random.default_rng(9)
+    hits = 0
+    for _ in range(400):
+        rs, rc, hh = rng.uniform(0.05, 0.2), rng.uniform(0.05, 0.3), rng.uniform(0.05, 0.3)
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        w = M.WorldModel(dt=2e-3, gravity=(0.0, 0.0, -9.81), solver=M.SOLVER_PGS, iterations=20)
+        a = w.add_body(1.0, M._diag9(0.01, 0.01, 0.01))
+        c = w.add_body(1.0, M._diag9(0.01, 0.01, 0.01))
+        w.add_geom(M.Geom(shape=M.SHAPE_SPHERE, body=a, size=(rs, 0.0, 0.0)))
+        w.add_geom(M.Geom(shape=M.SHAPE_CYLINDER, body=c, size=(rc, hh, 0.0)))
+        cc = rng.uniform(-0.3, 0.3, 3)
+        cs = cc + rng.uniform(-0.5, 0.5, 3)
+        qpos = np.concatenate([cs, [1.0, 0.0, 0.0, 0.0], cc, q]).astype(np.float32)
+        pairs, data = oracle_py.contacts(M.PackedModels([w]), 0, qpos, np.zeros(12, np.float32), precision=1)
+        Rm = _rotmat(qpos[10:14].astype(np.float64) / np.linalg.norm(qpos[10:14].astype(np.float64)))
+        pl = Rm.T @ (qpos[0:3].astype(np.float64) - qpos[7:10].astype(np.float64))
+        R32, h32, r32 = (float(np.float32(x)) for x in (rc, hh, rs))
+        rxy, az = np.hypot(pl[0], pl[1]), abs(pl[2])
+        if rxy <= R32 and az <= h32:
+            sd = -min(R32 - rxy, h32 - az)
+        else:
+            sd = np.hypot(max(rxy - R32, 0.0), max(az - h32, 0.0))
+        pen = r32 - sd
+        if abs(pen) < 1e-7:
+            continue
+        if pen < 0:
+            assert len(pairs) == 0
+            continue
+        hits += 1
+        assert len(pairs) == 1 and tuple(pairs[0]) == (0, 1)
+        assert abs(data[0, 6] - pen) < 1e-8, (data[0, 6], pen)
+        assert abs(np.linalg.norm(data[0, 3:6]) - 1.0) < 1e-9
+    assert hits > 60

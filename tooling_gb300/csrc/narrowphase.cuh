@@ -12,6 +12,7 @@
 //   sphere_capsule newt/src/contact.rs:473-505
 //   capsule_capsule newt/src/contact.rs:1249-1272
 //   cylinder_plane newt/src/contact.rs:1296-1373
+//   sphere_cylinder newt/src/contact.rs:1519-1628
 //   ellipsoid_plane newt/src/contact.rs:1381-1426
 //   sphere_box     extension (newt defers this pair, contact.rs:236-257):
 //                  closed-form closest point on the oriented box
@@ -211,6 +212,30 @@ NEWT_D int np_ellipsoid_plane(const GPose& e, V3 ax, float margin, const GPose& 
   const float pen = margin - sg;
   if (!(pen >= 0.f)) return 0;
   out[0] = CRes{sw - n * (sg * 0.5f), n, pen};
+  return 1;
+}
+
+// Sphere (A) vs cylinder (B): the closest point of the solid cylinder to the
+// sphere centre in the cylinder frame; a centre inside leaves through the
+// nearer of cap and side, the cap on ties (contact.rs:1519-1628).
+NEWT_D int np_sphere_cylinder(V3 cs, float rs, const GPose& c, float rc, float hh, float margin, CRes* out) {
+  const V3 pl = qrot_inv(c.q, cs - c.p);
+  const float z = pl.z, dr = sqrtf(pl.x * pl.x + pl.y * pl.y);
+  const bool inside = fabsf(z) <= hh && dr <= rc;
+  const float ux = dr > 0.f ? pl.x / dr : 1.f, uy = dr > 0.f ? pl.y / dr : 0.f;
+  V3 cl;
+  if (inside) {
+    cl = (hh - fabsf(z) <= rc - dr) ? v3(pl.x, pl.y, (z >= 0.f ? 1.f : -1.f) * hh) : v3(ux * rc, uy * rc, z);
+  } else {
+    const float zc = z > hh ? hh : (z < -hh ? -hh : z), rcl = dr > rc ? rc : dr;
+    cl = v3(ux * rcl, uy * rcl, zc);
+  }
+  const V3 dl = pl - cl;
+  const float dist = sqrtf(len2(dl));
+  const float pen = (inside ? rs + dist : rs - dist) + margin;
+  if (!(pen > 0.f)) return 0;
+  const V3 nl = dist > 1.0e-9f ? (inside ? dl * (-1.f / dist) : dl * (1.f / dist)) : v3(0.f, 0.f, 1.f);
+  out[0] = CRes{c.p + qrot(c.q, cl), qrot(c.q, nl), pen};
   return 1;
 }
 

@@ -283,6 +283,8 @@ NEWT_D void collide(const WsLay& L, float* wf, int* wi, int lane) {
       else if (sa == SH_CYLINDER && sb == SH_PLANE)
         cnt = np_cylinder_plane(pa, wf[L.size + 3 * ea], wf[L.size + 3 * ea + 1], margin, pb, res);
       else if (sa == SH_ELLIPSOID && sb == SH_PLANE) cnt = np_ellipsoid_plane(pa, ld3(wf + L.size + 3 * ea), margin, pb, res);
+      else if (sa == SH_SPHERE && sb == SH_CYLINDER)
+        cnt = np_sphere_cylinder(pa.p, wf[L.size + 3 * ea], pb, wf[L.size + 3 * eb], wf[L.size + 3 * eb + 1], margin, res);
       else if (sa == SH_SPHERE && sb == SH_CAPSULE)
         cnt = np_sphere_capsule(pa.p, wf[L.size + 3 * ea], pb, wf[L.size + 3 * eb], wf[L.size + 3 * eb + 1], margin, res);
       else if (sa == SH_CAPSULE && sb == SH_CAPSULE)
@@ -298,6 +300,8 @@ NEWT_D void collide(const WsLay& L, float* wf, int* wi, int lane) {
         else if (sb == SH_CYLINDER && sa == SH_PLANE)
           cnt = np_cylinder_plane(pb, wf[L.size + 3 * eb], wf[L.size + 3 * eb + 1], margin, pa, res);
         else if (sb == SH_ELLIPSOID && sa == SH_PLANE) cnt = np_ellipsoid_plane(pb, ld3(wf + L.size + 3 * eb), margin, pa, res);
+        else if (sb == SH_SPHERE && sa == SH_CYLINDER)
+          cnt = np_sphere_cylinder(pb.p, wf[L.size + 3 * eb], pa, wf[L.size + 3 * ea], wf[L.size + 3 * ea + 1], margin, res);
         else if (sb == SH_SPHERE && sa == SH_CAPSULE)
           cnt = np_sphere_capsule(pb.p, wf[L.size + 3 * eb], pa, wf[L.size + 3 * ea], wf[L.size + 3 * ea + 1], margin, res);
       }

@@ -112,14 +112,17 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
         if (A.body < 0 || B.body < 0) continue;
         const bool cb = (A.shape == NEWT_SHAPE_CAPSULE && B.shape == NEWT_SHAPE_BOX) ||
                         (A.shape == NEWT_SHAPE_BOX && B.shape == NEWT_SHAPE_CAPSULE);
-        const bool round = A.shape == NEWT_SHAPE_CYLINDER || A.shape == NEWT_SHAPE_ELLIPSOID ||
-                           B.shape == NEWT_SHAPE_CYLINDER || B.shape == NEWT_SHAPE_ELLIPSOID;
+        const bool sph_cyl = (A.shape == NEWT_SHAPE_SPHERE && B.shape == NEWT_SHAPE_CYLINDER) ||
+                             (A.shape == NEWT_SHAPE_CYLINDER && B.shape == NEWT_SHAPE_SPHERE);
+        const bool round = !sph_cyl && (A.shape == NEWT_SHAPE_CYLINDER || A.shape == NEWT_SHAPE_ELLIPSOID ||
+                                        B.shape == NEWT_SHAPE_CYLINDER || B.shape == NEWT_SHAPE_ELLIPSOID);
         if (!(cb || round) || !((A.group & B.mask) != 0u && (B.group & A.mask) != 0u)) continue;
         if (cb) return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "capsule-box pairs are not supported (newt/src/contact.rs:232-257)");
-        // cylinders and ellipsoids touch planes only here; newt's sphere-cylinder
-        // and sphere-ellipsoid routes (contact.rs:1519-1725) are not on the GPU path
+        // cylinders touch planes and spheres here, ellipsoids planes only; newt's
+        // sphere-ellipsoid route (contact.rs:1630-1725) is not on the GPU path
         return fail(ctx, NEWT_E_UNSUPPORTED_PAIR,
-                    "a cylinder or ellipsoid body may only collide with planes on the GPU path (filter its body pairs)");
+                    "cylinder bodies may collide with planes and spheres, ellipsoid bodies with planes only, on the GPU "
+                    "path (filter the other body pairs)");
       }
     for (int b = 0; b < d.n_bodies; ++b) {
       if (per_body[b] != 1) return fail(ctx, NEWT_E_INVALID, "GPU piles need exactly one geom per body");
