@@ -139,6 +139,27 @@ NEWT_D GPose geom_pose(const WsLay& L, const float* wf, int e) {
 // ---------------------------------------------------------------------------
 // collision: AABBs, sort-and-sweep pair marking, ordered pair list, narrowphase
 // ---------------------------------------------------------------------------
+// Pairs with a capsule, cylinder or ellipsoid (sizes `za`, `zb`: radius and
+// half height, or semi-axes), out of line so that the sphere/box pairs keep
+// the narrowphase loop's instruction footprint.  Tries (A, B), then (B, A)
+// with *flip set (the caller relabels, newt/src/contact.rs:2561-2586).
+__device__ __noinline__ int np_round_pair(int sa, int sb, GPose pa, GPose pb, const float* za, const float* zb,
+                                          float margin, CRes* res, bool* flip) {
+  if (sa == SH_CAPSULE && sb == SH_PLANE) return np_capsule_plane(pa, za[0], za[1], margin, pb, res);
+  if (sa == SH_CYLINDER && sb == SH_PLANE) return np_cylinder_plane(pa, za[0], za[1], margin, pb, res);
+  if (sa == SH_ELLIPSOID && sb == SH_PLANE) return np_ellipsoid_plane(pa, v3(za[0], za[1], za[2]), margin, pb, res);
+  if (sa == SH_SPHERE && sb == SH_CYLINDER) return np_sphere_cylinder(pa.p, za[0], pb, zb[0], zb[1], margin, res);
+  if (sa == SH_SPHERE && sb == SH_CAPSULE) return np_sphere_capsule(pa.p, za[0], pb, zb[0], zb[1], margin, res);
+  if (sa == SH_CAPSULE && sb == SH_CAPSULE) return np_capsule_capsule(pa, za[0], za[1], pb, zb[0], zb[1], margin, res);
+  *flip = true;
+  if (sb == SH_CAPSULE && sa == SH_PLANE) return np_capsule_plane(pb, zb[0], zb[1], margin, pa, res);
+  if (sb == SH_CYLINDER && sa == SH_PLANE) return np_cylinder_plane(pb, zb[0], zb[1], margin, pa, res);
+  if (sb == SH_ELLIPSOID && sa == SH_PLANE) return np_ellipsoid_plane(pb, v3(zb[0], zb[1], zb[2]), margin, pa, res);
+  if (sb == SH_SPHERE && sa == SH_CYLINDER) return np_sphere_cylinder(pb.p, zb[0], pa, za[0], za[1], margin, res);
+  if (sb == SH_SPHERE && sa == SH_CAPSULE) return np_sphere_capsule(pb.p, zb[0], pa, za[0], za[1], margin, res);
+  return 0;
+}
+
 NEWT_D void collide(const WsLay& L, float* wf, int* wi, int lane) {
   const int ng = L.ng, nb = L.nb, W = L.words;
   // AABBs per geom index (newt/src/broadphase.rs:708-756); planes unbounded
@@ -273,37 +294,18 @@ NEWT_D void collide(const WsLay& L, float* wf, int* wi, int lane) {
       float margin = fmaxf(wf[L.margin + ea], wf[L.margin + eb]);
       GPose pa = geom_pose(L, wf, ea), pb = geom_pose(L, wf, eb);
       // try (A, B); otherwise (B, A) and relabel (newt/src/contact.rs:2561-2586)
-      if (sa == SH_SPHERE && sb == SH_PLANE) cnt = np_sphere_plane(pa, wf[L.size + 3 * ea], margin, pb, res);
+      if (sa >= SH_CAPSULE || sb >= SH_CAPSULE) {
+        cnt = np_round_pair(sa, sb, pa, pb, wf + L.size + 3 * ea, wf + L.size + 3 * eb, margin, res, &flip);
+      } else if (sa == SH_SPHERE && sb == SH_PLANE) cnt = np_sphere_plane(pa, wf[L.size + 3 * ea], margin, pb, res);
       else if (sa == SH_BOX && sb == SH_PLANE) cnt = np_box_plane(pa, ld3(wf + L.size + 3 * ea), margin, pb, res);
       else if (sa == SH_SPHERE && sb == SH_SPHERE) cnt = np_sphere_sphere(pa.p, wf[L.size + 3 * ea], pb.p, wf[L.size + 3 * eb], margin, res);
       else if (sa == SH_BOX && sb == SH_BOX) cnt = np_box_box(pa, ld3(wf + L.size + 3 * ea), pb, ld3(wf + L.size + 3 * eb), margin, res);
       else if (sa == SH_SPHERE && sb == SH_BOX) cnt = np_sphere_box(pa, wf[L.size + 3 * ea], pb, ld3(wf + L.size + 3 * eb), margin, res);
-      else if (sa == SH_CAPSULE && sb == SH_PLANE)
-        cnt = np_capsule_plane(pa, wf[L.size + 3 * ea], wf[L.size + 3 * ea + 1], margin, pb, res);
-      else if (sa == SH_CYLINDER && sb == SH_PLANE)
-        cnt = np_cylinder_plane(pa, wf[L.size + 3 * ea], wf[L.size + 3 * ea + 1], margin, pb, res);
-      else if (sa == SH_ELLIPSOID && sb == SH_PLANE) cnt = np_ellipsoid_plane(pa, ld3(wf + L.size + 3 * ea), margin, pb, res);
-      else if (sa == SH_SPHERE && sb == SH_CYLINDER)
-        cnt = np_sphere_cylinder(pa.p, wf[L.size + 3 * ea], pb, wf[L.size + 3 * eb], wf[L.size + 3 * eb + 1], margin, res);
-      else if (sa == SH_SPHERE && sb == SH_CAPSULE)
-        cnt = np_sphere_capsule(pa.p, wf[L.size + 3 * ea], pb, wf[L.size + 3 * eb], wf[L.size + 3 * eb + 1], margin, res);
-      else if (sa == SH_CAPSULE && sb == SH_CAPSULE)
-        cnt = np_capsule_capsule(pa, wf[L.size + 3 * ea], wf[L.size + 3 * ea + 1], pb, wf[L.size + 3 * eb],
-                                 wf[L.size + 3 * eb + 1], margin, res);
       else {
         flip = true;
         if (sb == SH_SPHERE && sa == SH_PLANE) cnt = np_sphere_plane(pb, wf[L.size + 3 * eb], margin, pa, res);
         else if (sb == SH_BOX && sa == SH_PLANE) cnt = np_box_plane(pb, ld3(wf + L.size + 3 * eb), margin, pa, res);
         else if (sb == SH_SPHERE && sa == SH_BOX) cnt = np_sphere_box(pb, wf[L.size + 3 * eb], pa, ld3(wf + L.size + 3 * ea), margin, res);
-        else if (sb == SH_CAPSULE && sa == SH_PLANE)
-          cnt = np_capsule_plane(pb, wf[L.size + 3 * eb], wf[L.size + 3 * eb + 1], margin, pa, res);
-        else if (sb == SH_CYLINDER && sa == SH_PLANE)
-          cnt = np_cylinder_plane(pb, wf[L.size + 3 * eb], wf[L.size + 3 * eb + 1], margin, pa, res);
-        else if (sb == SH_ELLIPSOID && sa == SH_PLANE) cnt = np_ellipsoid_plane(pb, ld3(wf + L.size + 3 * eb), margin, pa, res);
-        else if (sb == SH_SPHERE && sa == SH_CYLINDER)
-          cnt = np_sphere_cylinder(pb.p, wf[L.size + 3 * eb], pa, wf[L.size + 3 * ea], wf[L.size + 3 * ea + 1], margin, res);
-        else if (sb == SH_SPHERE && sa == SH_CAPSULE)
-          cnt = np_sphere_capsule(pb.p, wf[L.size + 3 * eb], pa, wf[L.size + 3 * ea], wf[L.size + 3 * ea + 1], margin, res);
       }
     }
     int incl = cnt;
