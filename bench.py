@@ -5,8 +5,14 @@ Workload (the metric's headline configuration): 8192 independent worlds, each
 friction, PGS 50 iterations, dt = 2e-3 -- seeded synthetic worlds.
 
 A bench step advances every world by `--substeps` env-steps with one call of
-the C ABI's batched step (one CUDA-graph replay: per env-step and world-range
-branch, collide, the island-class solvers on forked streams, integrate).
+the C ABI's batched step (one CUDA-graph replay of one world-persistent
+launch: a warp per world runs collide, PGS and integration for every
+env-step of the call, worlds pulled from a queue).  The same line carries the
+plain form (one launch per stage per env-step) on the same worlds and horizon,
+the one-step error against the FP64 oracle on a sample of the timed region's
+start state, and two compact runs of the other metric configurations: the
+uneven batch (batched vs plain, finite worlds counted apart) and a served
+Poisson stream (p50/p99 latency).
 Other workloads: --workload quadruped (16384 quadrupeds, Newton), uneven
 (32768 chains and piles of 2..64 bodies, batched vs plain), serve (Poisson
 request streams through the served-rollout loop).  Timing:
@@ -26,6 +32,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -35,6 +42,17 @@ sys.path.insert(0, ROOT)
 
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
+# FP32 pipe peak of a GB300 derived from its datasheet figures: 152 SMs x 128
+# FP32 lanes x 2 FLOP per fused multiply-add x 2.07 GHz maximum SM clock
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+# newt's PGS work per active contact and sweep (5 row updates x ~235 FLOP,
+# newt/src/solver.rs:1448-1518 with the residuals of :1980 and the impulse
+# application of :2022)
+PGS_FLOP_PER_CONTACT_SWEEP = 5 * 235
+# DRAM bytes (read + write) per world and env-step of pile_k_fused, from the
+# ncu capture summarised in profiles/pile_k_fused_2048worlds_full.md (2048
+# worlds, one launch of 25 env-steps), scaled by worlds x env-steps
+FUSED_DRAM_BYTES_PER_WORLD_STEP = None
 
 
 def parse():
@@ -46,7 +64,9 @@ def parse():
     ap.add_argument("--worlds", type=int, default=8192)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
-    ap.add_argument("--plain", action="store_true", help="also time the plain (per-stage launch) form")
+    ap.add_argument("--no-plain", action="store_true", help="skip timing the plain (per-stage launch) form")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="headline only: skip the FP64 error sample and the uneven / served sub-runs")
     ap.add_argument("--rates", default="1000,5000,10000,20000,50000",
                     help="serve workload: Poisson request rates (req/s), one timed run each")
     ap.add_argument("--duration", type=float, default=1.5, help="serve workload: seconds of arrivals per rate")
@@ -96,10 +116,10 @@ class Clocks:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        fd, self.path = tempfile.mkstemp(prefix="newt_clocks_", suffix=".csv")
+        os.close(fd)
 
     def start(self):
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -118,7 +138,10 @@ class Clocks:
         self.proc.wait(timeout=10)
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        with open(self.path) as f:
+            lines = f.readlines()
+        os.unlink(self.path)
+        for line in lines:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -159,18 +182,67 @@ def pile_kernel_bytes(kernel: str, n_worlds: int, nb: int, work: dict) -> float:
     return 4.0 * (int(contacts[c]) * (ROW_WORDS + 4) + int(bodies[c]) * 6)
 
 
+def fused_kernel_bytes(n_worlds: int, nb: int, contacts_last_step: float) -> float:
+    """Algorithmic HBM bytes of one pile_k_fused launch: every world record
+    read once (per body: position, velocity, angular velocity, size, geom
+    offset 3 each; orientation, geom orientation 4 each; inverse and body
+    inertia 6 each; mass, shape; per geom friction, margin, filter; plane 7,
+    soft parameters 7, dt and gravity 4), the 13 state words per body written
+    once, and the last env-step's contacts (pair 2, point, normal, depth 7,
+    impulses 4) written once.  The per-env-step solver records live in the
+    world's scratch and are not algorithmic traffic."""
+    rec = nb * 37 + 7 + 3 * (nb + 1) + 7 + 4
+    return 4.0 * (n_worlds * (rec + 13 * nb) + contacts_last_step * 13)
+
+
+def fp64_one_step_error(eng, batch, slots, start_qpos, start_qvel, n_sample=64):
+    """One env-step from the timed region's start state: the GPU's velocity
+    change against the FP64 oracle's on a spread sample of worlds, as the
+    relative error of the generalised acceleration (qacc = dv / dt) per world,
+    max-norm over the world's DoF."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+    from tooling_gb300 import STEP_BATCHED
+    W = len(batch)
+    idx = np.unique(np.linspace(0, W - 1, min(n_sample, W)).astype(np.int64))
+    eng.set_state(slots, start_qpos, start_qvel)
+    eng.step(1, STEP_BATCHED)
+    q1, v1 = eng.get_state(slots, int(batch.nq.sum()), int(batch.nv.sum()))
+    qp = np.concatenate([start_qpos[batch.q_off[w]:batch.q_off[w] + batch.nq[w]] for w in idx])
+    qv = np.concatenate([start_qvel[batch.v_off[w]:batch.v_off[w] + batch.nv[w]] for w in idx])
+    rq, rv = oracle_py.run(batch, idx, qp, qv, None, 1, precision=1, n_threads=os.cpu_count() or 1)
+    rel, dq = [], []
+    vo = 0
+    qo = 0
+    for w in idx:
+        nv, nq = int(batch.nv[w]), int(batch.nq[w])
+        v0 = start_qvel[batch.v_off[w]:batch.v_off[w] + nv].astype(np.float64)
+        dg = v1[batch.v_off[w]:batch.v_off[w] + nv] - v0
+        dr = rv[vo:vo + nv] - v0
+        rel.append(float(np.abs(dg - dr).max() / max(np.abs(dr).max(), 1e-30)))
+        dq.append(float(np.abs(q1[batch.q_off[w]:batch.q_off[w] + nq] - rq[qo:qo + nq]).max()))
+        vo += nv
+        qo += nq
+    rel = np.array(rel)
+    return {"worlds": int(len(idx)), "qacc_rel_max": float(rel.max()), "qacc_rel_median": float(np.median(rel)),
+            "worlds_within_1e-4": int((rel <= 1e-4).sum()), "qpos_abs_max": float(max(dq)),
+            "what": "one env-step from the timed region's start state; qacc = dv/dt per world, max-norm relative "
+                    "error against the FP64 oracle (oracle/, newt's step in double)"}
+
+
 def run_gpu(args, rank, ws, local, dist):
     from tooling_gb300 import build as B
     B.build()
     from tooling_gb300 import Engine, STEP_BATCHED, STEP_PLAIN, scenes
-    eng = Engine(device=local)
     W = args.worlds
     batch = scenes.pile_batch(n_worlds=W, first_world=rank * W)
+    eng = Engine(device=local)
     ids = eng.upload(batch)
     slots = eng.alloc(ids)
     eng.set_state(slots, batch.qpos, batch.qvel)
     S = args.substeps
-    # per-kernel timing events ride in the captured graph (on each kernel's stream)
+    nq_t, nv_t = int(batch.nq.sum()), int(batch.nv.sum())
+    # the persistent launch's timing events ride in the captured graph
     eng.pile_profile(1)
     # warm-up (also captures the CUDA graph), then the launch-choice autotuner
     # (it leaves the worlds' state as it found it)
@@ -178,14 +250,13 @@ def run_gpu(args, rank, ws, local, dist):
         eng.step(S, STEP_BATCHED)
     tuned = eng.autotune(S)
     eng.sync()
-    start_qpos, start_qvel = eng.get_state(slots, int(batch.nq.sum()), int(batch.nv.sum()))
+    start_qpos, start_qvel = eng.get_state(slots, nq_t, nv_t)
     launches0 = eng.launch_count()
     clocks = Clocks(local)
     clocks.start()
-    per_step = []
-    kernel_ms = {}
-    work = None
-    n_launch = 0  # launches of each pile kernel in the timed region
+    per_step, fused_ms, kernel_ms = [], 0.0, {}
+    fwork = {"contacts": 0, "rounds": 0, "levels": 0, "worlds": 0}
+    n_launch = 0
     barrier(dist)
     eng.sync()
     for _ in range(args.steps):
@@ -194,6 +265,10 @@ def run_gpu(args, rank, ws, local, dist):
         eng.step(S, STEP_BATCHED)
         eng.event(1)
         per_step.append(eng.elapsed_ms())
+        ms, fw = eng.fused_profile()
+        fused_ms += ms
+        for k in fwork:
+            fwork[k] += fw[k]
         kms, work = eng.pile_profile()
         n_launch += work["launches"]
         for k, v in kms.items():
@@ -216,12 +291,12 @@ def run_gpu(args, rank, ws, local, dist):
     for _ in range(args.steps):
         eng.set_state(slots, qp, qv)
         eng.step(S, STEP_BATCHED)
-        qp, qv = eng.get_state(slots, int(batch.nq.sum()), int(batch.nv.sum()))
+        qp, qv = eng.get_state(slots, nq_t, nv_t)
     eng.sync()
     e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
     e2e = env_steps / e2e_s
     plain = None
-    if args.plain:
+    if not args.no_plain:
         # the same timed horizon from the same start state, plain form
         eng.set_state(slots, start_qpos, start_qvel)
         eng.step(1, STEP_PLAIN)
@@ -234,43 +309,158 @@ def run_gpu(args, rank, ws, local, dist):
             eng.step(S, STEP_PLAIN)
             eng.event(1)
             pms += eng.elapsed_ms()
-        plain = W * S * args.steps / (pms / 1e3)
+        plain = W * S * args.steps / (max_over_ranks(dist, pms) / 1e3)
+    err = None
+    if not args.no_extras and rank == 0:
+        err = fp64_one_step_error(eng, batch, slots, start_qpos, start_qvel)
     hbm, src = peaks()
     avg_ms = total_ms / args.steps
-    branches = n_launch / (args.steps * S)  # world-range branches per env-step
-    dom = max(kernel_ms, key=kernel_ms.get)
-    dom_ms = kernel_ms[dom] / n_launch
-    alg = pile_kernel_bytes(dom, W, int(batch.n_bodies[0]), work) / branches
-    achieved = alg / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else None
-    tot_k = sum(kernel_ms.values())
-    kernels = {k: {"ms_per_launch": v / n_launch, "share": v / tot_k if tot_k else None,
-                   "algorithmic_bytes": pile_kernel_bytes(k, W, int(batch.n_bodies[0]), work) / branches}
-               for k, v in kernel_ms.items()}
+    nb = int(batch.n_bodies[0])
+    persistent = fwork["worlds"] > 0
+    if persistent:
+        # the world-persistent kernel: FP32 work of newt's PGS over the
+        # contacts it solved, per launch, against the FP32 pipe's peak
+        dom, dom_ms = "pile_k_fused", fused_ms / args.steps
+        flops = PGS_FLOP_PER_CONTACT_SWEEP * 50 * fwork["contacts"] / args.steps
+        achieved = flops / (dom_ms / 1e3) / 1e12 if dom_ms > 0 else None
+        contacts_last = fwork["contacts"] / (args.steps * S)
+        alg = fused_kernel_bytes(W, nb, contacts_last)
+        hbm_ach = alg / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else None
+        traffic = (FUSED_DRAM_BYTES_PER_WORLD_STEP * W * S) if FUSED_DRAM_BYTES_PER_WORLD_STEP else None
+        roof = {"bound": "fp32", "kernel": dom, "achieved": achieved, "peak": FP32_PEAK_TFLOPS, "unit": "TFLOP/s",
+                "frac": achieved / FP32_PEAK_TFLOPS if achieved else None, "traffic": traffic,
+                "peak_source": "derived from datasheet figures (152 SMs x 128 FP32 lanes x 2 x 2.07 GHz); "
+                               "MEASURED_PEAKS.json has no FP32 figure",
+                "flop_per_launch": flops, "flop_formula": "5 x 235 FLOP x 50 sweeps per active contact and env-step "
+                                                          "(newt's PGS row updates), contacts counted by the kernel",
+                "ms_per_launch": dom_ms, "active_contacts_per_world_step": fwork["contacts"] / (W * S * args.steps),
+                "dependency_rounds_per_world_sweep": fwork["rounds"] / (50.0 * W * S * args.steps),
+                "hbm": {"achieved": hbm_ach, "peak": hbm, "unit": "GB/s", "frac": hbm_ach / hbm if hbm_ach else None,
+                        "peak_source": src, "algorithmic_bytes_per_launch": alg},
+                "note": "one launch per bench step (all worlds, all env-steps), timed live by an event pair on its "
+                        "stream inside the graph"}
+        kernels = {"pile_k_fused": {"ms_per_launch": dom_ms, "share": 1.0, "algorithmic_bytes": alg}}
+        mode = ("batched: one world-persistent launch per bench step (a warp per world for all its env-steps, "
+                "worlds from a size-sorted queue), CUDA graph")
+    else:
+        branches = n_launch / (args.steps * S)
+        dom = max(kernel_ms, key=kernel_ms.get)
+        dom_ms = kernel_ms[dom] / n_launch
+        alg = pile_kernel_bytes(dom, W, nb, work) / branches
+        achieved = alg / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else None
+        roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm if achieved else None, "traffic": None, "peak_source": src,
+                "algorithmic_bytes_per_launch": alg, "ms_per_launch": dom_ms}
+        tot_k = sum(kernel_ms.values())
+        kernels = {k: {"ms_per_launch": v / n_launch, "share": v / tot_k if tot_k else None,
+                       "algorithmic_bytes": pile_kernel_bytes(k, W, nb, work) / branches}
+                   for k, v in kernel_ms.items()}
+        mode = "batched: island-class pipeline, per env-step and world-range branch, CUDA graph"
     out = {
         "metric": "env-steps/s", "value": value, "unit": "env-steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": avg_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
         "config": {"workload": "pile: 16 free spheres/boxes on a plane per world, PGS 50 iterations, dt 2e-3",
                    "worlds_per_gpu": W, "bodies_per_world": 16, "env_steps_per_bench_step": S,
-                   "mode": "batched: 9 kernels per env-step and world-range branch, branches and island classes "
-                           "on forked streams, CUDA graph", "autotuned": tuned,
+                   "mode": mode, "autotuned": tuned,
                    "l2": "flushed between timed steps", "parallelism": f"replicas x{ws}"},
         "e2e": {"value": e2e, "unit": "env-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clk,
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm if achieved else None, "traffic": None, "peak_source": src,
-                     "algorithmic_bytes_per_launch": alg, "ms_per_launch": dom_ms,
-                     "note": "dependent Gauss-Seidel chains (latency-bound); timed live by event pairs "
-                             "on the kernel's stream inside the graph"},
+        "roofline": roof,
         "kernels": kernels,
         "status_flags": int(np.bitwise_or.reduce(st)) if len(st) else 0,
     }
     if plain is not None:
         out["plain_value"] = plain
         out["batched_over_plain"] = value / ws / plain
+    if err is not None:
+        out["error_vs_fp64"] = err
     eng.close()
     return out, (batch, start_qpos, start_qvel)
+
+
+def run_uneven_compact(rank, ws, local, dist, n_worlds=32768, substeps=25, steps=8):
+    """The uneven configuration in brief for the headline line: 32768 chains
+    and piles of 2..64 bodies, env-steps 0..200 from the start state, the
+    batched form (autotuned) against the plain form on the same worlds,
+    throughput over all worlds and over the worlds that stayed finite."""
+    from tooling_gb300 import scenes
+    batch = scenes.uneven_batch(n_worlds=n_worlds, first_world=rank * n_worlds)
+    from tooling_gb300 import Engine, STEP_BATCHED, STEP_PLAIN
+    eng = Engine(device=local)
+    slots = eng.alloc(eng.upload(batch))
+    nq, nv = int(batch.nq.sum()), int(batch.nv.sum())
+
+    def reset():
+        eng.set_state(slots, batch.qpos, batch.qvel)
+        eng.set_qfrc(slots, batch.qfrc)
+        eng.status(slots, clear=True)
+
+    reset()
+    eng.step(substeps, STEP_BATCHED)
+    tuned = eng.autotune(substeps)
+    out = {"worlds": n_worlds, "env_steps": substeps * steps, "autotuned": tuned}
+    for name, mode in (("batched", STEP_BATCHED), ("plain", STEP_PLAIN)):
+        reset()
+        eng.step(1, mode)  # captures / builds tables outside the timing
+        reset()
+        eng.sync()
+        barrier(dist)
+        ms = 0.0
+        for _ in range(steps):
+            eng.flush_l2()
+            eng.event(0)
+            eng.step(substeps, mode)
+            eng.event(1)
+            ms += eng.elapsed_ms()
+        ms = max_over_ranks(dist, ms)
+        st = eng.status(slots)
+        finite = int(((st & 0x1) == 0).sum())
+        out[name] = {"value": n_worlds * substeps * steps * ws / (ms / 1e3),
+                     "finite_value": finite * substeps * steps * ws / (ms / 1e3),
+                     "finite_worlds": finite, "status_flags": int(np.bitwise_or.reduce(st)), "ms": ms}
+    out["batched_over_plain"] = out["batched"]["value"] / out["plain"]["value"]
+    out["note"] = ("worlds flagged NEWT_WS_NONFINITE are long chains that newt's own algorithm also blows up on "
+                   "at dt 2e-3 (the FP64 oracle diverges on the same worlds); finite_value counts the others only")
+    eng.close()
+    return out
+
+
+def run_served_compact(rank, ws, local, dist, rate=10000.0, duration=1.0, pool_worlds=4096):
+    """The served configuration in brief: one Poisson stream at `rate` req/s
+    over a pool of uneven worlds, horizons log-uniform in 10..1000, tau ~
+    N(0,1) per DoF per env-step, through newt_gpu_serve; p50/p99 latency."""
+    from tooling_gb300 import scenes
+    pool = scenes.uneven_batch(n_worlds=pool_worlds, first_world=rank * pool_worlds)
+    from tooling_gb300 import Engine
+    eng = Engine(device=local)
+    ids = eng.upload(pool)
+    nv = pool.nv.astype(np.int64)
+    rng = np.random.default_rng(scenes.config_seed(4) + rank)
+    tau = rng.standard_normal(1 << 22).astype(np.float32)
+
+    def one(d):
+        arrivals, world, hz, coff = serve_requests(rng, len(pool), nv, rate, d, tau)
+        qp = np.concatenate([pool.qpos[pool.q_off[w]:pool.q_off[w] + pool.nq[w]] for w in world])
+        qv = np.concatenate([pool.qvel[pool.v_off[w]:pool.v_off[w] + pool.nv[w]] for w in world])
+        oq, ov, st, _, _ = eng.serve(ids[world], hz, arrivals, qp, qv, tau, coff)
+        qo = np.concatenate([[0], np.cumsum(pool.nq[world])])
+        bad = np.add.reduceat((~np.isfinite(oq)).astype(np.int64), qo[:-1]) if len(world) else np.zeros(0)
+        st["requests"] = len(world)
+        st["nonfinite_requests"] = int((bad > 0).sum())
+        return st
+
+    one(0.2)  # warm-up: groups grown, graph captured
+    barrier(dist)
+    st = one(duration)
+    keep = ["requests", "completed", "p50_ms", "p99_ms", "max_ms", "mean_active", "ticks", "wall_s",
+            "nonfinite_requests"]
+    out = {k: st[k] for k in keep}
+    out["rate_req_per_s"] = rate
+    out["env_steps_per_s"] = st["env_steps"] / st["wall_s"] if st["wall_s"] > 0 else 0.0
+    eng.close()
+    return out
 
 
 def tc_kernel_bytes(kernel: str, n_worlds: int, batch, contacts_per_world: float) -> float:
@@ -570,7 +760,7 @@ def run_gpu_serve(args, rank, ws, local, dist):
     clk = clk_runs[-1]
     clk["reasons"] = sorted(set(x for c in clk_runs for x in c.get("reasons", [])))
     top = runs[-1]
-    plain = serve(top["rate"], args.duration, STEP_PLAIN) if args.plain else None
+    plain = serve(top["rate"], args.duration, STEP_PLAIN) if not args.no_plain else None
     ticks = max(1, top["ticks"])
     value = max_over_ranks(dist, 1.0 / top["env_steps_per_s"]) if top["env_steps_per_s"] > 0 else 0.0
     value = ws / value if value > 0 else 0.0
@@ -727,6 +917,9 @@ def main():
             print(json.dumps(out))
         return
     out, (batch, qp, qv) = run_gpu(args, rank, ws, local, dist)
+    if not args.no_extras:
+        out["uneven"] = run_uneven_compact(rank, ws, local, dist)
+        out["served"] = run_served_compact(rank, ws, local, dist)
     if rank == 0:
         if not args.no_cpu and ws == 1:
             out["cpu_baseline"] = cpu_baseline(batch, qp, qv, args.substeps, steps=args.substeps * args.steps)

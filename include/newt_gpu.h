@@ -137,6 +137,11 @@ typedef struct newt_gpu_opts {
   int32_t device;                    /* CUDA device ordinal */
   int32_t max_worlds;                /* slot capacity */
   uint64_t hbm_budget_bytes;         /* 0 = free HBM at creation minus a reserve */
+  int32_t max_contacts;              /* pile worlds: contacts kept per world (0 = sized from the body
+                                      * count, 6 nb + 4 nb np, 64..512); raised to at least 64 and
+                                      * 2 nb.  Contacts past it are dropped in pair order and the
+                                      * world's status gets NEWT_WS_CONTACT_OVERFLOW (newt's contact
+                                      * list grows without bound, world.rs:2476-2515) */
 } newt_gpu_opts;
 
 /* Replaces building a `World` (newt/src/world.rs:325). */
@@ -170,9 +175,13 @@ NEWT_API int newt_gpu_set_qfrc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t 
  * mode NEWT_STEP_PLAIN: one launch per stage per step, fixed tiles.
  * mode NEWT_STEP_BATCHED: the whole call captured in one CUDA graph and
  *   replayed: trees run the horizon in one persistent launch per size bucket
- *   over a cost-sorted queue; pile worlds of every size share one table per
- *   world-range branch (collide, island-class solvers on forked streams,
- *   integrate per env-step); tree-contact worlds follow per env-step. */
+ *   over a cost-sorted queue; pile worlds of every size run theirs in one
+ *   world-persistent launch (a warp per world for the whole horizon, worlds
+ *   pulled from a queue sorted by size, largest first); tree-contact worlds
+ *   run their three kernels per env-step on a third branch of the graph.
+ *   newt_gpu_autotune may instead pick the island-class pipeline for piles
+ *   (collide, island-class solvers on forked streams, integrate, per
+ *   env-step). */
 #define NEWT_STEP_PLAIN 0
 #define NEWT_STEP_BATCHED 1
 NEWT_API int newt_gpu_step(newt_gpu_ctx* ctx, int32_t n_steps, int32_t mode);
@@ -255,13 +264,23 @@ NEWT_API int newt_gpu_event_elapsed_ms(newt_gpu_ctx* ctx, float* ms);
 NEWT_API int newt_gpu_flush_l2(newt_gpu_ctx* ctx);                              /* writes a buffer > L2 */
 /* Kernel launches issued by this context since creation. */
 NEWT_API int64_t newt_gpu_launch_count(const newt_gpu_ctx* ctx);
-/* Times the batched step's launch choices on the live worlds (world-range
- * branches of the pile step: 1, 2 or 3; tree persistent grid at full or half
- * residency), `n_steps` env-steps per trial from one snapshot of every
- * world, keeps the fastest for later NEWT_STEP_BATCHED calls and leaves every
- * world's state as it was.  `choice` (nullable, 3 ints): branches, tree grid
- * percent, and the winner's time in microseconds.  No counterpart in newt. */
+/* Times the batched step's launch choices on the live worlds (piles in the
+ * world-persistent launch at 100, 75 or 50% of full residency, or the
+ * island-class pipeline with 1, 2 or 3 world-range branches; tree persistent
+ * grid at full or half residency), `n_steps` env-steps per trial from two
+ * snapshots of every world (as they are, and 8 x n_steps env-steps later,
+ * once falling piles have settled), keeps the fastest summed over both for
+ * later NEWT_STEP_BATCHED calls and leaves every world's state as it was.
+ * `choice` (nullable, 5 ints): pile branches (0 for the persistent launch),
+ * tree grid percent, the winner's summed time in microseconds, 1 if piles
+ * use the persistent launch, its grid percent.  No counterpart in newt. */
 NEWT_API int newt_gpu_autotune(newt_gpu_ctx* ctx, int32_t n_steps, int32_t* choice);
+/* Sets the batched step's launch choices directly, in newt_gpu_autotune's
+ * `choice` layout: [0] pile world-range branches of the island-class
+ * pipeline (0: by world count), [1] tree persistent grid percent, [2]
+ * ignored, [3] 1 for the world-persistent pile launch, 0 for the pipeline,
+ * [4] its grid percent.  No counterpart in newt. */
+NEWT_API int newt_gpu_set_launch_choice(newt_gpu_ctx* ctx, const int32_t* choice);
 /* Device bytes the world groups hold (capacity x bytes per world: model,
  * state, contact and solver buffers) and the admission budget they are
  * checked against. */
@@ -343,6 +362,16 @@ NEWT_API int newt_gpu_serve(newt_gpu_ctx* ctx, newt_serve_request* reqs, int32_t
 #define NEWT_PILE_ISLAND_CLASSES 7
 NEWT_API int newt_gpu_pile_profile(newt_gpu_ctx* ctx, int32_t enable, float* kernel_ms, int32_t* work,
                                    int32_t* launches);
+
+/* Profiling surface of the world-persistent pile launch (no counterpart in
+ * newt).  After waiting for the last newt_gpu_step call: `kernel_ms` (nullable)
+ * its device time, when timing is on (newt_gpu_pile_profile's `enable`) and
+ * that call was batched with piles in the persistent launch, else 0; `work`
+ * (nullable, 4 counters, zero unless that call ran the launch): active
+ * contacts summed over every world's env-steps, contact-update rounds (a
+ * dependency level's groups of eight contacts) summed over the sweeps,
+ * dependency levels summed over env-steps, worlds stepped. */
+NEWT_API int newt_gpu_pile_fused_profile(newt_gpu_ctx* ctx, float* kernel_ms, uint64_t* work);
 
 /* Profiling surface of the tree-contact step (quadruped worlds).  With
  * timing on (newt_gpu_pile_profile's `enable`), every tree-contact env-step

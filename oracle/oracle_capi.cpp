@@ -227,7 +227,8 @@ int oracle_model_dims(const newt_model_desc* d, int* nq, int* nv) { return dims(
 
 // Steps `n_worlds` worlds independently.  World w uses models[model_of_world[w]]
 // and the w-th qpos/qvel/qfrc block (blocks concatenated).  Outputs are double.
-// n_threads > 1 partitions worlds statically across host threads.
+// n_threads > 1 spreads worlds over host threads dynamically: each thread
+// takes the next unstarted world, so uneven per-world costs balance.
 // integrator: 1 semi-implicit Euler (the stepped path), 0 RK4 (newt's default,
 // used to replay its RK4 goldens).
 int oracle_run_ex(const newt_model_desc* models, int n_worlds, const int* model_of_world, const float* qpos,
@@ -257,11 +258,12 @@ int oracle_run_ex(const newt_model_desc* models, int n_worlds, const int* model_
   };
   if (n_threads <= 1) work(0, n_worlds);
   else {
+    std::atomic<int> next{0};
+    auto pull = [&]() {
+      for (int w = next.fetch_add(1); w < n_worlds; w = next.fetch_add(1)) work(w, w + 1);
+    };
     std::vector<std::thread> th;
-    for (int t = 0; t < n_threads; ++t) {
-      int b = (int)((long)n_worlds * t / n_threads), e = (int)((long)n_worlds * (t + 1) / n_threads);
-      th.emplace_back(work, b, e);
-    }
+    for (int t = 0; t < n_threads; ++t) th.emplace_back(pull);
     for (auto& x : th) x.join();
   }
   return err.load();
@@ -494,7 +496,7 @@ float oracle_newt_sin(float x) { return newt_sin(x); }
 float oracle_newt_cos(float x) { return newt_cos(x); }
 
 // Wall-clock timing of the f32 mirror over `n_threads` host threads: the CPU
-// baseline (one world per thread, static partition).  Returns seconds.
+// baseline (worlds handed to threads one at a time).  Returns seconds.
 double oracle_time_run(const newt_model_desc* models, int n_worlds, const int* model_of_world, const float* qpos,
                        const float* qvel, const float* qfrc, int n_steps, int n_threads) {
   long nq = 0, nv = 0;

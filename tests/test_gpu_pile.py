@@ -4,8 +4,12 @@ Bars (stated here, checked below):
   * contact pair lists identical to the FP64 oracle's wherever no
     penetration lies within 1e-6 of the margin (ties at the activation
     threshold may legitimately flip);
-  * PGS row impulses within 1e-3 relative (of the world's largest impulse) at
-    equal iteration counts;
+  * PGS row impulses at equal iteration counts within 1e-3 of each row's own
+    FP64 value plus an absolute floor of 2e-5 of the world's largest impulse
+    (newt's own f32 arithmetic, the oracle's float mirror, stays within
+    1e-3 |row| + 1e-5 max on these worlds), for every solver path: the plain
+    form's island-class kernels, the batched form's world-persistent kernel
+    and the batched island-class pipeline;
   * short-horizon trajectories within 1e-3 m / 1e-2 m/s.
 """
 import numpy as np
@@ -17,6 +21,7 @@ from tooling_gb300 import Engine, STEP_BATCHED, STEP_PLAIN, scenes
 pytestmark = pytest.mark.gpu
 
 IMPULSE_RTOL = 1e-3
+IMPULSE_FLOOR = 2e-5  # of the world's largest impulse
 MARGIN_BAND = 1e-6
 
 
@@ -71,16 +76,25 @@ def test_contact_pair_lists_match_oracle(eng, settled, mode):
     eng.free(slots)
 
 
-def test_pgs_impulses_match_oracle_at_equal_iterations(eng, settled):
+@pytest.mark.parametrize("path", ["plain", "persistent", "pipeline"])
+def test_pgs_impulses_match_oracle_at_equal_iterations(eng, settled, path):
     b = settled
     slots = _load(eng, b)
-    eng.step(1, STEP_BATCHED)
-    eng.sync()
-    _, work = eng.pile_profile()
-    # the one-body kernels, the short multi-body kernel and the long-island
-    # chain kernel all have islands to solve here
-    assert (work["islands"][[0, 1, 2, 3, 5]] > 0).all(), work["islands"]
-    worst = 0.0
+    eng.set_launch_choice(persistent=path != "pipeline")
+    try:
+        eng.step(1, STEP_PLAIN if path == "plain" else STEP_BATCHED)
+        eng.sync()
+        if path == "persistent":
+            _, fw = eng.fused_profile()
+            assert fw["worlds"] == len(b) and fw["contacts"] > 0, fw
+        else:
+            _, work = eng.pile_profile()
+            # the one-body kernels, the short multi-body kernel and the long-island
+            # chain kernel all have islands to solve here
+            assert (work["islands"][[0, 1, 2, 3, 5]] > 0).all(), work["islands"]
+    finally:
+        eng.set_launch_choice(persistent=True)
+    worst, rows = 0.0, 0
     for w in range(len(b)):
         qp = b.qpos[b.q_off[w]:b.q_off[w] + b.nq[w]]
         qv = b.qvel[b.v_off[w]:b.v_off[w] + b.nv[w]]
@@ -93,8 +107,11 @@ def test_pgs_impulses_match_oracle_at_equal_iterations(eng, settled):
         g = gimp[active].reshape(-1)
         assert len(g) == len(ref), f"world {w}"
         if len(ref):
-            worst = max(worst, np.abs(g - ref).max() / max(1e-9, np.abs(ref).max()))
-    assert worst <= IMPULSE_RTOL, worst
+            tol = IMPULSE_RTOL * np.abs(ref) + IMPULSE_FLOOR * np.abs(ref).max()
+            worst = max(worst, float((np.abs(g - ref) / tol).max()))
+            rows += len(ref)
+    assert rows > 1000
+    assert worst <= 1.0, worst
     eng.free(slots)
 
 
@@ -153,13 +170,17 @@ def test_free_body_scenes_within_mujoco_windows(eng, name, qtol, vtol, mode):
 
 
 def test_world_range_branches_match_plain(eng):
-    """Past 4096 pile worlds the batched form splits every group into
-    world-range branches on their own streams; each world's arithmetic is
-    unchanged, so batched and plain agree bit for bit."""
+    """The batched island-class pipeline splits every group into world-range
+    branches on their own streams; each world's arithmetic is unchanged, so
+    it and the plain form agree bit for bit."""
     b = scenes.pile_batch(n_worlds=8300, first_world=9000)
     slots = _load(eng, b)
     nq, nv = int(b.nq.sum()), int(b.nv.sum())
-    eng.step(30, STEP_BATCHED)
+    eng.set_launch_choice(persistent=False, pile_branches=2)
+    try:
+        eng.step(30, STEP_BATCHED)
+    finally:
+        eng.set_launch_choice(persistent=True)
     qb, vb = eng.get_state(slots, nq, nv)
     eng.set_state(slots, b.qpos, b.qvel)
     eng.step(30, STEP_PLAIN)
@@ -167,3 +188,25 @@ def test_world_range_branches_match_plain(eng):
     eng.free(slots)
     np.testing.assert_array_equal(qb, qp)
     np.testing.assert_array_equal(vb, vp)
+
+
+def test_persistent_kernel_tracks_oracle_from_the_drop(eng):
+    """The world-persistent kernel over a whole horizon (one launch for 150
+    env-steps: the drop, the first impacts, the settling) against the FP64
+    oracle over the same horizon, on worlds where the trajectories are not
+    yet chaotic: positions within 1e-3 m over 60 env-steps, and every world
+    still finite and without overflow after 150."""
+    b = scenes.pile_batch(n_worlds=64, first_world=3000)
+    slots = _load(eng, b)
+    nq, nv = int(b.nq.sum()), int(b.nv.sum())
+    eng.step(60, STEP_BATCHED)
+    q, v = eng.get_state(slots, nq, nv)
+    rq, rv = oracle_py.run(b, np.arange(len(b)), b.qpos, b.qvel, None, 60, precision=1)
+    assert np.abs(q - rq).max() < 1e-3
+    assert np.abs(v - rv).max() < 1e-2
+    eng.step(90, STEP_BATCHED)
+    _, fw = eng.fused_profile()
+    assert fw["worlds"] == len(b) and fw["contacts"] > 0 and fw["levels"] > 0
+    st = eng.status(slots)
+    assert not (st & 0x5).any()
+    eng.free(slots)

@@ -4,8 +4,10 @@ through the C ABI, against the FP64 oracle.
 Bars (stated here, checked below):
   * contact pair lists identical to the oracle's wherever no penetration lies
     within 1e-6 of the margin;
-  * row impulses within 1e-3 relative (of the world's largest impulse), same
-    solver and iteration cap;
+  * row impulses, same solver and iteration cap, within 1e-3 of each row's
+    own FP64 value plus an absolute floor of 1e-4 of the world's largest
+    impulse (newt's own f32 arithmetic, the oracle's float mirror, uses 0.25
+    of that bar under Newton and 0.67 under PGS on these worlds);
   * short-horizon trajectories within 2e-3 m / 5e-2 m/s;
   * the MuJoCo capture of newt's tree-chain contact scene inside newt's own
     differential windows (qpos 8e-2 / 7e-2, qvel 1.3 / 0.7).
@@ -26,6 +28,7 @@ from test_oracle_golden import _tree_chain_contact, read_newtdif  # noqa: E402
 pytestmark = pytest.mark.gpu
 
 IMPULSE_RTOL = 1e-3
+IMPULSE_FLOOR = 1e-4  # of the world's largest impulse
 MARGIN_BAND = 1e-6
 
 
@@ -109,10 +112,11 @@ def test_impulses_match_oracle(eng, settled_newton, settled_pgs, which):
         g = eng.impulses(int(slots[w]))
         assert len(g) == len(ref), f"world {w}"
         if len(ref):
-            worst = max(worst, np.abs(g - ref).max() / max(1e-9, np.abs(ref).max()))
+            tol = IMPULSE_RTOL * np.abs(ref) + IMPULSE_FLOOR * np.abs(ref).max()
+            worst = max(worst, float((np.abs(g - ref) / tol).max()))
             rows += len(ref)
     assert rows > 0
-    assert worst <= IMPULSE_RTOL, worst
+    assert worst <= 1.0, worst
     st = eng.status(slots)
     assert not (st & 0x7).any(), st  # no NaN, no factorisation failure, no overflow
     eng.free(slots)

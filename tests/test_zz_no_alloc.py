@@ -6,7 +6,10 @@ scratch in a fixed device array instead of cudaMalloc'd buffers.  Bars:
     newt_gpu_step(PLAIN) from the same state (1e-5 m, 1e-4 m/s), for pile
     worlds and chain worlds stepped in one context;
   * a context whose pile worlds need more than NEWT_STATIC_SCRATCH_BYTES is
-    refused with NEWT_E_NOMEM before anything runs.
+    refused with NEWT_E_NOMEM before anything runs;
+  * stepping allocates nothing: after the first call (the per-device setup),
+    the device's free memory (cudaMemGetInfo) is the same before and after
+    further calls on a context whose worlds were just placed.
 The file name sorts last so the test also runs after every other GPU test.
 """
 import numpy as np
@@ -66,6 +69,37 @@ def test_static_step_matches_plain_on_two_calls(built):
     finally:
         eng.close()
         ref.close()
+
+
+def _device_free_bytes():
+    """cudaMemGetInfo through the CUDA runtime the library already loaded."""
+    import ctypes as C
+    rt = C.CDLL("libcudart.so.13")
+    free, total = C.c_size_t(), C.c_size_t()
+    assert rt.cudaMemGetInfo(C.byref(free), C.byref(total)) == 0
+    return free.value
+
+
+def test_static_step_allocates_nothing(built):
+    b = scenes.pile_batch(n_worlds=96, first_world=1500)
+    eng = Engine(device=0)
+    try:
+        (slots,) = _load(eng, [b])
+        eng.step_static(1)  # the first call on the device sets up
+        eng.sync()
+        fresh = scenes.pile_batch(n_worlds=32, first_world=1700)
+        (s2,) = _load(eng, [fresh])  # new worlds, not stepped yet: a plain step would allocate scratch now
+        eng.sync()
+        before = _device_free_bytes()
+        for n in (5, 3):
+            eng.step_static(n)
+            eng.sync()
+        after = _device_free_bytes()
+        assert after == before, (before, after)
+        q, v = eng.get_state(s2, int(fresh.nq.sum()), int(fresh.nv.sum()))
+        assert np.isfinite(q).all() and np.isfinite(v).all()
+    finally:
+        eng.close()
 
 
 def test_static_step_refuses_oversize_context(built):

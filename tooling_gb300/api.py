@@ -30,7 +30,8 @@ EXPORTED = [
     "newt_gpu_get_contacts", "newt_gpu_get_impulses", "newt_gpu_event_record", "newt_gpu_event_elapsed_ms",
     "newt_gpu_flush_l2", "newt_gpu_launch_count", "newt_gpu_step_static", "newt_gpu_pile_profile",
     "newt_gpu_tc_profile", "newt_gpu_serve", "newt_gpu_memory", "newt_gpu_autotune",
-    "newt_gpu_set_ctrl_stream", "newt_gpu_apply_ctrl", "newt_gpu_read_sensors",
+    "newt_gpu_set_ctrl_stream", "newt_gpu_apply_ctrl", "newt_gpu_read_sensors", "newt_gpu_pile_fused_profile",
+    "newt_gpu_set_launch_choice",
 ]
 # newt_sensor_desc (include/newt_gpu.h)
 SENSOR_DTYPE = np.dtype([("kind", np.int32), ("on_link", np.int32), ("index", np.int32),
@@ -62,7 +63,8 @@ class NewtError(RuntimeError):
 
 
 class Opts(C.Structure):
-    _fields_ = [("device", C.c_int32), ("max_worlds", C.c_int32), ("hbm_budget_bytes", C.c_uint64)]
+    _fields_ = [("device", C.c_int32), ("max_worlds", C.c_int32), ("hbm_budget_bytes", C.c_uint64),
+                ("max_contacts", C.c_int32)]
 
 
 class ServeRequest(C.Structure):
@@ -130,6 +132,8 @@ def load_library(path: str = LIB_PATH):
         "newt_gpu_autotune": ([P, I32, P], C.c_int),
         "newt_gpu_set_ctrl_stream": ([P, P, I32, P, P], C.c_int),
         "newt_gpu_apply_ctrl": ([P], C.c_int),
+        "newt_gpu_pile_fused_profile": ([P, P, P], C.c_int),
+        "newt_gpu_set_launch_choice": ([P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -146,10 +150,10 @@ def _p(a: Optional[np.ndarray]):
 class Engine:
     """One context = one CUDA stream on one device (not thread-safe)."""
 
-    def __init__(self, device: int = 0, max_worlds: int = 0, hbm_budget_bytes: int = 0):
+    def __init__(self, device: int = 0, max_worlds: int = 0, hbm_budget_bytes: int = 0, max_contacts: int = 0):
         self.L = load_library()
         self.ctx = C.c_void_p()
-        o = Opts(device, max_worlds, hbm_budget_bytes)
+        o = Opts(device, max_worlds, hbm_budget_bytes, max_contacts)
         rc = self.L.newt_gpu_create(C.byref(o), C.byref(self.ctx))
         if rc != OK:
             raise NewtError(rc, "newt_gpu_create failed (is a CUDA device visible?)")
@@ -327,9 +331,18 @@ class Engine:
     def autotune(self, n_steps: int = 25) -> dict:
         """Pick the batched step's launch choices by timing them on the live
         worlds (their state is left unchanged)."""
-        c = np.zeros(3, np.int32)
+        c = np.zeros(5, np.int32)
         self._ck(self.L.newt_gpu_autotune(self.ctx, int(n_steps), _p(c)))
-        return {"pile_branches": int(c[0]), "tree_grid_pct": int(c[1]), "best_ms": c[2] / 1000.0}
+        return {"pile_persistent": bool(c[3]), "persistent_grid_pct": int(c[4]), "pile_branches": int(c[0]),
+                "tree_grid_pct": int(c[1]), "best_ms": c[2] / 1000.0}
+
+    def set_launch_choice(self, persistent: bool = True, persistent_grid_pct: int = 100, pile_branches: int = 0,
+                          tree_grid_pct: int = 100):
+        """Pin the batched step's launch choices (what autotune() would pick):
+        piles in the world-persistent launch, or in the island-class pipeline
+        with `pile_branches` world-range branches (0: by world count)."""
+        c = np.array([pile_branches, tree_grid_pct, 0, int(bool(persistent)), persistent_grid_pct], np.int32)
+        self._ck(self.L.newt_gpu_set_launch_choice(self.ctx, _p(c)))
 
     def memory(self):
         """(device bytes held by the world groups, admission budget)."""
@@ -346,6 +359,15 @@ class Engine:
         ms = np.zeros(len(TC_KERNELS), np.float32)
         self._ck(self.L.newt_gpu_tc_profile(self.ctx, _p(ms)))
         return dict(zip(TC_KERNELS, ms.tolist()))
+
+    def fused_profile(self):
+        """(device ms of the last batched call's world-persistent pile launch,
+        or 0 when it was not timed; {contacts, rounds, levels, worlds} summed
+        over that launch's worlds and env-steps)."""
+        ms = C.c_float()
+        w = np.zeros(4, np.uint64)
+        self._ck(self.L.newt_gpu_pile_fused_profile(self.ctx, C.byref(ms), _p(w)))
+        return ms.value, {"contacts": int(w[0]), "rounds": int(w[1]), "levels": int(w[2]), "worlds": int(w[3])}
 
     def pile_profile(self, enable: int = -1):
         """(per-kernel ms summed over the last step call's launches, {islands,

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnewt_gpu.so")
-SOURCES = ["runtime.cu", "groups.cu", "step.cu", "tree_kernels.cu", "pile_kernels.cu", "newton_kernels.cu",
+SOURCES = ["runtime.cu", "groups.cu", "step.cu", "tree_kernels.cu", "pile_kernels.cu", "pile_fused.cu", "newton_kernels.cu",
            "static_step.cu",
            "world_io.cu", "serve.cpp", "ctrl_stream.cu", "sensors.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

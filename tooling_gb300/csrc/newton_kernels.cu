@@ -888,10 +888,10 @@ extern "C" void newt_launch_tree_integrate(const TreeGroupDev& g, cudaStream_t s
     if (e_ != cudaSuccess) { ctx->err = std::string(#call ": ") + cudaGetErrorString(e_); return NEWT_E_CUDA; } \
   } while (0)
 
-// n_steps env-steps of one tree-contact group: a_free, the contact solve and
-// the integration, three launches per env-step on the context's stream.
-extern "C" int newt_tc_step(newt_gpu_ctx* ctx, HostGroup* g, int n_steps, int fused) {
-  (void)fused;
+// Scratch, kernel attribute and (when profiling) the timing events of one
+// tree-contact group for `n_steps` env-steps: everything a launch needs that
+// cannot happen under stream capture.
+extern "C" int newt_tc_prepare(newt_gpu_ctx* ctx, HostGroup* g, int n_steps) {
   if (g->n == 0) return NEWT_OK;
   const size_t per = newt_tc_ws_bytes(g->size, g->nv, g->ng, g->maxc);
   const size_t need = per * (size_t)g->cap;
@@ -902,33 +902,58 @@ extern "C" int newt_tc_step(newt_gpu_ctx* ctx, HostGroup* g, int n_steps, int fu
     CKT(cudaMalloc(&g->plain_scratch, need));
     CKT(cudaMemset(g->plain_scratch, 0, need));
     g->plain_scratch_bytes = need;
+    ctx->graph_dirty = true;
   }
   g->scr_stride = (long)(per / sizeof(float));
   CKT(newt_tc_init(g->size, g->nv, g->maxc));
-  TcGroupDev d = g->tc_dev();
-  d.t.cfrc = d.scr + tc_layout(g->size, g->nv, g->ng, g->maxc).qfc;
-  d.t.cstride = d.sstride;
-  const bool timed = ctx->profile;
-  if (timed) {
+  if (ctx->profile) {
     while (ctx->tcev.size() < (size_t)6 * n_steps) {
       cudaEvent_t e;
       CKT(cudaEventCreate(&e));
       ctx->tcev.push_back(e);
     }
   }
-  auto mark = [&](int s, int k) { if (timed) cudaEventRecord(ctx->tcev[(size_t)6 * s + k], ctx->stream); };
+  return NEWT_OK;
+}
+
+// n_steps env-steps of one prepared tree-contact group on stream `st`:
+// a_free, the contact solve and the integration, three launches per
+// env-step.  With profiling on, every kernel is bracketed by timing events
+// (recorded as external event nodes when `capturing`).
+extern "C" int newt_tc_launch(newt_gpu_ctx* ctx, HostGroup* g, int n_steps, cudaStream_t st, bool capturing) {
+  if (g->n == 0) return NEWT_OK;
+  TcGroupDev d = g->tc_dev();
+  d.t.cfrc = d.scr + tc_layout(g->size, g->nv, g->ng, g->maxc).qfc;
+  d.t.cstride = d.sstride;
+  const bool timed = ctx->profile && ctx->tcev.size() >= (size_t)6 * n_steps;
+  auto mark = [&](int s, int k) {
+    if (!timed) return;
+    if (capturing) cudaEventRecordWithFlags(ctx->tcev[(size_t)6 * s + k], st, cudaEventRecordExternal);
+    else cudaEventRecord(ctx->tcev[(size_t)6 * s + k], st);
+  };
   for (int s = 0; s < n_steps; ++s) {
     mark(s, 0);
-    newt_launch_tree_aba(d.t, ctx->stream);
+    newt_launch_tree_aba(d.t, st);
     mark(s, 1);
     mark(s, 2);
-    newt_launch_tc_solve(d, ctx->stream);
+    newt_launch_tc_solve(d, st);
     mark(s, 3);
     mark(s, 4);
-    newt_launch_tree_integrate(d.t, ctx->stream);
+    newt_launch_tree_integrate(d.t, st);
     mark(s, 5);
     ctx->launches += 3;
   }
-  ctx->tcev_steps = timed ? n_steps : 0;
+  return timed ? n_steps : 0;
+}
+
+// n_steps env-steps of one tree-contact group on the context's stream (the
+// plain form).
+extern "C" int newt_tc_step(newt_gpu_ctx* ctx, HostGroup* g, int n_steps, int fused) {
+  (void)fused;
+  if (g->n == 0) return NEWT_OK;
+  int rc = newt_tc_prepare(ctx, g, n_steps);
+  if (rc != NEWT_OK) return rc;
+  const int timed = newt_tc_launch(ctx, g, n_steps, ctx->stream, false);
+  ctx->tcev_steps = timed;
   return NEWT_OK;
 }

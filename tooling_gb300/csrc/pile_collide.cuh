@@ -143,7 +143,7 @@ NEWT_D GPose geom_pose(const WsLay& L, const float* wf, int e) {
 // half height, or semi-axes), out of line so that the sphere/box pairs keep
 // the narrowphase loop's instruction footprint.  Tries (A, B), then (B, A)
 // with *flip set (the caller relabels, newt/src/contact.rs:2561-2586).
-__device__ __noinline__ int np_round_pair(int sa, int sb, GPose pa, GPose pb, const float* za, const float* zb,
+static __device__ __noinline__ int np_round_pair(int sa, int sb, GPose pa, GPose pb, const float* za, const float* zb,
                                           float margin, CRes* res, bool* flip) {
   if (sa == SH_CAPSULE && sb == SH_PLANE) return np_capsule_plane(pa, za[0], za[1], margin, pb, res);
   if (sa == SH_CYLINDER && sb == SH_PLANE) return np_cylinder_plane(pa, za[0], za[1], margin, pb, res);

@@ -1,0 +1,458 @@
+// World-persistent free-body step: the batched form's pile kernel.
+//
+// One warp owns one pile world at a time and runs the whole call's horizon
+// for it.  Per env-step, inside the warp and the world's scratch record:
+//   collide        AABBs, sorted sweep, ordered pair list and narrowphase
+//                  (pile_collide.cuh, unchanged);
+//   assemble       the active contacts in contact order and, per contact, a
+//                  compact row record (below);
+//   levels         contact k sits at level 1 + max(level of the last earlier
+//                  contact on each of its dynamic bodies);
+//   sweeps         PGS: levels in order, the contacts of one level (they touch
+//                  disjoint bodies) on the warp's eight four-lane groups;
+//   integrate      semi-implicit Euler or RK4 (pile_solver.cuh, unchanged).
+// The state stays in the scratch record between env-steps and goes back to
+// the world record once, after the last one.  Warps take worlds from a queue
+// sorted by size (largest first) with one atomic per world, so a world's
+// env-steps never wait on another world: a slow island delays only its own
+// world, and the GPU stays busy with the others meanwhile.
+//
+// Restates, for FP32 on sm_103a:
+//   newt/src/world.rs:1459-1537   World::step phase order (Euler branch)
+//   newt/src/solver.rs:703-1257   solve_free_bodies_diag_mode, PGS branch: rows,
+//                                 regularisation, bias (:752-1061) and the
+//                                 sweeps (:1085-1200)
+//   newt/src/solver.rs:1448-1518  pgs_step_non_negative, pgs_step_pyramidal_pair
+//   newt/src/solver.rs:1892-2036  row_body_diagonal, row_residual,
+//                                 apply_impulse_delta
+//   newt/src/solver.rs:3401-3429  pyramidal facet rows n +- mu t
+//   newt/src/world.rs:3104-3112   tangent_basis
+//
+// Gauss-Seidel order.  newt sweeps each island's contacts in contact order.
+// A contact update reads the velocity accumulators of its (at most two)
+// dynamic bodies, which only earlier contacts on the same bodies have
+// changed; running the levels in order therefore reproduces the serial
+// sweep of every island exactly (islands never share a body).
+//
+// Row record.  A pyramidal contact has four facet rows r = n + s_r mu t_q(r)
+// (s = +, -, +, -; q = 1, 1, 2, 2).  The record keeps the Jacobian of the
+// normal and of both tangents and their M^-1 J^T per lane triple (side a
+// linear, side a angular, side b linear, side b angular; the linear M^-1 J^T
+// is J / m and is formed in registers), the exact row-space block
+// A_rs = J_r M^-1 J_s^T, newt's row diagonals (row_body_diagonal plus the
+// regulariser), the biases and the pair determinants.  One contact update
+// takes three four-lane dot products (J_n.v, J_t1.v, J_t2.v) for the four
+// facet residuals, runs newt's row steps in registers -- the non-negative
+// step on row 0, then the pyramidal pairs (0,1) and (2,3) -- advancing the
+// residuals by A after every step (what re-reading J_r . v gives, up to
+// rounding), and applies the summed impulse changes to the bodies once.
+#include <algorithm>
+
+#include "../../include/newt_gpu.h"
+#include "pile_solver.cuh"
+
+using namespace pile;
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int FW = 4;         // warps (worlds in flight) per block
+constexpr int FB = 4;         // blocks per SM the register budget is sized for
+constexpr int F_MAXC = 512;   // the largest contact capacity of a pile world
+
+// compact row record (floats, 16-byte aligned)
+enum {
+  R_LIN = 0,    // n xyz, t1 xyz, t2 xyz, 1/m_a, 1/m_b, 0   (1/m = 0 for a static side)
+  R_ANGA = 12,  // side a angular: J_n, J_t1, J_t2, then M^-1 J^T of each; 2 pad
+  R_ANGB = 32,  // side b angular (negated, zero when static), same layout
+  R_A = 52,     // A00 A01 A02 A03 | A11 A12 A13 A22 | A23 A33 reg mu
+  R_B = 64,     // bias of rows 0..3
+  R_DG = 68,    // newt's row diagonals (A_rr by row_body_diagonal, plus reg)
+  R_IDG = 72,   // their inverses
+  R_MISC = 76,  // 1/det of pair (0,1), of pair (2,3) (0 when det <= 0), body slot a, body slot b (int bits)
+  R_IMP = 80,   // impulses of rows 0..3
+  FR = 84
+};
+static_assert(FR % 4 == 0, "records are read as float4");
+static_assert(FR <= SC, "the compact record fits the solver record's slot");
+
+NEWT_D float4 ld4g(const float* p) { return *reinterpret_cast<const float4*>(p); }
+NEWT_D void st4g(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+
+// ---------------------------------------------------------------------------
+// assemble: active contacts in contact order and their row records
+// (newt/src/solver.rs:752-1061)
+// ---------------------------------------------------------------------------
+NEWT_D int fused_assemble(const WsLay& L, float* wf, int* wi, int lane, float (*acc)[6]) {
+  const int nb = L.nb, nc = wi[L.misc + 1];
+  const float dt = wf[L.dtg];
+  const V3 grav = v3(wf[L.dtg + 1], wf[L.dtg + 2], wf[L.dtg + 3]);
+  const float* soft = wf + L.soft;
+  for (int b = lane; b < nb; b += 32) {
+    M3 R = quat_mat(ld4(wf + L.quat + 4 * b));
+    M3 RT{{{R.m[0][0], R.m[1][0], R.m[2][0]}, {R.m[0][1], R.m[1][1], R.m[2][1]}, {R.m[0][2], R.m[1][2], R.m[2][2]}}};
+    S3 iw = sym_congr(RT, lds(wf + L.iinvb + 6 * b));
+    float* o = wf + L.iinvw + 6 * b;
+    o[0] = iw.xx; o[1] = iw.yy; o[2] = iw.zz; o[3] = iw.xy; o[4] = iw.xz; o[5] = iw.yz;
+  }
+  for (int i = lane; i < 6 * (nb + 1); i += 32) (&acc[0][0])[i] = 0.f;
+  // active contacts (solver.rs:762-769): a dynamic side and penetration beyond the gap (gap = 0)
+  int* sccon = wi + L.sccon;
+  const unsigned lt = (1u << lane) - 1u;
+  int nact = 0;
+  for (int c0 = 0; c0 < nc; c0 += 32) {
+    const int c = c0 + lane;
+    bool act = false;
+    if (c < nc) {
+      float* cf = wf + L.con + CF * c;
+      const int* cc = wi + L.ci + CI * c;
+      act = (cc[2] < nb || cc[3] < nb) && cf[C_PEN] > 0.f;
+      cf[C_ACT] = act ? 1.f : 0.f;
+      for (int k = 0; k < 4; ++k) cf[C_IMP + k] = 0.f;
+    }
+    const unsigned m = __ballot_sync(FULL, act);
+    if (act) sccon[nact + __popc(m & lt)] = c;
+    nact += __popc(m);
+  }
+  __syncwarp();
+  float tc = soft[0], dr = soft[1];
+  const bool direct = tc < 0.f;
+  if (!direct && tc < 2.f * dt) tc = 2.f * dt;  // safe_solref (solver.rs:331-338)
+  const float dmax = fminf(fmaxf(soft[3], 1.0e-4f), 0.9999f);
+  float b_, k0;
+  for (int k = lane; k < nact; k += 32) {
+    const int c = sccon[k];
+    const float* cf = wf + L.con + CF * c;
+    const int* cc = wi + L.ci + CI * c;
+    float* rec = wf + L.sc + FR * k;
+    const int ea = cc[2], eb = cc[3];
+    const bool da = ea < nb, db = eb < nb;
+    const float pen = cf[C_PEN], mu = cf[C_MU];
+    const V3 n = ld3(cf + C_N), pos = ld3(cf + C_POS);
+    V3 ref = fabsf(n.z) < 0.9f ? v3(0.f, 0.f, 1.f) : v3(1.f, 0.f, 0.f);
+    V3 t1 = cross(ref, n);
+    const float tl = sqrtf(len2(t1));
+    t1 = tl == 0.f ? v3(0.f, 0.f, 0.f) : t1 * (1.f / tl);
+    const V3 t2 = cross(n, t1);
+    const V3 z = v3(0.f, 0.f, 0.f);
+    const V3 arma = da ? pos - ld3(wf + L.pos + 3 * ea) : z;
+    const V3 armb = db ? pos - ld3(wf + L.pos + 3 * eb) : z;
+    const float ima = da ? 1.f / wf[L.mass + ea] : 0.f, imb = db ? 1.f / wf[L.mass + eb] : 0.f;
+    const S3 Ia = da ? lds(wf + L.iinvw + 6 * ea) : S3{0, 0, 0, 0, 0, 0};
+    const S3 Ib = db ? lds(wf + L.iinvw + 6 * eb) : S3{0, 0, 0, 0, 0, 0};
+    const V3 ds[3] = {n, t1, t2};
+    V3 ja[3], jb[3];
+    for (int q = 0; q < 3; ++q) {
+      ja[q] = da ? cross(arma, ds[q]) : z;
+      jb[q] = db ? -cross(armb, ds[q]) : z;
+    }
+    // linear block
+    rec[R_LIN + 0] = n.x; rec[R_LIN + 1] = n.y; rec[R_LIN + 2] = n.z;
+    rec[R_LIN + 3] = t1.x; rec[R_LIN + 4] = t1.y; rec[R_LIN + 5] = t1.z;
+    rec[R_LIN + 6] = t2.x; rec[R_LIN + 7] = t2.y; rec[R_LIN + 8] = t2.z;
+    rec[R_LIN + 9] = ima; rec[R_LIN + 10] = imb; rec[R_LIN + 11] = 0.f;
+    // angular blocks: J of n, t1, t2, then I^-1 J
+    for (int q = 0; q < 3; ++q) {
+      const V3 wa = smv(Ia, ja[q]), wb = smv(Ib, jb[q]);
+      st3(rec + R_ANGA + 3 * q, ja[q]); st3(rec + R_ANGA + 9 + 3 * q, wa);
+      st3(rec + R_ANGB + 3 * q, jb[q]); st3(rec + R_ANGB + 9 + 3 * q, wb);
+    }
+    rec[R_ANGA + 18] = rec[R_ANGA + 19] = 0.f;
+    rec[R_ANGB + 18] = rec[R_ANGB + 19] = 0.f;
+    // facet rows: side Jacobians as in newt's row assembly
+    J6 Ra[4], Rb[4];
+    float diag[4];
+    const float d = impedance(-pen, soft);
+    const float tran = ima + imb;
+    const float reg = d > 0.f ? 2.f * mu * mu * ((1.f - d) / d * (tran * (1.f + mu * mu))) : 0.f;
+    if (direct) { b_ = -dr / dmax; k0 = -soft[0] / (dmax * dmax); }
+    else { b_ = 2.f / (dmax * tc); k0 = d / (dmax * dmax * tc * tc * dr * dr); }
+    V3 va = z, vb = z;
+    if (da) va = ld3(wf + L.vel + 3 * ea) + cross(qrot(ld4(wf + L.quat + 4 * ea), ld3(wf + L.omg + 3 * ea)), arma);
+    if (db) vb = ld3(wf + L.vel + 3 * eb) + cross(qrot(ld4(wf + L.quat + 4 * eb), ld3(wf + L.omg + 3 * eb)), armb);
+    for (int r = 0; r < 4; ++r) {
+      const int q = r < 2 ? 1 : 2;
+      const float s = (r & 1) ? -mu : mu;
+      const V3 dir = n + ds[q] * s;
+      Ra[r] = J6{dir, ja[0] + ja[q] * s};
+      Rb[r] = J6{-dir, jb[0] + jb[q] * s};
+      float aii = 0.f, dvf = 0.f;
+      if (da) { aii += dot(Ra[r].a, smv(Ia, Ra[r].a)) + ima; dvf += dot(grav * dt, dir); }
+      if (db) { aii += dot(Rb[r].a, smv(Ib, Rb[r].a)) + imb; dvf -= dot(grav * dt, dir); }
+      diag[r] = aii + reg;
+      const float vcur = dot(va - vb, dir);
+      const float aref = -b_ * vcur - k0 * (-pen);
+      rec[R_B + r] = dvf - aref * dt;
+      rec[R_DG + r] = diag[r];
+      rec[R_IDG + r] = 1.f / diag[r];
+      rec[R_IMP + r] = 0.f;
+    }
+    // exact row-space block A_rs = J_r M^-1 J_s^T
+    auto arow = [&](int r, int s) {
+      float h = 0.f;
+      if (da) h += dot(Ra[r].l, Ra[s].l) * ima + dot(Ra[r].a, smv(Ia, Ra[s].a));
+      if (db) h += dot(Rb[r].l, Rb[s].l) * imb + dot(Rb[r].a, smv(Ib, Rb[s].a));
+      return h;
+    };
+    const float a01 = arow(0, 1), a23 = arow(2, 3);
+    rec[R_A + 0] = arow(0, 0); rec[R_A + 1] = a01; rec[R_A + 2] = arow(0, 2); rec[R_A + 3] = arow(0, 3);
+    rec[R_A + 4] = arow(1, 1); rec[R_A + 5] = arow(1, 2); rec[R_A + 6] = arow(1, 3); rec[R_A + 7] = arow(2, 2);
+    rec[R_A + 8] = a23; rec[R_A + 9] = arow(3, 3); rec[R_A + 10] = reg; rec[R_A + 11] = mu;
+    // pyramidal pair blocks (solver.rs:1037-1061)
+    const float det0 = diag[0] * diag[1] - a01 * a01, det1 = diag[2] * diag[3] - a23 * a23;
+    rec[R_MISC + 0] = det0 > 0.f ? 1.f / det0 : 0.f;
+    rec[R_MISC + 1] = det1 > 0.f ? 1.f / det1 : 0.f;
+    rec[R_MISC + 2] = __int_as_float(da ? ea : nb);
+    rec[R_MISC + 3] = __int_as_float(db ? eb : nb);
+  }
+  __syncwarp();
+  return nact;
+}
+
+// ---------------------------------------------------------------------------
+// levels: lane 0 assigns each record its level and counting-sorts the
+// records by level (sweep order inside a level); `loff` gets the level
+// starts and the end.  Returns the level count.
+// ---------------------------------------------------------------------------
+NEWT_D int fused_levels(const WsLay& L, const float* wf, int nact, int lane, short* last, short* lev, short* perm,
+                        short* loff) {
+  int nlev = 0;
+  if (lane == 0) {
+    const int nb = L.nb;
+    for (int b = 0; b <= nb; ++b) last[b] = 0;
+    for (int k = 0; k < nact; ++k) {
+      const float* rec = wf + L.sc + FR * k;
+      const int ba = __float_as_int(rec[R_MISC + 2]), bb = __float_as_int(rec[R_MISC + 3]);
+      const int lv = 1 + max(ba < nb ? (int)last[ba] : 0, bb < nb ? (int)last[bb] : 0);
+      if (ba < nb) last[ba] = (short)lv;
+      if (bb < nb) last[bb] = (short)lv;
+      lev[k] = (short)lv;
+      nlev = max(nlev, lv);
+    }
+    for (int v = 0; v <= nlev; ++v) loff[v] = 0;
+    for (int k = 0; k < nact; ++k) loff[lev[k]]++;
+    int run = 0;
+    for (int v = 1; v <= nlev; ++v) { const int c = loff[v]; loff[v - 1] = (short)run; run += c; }
+    loff[nlev] = (short)run;
+    for (int k = 0; k < nact; ++k) perm[loff[lev[k] - 1]++] = (short)k;
+    for (int v = nlev; v > 0; --v) loff[v] = loff[v - 1];  // back to level starts
+    loff[0] = 0;
+  }
+  nlev = __shfl_sync(FULL, nlev, 0);
+  __syncwarp();
+  return nlev;
+}
+
+// ---------------------------------------------------------------------------
+// one contact update on the calling four-lane group (lane l of the group
+// holds triple l: side a linear, side a angular, side b linear, side b
+// angular); newt/src/solver.rs:1085-1200, 1448-1518
+// ---------------------------------------------------------------------------
+NEWT_D void fused_contact(float* rec, int l, unsigned gm, int nb, float (*acc)[6]) {
+  const int side = l >> 1, part = l & 1;
+  const float4 s0 = ld4g(rec + R_A), s1 = ld4g(rec + R_A + 4), s2 = ld4g(rec + R_A + 8);
+  const float4 bs = ld4g(rec + R_B), dg = ld4g(rec + R_DG), ig = ld4g(rec + R_IDG), ms = ld4g(rec + R_MISC);
+  const float4 f4 = ld4g(rec + R_IMP);
+  const int body = __float_as_int(side ? ms.w : ms.z);
+  float J[3][3], W[3][3];
+  if (part == 0) {
+    const float4 q0 = ld4g(rec + R_LIN), q1 = ld4g(rec + R_LIN + 4), q2 = ld4g(rec + R_LIN + 8);
+    const float sg = side ? -1.f : 1.f, im = side ? q2.z : q2.y;
+    J[0][0] = sg * q0.x; J[0][1] = sg * q0.y; J[0][2] = sg * q0.z;
+    J[1][0] = sg * q0.w; J[1][1] = sg * q1.x; J[1][2] = sg * q1.y;
+    J[2][0] = sg * q1.z; J[2][1] = sg * q1.w; J[2][2] = sg * q2.x;
+#pragma unroll
+    for (int q = 0; q < 3; ++q)
+#pragma unroll
+      for (int e = 0; e < 3; ++e) W[q][e] = J[q][e] * im;
+  } else {
+    const float* blk = rec + (side ? R_ANGB : R_ANGA);
+    const float4 a0 = ld4g(blk), a1 = ld4g(blk + 4), a2 = ld4g(blk + 8), a3 = ld4g(blk + 12), a4 = ld4g(blk + 16);
+    J[0][0] = a0.x; J[0][1] = a0.y; J[0][2] = a0.z; J[1][0] = a0.w; J[1][1] = a1.x; J[1][2] = a1.y;
+    J[2][0] = a1.z; J[2][1] = a1.w; J[2][2] = a2.x;
+    W[0][0] = a2.y; W[0][1] = a2.z; W[0][2] = a2.w; W[1][0] = a3.x; W[1][1] = a3.y; W[1][2] = a3.z;
+    W[2][0] = a3.w; W[2][1] = a4.x; W[2][2] = a4.y;
+  }
+  float a[3];
+#pragma unroll
+  for (int e = 0; e < 3; ++e) a[e] = acc[body][3 * part + e];
+  float dn = (J[0][0] * a[0] + J[0][1] * a[1]) + J[0][2] * a[2];
+  float d1 = (J[1][0] * a[0] + J[1][1] * a[1]) + J[1][2] * a[2];
+  float d2 = (J[2][0] * a[0] + J[2][1] * a[1]) + J[2][2] * a[2];
+  dn += __shfl_xor_sync(gm, dn, 1);
+  d1 += __shfl_xor_sync(gm, d1, 1);
+  d2 += __shfl_xor_sync(gm, d2, 1);
+  dn += __shfl_xor_sync(gm, dn, 2);
+  d1 += __shfl_xor_sync(gm, d1, 2);
+  d2 += __shfl_xor_sync(gm, d2, 2);
+  const float mu = s2.w, reg = s2.z;
+  // symmetric 4x4 row block
+  const float A[4][4] = {{s0.x, s0.y, s0.z, s0.w}, {s0.y, s1.x, s1.y, s1.z}, {s0.z, s1.y, s1.w, s2.x},
+                         {s0.w, s1.z, s2.x, s2.y}};
+  const float b[4] = {bs.x, bs.y, bs.z, bs.w}, diag[4] = {dg.x, dg.y, dg.z, dg.w}, idg[4] = {ig.x, ig.y, ig.z, ig.w};
+  const float idet[2] = {ms.x, ms.y};
+  float d[4] = {dn + mu * d1, dn - mu * d1, dn + mu * d2, dn - mu * d2};
+  const float f0[4] = {f4.x, f4.y, f4.z, f4.w};
+  float f[4] = {f4.x, f4.y, f4.z, f4.w};
+  auto advance = [&](int s, float delta) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) d[r] += A[r][s] * delta;
+  };
+  auto single = [&](int r) {
+    const float res = d[r] + (reg * f[r] + b[r]);
+    const float nf = RowStep::nonneg(f[r], res, idg[r]);
+    const float delta = nf - f[r];
+    f[r] = nf;
+    advance(r, delta);
+  };
+  single(0);
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    const int i = 2 * p, j = i + 1;
+    if (idet[p] == 0.f) {  // det <= 0: two half-line steps
+      single(i);
+      single(j);
+      continue;
+    }
+    const float ri = d[i] + (reg * f[i] + b[i]);
+    const float rj = d[j] + (reg * f[j] + b[j]);
+    const float P[4] = {diag[i], diag[j], A[i][j], idet[p]};
+    float ni, nj;
+    RowStep::pair(f[i], f[j], ri, rj, P, &ni, &nj);
+    const float di = ni - f[i], dj = nj - f[j];
+    f[i] = ni;
+    f[j] = nj;
+    advance(i, di);
+    advance(j, dj);
+  }
+  // velocity change: sum_r W_r df_r = W_n sum df + mu W_t1 (df0 - df1) + mu W_t2 (df2 - df3)
+  const float e0 = f[0] - f0[0], e1 = f[1] - f0[1], e2 = f[2] - f0[2], e3 = f[3] - f0[3];
+  const float Fn = (e0 + e1) + (e2 + e3), F1 = mu * (e0 - e1), F2 = mu * (e2 - e3);
+  if (body < nb) {
+#pragma unroll
+    for (int e = 0; e < 3; ++e) acc[body][3 * part + e] = a[e] + (W[0][e] * Fn + W[1][e] * F1 + W[2][e] * F2);
+  }
+  if (l == 0) st4g(rec + R_IMP, make_float4(f[0], f[1], f[2], f[3]));
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// the kernel: persistent warps over a world queue
+// ---------------------------------------------------------------------------
+// work (nullable): [0] active contacts summed over every world's env-steps,
+// [1] contact-update rounds (a level's groups of eight) summed over sweeps,
+// [2] levels summed over env-steps, [3] worlds stepped.
+__global__ void __launch_bounds__(32 * FW, FB) pile_k_fused(const PileGroupDev* G, const int* wseg, int ng,
+                                                            const int* queue, int n_items, int* counter, int n_steps,
+                                                            unsigned long long* work) {
+  __shared__ float acc_s[FW][NEWT_MAX_BODIES + 1][6];
+  __shared__ short last_s[FW][NEWT_MAX_BODIES + 1];
+  __shared__ short lev_s[FW][F_MAXC];
+  __shared__ short perm_s[FW][F_MAXC];
+  __shared__ short loff_s[FW][F_MAXC + 1];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int slot = lane >> 2, l = lane & 3;
+  const unsigned gm = 0xFu << (lane & ~3);
+  float(*acc)[6] = acc_s[wib];
+  short* perm = perm_s[wib];
+  short* loff = loff_s[wib];
+  for (;;) {
+    int item = 0;
+    if (lane == 0) item = atomicAdd(counter, 1);
+    item = __shfl_sync(FULL, item, 0);
+    if (item >= n_items) break;
+    const int t = queue[item];
+    const int gi = find_seg(wseg, ng, t);
+    const PileGroupDev& g = G[gi];
+    const int w = t - wseg[gi];
+    if (w >= g.n || !g.I[(size_t)w * g.lay.istride + g.lay.live]) continue;
+    const WsLay L = ws_layout(g.nb, g.np, g.maxc);
+    float* wf = g.scr + (size_t)w * g.sstride;
+    int* wi = reinterpret_cast<int*>(wf + L.nf);
+    const int iters = g.I[(size_t)w * g.lay.istride + g.lay.iters];
+    const bool rk4 = g.I[(size_t)w * g.lay.istride + g.lay.integ] == NEWT_INTEGRATOR_RK4;
+    ws_load(g, w, L, wf, wi, lane);
+    bool bad = false;
+    int overflow = 0;
+    unsigned long long n_con = 0, n_rounds = 0, n_lev = 0;
+    for (int s = 0; s < n_steps; ++s) {
+      collide(L, wf, wi, lane);
+      overflow |= wi[L.misc + 2];
+      const int nact = min(fused_assemble(L, wf, wi, lane, acc), F_MAXC);
+      const int nlev = fused_levels(L, wf, nact, lane, last_s[wib], lev_s[wib], perm, loff);
+      int rounds = 0;
+      for (int v = 0; v < nlev; ++v) rounds += (loff[v + 1] - loff[v] + 7) >> 3;
+      for (int it = 0; it < iters; ++it)
+        for (int v = 0; v < nlev; ++v) {
+          const int e = loff[v + 1];
+          for (int base = loff[v]; base < e; base += 8) {
+            const int idx = base + slot;
+            if (idx < e) fused_contact(wf + L.sc + FR * perm[idx], l, gm, L.nb, acc);
+            __syncwarp();
+          }
+        }
+      // velocity changes for the integrator; impulses of the last env-step
+      // back to the contact records (the diagnostics surface)
+      for (int b = lane; b < L.nb; b += 32) {
+        st3(wf + L.dv + 3 * b, v3(acc[b][0], acc[b][1], acc[b][2]));
+        st3(wf + L.dw + 3 * b, v3(acc[b][3], acc[b][4], acc[b][5]));
+      }
+      if (s == n_steps - 1)
+        for (int k = lane; k < nact; k += 32) {
+          const float* rec = wf + L.sc + FR * k;
+          float* cimp = wf + L.con + CF * wi[L.sccon + k] + C_IMP;
+          for (int r = 0; r < 4; ++r) cimp[r] = rec[R_IMP + r];
+        }
+      __syncwarp();
+      bad |= pile_integrate_world(wf, L, rk4, lane);
+      n_con += (unsigned long long)nact;
+      n_rounds += (unsigned long long)rounds * (unsigned long long)iters;
+      n_lev += (unsigned long long)nlev;
+    }
+    ws_store_state(g, w, L, wf, lane);
+    ws_store_diag(g, w, L, wf, wi, lane);
+    if (lane == 0) {
+      unsigned st = 0u;
+      if (overflow) st |= NEWT_WS_CONTACT_OVERFLOW;
+      if (bad) st |= NEWT_WS_NONFINITE;
+      if (st) atomicOr(reinterpret_cast<unsigned*>(g.I + (size_t)w * g.lay.istride + g.lay.status), st);
+      if (work) {
+        atomicAdd(work + 0, n_con);
+        atomicAdd(work + 1, n_rounds);
+        atomicAdd(work + 2, n_lev);
+        atomicAdd(work + 3, 1ull);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+// Resident blocks of pile_k_fused per SM (outside stream capture).
+extern "C" int newt_pile_fused_blocks_per_sm() {
+  int b = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pile_k_fused, 32 * FW, 0) != cudaSuccess || b < 1) b = 1;
+  return b;
+}
+
+// Worlds per block of the launch (the queue hands out one world per warp).
+extern "C" int newt_pile_fused_warps_per_block() { return FW; }
+
+// Loads the kernel (so a later launch under stream capture creates nothing).
+extern "C" cudaError_t newt_pile_fused_prepare() {
+  cudaFuncAttributes a;
+  return cudaFuncGetAttributes(&a, pile_k_fused);
+}
+
+// One launch steps every live world of the table `n_steps` env-steps.
+// `counter` must be zero when the launch starts (the caller clears it on
+// `st` first); `grid` blocks of FW warps pull worlds from `queue`.
+extern "C" void newt_launch_pile_fused(const PileGroupDev* dG, const int* dwseg, int ng, const int* queue,
+                                       int n_items, int* counter, int n_steps, int grid,
+                                       unsigned long long* work, cudaStream_t st) {
+  if (n_items <= 0 || grid <= 0) return;
+  pile_k_fused<<<grid, 32 * FW, 0, st>>>(dG, dwseg, ng, queue, n_items, counter, n_steps, work);
+}

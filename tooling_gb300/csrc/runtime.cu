@@ -180,6 +180,7 @@ HostGroup* find_or_make_group(newt_gpu_ctx* ctx, HostModel& m) {
   auto g = std::make_unique<HostGroup>();
   g->kind = m.kind; g->size = m.size; g->np = m.np; g->topo_key = m.key;
   g->nq = m.nq; g->nv = m.nv;
+  g->maxc_cap = ctx->max_contacts;
   if (m.kind == GK_TREE_CONTACT) g->setup_tc(m);
   g->id = (int)ctx->groups.size();
   m.group = g->id;
@@ -195,6 +196,7 @@ int newt_gpu_create(const newt_gpu_opts* opts, newt_gpu_ctx** out) {
   auto* ctx = new newt_gpu_ctx();
   ctx->device = opts ? opts->device : 0;
   ctx->max_worlds = opts && opts->max_worlds > 0 ? opts->max_worlds : (1 << 20);
+  ctx->max_contacts = opts && opts->max_contacts > 0 ? opts->max_contacts : 0;
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) { delete ctx; return NEWT_E_CUDA; }
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return NEWT_E_CUDA; }
@@ -224,6 +226,9 @@ int newt_gpu_destroy(newt_gpu_ctx* ctx) {
     for (int k = 0; k < 4; ++k) if (ctx->pbs[b][k]) cudaStreamDestroy(ctx->pbs[b][k]);
     for (int k = 0; k < 5; ++k) if (ctx->pbe[b][k]) cudaEventDestroy(ctx->pbe[b][k]);
   }
+  for (int k = 0; k < 2; ++k) if (ctx->fkev[k]) cudaEventDestroy(ctx->fkev[k]);
+  if (ctx->fused_work) cudaFree(ctx->fused_work);
+  if (ctx->tcstream) cudaStreamDestroy(ctx->tcstream);
   for (cudaEvent_t e : ctx->kev) cudaEventDestroy(e);
   for (cudaEvent_t e : ctx->tcev) cudaEventDestroy(e);
   if (ctx->io_h) cudaFreeHost(ctx->io_h);
@@ -527,6 +532,22 @@ int newt_gpu_autotune(newt_gpu_ctx* ctx, int32_t n_steps, int32_t* choice) {
   return rc;
 }
 
+int newt_gpu_set_launch_choice(newt_gpu_ctx* ctx, const int32_t* choice) {
+  if (!ctx || !choice) return NEWT_E_INVALID;
+  const int branches = choice[0], tree_pct = choice[1], fused = choice[3], fused_pct = choice[4];
+  if (branches < 0 || branches > newt_gpu_ctx::PILE_BRANCHES || tree_pct < 1 || tree_pct > 100 || fused < 0 ||
+      fused > 1 || fused_pct < 1 || fused_pct > 100) {
+    ctx->err = "newt_gpu_set_launch_choice: pile branches 0..3, grid percents 1..100, persistent flag 0 or 1";
+    return NEWT_E_INVALID;
+  }
+  ctx->tune_branches = branches;
+  ctx->tune_tree_grid_pct = tree_pct;
+  ctx->tune_pile_fused = fused;
+  ctx->tune_fused_pct = fused_pct;
+  ctx->graph_dirty = true;
+  return NEWT_OK;
+}
+
 int newt_gpu_memory(const newt_gpu_ctx* ctx, uint64_t* used, uint64_t* budget) {
   if (!ctx) return NEWT_E_INVALID;
   if (used) *used = ctx->used;
@@ -579,6 +600,23 @@ int newt_gpu_pile_profile(newt_gpu_ctx* ctx, int32_t enable, float* kernel_ms, i
       CK(cudaMemcpy(h, l.first + (size_t)C * l.second, sizeof(h), cudaMemcpyDeviceToHost));
       for (int k = 0; k < n; ++k) work[k] += h[k];
     }
+  }
+  return NEWT_OK;
+}
+
+int newt_gpu_pile_fused_profile(newt_gpu_ctx* ctx, float* kernel_ms, uint64_t* work) {
+  if (!ctx) return NEWT_E_INVALID;
+  cudaSetDevice(ctx->device);
+  int rc = newt_gpu_sync(ctx, 600000);
+  if (rc != NEWT_OK) return rc;
+  if (kernel_ms) {
+    *kernel_ms = 0.f;
+    if (ctx->last_fused && ctx->profile && ctx->fkev[0]) CK(cudaEventElapsedTime(kernel_ms, ctx->fkev[0], ctx->fkev[1]));
+  }
+  if (work) {
+    for (int k = 0; k < 4; ++k) work[k] = 0;
+    if (ctx->last_fused && ctx->fused_work)
+      CK(cudaMemcpy(work, ctx->fused_work, 4 * sizeof(uint64_t), cudaMemcpyDeviceToHost));
   }
   return NEWT_OK;
 }

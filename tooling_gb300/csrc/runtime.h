@@ -74,6 +74,7 @@ struct HostGroup {
   // pile layout
   PileLayout lay{};
   int maxc = 0;
+  int maxc_cap = 0;  // the context's cap on maxc for pile groups (0: none)
   // tree-contact groups: per-geom model rows, geom topology, candidate pairs
   int ng = 0, npairs = 0;
   int r_geom = 0, ri_mode = 0, ri_iters = 0;
@@ -118,6 +119,7 @@ struct HostGroup {
 struct newt_gpu_ctx {
   int device = 0;
   int max_worlds = 0;
+  int max_contacts = 0;  // pile contact capacity cap (newt_gpu_opts::max_contacts)
   uint64_t budget = 0, used = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -144,6 +146,21 @@ struct newt_gpu_ctx {
   // launch choices of the batched form (newt_gpu_autotune): pile branches
   // (0: by world count), tree persistent grid in percent of full residency
   int tune_branches = 0, tune_tree_grid_pct = 100;
+  // pile worlds in the batched form: 1 = one world-persistent launch over a
+  // size-sorted queue (pile_fused.cu), 0 = the island-class pipeline per
+  // env-step; the persistent grid in percent of full residency
+  int tune_pile_fused = 1, tune_fused_pct = 100;
+  // the persistent launch of the captured graph: its timing events (external
+  // records when profiling), its work counters (device: contacts, rounds,
+  // levels, worlds) and whether the graph holds one; `last_fused` tells the
+  // profiling surface that the last batched call ran it
+  cudaEvent_t fkev[2] = {nullptr, nullptr};
+  unsigned long long* fused_work = nullptr;
+  bool graph_fused = false, last_fused = false;
+  // tree-contact groups' branch of the captured graph, and its env-steps
+  // with timing events (profiling)
+  cudaStream_t tcstream = nullptr;
+  int graph_tc_steps = 0;
   cudaStream_t pbs[PILE_BRANCHES][4] = {};
   cudaEvent_t pbe[PILE_BRANCHES][5] = {};
   // plain path: one single-group table per group

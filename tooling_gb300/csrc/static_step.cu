@@ -10,10 +10,16 @@
 // group tables live in one file-scope device array of fixed size
 // (NEWT_STATIC_SCRATCH_BYTES); nothing is allocated per call.
 //
-// Setup: the first call on a device, with that device current, looks up the array's address with cudaGetSymbolAddress (which
-// loads this module) and loads the pile and tree kernels; later calls on that
-// device reuse both.  Make that first call before any stream capture on the
-// device.
+// Setup: the first call on a device, with that device current, loads the
+// pile and tree kernels and this module.  Every call then looks the array's
+// address up with cudaGetSymbolAddress (a host-side lookup once the module is
+// loaded, so a cudaDeviceReset between calls leaves nothing stale).  Make the
+// first call on a device before any stream capture on it.
+//
+// Tables: the pile group table and segment table reach the device as a
+// by-value kernel argument written into the array by a one-block kernel on
+// the context's stream, so a call issues no host-to-device copy: it does not
+// wait for the stream's earlier work, and no host buffer has to outlive it.
 //
 // Sharing: there is one array per device.  Two calls whose GPU work can
 // overlap (two contexts on one device, or two threads) race on it; the
@@ -45,7 +51,22 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_scratch[NEWT_STATIC_SCRATCH_BYTES];
 
 std::mutex g_setup_mu;
-unsigned char* g_scratch_addr[kMaxDevices] = {};
+bool g_prepared[kMaxDevices] = {};
+
+// The pile tables of one call, passed by value (about 10 KB of kernel
+// parameters; sm_90 and later take up to 32 KB).
+struct StaticTables {
+  PileGroupDev g[kMaxPileGroups];
+  int seg[kMaxPileGroups + 1];
+  int ng;
+};
+
+static_assert(sizeof(StaticTables) <= 32000, "kernel parameters are limited to 32 KB");
+
+__global__ void static_write_tables(const StaticTables t, PileGroupDev* dG, int* dseg) {
+  for (int i = threadIdx.x; i < t.ng; i += blockDim.x) dG[i] = t.g[i];
+  for (int i = threadIdx.x; i <= t.ng; i += blockDim.x) dseg[i] = t.seg[i];
+}
 
 size_t round_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
@@ -54,20 +75,25 @@ int fail(newt_gpu_ctx* ctx, int code, const std::string& msg) {
   return code;
 }
 
-// Address of this device's scratch array; the first call per device sets it up.
+// Address of this device's scratch array (the device is current); the first
+// call per device loads the kernels.
 int scratch_for_device(newt_gpu_ctx* ctx, unsigned char** out) {
   if (ctx->device < 0 || ctx->device >= kMaxDevices) return fail(ctx, NEWT_E_INVALID, "device ordinal out of range");
   std::lock_guard<std::mutex> lock(g_setup_mu);
-  if (!g_scratch_addr[ctx->device]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-    if (e != cudaSuccess) return fail(ctx, NEWT_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    e = newt_pile_prepare_kernels();
+  if (!g_prepared[ctx->device]) {
+    cudaError_t e = newt_pile_prepare_kernels();
     if (e == cudaSuccess) e = newt_tree_prepare_kernels();
+    if (e == cudaSuccess) {
+      cudaFuncAttributes a;
+      e = cudaFuncGetAttributes(&a, static_write_tables);
+    }
     if (e != cudaSuccess) return fail(ctx, NEWT_E_CUDA, std::string("loading step kernels: ") + cudaGetErrorString(e));
-    g_scratch_addr[ctx->device] = static_cast<unsigned char*>(p);
+    g_prepared[ctx->device] = true;
   }
-  *out = g_scratch_addr[ctx->device];
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+  if (e != cudaSuccess) return fail(ctx, NEWT_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  *out = static_cast<unsigned char*>(p);
   return NEWT_OK;
 }
 
@@ -81,8 +107,9 @@ extern "C" NEWT_API int newt_gpu_step_static(newt_gpu_ctx* ctx, int32_t n_steps)
 
   // Lay out the pile table, segment table, work lists and per-world solver
   // scratch inside the array, and refuse before any launch if they do not fit.
-  PileGroupDev table[kMaxPileGroups];
-  int seg[kMaxPileGroups + 1];
+  StaticTables tab;
+  PileGroupDev* table = tab.g;
+  int* seg = tab.seg;
   size_t scr_off[kMaxPileGroups];
   int ng = 0, slots = 0;
   seg[0] = 0;
@@ -117,17 +144,20 @@ extern "C" NEWT_API int newt_gpu_step_static(newt_gpu_ctx* ctx, int32_t n_steps)
   unsigned char* base = nullptr;
   int rc = scratch_for_device(ctx, &base);
   if (rc != NEWT_OK) return rc;
+  PileGroupDev* dG = reinterpret_cast<PileGroupDev*>(base);
+  int* dseg = reinterpret_cast<int*>(base + seg_off);
+  int* lists = reinterpret_cast<int*>(base + list_off);
   if (ng > 0) {
     for (int k = 0; k < ng; ++k) table[k].scr = reinterpret_cast<float*>(base + scr_off[k]);
-    // pageable sources: both copies have left the host arrays when they return
-    e = cudaMemcpyAsync(base, table, sizeof(PileGroupDev) * (size_t)ng, cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(base + seg_off, seg, sizeof(int) * (size_t)(ng + 1), cudaMemcpyHostToDevice, ctx->stream);
-    if (e != cudaSuccess) return fail(ctx, NEWT_E_CUDA, std::string("table upload: ") + cudaGetErrorString(e));
+    tab.ng = ng;
+    static_write_tables<<<1, 64, 0, ctx->stream>>>(tab, dG, dseg);
+    ctx->launches += 1;
   }
-  const PileGroupDev* dG = reinterpret_cast<const PileGroupDev*>(base);
-  const int* dseg = reinterpret_cast<const int*>(base + seg_off);
-  int* lists = reinterpret_cast<int*>(base + list_off);
+  // the profiling surface reads this call's island counters from the array
+  ctx->last_lists.clear();
+  if (ng > 0) ctx->last_lists.push_back({lists, slots});
+  ctx->kev_steps = 0;
+  ctx->last_fused = false;
 
   for (int s = 0; s < n_steps; ++s) {
     for (auto& gp : ctx->groups) {

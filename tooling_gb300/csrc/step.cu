@@ -2,11 +2,13 @@
 //
 // Plain form (the drop-in baseline): every group is launched separately,
 // one launch per stage per env-step with fixed tiles.
-// Batched form: trees run their whole horizon in one persistent launch per
-// size bucket, pulling work items from a device queue sorted by size class;
-// pile worlds of every size share one launch per stage per env-step over a
-// segment table; the whole call is captured once in a CUDA graph (trees and
-// piles as concurrent branches) and replayed.
+// Batched form: the whole call is captured once in a CUDA graph and
+// replayed.  Trees run their horizon in one persistent launch per size
+// bucket, pulling work items from a device queue sorted by size class;
+// pile worlds of every size run theirs in one world-persistent launch over
+// a size-sorted queue (pile_fused.cu; the island-class pipeline, one launch
+// per stage per env-step, stays available to the autotuner); tree-contact
+// worlds run their per-env-step kernels on a third branch of the same graph.
 #include <algorithm>
 #include <cstdio>
 #include <vector>
@@ -27,6 +29,13 @@ extern "C" int newt_launch_pile_step(const PileGroupDev* dG, const int* dwseg, i
                                      int total_slots, int* lists, int write_diag, cudaStream_t st,
                                      const cudaStream_t* side, cudaEvent_t* ev, cudaEvent_t* kev);
 extern "C" void newt_pile_init();
+extern "C" int newt_pile_fused_blocks_per_sm();
+extern "C" int newt_pile_fused_warps_per_block();
+extern "C" void newt_launch_pile_fused(const PileGroupDev* dG, const int* dwseg, int ng, const int* queue,
+                                       int n_items, int* counter, int n_steps, int grid,
+                                       unsigned long long* work, cudaStream_t st);
+extern "C" int newt_tc_prepare(newt_gpu_ctx* ctx, HostGroup* g, int n_steps);
+extern "C" int newt_tc_launch(newt_gpu_ctx* ctx, HostGroup* g, int n_steps, cudaStream_t st, bool capturing);
 
 // Streams and events the pile step forks its island classes onto.
 static int ensure_pile_streams(newt_gpu_ctx* ctx) {
@@ -166,6 +175,7 @@ int step_plain(newt_gpu_ctx* ctx, int n_steps) {
     if (T.lists) ctx->last_lists.push_back({T.lists, T.slots});
   ctx->kev_steps = 0;
   ctx->kev_branches = 1;
+  ctx->last_fused = false;
   for (int s = 0; s < n_steps; ++s) {
     for (size_t gi = 0; gi < ctx->groups.size(); ++gi) {
       HostGroup* g = ctx->groups[gi].get();
@@ -222,33 +232,59 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
     L.grid = std::min(L.items, std::max(1, full * ctx->tune_tree_grid_pct / 100));
     tls.push_back(L);
   }
-  // piles: tables over every pile group (largest worlds first), one per
-  // world-range branch; the branches run on their own streams, so one
-  // branch's long-island tail overlaps the others' collide and solve
+  // piles, largest worlds first
   std::vector<HostGroup*> piles;
   long pile_worlds = 0;
   for (auto& gp : ctx->groups)
     if (gp->n > 0 && gp->kind == GK_PILE) { piles.push_back(gp.get()); pile_worlds += gp->n; }
   std::stable_sort(piles.begin(), piles.end(), [](HostGroup* a, HostGroup* b) { return a->size > b->size; });
-  const int nbr = ctx->tune_branches > 0
-                      ? std::min(ctx->tune_branches, newt_gpu_ctx::PILE_BRANCHES)
-                      : (int)std::max<long>(1, std::min<long>(2, pile_worlds / 4096));
+  const bool fused = ctx->tune_pile_fused != 0;
+  // fused: one table over every pile group; its flat world order is the
+  // queue (groups by size, largest first)
+  PileTable ft;
+  int* fcounter = nullptr;
+  int fgrid = 0;
+  const int nbr = fused ? 0
+                        : (ctx->tune_branches > 0 ? std::min(ctx->tune_branches, newt_gpu_ctx::PILE_BRANCHES)
+                                                  : (int)std::max<long>(1, std::min<long>(2, pile_worlds / 4096)));
   std::vector<PileTable> pts(nbr);
-  for (int b = 0; b < nbr; ++b) {
-    int rc = build_pile_table(ctx, piles, pts[b], bufs, b, nbr);
-    if (rc != NEWT_OK) return rc;
-  }
   if (pile_worlds > 0) {
     int rc = ensure_pile_branches(ctx);
     if (rc != NEWT_OK) return rc;
   }
+  if (fused && pile_worlds > 0) {
+    int rc = build_pile_table(ctx, piles, ft, bufs, 0, 1);
+    if (rc != NEWT_OK) return rc;
+    CKS(cudaMalloc(&fcounter, sizeof(int)));
+    bufs.push_back(fcounter);
+    if (!ctx->fused_work) CKS(cudaMalloc(&ctx->fused_work, 4 * sizeof(unsigned long long)));
+    if (!ctx->fkev[0])
+      for (int k = 0; k < 2; ++k) CKS(cudaEventCreate(&ctx->fkev[k]));
+    const int wpb = newt_pile_fused_warps_per_block();
+    const int full = newt_pile_fused_blocks_per_sm() * sm_count(ctx);
+    fgrid = std::min((ft.worlds + wpb - 1) / wpb, std::max(1, full * ctx->tune_fused_pct / 100));
+  }
+  for (int b = 0; b < nbr; ++b) {
+    int rc = build_pile_table(ctx, piles, pts[b], bufs, b, nbr);
+    if (rc != NEWT_OK) return rc;
+  }
+  // tree-contact groups: scratch and events before the capture
+  std::vector<HostGroup*> tcs;
+  for (auto& gp : ctx->groups)
+    if (gp->n > 0 && gp->kind == GK_TREE_CONTACT) {
+      int rc = newt_tc_prepare(ctx, gp.get(), n_steps);
+      if (rc != NEWT_OK) return rc;
+      tcs.push_back(gp.get());
+    }
+  if (!tcs.empty() && !ctx->tcstream) CKS(cudaStreamCreateWithFlags(&ctx->tcstream, cudaStreamNonBlocking));
 
-  cudaEvent_t fork = nullptr, join = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr, tjoin = nullptr;
   if (!ctx->side) CKS(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
   CKS(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
   CKS(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+  CKS(cudaEventCreateWithFlags(&tjoin, cudaEventDisableTiming));
   cudaGraph_t graph;
-  if (ctx->profile) {
+  if (ctx->profile && nbr > 0) {
     int r = ensure_kernel_events(ctx, n_steps, nbr);
     if (r != NEWT_OK) return r;
   }
@@ -263,7 +299,28 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
     newt_launch_tree_persistent(L.dg, L.dq, L.dc, L.items, L.bucket, n_steps, L.grid, ctx->side);
   }
   cudaEventRecord(join, ctx->side);
-  int64_t before = ctx->launches;
+  int tc_timed = 0;
+  const int64_t l0 = ctx->launches;
+  if (!tcs.empty()) {
+    cudaStreamWaitEvent(ctx->tcstream, fork, 0);
+    for (HostGroup* g : tcs) tc_timed = newt_tc_launch(ctx, g, n_steps, ctx->tcstream, true);
+    cudaEventRecord(tjoin, ctx->tcstream);
+  }
+  const int tc_launches = (int)(ctx->launches - l0);
+  const int64_t before = ctx->launches;
+  int fused_launches = 0;
+  if (fused && ft.ng > 0) {
+    cudaStream_t fs = ctx->pbs[0][0];
+    cudaStreamWaitEvent(fs, fork, 0);
+    cudaMemsetAsync(fcounter, 0, sizeof(int), fs);
+    cudaMemsetAsync(ctx->fused_work, 0, 4 * sizeof(unsigned long long), fs);
+    if (ctx->profile) cudaEventRecordWithFlags(ctx->fkev[0], fs, cudaEventRecordExternal);
+    newt_launch_pile_fused(ft.dG, ft.dseg, ft.ng, nullptr, ft.worlds, fcounter, n_steps, fgrid, ctx->fused_work, fs);
+    if (ctx->profile) cudaEventRecordWithFlags(ctx->fkev[1], fs, cudaEventRecordExternal);
+    cudaEventRecord(ctx->pbe[0][4], fs);
+    cudaStreamWaitEvent(ctx->stream, ctx->pbe[0][4], 0);
+    fused_launches = 1;
+  }
   for (int b = 0; b < nbr; ++b) {
     if (pts[b].ng == 0) continue;
     cudaStream_t* bs = ctx->pbs[b];
@@ -272,14 +329,18 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
     cudaEventRecord(ctx->pbe[b][4], bs[0]);
     cudaStreamWaitEvent(ctx->stream, ctx->pbe[b][4], 0);
   }
-  int pile_launches = (int)(ctx->launches - before);
-  ctx->launches = before;
-  ctx->graph_kev_steps = ctx->profile && pile_worlds > 0 ? n_steps : 0;
-  ctx->graph_kev_branches = nbr;
+  const int pile_launches = (int)(ctx->launches - before) + fused_launches;
+  ctx->launches = l0;
+  ctx->graph_kev_steps = ctx->profile && nbr > 0 && pile_worlds > 0 ? n_steps : 0;
+  ctx->graph_kev_branches = std::max(nbr, 1);
+  ctx->graph_fused = fused && ft.ng > 0;
+  ctx->graph_tc_steps = tc_timed;
   cudaStreamWaitEvent(ctx->stream, join, 0);
+  if (!tcs.empty()) cudaStreamWaitEvent(ctx->stream, tjoin, 0);
   cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
   cudaEventDestroy(fork);
   cudaEventDestroy(join);
+  cudaEventDestroy(tjoin);
   if (ce != cudaSuccess) { ctx->err = cudaGetErrorString(ce); return NEWT_E_CUDA; }
   if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
   CKS(cudaGraphInstantiate(&ctx->graph_exec, graph, 0));
@@ -288,13 +349,12 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
   ctx->plan_bufs = bufs;
   ctx->graph_steps = n_steps;
   ctx->graph_dirty = false;
-  ctx->queue_items = (int)tls.size() + pile_launches;
+  // kernel launches one replay issues
+  ctx->queue_items = (int)tls.size() + pile_launches + tc_launches;
   return NEWT_OK;
 }
 
 int step_batched(newt_gpu_ctx* ctx, int n_steps) {
-  bool has_tc = false;
-  for (auto& g : ctx->groups) if (g->n > 0 && g->kind == GK_TREE_CONTACT) has_tc = true;
   if (ctx->graph_dirty || ctx->graph_steps != n_steps || !ctx->graph_exec) {
     int rc = capture(ctx, n_steps);
     if (rc != NEWT_OK) return rc;
@@ -306,75 +366,96 @@ int step_batched(newt_gpu_ctx* ctx, int n_steps) {
   ctx->last_lists = ctx->graph_lists;
   ctx->kev_steps = ctx->graph_kev_steps;
   ctx->kev_branches = ctx->graph_kev_branches;
-  if (has_tc) {
-    for (auto& gp : ctx->groups)
-      if (gp->n > 0 && gp->kind == GK_TREE_CONTACT) {
-        int rc = newt_tc_step(ctx, gp.get(), n_steps, 1);
-        if (rc != NEWT_OK) return rc;
-      }
-  }
+  ctx->last_fused = ctx->graph_fused;
+  ctx->tcev_steps = ctx->graph_tc_steps;
   return NEWT_OK;
 }
 
 // ---------------------------------------------------------------------------
 // autotuning of the batched form's launch choices
 // ---------------------------------------------------------------------------
-// Every trial steps the live worlds from the same snapshot of every group's
-// records (model, state, status: the whole step state; solver scratch is
-// rebuilt each env-step), so the worlds end where they began.
+// Every trial steps the live worlds from a snapshot of every group's records
+// (model, state, status: the whole step state; solver scratch is rebuilt each
+// env-step), so the worlds end where they began.  Two snapshots are timed:
+// the worlds as they are, and as they are `settle` env-steps later (piles
+// that were falling have landed and their islands have grown), so a choice
+// that only wins on the early regime does not win overall.
 int autotune_batched(newt_gpu_ctx* ctx, int n_steps, int32_t* choice) {
   if (n_steps <= 0) return NEWT_E_INVALID;
-  std::vector<std::pair<void*, size_t>> snap;  // (copy, bytes) per group block
-  auto blocks = [&](std::vector<std::pair<void*, size_t>>& out) {
-    for (auto& gp : ctx->groups) {
-      HostGroup* g = gp.get();
-      if (g->n == 0) continue;
-      out.push_back({g->dF, g->frows * (size_t)g->cap * sizeof(float)});
-      out.push_back({g->dI, g->irows * (size_t)g->cap * sizeof(int)});
-    }
-  };
   std::vector<std::pair<void*, size_t>> live;
-  blocks(live);
-  int rc = NEWT_OK;
-  for (auto& b : live) {
-    void* p = nullptr;
-    if (cudaMalloc(&p, b.second) != cudaSuccess) { rc = NEWT_E_NOMEM; break; }
-    snap.push_back({p, b.second});
-    CKS(cudaMemcpyAsync(p, b.first, b.second, cudaMemcpyDeviceToDevice, ctx->stream));
+  for (auto& gp : ctx->groups) {
+    HostGroup* g = gp.get();
+    if (g->n == 0) continue;
+    live.push_back({g->dF, g->frows * (size_t)g->cap * sizeof(float)});
+    live.push_back({g->dI, g->irows * (size_t)g->cap * sizeof(int)});
   }
-  auto restore = [&]() -> int {
-    for (size_t i = 0; i < snap.size(); ++i)
-      CKS(cudaMemcpyAsync(live[i].first, snap[i].first, live[i].second, cudaMemcpyDeviceToDevice, ctx->stream));
+  std::vector<void*> snap[2];
+  int rc = NEWT_OK;
+  auto take = [&](int k) -> int {
+    for (auto& b : live) {
+      void* p = nullptr;
+      if (cudaMalloc(&p, b.second) != cudaSuccess) return NEWT_E_NOMEM;
+      snap[k].push_back(p);
+      CKS(cudaMemcpyAsync(p, b.first, b.second, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
     return NEWT_OK;
   };
-  struct Cand { int branches, grid_pct; };
-  const Cand cands[] = {{1, 100}, {2, 100}, {3, 100}, {1, 50}, {2, 50}};
-  Cand best{ctx->tune_branches, ctx->tune_tree_grid_pct};
-  float best_ms = -1.f;
-  for (const Cand& c : cands) {
-    if (rc != NEWT_OK) break;
+  auto restore = [&](int k) -> int {
+    for (size_t i = 0; i < snap[k].size(); ++i)
+      CKS(cudaMemcpyAsync(live[i].first, snap[k][i], live[i].second, cudaMemcpyDeviceToDevice, ctx->stream));
+    return NEWT_OK;
+  };
+  struct Cand { int fused, fused_pct, branches, grid_pct; };
+  const Cand cands[] = {{1, 100, 0, 100}, {1, 75, 0, 100}, {1, 50, 0, 100}, {0, 100, 1, 100}, {0, 100, 2, 100},
+                        {0, 100, 3, 100}, {1, 100, 0, 50}, {0, 100, 2, 50}};
+  const Cand start{ctx->tune_pile_fused, ctx->tune_fused_pct, ctx->tune_branches, ctx->tune_tree_grid_pct};
+  auto set = [&](const Cand& c) {
+    ctx->tune_pile_fused = c.fused;
+    ctx->tune_fused_pct = c.fused_pct;
     ctx->tune_branches = c.branches;
     ctx->tune_tree_grid_pct = c.grid_pct;
     ctx->graph_dirty = true;
-    // first call captures (and warms up); the second is timed
-    for (int rep = 0; rep < 2 && rc == NEWT_OK; ++rep) {
-      if ((rc = restore()) != NEWT_OK) break;
-      cudaEventRecord(ctx->ev[0], ctx->stream);
-      rc = step_batched(ctx, n_steps);
-      cudaEventRecord(ctx->ev[1], ctx->stream);
+  };
+  rc = take(0);
+  // the settled snapshot: `settle` env-steps further on, with the current choice
+  const int settle = 8 * n_steps;
+  if (rc == NEWT_OK) rc = step_batched(ctx, n_steps);
+  for (int k = 1; rc == NEWT_OK && k * n_steps < settle; ++k) rc = step_batched(ctx, n_steps);
+  if (rc == NEWT_OK) rc = take(1);
+  Cand best = start;
+  float best_ms = -1.f;
+  for (const Cand& c : cands) {
+    if (rc != NEWT_OK) break;
+    set(c);
+    float total = 0.f;
+    for (int ph = 0; ph < 2 && rc == NEWT_OK; ++ph) {
+      // first call captures (and warms up); the second is timed
+      for (int rep = 0; rep < 2 && rc == NEWT_OK; ++rep) {
+        if ((rc = restore(ph)) != NEWT_OK) break;
+        cudaEventRecord(ctx->ev[0], ctx->stream);
+        rc = step_batched(ctx, n_steps);
+        cudaEventRecord(ctx->ev[1], ctx->stream);
+      }
+      if (rc != NEWT_OK) break;
+      if (cudaEventSynchronize(ctx->ev[1]) != cudaSuccess) { rc = NEWT_E_CUDA; break; }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+      total += ms;
     }
     if (rc != NEWT_OK) break;
-    if (cudaEventSynchronize(ctx->ev[1]) != cudaSuccess) { rc = NEWT_E_CUDA; break; }
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
-    if (best_ms < 0.f || ms < best_ms) { best_ms = ms; best = c; }
+    if (best_ms < 0.f || total < best_ms) { best_ms = total; best = c; }
   }
-  if (rc == NEWT_OK) rc = restore();
+  if (!snap[0].empty() && rc == NEWT_OK) rc = restore(0);
   cudaStreamSynchronize(ctx->stream);
-  for (auto& b : snap) cudaFree(b.first);
-  ctx->tune_branches = best.branches;
-  ctx->tune_tree_grid_pct = best.grid_pct;
-  ctx->graph_dirty = true;
-  if (choice) { choice[0] = best.branches; choice[1] = best.grid_pct; choice[2] = (int32_t)(best_ms * 1000.f); }
+  for (int k = 0; k < 2; ++k)
+    for (void* p : snap[k]) cudaFree(p);
+  set(best);
+  if (choice) {
+    choice[0] = best.fused ? 0 : best.branches;
+    choice[1] = best.grid_pct;
+    choice[2] = (int32_t)(best_ms * 1000.f);
+    choice[3] = best.fused;
+    choice[4] = best.fused_pct;
+  }
   return rc;
 }
