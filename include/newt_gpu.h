@@ -138,10 +138,10 @@ typedef struct newt_gpu_opts {
   int32_t max_worlds;                /* slot capacity */
   uint64_t hbm_budget_bytes;         /* 0 = free HBM at creation minus a reserve */
   int32_t max_contacts;              /* pile worlds: contacts kept per world (0 = sized from the body
-                                      * count, 6 nb + 4 nb np, 64..512); raised to at least 64 and
-                                      * 2 nb.  Contacts past it are dropped in pair order and the
-                                      * world's status gets NEWT_WS_CONTACT_OVERFLOW (newt's contact
-                                      * list grows without bound, world.rs:2476-2515) */
+                                      * count, 6 nb + 4 nb np, 64..512), rounded up to a multiple of
+                                      * 32.  Contacts past it are dropped in pair order and the world's
+                                      * status gets NEWT_WS_CONTACT_OVERFLOW (newt's contact list
+                                      * grows without bound, world.rs:2476-2515) */
 } newt_gpu_opts;
 
 /* Replaces building a `World` (newt/src/world.rs:325). */
@@ -207,6 +207,34 @@ NEWT_API int newt_gpu_sync(newt_gpu_ctx* ctx, int32_t timeout_ms);
 /* Per-world status words (NEWT_WS_*), accumulated since the last clear. */
 NEWT_API int newt_gpu_world_status(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, uint32_t* status,
                           int32_t clear);
+
+/* ---- convex contact queries -------------------------------------------------
+ * newt's general convex route, GJK then EPA (newt/src/contact/ccd.rs:1703-1911,
+ * the path newt takes for mesh pairs), run on the device for arbitrary pairs
+ * of spheres, boxes and capsules.  The step's narrowphase keeps its closed
+ * forms; this entry point is their second formulation (a cross-check) and a
+ * device query for callers.  A pose is position x y z, then quaternion
+ * x y z w; sizes as in newt_geom_desc.  `face_eps` is EPA's face-removal
+ * threshold relative to the pair extent (<= 0: newt's 1e-4; EPA then ends in
+ * newt's shallowest-axis fallback on curved features, and a threshold of
+ * 1e-7 lets it converge there).  Result: hit, path (1 distance GJK, 2 EPA,
+ * 3 EPA fallback), contact point, normal (from B into A), penetration and
+ * the witness points on A and B.  Pairs with another shape get
+ * NEWT_E_UNSUPPORTED_PAIR before anything runs. */
+typedef struct newt_convex_query {
+  int32_t shape_a, shape_b;          /* NEWT_SHAPE_SPHERE | _BOX | _CAPSULE */
+  float pose_a[7], size_a[3];
+  float pose_b[7], size_b[3];
+  float margin;
+} newt_convex_query;
+typedef struct newt_convex_result {
+  int32_t hit, path;
+  float pos[3], normal[3];
+  float penetration;
+  float witness_a[3], witness_b[3];
+} newt_convex_result;
+NEWT_API int newt_gpu_convex_contacts(newt_gpu_ctx* ctx, const newt_convex_query* queries, int32_t n, float face_eps,
+                                      newt_convex_result* out);
 
 /* ---- diagnostics (parity surfaces) -------------------------------------- */
 /* Generalised acceleration of the last step, newt layout (qdot order), nv per

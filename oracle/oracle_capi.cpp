@@ -15,6 +15,7 @@
 #include <thread>
 #include <vector>
 #include "../include/newt_gpu.h"
+#include "newt_ccd.hpp"
 #include "newt_step.hpp"
 
 using namespace oracle;
@@ -220,6 +221,41 @@ int run_one(const newt_model_desc& d, const float* qpos, const float* qvel, cons
 }
 
 }  // namespace
+
+// ---- single-pair narrowphase queries (cross-checks of the contact routes) ----
+// A pose is p xyz then quat x y z w; sizes as in newt_geom_desc; kinds are
+// NEWT_SHAPE_* (sphere, box, capsule for GJK/EPA).
+template <class R> static Pose<R> pose_of(const float* p) {
+  return Pose<R>{Vec3<R>(p[0], p[1], p[2]), Quat<R>(p[3], p[4], p[5], p[6])};
+}
+
+template <class R> static int ccd_pair_t(int ka, const float* pa, const float* sa, int kb, const float* pb,
+                                         const float* sb, float margin, float face_eps, double* out) {
+  const ccd::Shape<R> A{ka, Vec3<R>(pa[0], pa[1], pa[2]), Quat<R>(pa[3], pa[4], pa[5], pa[6]), Vec3<R>(sa[0], sa[1], sa[2])};
+  const ccd::Shape<R> B{kb, Vec3<R>(pb[0], pb[1], pb[2]), Quat<R>(pb[3], pb[4], pb[5], pb[6]), Vec3<R>(sb[0], sb[1], sb[2])};
+  const ccd::Result<R> r = ccd::convex_contact(A, B, (R)margin, face_eps > 0.f ? (R)face_eps : R(1.0e-4));
+  const double v[15] = {r.hit ? 1.0 : 0.0, (double)r.path, (double)r.pos.x, (double)r.pos.y, (double)r.pos.z,
+                        (double)r.n.x, (double)r.n.y, (double)r.n.z, (double)r.pen, (double)r.wa.x, (double)r.wa.y,
+                        (double)r.wa.z, (double)r.wb.x, (double)r.wb.y, (double)r.wb.z};
+  for (int k = 0; k < 15; ++k) out[k] = v[k];
+  return r.hit ? 1 : 0;
+}
+
+template <class R> static int np_pair_t(int ka, const float* pa, const float* sa, int kb, const float* pb,
+                                        const float* sb, float margin, double* out) {
+  Geom<R> a, b;
+  a.shape = ka; b.shape = kb;
+  for (int k = 0; k < 3; ++k) { a.size[k] = sa[k]; b.size[k] = sb[k]; }
+  CBuf<R> buf;
+  if (!try_np(0, a, pose_of<R>(pa), 1, b, pose_of<R>(pb), R(1), (R)margin, R(0), &buf)) return -1;
+  for (int c = 0; c < buf.len; ++c) {
+    const Contact<R>& x = buf.c[c];
+    const double v[7] = {(double)x.pos.x, (double)x.pos.y, (double)x.pos.z, (double)x.n.x, (double)x.n.y,
+                         (double)x.n.z, (double)x.pen};
+    for (int k = 0; k < 7; ++k) out[7 * c + k] = v[k];
+  }
+  return buf.len;
+}
 
 extern "C" {
 
@@ -489,6 +525,29 @@ int oracle_energy(const newt_model_desc* models, int n_worlds, const int* model_
     qo += nq; vo += nv;
   }
   return 0;
+}
+
+// newt's GJK/EPA contact of one pair (newt/src/contact/ccd.rs:1703-1911).
+// face_eps <= 0: newt's EPA face-removal threshold (1e-4 of the pair extent).
+// out (15 doubles): hit, path (1 distance GJK, 2 EPA, 3 EPA fallback), point
+// xyz, normal xyz (from B into A), penetration, witness on A, witness on B.
+int oracle_ccd_pair(int precision, int kind_a, const float* pose_a, const float* size_a, int kind_b,
+                    const float* pose_b, const float* size_b, float margin, float face_eps, double* out) {
+  auto ok = [](int k) { return k == ccd::SPHERE || k == ccd::BOX || k == ccd::CAPSULE; };
+  if (!ok(kind_a) || !ok(kind_b)) return -1;
+  return precision == 0 ? ccd_pair_t<float>(kind_a, pose_a, size_a, kind_b, pose_b, size_b, margin, face_eps, out)
+                        : ccd_pair_t<double>(kind_a, pose_a, size_a, kind_b, pose_b, size_b, margin, face_eps, out);
+}
+
+// The closed-form narrowphase of one pair as the step runs it (newt's
+// dispatch, contact.rs:2509-2587, with the sphere-box extension), without the
+// relabelling: (A, B) must be a routed order.  Up to 4 contacts of 7 doubles
+// (point, normal from B into A, penetration); returns the count, -1 when
+// (A, B) has no route.
+int oracle_np_pair(int precision, int kind_a, const float* pose_a, const float* size_a, int kind_b,
+                   const float* pose_b, const float* size_b, float margin, double* out) {
+  return precision == 0 ? np_pair_t<float>(kind_a, pose_a, size_a, kind_b, pose_b, size_b, margin, out)
+                        : np_pair_t<double>(kind_a, pose_a, size_a, kind_b, pose_b, size_b, margin, out);
 }
 
 // Raw f32 bits of newt's deterministic sin/cos (for the polynomial KATs).

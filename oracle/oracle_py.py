@@ -46,6 +46,10 @@ def lib():
         L.oracle_tree_impulses_ex.restype = C.c_int
         L.oracle_sensors.argtypes = [P, P, P, C.c_int, C.c_int, P, P, P]
         L.oracle_sensors.restype = C.c_int
+        L.oracle_ccd_pair.argtypes = [C.c_int, C.c_int, P, P, C.c_int, P, P, C.c_float, C.c_float, P]
+        L.oracle_ccd_pair.restype = C.c_int
+        L.oracle_np_pair.argtypes = [C.c_int, C.c_int, P, P, C.c_int, P, P, C.c_float, P]
+        L.oracle_np_pair.restype = C.c_int
         L.oracle_contacts.argtypes = [P, P, P, C.c_int, C.c_int, P, P, P]
         L.oracle_impulses.argtypes = [P, P, P, C.c_int, C.c_int, C.c_int, P, P]
         L.oracle_mass_matrix.argtypes = [P, P, C.c_int, P]
@@ -137,6 +141,46 @@ def sensors(packed, index: int, qpos: np.ndarray, qvel: np.ndarray, sens: np.nda
     d = C.cast(C.byref(packed.descs[index]), C.c_void_p)
     lib().oracle_sensors(d, _ptr(qpos), _ptr(qvel), precision, len(sens), _ptr(si), _ptr(sf), _ptr(out))
     return out
+
+
+def _pose7(pose) -> np.ndarray:
+    p = np.ascontiguousarray(pose, dtype=np.float32)
+    assert p.shape == (7,), "pose: position xyz, quaternion x y z w"
+    return p
+
+
+def ccd_pair(kind_a: int, pose_a, size_a, kind_b: int, pose_b, size_b, margin: float = 0.0, precision: int = 1,
+             face_eps: float = 0.0):
+    """newt's GJK/EPA contact of two primitive shapes (sphere, box, capsule).
+    Poses are (x, y, z, qx, qy, qz, qw).  face_eps: EPA's face-removal
+    threshold (0: newt's 1e-4 of the pair extent).  Returns None (no contact)
+    or a dict: path (1 distance GJK, 2 EPA, 3 EPA fallback), pos, normal (from
+    B into A), pen, witness_a, witness_b."""
+    out = np.zeros(15, np.float64)
+    sa = np.ascontiguousarray(size_a, np.float32)
+    sb = np.ascontiguousarray(size_b, np.float32)
+    rc = lib().oracle_ccd_pair(int(precision), int(kind_a), _ptr(_pose7(pose_a)), _ptr(sa), int(kind_b),
+                               _ptr(_pose7(pose_b)), _ptr(sb), C.c_float(margin), C.c_float(face_eps), _ptr(out))
+    if rc < 0:
+        raise ValueError("GJK/EPA takes spheres, boxes and capsules")
+    if rc == 0:
+        return None
+    return {"path": int(out[1]), "pos": out[2:5].copy(), "normal": out[5:8].copy(), "pen": float(out[8]),
+            "witness_a": out[9:12].copy(), "witness_b": out[12:15].copy()}
+
+
+def np_pair(kind_a: int, pose_a, size_a, kind_b: int, pose_b, size_b, margin: float = 0.0,
+            precision: int = 1) -> np.ndarray:
+    """The step's closed-form narrowphase for one routed pair (A, B): an
+    (n, 7) array of point, normal (from B into A), penetration."""
+    out = np.zeros(28, np.float64)
+    sa = np.ascontiguousarray(size_a, np.float32)
+    sb = np.ascontiguousarray(size_b, np.float32)
+    n = lib().oracle_np_pair(int(precision), int(kind_a), _ptr(_pose7(pose_a)), _ptr(sa), int(kind_b),
+                             _ptr(_pose7(pose_b)), _ptr(sb), C.c_float(margin), _ptr(out))
+    if n < 0:
+        raise ValueError("no narrowphase route for this (A, B) order")
+    return out[: 7 * n].reshape(n, 7)
 
 
 def mass_matrix(packed, index: int, q_native: np.ndarray, nv: int, precision: int = 1) -> np.ndarray:

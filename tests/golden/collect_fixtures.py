@@ -1,6 +1,7 @@
 """Copy newt's own golden vectors for the stepping path into tests/golden/.
 
-Runs only where the reference checkout is mounted (never on the GPU machine).
+Runs only where the reference checkout is available (never on the GPU machine):
+    python tests/golden/collect_fixtures.py <newt checkout>/tests
 The files are byte goldens written by newt's test suite (f32 little-endian
 state snapshots, newt/tests/goldens/*.bin) and MuJoCo 3.11.0 FP64 captures in
 newt's NEWTDIF1 format (newt/tests/references/*.bin), plus the scene files
@@ -11,7 +12,9 @@ import os
 import shutil
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/newt/tests"
+if len(sys.argv) != 2:
+    sys.exit("usage: collect_fixtures.py <newt checkout>/tests")
+REF = sys.argv[1]
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 FILES = [

@@ -76,8 +76,9 @@ def test_contact_overflow_is_flagged_and_isolated(built, mode):
         ref.step(400, STEP_PLAIN)  # settle: every body lands on the plane
         settled = [ref.get_state(s, int(b.nq.sum()), int(b.nv.sum())) for s, b in zip(rs, (big, small))]
         cs = [cap.alloc(cap.upload(b)) for b in (big, small)]
-        for s, (q, v) in zip(cs, settled):
-            cap.set_state(s, q, v)
+        for c, r, (q, v) in zip(cs, rs, settled):  # both contexts start from the same host state
+            cap.set_state(c, q, v)
+            ref.set_state(r, q, v)
         cap.step(1, mode)
         ref.step(1, mode)
         st_big, st_small = cap.status(cs[0]), cap.status(cs[1])

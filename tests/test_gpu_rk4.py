@@ -219,15 +219,44 @@ def test_pile_rk4_tracks_newt_goldens(eng, name, qtol, vtol, mode):
     assert all(dq < qtol and dv < vtol for _, dq, dv in errs), errs
 
 
+def _stack_envelope(n_runs=48, nudge=1e-7):
+    """How far newt's own f32 arithmetic lands from newt's stack snapshots
+    when the start positions move by 1e-7 m: the oracle's float mirror (byte-
+    identical to newt unperturbed) over `n_runs` nudged starts, the largest
+    position and velocity distances at each snapshot."""
+    w, q, v, gold, marks = _pile_world("stack")
+    w.integrator = M.INTEGRATOR_RK4
+    nb = len(w.bodies)
+    rng = np.random.default_rng(7)
+    qs = np.tile(np.asarray(q, np.float32).reshape(nb, 7), (n_runs, 1, 1))
+    qs[:, :, :3] += rng.uniform(-nudge, nudge, (n_runs, nb, 3)).astype(np.float32)
+    vs = np.tile(np.asarray(v, np.float32), n_runs)
+    packed = M.PackedModels([w])
+    env, done = [], 0
+    qc, vc = qs.reshape(-1), vs
+    for row, n in enumerate(marks, start=1):
+        qo, vo = oracle_py.run(packed, np.zeros(n_runs, np.int32), qc, vc, None, n - done, precision=0, layout=1,
+                               integrator=0, n_threads=8)
+        done = n
+        qc, vc = qo.astype(np.float32), vo.astype(np.float32)
+        dq = np.abs(qc.reshape(n_runs, nb, 7) - gold[row][None, :, :7]).max()
+        dv = np.abs(vc.reshape(n_runs, nb * 6) - gold[row][:, 7:].reshape(-1)[None, :]).max()
+        env.append((n, float(dq), float(dv)))
+    return env
+
+
 @pytest.mark.parametrize("mode", [STEP_PLAIN, STEP_BATCHED])
 def test_pile_rk4_stack_stays_in_newts_envelope(eng, mode):
-    """Twelve f32 runs of newt's stack from start positions nudged by 1e-7 m
-    land up to 4.1 cm and 0.29 m/s from newt's snapshot at step 1000 (and
-    0.13 m/s at step 50, in the transient).  The GPU run must stay within
-    5 cm of newt's positions at every snapshot and within 0.3 m/s of its
-    velocities once the stack has settled (step 1000)."""
+    """newt's box stack is chaotic: 48 f32 runs of newt's own arithmetic from
+    start positions nudged by 1e-7 m spread up to a few cm and about 0.3 m/s
+    from newt's snapshot at step 1000.  The GPU run must stay within 5 cm, or
+    1.25 times that spread if larger, of newt's positions at every snapshot,
+    and within 1.25 times the velocity spread once the stack has settled
+    (step 1000)."""
     errs = _track(eng, "stack", mode)
-    assert all(dq < 5e-2 for _, dq, _ in errs) and errs[-1][2] < 0.3, errs
+    env = _stack_envelope()
+    ok_q = all(dq < max(5e-2, 1.25 * eq) for (_, dq, _), (_, eq, _) in zip(errs, env))
+    assert ok_q and errs[-1][2] < 1.25 * env[-1][2], (errs, env)
 
 
 def test_pile_rk4_one_step_from_newt_snapshots(eng):

@@ -170,3 +170,60 @@ def test_tree_chain_contact_within_mujoco_windows(eng, solver, name, qtol, vtol)
         worst_v = max(worst_v, np.abs(qv - ref["qvel"][k]).max())
     eng.free(slots)
     assert worst_q <= qtol and worst_v <= vtol, (worst_q, worst_v)
+
+
+def _snake(n_hinges, foot_every=5):
+    """A free root and `n_hinges` hinged links in a line along x, axes
+    alternating z and y, masses alternating 1 and 0.05 kg, sphere feet on
+    every fifth link resting 0.5 mm into the plane; Newton, dt 2e-3."""
+    w = M.WorldModel(dt=0.002, gravity=(0.0, 0.0, -9.81), solver=M.SOLVER_NEWTON, iterations=20)
+    w.add_geom(M.static_plane(friction=0.8))
+    for i in range(n_hinges + 1):
+        m = 1.0 if i % 2 == 0 else 0.05
+        inert = 0.4 * m * 0.03 ** 2 + m * 0.05 ** 2 / 3
+        if i == 0:
+            w.push_link(M.Link(parent=-1, joint=M.JOINT_FREE, mass=m, inertia=M._diag9(inert, inert, inert)))
+        else:
+            ax = (0.0, 0.0, 1.0) if i % 2 else (0.0, 1.0, 0.0)
+            w.push_link(M.Link(parent=i - 1, joint=M.JOINT_HINGE, axis=ax, jp_pos=(0.05, 0.0, 0.0),
+                               jc_pos=(-0.05, 0.0, 0.0), mass=m, inertia=M._diag9(inert, inert, inert),
+                               damping=0.01))
+        if i % foot_every == 0:
+            w.add_geom(M.Geom(shape=M.SHAPE_SPHERE, link=i, size=(0.03, 0.0, 0.0), friction=0.8))
+    rng = np.random.default_rng(n_hinges)
+    qpos = np.zeros(w.nq, np.float32)  # straight, every foot 0.5 mm into the plane
+    qpos[2], qpos[3] = 0.0295, 1.0
+    qvel = rng.normal(0.0, 0.1, w.nv).astype(np.float32)
+    return w, qpos, qvel
+
+
+@pytest.mark.parametrize("n_hinges", [25, 39])
+def test_long_chain_contact_qacc_matches_fp64(eng, n_hinges):
+    """Trees above 32 DoF take one FP64 residual-refinement step of the
+    mass-matrix solve (M + dt B) x = J^T f / dt.  On a 45-DoF snake (refined)
+    and a 31-DoF one (not), lying straight with every foot in contact (8 and
+    6), the contact pairs equal the oracle's, the impulses meet the per-row
+    bar, and the one-step qacc stays within 1e-4 (max-norm relative) of the
+    FP64 oracle's, where newt's own f32 arithmetic is 4.0e-5 and 1.6e-4
+    away."""
+    w, qpos, qvel = _snake(n_hinges)
+    packed = M.PackedModels([w])
+    rp, _ = oracle_py.contacts(packed, 0, qpos, qvel)
+    assert len(rp) == n_hinges // 5 + 1  # every foot
+    slots = eng.alloc(eng.upload(packed))
+    eng.set_state(slots, qpos, qvel)
+    eng.step(1, STEP_PLAIN)
+    qacc = eng.get_qacc(slots, w.nv)
+    st = int(eng.status(slots)[0])
+    gp, _ = eng.contacts(int(slots[0]))
+    g_imp = eng.impulses(int(slots[0]))
+    eng.free(slots)
+    assert np.array_equal(gp, rp)
+    ref_imp, _ = oracle_py.tree_impulses(packed, 0, qpos, qvel, None)
+    imp_err = np.abs(g_imp - ref_imp) / (IMPULSE_RTOL * np.abs(ref_imp) + IMPULSE_FLOOR * np.abs(ref_imp).max())
+    assert imp_err.max() <= 1.0, (w.nv, imp_err.max())
+    _, v64 = oracle_py.run(packed, np.zeros(1, np.int32), qpos, qvel, None, 1, precision=1)
+    ref = (v64 - qvel.astype(np.float64)) / w.dt  # semi-implicit Euler: qdot += qacc dt
+    rel = np.abs(qacc - ref).max() / np.abs(ref).max()
+    assert not st & 0x3, hex(st)
+    assert rel <= 1e-4, (w.nv, rel)

@@ -31,7 +31,7 @@ EXPORTED = [
     "newt_gpu_flush_l2", "newt_gpu_launch_count", "newt_gpu_step_static", "newt_gpu_pile_profile",
     "newt_gpu_tc_profile", "newt_gpu_serve", "newt_gpu_memory", "newt_gpu_autotune",
     "newt_gpu_set_ctrl_stream", "newt_gpu_apply_ctrl", "newt_gpu_read_sensors", "newt_gpu_pile_fused_profile",
-    "newt_gpu_set_launch_choice",
+    "newt_gpu_set_launch_choice", "newt_gpu_convex_contacts",
 ]
 # newt_sensor_desc (include/newt_gpu.h)
 SENSOR_DTYPE = np.dtype([("kind", np.int32), ("on_link", np.int32), ("index", np.int32),
@@ -49,6 +49,13 @@ def sensors(*specs) -> np.ndarray:
         out[i]["local_pos"] = sp[3] if len(sp) > 3 else (0.0, 0.0, 0.0)
         out[i]["local_quat"] = sp[4] if len(sp) > 4 else (0.0, 0.0, 0.0, 1.0)
     return out
+# newt_convex_query / newt_convex_result (include/newt_gpu.h)
+CONVEX_QUERY_DTYPE = np.dtype([("shape_a", np.int32), ("shape_b", np.int32), ("pose_a", np.float32, 7),
+                               ("size_a", np.float32, 3), ("pose_b", np.float32, 7), ("size_b", np.float32, 3),
+                               ("margin", np.float32)])
+CONVEX_RESULT_DTYPE = np.dtype([("hit", np.int32), ("path", np.int32), ("pos", np.float32, 3),
+                                ("normal", np.float32, 3), ("penetration", np.float32),
+                                ("witness_a", np.float32, 3), ("witness_b", np.float32, 3)])
 TC_KERNELS = ["tree_aba_kernel", "tc_k_solve", "tree_integrate_kernel"]
 PILE_KERNELS = ["pile_k_collide", "pile_k_pgs_small<1>", "pile_k_pgs_small<2>", "pile_k_pgs_small<4>",
                 "pile_k_pgs_quad[3]", "pile_k_pgs_quad[4]", "pile_k_pgs_quad[5]", "pile_k_pgs_levels[6]",
@@ -134,6 +141,7 @@ def load_library(path: str = LIB_PATH):
         "newt_gpu_apply_ctrl": ([P], C.c_int),
         "newt_gpu_pile_fused_profile": ([P, P, P], C.c_int),
         "newt_gpu_set_launch_choice": ([P, P], C.c_int),
+        "newt_gpu_convex_contacts": ([P, P, I32, C.c_float, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -300,6 +308,14 @@ class Engine:
         self._ck(self.L.newt_gpu_serve(self.ctx, r.ctypes.data, n, C.byref(opts), C.byref(st)))
         stats = {k: getattr(st, k) for k, _ in ServeStats._fields_}
         return oq, ov, stats, r["admit_s"].copy(), r["done_s"].copy()
+
+    def convex_contacts(self, queries: np.ndarray, face_eps: float = 0.0) -> np.ndarray:
+        """GJK/EPA contacts of sphere/box/capsule pairs on the device
+        (`queries`: CONVEX_QUERY_DTYPE records); CONVEX_RESULT_DTYPE records."""
+        q = np.ascontiguousarray(queries, CONVEX_QUERY_DTYPE)
+        out = np.zeros(len(q), CONVEX_RESULT_DTYPE)
+        self._ck(self.L.newt_gpu_convex_contacts(self.ctx, _p(q), len(q), C.c_float(face_eps), _p(out)))
+        return out
 
     # -- diagnostics ----------------------------------------------------------
     def contacts(self, slot: int, cap: int = 1024):

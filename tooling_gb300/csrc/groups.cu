@@ -85,10 +85,8 @@ static int pile_maxc(int nb, int np) {
 static void pile_rows(HostGroup& g) {
   const int nb = g.size, np = g.np, ng = nb + np;
   g.maxc = pile_maxc(nb, np);
-  if (g.maxc_cap > 0) {  // the context's cap, kept at or above what collide's scratch borrows (64, 2 nb)
-    const int lo = std::max(64, (2 * nb + 31) / 32 * 32);
-    g.maxc = std::min(g.maxc, std::max(lo, (g.maxc_cap + 31) / 32 * 32));
-  }
+  if (g.maxc_cap > 0)  // the context's cap, rounded up to a multiple of 32
+    g.maxc = std::min(g.maxc, (g.maxc_cap + 31) / 32 * 32);
   PileLayout& l = g.lay;
   int r = 0;
   l.mass = r; r += nb;

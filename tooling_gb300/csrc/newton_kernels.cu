@@ -41,7 +41,13 @@
 //     the contact forces (the ABA is linear in the applied forces).
 // FP64: when the FP32 Cholesky of the Newton Hessian has a pivot ratio
 // (max L_ii / min L_ii)^2 above 1e6, the factor and the direction solves are
-// redone in FP64 (status bit NEWT_WS_FP64_FALLBACK).
+// redone in FP64 (status bit NEWT_WS_FP64_FALLBACK).  Trees above 32 DoF get
+// one FP64 residual-refinement step of the mass-matrix solve that turns the
+// contact impulses into accelerations: with x the FP32 solution of
+// M' x = J^T f / dt (M' = M + dt B, factored in FP32), r = J^T f / dt - M' x
+// is formed in FP64 from an FP32 copy of M', the correction solved in FP64
+// with the FP32 factor, and x += that correction (the mixed-precision
+// refinement of the solve newt runs in cholesky_solve, dynamics.rs:630-648).
 #include <algorithm>
 
 #include "../../include/newt_gpu.h"
@@ -113,9 +119,10 @@ NEWT_D float reference_accel(float position, float velocity, float tc, float dr,
 // ---------------------------------------------------------------------------
 struct TcLay {
   int L, nv, ng, maxc, ld;
-  int jv, jw, iw, con, jt, H, LH, LHd, imp, misc, qfc, words;
+  int jv, jw, iw, con, jt, H, LH, LHd, imp, misc, qfc, mc, rd, words;
 };
 NEWT_HD int up4(int n) { return (n + 3) / 4 * 4; }
+constexpr int REFINE_NV = 32;  // DoF above which the mass-matrix solve is refined in FP64
 NEWT_HD TcLay tc_layout(int L, int nv, int ng, int maxc) {
   TcLay t;
   t.L = L; t.nv = nv; t.ng = ng; t.maxc = maxc;
@@ -132,6 +139,8 @@ NEWT_HD TcLay tc_layout(int L, int nv, int ng, int maxc) {
   t.imp = f; f += up4(t.ld);
   t.misc = f; f += 8;  // ncon, nrows, newton iterations
   t.qfc = f; f += up4(nv);  // RK4 worlds: J^T f / dt, held over the integrator's stages
+  t.mc = f; f += nv > REFINE_NV ? up4(nv * nv) : 0;  // trees above REFINE_NV DoF: M' before factoring
+  t.rd = f; f += nv > REFINE_NV ? up4(4 * nv) : 0;   // and two FP64 vectors (right-hand side, residual)
   t.words = (f + 31) / 32 * 32;
   return t;
 }
@@ -261,6 +270,28 @@ NEWT_D void warp_lt_solve(const float* Lf, int n, int ld, float* v, int lane) {
     for (int m = k + 1 + lane; m < n; m += 32) s += Lf[(size_t)k * ld + m] * v[m];
     s = warp_sum(s);
     const float zk = (v[k] - s) / Lf[(size_t)k * ld + k];
+    __syncwarp();
+    if (lane == 0) v[k] = zk;
+  }
+  __syncwarp();
+}
+
+// Solves L L^T z = v in FP64 with the FP32 column-major factor L (FP64
+// vector `v`, in place; forward then backward substitution).
+NEWT_D void warp_llt_solve_mixed(const float* Lf, int n, int ld, double* v, int lane) {
+  for (int k = 0; k < n; ++k) {
+    __syncwarp();
+    const double yk = v[k] / (double)Lf[(size_t)k * ld + k];
+    __syncwarp();
+    if (lane == 0) v[k] = yk;
+    for (int i = k + 1 + lane; i < n; i += 32) v[i] -= (double)Lf[(size_t)k * ld + i] * yk;
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    __syncwarp();
+    double s = 0.0;
+    for (int m = k + 1 + lane; m < n; m += 32) s += (double)Lf[(size_t)k * ld + m] * v[m];
+    s = warp_sumd(s);
+    const double zk = (v[k] - s) / (double)Lf[(size_t)k * ld + k];
     __syncwarp();
     if (lane == 0) v[k] = zk;
   }
@@ -586,6 +617,12 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
     }
   }
   __syncwarp();
+  const bool refine = nv > REFINE_NV;
+  if (refine) {  // M' (lower triangle) for the FP64 residual
+    float* mc = wf + lay.mc;
+    for (int k = lane; k < nv * nv; k += 32) mc[k] = LM[k];
+    __syncwarp();
+  }
   float mn, mx;
   if (!warp_cholesky2(LM, LD, nv, nv, lane)) {
     if (lane == 0) atomicOr(g.status + w, status | NEWT_WS_NOT_PD);
@@ -845,7 +882,33 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
       g.cfrc[(size_t)w * g.cstride + i] = s;
     }
   __syncwarp();
+  double* rhs = refine ? reinterpret_cast<double*>(wf + lay.rd) : nullptr;
+  if (refine)  // J^T f / dt = L (Y f) / dt, in FP64 from the FP32 factor
+    for (int i = lane; i < nv; i += 32) {
+      double s = 0.0;
+      for (int k = 0; k <= i; ++k) s += (double)LM[(size_t)k * nv + i] * (double)vg[k];
+      rhs[i] = s;
+    }
   warp_lt_solve(LM, nv, nv, vg, lane);
+  if (refine) {
+    // r = rhs - M' x in FP64 (M' symmetric, its lower triangle kept), then
+    // M' d = r with the FP32 factor in FP64 arithmetic, x += d
+    const float* mc = wf + lay.mc;
+    double* r = rhs + nv;
+    __syncwarp();
+    for (int i = lane; i < nv; i += 32) {
+      double s = rhs[i];
+      for (int j = 0; j < nv; ++j) {
+        const float mij = i >= j ? mc[(size_t)j * nv + i] : mc[(size_t)i * nv + j];
+        s -= (double)mij * (double)vg[j];
+      }
+      r[i] = s;
+    }
+    __syncwarp();
+    warp_llt_solve_mixed(LM, nv, nv, r, lane);
+    for (int i = lane; i < nv; i += 32) vg[i] = (float)((double)vg[i] + r[i]);
+    __syncwarp();
+  }
   for (int k = lane; k < nv; k += 32) g.qacc[k * cap + w] += vg[k];
   if (lane == 0) {
     wf[lay.misc + 2] = __int_as_float(done_it);

@@ -61,7 +61,8 @@ __host__ __device__ inline WsLay ws_layout(int nb, int np, int maxc) {
   L.nf = (f + 3) / 4 * 4;
   int i = 0;
   L.shape = i; i += nb; L.gent = i; i += L.ng; L.pairs = i; i += 2 * L.pcap; L.bits = i; i += L.ng * L.words;
-  L.ci = i; i += CI * maxc; L.perm = i; i += maxc; L.lcnt = i; i += 33; L.uf = i; i += nb; L.misc = i; i += 4;
+  // perm also holds the broadphase's 64 sort keys and the island masks (2 nb words)
+  L.ci = i; i += CI * maxc; L.perm = i; i += max(maxc, max(64, 2 * nb)); L.lcnt = i; i += 33; L.uf = i; i += nb; L.misc = i; i += 4;
   L.istart = i; i += nb; L.icount = i; i += nb; L.inb = i; i += nb; L.ibstart = i; i += nb; L.ibody = i; i += nb;
   L.blocal = i; i += nb; L.scid = i; i += 2 * maxc; L.sccon = i; i += maxc;
   L.ni = (i + 3) / 4 * 4;
@@ -201,7 +202,7 @@ NEWT_D void collide(const WsLay& L, float* wf, int* wi, int lane) {
     // planes (and unused keys) sort last: only body geoms are swept
     float v0 = (key0 < ng && wi[L.gent + key0] < nb) ? wf[L.aabb + 6 * key0] : INFINITY;
     float v1 = (key1 < ng && wi[L.gent + key1] < nb) ? wf[L.aabb + 6 * key1] : INFINITY;
-    int* order = wi + L.perm;  // borrows the permutation buffer (maxc >= 64)
+    int* order = wi + L.perm;  // borrows the permutation buffer (at least 64 ints)
     // bitonic sort of 64 (value, index) pairs held two per lane
     for (int size = 2; size <= 64; size <<= 1) {
       for (int stride = size >> 1; stride > 0; stride >>= 1) {

@@ -12,10 +12,19 @@
 //                  disjoint bodies) on the warp's eight four-lane groups;
 //   integrate      semi-implicit Euler or RK4 (pile_solver.cuh, unchanged).
 // The state stays in the scratch record between env-steps and goes back to
-// the world record once, after the last one.  Warps take worlds from a queue
-// sorted by size (largest first) with one atomic per world, so a world's
-// env-steps never wait on another world: a slow island delays only its own
-// world, and the GPU stays busy with the others meanwhile.
+// the world record once, after the last one.
+//
+// Scheduling.  One block of GANG warps runs per SM and takes GANG worlds at
+// a time from a device queue; the gang's warps move through each phase of an
+// env-step together (a block barrier after collide and assembly, after the
+// sweeps and after integration), so every warp on the SM executes the same
+// code region and the instruction caches hold it (with warps spread over the
+// whole kernel, instruction fetch was the dominant stall).  The queue is
+// sorted by each world's measured cost from the previous call, most costly
+// first (pile_k_queue_sort, a one-block counting sort at the head of the
+// call), so the worlds of a gang cost about the same (short barrier waits)
+// and the last gangs to start are the cheapest (a short tail).  No world ever
+// waits on another world's env-step.
 //
 // Restates, for FP32 on sm_103a:
 //   newt/src/world.rs:1459-1537   World::step phase order (Euler branch)
@@ -56,9 +65,9 @@ using namespace pile;
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
-constexpr int FW = 4;         // warps (worlds in flight) per block
-constexpr int FB = 4;         // blocks per SM the register budget is sized for
+constexpr int GANG = 16;      // warps (worlds in flight) per block: one block per SM at 128 registers
 constexpr int F_MAXC = 512;   // the largest contact capacity of a pile world
+constexpr int N_BUCKET = 256; // cost classes of the queue sort
 
 // compact row record (floats, 16-byte aligned)
 enum {
@@ -338,121 +347,216 @@ NEWT_D void fused_contact(float* rec, int l, unsigned gm, int nb, float (*acc)[6
 }  // namespace
 
 // ---------------------------------------------------------------------------
-// the kernel: persistent warps over a world queue
+// the queue: worlds sorted by last call's cost, most costly first
+// ---------------------------------------------------------------------------
+// Counting sort by cost class (4 classes per octave of cost); the order
+// inside a class is unspecified, which changes which warp steps a world and
+// never what it computes.  One block.
+__global__ void __launch_bounds__(1024) pile_k_queue_sort(const unsigned* __restrict__ cost, int n,
+                                                          int* __restrict__ queue) {
+  __shared__ int hist[N_BUCKET];
+  auto bucket = [](unsigned c) {
+    const float l = log2f((float)c + 1.f) * 4.f;
+    const int b = (int)l;
+    return b < N_BUCKET ? b : N_BUCKET - 1;
+  };
+  for (int b = threadIdx.x; b < N_BUCKET; b += blockDim.x) hist[b] = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) atomicAdd(&hist[bucket(cost[i])], 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {  // exclusive starts, most costly class first
+    int run = 0;
+    for (int b = N_BUCKET - 1; b >= 0; --b) { const int c = hist[b]; hist[b] = run; run += c; }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) queue[atomicAdd(&hist[bucket(cost[i])], 1)] = i;
+}
+
+// Shared memory of one warp: velocity accumulators (nb + 1 bodies, the last
+// a static side's zero), the level sort (last level per body, level per
+// record, records by level, level starts), each part 16-byte aligned.
+struct WarpSmem {
+  int acc, last, lev, perm, loff, bytes;
+};
+NEWT_HD int up16(int b) { return (b + 15) / 16 * 16; }
+NEWT_HD WarpSmem warp_smem(int nbm, int cm) {
+  WarpSmem w;
+  int o = 0;
+  w.acc = o; o += up16((nbm + 1) * 6 * 4);
+  w.last = o; o += up16((nbm + 1) * 2);
+  w.lev = o; o += up16(cm * 2);
+  w.perm = o; o += up16(cm * 2);
+  w.loff = o; o += up16((cm + 1) * 2);
+  w.bytes = o;
+  return w;
+}
+
+// ---------------------------------------------------------------------------
+// the kernel: gangs of warps over the world queue
 // ---------------------------------------------------------------------------
 // work (nullable): [0] active contacts summed over every world's env-steps,
 // [1] contact-update rounds (a level's groups of eight) summed over sweeps,
-// [2] levels summed over env-steps, [3] worlds stepped.
-__global__ void __launch_bounds__(32 * FW, FB) pile_k_fused(const PileGroupDev* G, const int* wseg, int ng,
-                                                            const int* queue, int n_items, int* counter, int n_steps,
-                                                            unsigned long long* work) {
-  __shared__ float acc_s[FW][NEWT_MAX_BODIES + 1][6];
-  __shared__ short last_s[FW][NEWT_MAX_BODIES + 1];
-  __shared__ short lev_s[FW][F_MAXC];
-  __shared__ short perm_s[FW][F_MAXC];
-  __shared__ short loff_s[FW][F_MAXC + 1];
+// [2] levels summed over env-steps, [3] worlds stepped.  cost (per flat world
+// index): this call's contact-update rounds plus 64 per contact, the sort key
+// of the next call's queue.  nbm / cm: the table's largest body count and
+// contact capacity (they size the shared memory).
+__global__ void __launch_bounds__(32 * GANG, 1) pile_k_fused(const PileGroupDev* G, const int* wseg, int ng,
+                                                             const int* queue, int n_items, int* counter, int n_steps,
+                                                             unsigned long long* work, unsigned* cost, int nbm,
+                                                             int cm) {
+  extern __shared__ __align__(16) unsigned char fsm[];
+  __shared__ int gang_base;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int slot = lane >> 2, l = lane & 3;
   const unsigned gm = 0xFu << (lane & ~3);
-  float(*acc)[6] = acc_s[wib];
-  short* perm = perm_s[wib];
-  short* loff = loff_s[wib];
+  const WarpSmem ws = warp_smem(nbm, cm);
+  unsigned char* mine = fsm + (size_t)wib * ws.bytes;
+  float(*acc)[6] = reinterpret_cast<float(*)[6]>(mine + ws.acc);
+  short* last = reinterpret_cast<short*>(mine + ws.last);
+  short* lev = reinterpret_cast<short*>(mine + ws.lev);
+  short* perm = reinterpret_cast<short*>(mine + ws.perm);
+  short* loff = reinterpret_cast<short*>(mine + ws.loff);
   for (;;) {
-    int item = 0;
-    if (lane == 0) item = atomicAdd(counter, 1);
-    item = __shfl_sync(FULL, item, 0);
-    if (item >= n_items) break;
-    const int t = queue[item];
-    const int gi = find_seg(wseg, ng, t);
-    const PileGroupDev& g = G[gi];
-    const int w = t - wseg[gi];
-    if (w >= g.n || !g.I[(size_t)w * g.lay.istride + g.lay.live]) continue;
-    const WsLay L = ws_layout(g.nb, g.np, g.maxc);
-    float* wf = g.scr + (size_t)w * g.sstride;
-    int* wi = reinterpret_cast<int*>(wf + L.nf);
-    const int iters = g.I[(size_t)w * g.lay.istride + g.lay.iters];
-    const bool rk4 = g.I[(size_t)w * g.lay.istride + g.lay.integ] == NEWT_INTEGRATOR_RK4;
-    ws_load(g, w, L, wf, wi, lane);
+    __syncthreads();  // every warp is done with the previous gang's base
+    if (threadIdx.x == 0) gang_base = atomicAdd(counter, GANG);
+    __syncthreads();
+    const int item = gang_base + wib;
+    if (gang_base >= n_items) break;  // uniform over the block
+    // this warp's world, if any (a gang at the end of the queue is partial)
+    int t = -1;
+    if (item < n_items) t = queue ? queue[item] : item;
+    const PileGroupDev* g = nullptr;
+    int w = 0;
+    if (t >= 0 && t < wseg[ng]) {
+      const int gi = find_seg(wseg, ng, t);
+      g = G + gi;
+      w = t - wseg[gi];
+      if (w >= g->n || !g->I[(size_t)w * g->lay.istride + g->lay.live]) g = nullptr;
+    }
+    const bool have = g != nullptr;  // uniform over the warp
+    WsLay L{};
+    float* wf = nullptr;
+    int* wi = nullptr;
+    int iters = 0;
+    bool rk4 = false;
+    if (have) {
+      L = ws_layout(g->nb, g->np, g->maxc);
+      wf = g->scr + (size_t)w * g->sstride;
+      wi = reinterpret_cast<int*>(wf + L.nf);
+      iters = g->I[(size_t)w * g->lay.istride + g->lay.iters];
+      rk4 = g->I[(size_t)w * g->lay.istride + g->lay.integ] == NEWT_INTEGRATOR_RK4;
+      ws_load(*g, w, L, wf, wi, lane);
+    }
     bool bad = false;
     int overflow = 0;
     unsigned long long n_con = 0, n_rounds = 0, n_lev = 0;
     for (int s = 0; s < n_steps; ++s) {
-      collide(L, wf, wi, lane);
-      overflow |= wi[L.misc + 2];
-      const int nact = min(fused_assemble(L, wf, wi, lane, acc), F_MAXC);
-      const int nlev = fused_levels(L, wf, nact, lane, last_s[wib], lev_s[wib], perm, loff);
-      int rounds = 0;
-      for (int v = 0; v < nlev; ++v) rounds += (loff[v + 1] - loff[v] + 7) >> 3;
-      for (int it = 0; it < iters; ++it)
-        for (int v = 0; v < nlev; ++v) {
-          const int e = loff[v + 1];
-          for (int base = loff[v]; base < e; base += 8) {
-            const int idx = base + slot;
-            if (idx < e) fused_contact(wf + L.sc + FR * perm[idx], l, gm, L.nb, acc);
-            __syncwarp();
+      int nact = 0, nlev = 0;
+      if (have) {
+        collide(L, wf, wi, lane);
+        overflow |= wi[L.misc + 2];
+        nact = min(fused_assemble(L, wf, wi, lane, acc), F_MAXC);
+        nlev = fused_levels(L, wf, nact, lane, last, lev, perm, loff);
+      }
+      __syncthreads();  // the gang leaves collide and assembly together
+      if (have) {
+        int rounds = 0;
+        for (int v = 0; v < nlev; ++v) rounds += (loff[v + 1] - loff[v] + 7) >> 3;
+        for (int it = 0; it < iters; ++it)
+          for (int v = 0; v < nlev; ++v) {
+            const int e = loff[v + 1];
+            for (int base = loff[v]; base < e; base += 8) {
+              const int idx = base + slot;
+              if (idx < e) fused_contact(wf + L.sc + FR * perm[idx], l, gm, L.nb, acc);
+              __syncwarp();
+            }
           }
-        }
-      // velocity changes for the integrator; impulses of the last env-step
-      // back to the contact records (the diagnostics surface)
-      for (int b = lane; b < L.nb; b += 32) {
-        st3(wf + L.dv + 3 * b, v3(acc[b][0], acc[b][1], acc[b][2]));
-        st3(wf + L.dw + 3 * b, v3(acc[b][3], acc[b][4], acc[b][5]));
+        n_con += (unsigned long long)nact;
+        n_rounds += (unsigned long long)rounds * (unsigned long long)iters;
+        n_lev += (unsigned long long)nlev;
       }
-      if (s == n_steps - 1)
-        for (int k = lane; k < nact; k += 32) {
-          const float* rec = wf + L.sc + FR * k;
-          float* cimp = wf + L.con + CF * wi[L.sccon + k] + C_IMP;
-          for (int r = 0; r < 4; ++r) cimp[r] = rec[R_IMP + r];
+      __syncthreads();  // and the sweeps
+      if (have) {
+        // velocity changes for the integrator; impulses of the last env-step
+        // back to the contact records (the diagnostics surface)
+        for (int b = lane; b < L.nb; b += 32) {
+          st3(wf + L.dv + 3 * b, v3(acc[b][0], acc[b][1], acc[b][2]));
+          st3(wf + L.dw + 3 * b, v3(acc[b][3], acc[b][4], acc[b][5]));
         }
-      __syncwarp();
-      bad |= pile_integrate_world(wf, L, rk4, lane);
-      n_con += (unsigned long long)nact;
-      n_rounds += (unsigned long long)rounds * (unsigned long long)iters;
-      n_lev += (unsigned long long)nlev;
-    }
-    ws_store_state(g, w, L, wf, lane);
-    ws_store_diag(g, w, L, wf, wi, lane);
-    if (lane == 0) {
-      unsigned st = 0u;
-      if (overflow) st |= NEWT_WS_CONTACT_OVERFLOW;
-      if (bad) st |= NEWT_WS_NONFINITE;
-      if (st) atomicOr(reinterpret_cast<unsigned*>(g.I + (size_t)w * g.lay.istride + g.lay.status), st);
-      if (work) {
-        atomicAdd(work + 0, n_con);
-        atomicAdd(work + 1, n_rounds);
-        atomicAdd(work + 2, n_lev);
-        atomicAdd(work + 3, 1ull);
+        if (s == n_steps - 1)
+          for (int k = lane; k < nact; k += 32) {
+            const float* rec = wf + L.sc + FR * k;
+            float* cimp = wf + L.con + CF * wi[L.sccon + k] + C_IMP;
+            for (int r = 0; r < 4; ++r) cimp[r] = rec[R_IMP + r];
+          }
+        __syncwarp();
+        bad |= pile_integrate_world(wf, L, rk4, lane);
       }
     }
-    __syncwarp();
+    if (have) {
+      ws_store_state(*g, w, L, wf, lane);
+      ws_store_diag(*g, w, L, wf, wi, lane);
+      if (lane == 0) {
+        unsigned st = 0u;
+        if (overflow) st |= NEWT_WS_CONTACT_OVERFLOW;
+        if (bad) st |= NEWT_WS_NONFINITE;
+        if (st) atomicOr(reinterpret_cast<unsigned*>(g->I + (size_t)w * g->lay.istride + g->lay.status), st);
+        if (cost) cost[t] = (unsigned)min(n_rounds + 64ull * n_con, 0xffffffffull);
+        if (work) {
+          atomicAdd(work + 0, n_con);
+          atomicAdd(work + 1, n_rounds);
+          atomicAdd(work + 2, n_lev);
+          atomicAdd(work + 3, 1ull);
+        }
+      }
+    }
   }
 }
 
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-// Resident blocks of pile_k_fused per SM (outside stream capture).
-extern "C" int newt_pile_fused_blocks_per_sm() {
+// Dynamic shared memory of one block for a table whose largest world has
+// `nbm` bodies and contact capacity `cm`.
+extern "C" size_t newt_pile_fused_smem_bytes(int nbm, int cm) {
+  return (size_t)GANG * warp_smem(nbm, cm).bytes;
+}
+
+// Resident blocks of pile_k_fused per SM for that table (outside stream
+// capture; sets the kernel's dynamic shared memory limit first).
+extern "C" int newt_pile_fused_blocks_per_sm(int nbm, int cm) {
+  const int bytes = (int)newt_pile_fused_smem_bytes(nbm, cm);
+  cudaFuncSetAttribute(pile_k_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   int b = 1;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pile_k_fused, 32 * FW, 0) != cudaSuccess || b < 1) b = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pile_k_fused, 32 * GANG, bytes) != cudaSuccess || b < 1) b = 1;
   return b;
 }
 
-// Worlds per block of the launch (the queue hands out one world per warp).
-extern "C" int newt_pile_fused_warps_per_block() { return FW; }
+// Worlds per block of the launch.
+extern "C" int newt_pile_fused_warps_per_block() { return GANG; }
 
-// Loads the kernel (so a later launch under stream capture creates nothing).
+// Loads the kernels (so a later launch under stream capture creates nothing).
 extern "C" cudaError_t newt_pile_fused_prepare() {
   cudaFuncAttributes a;
-  return cudaFuncGetAttributes(&a, pile_k_fused);
+  cudaError_t e = cudaFuncGetAttributes(&a, pile_k_fused);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, pile_k_queue_sort);
+  return e;
 }
 
-// One launch steps every live world of the table `n_steps` env-steps.
-// `counter` must be zero when the launch starts (the caller clears it on
-// `st` first); `grid` blocks of FW warps pull worlds from `queue`.
-extern "C" void newt_launch_pile_fused(const PileGroupDev* dG, const int* dwseg, int ng, const int* queue,
-                                       int n_items, int* counter, int n_steps, int grid,
-                                       unsigned long long* work, cudaStream_t st) {
-  if (n_items <= 0 || grid <= 0) return;
-  pile_k_fused<<<grid, 32 * FW, 0, st>>>(dG, dwseg, ng, queue, n_items, counter, n_steps, work);
+// One call's launches on `st`: the queue sort by last call's costs (when
+// `cost` and `queue` are given), then the gangs.  `counter` must be zero
+// when the gangs start (the caller clears it on `st` first).  Every live
+// world of the table advances `n_steps` env-steps.
+extern "C" int newt_launch_pile_fused(const PileGroupDev* dG, const int* dwseg, int ng, int* queue, int n_items,
+                                      int* counter, int n_steps, int grid, unsigned long long* work, unsigned* cost,
+                                      int nbm, int cm, cudaStream_t st) {
+  if (n_items <= 0 || grid <= 0) return 0;
+  int launches = 0;
+  if (queue && cost) {
+    pile_k_queue_sort<<<1, 1024, 0, st>>>(cost, n_items, queue);
+    ++launches;
+  }
+  pile_k_fused<<<grid, 32 * GANG, newt_pile_fused_smem_bytes(nbm, cm), st>>>(dG, dwseg, ng, queue, n_items, counter,
+                                                                            n_steps, work, cost, nbm, cm);
+  return launches + 1;
 }

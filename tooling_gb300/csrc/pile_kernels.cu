@@ -118,7 +118,7 @@ NEWT_D void assemble(const WsLay& L, float* wf, int* wi, int lane, int t_world, 
   // an island is named by its smallest body and islands are numbered in that
   // order; bodies keep body order and contacts contact order inside an island
   // (the sweep order of newt's solver)
-  unsigned* clo = reinterpret_cast<unsigned*>(wi + L.perm);  // component mask, low word (maxc >= 2 nb)
+  unsigned* clo = reinterpret_cast<unsigned*>(wi + L.perm);  // component mask, low word (perm holds >= 2 nb)
   unsigned* chi = clo + nb;                                   // high word
   auto comp = [&](int b) { return ((unsigned long long)chi[b] << 32) | clo[b]; };
   auto active = [&](int c) { return wf[L.con + CF * c + C_ACT] != 0.f; };

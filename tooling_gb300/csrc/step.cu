@@ -29,11 +29,11 @@ extern "C" int newt_launch_pile_step(const PileGroupDev* dG, const int* dwseg, i
                                      int total_slots, int* lists, int write_diag, cudaStream_t st,
                                      const cudaStream_t* side, cudaEvent_t* ev, cudaEvent_t* kev);
 extern "C" void newt_pile_init();
-extern "C" int newt_pile_fused_blocks_per_sm();
+extern "C" int newt_pile_fused_blocks_per_sm(int nbm, int cm);
 extern "C" int newt_pile_fused_warps_per_block();
-extern "C" void newt_launch_pile_fused(const PileGroupDev* dG, const int* dwseg, int ng, const int* queue,
-                                       int n_items, int* counter, int n_steps, int grid,
-                                       unsigned long long* work, cudaStream_t st);
+extern "C" int newt_launch_pile_fused(const PileGroupDev* dG, const int* dwseg, int ng, int* queue, int n_items,
+                                      int* counter, int n_steps, int grid, unsigned long long* work, unsigned* cost,
+                                      int nbm, int cm, cudaStream_t st);
 extern "C" int newt_tc_prepare(newt_gpu_ctx* ctx, HostGroup* g, int n_steps);
 extern "C" int newt_tc_launch(newt_gpu_ctx* ctx, HostGroup* g, int n_steps, cudaStream_t st, bool capturing);
 
@@ -243,7 +243,9 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
   // queue (groups by size, largest first)
   PileTable ft;
   int* fcounter = nullptr;
-  int fgrid = 0;
+  int* fqueue = nullptr;
+  unsigned* fcost = nullptr;
+  int fgrid = 0, fnbm = 0, fcm = 0;
   const int nbr = fused ? 0
                         : (ctx->tune_branches > 0 ? std::min(ctx->tune_branches, newt_gpu_ctx::PILE_BRANCHES)
                                                   : (int)std::max<long>(1, std::min<long>(2, pile_worlds / 4096)));
@@ -256,12 +258,18 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
     int rc = build_pile_table(ctx, piles, ft, bufs, 0, 1);
     if (rc != NEWT_OK) return rc;
     CKS(cudaMalloc(&fcounter, sizeof(int)));
+    CKS(cudaMalloc(&fqueue, sizeof(int) * (size_t)ft.worlds));
+    CKS(cudaMalloc(&fcost, sizeof(unsigned) * (size_t)ft.worlds));
+    CKS(cudaMemset(fcost, 0, sizeof(unsigned) * (size_t)ft.worlds));  // first call: any order
     bufs.push_back(fcounter);
+    bufs.push_back(fqueue);
+    bufs.push_back(fcost);
     if (!ctx->fused_work) CKS(cudaMalloc(&ctx->fused_work, 4 * sizeof(unsigned long long)));
     if (!ctx->fkev[0])
       for (int k = 0; k < 2; ++k) CKS(cudaEventCreate(&ctx->fkev[k]));
+    for (HostGroup* g : piles) { fnbm = std::max(fnbm, g->size); fcm = std::max(fcm, g->maxc); }
     const int wpb = newt_pile_fused_warps_per_block();
-    const int full = newt_pile_fused_blocks_per_sm() * sm_count(ctx);
+    const int full = newt_pile_fused_blocks_per_sm(fnbm, fcm) * sm_count(ctx);
     fgrid = std::min((ft.worlds + wpb - 1) / wpb, std::max(1, full * ctx->tune_fused_pct / 100));
   }
   for (int b = 0; b < nbr; ++b) {
@@ -315,11 +323,11 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
     cudaMemsetAsync(fcounter, 0, sizeof(int), fs);
     cudaMemsetAsync(ctx->fused_work, 0, 4 * sizeof(unsigned long long), fs);
     if (ctx->profile) cudaEventRecordWithFlags(ctx->fkev[0], fs, cudaEventRecordExternal);
-    newt_launch_pile_fused(ft.dG, ft.dseg, ft.ng, nullptr, ft.worlds, fcounter, n_steps, fgrid, ctx->fused_work, fs);
+    fused_launches = newt_launch_pile_fused(ft.dG, ft.dseg, ft.ng, fqueue, ft.worlds, fcounter, n_steps, fgrid,
+                                            ctx->fused_work, fcost, fnbm, fcm, fs);
     if (ctx->profile) cudaEventRecordWithFlags(ctx->fkev[1], fs, cudaEventRecordExternal);
     cudaEventRecord(ctx->pbe[0][4], fs);
     cudaStreamWaitEvent(ctx->stream, ctx->pbe[0][4], 0);
-    fused_launches = 1;
   }
   for (int b = 0; b < nbr; ++b) {
     if (pts[b].ng == 0) continue;
