@@ -27,6 +27,19 @@ template <class R> Deriv<R> evaluate(const Body<R>& s, Vec3<R> g, Vec3<R> f, Vec
   return {dlin, dang};
 }
 
+// The free-body constraint solve newt's solver mode selects (world.rs:1705-1817):
+// PGS (solve_free_bodies_diag_mode) or the dense Newton solve
+// (solve_free_bodies_newton, solver.rs:572 -> :1295-1407).
+template <class R> void solve_free_bodies(const World<R>& w, const std::vector<Contact<R>>& contacts,
+                                          std::vector<Wrench<R>>& ext) {
+  if (w.solver_mode == M_NEWTON) {
+    if (!solve_free_bodies_newton(w.bodies, w.geoms, contacts, w.gravity, w.dt, w.iterations, ext))
+      throw std::runtime_error("Newton free-body solve failed: the Hessian is not positive definite");
+  } else {
+    solve_free_bodies_pgs(w.bodies, w.geoms, contacts, w.gravity, w.dt, w.iterations, ext);
+  }
+}
+
 // step_bodies (world.rs:1705-1788): the solver wrenches are computed once at
 // the start state and held over the four stages; stage states start from s0
 // (advance_all, world.rs:3258-3271) and keep their orientations unnormalised.
@@ -34,7 +47,7 @@ template <class R> void World<R>::step_bodies_rk4(bool solver, const std::vector
   const size_t n = bodies.size();
   std::vector<Wrench<R>> ext(n, Wrench<R>{Vec3<R>(), Vec3<R>()});
   if (solver) {
-    solve_free_bodies_pgs(bodies, geoms, free_contacts, gravity, dt, iterations, ext);
+    solve_free_bodies(*this, free_contacts, ext);
     for (size_t i = 0; i < n; ++i) { ext[i].f += tree_body_wrenches[i].f; ext[i].t += tree_body_wrenches[i].t; }
   }
   struct K { Vec3<R> dp, dv; Quat<R> dq; Vec3<R> dw; };
@@ -119,7 +132,7 @@ template <class R> void World<R>::step() {
   // step_bodies_euler (world.rs:1790-1817)
   std::vector<Wrench<R>> ext(bodies.size(), Wrench<R>{Vec3<R>(), Vec3<R>()});
   if (solver) {
-    solve_free_bodies_pgs(bodies, geoms, free_contacts, gravity, dt, iterations, ext);
+    solve_free_bodies(*this, free_contacts, ext);
     for (size_t i = 0; i < bodies.size(); ++i) { ext[i].f += tree_body_wrenches[i].f; ext[i].t += tree_body_wrenches[i].t; }
   }
   for (size_t i = 0; i < bodies.size(); ++i) {

@@ -253,6 +253,47 @@ bool newton_solve(const std::vector<R>& H, const std::vector<R>& b, const std::v
   return true;
 }
 
+// solve_free_body_newton_impulses (solver.rs:1295-1407) for pyramidal
+// condim-3 and condim-1 contacts between free bodies: the dense response
+// matrix (column j holds every row's residual after a unit impulse on row
+// j, solver.rs:1303-1316), H = A + diag(R), and NewtonSystem::solve with a
+// non-negative projection on every facet row and normal row, at most
+// max(iterations, 1) iterations, cost tolerance 1e-7.  Returns false when H
+// is not positive definite (newt panics there).
+template <class R>
+bool solve_free_bodies_newton(const std::vector<Body<R>>& bodies, const std::vector<Geom<R>>& geoms,
+                              const std::vector<Contact<R>>& contacts, Vec3<R> gravity, R dt, int iterations,
+                              std::vector<Wrench<R>>& wrenches, std::vector<R>* impulses_out = nullptr,
+                              std::vector<int>* row_contact_out = nullptr) {
+  const int nb = (int)bodies.size();
+  wrenches.assign(nb, Wrench<R>{Vec3<R>(), Vec3<R>()});
+  if (impulses_out) impulses_out->clear();
+  if (row_contact_out) row_contact_out->clear();
+  if (contacts.empty() || dt <= R(0)) return true;
+  FreeSystem<R> sys;
+  assemble_free_rows(bodies, geoms, contacts, gravity, dt, sys);
+  const int n = (int)sys.rows.size();
+  if (n == 0) return true;
+  std::vector<R> H((size_t)n * n, R(0));
+  std::vector<BDelta<R>> resp(nb);
+  for (int j = 0; j < n; ++j) {
+    for (auto& d : resp) d = BDelta<R>{Vec3<R>(), Vec3<R>()};
+    apply_impulse(sys.rows[j], R(1), resp, bodies, sys.iinv);
+    for (int i = 0; i < n; ++i) H[(size_t)i * n + j] = row_residual(sys.rows[i], resp, bodies);
+  }
+  for (int i = 0; i < n; ++i) H[(size_t)i * n + i] += sys.rows[i].reg;
+  std::vector<int> nonneg;
+  for (const FreePC<R>& pc : sys.pcs)
+    for (int k = 0; k < (pc.condim == 3 ? 4 : 1); ++k) nonneg.push_back(pc.start + k);
+  std::vector<R> bias(n), imp;
+  for (int i = 0; i < n; ++i) bias[i] = sys.rows[i].bias;
+  if (!newton_solve(H, bias, nonneg, iterations > 1 ? iterations : 1, R(1e-7), imp)) return false;
+  free_row_wrenches(sys, imp, dt, wrenches);
+  if (impulses_out) *impulses_out = imp;
+  if (row_contact_out) free_row_contacts(sys, row_contact_out);
+  return true;
+}
+
 // solve_tree_contacts (solver.rs:2805-3366).  `implicit`: the Euler form
 // (factors of M + dt*B, free velocity from the implicit ABA); otherwise the
 // RK4 form (factors of M, explicit ABA).  Writes w.tree_qfrc and

@@ -647,21 +647,24 @@ template <class R> R point_dir_velocity(const std::vector<Body<R>>& bodies, int 
 
 struct PgsContactInfo { int start_row; int condim; int contact_index; };
 
-// Returns per-body (force, torque) wrenches; optionally the per-row impulses
-// and row metadata (for the impulse-parity tests).
-template <class R>
-void solve_free_bodies_pgs(const std::vector<Body<R>>& bodies, const std::vector<Geom<R>>& geoms,
-                           const std::vector<Contact<R>>& contacts, Vec3<R> gravity, R dt, int iterations,
-                           std::vector<Wrench<R>>& wrenches, std::vector<R>* impulses_out = nullptr,
-                           std::vector<int>* row_contact_out = nullptr) {
-  const int nb = (int)bodies.size();
-  wrenches.assign(nb, Wrench<R>{Vec3<R>(), Vec3<R>()});
-  if (impulses_out) impulses_out->clear();
-  if (row_contact_out) row_contact_out->clear();
-  if (contacts.empty() || dt <= R(0)) return;
+// Rows of the free-body contact system (solver.rs:752-1061): per active
+// contact its facet rows (pyramidal condim 3) or normal row (condim 1), with
+// regularisation, diagonal and bias; `pcs` keeps the contact blocks.
+template <class R> struct FreePC { int ci, start, condim; SolRef<R> sr; SolImp<R> si; R pen, mu; R h01a, h01b; };
+template <class R> struct FreeSystem {
   std::vector<Row<R>> rows;
-  struct PC { int ci, start, condim; SolRef<R> sr; SolImp<R> si; R pen, mu; R h01a, h01b; };
-  std::vector<PC> pcs;
+  std::vector<FreePC<R>> pcs;
+  std::vector<Mat3<R>> iinv;
+};
+
+template <class R>
+void assemble_free_rows(const std::vector<Body<R>>& bodies, const std::vector<Geom<R>>& geoms,
+                        const std::vector<Contact<R>>& contacts, Vec3<R> gravity, R dt, FreeSystem<R>& sys) {
+  const int nb = (int)bodies.size();
+  std::vector<Row<R>>& rows = sys.rows;
+  std::vector<FreePC<R>>& pcs = sys.pcs;
+  rows.clear();
+  pcs.clear();
   std::vector<Vec3<R>> dvfree(nb);
   for (int i = 0; i < nb; ++i) dvfree[i] = gravity * dt;
   for (int ci = 0; ci < (int)contacts.size(); ++ci) {
@@ -690,11 +693,11 @@ void solve_free_bodies_pgs(const std::vector<Body<R>>& bodies, const std::vector
     }
     pcs.push_back({ci, start, condim, sr, si, pen_active, mu, R(0), R(0)});
   }
-  const int nrows = (int)rows.size();
-  if (nrows == 0) return;
-  std::vector<Mat3<R>> iinv(nb);
+  if (rows.empty()) return;
+  sys.iinv.resize(nb);
+  std::vector<Mat3<R>>& iinv = sys.iinv;
   for (int i = 0; i < nb; ++i) { Mat3<R> r = bodies[i].ori.to_mat3(); iinv[i] = r * bodies[i].inertia_inv * r.transpose(); }
-  for (PC& pc : pcs) {
+  for (FreePC<R>& pc : pcs) {
     int nr = pc.condim == 3 ? 4 : 1;
     for (int k = 0; k < nr; ++k) {
       Row<R>& r = rows[pc.start + k];
@@ -726,8 +729,47 @@ void solve_free_bodies_pgs(const std::vector<Body<R>>& bodies, const std::vector
       r.bias = dvf - aref * dt;
     }
   }
+}
+
+// Per-body wrenches (impulse / dt) from the rows' impulses (solver.rs:1204-1234).
+template <class R>
+void free_row_wrenches(const FreeSystem<R>& sys, const std::vector<R>& imp, R dt, std::vector<Wrench<R>>& wrenches) {
+  for (int ri = 0; ri < (int)sys.rows.size(); ++ri) {
+    R f = imp[ri];
+    if (f == R(0)) continue;
+    const Row<R>& r = sys.rows[ri];
+    Vec3<R> fa = r.dir * (f / dt);
+    if (r.ba >= 0) { wrenches[r.ba].f += fa; wrenches[r.ba].t += r.arm_a.cross(fa); }
+    if (r.bb >= 0) { Vec3<R> fb = -fa; wrenches[r.bb].f += fb; wrenches[r.bb].t += r.arm_b.cross(fb); }
+  }
+}
+
+template <class R> void free_row_contacts(const FreeSystem<R>& sys, std::vector<int>* row_contact_out) {
+  row_contact_out->assign(sys.rows.size(), -1);
+  for (const FreePC<R>& pc : sys.pcs)
+    for (int k = 0; k < (pc.condim == 3 ? 4 : 1); ++k) (*row_contact_out)[pc.start + k] = pc.ci;
+}
+
+// Returns per-body (force, torque) wrenches; optionally the per-row impulses
+// and row metadata (for the impulse-parity tests).
+template <class R>
+void solve_free_bodies_pgs(const std::vector<Body<R>>& bodies, const std::vector<Geom<R>>& geoms,
+                           const std::vector<Contact<R>>& contacts, Vec3<R> gravity, R dt, int iterations,
+                           std::vector<Wrench<R>>& wrenches, std::vector<R>* impulses_out = nullptr,
+                           std::vector<int>* row_contact_out = nullptr) {
+  const int nb = (int)bodies.size();
+  wrenches.assign(nb, Wrench<R>{Vec3<R>(), Vec3<R>()});
+  if (impulses_out) impulses_out->clear();
+  if (row_contact_out) row_contact_out->clear();
+  if (contacts.empty() || dt <= R(0)) return;
+  FreeSystem<R> sys;
+  assemble_free_rows(bodies, geoms, contacts, gravity, dt, sys);
+  std::vector<Row<R>>& rows = sys.rows;
+  const std::vector<Mat3<R>>& iinv = sys.iinv;
+  const int nrows = (int)rows.size();
+  if (nrows == 0) return;
   std::vector<BDelta<R>> scratch(nb);
-  for (PC& pc : pcs) {
+  for (FreePC<R>& pc : sys.pcs) {
     if (pc.condim != 3) continue;
     for (int pair = 0; pair < 2; ++pair) {
       const Row<R>& ri = rows[pc.start + 2 * pair];
@@ -771,24 +813,14 @@ void solve_free_bodies_pgs(const std::vector<Body<R>>& bodies, const std::vector
     apply_impulse(rows[rj], aj, bd, bodies, iinv);
   };
   for (int it = 0; it < iterations; ++it) {
-    for (const PC& pc : pcs) {
+    for (const FreePC<R>& pc : sys.pcs) {
       step_nonneg(pc.start);
       if (pc.condim == 3) { step_pair(pc.start, pc.h01a); step_pair(pc.start + 2, pc.h01b); }
     }
   }
-  for (int ri = 0; ri < nrows; ++ri) {
-    R f = imp[ri];
-    if (f == R(0)) continue;
-    const Row<R>& r = rows[ri];
-    Vec3<R> fa = r.dir * (f / dt);
-    if (r.ba >= 0) { wrenches[r.ba].f += fa; wrenches[r.ba].t += r.arm_a.cross(fa); }
-    if (r.bb >= 0) { Vec3<R> fb = -fa; wrenches[r.bb].f += fb; wrenches[r.bb].t += r.arm_b.cross(fb); }
-  }
+  free_row_wrenches(sys, imp, dt, wrenches);
   if (impulses_out) *impulses_out = imp;
-  if (row_contact_out) {
-    row_contact_out->assign(nrows, -1);
-    for (const PC& pc : pcs) for (int k = 0; k < (pc.condim == 3 ? 4 : 1); ++k) (*row_contact_out)[pc.start + k] = pc.ci;
-  }
+  if (row_contact_out) free_row_contacts(sys, row_contact_out);
 }
 
 // --------------------------------------------------------------------------

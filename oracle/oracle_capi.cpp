@@ -472,7 +472,12 @@ int oracle_impulses(const newt_model_desc* d, const float* qpos, const float* qv
     w.detect_contacts(cs);
     std::vector<Wrench<R>> wr;
     std::vector<R> imp;
-    solve_free_bodies_pgs(w.bodies, w.geoms, cs, w.gravity, w.dt, iterations > 0 ? iterations : w.iterations, wr, &imp);
+    const int its = iterations > 0 ? iterations : w.iterations;
+    if (w.solver_mode == M_NEWTON) {
+      if (!solve_free_bodies_newton(w.bodies, w.geoms, cs, w.gravity, w.dt, its, wr, &imp)) imp.clear();
+    } else {
+      solve_free_bodies_pgs(w.bodies, w.geoms, cs, w.gravity, w.dt, its, wr, &imp);
+    }
     *n_out = (int)imp.size();
     for (int i = 0; i < (int)imp.size() && i < cap; ++i) impulses[i] = imp[i];
   };

@@ -29,6 +29,7 @@ FILES = [
     "goldens/solver_stack.bin",
     "goldens/solver_incline.bin",
     "goldens/solver_newton_stack.bin",
+    "goldens/solver_newton_incline.bin",
     "goldens/solver_tree.bin",
     "goldens/solver_newton_tree.bin",
     "references/double_pendulum_euler.bin",

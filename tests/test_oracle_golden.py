@@ -56,14 +56,15 @@ def test_integrator_rk4_golden_is_byte_identical():
     assert got.tobytes() == gold.tobytes(), np.abs(got - gold).max()
 
 
-def _solver_box_scene(name):
-    """newt/tests/solver_golden.rs:27-79: the PGS stack (three unit boxes with
+def _solver_box_scene(name, solver=M.SOLVER_PGS):
+    """newt/tests/solver_golden.rs:27-91: the stack (three unit boxes with
     1 cm x offsets) and the incline (one asymmetric box under tilted gravity),
     World::new() defaults (RK4, pyramidal cone), solref (0.05, 1.5) on every
-    geom.  Returns (model, qpos, qvel) in newt's layout."""
+    geom, PGS or (newton_stack_scene, newton_incline_scene) Newton.  Returns
+    (model, qpos, qvel) in newt's layout."""
     sr = (0.05, 1.5)
     if name == "stack":
-        w = M.WorldModel(dt=0.005, gravity=(0.0, 0.0, -9.81), solver=M.SOLVER_PGS, iterations=30)
+        w = M.WorldModel(dt=0.005, gravity=(0.0, 0.0, -9.81), solver=solver, iterations=30)
         fric, halves = 0.8, [(0.25, 0.25, 0.25)] * 3
         poses = [(f32(0.01) * f32(k), 0.0, f32(0.25) + f32(0.5) * f32(k)) for k in range(3)]
     else:
@@ -72,7 +73,7 @@ def _solver_box_scene(name):
         g = f32(9.81)
         gz = -(g * f32(L.oracle_newt_cos(float(ang))))
         w = M.WorldModel(dt=0.005, gravity=(float(g * f32(L.oracle_newt_sin(float(ang)))), 0.0, float(gz)),
-                         solver=M.SOLVER_PGS, iterations=30)
+                         solver=solver, iterations=30)
         fric, halves, poses = 0.5, [(0.2, 0.21, 0.19)], [(0.01, 0.0, 0.2)]
     plane = M.static_plane(friction=fric)
     plane.solref = sr
@@ -86,13 +87,15 @@ def _solver_box_scene(name):
     return w, np.array(qpos, np.float32), np.array(qvel, np.float32)
 
 
+@pytest.mark.parametrize("solver,file", [(M.SOLVER_PGS, ""), (M.SOLVER_NEWTON, "newton_")])
 @pytest.mark.parametrize("name", ["stack", "incline"])
-def test_solver_rk4_zoh_goldens_are_byte_identical(name):
-    """newt/tests/solver_golden.rs:164-244: free-body PGS solved once per step
-    and held over the RK4 stages, snapshots after 0, 50, 200 and 1000 steps."""
-    w, qpos, qvel = _solver_box_scene(name)
+def test_solver_rk4_zoh_goldens_are_byte_identical(name, solver, file):
+    """newt/tests/solver_golden.rs:164-258: free-body PGS, or the dense
+    free-body Newton solve, solved once per step and held over the RK4
+    stages, snapshots after 0, 50, 200 and 1000 steps."""
+    w, qpos, qvel = _solver_box_scene(name, solver)
     nb = len(w.bodies)
-    gold = _read_f32(f"solver_{name}.bin").reshape(4, nb, 13)
+    gold = _read_f32(f"solver_{file}{name}.bin").reshape(4, nb, 13)
     got = [np.concatenate([qpos.reshape(nb, 7), qvel.reshape(nb, 6)], axis=1)]
     packed = M.PackedModels([w])
     for n in (50, 200, 1000):

@@ -349,15 +349,16 @@ class Engine:
         worlds (their state is left unchanged)."""
         c = np.zeros(5, np.int32)
         self._ck(self.L.newt_gpu_autotune(self.ctx, int(n_steps), _p(c)))
-        return {"pile_persistent": bool(c[3]), "persistent_grid_pct": int(c[4]), "pile_branches": int(c[0]),
+        return {"pile_persistent": bool(c[3]), "persistent_shape": int(c[4]), "pile_branches": int(c[0]),
                 "tree_grid_pct": int(c[1]), "best_ms": c[2] / 1000.0}
 
-    def set_launch_choice(self, persistent: bool = True, persistent_grid_pct: int = 100, pile_branches: int = 0,
+    def set_launch_choice(self, persistent: bool = True, persistent_shape: int = 1, pile_branches: int = 0,
                           tree_grid_pct: int = 100):
         """Pin the batched step's launch choices (what autotune() would pick):
-        piles in the world-persistent launch, or in the island-class pipeline
-        with `pile_branches` world-range branches (0: by world count)."""
-        c = np.array([pile_branches, tree_grid_pct, 0, int(bool(persistent)), persistent_grid_pct], np.int32)
+        piles in the world-persistent launch of shape `persistent_shape`, or
+        in the island-class pipeline with `pile_branches` world-range
+        branches (0: by world count)."""
+        c = np.array([pile_branches, tree_grid_pct, 0, int(bool(persistent)), persistent_shape], np.int32)
         self._ck(self.L.newt_gpu_set_launch_choice(self.ctx, _p(c)))
 
     def memory(self):

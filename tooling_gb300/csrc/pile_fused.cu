@@ -65,7 +65,8 @@ using namespace pile;
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
-constexpr int GANG = 16;      // warps (worlds in flight) per block: one block per SM at 128 registers
+// gang sizes (warps per block, one block per SM): 16 warps run at 128
+// registers (spilling in the sweeps), 12 at 168 and 8 at 255 without
 constexpr int F_MAXC = 512;   // the largest contact capacity of a pile world
 constexpr int N_BUCKET = 256; // cost classes of the queue sort
 
@@ -392,6 +393,47 @@ NEWT_HD WarpSmem warp_smem(int nbm, int cm) {
 }
 
 // ---------------------------------------------------------------------------
+// the phases of one env-step around the sweeps, out of line: each rebuilds
+// the world's scratch layout itself, so the sweep loop keeps only a few
+// registers live across them
+// ---------------------------------------------------------------------------
+// collide, assemble and levels; returns (active contacts, levels) and ORs
+// the contact-overflow flag into *overflow
+__device__ __noinline__ int2 fused_prepare(const PileGroupDev* g, int w, int lane, float (*acc)[6], short* last,
+                                           short* lev, short* perm, short* loff, int* overflow) {
+  const WsLay L = ws_layout(g->nb, g->np, g->maxc);
+  float* wf = g->scr + (size_t)w * g->sstride;
+  int* wi = reinterpret_cast<int*>(wf + L.nf);
+  collide(L, wf, wi, lane);
+  *overflow |= wi[L.misc + 2];
+  const int nact = min(fused_assemble(L, wf, wi, lane, acc), F_MAXC);
+  const int nlev = fused_levels(L, wf, nact, lane, last, lev, perm, loff);
+  return make_int2(nact, nlev);
+}
+
+// the sweeps' velocity changes to the integrator, the impulses of the last
+// env-step back to the contact records (the diagnostics surface), then the
+// integration; returns whether a body went non-finite
+__device__ __noinline__ bool fused_finish(const PileGroupDev* g, int w, int lane, float (*acc)[6], int nact,
+                                          bool last_step, bool rk4) {
+  const WsLay L = ws_layout(g->nb, g->np, g->maxc);
+  float* wf = g->scr + (size_t)w * g->sstride;
+  const int* wi = reinterpret_cast<const int*>(wf + L.nf);
+  for (int b = lane; b < L.nb; b += 32) {
+    st3(wf + L.dv + 3 * b, v3(acc[b][0], acc[b][1], acc[b][2]));
+    st3(wf + L.dw + 3 * b, v3(acc[b][3], acc[b][4], acc[b][5]));
+  }
+  if (last_step)
+    for (int k = lane; k < nact; k += 32) {
+      const float* rec = wf + L.sc + FR * k;
+      float* cimp = wf + L.con + CF * wi[L.sccon + k] + C_IMP;
+      for (int r = 0; r < 4; ++r) cimp[r] = rec[R_IMP + r];
+    }
+  __syncwarp();
+  return pile_integrate_world(wf, L, rk4, lane);
+}
+
+// ---------------------------------------------------------------------------
 // the kernel: gangs of warps over the world queue
 // ---------------------------------------------------------------------------
 // work (nullable): [0] active contacts summed over every world's env-steps,
@@ -400,6 +442,9 @@ NEWT_HD WarpSmem warp_smem(int nbm, int cm) {
 // index): this call's contact-update rounds plus 64 per contact, the sort key
 // of the next call's queue.  nbm / cm: the table's largest body count and
 // contact capacity (they size the shared memory).
+// GANG: warps per block; MID: a block barrier between assembly and the
+// sweeps as well as after integration (otherwise only after integration).
+template <int GANG, bool MID>
 __global__ void __launch_bounds__(32 * GANG, 1) pile_k_fused(const PileGroupDev* G, const int* wseg, int ng,
                                                              const int* queue, int n_items, int* counter, int n_steps,
                                                              unsigned long long* work, unsigned* cost, int nbm,
@@ -434,32 +479,27 @@ __global__ void __launch_bounds__(32 * GANG, 1) pile_k_fused(const PileGroupDev*
       if (w >= g->n || !g->I[(size_t)w * g->lay.istride + g->lay.live]) g = nullptr;
     }
     const bool have = g != nullptr;  // uniform over the warp
-    WsLay L{};
-    float* wf = nullptr;
-    int* wi = nullptr;
-    int iters = 0;
+    float* sc = nullptr;  // the world's row records
+    int nb = 0, iters = 0;
     bool rk4 = false;
     if (have) {
-      L = ws_layout(g->nb, g->np, g->maxc);
-      wf = g->scr + (size_t)w * g->sstride;
-      wi = reinterpret_cast<int*>(wf + L.nf);
+      const WsLay L = ws_layout(g->nb, g->np, g->maxc);
+      float* wf = g->scr + (size_t)w * g->sstride;
+      sc = wf + L.sc;
+      nb = g->nb;
       iters = g->I[(size_t)w * g->lay.istride + g->lay.iters];
       rk4 = g->I[(size_t)w * g->lay.istride + g->lay.integ] == NEWT_INTEGRATOR_RK4;
-      ws_load(*g, w, L, wf, wi, lane);
+      ws_load(*g, w, L, wf, reinterpret_cast<int*>(wf + L.nf), lane);
     }
     bool bad = false;
     int overflow = 0;
     unsigned long long n_con = 0, n_rounds = 0, n_lev = 0;
     for (int s = 0; s < n_steps; ++s) {
-      int nact = 0, nlev = 0;
+      int2 nn = make_int2(0, 0);
+      if (have) nn = fused_prepare(g, w, lane, acc, last, lev, perm, loff, &overflow);
+      if (MID) __syncthreads();  // the gang leaves collide and assembly together
       if (have) {
-        collide(L, wf, wi, lane);
-        overflow |= wi[L.misc + 2];
-        nact = min(fused_assemble(L, wf, wi, lane, acc), F_MAXC);
-        nlev = fused_levels(L, wf, nact, lane, last, lev, perm, loff);
-      }
-      __syncthreads();  // the gang leaves collide and assembly together
-      if (have) {
+        const int nlev = nn.y;
         int rounds = 0;
         for (int v = 0; v < nlev; ++v) rounds += (loff[v + 1] - loff[v] + 7) >> 3;
         for (int it = 0; it < iters; ++it)
@@ -467,35 +507,23 @@ __global__ void __launch_bounds__(32 * GANG, 1) pile_k_fused(const PileGroupDev*
             const int e = loff[v + 1];
             for (int base = loff[v]; base < e; base += 8) {
               const int idx = base + slot;
-              if (idx < e) fused_contact(wf + L.sc + FR * perm[idx], l, gm, L.nb, acc);
+              if (idx < e) fused_contact(sc + FR * perm[idx], l, gm, nb, acc);
               __syncwarp();
             }
           }
-        n_con += (unsigned long long)nact;
+        n_con += (unsigned long long)nn.x;
         n_rounds += (unsigned long long)rounds * (unsigned long long)iters;
         n_lev += (unsigned long long)nlev;
       }
-      __syncthreads();  // and the sweeps
-      if (have) {
-        // velocity changes for the integrator; impulses of the last env-step
-        // back to the contact records (the diagnostics surface)
-        for (int b = lane; b < L.nb; b += 32) {
-          st3(wf + L.dv + 3 * b, v3(acc[b][0], acc[b][1], acc[b][2]));
-          st3(wf + L.dw + 3 * b, v3(acc[b][3], acc[b][4], acc[b][5]));
-        }
-        if (s == n_steps - 1)
-          for (int k = lane; k < nact; k += 32) {
-            const float* rec = wf + L.sc + FR * k;
-            float* cimp = wf + L.con + CF * wi[L.sccon + k] + C_IMP;
-            for (int r = 0; r < 4; ++r) cimp[r] = rec[R_IMP + r];
-          }
-        __syncwarp();
-        bad |= pile_integrate_world(wf, L, rk4, lane);
-      }
+      if (MID) __syncthreads();  // and the sweeps
+      if (have) bad |= fused_finish(g, w, lane, acc, nn.x, s == n_steps - 1, rk4);
+      if (!MID) __syncthreads();  // one barrier per env-step
     }
     if (have) {
+      const WsLay L = ws_layout(g->nb, g->np, g->maxc);
+      float* wf = g->scr + (size_t)w * g->sstride;
       ws_store_state(*g, w, L, wf, lane);
-      ws_store_diag(*g, w, L, wf, wi, lane);
+      ws_store_diag(*g, w, L, wf, reinterpret_cast<const int*>(wf + L.nf), lane);
       if (lane == 0) {
         unsigned st = 0u;
         if (overflow) st |= NEWT_WS_CONTACT_OVERFLOW;
@@ -516,47 +544,70 @@ __global__ void __launch_bounds__(32 * GANG, 1) pile_k_fused(const PileGroupDev*
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-// Dynamic shared memory of one block for a table whose largest world has
-// `nbm` bodies and contact capacity `cm`.
-extern "C" size_t newt_pile_fused_smem_bytes(int nbm, int cm) {
-  return (size_t)GANG * warp_smem(nbm, cm).bytes;
+// The launch shapes the autotuner chooses among: (gang warps, barrier between
+// assembly and sweeps).
+namespace {
+struct FusedShape { int gang; bool mid; };
+constexpr FusedShape kShapes[] = {{16, true}, {12, true}, {12, false}, {8, true}};
+constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
+template <class F> void with_kernel(int shape, F f) {
+  switch (shape) {
+    case 0: f(pile_k_fused<16, true>, 16); break;
+    case 1: f(pile_k_fused<12, true>, 12); break;
+    case 2: f(pile_k_fused<12, false>, 12); break;
+    default: f(pile_k_fused<8, true>, 8); break;
+  }
+}
+}  // namespace
+
+extern "C" int newt_pile_fused_shapes() { return kNumShapes; }
+
+// Warps (worlds in flight) per block of launch shape `shape`.
+extern "C" int newt_pile_fused_warps_per_block(int shape) { return kShapes[shape % kNumShapes].gang; }
+
+// Dynamic shared memory of one block of `gang` warps for a table whose
+// largest world has `nbm` bodies and contact capacity `cm`.
+extern "C" size_t newt_pile_fused_smem_bytes(int gang, int nbm, int cm) {
+  return (size_t)gang * warp_smem(nbm, cm).bytes;
 }
 
-// Resident blocks of pile_k_fused per SM for that table (outside stream
-// capture; sets the kernel's dynamic shared memory limit first).
-extern "C" int newt_pile_fused_blocks_per_sm(int nbm, int cm) {
-  const int bytes = (int)newt_pile_fused_smem_bytes(nbm, cm);
-  cudaFuncSetAttribute(pile_k_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+// Resident blocks per SM of launch shape `shape` for that table (outside
+// stream capture; sets the kernel's dynamic shared memory limit first).
+extern "C" int newt_pile_fused_blocks_per_sm(int shape, int nbm, int cm) {
   int b = 1;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pile_k_fused, 32 * GANG, bytes) != cudaSuccess || b < 1) b = 1;
+  with_kernel(shape, [&](auto kern, int gang) {
+    const int bytes = (int)newt_pile_fused_smem_bytes(gang, nbm, cm);
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 32 * gang, bytes) != cudaSuccess || b < 1) b = 1;
+  });
   return b;
 }
-
-// Worlds per block of the launch.
-extern "C" int newt_pile_fused_warps_per_block() { return GANG; }
 
 // Loads the kernels (so a later launch under stream capture creates nothing).
 extern "C" cudaError_t newt_pile_fused_prepare() {
   cudaFuncAttributes a;
-  cudaError_t e = cudaFuncGetAttributes(&a, pile_k_fused);
-  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, pile_k_queue_sort);
+  cudaError_t e = cudaFuncGetAttributes(&a, pile_k_queue_sort);
+  for (int k = 0; k < kNumShapes && e == cudaSuccess; ++k)
+    with_kernel(k, [&](auto kern, int) { e = cudaFuncGetAttributes(&a, kern); });
   return e;
 }
 
 // One call's launches on `st`: the queue sort by last call's costs (when
-// `cost` and `queue` are given), then the gangs.  `counter` must be zero
-// when the gangs start (the caller clears it on `st` first).  Every live
-// world of the table advances `n_steps` env-steps.
+// `cost` and `queue` are given), then the gangs of launch shape `shape`.
+// `counter` must be zero when the gangs start (the caller clears it on `st`
+// first).  Every live world of the table advances `n_steps` env-steps.
 extern "C" int newt_launch_pile_fused(const PileGroupDev* dG, const int* dwseg, int ng, int* queue, int n_items,
                                       int* counter, int n_steps, int grid, unsigned long long* work, unsigned* cost,
-                                      int nbm, int cm, cudaStream_t st) {
+                                      int nbm, int cm, int shape, cudaStream_t st) {
   if (n_items <= 0 || grid <= 0) return 0;
   int launches = 0;
   if (queue && cost) {
     pile_k_queue_sort<<<1, 1024, 0, st>>>(cost, n_items, queue);
     ++launches;
   }
-  pile_k_fused<<<grid, 32 * GANG, newt_pile_fused_smem_bytes(nbm, cm), st>>>(dG, dwseg, ng, queue, n_items, counter,
-                                                                            n_steps, work, cost, nbm, cm);
+  with_kernel(shape, [&](auto kern, int gang) {
+    kern<<<grid, 32 * gang, newt_pile_fused_smem_bytes(gang, nbm, cm), st>>>(dG, dwseg, ng, queue, n_items, counter,
+                                                                             n_steps, work, cost, nbm, cm);
+  });
   return launches + 1;
 }

@@ -532,18 +532,21 @@ int newt_gpu_autotune(newt_gpu_ctx* ctx, int32_t n_steps, int32_t* choice) {
   return rc;
 }
 
+extern "C" int newt_pile_fused_shapes();
+
 int newt_gpu_set_launch_choice(newt_gpu_ctx* ctx, const int32_t* choice) {
   if (!ctx || !choice) return NEWT_E_INVALID;
-  const int branches = choice[0], tree_pct = choice[1], fused = choice[3], fused_pct = choice[4];
+  const int branches = choice[0], tree_pct = choice[1], fused = choice[3], shape = choice[4];
   if (branches < 0 || branches > newt_gpu_ctx::PILE_BRANCHES || tree_pct < 1 || tree_pct > 100 || fused < 0 ||
-      fused > 1 || fused_pct < 1 || fused_pct > 100) {
-    ctx->err = "newt_gpu_set_launch_choice: pile branches 0..3, grid percents 1..100, persistent flag 0 or 1";
+      fused > 1 || shape < 0 || shape >= newt_pile_fused_shapes()) {
+    ctx->err = "newt_gpu_set_launch_choice: pile branches 0..3, tree grid percent 1..100, persistent flag 0 or 1, "
+               "persistent shape 0.." + std::to_string(newt_pile_fused_shapes() - 1);
     return NEWT_E_INVALID;
   }
   ctx->tune_branches = branches;
   ctx->tune_tree_grid_pct = tree_pct;
   ctx->tune_pile_fused = fused;
-  ctx->tune_fused_pct = fused_pct;
+  ctx->tune_fused_shape = shape;
   ctx->graph_dirty = true;
   return NEWT_OK;
 }

@@ -147,9 +147,11 @@ struct newt_gpu_ctx {
   // (0: by world count), tree persistent grid in percent of full residency
   int tune_branches = 0, tune_tree_grid_pct = 100;
   // pile worlds in the batched form: 1 = one world-persistent launch over a
-  // size-sorted queue (pile_fused.cu), 0 = the island-class pipeline per
-  // env-step; the persistent grid in percent of full residency
-  int tune_pile_fused = 1, tune_fused_pct = 100;
+  // cost-sorted queue (pile_fused.cu), 0 = the island-class pipeline per
+  // env-step; the persistent launch's shape (gang size and barriers, an
+  // index into pile_fused.cu's shape table) and grid in percent of full
+  // residency
+  int tune_pile_fused = 1, tune_fused_shape = 1, tune_fused_pct = 100;
   // the persistent launch of the captured graph: its timing events (external
   // records when profiling), its work counters (device: contacts, rounds,
   // levels, worlds) and whether the graph holds one; `last_fused` tells the

@@ -29,11 +29,11 @@ extern "C" int newt_launch_pile_step(const PileGroupDev* dG, const int* dwseg, i
                                      int total_slots, int* lists, int write_diag, cudaStream_t st,
                                      const cudaStream_t* side, cudaEvent_t* ev, cudaEvent_t* kev);
 extern "C" void newt_pile_init();
-extern "C" int newt_pile_fused_blocks_per_sm(int nbm, int cm);
-extern "C" int newt_pile_fused_warps_per_block();
+extern "C" int newt_pile_fused_blocks_per_sm(int shape, int nbm, int cm);
+extern "C" int newt_pile_fused_warps_per_block(int shape);
 extern "C" int newt_launch_pile_fused(const PileGroupDev* dG, const int* dwseg, int ng, int* queue, int n_items,
                                       int* counter, int n_steps, int grid, unsigned long long* work, unsigned* cost,
-                                      int nbm, int cm, cudaStream_t st);
+                                      int nbm, int cm, int shape, cudaStream_t st);
 extern "C" int newt_tc_prepare(newt_gpu_ctx* ctx, HostGroup* g, int n_steps);
 extern "C" int newt_tc_launch(newt_gpu_ctx* ctx, HostGroup* g, int n_steps, cudaStream_t st, bool capturing);
 
@@ -268,8 +268,8 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
     if (!ctx->fkev[0])
       for (int k = 0; k < 2; ++k) CKS(cudaEventCreate(&ctx->fkev[k]));
     for (HostGroup* g : piles) { fnbm = std::max(fnbm, g->size); fcm = std::max(fcm, g->maxc); }
-    const int wpb = newt_pile_fused_warps_per_block();
-    const int full = newt_pile_fused_blocks_per_sm(fnbm, fcm) * sm_count(ctx);
+    const int wpb = newt_pile_fused_warps_per_block(ctx->tune_fused_shape);
+    const int full = newt_pile_fused_blocks_per_sm(ctx->tune_fused_shape, fnbm, fcm) * sm_count(ctx);
     fgrid = std::min((ft.worlds + wpb - 1) / wpb, std::max(1, full * ctx->tune_fused_pct / 100));
   }
   for (int b = 0; b < nbr; ++b) {
@@ -324,7 +324,7 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
     cudaMemsetAsync(ctx->fused_work, 0, 4 * sizeof(unsigned long long), fs);
     if (ctx->profile) cudaEventRecordWithFlags(ctx->fkev[0], fs, cudaEventRecordExternal);
     fused_launches = newt_launch_pile_fused(ft.dG, ft.dseg, ft.ng, fqueue, ft.worlds, fcounter, n_steps, fgrid,
-                                            ctx->fused_work, fcost, fnbm, fcm, fs);
+                                            ctx->fused_work, fcost, fnbm, fcm, ctx->tune_fused_shape, fs);
     if (ctx->profile) cudaEventRecordWithFlags(ctx->fkev[1], fs, cudaEventRecordExternal);
     cudaEventRecord(ctx->pbe[0][4], fs);
     cudaStreamWaitEvent(ctx->stream, ctx->pbe[0][4], 0);
@@ -413,13 +413,17 @@ int autotune_batched(newt_gpu_ctx* ctx, int n_steps, int32_t* choice) {
       CKS(cudaMemcpyAsync(live[i].first, snap[k][i], live[i].second, cudaMemcpyDeviceToDevice, ctx->stream));
     return NEWT_OK;
   };
-  struct Cand { int fused, fused_pct, branches, grid_pct; };
-  const Cand cands[] = {{1, 100, 0, 100}, {1, 75, 0, 100}, {1, 50, 0, 100}, {0, 100, 1, 100}, {0, 100, 2, 100},
-                        {0, 100, 3, 100}, {1, 100, 0, 50}, {0, 100, 2, 50}};
-  const Cand start{ctx->tune_pile_fused, ctx->tune_fused_pct, ctx->tune_branches, ctx->tune_tree_grid_pct};
+  // piles: the persistent launch in each gang shape (warps per block, and
+  // whether the gang also meets between assembly and sweeps), or the
+  // island-class pipeline with 1, 2 or 3 world-range branches; trees: full
+  // or half persistent grid
+  struct Cand { int fused, shape, branches, grid_pct; };
+  const Cand cands[] = {{1, 0, 0, 100}, {1, 1, 0, 100}, {1, 2, 0, 100}, {1, 3, 0, 100}, {0, 0, 1, 100},
+                        {0, 0, 2, 100}, {0, 0, 3, 100}, {1, 1, 0, 50}, {0, 0, 2, 50}};
+  const Cand start{ctx->tune_pile_fused, ctx->tune_fused_shape, ctx->tune_branches, ctx->tune_tree_grid_pct};
   auto set = [&](const Cand& c) {
     ctx->tune_pile_fused = c.fused;
-    ctx->tune_fused_pct = c.fused_pct;
+    ctx->tune_fused_shape = c.shape;
     ctx->tune_branches = c.branches;
     ctx->tune_tree_grid_pct = c.grid_pct;
     ctx->graph_dirty = true;
@@ -463,7 +467,7 @@ int autotune_batched(newt_gpu_ctx* ctx, int n_steps, int32_t* choice) {
     choice[1] = best.grid_pct;
     choice[2] = (int32_t)(best_ms * 1000.f);
     choice[3] = best.fused;
-    choice[4] = best.fused_pct;
+    choice[4] = best.shape;
   }
   return rc;
 }
