@@ -248,7 +248,7 @@ def run_gpu(args, rank, ws, local, dist):
     # (it leaves the worlds' state as it found it)
     for _ in range(max(3, args.warmup)):
         eng.step(S, STEP_BATCHED)
-    tuned = eng.autotune(S)
+    tuned = eng.autotune(S, horizon=S * args.steps)
     eng.sync()
     start_qpos, start_qvel = eng.get_state(slots, nq_t, nv_t)
     launches0 = eng.launch_count()
@@ -399,7 +399,7 @@ def run_uneven_compact(rank, ws, local, dist, n_worlds=32768, substeps=25, steps
 
     reset()
     eng.step(substeps, STEP_BATCHED)
-    tuned = eng.autotune(substeps)
+    tuned = eng.autotune(substeps, horizon=substeps * steps)
     out = {"worlds": n_worlds, "env_steps": substeps * steps, "autotuned": tuned}
     for name, mode in (("batched", STEP_BATCHED), ("plain", STEP_PLAIN)):
         reset()
@@ -598,7 +598,7 @@ def run_gpu_uneven(args, rank, ws, local, dist):
     # 0 .. steps x substeps of every world
     for _ in range(max(3, args.warmup)):
         eng.step(S, STEP_BATCHED)
-    tuned = eng.autotune(S)
+    tuned = eng.autotune(S, horizon=S * args.steps)
     eng.step(S, STEP_BATCHED)
     eng.sync()
     nq, nv = int(batch.nq.sum()), int(batch.nv.sum())

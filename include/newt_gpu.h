@@ -293,19 +293,22 @@ NEWT_API int newt_gpu_flush_l2(newt_gpu_ctx* ctx);                              
 /* Kernel launches issued by this context since creation. */
 NEWT_API int64_t newt_gpu_launch_count(const newt_gpu_ctx* ctx);
 /* Times the batched step's launch choices on the live worlds (piles in the
- * world-persistent launch in each of its shapes -- gangs of 16, 12 or 8
- * warps per block, with or without a barrier between assembly and sweeps --
+ * world-persistent launch in each of its shapes -- gangs of 32, 24, 16, 12
+ * or 8 warps per block, with or without a barrier between assembly and sweeps --
  * or in the island-class pipeline with 1, 2 or 3 world-range branches; tree
- * persistent grid at full or half residency), `n_steps` env-steps per trial
- * from two snapshots of every world (as they are, and 8 x n_steps env-steps
- * later, once falling piles have settled), keeps the fastest summed over both
- * for later NEWT_STEP_BATCHED calls and leaves every world's state as it was.
+ * persistent grid at full or half residency), `n_steps` env-steps per trial,
+ * and keeps the fastest for later NEWT_STEP_BATCHED calls.  `horizon` is how
+ * many env-steps the caller means to run next (<= 0: 8 x n_steps): every
+ * choice is timed from three snapshots of every world -- as they are, and
+ * horizon/2 and horizon env-steps later (falling piles land and their
+ * islands grow) -- and judged by the trapezoid average over the horizon
+ * (weights 1/4, 1/2, 1/4).  Every world's state is left as it was.
  * `choice` (nullable, 5 ints): pile branches (0 for the persistent launch),
- * tree grid percent, the winner's summed time in microseconds, 1 if piles
- * use the persistent launch, its shape index (0: 16 warps; 1: 12 warps;
- * 2: 12 warps, one barrier per env-step; 3: 8 warps).  No counterpart in
- * newt. */
-NEWT_API int newt_gpu_autotune(newt_gpu_ctx* ctx, int32_t n_steps, int32_t* choice);
+ * tree grid percent, the winner's averaged time per trial in microseconds,
+ * 1 if piles use the persistent launch, its shape index (0: 16 warps; 1: 12
+ * warps; 2: 12 warps, one barrier per env-step; 3: 8 warps; 4: 24 warps; 5:
+ * 32 warps).  No counterpart in newt. */
+NEWT_API int newt_gpu_autotune(newt_gpu_ctx* ctx, int32_t n_steps, int32_t horizon, int32_t* choice);
 /* Sets the batched step's launch choices directly, in newt_gpu_autotune's
  * `choice` layout: [0] pile world-range branches of the island-class
  * pipeline (0: by world count), [1] tree persistent grid percent, [2]

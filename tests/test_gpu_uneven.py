@@ -78,14 +78,14 @@ def test_status_reports_blow_up_right_after_the_step(eng, mode):
 
 def test_autotune_keeps_state_and_results(eng, batch):
     """newt_gpu_autotune times the batched form's launch choices on the live
-    worlds from two snapshots: the worlds end where they began, and the
-    chosen form still agrees with the plain one."""
+    worlds from three snapshots over a 20-env-step horizon: the worlds end
+    where they began, and the chosen form still agrees with the plain one."""
     slots = eng.alloc(eng.upload(batch))
     eng.set_state(slots, batch.qpos, batch.qvel)
     eng.set_qfrc(slots, batch.qfrc)
     nq, nv = int(batch.nq.sum()), int(batch.nv.sum())
     q0, v0 = eng.get_state(slots, nq, nv)
-    choice = eng.autotune(5)
+    choice = eng.autotune(5, horizon=20)
     q1, v1 = eng.get_state(slots, nq, nv)
     np.testing.assert_array_equal(q0, q1)
     np.testing.assert_array_equal(v0, v1)

@@ -136,7 +136,7 @@ def load_library(path: str = LIB_PATH):
         "newt_gpu_tc_profile": ([P, P], C.c_int),
         "newt_gpu_serve": ([P, P, I32, P, P], C.c_int),
         "newt_gpu_memory": ([P, P, P], C.c_int),
-        "newt_gpu_autotune": ([P, I32, P], C.c_int),
+        "newt_gpu_autotune": ([P, I32, I32, P], C.c_int),
         "newt_gpu_set_ctrl_stream": ([P, P, I32, P, P], C.c_int),
         "newt_gpu_apply_ctrl": ([P], C.c_int),
         "newt_gpu_pile_fused_profile": ([P, P, P], C.c_int),
@@ -344,11 +344,13 @@ class Engine:
     def flush_l2(self):
         self._ck(self.L.newt_gpu_flush_l2(self.ctx))
 
-    def autotune(self, n_steps: int = 25) -> dict:
+    def autotune(self, n_steps: int = 25, horizon: int = 0) -> dict:
         """Pick the batched step's launch choices by timing them on the live
-        worlds (their state is left unchanged)."""
+        worlds, `n_steps` env-steps per trial, averaged over the next
+        `horizon` env-steps (0: 8 x n_steps); the worlds' state is left
+        unchanged."""
         c = np.zeros(5, np.int32)
-        self._ck(self.L.newt_gpu_autotune(self.ctx, int(n_steps), _p(c)))
+        self._ck(self.L.newt_gpu_autotune(self.ctx, int(n_steps), int(horizon), _p(c)))
         return {"pile_persistent": bool(c[3]), "persistent_shape": int(c[4]), "pile_branches": int(c[0]),
                 "tree_grid_pct": int(c[1]), "best_ms": c[2] / 1000.0}
 

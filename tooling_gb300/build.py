@@ -20,6 +20,12 @@ SOURCES = ["runtime.cu", "groups.cu", "step.cu", "tree_kernels.cu", "pile_kernel
            "static_step.cu", "ccd_query.cu",
            "world_io.cu", "serve.cpp", "ctrl_stream.cu", "sensors.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# GJK/EPA compiled without multiply-add contraction: with its face threshold
+# at the f32 rounding level, newt's routine only takes the same polytope
+# path when every product and sum is rounded on its own, as newt's (and the
+# oracle's) arithmetic is.  Division and square root stay IEEE-rounded (the
+# nvcc defaults without fast math).
+EXTRA_FLAGS = {"ccd_query.cu": ["-fmad=false"]}
 
 
 def _nvcc() -> str:
@@ -52,7 +58,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def comp(src):
         obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-        cmd = [nvcc] + flags + ["-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [nvcc] + flags + EXTRA_FLAGS.get(src, []) + ["-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")

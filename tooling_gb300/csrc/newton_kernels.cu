@@ -119,7 +119,7 @@ NEWT_D float reference_accel(float position, float velocity, float tc, float dr,
 // ---------------------------------------------------------------------------
 struct TcLay {
   int L, nv, ng, maxc, ld;
-  int jv, jw, iw, con, jt, H, LH, LHd, imp, misc, qfc, mc, rd, words;
+  int jv, jw, iw, con, jt, j0, H, LH, LHd, imp, misc, qfc, mc, rd, words;
 };
 NEWT_HD int up4(int n) { return (n + 3) / 4 * 4; }
 constexpr int REFINE_NV = 32;  // DoF above which the mass-matrix solve is refined in FP64
@@ -133,6 +133,7 @@ NEWT_HD TcLay tc_layout(int L, int nv, int ng, int maxc) {
   t.iw = f; f += up4(7 * L);  // world inertias (6 per link), then link masses
   t.con = f; f += up4(CREC * maxc);
   t.jt = f; f += up4(nv * t.ld);  // J^T, then Y in place, when the rows exceed the shared tile
+  t.j0 = f; f += up4(nv * t.ld);  // J^T kept for the contact force J^T f
   t.H = f; f += up4(t.ld * t.ld);
   t.LH = f; f += up4(t.ld * t.ld);       // factor of H when it exceeds the shared tile
   t.LHd = f; f += up4(2 * t.ld * t.ld);  // FP64 factor (offset is a multiple of 4 floats)
@@ -261,21 +262,6 @@ NEWT_D void warp_llt_solve(const T* Lf, int n, int ld, float* v, int lane) {
   __syncwarp();
 }
 
-// Solves L^T z = rhs in place on the shared vector `v` (backward
-// substitution by row dot products of the column-major factor L).
-NEWT_D void warp_lt_solve(const float* Lf, int n, int ld, float* v, int lane) {
-  for (int k = n - 1; k >= 0; --k) {
-    __syncwarp();
-    float s = 0.f;
-    for (int m = k + 1 + lane; m < n; m += 32) s += Lf[(size_t)k * ld + m] * v[m];
-    s = warp_sum(s);
-    const float zk = (v[k] - s) / Lf[(size_t)k * ld + k];
-    __syncwarp();
-    if (lane == 0) v[k] = zk;
-  }
-  __syncwarp();
-}
-
 // Solves L L^T z = v in FP64 with the FP32 column-major factor L (FP64
 // vector `v`, in place; forward then backward substitution).
 NEWT_D void warp_llt_solve_mixed(const float* Lf, int n, int ld, double* v, int lane) {
@@ -312,6 +298,13 @@ NEWT_D float warp_dot(const float* a, const float* b, int n, int lane) {
   float s = 0.f;
   for (int r = lane; r < n; r += 32) s += a[r] * b[r];
   return warp_sum(s);
+}
+// the same dot accumulated in FP64 (each f32 product is exact in double)
+NEWT_D double warp_dot_d(const float* a, const float* b, int n, int lane) {
+  double s = 0.0;
+  for (int r = lane; r < n; r += 32) s += (double)a[r] * (double)b[r];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  return s;
 }
 
 }  // namespace
@@ -632,6 +625,7 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   // ---- Jacobian rows of the cone facets, velocities, lane per row ----
   const bool rows_shared = nr <= sm.nrs;
   float* Jt = rows_shared ? sv + sm.jy : wf + lay.jt;  // J^T, column-major; becomes Y
+  float* J0 = wf + lay.j0;                              // J^T, kept
   const int ldj = rows_shared ? sm.nrs : ld;
   float* tw = sv + sm.tw;  // 1 marks a link that owns rows; then its inverse weight
   for (int l = lane; l < L; l += 32) tw[l] = 0.f;
@@ -656,6 +650,7 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
     float vel = 0.f, vfree = 0.f;
     for (int k = 0; k < nv; ++k) {
       const float jk = Jt[(size_t)k * ldj + r];
+      J0[(size_t)k * ld + r] = jk;
       vel += jk * g.qd[k * cap + w];
       vfree += jk * g.qacc[k * cap + w];
     }
@@ -786,11 +781,19 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
       status |= NEWT_WS_NOT_PD;
       for (int r = lane; r < nr; r += 32) vx[r] = 0.f;
     } else {
-      float cur = 0.f;  // cost at x = 0
+      // The costs that steer the line search and the stopping test are kept
+      // in FP64: the window products below change by incremental updates as
+      // coordinates leave the free set, and the stopping test compares cost
+      // decreases at 1e-7 of the cost, the f32 rounding level of the sums.
+      // The cost at the current point is evaluated afresh every iteration,
+      // 0.5 x.(H x) + b.x, as newt's quad_cost does, not carried over from
+      // the line search's estimate.
+      double cur = 0.0;  // cost at x = 0
       const int max_it = iters > 1 ? iters : 1;
       for (int it = 0; it < max_it; ++it) {
         // gradient g = H x + b, direction d = -(L L^T)^-1 g
         warp_matvec(H, nr, ld, vx, vg, lane);
+        if (it > 0) cur = 0.5 * warp_dot_d(vx, vg, nr, lane) + warp_dot_d(vx, vb, nr, lane);  // vg = H x here
         for (int r = lane; r < nr; r += 32) { vg[r] += vb[r]; vd[r] = -vg[r]; }
         __syncwarp();
         if (use64) warp_llt_solve(LHd, nr, ld, vd, lane);
@@ -807,11 +810,12 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
         }
         warp_matvec(H, nr, ld, vp, vu, lane);
         warp_matvec(H, nr, ld, vs, vv, lane);
-        float best_a = 0.f, best_c = cur, lo = 0.f;
+        float best_a = 0.f, lo = 0.f;
+        double best_c = cur;
         // cost on a window: c0 + c1 a + c2 a^2 / 2 with p = P + a S; the five
         // products are updated in O(1) when a coordinate leaves the free set
-        float Pu = warp_dot(vp, vu, nr, lane), Pv = warp_dot(vp, vv, nr, lane);
-        float Sv = warp_dot(vs, vv, nr, lane), bP = warp_dot(vb, vp, nr, lane), bS = warp_dot(vb, vs, nr, lane);
+        double Pu = warp_dot_d(vp, vu, nr, lane), Pv = warp_dot_d(vp, vv, nr, lane);
+        double Sv = warp_dot_d(vs, vv, nr, lane), bP = warp_dot_d(vb, vp, nr, lane), bS = warp_dot_d(vb, vs, nr, lane);
         for (int guard = 0; guard <= nr; ++guard) {
           // next breakpoint (warp argmin)
           float bm = 2.f;
@@ -824,41 +828,40 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
           }
           const float hi = bm < 1.f ? bm : 1.f;
           if (hi - lo > 1.0e-7f) {
-            const float c0 = 0.5f * Pu + bP, c1 = Pv + bS, c2 = Sv;
-            const float opt = c2 > 0.f ? fminf(fmaxf(-c1 / c2, lo), hi) : 0.5f * (lo + hi);
+            const double c0 = 0.5 * Pu + bP, c1 = Pv + bS, c2 = Sv;
+            const float opt = c2 > 0.0 ? fminf(fmaxf((float)(-c1 / c2), lo), hi) : 0.5f * (lo + hi);
             const float cand[3] = {lo, hi, opt};
             for (int k = 0; k < 3; ++k) {
-              const float a = cand[k];
-              const float cost = c0 + c1 * a + 0.5f * c2 * a * a;
-              if (cost < best_c) { best_c = cost; best_a = a; }
+              const double a = cand[k];
+              const double cost = c0 + c1 * a + 0.5 * c2 * a * a;
+              if (cost < best_c) { best_c = cost; best_a = cand[k]; }
             }
           }
           if (bi < 0) break;
           // coordinate bi leaves the free set: P, S lose it, H P and H S a column
-          const float xj = vp[bi], dj = vs[bi], uj = vu[bi], vj = vv[bi], bj = vb[bi];
-          const float hjj = H[(size_t)bi * ld + bi];
-          Pu += (xj * hjj - 2.f * uj) * xj;
+          const double xj = vp[bi], dj = vs[bi], uj = vu[bi], vj = vv[bi], bj = vb[bi];
+          const double hjj = H[(size_t)bi * ld + bi];
+          Pu += (xj * hjj - 2.0 * uj) * xj;
           Pv += xj * dj * hjj - xj * vj - dj * uj;
-          Sv += (dj * hjj - 2.f * vj) * dj;
+          Sv += (dj * hjj - 2.0 * vj) * dj;
           bP -= bj * xj;
           bS -= bj * dj;
           __syncwarp();
           for (int r = lane; r < nr; r += 32) {
             const float hc = H[(size_t)bi * ld + r];
-            vu[r] -= xj * hc;
-            vv[r] -= dj * hc;
+            vu[r] -= (float)xj * hc;
+            vv[r] -= (float)dj * hc;
           }
           if (lane == 0) { vp[bi] = 0.f; vs[bi] = 0.f; vreg[bi] = 2.f; }
           __syncwarp();
           lo = hi;
         }
-        if (best_a <= 0.f || cur - best_c <= 1.0e-7f * (1.f + fabsf(cur))) break;
+        if (best_a <= 0.f || cur - best_c <= 1.0e-7 * (1.0 + fabs(cur))) break;
         for (int r = lane; r < nr; r += 32) {
           const float x = vx[r] + best_a * vd[r];
           vx[r] = x < 0.f ? 0.f : x;
         }
         __syncwarp();
-        cur = best_c;
         done_it = it + 1;
       }
       if (done_it == max_it) status |= NEWT_WS_ITER_CAP;
@@ -867,29 +870,26 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   __syncwarp();
 
   // ---- outputs: impulses, J^T f / dt, qacc = a_free + (M + dt B)^-1 J^T f / dt ----
-  // J^T = L Y, so (L L^T)^-1 J^T f / dt = L^-T (Y f) / dt: one back substitution
+  // The contact force is formed from the kept J^T, not as L (Y f): Y = L^-1
+  // J^T carries the f32 rounding of the forward substitution, which L Y does
+  // not undo on long chains of light links, and the FP64 refinement below
+  // needs the true right-hand side to converge to.
   for (int r = lane; r < nr; r += 32) wf[lay.imp + r] = vx[r];
+  double* rhs = refine ? reinterpret_cast<double*>(wf + lay.rd) : nullptr;
   for (int k = lane; k < nv; k += 32) {
     float s = 0.f;
-    for (int r = 0; r < nr; ++r) s += Y[(size_t)k * ldj + r] * vx[r];
+    double sd = 0.0;
+    for (int r = 0; r < nr; ++r) {
+      const float jk = J0[(size_t)k * ld + r];
+      s += jk * vx[r];
+      if (refine) sd += (double)jk * (double)vx[r];
+    }
     vg[k] = s / dt;
+    if (refine) rhs[k] = sd / dt;
+    if (rk4) g.cfrc[(size_t)w * g.cstride + k] = vg[k];  // the generalised force, held over the stages
   }
   __syncwarp();
-  if (rk4)  // the generalised force itself, J^T f / dt = L (Y f) / dt (L column-major lower)
-    for (int i = lane; i < nv; i += 32) {
-      float s = 0.f;
-      for (int k = 0; k <= i; ++k) s += LM[(size_t)k * nv + i] * vg[k];
-      g.cfrc[(size_t)w * g.cstride + i] = s;
-    }
-  __syncwarp();
-  double* rhs = refine ? reinterpret_cast<double*>(wf + lay.rd) : nullptr;
-  if (refine)  // J^T f / dt = L (Y f) / dt, in FP64 from the FP32 factor
-    for (int i = lane; i < nv; i += 32) {
-      double s = 0.0;
-      for (int k = 0; k <= i; ++k) s += (double)LM[(size_t)k * nv + i] * (double)vg[k];
-      rhs[i] = s;
-    }
-  warp_lt_solve(LM, nv, nv, vg, lane);
+  warp_llt_solve(LM, nv, nv, vg, lane);
   if (refine) {
     // r = rhs - M' x in FP64 (M' symmetric, its lower triangle kept), then
     // M' d = r with the FP32 factor in FP64 arithmetic, x += d

@@ -46,8 +46,8 @@
 // Row record.  A pyramidal contact has four facet rows r = n + s_r mu t_q(r)
 // (s = +, -, +, -; q = 1, 1, 2, 2).  The record keeps the Jacobian of the
 // normal and of both tangents and their M^-1 J^T per lane triple (side a
-// linear, side a angular, side b linear, side b angular; the linear M^-1 J^T
-// is J / m and is formed in registers), the exact row-space block
+// linear, side a angular, side b linear, side b angular; zero for a static
+// side), so the four lanes of a contact run one code path, the exact row-space block
 // A_rs = J_r M^-1 J_s^T, newt's row diagonals (row_body_diagonal plus the
 // regulariser), the biases and the pair determinants.  One contact update
 // takes three four-lane dot products (J_n.v, J_t1.v, J_t2.v) for the four
@@ -65,23 +65,24 @@ using namespace pile;
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
-// gang sizes (warps per block, one block per SM): 16 warps run at 128
-// registers (spilling in the sweeps), 12 at 168 and 8 at 255 without
+// gang sizes (warps per block, one block per SM): 32 warps run at 64
+// registers and 24 at 80 (both spilling), 16 at 128 (spilling in the
+// sweeps), 12 at 168 and 8 at 182 without
 constexpr int F_MAXC = 512;   // the largest contact capacity of a pile world
 constexpr int N_BUCKET = 256; // cost classes of the queue sort
 
 // compact row record (floats, 16-byte aligned)
 enum {
-  R_LIN = 0,    // n xyz, t1 xyz, t2 xyz, 1/m_a, 1/m_b, 0   (1/m = 0 for a static side)
-  R_ANGA = 12,  // side a angular: J_n, J_t1, J_t2, then M^-1 J^T of each; 2 pad
-  R_ANGB = 32,  // side b angular (negated, zero when static), same layout
-  R_A = 52,     // A00 A01 A02 A03 | A11 A12 A13 A22 | A23 A33 reg mu
-  R_B = 64,     // bias of rows 0..3
-  R_DG = 68,    // newt's row diagonals (A_rr by row_body_diagonal, plus reg)
-  R_IDG = 72,   // their inverses
-  R_MISC = 76,  // 1/det of pair (0,1), of pair (2,3) (0 when det <= 0), body slot a, body slot b (int bits)
-  R_IMP = 80,   // impulses of rows 0..3
-  FR = 84
+  R_TRI = 0,    // per lane triple l (0 side a linear, 1 side a angular, 2 side b
+                // linear, 3 side b angular), 20 floats at R_TRI + 20 l: J of n,
+                // t1, t2, then M^-1 J^T of each, 2 pad (zero for a static side)
+  R_A = 80,     // A00 A01 A02 A03 | A11 A12 A13 A22 | A23 A33 reg mu
+  R_B = 92,     // bias of rows 0..3
+  R_DG = 96,    // newt's row diagonals (A_rr by row_body_diagonal, plus reg)
+  R_IDG = 100,  // their inverses
+  R_MISC = 104, // 1/det of pair (0,1), of pair (2,3) (0 when det <= 0), body slot a, body slot b (int bits)
+  R_IMP = 108,  // impulses of rows 0..3
+  FR = 112
 };
 static_assert(FR % 4 == 0, "records are read as float4");
 static_assert(FR <= SC, "the compact record fits the solver record's slot");
@@ -156,19 +157,15 @@ NEWT_D int fused_assemble(const WsLay& L, float* wf, int* wi, int lane, float (*
       ja[q] = da ? cross(arma, ds[q]) : z;
       jb[q] = db ? -cross(armb, ds[q]) : z;
     }
-    // linear block
-    rec[R_LIN + 0] = n.x; rec[R_LIN + 1] = n.y; rec[R_LIN + 2] = n.z;
-    rec[R_LIN + 3] = t1.x; rec[R_LIN + 4] = t1.y; rec[R_LIN + 5] = t1.z;
-    rec[R_LIN + 6] = t2.x; rec[R_LIN + 7] = t2.y; rec[R_LIN + 8] = t2.z;
-    rec[R_LIN + 9] = ima; rec[R_LIN + 10] = imb; rec[R_LIN + 11] = 0.f;
-    // angular blocks: J of n, t1, t2, then I^-1 J
+    // the four lane triples: J of n, t1, t2, then M^-1 J^T of each
     for (int q = 0; q < 3; ++q) {
-      const V3 wa = smv(Ia, ja[q]), wb = smv(Ib, jb[q]);
-      st3(rec + R_ANGA + 3 * q, ja[q]); st3(rec + R_ANGA + 9 + 3 * q, wa);
-      st3(rec + R_ANGB + 3 * q, jb[q]); st3(rec + R_ANGB + 9 + 3 * q, wb);
+      const V3 la = da ? ds[q] : z, lb = db ? -ds[q] : z;
+      st3(rec + R_TRI + 3 * q, la);      st3(rec + R_TRI + 9 + 3 * q, la * ima);
+      st3(rec + R_TRI + 20 + 3 * q, ja[q]); st3(rec + R_TRI + 29 + 3 * q, smv(Ia, ja[q]));
+      st3(rec + R_TRI + 40 + 3 * q, lb);  st3(rec + R_TRI + 49 + 3 * q, lb * imb);
+      st3(rec + R_TRI + 60 + 3 * q, jb[q]); st3(rec + R_TRI + 69 + 3 * q, smv(Ib, jb[q]));
     }
-    rec[R_ANGA + 18] = rec[R_ANGA + 19] = 0.f;
-    rec[R_ANGB + 18] = rec[R_ANGB + 19] = 0.f;
+    for (int t = 0; t < 4; ++t) rec[R_TRI + 20 * t + 18] = rec[R_TRI + 20 * t + 19] = 0.f;
     // facet rows: side Jacobians as in newt's row assembly
     J6 Ra[4], Rb[4];
     float diag[4];
@@ -253,6 +250,20 @@ NEWT_D int fused_levels(const WsLay& L, const float* wf, int nact, int lane, sho
   return nlev;
 }
 
+// newt's pyramidal pair step (RowStep::pair, solver.rs:1476-1518) with its
+// four cases chosen by selects rather than branches (the eight contacts of a
+// round take different cases) and the one-row fallbacks' division by the row
+// diagonal done as a product with its stored inverse.
+NEWT_D void pair_select(float ii, float ij, float ri, float rj, float h00, float h11, float h01, float idet,
+                        float i00, float i11, float* ni, float* nj) {
+  const float ui = ii + (-ri * h11 + h01 * rj) * idet;
+  const float uj = ij + (h01 * ri - h00 * rj) * idet;
+  const float si = fmaxf(ii - ri * i00, 0.f), sj = fmaxf(ij - rj * i11, 0.f);
+  const bool pi = ui >= 0.f, pj = uj >= 0.f;
+  *ni = pi ? (pj ? ui : si) : 0.f;  // both >= 0: the pair; one < 0: it is 0 and the other steps alone
+  *nj = pj ? (pi ? uj : sj) : 0.f;
+}
+
 // ---------------------------------------------------------------------------
 // one contact update on the calling four-lane group (lane l of the group
 // holds triple l: side a linear, side a angular, side b linear, side b
@@ -264,25 +275,10 @@ NEWT_D void fused_contact(float* rec, int l, unsigned gm, int nb, float (*acc)[6
   const float4 bs = ld4g(rec + R_B), dg = ld4g(rec + R_DG), ig = ld4g(rec + R_IDG), ms = ld4g(rec + R_MISC);
   const float4 f4 = ld4g(rec + R_IMP);
   const int body = __float_as_int(side ? ms.w : ms.z);
-  float J[3][3], W[3][3];
-  if (part == 0) {
-    const float4 q0 = ld4g(rec + R_LIN), q1 = ld4g(rec + R_LIN + 4), q2 = ld4g(rec + R_LIN + 8);
-    const float sg = side ? -1.f : 1.f, im = side ? q2.z : q2.y;
-    J[0][0] = sg * q0.x; J[0][1] = sg * q0.y; J[0][2] = sg * q0.z;
-    J[1][0] = sg * q0.w; J[1][1] = sg * q1.x; J[1][2] = sg * q1.y;
-    J[2][0] = sg * q1.z; J[2][1] = sg * q1.w; J[2][2] = sg * q2.x;
-#pragma unroll
-    for (int q = 0; q < 3; ++q)
-#pragma unroll
-      for (int e = 0; e < 3; ++e) W[q][e] = J[q][e] * im;
-  } else {
-    const float* blk = rec + (side ? R_ANGB : R_ANGA);
-    const float4 a0 = ld4g(blk), a1 = ld4g(blk + 4), a2 = ld4g(blk + 8), a3 = ld4g(blk + 12), a4 = ld4g(blk + 16);
-    J[0][0] = a0.x; J[0][1] = a0.y; J[0][2] = a0.z; J[1][0] = a0.w; J[1][1] = a1.x; J[1][2] = a1.y;
-    J[2][0] = a1.z; J[2][1] = a1.w; J[2][2] = a2.x;
-    W[0][0] = a2.y; W[0][1] = a2.z; W[0][2] = a2.w; W[1][0] = a3.x; W[1][1] = a3.y; W[1][2] = a3.z;
-    W[2][0] = a3.w; W[2][1] = a4.x; W[2][2] = a4.y;
-  }
+  const float* blk = rec + R_TRI + 20 * l;
+  const float4 a0 = ld4g(blk), a1 = ld4g(blk + 4), a2 = ld4g(blk + 8), a3 = ld4g(blk + 12), a4 = ld4g(blk + 16);
+  const float J[3][3] = {{a0.x, a0.y, a0.z}, {a0.w, a1.x, a1.y}, {a1.z, a1.w, a2.x}};
+  const float W[3][3] = {{a2.y, a2.z, a2.w}, {a3.x, a3.y, a3.z}, {a3.w, a4.x, a4.y}};
   float a[3];
 #pragma unroll
   for (int e = 0; e < 3; ++e) a[e] = acc[body][3 * part + e];
@@ -326,9 +322,8 @@ NEWT_D void fused_contact(float* rec, int l, unsigned gm, int nb, float (*acc)[6
     }
     const float ri = d[i] + (reg * f[i] + b[i]);
     const float rj = d[j] + (reg * f[j] + b[j]);
-    const float P[4] = {diag[i], diag[j], A[i][j], idet[p]};
     float ni, nj;
-    RowStep::pair(f[i], f[j], ri, rj, P, &ni, &nj);
+    pair_select(f[i], f[j], ri, rj, diag[i], diag[j], A[i][j], idet[p], idg[i], idg[j], &ni, &nj);
     const float di = ni - f[i], dj = nj - f[j];
     f[i] = ni;
     f[j] = nj;
@@ -548,14 +543,16 @@ __global__ void __launch_bounds__(32 * GANG, 1) pile_k_fused(const PileGroupDev*
 // assembly and sweeps).
 namespace {
 struct FusedShape { int gang; bool mid; };
-constexpr FusedShape kShapes[] = {{16, true}, {12, true}, {12, false}, {8, true}};
+constexpr FusedShape kShapes[] = {{16, true}, {12, true}, {12, false}, {8, true}, {24, true}, {32, true}};
 constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 template <class F> void with_kernel(int shape, F f) {
   switch (shape) {
     case 0: f(pile_k_fused<16, true>, 16); break;
     case 1: f(pile_k_fused<12, true>, 12); break;
     case 2: f(pile_k_fused<12, false>, 12); break;
-    default: f(pile_k_fused<8, true>, 8); break;
+    case 3: f(pile_k_fused<8, true>, 8); break;
+    case 4: f(pile_k_fused<24, true>, 24); break;
+    default: f(pile_k_fused<32, true>, 32); break;
   }
 }
 }  // namespace

@@ -524,10 +524,10 @@ int newt_gpu_flush_l2(newt_gpu_ctx* ctx) {
 
 int64_t newt_gpu_launch_count(const newt_gpu_ctx* ctx) { return ctx ? ctx->launches : -1; }
 
-int newt_gpu_autotune(newt_gpu_ctx* ctx, int32_t n_steps, int32_t* choice) {
+int newt_gpu_autotune(newt_gpu_ctx* ctx, int32_t n_steps, int32_t horizon, int32_t* choice) {
   if (!ctx || n_steps <= 0) return NEWT_E_INVALID;
   cudaSetDevice(ctx->device);
-  int rc = autotune_batched(ctx, n_steps, choice);
+  int rc = autotune_batched(ctx, n_steps, horizon > 0 ? horizon : 8 * n_steps, choice);
   if (rc != NEWT_OK && ctx->err.empty()) ctx->err = "autotune failed";
   return rc;
 }

@@ -216,7 +216,7 @@ void ctrl_release_slot(newt_gpu_ctx* ctx, int slot);                     // ends
 HostGroup* find_or_make_group(newt_gpu_ctx* ctx, HostModel& m);
 int step_plain(newt_gpu_ctx* ctx, int n_steps);
 int step_batched(newt_gpu_ctx* ctx, int n_steps);
-int autotune_batched(newt_gpu_ctx* ctx, int n_steps, int32_t* choice);
+int autotune_batched(newt_gpu_ctx* ctx, int n_steps, int horizon, int32_t* choice);
 
 // kernel launchers (defined in the .cu kernel files)
 extern "C" int newt_tree_bucket(int L);

@@ -384,12 +384,13 @@ int step_batched(newt_gpu_ctx* ctx, int n_steps) {
 // ---------------------------------------------------------------------------
 // Every trial steps the live worlds from a snapshot of every group's records
 // (model, state, status: the whole step state; solver scratch is rebuilt each
-// env-step), so the worlds end where they began.  Two snapshots are timed:
-// the worlds as they are, and as they are `settle` env-steps later (piles
-// that were falling have landed and their islands have grown), so a choice
-// that only wins on the early regime does not win overall.
-int autotune_batched(newt_gpu_ctx* ctx, int n_steps, int32_t* choice) {
-  if (n_steps <= 0) return NEWT_E_INVALID;
+// env-step), so the worlds end where they began.  Three snapshots are timed:
+// the worlds as they are, and horizon/2 and horizon env-steps later (piles
+// that were falling have landed and their islands have grown); a choice is
+// judged by the trapezoid average of its three times, so one that only wins
+// on the early regime does not win a horizon spent mostly settled.
+int autotune_batched(newt_gpu_ctx* ctx, int n_steps, int horizon, int32_t* choice) {
+  if (n_steps <= 0 || horizon <= 0) return NEWT_E_INVALID;
   std::vector<std::pair<void*, size_t>> live;
   for (auto& gp : ctx->groups) {
     HostGroup* g = gp.get();
@@ -397,7 +398,8 @@ int autotune_batched(newt_gpu_ctx* ctx, int n_steps, int32_t* choice) {
     live.push_back({g->dF, g->frows * (size_t)g->cap * sizeof(float)});
     live.push_back({g->dI, g->irows * (size_t)g->cap * sizeof(int)});
   }
-  std::vector<void*> snap[2];
+  constexpr int NSNAP = 3;
+  std::vector<void*> snap[NSNAP];
   int rc = NEWT_OK;
   auto take = [&](int k) -> int {
     for (auto& b : live) {
@@ -418,8 +420,9 @@ int autotune_batched(newt_gpu_ctx* ctx, int n_steps, int32_t* choice) {
   // island-class pipeline with 1, 2 or 3 world-range branches; trees: full
   // or half persistent grid
   struct Cand { int fused, shape, branches, grid_pct; };
-  const Cand cands[] = {{1, 0, 0, 100}, {1, 1, 0, 100}, {1, 2, 0, 100}, {1, 3, 0, 100}, {0, 0, 1, 100},
-                        {0, 0, 2, 100}, {0, 0, 3, 100}, {1, 1, 0, 50}, {0, 0, 2, 50}};
+  const Cand cands[] = {{1, 0, 0, 100}, {1, 1, 0, 100}, {1, 2, 0, 100}, {1, 3, 0, 100}, {1, 4, 0, 100},
+                        {1, 5, 0, 100}, {0, 0, 1, 100}, {0, 0, 2, 100}, {0, 0, 3, 100}, {1, 1, 0, 50},
+                        {0, 0, 2, 50}};
   const Cand start{ctx->tune_pile_fused, ctx->tune_fused_shape, ctx->tune_branches, ctx->tune_tree_grid_pct};
   auto set = [&](const Cand& c) {
     ctx->tune_pile_fused = c.fused;
@@ -428,19 +431,25 @@ int autotune_batched(newt_gpu_ctx* ctx, int n_steps, int32_t* choice) {
     ctx->tune_tree_grid_pct = c.grid_pct;
     ctx->graph_dirty = true;
   };
+  // snapshots at env-steps 0, horizon/2 and horizon, stepped with the current choice
   rc = take(0);
-  // the settled snapshot: `settle` env-steps further on, with the current choice
-  const int settle = 8 * n_steps;
-  if (rc == NEWT_OK) rc = step_batched(ctx, n_steps);
-  for (int k = 1; rc == NEWT_OK && k * n_steps < settle; ++k) rc = step_batched(ctx, n_steps);
-  if (rc == NEWT_OK) rc = take(1);
+  for (int k = 1, done = 0; k < NSNAP && rc == NEWT_OK; ++k) {
+    const int target = (int)((int64_t)horizon * k / (NSNAP - 1));
+    while (rc == NEWT_OK && done < target) {
+      const int m = std::min(n_steps, target - done);
+      rc = step_batched(ctx, m);
+      done += m;
+    }
+    if (rc == NEWT_OK) rc = take(k);
+  }
+  const float weight[NSNAP] = {0.25f, 0.5f, 0.25f};
   Cand best = start;
   float best_ms = -1.f;
   for (const Cand& c : cands) {
     if (rc != NEWT_OK) break;
     set(c);
     float total = 0.f;
-    for (int ph = 0; ph < 2 && rc == NEWT_OK; ++ph) {
+    for (int ph = 0; ph < NSNAP && rc == NEWT_OK; ++ph) {
       // first call captures (and warms up); the second is timed
       for (int rep = 0; rep < 2 && rc == NEWT_OK; ++rep) {
         if ((rc = restore(ph)) != NEWT_OK) break;
@@ -452,14 +461,14 @@ int autotune_batched(newt_gpu_ctx* ctx, int n_steps, int32_t* choice) {
       if (cudaEventSynchronize(ctx->ev[1]) != cudaSuccess) { rc = NEWT_E_CUDA; break; }
       float ms = 0.f;
       cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
-      total += ms;
+      total += weight[ph] * ms;
     }
     if (rc != NEWT_OK) break;
     if (best_ms < 0.f || total < best_ms) { best_ms = total; best = c; }
   }
   if (!snap[0].empty() && rc == NEWT_OK) rc = restore(0);
   cudaStreamSynchronize(ctx->stream);
-  for (int k = 0; k < 2; ++k)
+  for (int k = 0; k < NSNAP; ++k)
     for (void* p : snap[k]) cudaFree(p);
   set(best);
   if (choice) {
