@@ -29,7 +29,8 @@
 //                                 (plane, geom) label swap of :2509-2587
 // Changes that only move rounding:
 //   * M = sum_l J_l^T diag(m_l, I_l) J_l from the link COM Jacobians (the CRB
-//     recursion's matrix);
+//     recursion's matrix), their lever arms carried up the chain joint by
+//     joint, as the recursion's local transforms carry them;
 //   * A = Y^T Y with Y = L^-1 J^T (newt solves M^-1 J^T column by column);
 //   * the line search walks newt's candidate set (the breakpoints where a
 //     non-negative coordinate reaches zero, and each window's minimiser of
@@ -41,13 +42,17 @@
 //     the contact forces (the ABA is linear in the applied forces).
 // FP64: when the FP32 Cholesky of the Newton Hessian has a pivot ratio
 // (max L_ii / min L_ii)^2 above 1e6, the factor and the direction solves are
-// redone in FP64 (status bit NEWT_WS_FP64_FALLBACK).  Trees above 32 DoF get
-// one FP64 residual-refinement step of the mass-matrix solve that turns the
-// contact impulses into accelerations: with x the FP32 solution of
-// M' x = J^T f / dt (M' = M + dt B, factored in FP32), r = J^T f / dt - M' x
-// is formed in FP64 from an FP32 copy of M', the correction solved in FP64
-// with the FP32 factor, and x += that correction (the mixed-precision
-// refinement of the solve newt runs in cholesky_solve, dynamics.rs:630-648).
+// redone in FP64 (status bit NEWT_WS_FP64_FALLBACK).  Trees above 24 DoF sum
+// the mass matrix in FP64 (from the f32 Jacobians; each product is exact in
+// double) and get one FP64 residual-refinement step of the mass-matrix solve
+// that turns the contact impulses into accelerations: with x the FP32
+// solution of M' x = J^T f / dt (M' = M + dt B, its FP64 sum rounded and
+// factored in FP32), r = J^T f / dt - M' x is formed in FP64 with the FP64
+// M', the correction solved in FP64 with the FP32 factor, and x += that
+// correction (the mixed-precision refinement of the solve newt runs in
+// cholesky_solve, dynamics.rs:630-648).  On a straight 45-DoF chain an f32
+// sum of M alone leaves 3e-3 of relative error in qacc after an f32 solve,
+// the FP64 sum with the refinement 1e-5.
 #include <algorithm>
 
 #include "../../include/newt_gpu.h"
@@ -122,7 +127,7 @@ struct TcLay {
   int jv, jw, iw, con, jt, j0, H, LH, LHd, imp, misc, qfc, mc, rd, words;
 };
 NEWT_HD int up4(int n) { return (n + 3) / 4 * 4; }
-constexpr int REFINE_NV = 32;  // DoF above which the mass-matrix solve is refined in FP64
+constexpr int REFINE_NV = 24;  // DoF above which M is summed and the mass-matrix solve refined in FP64
 NEWT_HD TcLay tc_layout(int L, int nv, int ng, int maxc) {
   TcLay t;
   t.L = L; t.nv = nv; t.ng = ng; t.maxc = maxc;
@@ -140,7 +145,7 @@ NEWT_HD TcLay tc_layout(int L, int nv, int ng, int maxc) {
   t.imp = f; f += up4(t.ld);
   t.misc = f; f += 8;  // ncon, nrows, newton iterations
   t.qfc = f; f += up4(nv);  // RK4 worlds: J^T f / dt, held over the integrator's stages
-  t.mc = f; f += nv > REFINE_NV ? up4(nv * nv) : 0;  // trees above REFINE_NV DoF: M' before factoring
+  t.mc = f; f += nv > REFINE_NV ? up4(2 * nv * nv) : 0;  // trees above REFINE_NV DoF: M' in FP64 (lower)
   t.rd = f; f += nv > REFINE_NV ? up4(4 * nv) : 0;   // and two FP64 vectors (right-hand side, residual)
   t.words = (f + 31) / 32 * 32;
   return t;
@@ -314,34 +319,46 @@ namespace {
 
 // Columns of the world-frame point Jacobian of link `l` at `pt`
 // (jacobian.rs:38-120), walking the chain to the root; `col(k, rot, trans)`
-// receives every DoF column of the chain.
+// receives every DoF column of the chain.  The lever arm from each joint to
+// `pt` is carried up the chain as `d`, the point relative to the current
+// link's origin, advanced by the joint's own offsets (origin_i - origin_p =
+// R_p jp (+ R_p axis q for a slide) - R_i jc); differencing world positions
+// instead rounds every arm at the scale of the distance from the world
+// origin, which on long chains costs most of the digits of the short arms
+// between neighbouring links.
 template <class F>
 NEWT_D void chain_columns(const TreeGroupDev& g, int w, const float* pose, int l, V3 pt, F col) {
   const int cap = g.cap;
+  V3 d = pt - ldv3(pose + 7 * l);
   for (int i = l; i >= 0; i = g.topo[4 * i]) {
     const int jt = g.topo[4 * i + 1], vo = g.topo[4 * i + 3];
-    if (jt == JF) {
-      const float* pi = pose + 7 * i;
-      const Q4 o = Q4{pi[3], pi[4], pi[5], pi[6]};
-      const V3 r = pt - ldv3(pi);
+    const float* pi = pose + 7 * i;
+    const Q4 oi = Q4{pi[3], pi[4], pi[5], pi[6]};
+    if (jt == JF) {  // the root (links 1.. have hinge, slide or fixed joints)
       for (int k = 0; k < 3; ++k) {
-        const V3 aw = qrot(o, v3(k == 0 ? 1.f : 0.f, k == 1 ? 1.f : 0.f, k == 2 ? 1.f : 0.f));
-        col(vo + k, aw, cross(aw, r));
+        const V3 aw = qrot(oi, v3(k == 0 ? 1.f : 0.f, k == 1 ? 1.f : 0.f, k == 2 ? 1.f : 0.f));
+        col(vo + k, aw, cross(aw, d));
         col(vo + 3 + k, v3(0.f, 0.f, 0.f), aw);
       }
-    } else if (jt == JH || jt == JS) {
-      const float* pp = pose + 7 * g.topo[4 * i];
-      const Q4 po = Q4{pp[3], pp[4], pp[5], pp[6]};
+    }
+    if (i == 0) break;
+    const float* pp = pose + 7 * g.topo[4 * i];
+    const Q4 po = Q4{pp[3], pp[4], pp[5], pp[6]};
+    const V3 jp = v3(g.jp[(3 * i) * cap + w], g.jp[(3 * i + 1) * cap + w], g.jp[(3 * i + 2) * cap + w]);
+    const V3 jc = v3(g.jc[(3 * i) * cap + w], g.jc[(3 * i + 1) * cap + w], g.jc[(3 * i + 2) * cap + w]);
+    const V3 cw = qrot(oi, jc);  // joint anchor relative to link i's origin
+    V3 step = qrot(po, jp) - cw;  // link i's origin relative to its parent's
+    if (jt == JH || jt == JS) {
       const V3 ax = v3(g.axis[(3 * i) * cap + w], g.axis[(3 * i + 1) * cap + w], g.axis[(3 * i + 2) * cap + w]);
       const V3 aw = qrot(po, ax);
       if (jt == JH) {
-        const V3 jp = v3(g.jp[(3 * i) * cap + w], g.jp[(3 * i + 1) * cap + w], g.jp[(3 * i + 2) * cap + w]);
-        const V3 jw = ldv3(pp) + qrot(po, jp);
-        col(vo, aw, cross(aw, pt - jw));
+        col(vo, aw, cross(aw, d - cw));
       } else {
         col(vo, v3(0.f, 0.f, 0.f), aw);
+        step = step + qrot(po, ax * g.q[g.topo[4 * i + 2] * cap + w]);
       }
     }
+    d = d + step;
   }
 }
 
@@ -575,11 +592,19 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   auto subtree = [&](int a) {
     return ((unsigned long long)(unsigned)dmask[2 * a + 1] << 32) | (unsigned)dmask[2 * a];
   };
+  // Trees above REFINE_NV DoF sum the entries in FP64 (every f32 product is
+  // exact in double) and keep that M' for the refinement's residual: on long
+  // chains the f32 sums of long-lever products lose the digits that the
+  // ill-conditioned solve amplifies, and a refinement against an f32 M'
+  // converges to the wrong matrix's solution.
+  const bool refine = nv > REFINE_NV;
+  double* Md = refine ? reinterpret_cast<double*>(wf + lay.mc) : nullptr;
   for (int e = lane; e < nv * nv; e += 32) {
     const int i = e % nv, j = e / nv;
     if (i < j) continue;
     const int ai = dlink[i], aj = dlink[j];
     float s = 0.f;
+    double sd = 0.0;
     if ((subtree(aj) >> ai) & 1ull)
       for (unsigned long long m = subtree(ai); m; m &= m - 1ull) {
         const int l = __ffsll((long long)m) - 1;
@@ -587,8 +612,21 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
         const float* jw = JW + 3 * nv * l;
         const float* iw = IW + 6 * l;
         const S3 I{iw[0], iw[1], iw[2], iw[3], iw[4], iw[5]};
-        s += MS[l] * dot(ldv3(jv + 3 * i), ldv3(jv + 3 * j)) + dot(ldv3(jw + 3 * i), smv(I, ldv3(jw + 3 * j)));
+        const V3 vi = ldv3(jv + 3 * i), vj = ldv3(jv + 3 * j), wi = ldv3(jw + 3 * i), wj = ldv3(jw + 3 * j);
+        if (refine) {
+          const double Iwj[3] = {(double)I.xx * wj.x + (double)I.xy * wj.y + (double)I.xz * wj.z,
+                                 (double)I.xy * wj.x + (double)I.yy * wj.y + (double)I.yz * wj.z,
+                                 (double)I.xz * wj.x + (double)I.yz * wj.y + (double)I.zz * wj.z};
+          sd += (double)MS[l] * ((double)vi.x * vj.x + (double)vi.y * vj.y + (double)vi.z * vj.z) +
+                ((double)wi.x * Iwj[0] + (double)wi.y * Iwj[1] + (double)wi.z * Iwj[2]);
+        } else {
+          s += MS[l] * dot(vi, vj) + dot(wi, smv(I, wj));
+        }
       }
+    if (refine) {
+      Md[(size_t)j * nv + i] = sd;
+      s = (float)sd;
+    }
     LD[j * nv + i] = s;
   }
   __syncwarp();
@@ -601,21 +639,20 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
       const int jt = g.topo[4 * i + 1], vo = g.topo[4 * i + 3];
       if (jt == JF) {
         const float dm = rk4 ? 0.f : dt * g.damp[i * cap + w];
-        for (int k = 0; k < 6; ++k) LM[(vo + k) * nv + vo + k] += dm;
+        for (int k = 0; k < 6; ++k) {
+          LM[(vo + k) * nv + vo + k] += dm;
+          if (refine) Md[(size_t)(vo + k) * nv + vo + k] += (double)dm;
+        }
       } else if (jt == JH || jt == JS) {
         const float arm = g.arm[i * cap + w];
+        const float add = arm + (rk4 ? 0.f : dt * g.damp[i * cap + w]);
         LD[vo * nv + vo] += arm;
-        LM[vo * nv + vo] += arm + (rk4 ? 0.f : dt * g.damp[i * cap + w]);
+        LM[vo * nv + vo] += add;
+        if (refine) Md[(size_t)vo * nv + vo] += (double)add;
       }
     }
   }
   __syncwarp();
-  const bool refine = nv > REFINE_NV;
-  if (refine) {  // M' (lower triangle) for the FP64 residual
-    float* mc = wf + lay.mc;
-    for (int k = lane; k < nv * nv; k += 32) mc[k] = LM[k];
-    __syncwarp();
-  }
   float mn, mx;
   if (!warp_cholesky2(LM, LD, nv, nv, lane)) {
     if (lane == 0) atomicOr(g.status + w, status | NEWT_WS_NOT_PD);
@@ -891,17 +928,14 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   __syncwarp();
   warp_llt_solve(LM, nv, nv, vg, lane);
   if (refine) {
-    // r = rhs - M' x in FP64 (M' symmetric, its lower triangle kept), then
-    // M' d = r with the FP32 factor in FP64 arithmetic, x += d
-    const float* mc = wf + lay.mc;
+    // r = rhs - M' x in FP64 (M' summed in FP64, symmetric, its lower
+    // triangle kept), then M' d = r with the FP32 factor in FP64 arithmetic,
+    // x += d
     double* r = rhs + nv;
     __syncwarp();
     for (int i = lane; i < nv; i += 32) {
       double s = rhs[i];
-      for (int j = 0; j < nv; ++j) {
-        const float mij = i >= j ? mc[(size_t)j * nv + i] : mc[(size_t)i * nv + j];
-        s -= (double)mij * (double)vg[j];
-      }
+      for (int j = 0; j < nv; ++j) s -= (i >= j ? Md[(size_t)j * nv + i] : Md[(size_t)i * nv + j]) * (double)vg[j];
       r[i] = s;
     }
     __syncwarp();

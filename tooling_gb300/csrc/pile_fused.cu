@@ -6,10 +6,11 @@
 //                  (pile_collide.cuh, unchanged);
 //   assemble       the active contacts in contact order and, per contact, a
 //                  compact row record (below);
-//   levels         contact k sits at level 1 + max(level of the last earlier
-//                  contact on each of its dynamic bodies);
-//   sweeps         PGS: levels in order, the contacts of one level (they touch
-//                  disjoint bodies) on the warp's eight four-lane groups;
+//   rounds         contact k goes to the first round after the rounds of
+//                  the last earlier contacts on its dynamic bodies that still
+//                  has one of the warp's eight four-lane groups free;
+//   sweeps         PGS: rounds in order, the contacts of one round (they touch
+//                  disjoint bodies) on the warp's four-lane groups;
 //   integrate      semi-implicit Euler or RK4 (pile_solver.cuh, unchanged).
 // The state stays in the scratch record between env-steps and goes back to
 // the world record once, after the last one.
@@ -40,16 +41,17 @@
 // Gauss-Seidel order.  newt sweeps each island's contacts in contact order.
 // A contact update reads the velocity accumulators of its (at most two)
 // dynamic bodies, which only earlier contacts on the same bodies have
-// changed; running the levels in order therefore reproduces the serial
+// changed; running the rounds in order therefore reproduces the serial
 // sweep of every island exactly (islands never share a body).
 //
 // Row record.  A pyramidal contact has four facet rows r = n + s_r mu t_q(r)
 // (s = +, -, +, -; q = 1, 1, 2, 2).  The record keeps the Jacobian of the
 // normal and of both tangents and their M^-1 J^T per lane triple (side a
 // linear, side a angular, side b linear, side b angular; zero for a static
-// side), so the four lanes of a contact run one code path, the exact row-space block
-// A_rs = J_r M^-1 J_s^T, newt's row diagonals (row_body_diagonal plus the
-// regulariser), the biases and the pair determinants.  One contact update
+// side, so the four lanes of a contact run one code path), the exact
+// row-space block A_rs = J_r M^-1 J_s^T, newt's row diagonals
+// (row_body_diagonal plus the regulariser), the biases and the pair
+// determinants.  One contact update
 // takes three four-lane dot products (J_n.v, J_t1.v, J_t2.v) for the four
 // facet residuals, runs newt's row steps in registers -- the non-negative
 // step on row 0, then the pyramidal pairs (0,1) and (2,3) -- advancing the
@@ -217,27 +219,36 @@ NEWT_D int fused_assemble(const WsLay& L, float* wf, int* wi, int lane, float (*
 }
 
 // ---------------------------------------------------------------------------
-// levels: lane 0 assigns each record its level and counting-sorts the
-// records by level (sweep order inside a level); `loff` gets the level
-// starts and the end.  Returns the level count.
+// levels: lane 0 assigns each record its round (at most eight records, on
+// disjoint bodies) and counting-sorts the records by round (sweep order
+// inside a round); `loff` gets the round starts and the end.  Returns the
+// round count.
 // ---------------------------------------------------------------------------
 NEWT_D int fused_levels(const WsLay& L, const float* wf, int nact, int lane, short* last, short* lev, short* perm,
                         short* loff) {
   int nlev = 0;
+  for (int v = lane; v <= nact; v += 32) loff[v] = 0;  // contacts per round
+  __syncwarp();
   if (lane == 0) {
+    // List scheduling with eight contacts (the warp's four-lane groups) per
+    // round: contact k takes the first round after the last rounds of its
+    // bodies that still has a free group.  Every body still sees its
+    // contacts in contact order and no round holds two contacts of one
+    // body, so the sweep equals the serial one; islands fill each other's
+    // rounds instead of spilling a crowded level into a second round.
     const int nb = L.nb;
     for (int b = 0; b <= nb; ++b) last[b] = 0;
     for (int k = 0; k < nact; ++k) {
       const float* rec = wf + L.sc + FR * k;
       const int ba = __float_as_int(rec[R_MISC + 2]), bb = __float_as_int(rec[R_MISC + 3]);
-      const int lv = 1 + max(ba < nb ? (int)last[ba] : 0, bb < nb ? (int)last[bb] : 0);
+      int lv = 1 + max(ba < nb ? (int)last[ba] : 0, bb < nb ? (int)last[bb] : 0);
+      while (loff[lv] >= 8) ++lv;  // lv <= k + 1 <= nact: rounds 1..k hold at most k contacts
+      loff[lv]++;
       if (ba < nb) last[ba] = (short)lv;
       if (bb < nb) last[bb] = (short)lv;
       lev[k] = (short)lv;
       nlev = max(nlev, lv);
     }
-    for (int v = 0; v <= nlev; ++v) loff[v] = 0;
-    for (int k = 0; k < nact; ++k) loff[lev[k]]++;
     int run = 0;
     for (int v = 1; v <= nlev; ++v) { const int c = loff[v]; loff[v - 1] = (short)run; run += c; }
     loff[nlev] = (short)run;
@@ -369,8 +380,8 @@ __global__ void __launch_bounds__(1024) pile_k_queue_sort(const unsigned* __rest
 }
 
 // Shared memory of one warp: velocity accumulators (nb + 1 bodies, the last
-// a static side's zero), the level sort (last level per body, level per
-// record, records by level, level starts), each part 16-byte aligned.
+// a static side's zero), the round schedule (last round per body, round per
+// record, records by round, round starts), each part 16-byte aligned.
 struct WarpSmem {
   int acc, last, lev, perm, loff, bytes;
 };
