@@ -50,9 +50,10 @@ FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 # application of :2022)
 PGS_FLOP_PER_CONTACT_SWEEP = 5 * 235
 # DRAM bytes (read + write) per world and env-step of pile_k_fused, from the
-# ncu capture summarised in profiles/pile_k_fused_2048worlds_full.md (2048
-# worlds, one launch of 25 env-steps), scaled by worlds x env-steps
-FUSED_DRAM_BYTES_PER_WORLD_STEP = None
+# ncu capture summarised in profiles/pile_k_fused_2048worlds_settled_full.md
+# (2048 settled worlds, one launch of 25 env-steps: 25.5 MB read + 211.3 MB
+# written), scaled by worlds x env-steps
+FUSED_DRAM_BYTES_PER_WORLD_STEP = (25.547776e6 + 211.28448e6) / (2048 * 25)
 
 
 def parse():
@@ -329,6 +330,9 @@ def run_gpu(args, rank, ws, local, dist):
         traffic = (FUSED_DRAM_BYTES_PER_WORLD_STEP * W * S) if FUSED_DRAM_BYTES_PER_WORLD_STEP else None
         roof = {"bound": "fp32", "kernel": dom, "achieved": achieved, "peak": FP32_PEAK_TFLOPS, "unit": "TFLOP/s",
                 "frac": achieved / FP32_PEAK_TFLOPS if achieved else None, "traffic": traffic,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one settled 2048-world "
+                                  "launch (profiles/pile_k_fused_2048worlds_settled_full.md), per world-step, "
+                                  "scaled to this launch's worlds x env-steps",
                 "peak_source": "derived from datasheet figures (152 SMs x 128 FP32 lanes x 2 x 2.07 GHz); "
                                "MEASURED_PEAKS.json has no FP32 figure",
                 "flop_per_launch": flops, "flop_formula": "5 x 235 FLOP x 50 sweeps per active contact and env-step "
