@@ -177,11 +177,14 @@ NEWT_API int newt_gpu_set_qfrc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t 
  *   replayed: trees run the horizon in one persistent launch per size bucket
  *   over a cost-sorted queue; pile worlds of every size run theirs in one
  *   world-persistent launch (a warp per world for the whole horizon, worlds
- *   pulled from a queue sorted by size, largest first); tree-contact worlds
- *   run their three kernels per env-step on a third branch of the graph.
- *   newt_gpu_autotune may instead pick the island-class pipeline for piles
- *   (collide, island-class solvers on forked streams, integrate, per
- *   env-step). */
+ *   pulled from a queue sorted by the previous call's cost, most costly
+ *   first); tree-contact worlds run their three kernels per env-step on a
+ *   branch of the graph.  newt_gpu_autotune may instead pick the
+ *   island-class pipeline for piles (collide, island-class solvers on forked
+ *   streams, integrate, per env-step).  Pile worlds under the Newton solver
+ *   (solve_free_body_newton_impulses, newt/src/solver.rs:1295-1407) run
+ *   collide, a dense Newton solve (a warp per world) and integrate per
+ *   env-step in both modes. */
 #define NEWT_STEP_PLAIN 0
 #define NEWT_STEP_BATCHED 1
 NEWT_API int newt_gpu_step(newt_gpu_ctx* ctx, int32_t n_steps, int32_t mode);
@@ -194,7 +197,8 @@ NEWT_API int newt_gpu_step(newt_gpu_ctx* ctx, int32_t n_steps, int32_t mode);
  * allocate or free device memory while they step.  About 131 KB per
  * 16-body pile world (some 250 such worlds fit); a context that needs more
  * gets NEWT_E_NOMEM before anything is launched.  Tree worlds need no
- * scratch; tree-contact worlds are refused (NEWT_E_INVALID).
+ * scratch; tree-contact worlds and pile worlds under the Newton solver are
+ * refused (NEWT_E_INVALID).
  * The first call on a device sets up (symbol lookup, kernel loading): make it
  * before any stream capture.  There is one array per device, so calls whose
  * GPU work can overlap (two contexts or threads on one device) race; order

@@ -130,6 +130,7 @@ static void pile_rows(HostGroup& g) {
 size_t HostGroup::bytes_per_world() const {
   size_t b = frows * sizeof(float) + irows * sizeof(int);
   if (kind == GK_PILE) b += newt_pile_ws_bytes(size, np, maxc);
+  if (kind == GK_PILE && pile_newton) b += newt_pile_newton_bytes(maxc);
   if (kind == GK_TREE_CONTACT) b += newt_tc_ws_bytes(size, nv, ng, maxc);
   return b;
 }

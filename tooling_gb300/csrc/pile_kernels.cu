@@ -972,6 +972,26 @@ extern "C" int newt_launch_pile_step(const PileGroupDev* dG, const int* dwseg, i
   return N_ICLASS + 2;
 }
 
+// The collide and integrate stages alone, for the free-body Newton step
+// (pile_newton.cu): the island lists collide appends to are not read there,
+// but their counters are zeroed so every append stays in bounds.
+extern "C" void pile_k_collide_launch(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
+                                      int total_slots, int* lists, cudaStream_t st) {
+  IslandLists il;
+  il.items = lists;
+  il.cap = total_slots;
+  il.stats = 0;
+  il.counts = lists + (size_t)N_ICLASS * total_slots;
+  cudaMemsetAsync(il.counts, 0, N_COUNTERS * sizeof(int), st);
+  const int wpb = 4;
+  pile_k_collide<<<(total_worlds + wpb - 1) / wpb, 32 * wpb, 0, st>>>(dG, dwseg, ng, total_worlds, il);
+}
+extern "C" void pile_k_integrate_launch(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
+                                        int write_diag, cudaStream_t st) {
+  const int wpb = 4;
+  pile_k_integrate<<<(total_worlds + wpb - 1) / wpb, 32 * wpb, 0, st>>>(dG, dwseg, ng, total_worlds, write_diag);
+}
+
 // Loads every kernel of the pile step and sizes the list grids, so that the
 // launches that follow create nothing on the device.  Returns the first CUDA
 // error met.

@@ -134,7 +134,8 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
         return fail(ctx, NEWT_E_INVALID, "free bodies need a positive mass and an invertible inertia");
     }
     if (np > NEWT_MAX_PLANES) return fail(ctx, NEWT_E_INVALID, "too many planes");
-    if (d.solver != NEWT_SOLVER_PGS) return fail(ctx, NEWT_E_INVALID, "GPU piles use the PGS solver");
+    if (d.solver != NEWT_SOLVER_PGS && d.solver != NEWT_SOLVER_NEWTON)
+      return fail(ctx, NEWT_E_INVALID, "GPU piles need the PGS or Newton solver");
     m.kind = GK_PILE; m.size = d.n_bodies; m.np = np;
     return NEWT_OK;
   }
@@ -181,6 +182,7 @@ HostGroup* find_or_make_group(newt_gpu_ctx* ctx, HostModel& m) {
   g->kind = m.kind; g->size = m.size; g->np = m.np; g->topo_key = m.key;
   g->nq = m.nq; g->nv = m.nv;
   g->maxc_cap = ctx->max_contacts;
+  g->pile_newton = m.kind == GK_PILE && m.solver == NEWT_SOLVER_NEWTON;
   if (m.kind == GK_TREE_CONTACT) g->setup_tc(m);
   g->id = (int)ctx->groups.size();
   m.group = g->id;

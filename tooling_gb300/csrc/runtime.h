@@ -36,8 +36,10 @@ struct HostModel {
       }
     }
     if (kind == GK_PILE) {
-      // geom order fixes the pair order; shapes may differ per world
+      // geom order fixes the pair order; shapes may differ per world; the
+      // solver picks the step's kernels
       k += "np"; k += std::to_string(np);
+      if (solver == NEWT_SOLVER_NEWTON) k += "newton";
     }
     return k;
   }
@@ -82,6 +84,7 @@ struct HostGroup {
   int* dgtopo = nullptr;
   int* dpairs = nullptr;
   bool soa() const { return kind == GK_TREE || kind == GK_TREE_CONTACT; }
+  bool pile_newton = false;  // pile worlds under newt's free-body Newton solve (pile_newton.cu)
   TcGroupDev tc_dev() const;
   void setup_tc(const HostModel& m);
   void* plain_scratch = nullptr;  // pile solver scratch, cap worlds (both step forms)
@@ -226,3 +229,4 @@ extern "C" void newt_launch_tree_plain(const TreeGroupDev& g, cudaStream_t st);
 extern "C" void newt_tc_offsets(int L, int nv, int ng, int maxc, int* con, int* imp, int* misc);
 extern "C" size_t newt_tc_ws_bytes(int L, int nv, int ng, int maxc);
 extern "C" size_t newt_pile_ws_bytes(int nb, int np, int maxc);
+extern "C" size_t newt_pile_newton_bytes(int maxc);

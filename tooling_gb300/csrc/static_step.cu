@@ -118,6 +118,7 @@ extern "C" NEWT_API int newt_gpu_step_static(newt_gpu_ctx* ctx, int32_t n_steps)
     if (g->n == 0) continue;
     if (g->kind == GK_TREE_CONTACT) return fail(ctx, NEWT_E_INVALID, "tree-contact worlds are not supported");
     if (g->kind != GK_PILE) continue;
+    if (g->pile_newton) return fail(ctx, NEWT_E_INVALID, "pile worlds under the Newton solver are not supported");
     if (ng == kMaxPileGroups) return fail(ctx, NEWT_E_INVALID, "more than 64 pile groups (distinct body counts)");
     table[ng] = g->pile_dev();
     seg[ng + 1] = seg[ng] + g->n;

@@ -35,6 +35,9 @@ extern "C" int newt_launch_pile_fused(const PileGroupDev* dG, const int* dwseg, 
                                       int* counter, int n_steps, int grid, unsigned long long* work, unsigned* cost,
                                       int nbm, int cm, int shape, cudaStream_t st);
 extern "C" int newt_tc_prepare(newt_gpu_ctx* ctx, HostGroup* g, int n_steps);
+extern "C" size_t newt_pile_newton_bytes(int maxc);
+extern "C" int newt_launch_pile_newton_step(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
+                                            int total_slots, int* lists, int write_diag, cudaStream_t st);
 extern "C" int newt_tc_launch(newt_gpu_ctx* ctx, HostGroup* g, int n_steps, cudaStream_t st, bool capturing);
 
 // Streams and events the pile step forks its island classes onto.
@@ -59,6 +62,7 @@ static int ensure_pile_scratch(newt_gpu_ctx* ctx, HostGroup* g) {
   int rs = ensure_pile_streams(ctx);
   if (rs != NEWT_OK) return rs;
   size_t per = newt_pile_ws_bytes(g->size, g->np, g->maxc);
+  if (g->pile_newton) per += newt_pile_newton_bytes(g->maxc);  // H, its factors, the solver vectors
   size_t need = per * (size_t)g->cap;
   if (g->plain_scratch_bytes < need) {
     if (g->plain_scratch) cudaFree(g->plain_scratch);
@@ -183,6 +187,10 @@ int step_plain(newt_gpu_ctx* ctx, int n_steps) {
       if (g->kind == GK_TREE) {
         newt_launch_tree_plain(g->tree_dev(), ctx->stream);
         ctx->launches += 2;
+      } else if (g->kind == GK_PILE && g->pile_newton) {
+        const auto& T = ctx->plain_tables[gi];
+        ctx->launches += newt_launch_pile_newton_step((const PileGroupDev*)T.dG, T.dseg, T.ng, T.worlds, T.slots,
+                                                      T.lists, s == n_steps - 1, ctx->stream);
       } else if (g->kind == GK_PILE) {
         const auto& T = ctx->plain_tables[gi];
         ctx->launches += newt_launch_pile_step((const PileGroupDev*)T.dG, T.dseg, T.ng, T.worlds, T.slots, T.lists,
@@ -232,11 +240,21 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
     L.grid = std::min(L.items, std::max(1, full * ctx->tune_tree_grid_pct / 100));
     tls.push_back(L);
   }
-  // piles, largest worlds first
-  std::vector<HostGroup*> piles;
+  // PGS piles, largest worlds first; Newton piles apart (their own table,
+  // stepped per env-step: collide, the dense Newton solve, integrate)
+  std::vector<HostGroup*> piles, npiles;
   long pile_worlds = 0;
   for (auto& gp : ctx->groups)
-    if (gp->n > 0 && gp->kind == GK_PILE) { piles.push_back(gp.get()); pile_worlds += gp->n; }
+    if (gp->n > 0 && gp->kind == GK_PILE) {
+      if (gp->pile_newton) { npiles.push_back(gp.get()); continue; }
+      piles.push_back(gp.get());
+      pile_worlds += gp->n;
+    }
+  PileTable nt;
+  if (!npiles.empty()) {
+    int rc = build_pile_table(ctx, npiles, nt, bufs, 0, 1);
+    if (rc != NEWT_OK) return rc;
+  }
   std::stable_sort(piles.begin(), piles.end(), [](HostGroup* a, HostGroup* b) { return a->size > b->size; });
   const bool fused = ctx->tune_pile_fused != 0;
   // fused: one table over every pile group; its flat world order is the
@@ -316,6 +334,9 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
   }
   const int tc_launches = (int)(ctx->launches - l0);
   const int64_t before = ctx->launches;
+  for (int s = 0; s < n_steps && nt.ng > 0; ++s)
+    ctx->launches += newt_launch_pile_newton_step(nt.dG, nt.dseg, nt.ng, nt.worlds, nt.slots, nt.lists,
+                                                  s == n_steps - 1, ctx->stream);
   int fused_launches = 0;
   if (fused && ft.ng > 0) {
     cudaStream_t fs = ctx->pbs[0][0];
