@@ -100,11 +100,12 @@ __global__ void __launch_bounds__(32) pile_k_newton(const PileGroupDev* G, const
     *ba = cc[2];
     *bb = cc[3];
   };
-  // H (lower triangle, column-major), the bias and a zero-friction flag
+  // H (column-major, every entry: newt's matrix is J_i M^-1 J_j^T entry by
+  // entry, its factor reads the lower triangle and its products the whole),
+  // the bias and a zero-friction flag
   bool zero_mu = false;
   for (int e = lane; e < nr * nr; e += 32) {
     const int i = e % nr, j = e / nr;
-    if (i < j) continue;
     const int ki = ord[i >> 2], kj = ord[j >> 2];
     const float* ri = sc0 + (size_t)SC * ki + S_ROWS + 32 * (i & 3);       // J of row i
     const float* rj = sc0 + (size_t)SC * kj + S_ROWS + 32 * (j & 3) + 16;  // M^-1 J^T of row j
