@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--rates", default="1000,5000,10000,20000,50000",
                     help="serve workload: Poisson request rates (req/s), one timed run each")
     ap.add_argument("--duration", type=float, default=1.5, help="serve workload: seconds of arrivals per rate")
+    ap.add_argument("--steps-per-tick", type=int, default=8,
+                    help="served rollouts: env-steps queued per serving tick (worlds held where their horizon ends)")
     ap.add_argument("--workload", default="pile", choices=["pile", "quadruped", "uneven", "serve"],
                     help="pile: 16 free bodies on a plane (default); quadruped: Newton tree contact; "
                          "uneven: chains and piles of 2..64 bodies, batched vs plain")
@@ -431,10 +433,11 @@ def run_uneven_compact(rank, ws, local, dist, n_worlds=32768, substeps=25, steps
     return out
 
 
-def run_served_compact(rank, ws, local, dist, rate=10000.0, duration=1.0, pool_worlds=4096):
+def run_served_compact(rank, ws, local, dist, rate=10000.0, duration=1.0, pool_worlds=4096, steps_per_tick=8):
     """The served configuration in brief: one Poisson stream at `rate` req/s
     over a pool of uneven worlds, horizons log-uniform in 10..1000, tau ~
-    N(0,1) per DoF per env-step, through newt_gpu_serve; p50/p99 latency."""
+    N(0,1) per DoF per env-step, through newt_gpu_serve with
+    `steps_per_tick` env-steps per serving tick; p50/p99 latency."""
     from tooling_gb300 import scenes
     pool = scenes.uneven_batch(n_worlds=pool_worlds, first_world=rank * pool_worlds)
     from tooling_gb300 import Engine
@@ -448,7 +451,7 @@ def run_served_compact(rank, ws, local, dist, rate=10000.0, duration=1.0, pool_w
         arrivals, world, hz, coff = serve_requests(rng, len(pool), nv, rate, d, tau)
         qp = np.concatenate([pool.qpos[pool.q_off[w]:pool.q_off[w] + pool.nq[w]] for w in world])
         qv = np.concatenate([pool.qvel[pool.v_off[w]:pool.v_off[w] + pool.nv[w]] for w in world])
-        oq, ov, st, _, _ = eng.serve(ids[world], hz, arrivals, qp, qv, tau, coff)
+        oq, ov, st, _, _ = eng.serve(ids[world], hz, arrivals, qp, qv, tau, coff, steps_per_tick=steps_per_tick)
         qo = np.concatenate([[0], np.cumsum(pool.nq[world])])
         bad = np.add.reduceat((~np.isfinite(oq)).astype(np.int64), qo[:-1]) if len(world) else np.zeros(0)
         st["requests"] = len(world)
@@ -462,6 +465,7 @@ def run_served_compact(rank, ws, local, dist, rate=10000.0, duration=1.0, pool_w
             "nonfinite_requests"]
     out = {k: st[k] for k in keep}
     out["rate_req_per_s"] = rate
+    out["steps_per_tick"] = steps_per_tick
     out["env_steps_per_s"] = st["env_steps"] / st["wall_s"] if st["wall_s"] > 0 else 0.0
     eng.close()
     return out
@@ -732,12 +736,13 @@ def run_gpu_serve(args, rank, ws, local, dist):
         qv = np.concatenate([pool.qvel[pool.v_off[w]:pool.v_off[w] + pool.nv[w]] for w in world])
         return qp, qv
 
-    def serve(rate, duration, mode=STEP_BATCHED):
+    def serve(rate, duration, mode=STEP_BATCHED, k=args.steps_per_tick):
         arrivals, world, hz, coff = serve_requests(rng, len(pool), nv, rate, duration, tau)
         qp, qv = inputs(world)
         barrier(dist)
         l0 = eng.launch_count()
-        oq, ov, st, admit, done = eng.serve(ids[world], hz, arrivals, qp, qv, tau, coff, mode=mode)
+        oq, ov, st, admit, done = eng.serve(ids[world], hz, arrivals, qp, qv, tau, coff, mode=mode,
+                                            steps_per_tick=k)
         st["launches"] = eng.launch_count() - l0
         st["requests"] = len(world)
         st["rate"] = rate
@@ -765,6 +770,7 @@ def run_gpu_serve(args, rank, ws, local, dist):
     clk["reasons"] = sorted(set(x for c in clk_runs for x in c.get("reasons", [])))
     top = runs[-1]
     plain = serve(top["rate"], args.duration, STEP_PLAIN) if not args.no_plain else None
+    one_step = serve(top["rate"], args.duration, k=1) if args.steps_per_tick > 1 else None
     ticks = max(1, top["ticks"])
     value = max_over_ranks(dist, 1.0 / top["env_steps_per_s"]) if top["env_steps_per_s"] > 0 else 0.0
     value = ws / value if value > 0 else 0.0
@@ -778,7 +784,8 @@ def run_gpu_serve(args, rank, ws, local, dist):
         "config": {"workload": "served rollouts: Poisson arrivals, uneven worlds (chains and piles, 2..64 "
                                "bodies), tau ~ N(0,1) per DoF per env-step, horizon log-uniform 10..1000",
                    "world_pool": len(pool), "rates_req_per_s": rates, "seconds_of_arrivals": args.duration,
-                   "step": "one env-step per tick, batched form (CUDA graph)",
+                   "step": f"{args.steps_per_tick} env-steps queued per tick (worlds held where their horizon "
+                           "ends), one step call per env-step, batched form (CUDA graph)",
                    "l2": "inputs resident; working set above L2 at the top rates",
                    "parallelism": f"replicas x{ws}"},
         "served": [{k: r[k] for k in keep} for r in runs],
@@ -789,6 +796,8 @@ def run_gpu_serve(args, rank, ws, local, dist):
         "gpu_launches": int(sum(r["launches"] for r in runs)),
         "clocks": clk,
     }
+    if one_step is not None:
+        out["one_step_ticks"] = {k: one_step[k] for k in keep}
     if plain is not None:
         out["plain_served"] = {k: plain[k] for k in keep}
         out["batched_over_plain"] = top["env_steps_per_s"] / plain["env_steps_per_s"] if plain["env_steps_per_s"] else None
@@ -923,7 +932,7 @@ def main():
     out, (batch, qp, qv) = run_gpu(args, rank, ws, local, dist)
     if not args.no_extras:
         out["uneven"] = run_uneven_compact(rank, ws, local, dist)
-        out["served"] = run_served_compact(rank, ws, local, dist)
+        out["served"] = run_served_compact(rank, ws, local, dist, steps_per_tick=args.steps_per_tick)
     if rank == 0:
         if not args.no_cpu and ws == 1:
             out["cpu_baseline"] = cpu_baseline(batch, qp, qv, args.substeps, steps=args.substeps * args.steps)

@@ -205,6 +205,13 @@ NEWT_API int newt_gpu_step(newt_gpu_ctx* ctx, int32_t n_steps, int32_t mode);
  * them (newt_gpu_sync between contexts). */
 #define NEWT_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
 NEWT_API int newt_gpu_step_static(newt_gpu_ctx* ctx, int32_t n_steps);
+/* Stops the named worlds from being stepped, on the device and without a
+ * host wait: ordered on the context's stream after the work already issued,
+ * so a caller that queues several step calls can end one world's horizon
+ * between two of them.  The worlds keep their state (newt_gpu_get_state
+ * reads it) and their slots until newt_gpu_free_worlds.  No counterpart in
+ * newt, whose caller simply stops calling World::step. */
+NEWT_API int newt_gpu_hold_worlds(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n);
 /* Waits for the context's stream (bounded host wait; NEWT_E_TIMEOUT). */
 NEWT_API int newt_gpu_sync(newt_gpu_ctx* ctx, int32_t timeout_ms);
 
@@ -344,8 +351,9 @@ NEWT_API int newt_gpu_apply_ctrl(newt_gpu_ctx* ctx);
  * world slot once it has arrived and the device budget allows
  * (newt_gpu_alloc_worlds answers NEWT_E_NOMEM past it; the request then
  * waits), its state stays on the device, every admitted world advances by
- * one env-step per tick through one step call (requests join and leave
- * between ticks), row t of its controls is applied as qfrc at its step t,
+ * one env-step per step call, `steps_per_tick` of them per tick (requests
+ * join and leave between ticks), row t of its controls is applied as qfrc
+ * at its step t,
  * and its final state is read back when its horizon completes (a horizon of
  * 0 returns the initial state without admission).  Latency = completion -
  * arrival (completion - call start when real_time is 0). */
@@ -365,6 +373,15 @@ typedef struct newt_serve_opts {
   int32_t max_active;      /* cap on admitted requests (0: the device budget only) */
   int32_t real_time;       /* 1: arrivals follow the wall clock; 0: all present at start */
   int32_t step_mode;       /* NEWT_STEP_BATCHED or NEWT_STEP_PLAIN */
+  int32_t steps_per_tick;  /* env-steps per tick (0 or 1: one).  Above one, a
+                            * tick queues that many env-steps (each with its
+                            * control row) without a host wait between them,
+                            * holds every world whose horizon ends inside the
+                            * tick at that env-step (newt_gpu_hold_worlds), and
+                            * admits and completes requests once per tick:
+                            * results are unchanged, host round trips per
+                            * env-step fall by that factor, and a request
+                            * waits up to a tick for admission. */
 } newt_serve_opts;
 typedef struct newt_serve_stats {
   int32_t completed, peak_active;

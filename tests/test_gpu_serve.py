@@ -4,8 +4,9 @@ between env-steps.  A request's result must not depend on what it was
 batched with: each final state equals, bit for bit, the same rollout run
 alone (one world, the same per-step controls, the same step form).
 
-Also covered: slot reuse under a captured step graph, admission against a
-device budget, Poisson arrivals on the wall clock, and the plain step form."""
+Also covered: several env-steps per tick (worlds held where their horizon
+ends), slot reuse under a captured step graph, admission against a device
+budget, Poisson arrivals on the wall clock, and the plain step form."""
 import numpy as np
 import pytest
 
@@ -98,6 +99,23 @@ def test_served_results_equal_alone(eng, worlds):
     assert e.memory()[0] > 0
     got = _split(e, mids, oq, ov)
     _check_alone(e, mids, hz, init, pool, coff, nv, got, range(len(mids)))
+
+
+@pytest.mark.parametrize("k", [4, 7])
+def test_multi_step_ticks_equal_alone(eng, worlds, k):
+    """steps_per_tick = k: a tick queues k env-steps (each with its control
+    row) without a host wait and holds every world whose horizon ends inside
+    it at that env-step.  Every result still equals its rollout run alone, bit
+    for bit, and the ticks fall by about k."""
+    e, ids = eng
+    mids, hz, qp, qv, pool, coff, nv, init = _requests(eng, ids, worlds, 60, seed=11)
+    _, _, one, _, _ = e.serve(mids, hz, np.zeros(len(mids)), qp, qv, pool, coff, max_active=16, real_time=False)
+    oq, ov, st, admit, done = e.serve(mids, hz, np.zeros(len(mids)), qp, qv, pool, coff, max_active=16,
+                                      real_time=False, steps_per_tick=k)
+    assert st["completed"] == len(mids) and st["env_steps"] == hz.sum()
+    assert (admit >= 0).all() and (done >= admit).all()
+    assert st["ticks"] * k >= one["ticks"] and st["ticks"] < one["ticks"] / (k / 2.0), (st["ticks"], one["ticks"])
+    _check_alone(e, mids, hz, init, pool, coff, nv, _split(e, mids, oq, ov), range(len(mids)))
 
 
 def test_plain_step_form(eng, worlds):

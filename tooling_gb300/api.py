@@ -31,7 +31,7 @@ EXPORTED = [
     "newt_gpu_flush_l2", "newt_gpu_launch_count", "newt_gpu_step_static", "newt_gpu_pile_profile",
     "newt_gpu_tc_profile", "newt_gpu_serve", "newt_gpu_memory", "newt_gpu_autotune",
     "newt_gpu_set_ctrl_stream", "newt_gpu_apply_ctrl", "newt_gpu_read_sensors", "newt_gpu_pile_fused_profile",
-    "newt_gpu_set_launch_choice", "newt_gpu_convex_contacts",
+    "newt_gpu_set_launch_choice", "newt_gpu_convex_contacts", "newt_gpu_hold_worlds",
 ]
 # newt_sensor_desc (include/newt_gpu.h)
 SENSOR_DTYPE = np.dtype([("kind", np.int32), ("on_link", np.int32), ("index", np.int32),
@@ -81,7 +81,8 @@ class ServeRequest(C.Structure):
 
 
 class ServeOpts(C.Structure):
-    _fields_ = [("max_active", C.c_int32), ("real_time", C.c_int32), ("step_mode", C.c_int32)]
+    _fields_ = [("max_active", C.c_int32), ("real_time", C.c_int32), ("step_mode", C.c_int32),
+                ("steps_per_tick", C.c_int32)]
 
 
 # newt_serve_request as a numpy record (same layout), so request tables are
@@ -141,6 +142,7 @@ def load_library(path: str = LIB_PATH):
         "newt_gpu_apply_ctrl": ([P], C.c_int),
         "newt_gpu_pile_fused_profile": ([P, P, P], C.c_int),
         "newt_gpu_set_launch_choice": ([P, P], C.c_int),
+        "newt_gpu_hold_worlds": ([P, P, I32], C.c_int),
         "newt_gpu_convex_contacts": ([P, P, I32, C.c_float, P], C.c_int),
     }
     for name, (args, res) in sig.items():
@@ -204,6 +206,12 @@ class Engine:
     def free(self, slots: Sequence[int]):
         s = np.ascontiguousarray(slots, np.int32)
         self._ck(self.L.newt_gpu_free_worlds(self.ctx, _p(s), len(s)))
+
+    def hold(self, slots: Sequence[int]):
+        """Stop stepping these worlds from the next step call on (queued on
+        the device, no wait); they keep their state until freed."""
+        s = np.ascontiguousarray(slots, np.int32)
+        self._ck(self.L.newt_gpu_hold_worlds(self.ctx, _p(s), len(s)))
 
     # -- state --------------------------------------------------------------
     def set_state(self, slots, qpos: np.ndarray, qvel: np.ndarray):
@@ -271,14 +279,16 @@ class Engine:
     # -- served rollouts -------------------------------------------------------
     def serve(self, model_ids, horizons, arrivals_s, qpos: np.ndarray, qvel: np.ndarray,
               ctrl: Optional[np.ndarray] = None, ctrl_off=None, max_active: int = 0,
-              real_time: bool = True, mode: int = STEP_BATCHED):
+              real_time: bool = True, mode: int = STEP_BATCHED, steps_per_tick: int = 1):
         """Serve rollout requests through the native loop (newt_gpu_serve).
 
         qpos / qvel: the requests' initial states concatenated in request
         order (MuJoCo layout).  ctrl: one flat float32 array; request i reads
         horizon_i x nv_i values from element ctrl_off[i] (-1: no controls).
-        Returns (final qpos, final qvel) concatenated like the inputs, a
-        stats dict, and the admission and completion times (s)."""
+        steps_per_tick: env-steps queued per tick (worlds that finish inside
+        a tick are held at their last env-step).  Returns (final qpos, final
+        qvel) concatenated like the inputs, a stats dict, and the admission
+        and completion times (s)."""
         n = len(model_ids)
         ids = np.ascontiguousarray(model_ids, np.int32)
         hz = np.ascontiguousarray(horizons, np.int32)
@@ -303,7 +313,7 @@ class Engine:
             if np.any((co >= 0) & (need > c.size)):
                 raise ValueError("a control window runs past the end of ctrl")
             r["ctrl"] = np.where(co >= 0, c.ctypes.data + 4 * np.maximum(co, 0), 0).astype(np.uint64)
-        opts = ServeOpts(int(max_active), int(bool(real_time)), int(mode))
+        opts = ServeOpts(int(max_active), int(bool(real_time)), int(mode), int(steps_per_tick))
         st = ServeStats()
         self._ck(self.L.newt_gpu_serve(self.ctx, r.ctypes.data, n, C.byref(opts), C.byref(st)))
         stats = {k: getattr(st, k) for k, _ in ServeStats._fields_}

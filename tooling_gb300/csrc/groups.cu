@@ -225,6 +225,11 @@ int HostGroup::reserve_indices(newt_gpu_ctx* ctx, int k, std::vector<int>& out) 
   return NEWT_OK;
 }
 
+int* HostGroup::live_flag(int idx) {
+  const int lrow = soa() ? ri_live : lay.live;
+  return soa() ? dI + (size_t)lrow * cap + idx : dI + (size_t)idx * irows + lrow;
+}
+
 int* HostGroup::release_index(int idx) {
   int lrow = soa() ? ri_live : lay.live;
   I(lrow, idx) = 0;

@@ -351,6 +351,20 @@ int newt_gpu_free_worlds(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n) {
   return release_slots(ctx, slots, n);
 }
 
+int newt_gpu_hold_worlds(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n) {
+  if (!ctx || (n > 0 && !slots) || n < 0) return NEWT_E_INVALID;
+  cudaSetDevice(ctx->device);
+  std::vector<int*> flags;
+  flags.reserve(n);
+  for (int i = 0; i < n; ++i) {
+    const int s = slots[i];
+    if (s < 0 || s >= (int)ctx->slots.size() || !ctx->slots[s].live) return fail(ctx, NEWT_E_INVALID, "bad slot");
+    const SlotRef& r = ctx->slots[s];
+    flags.push_back(ctx->groups[r.group]->live_flag(r.index));
+  }
+  return io_hold_flags(ctx, flags);
+}
+
 // Collects, per group, the worlds a call names (in call order), checking
 // every slot first.
 static int group_worlds(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, std::vector<std::vector<int>>& by_group) {

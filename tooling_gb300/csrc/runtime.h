@@ -93,6 +93,7 @@ struct HostGroup {
 
   int reserve_indices(newt_gpu_ctx* ctx, int k, std::vector<int>& out);
   int* release_index(int idx);  // host side; returns the world's device live flag
+  int* live_flag(int idx);      // the world's device live flag
   void write_model(newt_gpu_ctx* ctx, int idx, const HostModel& m);
   int flush_model(newt_gpu_ctx* ctx);
   // state in the host mirror for one world; moved to and from the device
@@ -215,6 +216,7 @@ struct RowMove {
 int io_scatter(newt_gpu_ctx* ctx, const std::vector<RowMove>& mv);  // host mirror -> device
 int io_gather(newt_gpu_ctx* ctx, const std::vector<RowMove>& mv);   // device -> host mirror
 int io_clear_flags(newt_gpu_ctx* ctx, const std::vector<int*>& flags);  // *flag = 0 on the device
+int io_hold_flags(newt_gpu_ctx* ctx, const std::vector<int*>& flags);   // the same, queued without a wait
 void ctrl_release_slot(newt_gpu_ctx* ctx, int slot);                     // ends the slot's control stream
 
 HostGroup* find_or_make_group(newt_gpu_ctx* ctx, HostModel& m);

@@ -8,11 +8,14 @@
 //               finds room in the device budget (NEWT_E_NOMEM: the request
 //               waits for completions); freed world slots are reused, so the
 //               captured step graph stays valid while no group grows
-//   tick        the next row of each admitted request's control stream
-//               (uploaded once at admission, newt_gpu_set_ctrl_stream) goes
-//               to its qfrc on the device, then one step call of one
-//               env-step advances every admitted world together (continuous
-//               batching)
+//   tick        `steps_per_tick` times: the next row of each admitted
+//               request's control stream (uploaded once at admission,
+//               newt_gpu_set_ctrl_stream) goes to its qfrc on the device,
+//               then one step call of one env-step advances every admitted
+//               world together (continuous batching); the env-steps of a
+//               tick are queued without a host wait, and a world whose
+//               horizon ends inside the tick is held at that env-step
+//               (newt_gpu_hold_worlds)
 //   completion  a request whose horizon is reached has its final state read
 //               back and its slot freed; latency = completion - arrival
 #include <algorithm>
@@ -48,6 +51,7 @@ extern "C" NEWT_API int newt_gpu_serve(newt_gpu_ctx* ctx, newt_serve_request* re
   const int max_active = opts && opts->max_active > 0 ? opts->max_active : (1 << 30);
   const bool real_time = !opts || opts->real_time != 0;
   const int mode = opts ? opts->step_mode : NEWT_STEP_BATCHED;
+  const int ksteps = opts && opts->steps_per_tick > 1 ? opts->steps_per_tick : 1;
   if (mode != NEWT_STEP_BATCHED && mode != NEWT_STEP_PLAIN) return NEWT_E_INVALID;
   std::memset(stats, 0, sizeof(*stats));
   for (int i = 0; i < n; ++i) {
@@ -68,7 +72,7 @@ extern "C" NEWT_API int newt_gpu_serve(newt_gpu_ctx* ctx, newt_serve_request* re
   size_t next = 0;
   int done = 0;
   double active_sum = 0.0;
-  std::vector<int32_t> ids, slots;
+  std::vector<int32_t> ids, slots, hold;
   std::vector<float> qp, qv, qf;
   bool full = false;  // the budget refused a world: wait for a completion
   // on an error the admitted worlds are released before returning
@@ -162,26 +166,39 @@ extern "C" NEWT_API int newt_gpu_serve(newt_gpu_ctx* ctx, newt_serve_request* re
       }
       continue;
     }
-    // ---- tick: the next control row of every stream, then one env-step ----
-    const double tc = now();
-    {
-      int rc = newt_gpu_apply_ctrl(ctx);
-      if (rc != NEWT_OK) return bail(rc);
+    // ---- tick: kt env-steps, each the next control row of every stream and
+    //      one step call, queued without a host wait; a world whose horizon
+    //      ends inside the tick is held at that env-step ----
+    int kt = 1;
+    for (const Active& a : active) kt = std::max(kt, std::min(ksteps, reqs[a.req].horizon - a.t));
+    int rc = NEWT_OK;
+    for (int s = 0; s < kt && rc == NEWT_OK; ++s) {
+      const double tc = now();
+      rc = newt_gpu_apply_ctrl(ctx);
+      const double ts = now();
+      stats->ctrl_s += ts - tc;
+      if (rc == NEWT_OK) rc = newt_gpu_step(ctx, 1, mode);
+      if (rc == NEWT_OK && s + 1 < kt) {
+        hold.clear();
+        for (const Active& a : active)
+          if (a.t + s + 1 == reqs[a.req].horizon) hold.push_back(a.slot);
+        if (!hold.empty()) rc = newt_gpu_hold_worlds(ctx, hold.data(), (int32_t)hold.size());
+      }
+      stats->step_s += now() - ts;
     }
-    const double ts = now();
-    stats->ctrl_s += ts - tc;
-    int rc = newt_gpu_step(ctx, 1, mode);
-    if (rc == NEWT_OK) rc = newt_gpu_sync(ctx, 600000);
+    if (rc == NEWT_OK) {
+      const double ts = now();
+      rc = newt_gpu_sync(ctx, 600000);
+      stats->step_s += now() - ts;
+    }
     if (rc != NEWT_OK) return bail(rc);
-    const double te = now();
-    stats->step_s += te - ts;
     stats->ticks += 1;
     active_sum += (double)active.size();
     stats->peak_active = std::max<int32_t>(stats->peak_active, (int32_t)active.size());
     // ---- completions ----
     std::vector<size_t> fin;
     for (size_t k = 0; k < active.size(); ++k) {
-      active[k].t += 1;
+      active[k].t = std::min(active[k].t + kt, reqs[active[k].req].horizon);
       if (active[k].t >= reqs[active[k].req].horizon) fin.push_back(k);
     }
     if (fin.empty()) continue;

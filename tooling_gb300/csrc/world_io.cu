@@ -220,6 +220,29 @@ int io_gather(newt_gpu_ctx* ctx, const std::vector<RowMove>& all) {
   return NEWT_OK;
 }
 
+// Up to 1024 live flags cleared by one launch with the pointers passed by
+// value (8 KB of parameters): nothing to stage, so the call returns at once.
+struct HoldList {
+  int n;
+  int* f[1024];
+};
+__global__ void flags_hold(HoldList L) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < L.n) *L.f[i] = 0;
+}
+
+int io_hold_flags(newt_gpu_ctx* ctx, const std::vector<int*>& flags) {
+  for (size_t a = 0; a < flags.size(); a += 1024) {
+    HoldList L;
+    L.n = (int)std::min<size_t>(1024, flags.size() - a);
+    for (int i = 0; i < L.n; ++i) L.f[i] = flags[a + i];
+    flags_hold<<<(L.n + 255) / 256, 256, 0, ctx->stream>>>(L);
+    ctx->launches++;
+    CKW(cudaGetLastError());
+  }
+  return NEWT_OK;
+}
+
 int io_clear_flags(newt_gpu_ctx* ctx, const std::vector<int*>& flags) {
   if (flags.empty()) return NEWT_OK;
   int rc = ensure_staging(ctx, 0, 2 * flags.size());  // one pointer = two floats' room
