@@ -716,8 +716,9 @@ def run_gpu_serve(args, rank, ws, local, dist):
     """Served rollouts: Poisson request streams over a pool of uneven worlds
     (chains and piles, 2..64 bodies), each request an initial state, a
     control sequence tau ~ N(0,1) per DoF per env-step and a log-uniform
-    horizon in 10..1000; admitted into free world slots, stepped one env-step
-    per tick with every other admitted request, read back at completion.
+    horizon in 10..1000; admitted into free world slots, stepped with every
+    other admitted request (--steps-per-tick env-steps per serving tick, a
+    world held at the env-step its horizon ends), read back at completion.
     Timed on the wall clock through newt_gpu_serve (host buffers in and out)."""
     from tooling_gb300 import build as B
     B.build()
