@@ -461,6 +461,72 @@ int oracle_sensors(const newt_model_desc* d, const float* qpos, const float* qve
   return 0;
 }
 
+// newt's post-step contact sensors for a free-body world
+// (world.rs:1545-1612 build_sensor_inputs, sensor.rs:446-757 evaluate,
+// :1030-1087 accelerometer_reading, :1103-1112 touch_reading): one step from
+// (qpos, qvel), then the step's contact set re-solved at the post-step
+// bodies with the world's solver (solve_free_bodies_diag or its Newton
+// variant, solver.rs:596-640), giving the body wrenches and the per-contact
+// normal forces (the contact's row impulses summed in row order, over dt,
+// solver.rs:1240-1253).  Kinds: 9 accelerometer (site on body `index`), 10
+// touch (geom `index`).  Writes the readings and the post-step state
+// (MuJoCo layout); returns -1 for a world with a tree or a failed Newton
+// factor.
+int oracle_contact_sensors(const newt_model_desc* d, const float* qpos, const float* qvel, int precision, int ns,
+                           const int* si, const float* sf, double* out, double* qpos_out, double* qvel_out) {
+  int rc = 0;
+  auto go = [&](auto tag) {
+    using R = decltype(tag);
+    World<R> w = build_world<R>(*d);
+    if (!w.trees.empty()) { rc = -1; return; }
+    set_state(w, qpos, qvel, 0);
+    std::vector<Contact<R>> contacts;
+    w.detect_contacts(contacts);
+    w.step();
+    std::vector<Wrench<R>> wr;
+    std::vector<R> imp;
+    std::vector<int> row_contact;
+    if (w.solver_mode == M_NEWTON) {
+      if (!solve_free_bodies_newton(w.bodies, w.geoms, contacts, w.gravity, w.dt, w.iterations, wr, &imp,
+                                    &row_contact)) { rc = -1; return; }
+    } else {
+      solve_free_bodies_pgs(w.bodies, w.geoms, contacts, w.gravity, w.dt, w.iterations, wr, &imp, &row_contact);
+    }
+    if (wr.empty()) wr.assign(w.bodies.size(), Wrench<R>{Vec3<R>(), Vec3<R>()});
+    std::vector<R> fn(contacts.size(), R(0));
+    for (size_t r = 0; r < imp.size(); ++r) fn[row_contact[r]] += imp[r];
+    for (R& x : fn) x = x / w.dt;
+    int o = 0;
+    for (int k = 0; k < ns; ++k) {
+      const int kind = si[3 * k], idx = si[3 * k + 2];
+      if (kind == 10) {
+        R sum = R(0);
+        for (size_t c = 0; c < contacts.size(); ++c)
+          if (contacts[c].ga == idx || contacts[c].gb == idx) sum += fn[c] < R(0) ? -fn[c] : fn[c];
+        out[o++] = (double)sum;
+        continue;
+      }
+      const Vec3<R> lp(sf[7 * k], sf[7 * k + 1], sf[7 * k + 2]);
+      const Quat<R> lq(sf[7 * k + 3], sf[7 * k + 4], sf[7 * k + 5], sf[7 * k + 6]);
+      const Body<R>& b = w.bodies[idx];
+      const Vec3<R> a_com = w.gravity + wr[idx].f / b.mass;
+      const Vec3<R> tau_body = b.ori.inverse_rotate(wr[idx].t);
+      const Vec3<R> iw = b.inertia * b.omega_body;
+      const Vec3<R> gyro = -(b.omega_body.cross(iw));
+      const Vec3<R> alpha_body = b.inertia_inv * (tau_body + gyro);
+      const Vec3<R> omega_world = b.ori.rotate(b.omega_body), alpha_world = b.ori.rotate(alpha_body);
+      const Vec3<R> r = b.ori.rotate(lp);
+      const Vec3<R> a_site = a_com + alpha_world.cross(r) + omega_world.cross(omega_world.cross(r));
+      const Vec3<R> a_proper = a_site - w.gravity;
+      const Vec3<R> v = (b.ori * lq).inverse_rotate(a_proper);
+      out[o++] = (double)v.x; out[o++] = (double)v.y; out[o++] = (double)v.z;
+    }
+    get_state(w, qpos_out, qvel_out, 0);
+  };
+  if (precision == 0) go(0.0f); else go(0.0);
+  return rc;
+}
+
 // PGS row impulses of one free-body world at its state (one step's solve).
 int oracle_impulses(const newt_model_desc* d, const float* qpos, const float* qvel, int precision, int iterations,
                     int cap, int* n_out, double* impulses) {

@@ -46,6 +46,8 @@ def lib():
         L.oracle_tree_impulses_ex.restype = C.c_int
         L.oracle_sensors.argtypes = [P, P, P, C.c_int, C.c_int, P, P, P]
         L.oracle_sensors.restype = C.c_int
+        L.oracle_contact_sensors.argtypes = [P, P, P, C.c_int, C.c_int, P, P, P, P, P]
+        L.oracle_contact_sensors.restype = C.c_int
         L.oracle_ccd_pair.argtypes = [C.c_int, C.c_int, P, P, C.c_int, P, P, C.c_float, C.c_float, P]
         L.oracle_ccd_pair.restype = C.c_int
         L.oracle_np_pair.argtypes = [C.c_int, C.c_int, P, P, C.c_int, P, P, C.c_float, P]
@@ -126,6 +128,27 @@ def tree_impulses(packed, index: int, qpos: np.ndarray, qvel: np.ndarray, qfrc: 
                                      _ptr(qc), int(integrator)):
         raise RuntimeError("oracle_tree_impulses failed")
     return out[: min(n.value, cap)], qc
+
+
+def contact_sensors(packed, index: int, qpos: np.ndarray, qvel: np.ndarray, sens: np.ndarray, precision: int = 1):
+    """newt's post-step contact sensors of one free-body world: one step from
+    (qpos, qvel) (MuJoCo layout), the step's contacts re-solved at the
+    post-step state; kinds 9 accelerometer (3), 10 touch (1).  Returns the
+    readings and the post-step (qpos, qvel)."""
+    qpos = np.ascontiguousarray(qpos, dtype=np.float32)
+    qvel = np.ascontiguousarray(qvel, dtype=np.float32)
+    si = np.ascontiguousarray(np.stack([sens["kind"], sens["on_link"], sens["index"]], 1), np.int32)
+    sf = np.ascontiguousarray(np.concatenate([sens["local_pos"], sens["local_quat"]], 1), np.float32)
+    D = int(sum(1 if k == 10 else 3 for k in sens["kind"]))
+    out = np.zeros(D, dtype=np.float64)
+    qo = np.zeros(qpos.size, dtype=np.float64)
+    vo = np.zeros(qvel.size, dtype=np.float64)
+    d = C.cast(C.byref(packed.descs[index]), C.c_void_p)
+    rc = lib().oracle_contact_sensors(d, _ptr(qpos), _ptr(qvel), precision, len(sens), _ptr(si), _ptr(sf), _ptr(out),
+                                      _ptr(qo), _ptr(vo))
+    if rc < 0:
+        raise ValueError("contact sensors take free-body worlds (and a positive definite Newton factor)")
+    return out, qo, vo
 
 
 def sensors(packed, index: int, qpos: np.ndarray, qvel: np.ndarray, sens: np.ndarray, precision: int = 1) -> np.ndarray:

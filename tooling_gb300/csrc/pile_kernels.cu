@@ -384,6 +384,47 @@ __global__ void __launch_bounds__(128, 6) pile_k_collide(const PileGroupDev* G, 
   assemble(L, wf, wi, lane, t, il);
 }
 
+// The post-step contact re-solve behind the contact sensors (newt's
+// build_sensor_inputs, world.rs:1545-1612): the world's current state with
+// the contacts its last step detected, which every step form leaves in the
+// world record (pairs, point, normal, depth; a new world has none).  The
+// scratch's contact records are rebuilt from them as the narrowphase wrote
+// them (bodies from the geoms, friction the smaller of the two), then the
+// rows and islands at the current state; no narrowphase runs.
+__global__ void __launch_bounds__(128, 6) pile_k_reassemble(const PileGroupDev* G, const int* wseg, int ng,
+                                                          int total, IslandLists il) {
+  const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (t >= total) return;
+  const int gi = find_seg(wseg, ng, t);
+  const PileGroupDev& g = G[gi];
+  const int w = t - wseg[gi];
+  if (w >= g.n || !g.I[(size_t)w * g.lay.istride + g.lay.live]) return;
+  const WsLay L = ws_layout(g.nb, g.np, g.maxc);
+  float* wf = g.scr + (size_t)w * g.sstride;
+  int* wi = reinterpret_cast<int*>(wf + L.nf);
+  const int lane = threadIdx.x & 31;
+  ws_load(g, w, L, wf, wi, lane);
+  const PileLayout& P = g.lay;
+  const float* F = g.F + (size_t)w * P.fstride;
+  const int* I = g.I + (size_t)w * P.istride;
+  const int nc = min(max(I[P.ncon], 0), L.maxc);
+  for (int c = lane; c < nc; c += 32) {
+    float* cf = wf + L.con + CF * c;
+    int* cc = wi + L.ci + CI * c;
+    const int ga = I[P.cpair + 2 * c], gb = I[P.cpair + 2 * c + 1];
+    const int ea = wi[L.gent + ga], eb = wi[L.gent + gb];
+    for (int k = 0; k < 7; ++k) cf[C_POS + k] = F[P.cdata + 7 * c + k];
+    cf[C_MU] = fminf(wf[L.fric + ea], wf[L.fric + eb]);
+    cc[0] = ga; cc[1] = gb; cc[2] = ea; cc[3] = eb;
+  }
+  if (lane == 0) {
+    wi[L.misc + 1] = nc;
+    wi[L.misc + 2] = 0;
+  }
+  __syncwarp();
+  assemble(L, wf, wi, lane, t, il);
+}
+
 // Resolve a list item to its world scratch and island.
 struct IslandRef {
   const PileGroupDev* g;
@@ -970,6 +1011,99 @@ extern "C" int newt_launch_pile_step(const PileGroupDev* dG, const int* dwseg, i
   pile_k_integrate<<<(total_worlds + wpb - 1) / wpb, 32 * wpb, 0, st>>>(dG, dwseg, ng, total_worlds, write_diag);
   mark(N_ICLASS + 1, 1, st);
   return N_ICLASS + 2;
+}
+
+extern "C" void newt_launch_pile_newton_solve(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
+                                              cudaStream_t st);
+
+// The contact re-solve of every world of a table at its current state
+// (pile_k_reassemble, then the island-class PGS solvers or the dense Newton
+// solve; nothing is integrated): the velocity changes and the contacts'
+// impulses the contact sensors read.  Returns the launches issued.
+extern "C" int newt_launch_pile_resolve(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
+                                        int total_slots, int* lists, int newton, cudaStream_t st) {
+  if (total_worlds <= 0) return 0;
+  IslandLists il;
+  il.items = lists;
+  il.cap = total_slots;
+  il.stats = 0;
+  il.counts = lists + (size_t)N_ICLASS * total_slots;
+  cudaMemsetAsync(il.counts, 0, N_COUNTERS * sizeof(int), st);
+  const int wpb = 4;
+  pile_k_reassemble<<<(total_worlds + wpb - 1) / wpb, 32 * wpb, 0, st>>>(dG, dwseg, ng, total_worlds, il);
+  if (newton) {
+    newt_launch_pile_newton_solve(dG, dwseg, ng, total_worlds, st);
+    return 2;
+  }
+  const int grid = std::min((total_slots + 127) / 128, cap128);
+  for (int cl = N_ICLASS - 1; cl >= 0; --cl) launch_class(cl, dG, dwseg, ng, il, grid, st);
+  return 1 + N_ICLASS;
+}
+
+// Contact sensors of the named worlds from the re-solve (newt's
+// sensor.rs:1030-1087 accelerometer_reading, :1103-1112 touch_reading, with
+// the body accelerations of :586-600).  The velocity changes dv, dw (world
+// frame) are M^-1 J^T f, so newt's wrench is F = m dv / dt and
+// tau_world = I_world dw / dt; a contact's normal force is its facet
+// impulses summed over dt.  Writes only the accelerometer and touch entries
+// of each output row (the state sensors' kernel writes the rest).
+__global__ void __launch_bounds__(64) pile_contact_sensors_kernel(PileGroupDev g, const int* idx, int n,
+                                                                 const newt_sensor_desc* S, int ns, float* out,
+                                                                 int D) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int w = idx[t];
+  const WsLay L = ws_layout(g.nb, g.np, g.maxc);
+  const float* wf = g.scr + (size_t)w * g.sstride;
+  const int* wi = reinterpret_cast<const int*>(wf + L.nf);
+  const int nc = min(max(wi[L.misc + 1], 0), g.maxc);
+  const float dt = wf[L.dtg];
+  const V3 grav = v3(wf[L.dtg + 1], wf[L.dtg + 2], wf[L.dtg + 3]);
+  float* row = out + (size_t)t * D;
+  int o = 0;
+  for (int k = 0; k < ns; ++k) {
+    const int kind = S[k].kind;
+    if (kind == NEWT_SENSOR_TOUCH) {
+      float sum = 0.f;
+      for (int c = 0; c < nc; ++c) {
+        const int* cc = wi + L.ci + CI * c;
+        if (cc[0] != S[k].index && cc[1] != S[k].index) continue;
+        const float* cf = wf + L.con + CF * c;
+        const float f = (((0.f + cf[C_IMP]) + cf[C_IMP + 1]) + cf[C_IMP + 2]) + cf[C_IMP + 3];
+        sum += fabsf(f / dt);
+      }
+      row[o++] = sum;
+      continue;
+    }
+    if (kind != NEWT_SENSOR_ACCELEROMETER) {
+      o += kind <= NEWT_SENSOR_JOINTVEL ? 1 : (kind == NEWT_SENSOR_FRAMEQUAT ? 4 : 3);
+      continue;
+    }
+    const int b = S[k].index;
+    const Q4 q = ld4(wf + L.quat + 4 * b);
+    const V3 wb = ld3(wf + L.omg + 3 * b);
+    const S3 Ib = lds(wf + L.inertb + 6 * b), Ibi = lds(wf + L.iinvb + 6 * b);
+    const float m = wf[L.mass + b];
+    const V3 F = ld3(wf + L.dv + 3 * b) * (m / dt);
+    const V3 tau_world = qrot(q, smv(Ib, qrot_inv(q, ld3(wf + L.dw + 3 * b)))) / dt;  // R Ib R^T dw / dt
+    const V3 a_com = grav + F / m;
+    const V3 tau_body = qrot_inv(q, tau_world);
+    const V3 gyro = -cross(wb, smv(Ib, wb));
+    const V3 alpha_body = smv(Ibi, tau_body + gyro);
+    const V3 w_world = qrot(q, wb), a_world = qrot(q, alpha_body);
+    const V3 lp = v3(S[k].local_pos[0], S[k].local_pos[1], S[k].local_pos[2]);
+    const Q4 lq{S[k].local_quat[0], S[k].local_quat[1], S[k].local_quat[2], S[k].local_quat[3]};
+    const V3 r = qrot(q, lp);
+    const V3 a_site = a_com + cross(a_world, r) + cross(w_world, cross(w_world, r));
+    const V3 v = qrot_inv(qmul(q, lq), a_site - grav);
+    row[o++] = v.x; row[o++] = v.y; row[o++] = v.z;
+  }
+}
+
+extern "C" void newt_launch_pile_contact_sensors(const PileGroupDev& g, const int* idx, int n,
+                                                 const newt_sensor_desc* S, int ns, float* out, int D,
+                                                 cudaStream_t st) {
+  if (n > 0) pile_contact_sensors_kernel<<<(n + 63) / 64, 64, 0, st>>>(g, idx, n, S, ns, out, D);
 }
 
 // The collide and integrate stages alone, for the free-body Newton step

@@ -170,6 +170,12 @@ extern "C" void pile_k_collide_launch(const PileGroupDev* dG, const int* dwseg, 
 extern "C" void pile_k_integrate_launch(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
                                         int write_diag, cudaStream_t st);
 
+// The dense Newton solve alone (the contact sensors' re-solve).
+extern "C" void newt_launch_pile_newton_solve(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
+                                              cudaStream_t st) {
+  if (total_worlds > 0) pile_k_newton<<<total_worlds, 32, 0, st>>>(dG, dwseg, ng, total_worlds);
+}
+
 // One env-step of a table of Newton pile groups on `st`: collide, the
 // Newton solve, integrate.  Returns the launches issued.
 extern "C" int newt_launch_pile_newton_step(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,

@@ -1,6 +1,9 @@
-// Post-step sensors that read the state alone: one thread per world walks the
-// tree (forward kinematics and link velocities) or reads the free bodies, then
-// writes every requested sensor's values into the world's output row.
+// Post-step sensors: one thread per world walks the tree (forward kinematics
+// and link velocities) or reads the free bodies, then writes every requested
+// sensor's values into the world's output row.  Accelerometer and touch
+// readings on pile worlds come from newt's post-step contact re-solve
+// (pile_kernels.cu: pile_k_reassemble, the solvers, then
+// pile_contact_sensors_kernel), run for the group before its sensors.
 //
 // Restates, for FP32 on sm_103a:
 //   newt/src/sensor.rs:560-700   evaluate (JointPos, JointVel, FramePos,
@@ -25,7 +28,10 @@ namespace {
 enum { JF = 0, JX = 1, JH = 2, JS = 3 };
 
 __host__ __device__ int sensor_dim(int kind) {
-  return kind <= NEWT_SENSOR_JOINTVEL ? 1 : (kind == NEWT_SENSOR_FRAMEQUAT ? 4 : 3);
+  return kind <= NEWT_SENSOR_JOINTVEL || kind == NEWT_SENSOR_TOUCH ? 1 : (kind == NEWT_SENSOR_FRAMEQUAT ? 4 : 3);
+}
+__host__ __device__ bool contact_sensor(int kind) {
+  return kind == NEWT_SENSOR_ACCELEROMETER || kind == NEWT_SENSOR_TOUCH;
 }
 
 NEWT_D Q4 axis_angle(V3 axis, float angle) {  // newt/src/math.rs:574-580
@@ -47,6 +53,7 @@ NEWT_D void write_sensors(const newt_sensor_desc* S, int ns, const Frame* frames
   for (int k = 0; k < ns; ++k) {
     const newt_sensor_desc& s = S[k];
     const int kind = s.kind;
+    if (contact_sensor(kind)) { o += sensor_dim(kind); continue; }  // the contact sensors' kernel
     if (kind == NEWT_SENSOR_JOINTPOS) { row[o++] = q[qoff[s.index]]; continue; }
     if (kind == NEWT_SENSOR_JOINTVEL) { row[o++] = qd[voff[s.index]]; continue; }
     if (kind == NEWT_SENSOR_SUBTREECOM) {
@@ -149,7 +156,7 @@ __global__ void __launch_bounds__(64) tree_sensors_kernel(TreeGroupDev g, const 
       com[k] = m == 0.f ? v3(0.f, 0.f, 0.f) : acc / m;
       continue;
     }
-    if (s.kind <= NEWT_SENSOR_JOINTVEL) continue;
+    if (s.kind <= NEWT_SENSOR_JOINTVEL || contact_sensor(s.kind)) continue;
     fr[k] = Frame{P[l], O[l], Wn[l], Vn[l], qrot_inv(O[l], Wn[l])};
   }
   write_sensors(S, ns, fr, q, qd, qoff, voff, out + (size_t)t * D, com);
@@ -164,6 +171,7 @@ __global__ void __launch_bounds__(64) pile_sensors_kernel(PileGroupDev g, const 
   Frame fr[16];
   for (int k = 0; k < ns && k < 16; ++k) {
     const int b = S[k].index;
+    if (S[k].kind == NEWT_SENSOR_TOUCH) continue;  // a geom index, read by the contact sensors' kernel
     const Q4 o{F[g.lay.quat + 4 * b], F[g.lay.quat + 4 * b + 1], F[g.lay.quat + 4 * b + 2], F[g.lay.quat + 4 * b + 3]};
     const V3 wb = v3(F[g.lay.omg + 3 * b], F[g.lay.omg + 3 * b + 1], F[g.lay.omg + 3 * b + 2]);
     fr[k] = Frame{v3(F[g.lay.pos + 3 * b], F[g.lay.pos + 3 * b + 1], F[g.lay.pos + 3 * b + 2]), o, qrot(o, wb),
@@ -180,6 +188,10 @@ int bad(newt_gpu_ctx* ctx, const char* msg) {
 }  // namespace
 
 extern "C" int newt_tree_bucket(int L);
+extern "C" void newt_launch_pile_contact_sensors(const PileGroupDev& g, const int* idx, int n,
+                                                 const newt_sensor_desc* S, int ns, float* out, int D,
+                                                 cudaStream_t st);
+int pile_resolve_group(newt_gpu_ctx* ctx, HostGroup* g);
 
 int newt_gpu_read_sensors(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, const newt_sensor_desc* sensors,
                           int32_t n_sensors, float* out) {
@@ -189,10 +201,12 @@ int newt_gpu_read_sensors(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, co
   if (n == 0 || n_sensors == 0) return NEWT_OK;
   cudaSetDevice(ctx->device);
   int D = 0;
+  bool needs_resolve = false;
   for (int k = 0; k < n_sensors; ++k) {
-    if (sensors[k].kind < NEWT_SENSOR_JOINTPOS || sensors[k].kind > NEWT_SENSOR_SUBTREECOM)
+    if (sensors[k].kind < NEWT_SENSOR_JOINTPOS || sensors[k].kind > NEWT_SENSOR_TOUCH)
       return bad(ctx, "unknown sensor kind");
     D += sensor_dim(sensors[k].kind);
+    needs_resolve = needs_resolve || contact_sensor(sensors[k].kind);
   }
   // validate every world against every sensor, and group the worlds
   std::vector<std::vector<int>> idx(ctx->groups.size()), rows(ctx->groups.size());
@@ -205,9 +219,12 @@ int newt_gpu_read_sensors(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, co
     for (int k = 0; k < n_sensors; ++k) {
       const newt_sensor_desc& d = sensors[k];
       const bool link_only = d.kind <= NEWT_SENSOR_JOINTVEL || d.kind == NEWT_SENSOR_SUBTREECOM;
+      if (contact_sensor(d.kind) && tree)
+        return bad(ctx, "accelerometer and touch sensors are read on pile worlds (free bodies)");
       if ((d.on_link != 0) != tree || (link_only && !d.on_link))
         return bad(ctx, "sensor attachment does not match the world (links for trees, bodies for piles)");
-      if (d.index < 0 || d.index >= (tree ? m.n_links : m.n_bodies)) return bad(ctx, "sensor index out of range");
+      const int lim = d.kind == NEWT_SENSOR_TOUCH ? m.n_geoms : (tree ? m.n_links : m.n_bodies);
+      if (d.index < 0 || d.index >= lim) return bad(ctx, "sensor index out of range");
       if (d.kind <= NEWT_SENSOR_JOINTVEL && m.links[d.index].joint != NEWT_JOINT_HINGE &&
           m.links[d.index].joint != NEWT_JOINT_SLIDE)
         return bad(ctx, "joint sensors read hinge or slide links");
@@ -224,6 +241,7 @@ int newt_gpu_read_sensors(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, co
   if (e == cudaSuccess) e = cudaMallocAsync(&dO, sizeof(float) * (size_t)n * D, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dS, sensors, sizeof(newt_sensor_desc) * n_sensors, cudaMemcpyHostToDevice, st);
   std::vector<int> order;  // the device rows' order: grouped
+  int resolve_rc = NEWT_OK;
   std::vector<float> host((size_t)n * D);
   size_t base = 0;
   for (size_t gi = 0; gi < idx.size() && e == cudaSuccess; ++gi) {
@@ -236,6 +254,12 @@ int newt_gpu_read_sensors(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, co
     float* o = dO + base * D;
     if (g->kind == GK_PILE) {
       pile_sensors_kernel<<<grid, 64, 0, st>>>(g->pile_dev(), dI + base, cnt, dS, n_sensors, o, D);
+      if (needs_resolve) {
+        resolve_rc = pile_resolve_group(ctx, g);
+        if (resolve_rc != NEWT_OK) break;
+        newt_launch_pile_contact_sensors(g->pile_dev(), dI + base, cnt, dS, n_sensors, o, D, st);
+        ctx->launches += 1;
+      }
     } else {
       const TreeGroupDev td = g->tree_dev();
       switch (newt_tree_bucket(td.L)) {
@@ -250,11 +274,13 @@ int newt_gpu_read_sensors(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, co
     order.insert(order.end(), rows[gi].begin(), rows[gi].end());
     base += cnt;
   }
-  if (e == cudaSuccess) e = cudaMemcpyAsync(host.data(), dO, sizeof(float) * host.size(), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && resolve_rc == NEWT_OK)
+    e = cudaMemcpyAsync(host.data(), dO, sizeof(float) * host.size(), cudaMemcpyDeviceToHost, st);
   if (dS) cudaFreeAsync(dS, st);
   if (dI) cudaFreeAsync(dI, st);
   if (dO) cudaFreeAsync(dO, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (resolve_rc != NEWT_OK) return resolve_rc;  // its message is in ctx->err
   if (e != cudaSuccess) {
     ctx->err = std::string("read_sensors: ") + cudaGetErrorString(e);
     return NEWT_E_CUDA;

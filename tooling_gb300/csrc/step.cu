@@ -158,8 +158,8 @@ static int ensure_pile_branches(newt_gpu_ctx* ctx) {
 // ---------------------------------------------------------------------------
 // plain
 // ---------------------------------------------------------------------------
-int step_plain(newt_gpu_ctx* ctx, int n_steps) {
-  // per-group single-entry tables (rebuilt when groups change)
+// Per-group single-entry tables (rebuilt when groups change).
+static int ensure_plain_tables(newt_gpu_ctx* ctx) {
   if (ctx->plain_dirty) {
     for (void* p : ctx->plain_bufs) cudaFree(p);
     ctx->plain_bufs.clear();
@@ -174,6 +174,26 @@ int step_plain(newt_gpu_ctx* ctx, int n_steps) {
     }
     ctx->plain_dirty = false;
   }
+  return NEWT_OK;
+}
+
+extern "C" int newt_launch_pile_resolve(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
+                                        int total_slots, int* lists, int newton, cudaStream_t st);
+
+// The contact sensors' re-solve of every world of pile group `g` at its
+// current state, on the context's stream (pile_kernels.cu).
+int pile_resolve_group(newt_gpu_ctx* ctx, HostGroup* g) {
+  int rc = ensure_plain_tables(ctx);
+  if (rc != NEWT_OK) return rc;
+  const auto& T = ctx->plain_tables[g->id];
+  ctx->launches += newt_launch_pile_resolve((const PileGroupDev*)T.dG, T.dseg, T.ng, T.worlds, T.slots, T.lists,
+                                            g->pile_newton ? 1 : 0, ctx->stream);
+  return NEWT_OK;
+}
+
+int step_plain(newt_gpu_ctx* ctx, int n_steps) {
+  int rc0 = ensure_plain_tables(ctx);
+  if (rc0 != NEWT_OK) return rc0;
   ctx->last_lists.clear();
   for (const auto& T : ctx->plain_tables)
     if (T.lists) ctx->last_lists.push_back({T.lists, T.slots});
