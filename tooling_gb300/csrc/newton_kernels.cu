@@ -214,6 +214,21 @@ NEWT_D bool warp_cholesky2(float* A, float* B, int n, int ld, int lane) {
   return true;
 }
 
+// Solves L^T z = rhs in place on the shared vector `v` (backward
+// substitution by row dot products of the column-major factor L).
+NEWT_D void warp_lt_solve(const float* Lf, int n, int ld, float* v, int lane) {
+  for (int k = n - 1; k >= 0; --k) {
+    __syncwarp();
+    float s = 0.f;
+    for (int m = k + 1 + lane; m < n; m += 32) s += Lf[(size_t)k * ld + m] * v[m];
+    s = warp_sum(s);
+    const float zk = (v[k] - s) / Lf[(size_t)k * ld + k];
+    __syncwarp();
+    if (lane == 0) v[k] = zk;
+  }
+  __syncwarp();
+}
+
 }  // namespace
 
 
@@ -269,6 +284,9 @@ NEWT_D void chain_columns(const TreeGroupDev& g, int w, const float* pose, int l
 // ---------------------------------------------------------------------------
 // K_B: one warp per world
 // ---------------------------------------------------------------------------
+// REFINE: the instance for trees above REFINE_NV DoF (FP64 sum of M and the
+// refinement step); the smaller trees' instance compiles without those paths.
+template <bool REFINE>
 __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   extern __shared__ __align__(16) float tcs[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -499,7 +517,7 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   // chains the f32 sums of long-lever products lose the digits that the
   // ill-conditioned solve amplifies, and a refinement against an f32 M'
   // converges to the wrong matrix's solution.
-  const bool refine = nv > REFINE_NV;
+  constexpr bool refine = REFINE;
   double* Md = refine ? reinterpret_cast<double*>(wf + lay.mc) : nullptr;
   for (int e = lane; e < nv * nv; e += 32) {
     const int i = e % nv, j = e / nv;
@@ -563,7 +581,8 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   // ---- Jacobian rows of the cone facets, velocities, lane per row ----
   const bool rows_shared = nr <= sm.nrs;
   float* Jt = rows_shared ? sv + sm.jy : wf + lay.jt;  // J^T, column-major; becomes Y
-  float* J0 = wf + lay.j0;                              // J^T, kept
+  float* J0 = wf + lay.j0;                              // J^T, kept (refined or RK4 worlds)
+  const bool keep_j = refine || rk4;
   const int ldj = rows_shared ? sm.nrs : ld;
   float* tw = sv + sm.tw;  // 1 marks a link that owns rows; then its inverse weight
   for (int l = lane; l < L; l += 32) tw[l] = 0.f;
@@ -588,7 +607,7 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
     float vel = 0.f, vfree = 0.f;
     for (int k = 0; k < nv; ++k) {
       const float jk = Jt[(size_t)k * ldj + r];
-      J0[(size_t)k * ld + r] = jk;
+      if (keep_j) J0[(size_t)k * ld + r] = jk;
       vel += jk * g.qd[k * cap + w];
       vfree += jk * g.qacc[k * cap + w];
     }
@@ -692,26 +711,38 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   __syncwarp();
 
   // ---- outputs: impulses, J^T f / dt, qacc = a_free + (M + dt B)^-1 J^T f / dt ----
-  // The contact force is formed from the kept J^T, not as L (Y f): Y = L^-1
-  // J^T carries the f32 rounding of the forward substitution, which L Y does
-  // not undo on long chains of light links, and the FP64 refinement below
-  // needs the true right-hand side to converge to.
+  // Refined trees form the contact force from the kept J^T: Y = L^-1 J^T
+  // carries the f32 rounding of the forward substitution, which L Y does not
+  // undo on long chains, and the FP64 refinement below needs the true
+  // right-hand side to converge to.  The rest take J^T = L Y, so
+  // (L L^T)^-1 J^T f / dt = L^-T (Y f) / dt: one back substitution.  RK4
+  // worlds hold J^T f / dt over the integrator's stages (from the kept J^T).
   for (int r = lane; r < nr; r += 32) wf[lay.imp + r] = vx[r];
   double* rhs = refine ? reinterpret_cast<double*>(wf + lay.rd) : nullptr;
   for (int k = lane; k < nv; k += 32) {
-    float s = 0.f;
-    double sd = 0.0;
-    for (int r = 0; r < nr; ++r) {
-      const float jk = J0[(size_t)k * ld + r];
-      s += jk * vx[r];
-      if (refine) sd += (double)jk * (double)vx[r];
+    if (keep_j) {
+      float s = 0.f;
+      double sd = 0.0;
+      for (int r = 0; r < nr; ++r) {
+        const float jk = J0[(size_t)k * ld + r];
+        s += jk * vx[r];
+        if (refine) sd += (double)jk * (double)vx[r];
+      }
+      if (rk4) g.cfrc[(size_t)w * g.cstride + k] = s / dt;  // the generalised force, held over the stages
+      if (refine) {
+        vg[k] = s / dt;
+        rhs[k] = sd / dt;
+      }
     }
-    vg[k] = s / dt;
-    if (refine) rhs[k] = sd / dt;
-    if (rk4) g.cfrc[(size_t)w * g.cstride + k] = vg[k];  // the generalised force, held over the stages
+    if (!refine) {
+      float s = 0.f;
+      for (int r = 0; r < nr; ++r) s += Y[(size_t)k * ldj + r] * vx[r];
+      vg[k] = s / dt;
+    }
   }
   __syncwarp();
-  warp_llt_solve(LM, nv, nv, vg, lane);
+  if (refine) warp_llt_solve(LM, nv, nv, vg, lane);
+  else warp_lt_solve(LM, nv, nv, vg, lane);
   if (refine) {
     // r = rhs - M' x in FP64 (M' summed in FP64, symmetric, its lower
     // triangle kept), then M' d = r with the FP32 factor in FP64 arithmetic,
@@ -746,13 +777,16 @@ extern "C" size_t newt_tc_smem_bytes(int L, int nv, int maxc) {
 }
 // Kernel attribute for the dynamic shared memory (outside stream capture).
 extern "C" cudaError_t newt_tc_init(int L, int nv, int maxc) {
-  return cudaFuncSetAttribute(tc_k_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)newt_tc_smem_bytes(L, nv, maxc));
+  const int bytes = (int)newt_tc_smem_bytes(L, nv, maxc);
+  if (nv > REFINE_NV) return cudaFuncSetAttribute(tc_k_solve<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  return cudaFuncSetAttribute(tc_k_solve<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 extern "C" void newt_launch_tc_solve(const TcGroupDev& G, cudaStream_t st) {
   const int grid = (G.t.n + TC_WARPS - 1) / TC_WARPS;
   if (grid == 0) return;
-  tc_k_solve<<<grid, 32 * TC_WARPS, newt_tc_smem_bytes(G.t.L, G.t.nv, G.maxc), st>>>(G);
+  const size_t bytes = newt_tc_smem_bytes(G.t.L, G.t.nv, G.maxc);
+  if (G.t.nv > REFINE_NV) tc_k_solve<true><<<grid, 32 * TC_WARPS, bytes, st>>>(G);
+  else tc_k_solve<false><<<grid, 32 * TC_WARPS, bytes, st>>>(G);
 }
 extern "C" void newt_tc_offsets(int L, int nv, int ng, int maxc, int* con, int* imp, int* misc) {
   const TcLay t = tc_layout(L, nv, ng, maxc);
