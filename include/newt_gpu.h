@@ -72,6 +72,8 @@ extern "C" {
 
 #define NEWT_SOLVER_PGS 1
 #define NEWT_SOLVER_NEWTON 2
+#define NEWT_CONE_PYRAMIDAL 0
+#define NEWT_CONE_ELLIPTIC 1
 
 /* Semi-implicit Euler (the configs' integrator, implicit joint damping) or
  * classic RK4 (newt's default: four explicit ABA stages, root quaternion
@@ -113,8 +115,10 @@ typedef struct newt_geom_desc {      /* newt::geom::Geom */
   float solref[2];                   /* timeconst, dampratio */
   float solimp[5];                   /* dmin, dmax, width, midpoint, power */
   float margin, gap;
-  int32_t condim;                    /* 1 or 3 (pyramidal cone) */
+  int32_t condim;                    /* 1, 3, 4 or 6 (newt/src/solver.rs:1409-1428); 4 and 6 on pile worlds */
   uint32_t group, mask;              /* collision filter (newt/src/broadphase.rs:16) */
+  float torsional_friction;          /* condim >= 4: torsion cap mu_t f_n (geom.rs:397-403) */
+  float rolling_friction;            /* condim 6: rolling cap mu_r f_n (geom.rs:404-409) */
 } newt_geom_desc;
 
 typedef struct newt_model_desc {     /* one world's model: at most one tree */
@@ -128,6 +132,8 @@ typedef struct newt_model_desc {     /* one world's model: at most one tree */
   int32_t iterations;                /* PGS sweeps / Newton iteration cap */
   int32_t tree_self_collision;       /* 0: in-tree geom pairs are skipped */
   int32_t integrator;                /* NEWT_INTEGRATOR_*: World::integrator (newt/src/world.rs:76-84) */
+  int32_t cone;                      /* NEWT_CONE_*: SolverConfig::cone (newt/src/solver.rs:75-110);
+                                      * elliptic on pile worlds under PGS */
 } newt_model_desc;
 
 /* ---- context ------------------------------------------------------------ */

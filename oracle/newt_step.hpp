@@ -33,10 +33,14 @@ template <class R> Deriv<R> evaluate(const Body<R>& s, Vec3<R> g, Vec3<R> f, Vec
 template <class R> void solve_free_bodies(const World<R>& w, const std::vector<Contact<R>>& contacts,
                                           std::vector<Wrench<R>>& ext) {
   if (w.solver_mode == M_NEWTON) {
+    if (w.cone != 0) throw std::runtime_error("Newton takes the pyramidal cone (solver.rs:89-91)");
+    for (const Contact<R>& c : contacts)
+      if (std::min(w.geoms[c.ga].condim, w.geoms[c.gb].condim) >= 4)
+        throw std::runtime_error("the free-body Newton solve takes condim 1 and 3 here");
     if (!solve_free_bodies_newton(w.bodies, w.geoms, contacts, w.gravity, w.dt, w.iterations, ext))
       throw std::runtime_error("Newton free-body solve failed: the Hessian is not positive definite");
   } else {
-    solve_free_bodies_pgs(w.bodies, w.geoms, contacts, w.gravity, w.dt, w.iterations, ext);
+    solve_free_bodies_pgs<R>(w.bodies, w.geoms, contacts, w.gravity, w.dt, w.iterations, ext, nullptr, nullptr, w.cone);
   }
 }
 

@@ -89,6 +89,7 @@ template <class R> struct Geom {
   R margin = 0, gap = 0;
   int condim = 3;
   unsigned group = 0xffffffffu, mask = 0xffffffffu;
+  R torsional_friction = 0, rolling_friction = 0;  // geom.rs:397-409 (condim 4 / 6)
   // attachment key: 0 static, 1 body, 2 link
   int att_kind() const { return link >= 0 ? 2 : body >= 0 ? 1 : 0; }
 };
@@ -604,27 +605,42 @@ template <class R> void tangent_basis(Vec3<R> n, Vec3<R>* t1, Vec3<R>* t2) {  //
 // --------------------------------------------------------------------------
 // Free-body PGS (solver.rs:703-1257), pyramidal cone, condim 3 and 1.
 // --------------------------------------------------------------------------
-template <class R> struct Row {
-  Vec3<R> dir; int ba, bb; Vec3<R> arm_a, arm_b; R reg, diag, bias;
+template <class R> struct Row {  // solver.rs ConstraintRow; `ang`: RowGeom::Angular (torque about dir)
+  Vec3<R> dir; int ba, bb; Vec3<R> arm_a, arm_b; R reg, diag, bias; bool ang = false;
 };
 template <class R> struct BDelta { Vec3<R> dv, dw; };
 
 template <class R> struct PgsStats { int rows = 0; int contacts = 0; };
 
 template <class R> R row_body_diagonal(const Row<R>& r, const std::vector<Body<R>>& bodies, const std::vector<Mat3<R>>& iinv) {
-  R a = R(0);
+  R a = R(0);  // solver.rs:1892-1924
+  if (r.ang) {
+    if (r.ba >= 0) a += r.dir.dot(iinv[r.ba] * r.dir);
+    if (r.bb >= 0) a += r.dir.dot(iinv[r.bb] * r.dir);
+    return a;
+  }
   if (r.ba >= 0) { Vec3<R> rc = r.arm_a.cross(r.dir); a += rc.dot(iinv[r.ba] * rc) + R(1) / bodies[r.ba].mass; }
   if (r.bb >= 0) { Vec3<R> rc = r.arm_b.cross(r.dir); a += rc.dot(iinv[r.bb] * rc) + R(1) / bodies[r.bb].mass; }
   return a;
 }
 template <class R> R row_residual(const Row<R>& r, const std::vector<BDelta<R>>& bd, const std::vector<Body<R>>& bodies) {
-  R s = R(0);
+  R s = R(0);  // solver.rs:1980-2018
+  if (r.ang) {
+    if (r.ba >= 0) s += bodies[r.ba].ori.rotate(bd[r.ba].dw).dot(r.dir);
+    if (r.bb >= 0) s -= bodies[r.bb].ori.rotate(bd[r.bb].dw).dot(r.dir);
+    return s;
+  }
   if (r.ba >= 0) { Vec3<R> dw = bodies[r.ba].ori.rotate(bd[r.ba].dw); Vec3<R> vp = bd[r.ba].dv + dw.cross(r.arm_a); s += vp.dot(r.dir); }
   if (r.bb >= 0) { Vec3<R> dw = bodies[r.bb].ori.rotate(bd[r.bb].dw); Vec3<R> vp = bd[r.bb].dv + dw.cross(r.arm_b); s -= vp.dot(r.dir); }
   return s;
 }
 template <class R> void apply_impulse(const Row<R>& r, R df, std::vector<BDelta<R>>& bd, const std::vector<Body<R>>& bodies, const std::vector<Mat3<R>>& iinv) {
-  if (df == R(0)) return;
+  if (df == R(0)) return;  // solver.rs:2022-2066
+  if (r.ang) {
+    if (r.ba >= 0) { Vec3<R> tq = r.dir * df; bd[r.ba].dw += bodies[r.ba].ori.inverse_rotate(iinv[r.ba] * tq); }
+    if (r.bb >= 0) { Vec3<R> tq = -r.dir * df; bd[r.bb].dw += bodies[r.bb].ori.inverse_rotate(iinv[r.bb] * tq); }
+    return;
+  }
   if (r.ba >= 0) {
     Vec3<R> f = r.dir * df; Vec3<R> tq = r.arm_a.cross(f);
     bd[r.ba].dv += f / bodies[r.ba].mass;
@@ -650,11 +666,17 @@ struct PgsContactInfo { int start_row; int condim; int contact_index; };
 // Rows of the free-body contact system (solver.rs:752-1061): per active
 // contact its facet rows (pyramidal condim 3) or normal row (condim 1), with
 // regularisation, diagonal and bias; `pcs` keeps the contact blocks.
-template <class R> struct FreePC { int ci, start, condim; SolRef<R> sr; SolImp<R> si; R pen, mu; R h01a, h01b; };
+template <class R> struct FreePC {
+  int ci, start, condim; SolRef<R> sr; SolImp<R> si; R pen, mu; R h01a, h01b;
+  R mu_t = 0, mu_r = 0; int nrows = 1;  // torsional / rolling friction, rows of the block
+};
 template <class R> struct FreeSystem {
   std::vector<Row<R>> rows;
   std::vector<FreePC<R>> pcs;
   std::vector<Mat3<R>> iinv;
+  int cone = 0;  // 0 pyramidal, 1 elliptic (solver.rs:75-88)
+  // pyramidal condim 3: the four facet rows n +- mu t
+  bool facets(const FreePC<R>& pc) const { return cone == 0 && pc.condim == 3; }
 };
 
 template <class R>
@@ -685,20 +707,40 @@ void assemble_free_rows(const std::vector<Body<R>>& bodies, const std::vector<Ge
     Vec3<R> arm_a = ba >= 0 ? c.pos - bodies[ba].pos : Vec3<R>();
     Vec3<R> arm_b = bb >= 0 ? c.pos - bodies[bb].pos : Vec3<R>();
     int start = (int)rows.size();
-    if (condim == 3) {
+    FreePC<R> pc{ci, start, condim, sr, si, pen_active, mu, R(0), R(0)};
+    pc.mu_t = cmin(ga.torsional_friction, gb.torsional_friction);  // combine_torsional_friction
+    pc.mu_r = cmin(ga.rolling_friction, gb.rolling_friction);      // combine_rolling_friction
+    // contact_row_directions (solver.rs:3401-3429) and the torsion / rolling
+    // rows (:820-848); newt pushes the angular rows a second time after the
+    // directions, rows that get no constants and are never swept, so only
+    // the block's own rows are kept here
+    if (sys.cone == 0 && condim == 3) {
       Vec3<R> dirs[4] = {n + t1 * mu, n - t1 * mu, n + t2 * mu, n - t2 * mu};
       for (int k = 0; k < 4; ++k) rows.push_back({dirs[k], ba, bb, arm_a, arm_b, R(0), R(0), R(0)});
+      pc.nrows = 4;
     } else {
       rows.push_back({n, ba, bb, arm_a, arm_b, R(0), R(0), R(0)});
+      if (condim >= 3) {
+        rows.push_back({t1, ba, bb, arm_a, arm_b, R(0), R(0), R(0)});
+        rows.push_back({t2, ba, bb, arm_a, arm_b, R(0), R(0), R(0)});
+      }
+      const Vec3<R> z;
+      if (condim >= 4) rows.push_back({n, ba, bb, z, z, R(0), R(0), R(0), true});
+      if (condim >= 6) {
+        rows.push_back({t1, ba, bb, z, z, R(0), R(0), R(0), true});
+        rows.push_back({t2, ba, bb, z, z, R(0), R(0), R(0), true});
+      }
+      pc.nrows = (int)rows.size() - start;
     }
-    pcs.push_back({ci, start, condim, sr, si, pen_active, mu, R(0), R(0)});
+    pcs.push_back(pc);
   }
   if (rows.empty()) return;
   sys.iinv.resize(nb);
   std::vector<Mat3<R>>& iinv = sys.iinv;
   for (int i = 0; i < nb; ++i) { Mat3<R> r = bodies[i].ori.to_mat3(); iinv[i] = r * bodies[i].inertia_inv * r.transpose(); }
   for (FreePC<R>& pc : pcs) {
-    int nr = pc.condim == 3 ? 4 : 1;
+    const int nr = pc.nrows;
+    const bool fac = sys.facets(pc);
     for (int k = 0; k < nr; ++k) {
       Row<R>& r = rows[pc.start + k];
       R aii = row_body_diagonal(r, bodies, iinv);
@@ -709,21 +751,29 @@ void assemble_free_rows(const std::vector<Body<R>>& bodies, const std::vector<Ge
         R tran = R(0);
         if (r.ba >= 0) tran += R(1) / bodies[r.ba].mass;
         if (r.bb >= 0) tran += R(1) / bodies[r.bb].mass;
-        R base = pc.condim == 3 ? tran * (R(1) + pc.mu * pc.mu) : row_body_diagonal(r, bodies, iinv);
+        R base = fac ? tran * (R(1) + pc.mu * pc.mu) : row_body_diagonal(r, bodies, iinv);
         R breg = (R(1) - d) / d * base;
-        reg = pc.condim == 3 ? R(2) * pc.mu * pc.mu * breg : breg;
+        reg = fac ? R(2) * pc.mu * pc.mu * breg : breg;
       }
       r.reg = reg;
       r.diag = aii + reg;
     }
     for (int k = 0; k < nr; ++k) {
       Row<R>& r = rows[pc.start + k];
-      R vcur = point_dir_velocity(bodies, r.ba, r.bb, r.arm_a, r.arm_b, r.dir);
-      // free_step_velocity_contribution with zero angular free step
-      R dvf = R(0);
-      if (r.ba >= 0) { Vec3<R> dw = bodies[r.ba].ori.rotate(Vec3<R>()); Vec3<R> vp = dvfree[r.ba] + dw.cross(r.arm_a); dvf += vp.dot(r.dir); }
-      if (r.bb >= 0) { Vec3<R> dw = bodies[r.bb].ori.rotate(Vec3<R>()); Vec3<R> vp = dvfree[r.bb] + dw.cross(r.arm_b); dvf -= vp.dot(r.dir); }
-      R position = -pc.pen;  // pyramidal condim 3 rows and the normal row share the position
+      R vcur, dvf = R(0);
+      if (r.ang) {  // row_current_velocity (solver.rs:2071-2093); no angular free step (:2108-2127)
+        Vec3<R> wa, wb;
+        if (r.ba >= 0) wa = bodies[r.ba].ori.rotate(bodies[r.ba].omega_body);
+        if (r.bb >= 0) wb = bodies[r.bb].ori.rotate(bodies[r.bb].omega_body);
+        vcur = (wa - wb).dot(r.dir);
+      } else {
+        vcur = point_dir_velocity(bodies, r.ba, r.bb, r.arm_a, r.arm_b, r.dir);
+        // free_step_velocity_contribution with zero angular free step
+        if (r.ba >= 0) { Vec3<R> dw = bodies[r.ba].ori.rotate(Vec3<R>()); Vec3<R> vp = dvfree[r.ba] + dw.cross(r.arm_a); dvf += vp.dot(r.dir); }
+        if (r.bb >= 0) { Vec3<R> dw = bodies[r.bb].ori.rotate(Vec3<R>()); Vec3<R> vp = dvfree[r.bb] + dw.cross(r.arm_b); dvf -= vp.dot(r.dir); }
+      }
+      // the penetration drives the facets and the normal row only (solver.rs:944-948)
+      R position = (fac || k == 0) ? -pc.pen : R(0);
       SolRef<R> sr = safe_solref(pc.sr, dt);
       R aref = reference_accel(position, vcur, sr, pc.si);
       r.bias = dvf - aref * dt;
@@ -739,6 +789,11 @@ void free_row_wrenches(const FreeSystem<R>& sys, const std::vector<R>& imp, R dt
     if (f == R(0)) continue;
     const Row<R>& r = sys.rows[ri];
     Vec3<R> fa = r.dir * (f / dt);
+    if (r.ang) {  // a pure torque along dir
+      if (r.ba >= 0) wrenches[r.ba].t += fa;
+      if (r.bb >= 0) wrenches[r.bb].t += -fa;
+      continue;
+    }
     if (r.ba >= 0) { wrenches[r.ba].f += fa; wrenches[r.ba].t += r.arm_a.cross(fa); }
     if (r.bb >= 0) { Vec3<R> fb = -fa; wrenches[r.bb].f += fb; wrenches[r.bb].t += r.arm_b.cross(fb); }
   }
@@ -747,7 +802,7 @@ void free_row_wrenches(const FreeSystem<R>& sys, const std::vector<R>& imp, R dt
 template <class R> void free_row_contacts(const FreeSystem<R>& sys, std::vector<int>* row_contact_out) {
   row_contact_out->assign(sys.rows.size(), -1);
   for (const FreePC<R>& pc : sys.pcs)
-    for (int k = 0; k < (pc.condim == 3 ? 4 : 1); ++k) (*row_contact_out)[pc.start + k] = pc.ci;
+    for (int k = 0; k < pc.nrows; ++k) (*row_contact_out)[pc.start + k] = pc.ci;
 }
 
 // Returns per-body (force, torque) wrenches; optionally the per-row impulses
@@ -756,13 +811,14 @@ template <class R>
 void solve_free_bodies_pgs(const std::vector<Body<R>>& bodies, const std::vector<Geom<R>>& geoms,
                            const std::vector<Contact<R>>& contacts, Vec3<R> gravity, R dt, int iterations,
                            std::vector<Wrench<R>>& wrenches, std::vector<R>* impulses_out = nullptr,
-                           std::vector<int>* row_contact_out = nullptr) {
+                           std::vector<int>* row_contact_out = nullptr, int cone = 0) {
   const int nb = (int)bodies.size();
   wrenches.assign(nb, Wrench<R>{Vec3<R>(), Vec3<R>()});
   if (impulses_out) impulses_out->clear();
   if (row_contact_out) row_contact_out->clear();
   if (contacts.empty() || dt <= R(0)) return;
   FreeSystem<R> sys;
+  sys.cone = cone;
   assemble_free_rows(bodies, geoms, contacts, gravity, dt, sys);
   std::vector<Row<R>>& rows = sys.rows;
   const std::vector<Mat3<R>>& iinv = sys.iinv;
@@ -770,7 +826,7 @@ void solve_free_bodies_pgs(const std::vector<Body<R>>& bodies, const std::vector
   if (nrows == 0) return;
   std::vector<BDelta<R>> scratch(nb);
   for (FreePC<R>& pc : sys.pcs) {
-    if (pc.condim != 3) continue;
+    if (!sys.facets(pc)) continue;
     for (int pair = 0; pair < 2; ++pair) {
       const Row<R>& ri = rows[pc.start + 2 * pair];
       const Row<R>& rj = rows[pc.start + 2 * pair + 1];
@@ -812,10 +868,49 @@ void solve_free_bodies_pgs(const std::vector<Body<R>>& bodies, const std::vector
     apply_impulse(rows[ri], ai, bd, bodies, iinv);
     apply_impulse(rows[rj], aj, bd, bodies, iinv);
   };
+  auto step_cap = [&](int ri, R cap) {  // pgs_step_scalar_cap (solver.rs:1561-1579)
+    const Row<R>& r = rows[ri];
+    R res = row_residual(r, bd, bodies) + r.reg * imp[ri] + r.bias;
+    R delta = -res / r.diag;
+    R nf = imp[ri] + delta;
+    R proj = nf > cap ? cap : (nf < -cap ? -cap : nf);  // project_pyramidal
+    delta = proj - imp[ri];
+    imp[ri] = proj;
+    apply_impulse(r, delta, bd, bodies, iinv);
+  };
+  auto step_cone = [&](int r1, int r2, R cap, R mu1, R mu2) {  // pgs_step_pair_cone (solver.rs:1620-1676)
+    if (sys.cone == 0) { step_cap(r1, mu1 * cap); step_cap(r2, mu2 * cap); return; }
+    R res1 = row_residual(rows[r1], bd, bodies) + rows[r1].reg * imp[r1] + rows[r1].bias;
+    R res2 = row_residual(rows[r2], bd, bodies) + rows[r2].reg * imp[r2] + rows[r2].bias;
+    R f1 = imp[r1] - res1 / rows[r1].diag;
+    R f2 = imp[r2] - res2 / rows[r2].diag;
+    // project_elliptic (solver.rs:398-411); the two coefficients are equal
+    // here (isotropic friction), so project_elliptic_axes is not reached
+    R p1 = R(0), p2 = R(0);
+    if (cap > R(0) && mu1 > R(0)) {
+      const R c = mu1 * cap;
+      const R mag2 = f1 * f1 + f2 * f2;
+      if (mag2 <= c * c) { p1 = f1; p2 = f2; }
+      else { const R sc = c / Sc<R>::sqrt(mag2); p1 = f1 * sc; p2 = f2 * sc; }
+    }
+    R d1 = p1 - imp[r1], d2 = p2 - imp[r2];
+    imp[r1] = p1; imp[r2] = p2;
+    apply_impulse(rows[r1], d1, bd, bodies, iinv);
+    apply_impulse(rows[r2], d2, bd, bodies, iinv);
+  };
+  // solver.rs:1085-1200: per contact the normal row, then the pyramidal
+  // pairs, or the tangent pair under the cone, torsion and the rolling pair,
+  // every cap from the just-updated normal impulse
   for (int it = 0; it < iterations; ++it) {
     for (const FreePC<R>& pc : sys.pcs) {
       step_nonneg(pc.start);
-      if (pc.condim == 3) { step_pair(pc.start, pc.h01a); step_pair(pc.start + 2, pc.h01b); }
+      if (sys.facets(pc)) { step_pair(pc.start, pc.h01a); step_pair(pc.start + 2, pc.h01b); }
+      else if (pc.condim >= 3) {
+        const R cap = imp[pc.start];
+        step_cone(pc.start + 1, pc.start + 2, cap, pc.mu, pc.mu);
+        if (pc.condim >= 4) step_cap(pc.start + 3, pc.mu_t * cap);
+        if (pc.condim >= 6) step_cone(pc.start + 4, pc.start + 5, cap, pc.mu_r, pc.mu_r);
+      }
     }
   }
   free_row_wrenches(sys, imp, dt, wrenches);
@@ -833,6 +928,7 @@ template <class R> struct World {
   Vec3<R> gravity = Vec3<R>(0, 0, R(-9.81));
   int solver_mode = M_PGS;
   int iterations = 20;
+  int cone = 0;  // SolverConfig::cone: 0 pyramidal, 1 elliptic
   int integrator = 1;  // 0: RK4 (newt's default), 1: semi-implicit Euler (world.rs:76-84)
   std::vector<Body<R>> bodies;
   std::vector<Tree<R>> trees;

@@ -32,6 +32,7 @@ template <class R> World<R> build_world(const newt_model_desc& d) {
   w.gravity = v3<R>(d.gravity);
   w.solver_mode = d.solver == NEWT_SOLVER_NEWTON ? M_NEWTON : (d.solver == NEWT_SOLVER_PGS ? M_PGS : M_PENALTY);
   w.iterations = d.iterations;
+  w.cone = d.cone;
   for (int i = 0; i < d.n_bodies; ++i) {
     const newt_body_desc& b = d.bodies[i];
     w.bodies.push_back(make_body<R>(b.mass, m3<R>(b.inertia), Vec3<R>(), Quat<R>()));
@@ -63,6 +64,7 @@ template <class R> World<R> build_world(const newt_model_desc& d) {
     g.solimp.dmin = G.solimp[0]; g.solimp.dmax = G.solimp[1]; g.solimp.width = G.solimp[2];
     g.solimp.midpoint = G.solimp[3]; g.solimp.power = (int)G.solimp[4];
     g.margin = G.margin; g.gap = G.gap; g.condim = G.condim;
+    g.torsional_friction = G.torsional_friction; g.rolling_friction = G.rolling_friction;
     g.group = G.group; g.mask = G.mask;
     w.geoms.push_back(g);
   }
@@ -490,11 +492,19 @@ int oracle_contact_sensors(const newt_model_desc* d, const float* qpos, const fl
       if (!solve_free_bodies_newton(w.bodies, w.geoms, contacts, w.gravity, w.dt, w.iterations, wr, &imp,
                                     &row_contact)) { rc = -1; return; }
     } else {
-      solve_free_bodies_pgs(w.bodies, w.geoms, contacts, w.gravity, w.dt, w.iterations, wr, &imp, &row_contact);
+      solve_free_bodies_pgs(w.bodies, w.geoms, contacts, w.gravity, w.dt, w.iterations, wr, &imp, &row_contact,
+                            w.cone);
     }
     if (wr.empty()) wr.assign(w.bodies.size(), Wrench<R>{Vec3<R>(), Vec3<R>()});
+    // the facets' impulses summed (pyramidal condim 3), else the normal row's
     std::vector<R> fn(contacts.size(), R(0));
-    for (size_t r = 0; r < imp.size(); ++r) fn[row_contact[r]] += imp[r];
+    std::vector<char> seen(contacts.size(), 0);
+    for (size_t r = 0; r < imp.size(); ++r) {
+      const int c = row_contact[r];
+      const bool facets = w.cone == 0 && std::min(w.geoms[contacts[c].ga].condim, w.geoms[contacts[c].gb].condim) == 3;
+      if (facets || !seen[c]) fn[c] += imp[r];
+      seen[c] = 1;
+    }
     for (R& x : fn) x = x / w.dt;
     int o = 0;
     for (int k = 0; k < ns; ++k) {
@@ -542,7 +552,7 @@ int oracle_impulses(const newt_model_desc* d, const float* qpos, const float* qv
     if (w.solver_mode == M_NEWTON) {
       if (!solve_free_bodies_newton(w.bodies, w.geoms, cs, w.gravity, w.dt, its, wr, &imp)) imp.clear();
     } else {
-      solve_free_bodies_pgs(w.bodies, w.geoms, cs, w.gravity, w.dt, its, wr, &imp);
+      solve_free_bodies_pgs(w.bodies, w.geoms, cs, w.gravity, w.dt, its, wr, &imp, nullptr, w.cone);
     }
     *n_out = (int)imp.size();
     for (int i = 0; i < (int)imp.size() && i < cap; ++i) impulses[i] = imp[i];

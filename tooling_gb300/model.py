@@ -19,6 +19,7 @@ import numpy as np
 JOINT_FREE, JOINT_FIXED, JOINT_HINGE, JOINT_SLIDE, JOINT_BALL = 0, 1, 2, 3, 4
 SHAPE_PLANE, SHAPE_SPHERE, SHAPE_BOX, SHAPE_CAPSULE, SHAPE_CYLINDER, SHAPE_ELLIPSOID = 0, 1, 2, 3, 4, 5
 SOLVER_PGS, SOLVER_NEWTON = 1, 2
+CONE_PYRAMIDAL, CONE_ELLIPTIC = 0, 1
 INTEGRATOR_EULER, INTEGRATOR_RK4 = 0, 1
 JOINT_NQ = {JOINT_FREE: 7, JOINT_FIXED: 0, JOINT_HINGE: 1, JOINT_SLIDE: 1, JOINT_BALL: 4}
 JOINT_NV = {JOINT_FREE: 6, JOINT_FIXED: 0, JOINT_HINGE: 1, JOINT_SLIDE: 1, JOINT_BALL: 3}
@@ -44,6 +45,7 @@ class GeomDesc(C.Structure):
         ("local_pos", C.c_float * 3), ("local_quat", C.c_float * 4), ("friction", C.c_float),
         ("solref", C.c_float * 2), ("solimp", C.c_float * 5), ("margin", C.c_float), ("gap", C.c_float),
         ("condim", C.c_int32), ("group", C.c_uint32), ("mask", C.c_uint32),
+        ("torsional_friction", C.c_float), ("rolling_friction", C.c_float),
     ]
 
 
@@ -52,7 +54,7 @@ class ModelDesc(C.Structure):
         ("n_links", C.c_int32), ("n_bodies", C.c_int32), ("n_geoms", C.c_int32),
         ("links", C.POINTER(LinkDesc)), ("bodies", C.POINTER(BodyDesc)), ("geoms", C.POINTER(GeomDesc)),
         ("dt", C.c_float), ("gravity", C.c_float * 3), ("solver", C.c_int32), ("iterations", C.c_int32),
-        ("tree_self_collision", C.c_int32), ("integrator", C.c_int32),
+        ("tree_self_collision", C.c_int32), ("integrator", C.c_int32), ("cone", C.c_int32),
     ]
 
 
@@ -141,6 +143,8 @@ class Geom:
     condim: int = 3
     group: int = 0xFFFFFFFF
     mask: int = 0xFFFFFFFF
+    torsional_friction: float = 0.0  # condim >= 4 (newt Geom::torsional_friction)
+    rolling_friction: float = 0.0    # condim 6 (newt Geom::rolling_friction)
 
 
 @dataclass
@@ -153,6 +157,7 @@ class WorldModel:
     iterations: int = 20
     tree_self_collision: int = 0
     integrator: int = 0  # INTEGRATOR_EULER or INTEGRATOR_RK4
+    cone: int = CONE_PYRAMIDAL  # SolverConfig::cone
     links: List[Link] = field(default_factory=list)
     bodies: List[tuple] = field(default_factory=list)  # (mass, inertia9)
     geoms: List[Geom] = field(default_factory=list)
@@ -210,6 +215,7 @@ class PackedModels:
                 d.solref[:] = list(g.solref); d.solimp[:] = list(g.solimp)
                 d.margin, d.gap, d.condim = g.margin, g.gap, g.condim
                 d.group, d.mask = g.group & 0xFFFFFFFF, g.mask & 0xFFFFFFFF
+                d.torsional_friction, d.rolling_friction = g.torsional_friction, g.rolling_friction
             self._keep += [links, bodies, geoms]
             md = self.descs[i]
             md.n_links, md.n_bodies, md.n_geoms = len(m.links), len(m.bodies), len(m.geoms)
@@ -221,6 +227,7 @@ class PackedModels:
             md.solver, md.iterations = m.solver, m.iterations
             md.tree_self_collision = m.tree_self_collision
             md.integrator = m.integrator
+            md.cone = m.cone
 
     def __len__(self) -> int:
         return len(self.descs)
@@ -268,7 +275,7 @@ class Batch:
     """
 
     def __init__(self, links, n_links, bodies, n_bodies, geoms, n_geoms, dt, gravity, solver, iterations,
-                 self_coll=0, integrator=INTEGRATOR_EULER):
+                 self_coll=0, integrator=INTEGRATOR_EULER, cone=CONE_PYRAMIDAL):
         self.links = np.ascontiguousarray(links)
         self.bodies = np.ascontiguousarray(bodies)
         self.geoms = np.ascontiguousarray(geoms)
@@ -311,6 +318,7 @@ class Batch:
             d.gravity[0], d.gravity[1], d.gravity[2] = gravity
             d.solver, d.iterations, d.tree_self_collision = int(solver[w]), int(iters[w]), int(self_coll)
             d.integrator = int(integrator)
+            d.cone = int(cone)
         self.qpos = np.zeros(int(nq.sum()), np.float32)
         self.qvel = np.zeros(int(nv.sum()), np.float32)
         self.qfrc = np.zeros(int(nv.sum()), np.float32)
