@@ -309,7 +309,11 @@ NEWT_API int newt_gpu_read_sensors(newt_gpu_ctx* ctx, const int32_t* slots, int3
 NEWT_API int newt_gpu_get_contacts(newt_gpu_ctx* ctx, int32_t slot, int32_t cap, int32_t* n_out,
                           int32_t* pairs, float* data);
 /* Row impulses of the last step's constraint solve for one world, in the
- * solver's row order (4 pyramidal facet rows per contact). */
+ * solver's row order (newt's impulses, solver.rs:1204-1257), per detected
+ * contact (zeros for an inactive one): 4 pyramidal facet rows; on pile
+ * worlds with the elliptic cone or a condim other than 3, 6 slots per
+ * contact holding its rows first (facets, or normal, tangents, torsion,
+ * rolling as its condim has them) and zeros after. */
 NEWT_API int newt_gpu_get_impulses(newt_gpu_ctx* ctx, int32_t slot, int32_t cap, int32_t* n_out, float* impulses);
 
 /* ---- timing helpers for the benchmark (CUDA events on the ctx stream) ---- */

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnewt_gpu.so")
 SOURCES = ["runtime.cu", "groups.cu", "step.cu", "tree_kernels.cu", "pile_kernels.cu", "pile_fused.cu", "newton_kernels.cu",
-           "static_step.cu", "ccd_query.cu", "pile_newton.cu",
+           "static_step.cu", "ccd_query.cu", "pile_newton.cu", "pile_general.cu",
            "world_io.cu", "serve.cpp", "ctrl_stream.cu", "sensors.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # GJK/EPA compiled without multiply-add contraction: with its face threshold

@@ -97,6 +97,8 @@ static void pile_rows(HostGroup& g) {
   l.gquat = r; r += 4 * nb;
   l.fric = r; r += ng;
   l.margin = r; r += ng;
+  l.tfric = r; r += ng;
+  l.rfric = r; r += ng;
   l.soft = r; r += 7;
   l.plane = r; r += 7 * np;
   l.dtg = r; r += 4;
@@ -107,7 +109,8 @@ static void pile_rows(HostGroup& g) {
   l.omg = r; r += 3 * nb;
   r = (r + 3) / 4 * 4;
   l.cdata = r; r += 7 * g.maxc;
-  l.imp = r; r += 4 * g.maxc;
+  l.rpc = g.pile_general ? 6 : 4;
+  l.imp = r; r += l.rpc * g.maxc;
   r = (r + 31) / 32 * 32;
   l.fstride = r;
   int q = 0;
@@ -118,6 +121,8 @@ static void pile_rows(HostGroup& g) {
   l.ncon = q; q += 1;
   l.live = q; q += 1;
   l.integ = q; q += 1;
+  l.gcond = q; q += ng;
+  l.cone = q; q += 1;
   l.cpair = q; q += 2 * g.maxc;
   q = (q + 31) / 32 * 32;
   l.istride = q;
@@ -345,6 +350,9 @@ void HostGroup::write_model(newt_gpu_ctx*, int w, const HostModel& m) {
       I(l.gent + k, w) = e;
       F(l.fric + e, w) = G.friction;
       F(l.margin + e, w) = G.margin;
+      F(l.tfric + e, w) = G.torsional_friction;
+      F(l.rfric + e, w) = G.rolling_friction;
+      I(l.gcond + e, w) = G.condim;
       if (G.body >= 0) {
         I(l.shape + e, w) = G.shape;
         for (int a = 0; a < 3; ++a) { F(l.size + 3 * e + a, w) = G.size[a]; F(l.gpos + 3 * e + a, w) = G.local_pos[a]; }
@@ -373,6 +381,7 @@ void HostGroup::write_model(newt_gpu_ctx*, int w, const HostModel& m) {
     I(l.iters, w) = m.iterations;
     I(l.status, w) = 0; I(l.ncon, w) = 0; I(l.live, w) = 1;
     I(l.integ, w) = m.integrator;
+    I(l.cone, w) = m.cone;
   }
   model_dirty = true;
   pending.push_back(w);
@@ -572,7 +581,7 @@ int HostGroup::read_impulses(newt_gpu_ctx* ctx, int w, int cap_out, int* n_out, 
   CKG(cudaMemcpy(rec.data(), dI + (size_t)w * irows, irows * sizeof(int), cudaMemcpyDeviceToHost));
   CKG(cudaMemcpy(frec.data(), dF + (size_t)w * frows, frows * sizeof(float), cudaMemcpyDeviceToHost));
   int nc = std::min(rec[lay.ncon], maxc);
-  int nr = 4 * nc;
+  int nr = lay.rpc * nc;
   *n_out = nr;
   for (int i = 0; i < nr && i < cap_out; ++i) imp[i] = frec[lay.imp + i];
   return NEWT_OK;
@@ -613,6 +622,7 @@ PileGroupDev HostGroup::pile_dev() const {
   d.F = dF; d.I = dI;
   d.scr = (float*)plain_scratch;
   d.sstride = scr_stride;
+  d.solve = pile_newton ? PS_NEWTON : pile_general ? PS_GENERAL : PS_PGS;
   return d;
 }
 

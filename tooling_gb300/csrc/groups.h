@@ -68,11 +68,20 @@ struct PileLayout {
   int fstride, istride;
   // float fields
   int mass, inert, iinv, size, gpos, gquat, fric, margin, soft, plane, dtg;
+  int tfric, rfric;  // per entity: torsional and rolling friction
   int pos, quat, vel, omg;
   int cdata, imp;
+  int rpc;  // impulse slots per contact in `imp`: 4 (facet rows), 6 on general-row groups
   // int fields
   int shape, gent, iters, status, ncon, cpair, live, integ;
+  int gcond, cone;  // per entity: condim; the world's friction cone (NEWT_CONE_*)
 };
+
+// How a pile group's contacts are solved: PGS over the pyramidal facet rows
+// (condim 3 everywhere, the island-class and world-persistent kernels), the
+// dense Newton solve (pile_newton.cu), or PGS over newt's general rows
+// (elliptic cone, condim 1, 4 or 6: pile_general.cu).
+enum PileSolve { PS_PGS = 0, PS_NEWTON = 1, PS_GENERAL = 2 };
 
 // Free bodies with one geom each plus static planes (config 1 piles).
 struct PileGroupDev {
@@ -85,4 +94,5 @@ struct PileGroupDev {
   int* I;        // world-major int records
   float* scr;    // per-world solver scratch (world-major)
   long sstride;  // floats per world in `scr`
+  int solve;     // PileSolve
 };

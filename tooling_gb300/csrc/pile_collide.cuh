@@ -70,8 +70,10 @@ __host__ __device__ inline WsLay ws_layout(int nb, int np, int maxc) {
 }
 
 // contact float fields (offsets inside one contact's CF block)
-enum { C_POS = 0, C_N = 3, C_PEN = 6, C_MU = 7, C_T1 = 8, C_ARMA = 11, C_ARMB = 14, C_DIAG = 17, C_REG = 21,
-       C_BIAS = 25, C_IMP = 29, C_H01 = 33, C_ACT = 35, C_NR = 36 };
+// C_IMP: the contact's row impulses (four facet rows, or up to six general
+// rows: normal, two tangents, torsion, two rolling); C_ACT: 0 inactive, 1
+// active with facet rows, 2 active with general rows
+enum { C_POS = 0, C_N = 3, C_PEN = 6, C_MU = 7, C_IMP = 29, C_ACT = 35 };
 // contact int fields: ga, gb, ea, eb
 // misc ints: 0 npairs, 1 ncon, 2 overflow, 3 islands
 
@@ -119,7 +121,7 @@ NEWT_D void ws_store_diag(const PileGroupDev& g, int w, const WsLay& L, const fl
     const int* cc = wi + L.ci + CI * c;
     I[P.cpair + 2 * c] = cc[0]; I[P.cpair + 2 * c + 1] = cc[1];
     for (int k = 0; k < 7; ++k) F[P.cdata + 7 * c + k] = cf[C_POS + k];
-    for (int k = 0; k < 4; ++k) F[P.imp + 4 * c + k] = cf[C_IMP + k];
+    for (int k = 0; k < P.rpc; ++k) F[P.imp + P.rpc * c + k] = cf[C_IMP + k];
   }
   if (lane == 0) {
     I[P.ncon] = nc;

@@ -109,7 +109,7 @@ NEWT_D void assemble(const WsLay& L, float* wf, int* wi, int lane, int t_world, 
     float* cf = wf + L.con + CF * c;
     const int* cc = wi + L.ci + CI * c;
     cf[C_ACT] = ((cc[2] < nb || cc[3] < nb) && cf[C_PEN] > 0.f) ? 1.f : 0.f;
-    for (int k = 0; k < 4; ++k) cf[C_IMP + k] = 0.f;
+    for (int k = 0; k < 6; ++k) cf[C_IMP + k] = 0.f;  // six slots: general rows read them all
   }
   __syncwarp();
   // islands, warp-parallel: each body's component as a 64-bit body mask
@@ -1015,13 +1015,16 @@ extern "C" int newt_launch_pile_step(const PileGroupDev* dG, const int* dwseg, i
 
 extern "C" void newt_launch_pile_newton_solve(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
                                               cudaStream_t st);
+extern "C" void newt_launch_pile_general_solve(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
+                                               cudaStream_t st);
 
 // The contact re-solve of every world of a table at its current state
-// (pile_k_reassemble, then the island-class PGS solvers or the dense Newton
-// solve; nothing is integrated): the velocity changes and the contacts'
-// impulses the contact sensors read.  Returns the launches issued.
+// (pile_k_reassemble, then the island-class PGS solvers, the dense Newton
+// solve or the general-row solve, by `solve` (PileSolve); nothing is
+// integrated): the velocity changes and the contacts' impulses the contact
+// sensors read.  Returns the launches issued.
 extern "C" int newt_launch_pile_resolve(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
-                                        int total_slots, int* lists, int newton, cudaStream_t st) {
+                                        int total_slots, int* lists, int solve, cudaStream_t st) {
   if (total_worlds <= 0) return 0;
   IslandLists il;
   il.items = lists;
@@ -1031,8 +1034,12 @@ extern "C" int newt_launch_pile_resolve(const PileGroupDev* dG, const int* dwseg
   cudaMemsetAsync(il.counts, 0, N_COUNTERS * sizeof(int), st);
   const int wpb = 4;
   pile_k_reassemble<<<(total_worlds + wpb - 1) / wpb, 32 * wpb, 0, st>>>(dG, dwseg, ng, total_worlds, il);
-  if (newton) {
+  if (solve == PS_NEWTON) {
     newt_launch_pile_newton_solve(dG, dwseg, ng, total_worlds, st);
+    return 2;
+  }
+  if (solve == PS_GENERAL) {
+    newt_launch_pile_general_solve(dG, dwseg, ng, total_worlds, st);
     return 2;
   }
   const int grid = std::min((total_slots + 127) / 128, cap128);
@@ -1045,7 +1052,8 @@ extern "C" int newt_launch_pile_resolve(const PileGroupDev* dG, const int* dwseg
 // the body accelerations of :586-600).  The velocity changes dv, dw (world
 // frame) are M^-1 J^T f, so newt's wrench is F = m dv / dt and
 // tau_world = I_world dw / dt; a contact's normal force is its facet
-// impulses summed over dt.  Writes only the accelerometer and touch entries
+// impulses summed over dt (solver.rs:1240-1253), or its normal row's
+// impulse over dt where its rows are general.  Writes only the accelerometer and touch entries
 // of each output row (the state sensors' kernel writes the rest).
 __global__ void __launch_bounds__(64) pile_contact_sensors_kernel(PileGroupDev g, const int* idx, int n,
                                                                  const newt_sensor_desc* S, int ns, float* out,
@@ -1069,7 +1077,9 @@ __global__ void __launch_bounds__(64) pile_contact_sensors_kernel(PileGroupDev g
         const int* cc = wi + L.ci + CI * c;
         if (cc[0] != S[k].index && cc[1] != S[k].index) continue;
         const float* cf = wf + L.con + CF * c;
-        const float f = (((0.f + cf[C_IMP]) + cf[C_IMP + 1]) + cf[C_IMP + 2]) + cf[C_IMP + 3];
+        // the facets' impulses summed in row order, or a general block's normal row
+        const float f = cf[C_ACT] == 2.f ? cf[C_IMP]
+                                         : (((0.f + cf[C_IMP]) + cf[C_IMP + 1]) + cf[C_IMP + 2]) + cf[C_IMP + 3];
         sum += fabsf(f / dt);
       }
       row[o++] = sum;
@@ -1106,8 +1116,8 @@ extern "C" void newt_launch_pile_contact_sensors(const PileGroupDev& g, const in
   if (n > 0) pile_contact_sensors_kernel<<<(n + 63) / 64, 64, 0, st>>>(g, idx, n, S, ns, out, D);
 }
 
-// The collide and integrate stages alone, for the free-body Newton step
-// (pile_newton.cu): the island lists collide appends to are not read there,
+// The collide and integrate stages alone, for the pile worlds solved apart
+// (newt_launch_pile_solo_step): the island lists collide appends to are not read there,
 // but their counters are zeroed so every append stays in bounds.
 extern "C" void pile_k_collide_launch(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
                                       int total_slots, int* lists, cudaStream_t st) {

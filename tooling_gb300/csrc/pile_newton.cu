@@ -1,7 +1,7 @@
 // Free-body Newton: the contact solve of pile worlds whose solver is Newton.
 //
-// Per env-step (newt_launch_pile_newton_step): pile_k_collide as for PGS
-// (contacts, the active set, per contact the facet rows' J and M^-1 J^T and
+// Per env-step (newt_launch_pile_solo_step, pile_general.cu): pile_k_collide
+// as for PGS (contacts, the active set, per contact the facet rows' J and M^-1 J^T and
 // the row constants), then one warp per world here, then pile_k_integrate
 // with the velocity changes this kernel leaves (Euler, or RK4 with the
 // solver's wrench held over the stages).
@@ -63,6 +63,7 @@ __global__ void __launch_bounds__(32) pile_k_newton(const PileGroupDev* G, const
   if (t >= total) return;
   const int gi = find_seg(wseg, ng, t);
   const PileGroupDev& g = G[gi];
+  if (g.solve != PS_NEWTON) return;
   const int w = t - wseg[gi];
   if (w >= g.n || !g.I[(size_t)w * g.lay.istride + g.lay.live]) return;
   const int lane = threadIdx.x;
@@ -165,24 +166,8 @@ __global__ void __launch_bounds__(32) pile_k_newton(const PileGroupDev* G, const
 // Floats of one world's Newton region (past its pile scratch).
 extern "C" size_t newt_pile_newton_bytes(int maxc) { return (size_t)newton_layout(maxc).words * sizeof(float); }
 
-extern "C" void pile_k_collide_launch(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
-                                      int total_slots, int* lists, cudaStream_t st);
-extern "C" void pile_k_integrate_launch(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
-                                        int write_diag, cudaStream_t st);
-
-// The dense Newton solve alone (the contact sensors' re-solve).
+// The dense Newton solve (the solo step's and the contact sensors' re-solve).
 extern "C" void newt_launch_pile_newton_solve(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
                                               cudaStream_t st) {
   if (total_worlds > 0) pile_k_newton<<<total_worlds, 32, 0, st>>>(dG, dwseg, ng, total_worlds);
-}
-
-// One env-step of a table of Newton pile groups on `st`: collide, the
-// Newton solve, integrate.  Returns the launches issued.
-extern "C" int newt_launch_pile_newton_step(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
-                                            int total_slots, int* lists, int write_diag, cudaStream_t st) {
-  if (total_worlds <= 0) return 0;
-  pile_k_collide_launch(dG, dwseg, ng, total_worlds, total_slots, lists, st);
-  pile_k_newton<<<total_worlds, 32, 0, st>>>(dG, dwseg, ng, total_worlds);
-  pile_k_integrate_launch(dG, dwseg, ng, total_worlds, write_diag, st);
-  return 3;
 }

@@ -43,7 +43,9 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
   m.dt = d.dt; for (int k = 0; k < 3; ++k) m.g[k] = d.gravity[k];
   m.solver = d.solver; m.iterations = d.iterations; m.self_coll = d.tree_self_collision;
   m.integrator = d.integrator;
+  m.cone = d.cone;
   if (!(d.dt > 0.f)) return fail(ctx, NEWT_E_INVALID, "dt must be > 0");
+  if (d.cone != NEWT_CONE_PYRAMIDAL && d.cone != NEWT_CONE_ELLIPTIC) return fail(ctx, NEWT_E_INVALID, "unknown cone");
   if (d.integrator != NEWT_INTEGRATOR_EULER && d.integrator != NEWT_INTEGRATOR_RK4)
     return fail(ctx, NEWT_E_INVALID, "unknown integrator");
   if (d.solver != 0 && d.solver != NEWT_SOLVER_PGS && d.solver != NEWT_SOLVER_NEWTON)
@@ -102,8 +104,13 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
         if (G.shape != NEWT_SHAPE_PLANE) return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "static geoms must be planes");
         ++np;
       }
-      if (G.condim != 3 && G.condim != 1) return fail(ctx, NEWT_E_INVALID, "condim must be 1 or 3");
+      if (G.condim != 1 && G.condim != 3 && G.condim != 4 && G.condim != 6)
+        return fail(ctx, NEWT_E_INVALID, "condim must be 1, 3, 4 or 6 (newt/src/solver.rs:1409-1428)");
+      if (d.solver == NEWT_SOLVER_NEWTON && G.condim != 3)
+        return fail(ctx, NEWT_E_INVALID, "pile worlds under the Newton solver take condim 3 on the GPU path");
     }
+    if (d.solver == NEWT_SOLVER_NEWTON && d.cone != NEWT_CONE_PYRAMIDAL)
+      return fail(ctx, NEWT_E_INVALID, "the Newton solver takes the pyramidal cone (newt/src/solver.rs:89-91)");
     // newt has no capsule-box primitive (newt/src/contact.rs:232-257) and
     // panics when such a pair is active; the pair is refused here instead
     for (int i = 0; i < d.n_geoms; ++i)
@@ -155,8 +162,11 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
       } else if (G.shape != NEWT_SHAPE_PLANE) {
         return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "static geoms must be planes");
       }
-      if (G.condim != 3 && G.condim != 1) return fail(ctx, NEWT_E_INVALID, "condim must be 1 or 3");
+      if (G.condim != 3 && G.condim != 1)
+        return fail(ctx, NEWT_E_INVALID, "condim must be 1 or 3 on tree-contact worlds (4 and 6: pile worlds)");
     }
+    if (d.cone != NEWT_CONE_PYRAMIDAL)
+      return fail(ctx, NEWT_E_INVALID, "tree-contact worlds take the pyramidal cone on the GPU path");
     if (d.tree_self_collision && nlink_geoms > 1)
       return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "in-tree geom pairs are not on the GPU path (disable tree self-collision)");
     if (d.solver != NEWT_SOLVER_PGS && d.solver != NEWT_SOLVER_NEWTON)
@@ -183,6 +193,7 @@ HostGroup* find_or_make_group(newt_gpu_ctx* ctx, HostModel& m) {
   g->nq = m.nq; g->nv = m.nv;
   g->maxc_cap = ctx->max_contacts;
   g->pile_newton = m.kind == GK_PILE && m.solver == NEWT_SOLVER_NEWTON;
+  g->pile_general = m.kind == GK_PILE && !g->pile_newton && m.general_rows();
   if (m.kind == GK_TREE_CONTACT) g->setup_tc(m);
   g->id = (int)ctx->groups.size();
   m.group = g->id;

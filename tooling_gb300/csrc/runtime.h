@@ -20,8 +20,15 @@ struct HostModel {
   std::vector<newt_body_desc> bodies;
   std::vector<newt_geom_desc> geoms;
   float dt = 0.005f, g[3] = {0, 0, -9.81f};
-  int solver = 1, iterations = 20, self_coll = 0, integrator = NEWT_INTEGRATOR_EULER;
+  int solver = 1, iterations = 20, self_coll = 0, integrator = NEWT_INTEGRATOR_EULER, cone = NEWT_CONE_PYRAMIDAL;
   std::string key;  // topo_key(), computed once at upload
+  // pile worlds whose rows are not four pyramidal facets per contact
+  bool general_rows() const {
+    if (cone != NEWT_CONE_PYRAMIDAL) return true;
+    for (auto& gd : geoms)
+      if (gd.condim != 3) return true;
+    return false;
+  }
   int group = -1;   // the group its worlds live in, once one exists
   // topology key: trees in one group must share parent/joint layout
   std::string topo_key() const {
@@ -40,6 +47,7 @@ struct HostModel {
       // solver picks the step's kernels
       k += "np"; k += std::to_string(np);
       if (solver == NEWT_SOLVER_NEWTON) k += "newton";
+      else if (general_rows()) k += "general";
     }
     return k;
   }
@@ -84,7 +92,11 @@ struct HostGroup {
   int* dgtopo = nullptr;
   int* dpairs = nullptr;
   bool soa() const { return kind == GK_TREE || kind == GK_TREE_CONTACT; }
-  bool pile_newton = false;  // pile worlds under newt's free-body Newton solve (pile_newton.cu)
+  bool pile_newton = false;   // pile worlds under newt's free-body Newton solve (pile_newton.cu)
+  bool pile_general = false;  // pile worlds with the elliptic cone or condim 1, 4, 6 (pile_general.cu)
+  // solved apart from the facet-row PGS kernels: per env-step collide, the
+  // group's own solve, integrate
+  bool pile_solo() const { return pile_newton || pile_general; }
   TcGroupDev tc_dev() const;
   void setup_tc(const HostModel& m);
   void* plain_scratch = nullptr;  // pile solver scratch, cap worlds (both step forms)

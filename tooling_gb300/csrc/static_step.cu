@@ -119,6 +119,8 @@ extern "C" NEWT_API int newt_gpu_step_static(newt_gpu_ctx* ctx, int32_t n_steps)
     if (g->kind == GK_TREE_CONTACT) return fail(ctx, NEWT_E_INVALID, "tree-contact worlds are not supported");
     if (g->kind != GK_PILE) continue;
     if (g->pile_newton) return fail(ctx, NEWT_E_INVALID, "pile worlds under the Newton solver are not supported");
+    if (g->pile_general)
+      return fail(ctx, NEWT_E_INVALID, "pile worlds with the elliptic cone or condim 1, 4, 6 are not supported");
     if (ng == kMaxPileGroups) return fail(ctx, NEWT_E_INVALID, "more than 64 pile groups (distinct body counts)");
     table[ng] = g->pile_dev();
     seg[ng + 1] = seg[ng] + g->n;

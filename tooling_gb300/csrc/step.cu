@@ -36,8 +36,8 @@ extern "C" int newt_launch_pile_fused(const PileGroupDev* dG, const int* dwseg, 
                                       int nbm, int cm, int shape, cudaStream_t st);
 extern "C" int newt_tc_prepare(newt_gpu_ctx* ctx, HostGroup* g, int n_steps);
 extern "C" size_t newt_pile_newton_bytes(int maxc);
-extern "C" int newt_launch_pile_newton_step(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
-                                            int total_slots, int* lists, int write_diag, cudaStream_t st);
+extern "C" int newt_launch_pile_solo_step(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
+                                          int total_slots, int* lists, int write_diag, int kinds, cudaStream_t st);
 extern "C" int newt_tc_launch(newt_gpu_ctx* ctx, HostGroup* g, int n_steps, cudaStream_t st, bool capturing);
 
 // Streams and events the pile step forks its island classes onto.
@@ -178,7 +178,7 @@ static int ensure_plain_tables(newt_gpu_ctx* ctx) {
 }
 
 extern "C" int newt_launch_pile_resolve(const PileGroupDev* dG, const int* dwseg, int ng, int total_worlds,
-                                        int total_slots, int* lists, int newton, cudaStream_t st);
+                                        int total_slots, int* lists, int solve, cudaStream_t st);
 
 // The contact sensors' re-solve of every world of pile group `g` at its
 // current state, on the context's stream (pile_kernels.cu).
@@ -187,7 +187,7 @@ int pile_resolve_group(newt_gpu_ctx* ctx, HostGroup* g) {
   if (rc != NEWT_OK) return rc;
   const auto& T = ctx->plain_tables[g->id];
   ctx->launches += newt_launch_pile_resolve((const PileGroupDev*)T.dG, T.dseg, T.ng, T.worlds, T.slots, T.lists,
-                                            g->pile_newton ? 1 : 0, ctx->stream);
+                                            g->pile_dev().solve, ctx->stream);
   return NEWT_OK;
 }
 
@@ -207,10 +207,10 @@ int step_plain(newt_gpu_ctx* ctx, int n_steps) {
       if (g->kind == GK_TREE) {
         newt_launch_tree_plain(g->tree_dev(), ctx->stream);
         ctx->launches += 2;
-      } else if (g->kind == GK_PILE && g->pile_newton) {
+      } else if (g->kind == GK_PILE && g->pile_solo()) {
         const auto& T = ctx->plain_tables[gi];
-        ctx->launches += newt_launch_pile_newton_step((const PileGroupDev*)T.dG, T.dseg, T.ng, T.worlds, T.slots,
-                                                      T.lists, s == n_steps - 1, ctx->stream);
+        ctx->launches += newt_launch_pile_solo_step((const PileGroupDev*)T.dG, T.dseg, T.ng, T.worlds, T.slots,
+                                                    T.lists, s == n_steps - 1, 1 << g->pile_dev().solve, ctx->stream);
       } else if (g->kind == GK_PILE) {
         const auto& T = ctx->plain_tables[gi];
         ctx->launches += newt_launch_pile_step((const PileGroupDev*)T.dG, T.dseg, T.ng, T.worlds, T.slots, T.lists,
@@ -260,13 +260,19 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
     L.grid = std::min(L.items, std::max(1, full * ctx->tune_tree_grid_pct / 100));
     tls.push_back(L);
   }
-  // PGS piles, largest worlds first; Newton piles apart (their own table,
-  // stepped per env-step: collide, the dense Newton solve, integrate)
+  // facet-row PGS piles, largest worlds first; the piles solved apart
+  // (Newton, general rows) in their own table, stepped per env-step:
+  // collide, each group's solve, integrate
   std::vector<HostGroup*> piles, npiles;
   long pile_worlds = 0;
+  int solo_kinds = 0;
   for (auto& gp : ctx->groups)
     if (gp->n > 0 && gp->kind == GK_PILE) {
-      if (gp->pile_newton) { npiles.push_back(gp.get()); continue; }
+      if (gp->pile_solo()) {
+        npiles.push_back(gp.get());
+        solo_kinds |= 1 << gp->pile_dev().solve;
+        continue;
+      }
       piles.push_back(gp.get());
       pile_worlds += gp->n;
     }
@@ -355,8 +361,8 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
   const int tc_launches = (int)(ctx->launches - l0);
   const int64_t before = ctx->launches;
   for (int s = 0; s < n_steps && nt.ng > 0; ++s)
-    ctx->launches += newt_launch_pile_newton_step(nt.dG, nt.dseg, nt.ng, nt.worlds, nt.slots, nt.lists,
-                                                  s == n_steps - 1, ctx->stream);
+    ctx->launches += newt_launch_pile_solo_step(nt.dG, nt.dseg, nt.ng, nt.worlds, nt.slots, nt.lists,
+                                                s == n_steps - 1, solo_kinds, ctx->stream);
   int fused_launches = 0;
   if (fused && ft.ng > 0) {
     cudaStream_t fs = ctx->pbs[0][0];
