@@ -323,8 +323,9 @@ NEWT_API int newt_gpu_flush_l2(newt_gpu_ctx* ctx);                              
 /* Kernel launches issued by this context since creation. */
 NEWT_API int64_t newt_gpu_launch_count(const newt_gpu_ctx* ctx);
 /* Times the batched step's launch choices on the live worlds (piles in the
- * world-persistent launch in each of its shapes -- gangs of 32, 24, 16, 12
- * or 8 warps per block, with or without a barrier between assembly and sweeps --
+ * world-persistent launch in each of its shapes -- gangs of 4 to 32 warps,
+ * one to four gangs per SM, with or without a barrier between assembly and
+ * sweeps, one or two worlds per warp --
  * or in the island-class pipeline with 1, 2 or 3 world-range branches; tree
  * persistent grid at full or half residency), `n_steps` env-steps per trial,
  * and keeps the fastest for later NEWT_STEP_BATCHED calls.  `horizon` is how

@@ -9,7 +9,8 @@ Bars (stated here, checked below):
     (newt's own f32 arithmetic, the oracle's float mirror, stays within
     1e-3 |row| + 1e-5 max on these worlds), for every solver path: the plain
     form's island-class kernels, the batched form's world-persistent kernel
-    and the batched island-class pipeline;
+    (one and two worlds per warp) and the batched island-class pipeline;
+  * every launch shape of the world-persistent kernel bit-identical;
   * short-horizon trajectories within 1e-3 m / 1e-2 m/s.
 """
 import numpy as np
@@ -76,15 +77,16 @@ def test_contact_pair_lists_match_oracle(eng, settled, mode):
     eng.free(slots)
 
 
-@pytest.mark.parametrize("path", ["plain", "persistent", "pipeline"])
+@pytest.mark.parametrize("path", ["plain", "persistent", "persistent_pairs", "pipeline"])
 def test_pgs_impulses_match_oracle_at_equal_iterations(eng, settled, path):
     b = settled
     slots = _load(eng, b)
-    eng.set_launch_choice(persistent=path != "pipeline")
+    # shape 6: gangs of 12 warps, two worlds per warp
+    eng.set_launch_choice(persistent=path != "pipeline", persistent_shape=6 if path == "persistent_pairs" else 2)
     try:
         eng.step(1, STEP_PLAIN if path == "plain" else STEP_BATCHED)
         eng.sync()
-        if path == "persistent":
+        if path.startswith("persistent"):
             _, fw = eng.fused_profile()
             assert fw["worlds"] == len(b) and fw["contacts"] > 0, fw
         else:
@@ -167,6 +169,39 @@ def test_free_body_scenes_within_mujoco_windows(eng, name, qtol, vtol, mode):
         worst_v = max(worst_v, np.abs(v - ref["qvel"][k]).max())
     eng.free(slots)
     assert worst_q <= qtol and worst_v <= vtol, (worst_q, worst_v)
+
+
+def test_persistent_shapes_agree_bit_for_bit(eng, settled):
+    """Every launch shape of the world-persistent kernel (gang size, the
+    barrier between assembly and sweeps, one or two worlds per warp, with
+    rounds of eight or four contacts) runs the same arithmetic per world: a
+    body's contacts keep their order in any round schedule.  20 batched
+    env-steps from the settled state agree bit for bit across shapes."""
+    from tooling_gb300 import api as A
+    b = settled
+    nq, nv = int(b.nq.sum()), int(b.nv.sum())
+    ref, shape = None, 0
+    try:
+        while True:
+            try:
+                eng.set_launch_choice(persistent=True, persistent_shape=shape)
+            except A.NewtError:
+                break
+            slots = _load(eng, b)
+            eng.step(20, STEP_BATCHED)
+            q, v = eng.get_state(slots, nq, nv)
+            st = eng.status(slots)
+            eng.free(slots)
+            assert not (st & 0x5).any(), (shape, st)
+            if ref is None:
+                ref = (q, v)
+            else:
+                np.testing.assert_array_equal(q, ref[0], err_msg=f"shape {shape}")
+                np.testing.assert_array_equal(v, ref[1], err_msg=f"shape {shape}")
+            shape += 1
+    finally:
+        eng.set_launch_choice(persistent=True)
+    assert shape >= 9, shape
 
 
 def test_world_range_branches_match_plain(eng):

@@ -365,7 +365,7 @@ class Engine:
         return {"pile_persistent": bool(c[3]), "persistent_shape": int(c[4]), "pile_branches": int(c[0]),
                 "tree_grid_pct": int(c[1]), "best_ms": c[2] / 1000.0}
 
-    def set_launch_choice(self, persistent: bool = True, persistent_shape: int = 2, pile_branches: int = 0,
+    def set_launch_choice(self, persistent: bool = True, persistent_shape: int = 10, pile_branches: int = 0,
                           tree_grid_pct: int = 100):
         """Pin the batched step's launch choices (what autotune() would pick):
         piles in the world-persistent launch of shape `persistent_shape`, or

@@ -219,19 +219,19 @@ NEWT_D int fused_assemble(const WsLay& L, float* wf, int* wi, int lane, float (*
 }
 
 // ---------------------------------------------------------------------------
-// levels: lane 0 assigns each record its round (at most eight records, on
-// disjoint bodies) and counting-sorts the records by round (sweep order
-// inside a round); `loff` gets the round starts and the end.  Returns the
-// round count.
+// levels: lane 0 assigns each record its round (at most `cap` records, on
+// disjoint bodies: the four-lane groups the world has, eight on a whole
+// warp, four on a half) and counting-sorts the records by round (sweep
+// order inside a round); `loff` gets the round starts and the end.
+// Returns the round count.
 // ---------------------------------------------------------------------------
 NEWT_D int fused_levels(const WsLay& L, const float* wf, int nact, int lane, short* last, short* lev, short* perm,
-                        short* loff) {
+                        short* loff, int cap) {
   int nlev = 0;
   for (int v = lane; v <= nact; v += 32) loff[v] = 0;  // contacts per round
   __syncwarp();
   if (lane == 0) {
-    // List scheduling with eight contacts (the warp's four-lane groups) per
-    // round: contact k takes the first round after the last rounds of its
+    // List scheduling with `cap` contacts per round: contact k takes the first round after the last rounds of its
     // bodies that still has a free group.  Every body still sees its
     // contacts in contact order and no round holds two contacts of one
     // body, so the sweep equals the serial one; islands fill each other's
@@ -242,7 +242,7 @@ NEWT_D int fused_levels(const WsLay& L, const float* wf, int nact, int lane, sho
       const float* rec = wf + L.sc + FR * k;
       const int ba = __float_as_int(rec[R_MISC + 2]), bb = __float_as_int(rec[R_MISC + 3]);
       int lv = 1 + max(ba < nb ? (int)last[ba] : 0, bb < nb ? (int)last[bb] : 0);
-      while (loff[lv] >= 8) ++lv;  // lv <= k + 1 <= nact: rounds 1..k hold at most k contacts
+      while (loff[lv] >= cap) ++lv;  // lv <= k + 1 <= nact: rounds 1..k hold at most k contacts
       loff[lv]++;
       if (ba < nb) last[ba] = (short)lv;
       if (bb < nb) last[bb] = (short)lv;
@@ -406,14 +406,14 @@ NEWT_HD WarpSmem warp_smem(int nbm, int cm) {
 // collide, assemble and levels; returns (active contacts, levels) and ORs
 // the contact-overflow flag into *overflow
 __device__ __noinline__ int2 fused_prepare(const PileGroupDev* g, int w, int lane, float (*acc)[6], short* last,
-                                           short* lev, short* perm, short* loff, int* overflow) {
+                                           short* lev, short* perm, short* loff, int* overflow, int cap) {
   const WsLay L = ws_layout(g->nb, g->np, g->maxc);
   float* wf = g->scr + (size_t)w * g->sstride;
   int* wi = reinterpret_cast<int*>(wf + L.nf);
   collide(L, wf, wi, lane);
   *overflow |= wi[L.misc + 2];
   const int nact = min(fused_assemble(L, wf, wi, lane, acc), F_MAXC);
-  const int nlev = fused_levels(L, wf, nact, lane, last, lev, perm, loff);
+  const int nlev = fused_levels(L, wf, nact, lane, last, lev, perm, loff, cap);
   return make_int2(nact, nlev);
 }
 
@@ -439,107 +439,167 @@ __device__ __noinline__ bool fused_finish(const PileGroupDev* g, int w, int lane
   return pile_integrate_world(wf, L, rk4, lane);
 }
 
+// the sweeps of one env-step on the calling lane's four-lane group (its
+// half's world); out of line, so that only the sweep's own registers are
+// live in it (the collide phase needs about twice as many)
+__device__ __noinline__ void fused_sweeps(float* sc, const short* perm, const short* loff, float (*acc)[6], int nb,
+                                          int iters, int nlev, int itmax, int nlmax, int slot, int l, unsigned gm) {
+  for (int it = 0; it < itmax; ++it)
+    for (int v = 0; v < nlmax; ++v) {
+      if (it < iters && v < nlev) {
+        const int idx = loff[v] + slot;
+        if (idx < loff[v + 1]) fused_contact(sc + FR * perm[idx], l, gm, nb, acc);
+      }
+      __syncwarp();
+    }
+}
+
 // ---------------------------------------------------------------------------
 // the kernel: gangs of warps over the world queue
 // ---------------------------------------------------------------------------
 // work (nullable): [0] active contacts summed over every world's env-steps,
-// [1] contact-update rounds (a level's groups of eight) summed over sweeps,
-// [2] levels summed over env-steps, [3] worlds stepped.  cost (per flat world
-// index): this call's contact-update rounds plus 64 per contact, the sort key
-// of the next call's queue.  nbm / cm: the table's largest body count and
-// contact capacity (they size the shared memory).
+// [1] contact-update rounds summed over sweeps, [2] rounds summed over
+// env-steps, [3] worlds stepped.  cost (per flat world index): this call's
+// contact-update rounds plus 64 per contact, the sort key of the next
+// call's queue.  nbm / cm: the table's largest body count and contact
+// capacity (they size the shared memory).
 // GANG: warps per block; MID: a block barrier between assembly and the
-// sweeps as well as after integration (otherwise only after integration).
-template <int GANG, bool MID>
-__global__ void __launch_bounds__(32 * GANG, 1) pile_k_fused(const PileGroupDev* G, const int* wseg, int ng,
+// sweeps as well as after integration (otherwise only after integration);
+// MINB: blocks per SM the registers are sized for (smaller gangs wait at
+// their barrier on fewer worlds; several gangs share an SM);
+// WPW: worlds per warp.  With two, the warp takes two consecutive worlds of
+// the queue (of about the same cost), runs collide, assembly and
+// integration for each in turn on all 32 lanes, and sweeps both at once,
+// each on a half-warp with rounds of at most four contacts: the rounds of a
+// settled pile fill five of eight groups on average, so two half-filled
+// worlds share one warp's instructions.  A body's contacts keep their order
+// under either round capacity, so the results are the same.
+// Per-world bookkeeping of a warp's worlds, in shared memory (written by
+// lane 0, read by all) so that the sweep keeps only its own registers live.
+struct FusedSlot {
+  const PileGroupDev* g;  // null: no world
+  int w, t, iters, rk4, bad, overflow, nact, nlev;
+  unsigned long long n_con, n_rounds, n_lev;
+};
+
+template <int GANG, bool MID, int WPW, int MINB>
+__global__ void __launch_bounds__(32 * GANG, MINB) pile_k_fused(const PileGroupDev* G, const int* wseg, int ng,
                                                              const int* queue, int n_items, int* counter, int n_steps,
                                                              unsigned long long* work, unsigned* cost, int nbm,
                                                              int cm) {
+  static_assert(WPW == 1 || WPW == 2, "one or two worlds per warp");
+  static_assert(GANG * WPW <= 32, "slots per block");
   extern __shared__ __align__(16) unsigned char fsm[];
   __shared__ int gang_base;
+  __shared__ FusedSlot fslot[32];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int slot = lane >> 2, l = lane & 3;
+  const int half = WPW == 2 ? lane >> 4 : 0;  // the world this lane sweeps
+  const int slot = (lane >> 2) & (8 / WPW - 1), l = lane & 3;
+  const int cap = 8 / WPW;                    // contacts per round
   const unsigned gm = 0xFu << (lane & ~3);
   const WarpSmem ws = warp_smem(nbm, cm);
-  unsigned char* mine = fsm + (size_t)wib * ws.bytes;
-  float(*acc)[6] = reinterpret_cast<float(*)[6]>(mine + ws.acc);
-  short* last = reinterpret_cast<short*>(mine + ws.last);
-  short* lev = reinterpret_cast<short*>(mine + ws.lev);
-  short* perm = reinterpret_cast<short*>(mine + ws.perm);
-  short* loff = reinterpret_cast<short*>(mine + ws.loff);
+  FusedSlot* my = fslot + WPW * wib;
+  auto region = [&](int j) { return fsm + (size_t)(WPW * wib + j) * ws.bytes; };
+  auto acc_of = [&](int j) { return reinterpret_cast<float(*)[6]>(region(j) + ws.acc); };
+  auto sh_of = [&](int j, int off) { return reinterpret_cast<short*>(region(j) + off); };
   for (;;) {
     __syncthreads();  // every warp is done with the previous gang's base
-    if (threadIdx.x == 0) gang_base = atomicAdd(counter, GANG);
+    if (threadIdx.x == 0) gang_base = atomicAdd(counter, WPW * GANG);
     __syncthreads();
-    const int item = gang_base + wib;
     if (gang_base >= n_items) break;  // uniform over the block
-    // this warp's world, if any (a gang at the end of the queue is partial)
-    int t = -1;
-    if (item < n_items) t = queue ? queue[item] : item;
-    const PileGroupDev* g = nullptr;
-    int w = 0;
-    if (t >= 0 && t < wseg[ng]) {
-      const int gi = find_seg(wseg, ng, t);
-      g = G + gi;
-      w = t - wseg[gi];
-      if (w >= g->n || !g->I[(size_t)w * g->lay.istride + g->lay.live]) g = nullptr;
+    // this warp's worlds, if any (a gang at the end of the queue is partial)
+    for (int j = 0; j < WPW; ++j) {
+      const int item = gang_base + WPW * wib + j;
+      const int t = item < n_items ? (queue ? queue[item] : item) : -1;
+      const PileGroupDev* g = nullptr;
+      int w = 0;
+      if (t >= 0 && t < wseg[ng]) {
+        const int gi = find_seg(wseg, ng, t);
+        g = G + gi;
+        w = t - wseg[gi];
+        if (w >= g->n || !g->I[(size_t)w * g->lay.istride + g->lay.live]) g = nullptr;
+      }
+      if (lane == 0) {
+        FusedSlot f{};
+        f.g = g;
+        f.w = w;
+        f.t = t;
+        if (g) {
+          f.iters = g->I[(size_t)w * g->lay.istride + g->lay.iters];
+          f.rk4 = g->I[(size_t)w * g->lay.istride + g->lay.integ] == NEWT_INTEGRATOR_RK4;
+        }
+        my[j] = f;
+      }
+      if (g) {  // uniform over the warp
+        const WsLay L = ws_layout(g->nb, g->np, g->maxc);
+        float* wf = g->scr + (size_t)w * g->sstride;
+        ws_load(*g, w, L, wf, reinterpret_cast<int*>(wf + L.nf), lane);
+      }
     }
-    const bool have = g != nullptr;  // uniform over the warp
-    float* sc = nullptr;  // the world's row records
-    int nb = 0, iters = 0;
-    bool rk4 = false;
-    if (have) {
-      const WsLay L = ws_layout(g->nb, g->np, g->maxc);
-      float* wf = g->scr + (size_t)w * g->sstride;
-      sc = wf + L.sc;
-      nb = g->nb;
-      iters = g->I[(size_t)w * g->lay.istride + g->lay.iters];
-      rk4 = g->I[(size_t)w * g->lay.istride + g->lay.integ] == NEWT_INTEGRATOR_RK4;
-      ws_load(*g, w, L, wf, reinterpret_cast<int*>(wf + L.nf), lane);
-    }
-    bool bad = false;
-    int overflow = 0;
-    unsigned long long n_con = 0, n_rounds = 0, n_lev = 0;
+    __syncwarp();
     for (int s = 0; s < n_steps; ++s) {
-      int2 nn = make_int2(0, 0);
-      if (have) nn = fused_prepare(g, w, lane, acc, last, lev, perm, loff, &overflow);
+      for (int j = 0; j < WPW; ++j) {
+        const PileGroupDev* g = my[j].g;
+        if (!g) continue;
+        int ovf = 0;
+        const int2 nn = fused_prepare(g, my[j].w, lane, acc_of(j), sh_of(j, ws.last), sh_of(j, ws.lev),
+                                      sh_of(j, ws.perm), sh_of(j, ws.loff), &ovf, cap);
+        if (lane == 0) {
+          const short* loff = sh_of(j, ws.loff);
+          int rounds = 0;
+          for (int v = 0; v < nn.y; ++v) rounds += (loff[v + 1] - loff[v] + cap - 1) / cap;
+          FusedSlot& f = my[j];
+          f.overflow |= ovf;
+          f.nact = nn.x;
+          f.nlev = nn.y;
+          f.n_con += (unsigned long long)nn.x;
+          f.n_rounds += (unsigned long long)rounds * (unsigned long long)f.iters;
+          f.n_lev += (unsigned long long)nn.y;
+        }
+        __syncwarp();
+      }
       if (MID) __syncthreads();  // the gang leaves collide and assembly together
-      if (have) {
-        const int nlev = nn.y;
-        int rounds = 0;
-        for (int v = 0; v < nlev; ++v) rounds += (loff[v + 1] - loff[v] + 7) >> 3;
-        for (int it = 0; it < iters; ++it)
-          for (int v = 0; v < nlev; ++v) {
-            const int e = loff[v + 1];
-            for (int base = loff[v]; base < e; base += 8) {
-              const int idx = base + slot;
-              if (idx < e) fused_contact(sc + FR * perm[idx], l, gm, nb, acc);
-              __syncwarp();
-            }
-          }
-        n_con += (unsigned long long)nn.x;
-        n_rounds += (unsigned long long)rounds * (unsigned long long)iters;
-        n_lev += (unsigned long long)nlev;
+      {
+        // the sweeps: each lane's four-lane group on its half's world
+        int itmax = 0, nlmax = 0;
+        for (int j = 0; j < WPW; ++j)
+          if (my[j].g) { itmax = max(itmax, my[j].iters); nlmax = max(nlmax, my[j].nlev); }
+        const PileGroupDev* mg = my[half].g;
+        const int my_it = mg ? my[half].iters : 0, my_nl = mg ? my[half].nlev : 0, my_nb = mg ? mg->nb : 0;
+        float* my_sc = nullptr;
+        if (mg) my_sc = mg->scr + (size_t)my[half].w * mg->sstride + ws_layout(mg->nb, mg->np, mg->maxc).sc;
+        fused_sweeps(my_sc, sh_of(half, ws.perm), sh_of(half, ws.loff), acc_of(half), my_nb, my_it, my_nl, itmax,
+                     nlmax, slot, l, gm);
       }
       if (MID) __syncthreads();  // and the sweeps
-      if (have) bad |= fused_finish(g, w, lane, acc, nn.x, s == n_steps - 1, rk4);
+      for (int j = 0; j < WPW; ++j) {
+        const PileGroupDev* g = my[j].g;
+        if (!g) continue;
+        const bool b = fused_finish(g, my[j].w, lane, acc_of(j), my[j].nact, s == n_steps - 1, my[j].rk4);
+        if (lane == 0) my[j].bad |= b;
+        __syncwarp();
+      }
       if (!MID) __syncthreads();  // one barrier per env-step
     }
-    if (have) {
+    for (int j = 0; j < WPW; ++j) {
+      const PileGroupDev* g = my[j].g;
+      if (!g) continue;
+      const int w = my[j].w;
       const WsLay L = ws_layout(g->nb, g->np, g->maxc);
       float* wf = g->scr + (size_t)w * g->sstride;
       ws_store_state(*g, w, L, wf, lane);
       ws_store_diag(*g, w, L, wf, reinterpret_cast<const int*>(wf + L.nf), lane);
       if (lane == 0) {
+        const FusedSlot& f = my[j];
         unsigned st = 0u;
-        if (overflow) st |= NEWT_WS_CONTACT_OVERFLOW;
-        if (bad) st |= NEWT_WS_NONFINITE;
+        if (f.overflow) st |= NEWT_WS_CONTACT_OVERFLOW;
+        if (f.bad) st |= NEWT_WS_NONFINITE;
         if (st) atomicOr(reinterpret_cast<unsigned*>(g->I + (size_t)w * g->lay.istride + g->lay.status), st);
-        if (cost) cost[t] = (unsigned)min(n_rounds + 64ull * n_con, 0xffffffffull);
+        if (cost) cost[f.t] = (unsigned)min(f.n_rounds + 64ull * f.n_con, 0xffffffffull);
         if (work) {
-          atomicAdd(work + 0, n_con);
-          atomicAdd(work + 1, n_rounds);
-          atomicAdd(work + 2, n_lev);
+          atomicAdd(work + 0, f.n_con);
+          atomicAdd(work + 1, f.n_rounds);
+          atomicAdd(work + 2, f.n_lev);
           atomicAdd(work + 3, 1ull);
         }
       }
@@ -551,40 +611,57 @@ __global__ void __launch_bounds__(32 * GANG, 1) pile_k_fused(const PileGroupDev*
 // host side
 // ---------------------------------------------------------------------------
 // The launch shapes the autotuner chooses among: (gang warps, barrier between
-// assembly and sweeps).
+// assembly and sweeps, worlds per warp, blocks per SM the registers are
+// sized for).  On 8192 sixteen-body piles over env-steps 125..625 the gangs
+// of 8 warps, two per SM (shape 10), run 4% faster than one gang of 12;
+// more warps per SM at 80 or 64 registers run slower (the worlds' solver
+// records no longer fit in L1), and two worlds per warp 13% slower.
 namespace {
-struct FusedShape { int gang; bool mid; };
-constexpr FusedShape kShapes[] = {{16, true}, {12, true}, {12, false}, {8, true}, {24, true}, {32, true}};
+struct FusedShape { int gang; bool mid; int wpw; int minb; };
+constexpr FusedShape kShapes[] = {{16, true, 1, 1}, {12, true, 1, 1}, {12, false, 1, 1}, {8, true, 1, 1},
+                                  {24, true, 1, 1}, {32, true, 1, 1}, {12, false, 2, 1}, {4, false, 1, 3},
+                                  {6, false, 1, 2},  {4, false, 1, 4}, {8, false, 1, 2},  {7, false, 1, 4}};
 constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 template <class F> void with_kernel(int shape, F f) {
   switch (shape) {
-    case 0: f(pile_k_fused<16, true>, 16); break;
-    case 1: f(pile_k_fused<12, true>, 12); break;
-    case 2: f(pile_k_fused<12, false>, 12); break;
-    case 3: f(pile_k_fused<8, true>, 8); break;
-    case 4: f(pile_k_fused<24, true>, 24); break;
-    default: f(pile_k_fused<32, true>, 32); break;
+    case 0: f(pile_k_fused<16, true, 1, 1>, 16, 1); break;
+    case 1: f(pile_k_fused<12, true, 1, 1>, 12, 1); break;
+    case 2: f(pile_k_fused<12, false, 1, 1>, 12, 1); break;
+    case 3: f(pile_k_fused<8, true, 1, 1>, 8, 1); break;
+    case 4: f(pile_k_fused<24, true, 1, 1>, 24, 1); break;
+    case 5: f(pile_k_fused<32, true, 1, 1>, 32, 1); break;
+    case 6: f(pile_k_fused<12, false, 2, 1>, 12, 2); break;
+    case 7: f(pile_k_fused<4, false, 1, 3>, 4, 1); break;
+    case 8: f(pile_k_fused<6, false, 1, 2>, 6, 1); break;
+    case 9: f(pile_k_fused<4, false, 1, 4>, 4, 1); break;
+    case 10: f(pile_k_fused<8, false, 1, 2>, 8, 1); break;
+    default: f(pile_k_fused<7, false, 1, 4>, 7, 1); break;
   }
 }
 }  // namespace
 
 extern "C" int newt_pile_fused_shapes() { return kNumShapes; }
 
-// Warps (worlds in flight) per block of launch shape `shape`.
+// Warps per block of launch shape `shape`.
 extern "C" int newt_pile_fused_warps_per_block(int shape) { return kShapes[shape % kNumShapes].gang; }
 
-// Dynamic shared memory of one block of `gang` warps for a table whose
-// largest world has `nbm` bodies and contact capacity `cm`.
-extern "C" size_t newt_pile_fused_smem_bytes(int gang, int nbm, int cm) {
-  return (size_t)gang * warp_smem(nbm, cm).bytes;
+// Worlds in flight per block of launch shape `shape`.
+extern "C" int newt_pile_fused_worlds_per_block(int shape) {
+  return kShapes[shape % kNumShapes].gang * kShapes[shape % kNumShapes].wpw;
+}
+
+// Dynamic shared memory of one block holding `worlds` worlds in flight for a
+// table whose largest world has `nbm` bodies and contact capacity `cm`.
+extern "C" size_t newt_pile_fused_smem_bytes(int worlds, int nbm, int cm) {
+  return (size_t)worlds * warp_smem(nbm, cm).bytes;
 }
 
 // Resident blocks per SM of launch shape `shape` for that table (outside
 // stream capture; sets the kernel's dynamic shared memory limit first).
 extern "C" int newt_pile_fused_blocks_per_sm(int shape, int nbm, int cm) {
   int b = 1;
-  with_kernel(shape, [&](auto kern, int gang) {
-    const int bytes = (int)newt_pile_fused_smem_bytes(gang, nbm, cm);
+  with_kernel(shape, [&](auto kern, int gang, int wpw) {
+    const int bytes = (int)newt_pile_fused_smem_bytes(gang * wpw, nbm, cm);
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 32 * gang, bytes) != cudaSuccess || b < 1) b = 1;
   });
@@ -596,7 +673,7 @@ extern "C" cudaError_t newt_pile_fused_prepare() {
   cudaFuncAttributes a;
   cudaError_t e = cudaFuncGetAttributes(&a, pile_k_queue_sort);
   for (int k = 0; k < kNumShapes && e == cudaSuccess; ++k)
-    with_kernel(k, [&](auto kern, int) { e = cudaFuncGetAttributes(&a, kern); });
+    with_kernel(k, [&](auto kern, int, int) { e = cudaFuncGetAttributes(&a, kern); });
   return e;
 }
 
@@ -613,9 +690,10 @@ extern "C" int newt_launch_pile_fused(const PileGroupDev* dG, const int* dwseg, 
     pile_k_queue_sort<<<1, 1024, 0, st>>>(cost, n_items, queue);
     ++launches;
   }
-  with_kernel(shape, [&](auto kern, int gang) {
-    kern<<<grid, 32 * gang, newt_pile_fused_smem_bytes(gang, nbm, cm), st>>>(dG, dwseg, ng, queue, n_items, counter,
-                                                                             n_steps, work, cost, nbm, cm);
+  with_kernel(shape, [&](auto kern, int gang, int wpw) {
+    kern<<<grid, 32 * gang, newt_pile_fused_smem_bytes(gang * wpw, nbm, cm), st>>>(dG, dwseg, ng, queue, n_items,
+                                                                                   counter, n_steps, work, cost, nbm,
+                                                                                   cm);
   });
   return launches + 1;
 }

@@ -166,9 +166,9 @@ struct newt_gpu_ctx {
   // cost-sorted queue (pile_fused.cu), 0 = the island-class pipeline per
   // env-step; the persistent launch's shape (gang size and barriers, an
   // index into pile_fused.cu's shape table) and grid in percent of full
-  // residency (default: gangs of 12 warps meeting once per env-step, the
-  // fastest shape on settled 16-body piles)
-  int tune_pile_fused = 1, tune_fused_shape = 2, tune_fused_pct = 100;
+  // residency (default: gangs of 8 warps, two per SM, meeting once per
+  // env-step, the fastest shape on 8192 sixteen-body piles)
+  int tune_pile_fused = 1, tune_fused_shape = 10, tune_fused_pct = 100;
   // the persistent launch of the captured graph: its timing events (external
   // records when profiling), its work counters (device: contacts, rounds,
   // levels, worlds) and whether the graph holds one; `last_fused` tells the

@@ -30,7 +30,7 @@ extern "C" int newt_launch_pile_step(const PileGroupDev* dG, const int* dwseg, i
                                      const cudaStream_t* side, cudaEvent_t* ev, cudaEvent_t* kev);
 extern "C" void newt_pile_init();
 extern "C" int newt_pile_fused_blocks_per_sm(int shape, int nbm, int cm);
-extern "C" int newt_pile_fused_warps_per_block(int shape);
+extern "C" int newt_pile_fused_worlds_per_block(int shape);
 extern "C" int newt_launch_pile_fused(const PileGroupDev* dG, const int* dwseg, int ng, int* queue, int n_items,
                                       int* counter, int n_steps, int grid, unsigned long long* work, unsigned* cost,
                                       int nbm, int cm, int shape, cudaStream_t st);
@@ -312,7 +312,7 @@ static int capture(newt_gpu_ctx* ctx, int n_steps) {
     if (!ctx->fkev[0])
       for (int k = 0; k < 2; ++k) CKS(cudaEventCreate(&ctx->fkev[k]));
     for (HostGroup* g : piles) { fnbm = std::max(fnbm, g->size); fcm = std::max(fcm, g->maxc); }
-    const int wpb = newt_pile_fused_warps_per_block(ctx->tune_fused_shape);
+    const int wpb = newt_pile_fused_worlds_per_block(ctx->tune_fused_shape);
     const int full = newt_pile_fused_blocks_per_sm(ctx->tune_fused_shape, fnbm, fcm) * sm_count(ctx);
     fgrid = std::min((ft.worlds + wpb - 1) / wpb, std::max(1, full * ctx->tune_fused_pct / 100));
   }
@@ -462,14 +462,16 @@ int autotune_batched(newt_gpu_ctx* ctx, int n_steps, int horizon, int32_t* choic
       CKS(cudaMemcpyAsync(live[i].first, snap[k][i], live[i].second, cudaMemcpyDeviceToDevice, ctx->stream));
     return NEWT_OK;
   };
-  // piles: the persistent launch in each gang shape (warps per block, and
-  // whether the gang also meets between assembly and sweeps), or the
+  // piles: the persistent launch in each gang shape (warps per block,
+  // blocks per SM, whether the gang also meets between assembly and sweeps,
+  // one or two worlds per warp), or the
   // island-class pipeline with 1, 2 or 3 world-range branches; trees: full
   // or half persistent grid
   struct Cand { int fused, shape, branches, grid_pct; };
-  const Cand cands[] = {{1, 0, 0, 100}, {1, 1, 0, 100}, {1, 2, 0, 100}, {1, 3, 0, 100}, {1, 4, 0, 100},
-                        {1, 5, 0, 100}, {0, 0, 1, 100}, {0, 0, 2, 100}, {0, 0, 3, 100}, {1, 1, 0, 50},
-                        {0, 0, 2, 50}};
+  const Cand cands[] = {{1, 0, 0, 100},  {1, 1, 0, 100}, {1, 2, 0, 100}, {1, 3, 0, 100}, {1, 4, 0, 100},
+                        {1, 5, 0, 100},  {1, 6, 0, 100}, {1, 7, 0, 100}, {1, 8, 0, 100}, {1, 9, 0, 100},
+                        {1, 10, 0, 100}, {1, 11, 0, 100}, {0, 0, 1, 100}, {0, 0, 2, 100}, {0, 0, 3, 100},
+                        {1, 10, 0, 50},  {0, 0, 2, 50}};
   const Cand start{ctx->tune_pile_fused, ctx->tune_fused_shape, ctx->tune_branches, ctx->tune_tree_grid_pct};
   auto set = [&](const Cand& c) {
     ctx->tune_pile_fused = c.fused;
