@@ -130,7 +130,8 @@ typedef struct newt_model_desc {     /* one world's model: at most one tree */
   float gravity[3];
   int32_t solver;                    /* NEWT_SOLVER_PGS | NEWT_SOLVER_NEWTON */
   int32_t iterations;                /* PGS sweeps / Newton iteration cap */
-  int32_t tree_self_collision;       /* 0: in-tree geom pairs are skipped */
+  int32_t tree_self_collision;       /* nonzero (newt's default, world.rs:340): geoms on different links of
+                                      * the tree collide; 0: those pairs are skipped */
   int32_t integrator;                /* NEWT_INTEGRATOR_*: World::integrator (newt/src/world.rs:76-84) */
   int32_t cone;                      /* NEWT_CONE_*: SolverConfig::cone (newt/src/solver.rs:75-110);
                                       * elliptic on pile worlds under PGS */

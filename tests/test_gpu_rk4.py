@@ -9,9 +9,9 @@ solved once per step and held over the RK4 stages).  The stack is chaotic (the
 FP64 oracle and newt's f32 run drift 2 cm apart by step 200), so it is held
 to one-step parity from newt's own snapshots and to that FP64 window over 1000
 steps.  Tree-contact worlds hold the joint solve's generalised force over
-the stages; newt's own tree-contact goldens (solver_tree.bin) need in-tree
-box pairs, which the GPU path does not collide, so those run against the FP64
-oracle's RK4, itself byte-identical to newt on them."""
+the stages, here against the FP64 oracle's RK4; newt's own tree-contact
+goldens (solver_tree.bin, solver_newton_tree.bin, with their in-tree box
+pair) are held on the GPU in tests/test_gpu_intree.py."""
 import numpy as np
 import pytest
 

@@ -247,8 +247,9 @@ int* HostGroup::release_index(int idx) {
 // group, fixed by its first model (the topology key makes them uniform).
 void HostGroup::setup_tc(const HostModel& m) {
   ng = m.n_geoms;
-  // (static, link geom) pairs in newt's auto_pairs order with its filter
-  // (world.rs:1042-1069); link-link pairs are refused at upload
+  // (static, link geom) pairs and, with the tree's self-collision on, the
+  // pairs of geoms on different links, in newt's auto_pairs order with its
+  // filter (world.rs:1042-1069)
   gtopo.assign(3 * ng, 0);
   for (int k = 0; k < ng; ++k) {
     gtopo[2 * k] = m.geoms[k].shape;
@@ -260,10 +261,17 @@ void HostGroup::setup_tc(const HostModel& m) {
   for (int a = 0; a < ng; ++a)
     for (int b = a + 1; b < ng; ++b) {
       const newt_geom_desc &A = m.geoms[a], &B = m.geoms[b];
-      if ((A.link < 0) == (B.link < 0)) continue;
+      if (A.link < 0 && B.link < 0) continue;
+      const bool in_tree = A.link >= 0 && B.link >= 0;
+      if (in_tree && (!m.self_coll || A.link == B.link)) continue;
       if (!((A.group & B.mask) != 0u && (B.group & A.mask) != 0u)) continue;
       gpairs.push_back(a);
       gpairs.push_back(b);
+      if (in_tree) {  // box-box up to four contacts, capsule-capsule two, sphere pairs one
+        maxc += (A.shape == NEWT_SHAPE_BOX && B.shape == NEWT_SHAPE_BOX) ? 4
+              : (A.shape == NEWT_SHAPE_CAPSULE && B.shape == NEWT_SHAPE_CAPSULE) ? 2 : 1;
+        continue;
+      }
       const int shape = A.link >= 0 ? A.shape : B.shape;
       maxc += (shape == NEWT_SHAPE_BOX || shape == NEWT_SHAPE_CYLINDER) ? 4 : (shape == NEWT_SHAPE_CAPSULE ? 2 : 1);
     }

@@ -76,12 +76,38 @@ using dense::warp_sumd;
 constexpr int TC_WARPS = 1;  // warps (worlds) per block
 constexpr int CREC = 24;     // floats per contact record
 // contact record fields
+// K_LINK: the link of the row's tree side with sign K_SIGN; K_LINK2: for an
+// in-tree pair, the link of side b (sign -1), else -1
 enum { K_GA = 0, K_GB = 1, K_LINK = 2, K_SIGN = 3, K_POS = 4, K_N = 7, K_PEN = 10, K_GAP = 11, K_MU = 12,
-       K_SR = 13, K_SI = 15, K_CONDIM = 20, K_ROW = 21 };
+       K_SR = 13, K_SI = 15, K_CONDIM = 20, K_ROW = 21, K_LINK2 = 22 };
 constexpr int GREC = 21;  // SoA geom model rows: size3 pos3 quat4 fric margin gap solref2 solimp5
 enum { G_SIZE = 0, G_POS = 3, G_QUAT = 6, G_FRIC = 10, G_MARGIN = 11, G_GAP = 12, G_SR = 13, G_SI = 15 };
 enum { JF = 0, JX = 1, JH = 2, JS = 3 };
 
+
+// In-tree pairs (geoms on two links of the tree): newt's routine for the
+// shape pair as (A, B), else as (B, A) with *flip set (the caller relabels,
+// newt/src/contact.rs:2561-2586).  Sizes `za`, `zb`: radius / half extents /
+// radius and half height.  Out of line: the solve kernel's registers stay
+// sized for its own loops.
+static __device__ __noinline__ int np_link_pair(int sa, int sb, GPose pa, GPose pb, V3 za, V3 zb, float margin,
+                                                CRes* res, bool* flip) {
+  *flip = false;
+  if (sa == NEWT_SHAPE_SPHERE && sb == NEWT_SHAPE_SPHERE) return np_sphere_sphere(pa.p, za.x, pb.p, zb.x, margin, res);
+  if (sa == NEWT_SHAPE_BOX && sb == NEWT_SHAPE_BOX) return np_box_box(pa, za, pb, zb, margin, res);
+  if (sa == NEWT_SHAPE_SPHERE && sb == NEWT_SHAPE_BOX) return np_sphere_box(pa, za.x, pb, zb, margin, res);
+  if (sa == NEWT_SHAPE_SPHERE && sb == NEWT_SHAPE_CAPSULE) return np_sphere_capsule(pa.p, za.x, pb, zb.x, zb.y, margin, res);
+  if (sa == NEWT_SHAPE_SPHERE && sb == NEWT_SHAPE_CYLINDER)
+    return np_sphere_cylinder(pa.p, za.x, pb, zb.x, zb.y, margin, res);
+  if (sa == NEWT_SHAPE_CAPSULE && sb == NEWT_SHAPE_CAPSULE)
+    return np_capsule_capsule(pa, za.x, za.y, pb, zb.x, zb.y, margin, res);
+  *flip = true;
+  if (sb == NEWT_SHAPE_SPHERE && sa == NEWT_SHAPE_BOX) return np_sphere_box(pb, zb.x, pa, za, margin, res);
+  if (sb == NEWT_SHAPE_SPHERE && sa == NEWT_SHAPE_CAPSULE) return np_sphere_capsule(pb.p, zb.x, pa, za.x, za.y, margin, res);
+  if (sb == NEWT_SHAPE_SPHERE && sa == NEWT_SHAPE_CYLINDER)
+    return np_sphere_cylinder(pb.p, zb.x, pa, za.x, za.y, margin, res);
+  return 0;  // refused at upload
+}
 
 NEWT_D Q4 q_axis_angle(V3 axis, float angle) {  // math.rs:574-580
   const float l = sqrtf(len2(axis));
@@ -371,17 +397,40 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   }
   __syncwarp();
 
-  // ---- link-plane contacts in newt's pair order: lane per pair, a warp scan
+  // ---- contacts in newt's pair order (link-plane pairs, and in-tree pairs
+  //      when the tree collides with itself): lane per pair, a warp scan
   //      places each pair's contacts ----
   float* con = wf + lay.con;
   int ncon = 0;
   bool overflow = false;
+  auto link_geom_pose = [&](int gi) {
+    const float* lp = pose + 7 * G.gtopo[2 * gi + 1];
+    const Q4 lo = Q4{lp[3], lp[4], lp[5], lp[6]};
+    GPose gp;
+    gp.p = ldv3(lp) + qrot(lo, v3(gv(gi, G_POS), gv(gi, G_POS + 1), gv(gi, G_POS + 2)));
+    gp.q = qmul(lo, Q4{gv(gi, G_QUAT), gv(gi, G_QUAT + 1), gv(gi, G_QUAT + 2), gv(gi, G_QUAT + 3)});
+    return gp;
+  };
   for (int base = 0; base < G.npairs; base += 32) {
     const int pi = base + lane;
     CRes cr[4];
-    int nc = 0, a = 0, b = 0, link = 0;
-    bool a_static = false;
-    if (pi < G.npairs) {
+    int nc = 0, a = 0, b = 0, link = 0, link2 = -1;
+    bool a_static = false, flip = false;
+    if (pi < G.npairs && G.gtopo[2 * G.pairs[2 * pi] + 1] >= 0 && G.gtopo[2 * G.pairs[2 * pi + 1] + 1] >= 0) {
+      // in-tree pair: side a (+1) and side b (-1) both on the tree
+      a = G.pairs[2 * pi];
+      b = G.pairs[2 * pi + 1];
+      link = G.gtopo[2 * a + 1];
+      link2 = G.gtopo[2 * b + 1];
+      const float margin = fmaxf(gv(a, G_MARGIN), gv(b, G_MARGIN));
+      CRes ct[4];  // its own buffer: `cr` stays in registers on the link-plane path
+      nc = np_link_pair(G.gtopo[2 * a], G.gtopo[2 * b], link_geom_pose(a), link_geom_pose(b),
+                        v3(gv(a, G_SIZE), gv(a, G_SIZE + 1), gv(a, G_SIZE + 2)),
+                        v3(gv(b, G_SIZE), gv(b, G_SIZE + 1), gv(b, G_SIZE + 2)), margin, ct, &flip);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (k < nc) cr[k] = ct[k];
+    } else if (pi < G.npairs) {
       a = G.pairs[2 * pi];
       b = G.pairs[2 * pi + 1];
       a_static = G.gtopo[2 * a + 1] < 0;
@@ -423,9 +472,10 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
       c[K_GA] = __int_as_float(a);
       c[K_GB] = __int_as_float(b);
       c[K_LINK] = __int_as_float(link);
+      c[K_LINK2] = __int_as_float(link2);
       c[K_SIGN] = a_static ? -1.f : 1.f;
       stv3(c + K_POS, cr[k].pos);
-      stv3(c + K_N, a_static ? -cr[k].n : cr[k].n);
+      stv3(c + K_N, (a_static || flip) ? -cr[k].n : cr[k].n);
       c[K_PEN] = cr[k].pen;
       c[K_GAP] = fmaxf(gv(a, G_GAP), gv(b, G_GAP));
       c[K_MU] = fminf(gv(a, G_FRIC), gv(b, G_FRIC));
@@ -589,8 +639,9 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   __syncwarp();
   for (int r = lane; r < nr; r += 32) {
     const float* cc = con + CREC * rcon[r];
-    const int link = __float_as_int(cc[K_LINK]);
+    const int link = __float_as_int(cc[K_LINK]), link2 = __float_as_int(cc[K_LINK2]);
     tw[link] = 1.f;
+    if (link2 >= 0) tw[link2] = 1.f;
     const float sign = cc[K_SIGN], mu = cc[K_MU];
     const V3 n = ldv3(cc + K_N), pt = ldv3(cc + K_POS);
     V3 dir = n;
@@ -604,6 +655,8 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
     }
     for (int k = 0; k < nv; ++k) Jt[(size_t)k * ldj + r] = 0.f;
     chain_columns(g, w, pose, link, pt, [&](int k, V3, V3 tr) { Jt[(size_t)k * ldj + r] = dot(tr, dir) * sign; });
+    if (link2 >= 0)  // side b of an in-tree pair: the columns its chain shares with side a's take both
+      chain_columns(g, w, pose, link2, pt, [&](int k, V3, V3 tr) { Jt[(size_t)k * ldj + r] -= dot(tr, dir); });
     float vel = 0.f, vfree = 0.f;
     for (int k = 0; k < nv; ++k) {
       const float jk = Jt[(size_t)k * ldj + r];
@@ -664,7 +717,8 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
     const Soft s{cc[K_SR], cc[K_SR + 1], cc[K_SI], cc[K_SI + 1], cc[K_SI + 2], cc[K_SI + 3], (int)cc[K_SI + 4]};
     const float d = impedance_at(-pen, s);
     const bool pyr = rfac[r] >= 0;
-    const float twl = tw[__float_as_int(cc[K_LINK])];
+    const int link2 = __float_as_int(cc[K_LINK2]);  // tree_contact_diag_approx sums both tree sides
+    const float twl = tw[__float_as_int(cc[K_LINK])] + (link2 >= 0 ? tw[link2] : 0.f);
     const float base = (1.f - d) / d * (pyr ? twl * (1.f + mu * mu) : twl);
     const float reg = pyr ? 2.f * mu * mu * base : base;
     vreg[r] = reg;

@@ -149,7 +149,6 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
   if (d.n_links > 0 && d.n_bodies == 0 && d.n_geoms > 0) {
     // one tree whose link geoms (spheres, boxes, capsules) touch static planes
     if (d.n_links > 64) return fail(ctx, NEWT_E_INVALID, "tree-contact worlds have at most 64 links");
-    int nlink_geoms = 0;
     for (int k = 0; k < d.n_geoms; ++k) {
       const newt_geom_desc& G = d.geoms[k];
       if (G.body >= 0) return fail(ctx, NEWT_E_INVALID, "body geom in a world without free bodies");
@@ -158,7 +157,6 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
         if (G.shape < NEWT_SHAPE_SPHERE || G.shape > NEWT_SHAPE_ELLIPSOID)
           return fail(ctx, NEWT_E_UNSUPPORTED_PAIR,
                       "link geoms must be spheres, boxes, capsules, cylinders or ellipsoids on the GPU path");
-        ++nlink_geoms;
       } else if (G.shape != NEWT_SHAPE_PLANE) {
         return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "static geoms must be planes");
       }
@@ -167,8 +165,24 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
     }
     if (d.cone != NEWT_CONE_PYRAMIDAL)
       return fail(ctx, NEWT_E_INVALID, "tree-contact worlds take the pyramidal cone on the GPU path");
-    if (d.tree_self_collision && nlink_geoms > 1)
-      return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "in-tree geom pairs are not on the GPU path (disable tree self-collision)");
+    // in-tree pairs (newt collides geoms of different links of one tree unless
+    // its self-collision is off, world.rs:340, 1042-1069): the shape pairs
+    // newt has a routine for, as on pile worlds, plus sphere-box
+    if (d.tree_self_collision)
+      for (int i = 0; i < d.n_geoms; ++i)
+        for (int j = i + 1; j < d.n_geoms; ++j) {
+          const newt_geom_desc &A = d.geoms[i], &B = d.geoms[j];
+          if (A.link < 0 || B.link < 0 || A.link == B.link) continue;
+          if (!((A.group & B.mask) != 0u && (B.group & A.mask) != 0u)) continue;
+          const int lo = std::min(A.shape, B.shape), hi = std::max(A.shape, B.shape);
+          const bool ok = (lo == NEWT_SHAPE_SPHERE && hi <= NEWT_SHAPE_CYLINDER) ||
+                          (lo == NEWT_SHAPE_BOX && hi == NEWT_SHAPE_BOX) ||
+                          (lo == NEWT_SHAPE_CAPSULE && hi == NEWT_SHAPE_CAPSULE);
+          if (!ok)
+            return fail(ctx, NEWT_E_UNSUPPORTED_PAIR,
+                        "in-tree pairs on the GPU path: sphere with sphere, box, capsule or cylinder, box-box, "
+                        "capsule-capsule (filter the others or disable tree self-collision)");
+        }
     if (d.solver != NEWT_SOLVER_PGS && d.solver != NEWT_SOLVER_NEWTON)
       return fail(ctx, NEWT_E_INVALID, "tree-contact worlds need the PGS or Newton solver");
     m.kind = GK_TREE_CONTACT; m.size = d.n_links;

@@ -35,7 +35,9 @@ struct HostModel {
     std::string k;
     for (auto& l : links) { k += std::to_string(l.parent); k += ':'; k += std::to_string(l.joint); k += ','; }
     if (kind == GK_TREE_CONTACT) {
-      // shapes, attachments, condim and filters fix the pair list and the rows
+      // shapes, attachments, condim, filters and in-tree collision fix the
+      // pair list and the rows
+      k += self_coll ? "s" : "n";
       for (auto& gd : geoms) {
         k += 'g'; k += std::to_string(gd.shape); k += '@'; k += std::to_string(gd.link);
         k += 'c'; k += std::to_string(gd.condim); k += 'f'; k += std::to_string(gd.group); k += '/';
