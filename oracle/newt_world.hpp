@@ -9,7 +9,8 @@
 //   newt/src/contact.rs:269-470      sphere_plane, box_plane, capsule_plane, sphere_sphere
 //   newt/src/contact.rs:569-1247     box_box_full_manifold (SAT + face clipping)
 //   newt/src/contact.rs:473-505      sphere_capsule; :1249-1272 capsule_capsule
-//   newt/src/contact.rs:1296-1426    cylinder_plane, ellipsoid_plane; :1519-1628 sphere_cylinder
+//   newt/src/contact.rs:1296-1426    cylinder_plane, ellipsoid_plane; :1519-1628 sphere_cylinder;
+//                                    :1630-1725 sphere_ellipsoid
 //   newt/src/contact.rs:2313-2387    closest_point_on_segment, closest_points_on_segments
 //   newt/src/contact.rs:2509-2587    dispatch / swap rule
 //   newt/src/world.rs:1042-1069      auto_pairs (naive pair set; broadphase-independent contacts)
@@ -319,6 +320,52 @@ template <class R> CBuf<R> sphere_cylinder(int is, const Pose<R>& sp, R rs, int 
   return out;
 }
 
+// contact.rs:1630-1725 sphere_ellipsoid: the closest point q of the
+// ellipsoid surface to the sphere centre p (ellipsoid frame) from twelve
+// Newton steps, starting at t = 0, on the Lagrange parameter t of
+// q = (a^2 p.x / (a^2 + t), b^2 p.y / (b^2 + t), c^2 p.z / (c^2 + t)) with
+// f(t) = sum (a_k p_k / (a_k^2 + t))^2 - 1 (a zero denominator nudges t by
+// 1e-6 (a_k^2 + 1) and spends the step); the normal (p - q) / |p - q| from
+// the ellipsoid into the sphere, the contact point midway between q and the
+// sphere's surface along it; nothing when the centre is farther than
+// r + margin + the largest semi-axis + 1
+template <class R> CBuf<R> sphere_ellipsoid(int is, const Pose<R>& sp, R rs, int ie, const Pose<R>& ep, Vec3<R> ax, R fr, R margin, R gap) {
+  CBuf<R> out;
+  const Vec3<R> p = ep.o.inverse_rotate(sp.p - ep.p);
+  const R a = ax.x, b = ax.y, c = ax.z;
+  const R mx = a > b ? (a > c ? a : c) : (b > c ? b : c);
+  if (p.length() > rs + margin + mx + R(1)) return out;
+  const R ap[3] = {a * p.x, b * p.y, c * p.z};
+  const R a2[3] = {a * a, b * b, c * c};
+  R t = R(0);
+  for (int it = 0; it < 12; ++it) {
+    R f = R(-1), fp = R(0);
+    bool nudged = false;
+    for (int k = 0; k < 3 && !nudged; ++k) {
+      const R den = a2[k] + t;
+      if (den == R(0)) { t += R(1.0e-6) * (a2[k] + R(1)); nudged = true; break; }
+      const R inv = R(1) / den;
+      const R num = ap[k] * inv;
+      f += num * num;
+      fp += R(-2) * ap[k] * ap[k] * inv * inv * inv;
+    }
+    if (nudged) continue;
+    if (fp == R(0)) break;
+    t -= f / fp;
+  }
+  const Vec3<R> q(a2[0] * p.x / (a2[0] + t), a2[1] * p.y / (a2[1] + t), a2[2] * p.z / (a2[2] + t));
+  const Vec3<R> d = p - q;
+  const R dist = d.length();
+  const R pen = rs - dist + margin;
+  if (pen <= R(0)) return out;
+  const Vec3<R> nl = dist > R(1.0e-9) ? d / dist : Vec3<R>(0, 0, 1);
+  const Vec3<R> nw = ep.o.rotate(nl);
+  const Vec3<R> surf = ep.p + ep.o.rotate(q);
+  const Vec3<R> ssurf = sp.p - nw * rs;
+  out.push({is, ie, (surf + ssurf) * R(0.5), nw, pen, fr, gap});
+  return out;
+}
+
 // contact.rs:2313-2321 closest_point_on_segment
 template <class R> Vec3<R> closest_point_on_segment(Vec3<R> p, Vec3<R> a, Vec3<R> b) {
   Vec3<R> ab = b - a;
@@ -510,6 +557,10 @@ template <class R> bool try_np(int ia, const Geom<R>& a, const Pose<R>& pa, int 
   }
   if (a.shape == S_SPHERE && b.shape == S_CAPSULE) {
     *out = sphere_capsule(ia, pa, a.size[0], ib, pb, b.size[0], b.size[1], fr, margin, gap);
+    return true;
+  }
+  if (a.shape == S_SPHERE && b.shape == S_ELLIPSOID) {
+    *out = sphere_ellipsoid(ia, pa, a.size[0], ib, pb, Vec3<R>(b.size[0], b.size[1], b.size[2]), fr, margin, gap);
     return true;
   }
   if (a.shape == S_CAPSULE && b.shape == S_CAPSULE) {

@@ -1,5 +1,6 @@
-"""Known-answer checks of the oracle's cylinder-plane and ellipsoid-plane
-contacts (CPU only; newt/src/contact.rs:1296-1426).
+"""Known-answer checks of the oracle's cylinder-plane, ellipsoid-plane,
+sphere-cylinder and sphere-ellipsoid contacts (CPU only;
+newt/src/contact.rs:1296-1426, 1519-1725).
 
 Cylinder: an upright cylinder sunk by d gives four contacts of depth d, the
 bottom cap centre and the bottom rim at 0, 45 and 90 degrees (newt's tie
@@ -7,9 +8,16 @@ order); for random poses the contacts equal an independent evaluation of
 newt's rule (18 samples, the four deepest with penetration > 0, projected
 onto the plane).  Ellipsoid: the penetration equals the depth of the
 deepest surface point found by a dense search over the surface, and the
-contact lies midway between that point and the plane.
+contact lies midway between that point and the plane.  Sphere-ellipsoid:
+newt's anchors (contacts_geoms_v1.rs:1414-1446, 1470-1500: depth 0.1 within
+1e-6, normal +X, point (0.45, 0, 0) within 2e-3) in either geom order, and
+for sphere centres outside the ellipsoid the penetration, normal and point
+against the nearest surface point from a bisection on the Lagrange
+parameter in double (an independent solve): within 1e-6 (FP64) and 2e-5
+(f32, newt's arithmetic).
 """
 import numpy as np
+import pytest
 
 import oracle_py
 from tooling_gb300 import model as M
@@ -147,4 +155,82 @@ def test_sphere_cylinder_matches_signed_distance():
         assert len(pairs) == 1 and tuple(pairs[0]) == (0, 1)
         assert abs(data[0, 6] - pen) < 1e-8, (data[0, 6], pen)
         assert abs(np.linalg.norm(data[0, 3:6]) - 1.0) < 1e-9
+    assert hits > 60
+
+
+def _sphere_ellipsoid(rs, sp, ax, ep, eq, ell_first=False, precision=1):
+    w = M.WorldModel(dt=2e-3, gravity=(0.0, 0.0, -9.81), solver=M.SOLVER_PGS, iterations=20)
+    a = w.add_body(1.0, M._diag9(0.01, 0.01, 0.01))
+    b = w.add_body(1.0, M._diag9(0.01, 0.01, 0.01))
+    gs = M.Geom(shape=M.SHAPE_SPHERE, body=a, size=(rs, 0.0, 0.0))
+    ge = M.Geom(shape=M.SHAPE_ELLIPSOID, body=b, size=tuple(float(x) for x in ax))
+    for g in ((ge, gs) if ell_first else (gs, ge)):
+        w.add_geom(g)
+    qpos = np.concatenate([sp, [1.0, 0.0, 0.0, 0.0], ep, eq]).astype(np.float32)
+    return oracle_py.contacts(M.PackedModels([w]), 0, qpos, np.zeros(12, np.float32), precision=precision), qpos
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("ell_first", [False, True])
+def test_sphere_ellipsoid_anchor(precision, ell_first):
+    (pairs, data), _ = _sphere_ellipsoid(0.2, (0.6, 0.0, 0.0), (0.5, 0.3, 0.2), (0.0, 0.0, 0.0), (1.0, 0.0, 0.0, 0.0),
+                                         ell_first, precision)
+    assert len(pairs) == 1
+    sgn = -1.0 if ell_first else 1.0  # newt relabels (B, A) pairs with the normal flipped
+    assert tuple(pairs[0]) == (0, 1)
+    assert abs(data[0, 6] - 0.1) < 1e-6
+    assert np.abs(data[0, 3:6] - sgn * np.array([1.0, 0.0, 0.0])).max() < 1e-6
+    assert np.abs(data[0, 0:3] - np.array([0.45, 0.0, 0.0])).max() < 2e-3
+
+
+def _nearest_on_ellipsoid(p, a):
+    """The surface point nearest an outside point p by bisection on the
+    Lagrange parameter t of q = a^2 p / (a^2 + t) (f(t) = sum (a p / (a^2 +
+    t))^2 - 1 falls from f(0) > 0 to -1), in double: an independent solve of
+    the problem newt's twelve Newton steps address."""
+    f = lambda t: ((a * p / (a * a + t)) ** 2).sum() - 1.0
+    lo, hi = 0.0, 1.0
+    while f(hi) > 0.0:
+        hi *= 2.0
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        lo, hi = (mid, hi) if f(mid) > 0.0 else (lo, mid)
+    return a * a * p / (a * a + lo)
+
+
+@pytest.mark.parametrize("precision,ptol,ntol", [(1, 1e-6, 1e-4), (0, 2e-5, 1e-3)])
+def test_sphere_ellipsoid_matches_nearest_point(precision, ptol, ntol):
+    rng = np.random.default_rng(21)
+    hits = 0
+    for _ in range(300):
+        ax = rng.uniform(0.08, 0.3, 3)
+        rs = rng.uniform(0.05, 0.15)
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        ep = rng.uniform(-0.2, 0.2, 3)
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        sp = ep + d * (ax.min() + (ax.max() - ax.min() + rs) * rng.uniform(0.0, 1.2))
+        (pairs, data), qpos = _sphere_ellipsoid(rs, sp, ax, ep, q, precision=precision)
+        Rm = _rotmat(qpos[10:14].astype(np.float64) / np.linalg.norm(qpos[10:14].astype(np.float64)))
+        a32 = np.array([float(np.float32(x)) for x in ax])
+        p = Rm.T @ (qpos[0:3].astype(np.float64) - qpos[7:10].astype(np.float64))
+        if ((p / a32) ** 2).sum() <= 1.0:
+            continue  # newt's solver addresses centres outside the ellipsoid
+        qn = _nearest_on_ellipsoid(p, a32)
+        dist = np.linalg.norm(p - qn)
+        pen = float(np.float32(rs)) - dist
+        if abs(pen) < 1e-5:
+            continue
+        if pen < 0:
+            assert len(pairs) == 0
+            continue
+        hits += 1
+        assert len(pairs) == 1 and tuple(pairs[0]) == (0, 1)
+        assert abs(data[0, 6] - pen) < ptol, (data[0, 6], pen)
+        nrm = Rm @ ((p - qn) / dist)
+        assert np.abs(data[0, 3:6] - nrm).max() < ntol
+        surf = qpos[7:10].astype(np.float64) + Rm @ qn
+        mid = 0.5 * (surf + (qpos[0:3].astype(np.float64) - nrm * float(np.float32(rs))))
+        assert np.abs(data[0, 0:3] - mid).max() < 10 * ptol
     assert hits > 60

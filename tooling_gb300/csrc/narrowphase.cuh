@@ -14,6 +14,7 @@
 //   cylinder_plane newt/src/contact.rs:1296-1373
 //   sphere_cylinder newt/src/contact.rs:1519-1628
 //   ellipsoid_plane newt/src/contact.rs:1381-1426
+//   sphere_ellipsoid newt/src/contact.rs:1630-1725
 //   sphere_box     extension (newt defers this pair, contact.rs:236-257):
 //                  closed-form closest point on the oriented box
 #pragma once
@@ -236,6 +237,48 @@ NEWT_D int np_sphere_cylinder(V3 cs, float rs, const GPose& c, float rc, float h
   if (!(pen > 0.f)) return 0;
   const V3 nl = dist > 1.0e-9f ? (inside ? dl * (-1.f / dist) : dl * (1.f / dist)) : v3(0.f, 0.f, 1.f);
   out[0] = CRes{c.p + qrot(c.q, cl), qrot(c.q, nl), pen};
+  return 1;
+}
+
+// Sphere (A) vs ellipsoid (B, semi-axes ax): the closest point q of the
+// ellipsoid surface to the sphere centre p (ellipsoid frame) from twelve
+// Newton steps from t = 0 on the Lagrange parameter t of
+// q_k = ax_k^2 p_k / (ax_k^2 + t), f(t) = sum (ax_k p_k / (ax_k^2 + t))^2 - 1
+// (a zero denominator nudges t and spends the step); normal (p - q) / |p - q|
+// into the sphere, the contact point midway between q and the sphere's
+// surface (contact.rs:1630-1725).
+NEWT_D int np_sphere_ellipsoid(V3 cs, float rs, const GPose& e, V3 ax, float margin, CRes* out) {
+  const V3 p = qrot_inv(e.q, cs - e.p);
+  const float mx = ax.x > ax.y ? (ax.x > ax.z ? ax.x : ax.z) : (ax.y > ax.z ? ax.y : ax.z);
+  if (sqrtf(len2(p)) > rs + margin + mx + 1.f) return 0;
+  const float ap[3] = {ax.x * p.x, ax.y * p.y, ax.z * p.z};
+  const float a2[3] = {ax.x * ax.x, ax.y * ax.y, ax.z * ax.z};
+  float t = 0.f;
+  for (int it = 0; it < 12; ++it) {
+    float f = -1.f, fp = 0.f;
+    bool nudged = false;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      if (nudged) continue;
+      const float den = a2[k] + t;
+      if (den == 0.f) { t += 1.0e-6f * (a2[k] + 1.f); nudged = true; continue; }
+      const float inv = 1.f / den;
+      const float num = ap[k] * inv;
+      f += num * num;
+      fp += -2.f * ap[k] * ap[k] * inv * inv * inv;
+    }
+    if (nudged) continue;
+    if (fp == 0.f) break;
+    t -= f / fp;
+  }
+  const V3 q = v3(a2[0] * p.x / (a2[0] + t), a2[1] * p.y / (a2[1] + t), a2[2] * p.z / (a2[2] + t));
+  const V3 d = p - q;
+  const float dist = sqrtf(len2(d));
+  const float pen = rs - dist + margin;
+  if (!(pen > 0.f)) return 0;
+  const V3 nl = dist > 1.0e-9f ? d / dist : v3(0.f, 0.f, 1.f);
+  const V3 nw = qrot(e.q, nl);
+  out[0] = CRes{((e.p + qrot(e.q, q)) + (cs - nw * rs)) * 0.5f, nw, pen};
   return 1;
 }
 

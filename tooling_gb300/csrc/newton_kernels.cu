@@ -101,11 +101,13 @@ static __device__ __noinline__ int np_link_pair(int sa, int sb, GPose pa, GPose 
     return np_sphere_cylinder(pa.p, za.x, pb, zb.x, zb.y, margin, res);
   if (sa == NEWT_SHAPE_CAPSULE && sb == NEWT_SHAPE_CAPSULE)
     return np_capsule_capsule(pa, za.x, za.y, pb, zb.x, zb.y, margin, res);
+  if (sa == NEWT_SHAPE_SPHERE && sb == NEWT_SHAPE_ELLIPSOID) return np_sphere_ellipsoid(pa.p, za.x, pb, zb, margin, res);
   *flip = true;
   if (sb == NEWT_SHAPE_SPHERE && sa == NEWT_SHAPE_BOX) return np_sphere_box(pb, zb.x, pa, za, margin, res);
   if (sb == NEWT_SHAPE_SPHERE && sa == NEWT_SHAPE_CAPSULE) return np_sphere_capsule(pb.p, zb.x, pa, za.x, za.y, margin, res);
   if (sb == NEWT_SHAPE_SPHERE && sa == NEWT_SHAPE_CYLINDER)
     return np_sphere_cylinder(pb.p, zb.x, pa, za.x, za.y, margin, res);
+  if (sb == NEWT_SHAPE_SPHERE && sa == NEWT_SHAPE_ELLIPSOID) return np_sphere_ellipsoid(pb.p, zb.x, pa, za, margin, res);
   return 0;  // refused at upload
 }
 

@@ -154,12 +154,14 @@ static __device__ __noinline__ int np_round_pair(int sa, int sb, GPose pa, GPose
   if (sa == SH_SPHERE && sb == SH_CYLINDER) return np_sphere_cylinder(pa.p, za[0], pb, zb[0], zb[1], margin, res);
   if (sa == SH_SPHERE && sb == SH_CAPSULE) return np_sphere_capsule(pa.p, za[0], pb, zb[0], zb[1], margin, res);
   if (sa == SH_CAPSULE && sb == SH_CAPSULE) return np_capsule_capsule(pa, za[0], za[1], pb, zb[0], zb[1], margin, res);
+  if (sa == SH_SPHERE && sb == SH_ELLIPSOID) return np_sphere_ellipsoid(pa.p, za[0], pb, v3(zb[0], zb[1], zb[2]), margin, res);
   *flip = true;
   if (sb == SH_CAPSULE && sa == SH_PLANE) return np_capsule_plane(pb, zb[0], zb[1], margin, pa, res);
   if (sb == SH_CYLINDER && sa == SH_PLANE) return np_cylinder_plane(pb, zb[0], zb[1], margin, pa, res);
   if (sb == SH_ELLIPSOID && sa == SH_PLANE) return np_ellipsoid_plane(pb, v3(zb[0], zb[1], zb[2]), margin, pa, res);
   if (sb == SH_SPHERE && sa == SH_CYLINDER) return np_sphere_cylinder(pb.p, zb[0], pa, za[0], za[1], margin, res);
   if (sb == SH_SPHERE && sa == SH_CAPSULE) return np_sphere_capsule(pb.p, zb[0], pa, za[0], za[1], margin, res);
+  if (sb == SH_SPHERE && sa == SH_ELLIPSOID) return np_sphere_ellipsoid(pb.p, zb[0], pa, v3(za[0], za[1], za[2]), margin, res);
   return 0;
 }
 

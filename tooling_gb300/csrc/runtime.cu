@@ -119,17 +119,17 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
         if (A.body < 0 || B.body < 0) continue;
         const bool cb = (A.shape == NEWT_SHAPE_CAPSULE && B.shape == NEWT_SHAPE_BOX) ||
                         (A.shape == NEWT_SHAPE_BOX && B.shape == NEWT_SHAPE_CAPSULE);
-        const bool sph_cyl = (A.shape == NEWT_SHAPE_SPHERE && B.shape == NEWT_SHAPE_CYLINDER) ||
-                             (A.shape == NEWT_SHAPE_CYLINDER && B.shape == NEWT_SHAPE_SPHERE);
-        const bool round = !sph_cyl && (A.shape == NEWT_SHAPE_CYLINDER || A.shape == NEWT_SHAPE_ELLIPSOID ||
-                                        B.shape == NEWT_SHAPE_CYLINDER || B.shape == NEWT_SHAPE_ELLIPSOID);
+        const bool sph_round = (A.shape == NEWT_SHAPE_SPHERE && (B.shape == NEWT_SHAPE_CYLINDER || B.shape == NEWT_SHAPE_ELLIPSOID)) ||
+                               (B.shape == NEWT_SHAPE_SPHERE && (A.shape == NEWT_SHAPE_CYLINDER || A.shape == NEWT_SHAPE_ELLIPSOID));
+        const bool round = !sph_round && (A.shape == NEWT_SHAPE_CYLINDER || A.shape == NEWT_SHAPE_ELLIPSOID ||
+                                          B.shape == NEWT_SHAPE_CYLINDER || B.shape == NEWT_SHAPE_ELLIPSOID);
         if (!(cb || round) || !((A.group & B.mask) != 0u && (B.group & A.mask) != 0u)) continue;
         if (cb) return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "capsule-box pairs are not supported (newt/src/contact.rs:232-257)");
-        // cylinders touch planes and spheres here, ellipsoids planes only; newt's
-        // sphere-ellipsoid route (contact.rs:1630-1725) is not on the GPU path
+        // cylinders and ellipsoids touch planes and spheres here; newt routes
+        // their other pairs through its convex solver (contact.rs:2509-2587)
         return fail(ctx, NEWT_E_UNSUPPORTED_PAIR,
-                    "cylinder bodies may collide with planes and spheres, ellipsoid bodies with planes only, on the GPU "
-                    "path (filter the other body pairs)");
+                    "cylinder and ellipsoid bodies may collide with planes and spheres on the GPU path (filter the "
+                    "other body pairs)");
       }
     for (int b = 0; b < d.n_bodies; ++b) {
       if (per_body[b] != 1) return fail(ctx, NEWT_E_INVALID, "GPU piles need exactly one geom per body");
@@ -175,12 +175,12 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
           if (A.link < 0 || B.link < 0 || A.link == B.link) continue;
           if (!((A.group & B.mask) != 0u && (B.group & A.mask) != 0u)) continue;
           const int lo = std::min(A.shape, B.shape), hi = std::max(A.shape, B.shape);
-          const bool ok = (lo == NEWT_SHAPE_SPHERE && hi <= NEWT_SHAPE_CYLINDER) ||
+          const bool ok = (lo == NEWT_SHAPE_SPHERE && hi <= NEWT_SHAPE_ELLIPSOID) ||
                           (lo == NEWT_SHAPE_BOX && hi == NEWT_SHAPE_BOX) ||
                           (lo == NEWT_SHAPE_CAPSULE && hi == NEWT_SHAPE_CAPSULE);
           if (!ok)
             return fail(ctx, NEWT_E_UNSUPPORTED_PAIR,
-                        "in-tree pairs on the GPU path: sphere with sphere, box, capsule or cylinder, box-box, "
+                        "in-tree pairs on the GPU path: sphere with sphere, box, capsule, cylinder or ellipsoid, box-box, "
                         "capsule-capsule (filter the others or disable tree self-collision)");
         }
     if (d.solver != NEWT_SOLVER_PGS && d.solver != NEWT_SOLVER_NEWTON)
