@@ -56,6 +56,23 @@ PGS_FLOP_PER_CONTACT_SWEEP = 5 * 235
 FUSED_DRAM_BYTES_PER_WORLD_STEP = (30.373632e6 + 258.361344e6) / (2048 * 25)
 
 
+def pinned_like(a):
+    """A page-locked host copy of float32 array `a` (torch's pinned allocator),
+    or a plain copy where torch cannot pin."""
+    try:
+        import torch
+        t = torch.empty(a.size, dtype=torch.float32, pin_memory=True)
+        out = t.numpy()
+        out[:] = a
+        pinned_like.keep.append(t)  # the numpy view does not own the buffer
+        return out
+    except Exception:
+        return np.array(a, dtype=np.float32, copy=True)
+
+
+pinned_like.keep = []
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -284,9 +301,10 @@ def run_gpu(args, rank, ws, local, dist):
     env_steps = W * S * args.steps * ws
     value = env_steps / (total_ms / 1e3)
     st = eng.status(slots)
-    # e2e: host buffers in, host buffers out, every step
-    qp = start_qpos.copy()
-    qv = start_qvel.copy()
+    # e2e: host buffers in, host buffers out, every step (page-locked host
+    # buffers: the state moves by DMA, converted on the device)
+    qp = pinned_like(start_qpos)
+    qv = pinned_like(start_qvel)
     h2d = (qp.nbytes + qv.nbytes)
     d2h = h2d
     barrier(dist)
@@ -294,7 +312,7 @@ def run_gpu(args, rank, ws, local, dist):
     for _ in range(args.steps):
         eng.set_state(slots, qp, qv)
         eng.step(S, STEP_BATCHED)
-        qp, qv = eng.get_state(slots, nq_t, nv_t)
+        eng.get_state(slots, nq_t, nv_t, out=(qp, qv))
     eng.sync()
     e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
     e2e = env_steps / e2e_s
@@ -537,7 +555,7 @@ def run_gpu_quadruped(args, rank, ws, local, dist):
     sample = slots[:: max(1, W // 64)]
     contacts = float(np.mean([len(eng.contacts(int(s))[0]) for s in sample]))
     # e2e: host state and controls in, host state out, every bench step
-    qp, qv = start_qpos.copy(), start_qvel.copy()
+    qp, qv = pinned_like(start_qpos), pinned_like(start_qvel)
     h2d = qp.nbytes + qv.nbytes + ctrl[0].nbytes
     d2h = qp.nbytes + qv.nbytes
     barrier(dist)
@@ -546,7 +564,7 @@ def run_gpu_quadruped(args, rank, ws, local, dist):
         eng.set_state(slots, qp, qv)
         eng.set_qfrc(slots, ctrl[blk]); blk += 1
         eng.step(S, STEP_BATCHED)
-        qp, qv = eng.get_state(slots, int(batch.nq.sum()), int(batch.nv.sum()))
+        eng.get_state(slots, int(batch.nq.sum()), int(batch.nv.sum()), out=(qp, qv))
     eng.sync()
     e2e = W * S * args.steps * ws / max_over_ranks(dist, time.perf_counter() - t0)
     hbm, src = peaks()
@@ -652,13 +670,13 @@ def run_gpu_uneven(args, rank, ws, local, dist):
     plain_launches = eng.launch_count() - plain_launch0
     plain = W * S * args.steps / (max_over_ranks(dist, pms) / 1e3)
     # e2e through the C ABI with host buffers, batched form
-    qp, qv = start_qpos.copy(), start_qvel.copy()
+    qp, qv = pinned_like(start_qpos), pinned_like(start_qvel)
     barrier(dist)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         eng.set_state(slots, qp, qv)
         eng.step(S, STEP_BATCHED)
-        qp, qv = eng.get_state(slots, nq, nv)
+        eng.get_state(slots, nq, nv, out=(qp, qv))
     eng.sync()
     e2e = W * S * args.steps * ws / max_over_ranks(dist, time.perf_counter() - t0)
     hbm, src = peaks()

@@ -170,7 +170,12 @@ NEWT_API int newt_gpu_alloc_worlds(newt_gpu_ctx* ctx, const int32_t* model_ids, 
 NEWT_API int newt_gpu_free_worlds(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n);
 
 /* State in/out, MuJoCo layout, the worlds' vectors concatenated in `slots`
- * order.  Mirrors `World::apply_mujoco_qpos/qvel` (newt/src/world.rs:519-623). */
+ * order.  Mirrors `World::apply_mujoco_qpos/qvel` (newt/src/world.rs:519-623).
+ * Each call makes one host<->device copy per array and converts between the
+ * layouts on the device; arrays in page-locked host memory (cudaMallocHost,
+ * cudaHostRegister) are copied by DMA as they are, others through the
+ * context's staging buffer.  Both return once the caller's arrays are free
+ * again; a slot named twice in newt_gpu_set_state is refused. */
 NEWT_API int newt_gpu_set_state(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, const float* qpos,
                        const float* qvel);
 NEWT_API int newt_gpu_get_state(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, float* qpos, float* qvel);

@@ -221,10 +221,19 @@ class Engine:
         qv = np.ascontiguousarray(qvel, np.float32)
         self._ck(self.L.newt_gpu_set_state(self.ctx, _p(s), len(s), _p(qp), _p(qv)))
 
-    def get_state(self, slots, nq_total: int, nv_total: int):
+    def get_state(self, slots, nq_total: int, nv_total: int, out=None):
+        """MuJoCo-layout state of the worlds, into new arrays or into `out`
+        (a pair of contiguous float32 arrays; page-locked ones are filled by
+        DMA directly)."""
         s = np.ascontiguousarray(slots, np.int32)
-        qp = np.zeros(nq_total, np.float32)
-        qv = np.zeros(nv_total, np.float32)
+        if out is None:
+            qp = np.zeros(nq_total, np.float32)
+            qv = np.zeros(nv_total, np.float32)
+        else:
+            qp, qv = out
+            if not (qp.dtype == np.float32 and qv.dtype == np.float32 and qp.flags.c_contiguous
+                    and qv.flags.c_contiguous and qp.size >= nq_total and qv.size >= nv_total):
+                raise ValueError("out must be two contiguous float32 arrays large enough for the state")
         self._ck(self.L.newt_gpu_get_state(self.ctx, _p(s), len(s), _p(qp), _p(qv)))
         return qp, qv
 

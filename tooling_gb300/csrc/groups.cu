@@ -14,22 +14,6 @@
     if (e_ != cudaSuccess) { ctx->err = std::string(#call ": ") + cudaGetErrorString(e_); return NEWT_E_CUDA; } \
   } while (0)
 
-static void q_rotT(const float q[4], const float v[3], float o[3]) {  // R(q)^T v
-  float x = -q[0], y = -q[1], z = -q[2], w = q[3];
-  float tx = 2.f * (y * v[2] - z * v[1]), ty = 2.f * (z * v[0] - x * v[2]), tz = 2.f * (x * v[1] - y * v[0]);
-  o[0] = v[0] + w * tx + (y * tz - z * ty);
-  o[1] = v[1] + w * ty + (z * tx - x * tz);
-  o[2] = v[2] + w * tz + (x * ty - y * tx);
-}
-static void q_rot(const float q[4], const float v[3], float o[3]) {
-  float c[4] = {-q[0], -q[1], -q[2], q[3]};
-  q_rotT(c, v, o);
-}
-static void q_norm(float q[4]) {
-  float n = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
-  if (n == 0.f) { q[0] = q[1] = q[2] = 0.f; q[3] = 1.f; return; }
-  for (int k = 0; k < 4; ++k) q[k] /= n;
-}
 static void sym6(const float m9[9], float* o) {  // column-major 3x3 -> xx yy zz xy xz yz
   o[0] = m9[0]; o[1] = m9[4]; o[2] = m9[8]; o[3] = m9[3]; o[4] = m9[6]; o[5] = m9[7];
 }
@@ -426,74 +410,8 @@ int HostGroup::flush_model(newt_gpu_ctx* ctx) {
 // ---------------------------------------------------------------------------
 // state staging (MuJoCo layout in, newt layout on the device)
 // ---------------------------------------------------------------------------
-void HostGroup::state_rows(size_t* lo, size_t* cnt) const {
-  if (soa()) { *lo = r_q; *cnt = (size_t)nq + nv; }  // q then qd
-  else { *lo = lay.pos; *cnt = (size_t)(lay.omg + 3 * size - lay.pos); }
-}
-
-void HostGroup::stage_state(int w, const HostModel& m, const float* qpos, const float* qvel) {
-  if (soa()) {
-    int c = 0, v = 0;
-    for (int i = 0; i < size; ++i) {
-      int jt = topo[4 * i + 1], qo = topo[4 * i + 2], vo = topo[4 * i + 3];
-      if (jt == NEWT_JOINT_FREE) {
-        float q4[4] = {qpos[c + 4], qpos[c + 5], qpos[c + 6], qpos[c + 3]};
-        q_norm(q4);
-        for (int k = 0; k < 3; ++k) F(r_q + qo + k, w) = qpos[c + k];
-        for (int k = 0; k < 4; ++k) F(r_q + qo + 3 + k, w) = q4[k];
-        float vb[3];
-        q_rotT(q4, qvel + v, vb);
-        for (int k = 0; k < 3; ++k) { F(r_qd + vo + k, w) = qvel[v + 3 + k]; F(r_qd + vo + 3 + k, w) = vb[k]; }
-        c += 7; v += 6;
-      } else if (jt == NEWT_JOINT_HINGE || jt == NEWT_JOINT_SLIDE) {
-        F(r_q + qo, w) = qpos[c]; F(r_qd + vo, w) = qvel[v];
-        c += 1; v += 1;
-      }
-    }
-  } else if (kind == GK_PILE) {
-    for (int b = 0; b < size; ++b) {
-      const float* p = qpos + 7 * b;
-      const float* vv = qvel + 6 * b;
-      float q4[4] = {p[4], p[5], p[6], p[3]};
-      q_norm(q4);
-      for (int k = 0; k < 3; ++k) { F(lay.pos + 3 * b + k, w) = p[k]; F(lay.vel + 3 * b + k, w) = vv[k]; F(lay.omg + 3 * b + k, w) = vv[3 + k]; }
-      for (int k = 0; k < 4; ++k) F(lay.quat + 4 * b + k, w) = q4[k];
-    }
-  }
-  (void)m;
-}
-
 void HostGroup::stage_qfrc(int w, const HostModel& m, const float* qfrc) {
   if (soa()) for (int k = 0; k < nv; ++k) F(r_qfrc + k, w) = qfrc[k];
-  (void)m;
-}
-
-void HostGroup::read_state(int w, const HostModel& m, float* qpos, float* qvel) const {
-  if (soa()) {
-    int c = 0, v = 0;
-    for (int i = 0; i < size; ++i) {
-      int jt = topo[4 * i + 1], qo = topo[4 * i + 2], vo = topo[4 * i + 3];
-      if (jt == NEWT_JOINT_FREE) {
-        float q4[4] = {Fc(r_q + qo + 3, w), Fc(r_q + qo + 4, w), Fc(r_q + qo + 5, w), Fc(r_q + qo + 6, w)};
-        for (int k = 0; k < 3; ++k) qpos[c + k] = Fc(r_q + qo + k, w);
-        qpos[c + 3] = q4[3]; qpos[c + 4] = q4[0]; qpos[c + 5] = q4[1]; qpos[c + 6] = q4[2];
-        float vb[3] = {Fc(r_qd + vo + 3, w), Fc(r_qd + vo + 4, w), Fc(r_qd + vo + 5, w)}, vw[3];
-        q_rot(q4, vb, vw);
-        for (int k = 0; k < 3; ++k) { qvel[v + k] = vw[k]; qvel[v + 3 + k] = Fc(r_qd + vo + k, w); }
-        c += 7; v += 6;
-      } else if (jt == NEWT_JOINT_HINGE || jt == NEWT_JOINT_SLIDE) {
-        qpos[c] = Fc(r_q + qo, w); qvel[v] = Fc(r_qd + vo, w);
-        c += 1; v += 1;
-      }
-    }
-  } else if (kind == GK_PILE) {
-    for (int b = 0; b < size; ++b) {
-      float* p = qpos + 7 * b;
-      float* vv = qvel + 6 * b;
-      for (int k = 0; k < 3; ++k) { p[k] = Fc(lay.pos + 3 * b + k, w); vv[k] = Fc(lay.vel + 3 * b + k, w); vv[3 + k] = Fc(lay.omg + 3 * b + k, w); }
-      p[3] = Fc(lay.quat + 4 * b + 3, w); p[4] = Fc(lay.quat + 4 * b, w); p[5] = Fc(lay.quat + 4 * b + 1, w); p[6] = Fc(lay.quat + 4 * b + 2, w);
-    }
-  }
   (void)m;
 }
 

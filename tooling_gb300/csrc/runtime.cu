@@ -402,7 +402,7 @@ static int group_worlds(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, std:
   return NEWT_OK;
 }
 
-enum RowSet { ROWS_STATE, ROWS_QFRC, ROWS_QACC };
+enum RowSet { ROWS_QFRC, ROWS_QACC };
 
 static std::vector<RowMove> moves_for(newt_gpu_ctx* ctx, std::vector<std::vector<int>>& by_group, RowSet set) {
   std::vector<RowMove> mv;
@@ -410,29 +410,29 @@ static std::vector<RowMove> moves_for(newt_gpu_ctx* ctx, std::vector<std::vector
     if (by_group[gi].empty()) continue;
     HostGroup* g = ctx->groups[gi].get();
     size_t lo = 0, cnt = 0;
-    if (set == ROWS_STATE) g->state_rows(&lo, &cnt);
-    else if (!g->soa()) continue;  // free-body piles carry no generalised force or acceleration rows
-    else { lo = set == ROWS_QFRC ? g->r_qfrc : g->r_qacc; cnt = g->nv; }
+    if (!g->soa()) continue;  // free-body piles carry no generalised force or acceleration rows
+    lo = set == ROWS_QFRC ? g->r_qfrc : g->r_qacc;
+    cnt = g->nv;
     mv.push_back(RowMove{g, std::move(by_group[gi]), lo, cnt});
   }
   return mv;
 }
 
+// State goes in and out in MuJoCo layout, one copy each way, converted on the
+// device (world_io.cu); only the named worlds' rows change.  The host
+// mirror's state rows are not kept: every reader gathers from the device.
 int newt_gpu_set_state(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, const float* qpos, const float* qvel) {
   if (!ctx || (n > 0 && (!slots || !qpos || !qvel))) return NEWT_E_INVALID;
   cudaSetDevice(ctx->device);
   std::vector<std::vector<int>> by_group;
   int rc = group_worlds(ctx, slots, n, by_group);
   if (rc != NEWT_OK) return rc;
-  long qo = 0, vo = 0;
+  std::vector<char> seen(ctx->slots.size(), 0);
   for (int i = 0; i < n; ++i) {
-    const SlotRef& r = ctx->slots[slots[i]];
-    const HostModel& m = ctx->models[r.model];
-    ctx->groups[r.group]->stage_state(r.index, m, qpos + qo, qvel + vo);
-    qo += m.nq; vo += m.nv;
+    if (seen[slots[i]]) return fail(ctx, NEWT_E_INVALID, "slot named twice");
+    seen[slots[i]] = 1;
   }
-  // only the named worlds' rows move: the others keep their device state
-  return io_scatter(ctx, moves_for(ctx, by_group, ROWS_STATE));
+  return io_state_in(ctx, slots, n, qpos, qvel);
 }
 
 int newt_gpu_get_state(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, float* qpos, float* qvel) {
@@ -441,16 +441,7 @@ int newt_gpu_get_state(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, float
   std::vector<std::vector<int>> by_group;
   int rc = group_worlds(ctx, slots, n, by_group);
   if (rc != NEWT_OK) return rc;
-  rc = io_gather(ctx, moves_for(ctx, by_group, ROWS_STATE));
-  if (rc != NEWT_OK) return rc;
-  long qo = 0, vo = 0;
-  for (int i = 0; i < n; ++i) {
-    const SlotRef& r = ctx->slots[slots[i]];
-    const HostModel& m = ctx->models[r.model];
-    ctx->groups[r.group]->read_state(r.index, m, qpos + qo, qvel + vo);
-    qo += m.nq; vo += m.nv;
-  }
-  return NEWT_OK;
+  return io_state_out(ctx, slots, n, qpos, qvel);
 }
 
 int newt_gpu_set_qfrc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, const float* qfrc) {

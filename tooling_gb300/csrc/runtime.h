@@ -110,13 +110,9 @@ struct HostGroup {
   int* live_flag(int idx);      // the world's device live flag
   void write_model(newt_gpu_ctx* ctx, int idx, const HostModel& m);
   int flush_model(newt_gpu_ctx* ctx);
-  // state in the host mirror for one world; moved to and from the device
-  // per world by io_scatter / io_gather over state_rows (q, qd) or the
-  // qfrc / qacc rows
-  void stage_state(int idx, const HostModel& m, const float* qpos, const float* qvel);
+  // generalised force / acceleration rows of one world in the host mirror,
+  // moved per world by io_scatter / io_gather (state: io_state_in/out)
   void stage_qfrc(int idx, const HostModel& m, const float* qfrc);
-  void state_rows(size_t* lo, size_t* cnt) const;
-  void read_state(int idx, const HostModel& m, float* qpos, float* qvel) const;
   void read_qacc(int idx, const HostModel& m, float* qacc) const;
   int fetch_status(newt_gpu_ctx* ctx);
   int clear_status(newt_gpu_ctx* ctx);
@@ -230,6 +226,10 @@ struct RowMove {
 int io_scatter(newt_gpu_ctx* ctx, const std::vector<RowMove>& mv);  // host mirror -> device
 int io_gather(newt_gpu_ctx* ctx, const std::vector<RowMove>& mv);   // device -> host mirror
 int io_clear_flags(newt_gpu_ctx* ctx, const std::vector<int*>& flags);  // *flag = 0 on the device
+// MuJoCo-layout state of the named worlds in and out, converted on the device
+// (world_io.cu)
+int io_state_in(newt_gpu_ctx* ctx, const int32_t* slots, int n, const float* qpos, const float* qvel);
+int io_state_out(newt_gpu_ctx* ctx, const int32_t* slots, int n, float* qpos, float* qvel);
 int io_hold_flags(newt_gpu_ctx* ctx, const std::vector<int*>& flags);   // the same, queued without a wait
 void ctrl_release_slot(newt_gpu_ctx* ctx, int slot);                     // ends the slot's control stream
 

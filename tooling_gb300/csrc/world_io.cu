@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cstring>
 
+#include "common.cuh"
 #include "runtime.h"
 
 #define CKW(call)                                                               \
@@ -216,6 +217,214 @@ int io_gather(newt_gpu_ctx* ctx, const std::vector<RowMove>& all) {
         if (m.ints) std::memcpy(&g.I(m.lo + r, m.idx[j]), &v, sizeof(v));
         else g.F(m.lo + r, m.idx[j]) = v;
       }
+  }
+  return NEWT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// state in MuJoCo layout, converted on the device
+// ---------------------------------------------------------------------------
+// newt_gpu_set_state / newt_gpu_get_state move the caller's MuJoCo-layout
+// arrays in one copy each way and convert them here, a warp per world:
+// quaternions reordered (wxyz <-> xyzw) and, on the way in, normalised; a
+// free root's linear velocity rotated between world and body frame (newt's
+// apply_mujoco_qpos/qvel, world.rs:519-623, and its inverse).  A free root's
+// and a hinge's MuJoCo offsets equal newt's (7 and 1 coordinates, 6 and 1
+// rates), so a link's `topo` offsets index both layouts.
+namespace {
+
+struct StateGroup {
+  float* F;
+  int soa, cap, size;  // tree SoA (row * cap + w) or pile world-major (w * frows + row); bodies or links
+  long frows;
+  int pos, quat, vel, omg;  // pile rows
+  int rq, rqd;              // tree rows
+  const int* topo;          // tree: parent, joint, q offset, v offset per link
+};
+struct StateWorld { int g, w, qoff, voff; };
+
+NEWT_D float& frow(const StateGroup& g, int row, int w) {
+  return g.soa ? g.F[(size_t)row * g.cap + w] : g.F[(size_t)w * g.frows + row];
+}
+NEWT_D Q4 qnorm_or_identity(Q4 q) {  // the host's q_norm: a zero quaternion becomes the identity
+  const float n = sqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
+  return n == 0.f ? Q4{0.f, 0.f, 0.f, 1.f} : Q4{q.x / n, q.y / n, q.z / n, q.w / n};
+}
+
+__global__ void state_in(const StateGroup* __restrict__ G, const StateWorld* __restrict__ W, int n,
+                         const float* __restrict__ qpos, const float* __restrict__ qvel) {
+  const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (t >= n) return;
+  const StateWorld sw = W[t];
+  const StateGroup g = G[sw.g];
+  const float* qp = qpos + sw.qoff;
+  const float* qv = qvel + sw.voff;
+  for (int i = lane; i < g.size; i += 32) {
+    if (!g.soa) {  // free body i
+      const float* p = qp + 7 * i;
+      const float* v = qv + 6 * i;
+      const Q4 q = qnorm_or_identity(Q4{p[4], p[5], p[6], p[3]});
+      for (int k = 0; k < 3; ++k) {
+        frow(g, g.pos + 3 * i + k, sw.w) = p[k];
+        frow(g, g.vel + 3 * i + k, sw.w) = v[k];
+        frow(g, g.omg + 3 * i + k, sw.w) = v[3 + k];
+      }
+      frow(g, g.quat + 4 * i, sw.w) = q.x; frow(g, g.quat + 4 * i + 1, sw.w) = q.y;
+      frow(g, g.quat + 4 * i + 2, sw.w) = q.z; frow(g, g.quat + 4 * i + 3, sw.w) = q.w;
+      continue;
+    }
+    const int jt = g.topo[4 * i + 1], qo = g.topo[4 * i + 2], vo = g.topo[4 * i + 3];
+    if (jt == NEWT_JOINT_FREE) {  // pos, quat xyzw; omega_body, v_body
+      const Q4 q = qnorm_or_identity(Q4{qp[qo + 4], qp[qo + 5], qp[qo + 6], qp[qo + 3]});
+      const V3 vb = qrot_inv(q, v3(qv[vo], qv[vo + 1], qv[vo + 2]));
+      for (int k = 0; k < 3; ++k) frow(g, g.rq + qo + k, sw.w) = qp[qo + k];
+      frow(g, g.rq + qo + 3, sw.w) = q.x; frow(g, g.rq + qo + 4, sw.w) = q.y;
+      frow(g, g.rq + qo + 5, sw.w) = q.z; frow(g, g.rq + qo + 6, sw.w) = q.w;
+      for (int k = 0; k < 3; ++k) frow(g, g.rqd + vo + k, sw.w) = qv[vo + 3 + k];
+      frow(g, g.rqd + vo + 3, sw.w) = vb.x; frow(g, g.rqd + vo + 4, sw.w) = vb.y; frow(g, g.rqd + vo + 5, sw.w) = vb.z;
+    } else if (jt == NEWT_JOINT_HINGE || jt == NEWT_JOINT_SLIDE) {
+      frow(g, g.rq + qo, sw.w) = qp[qo];
+      frow(g, g.rqd + vo, sw.w) = qv[vo];
+    }
+  }
+}
+
+__global__ void state_out(const StateGroup* __restrict__ G, const StateWorld* __restrict__ W, int n,
+                          float* __restrict__ qpos, float* __restrict__ qvel) {
+  const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (t >= n) return;
+  const StateWorld sw = W[t];
+  const StateGroup g = G[sw.g];
+  float* qp = qpos + sw.qoff;
+  float* qv = qvel + sw.voff;
+  for (int i = lane; i < g.size; i += 32) {
+    if (!g.soa) {
+      float* p = qp + 7 * i;
+      float* v = qv + 6 * i;
+      for (int k = 0; k < 3; ++k) {
+        p[k] = frow(g, g.pos + 3 * i + k, sw.w);
+        v[k] = frow(g, g.vel + 3 * i + k, sw.w);
+        v[3 + k] = frow(g, g.omg + 3 * i + k, sw.w);
+      }
+      p[3] = frow(g, g.quat + 4 * i + 3, sw.w); p[4] = frow(g, g.quat + 4 * i, sw.w);
+      p[5] = frow(g, g.quat + 4 * i + 1, sw.w); p[6] = frow(g, g.quat + 4 * i + 2, sw.w);
+      continue;
+    }
+    const int jt = g.topo[4 * i + 1], qo = g.topo[4 * i + 2], vo = g.topo[4 * i + 3];
+    if (jt == NEWT_JOINT_FREE) {
+      const Q4 q{frow(g, g.rq + qo + 3, sw.w), frow(g, g.rq + qo + 4, sw.w), frow(g, g.rq + qo + 5, sw.w),
+                 frow(g, g.rq + qo + 6, sw.w)};
+      for (int k = 0; k < 3; ++k) qp[qo + k] = frow(g, g.rq + qo + k, sw.w);
+      qp[qo + 3] = q.w; qp[qo + 4] = q.x; qp[qo + 5] = q.y; qp[qo + 6] = q.z;
+      const V3 vw = qrot(q, v3(frow(g, g.rqd + vo + 3, sw.w), frow(g, g.rqd + vo + 4, sw.w),
+                               frow(g, g.rqd + vo + 5, sw.w)));
+      qv[vo] = vw.x; qv[vo + 1] = vw.y; qv[vo + 2] = vw.z;
+      for (int k = 0; k < 3; ++k) qv[vo + 3 + k] = frow(g, g.rqd + vo + k, sw.w);
+    } else if (jt == NEWT_JOINT_HINGE || jt == NEWT_JOINT_SLIDE) {
+      qp[qo] = frow(g, g.rq + qo, sw.w);
+      qv[vo] = frow(g, g.rqd + vo, sw.w);
+    }
+  }
+}
+
+bool host_pinned(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+  return a.type == cudaMemoryTypeHost;
+}
+
+// The call's worlds: per distinct group a StateGroup, per world its entry,
+// in the staging's head; returns the offsets of qpos and qvel in the staging.
+struct StatePlan { std::vector<StateGroup> groups; std::vector<StateWorld> worlds; long nq = 0, nv = 0; };
+StatePlan plan_state(newt_gpu_ctx* ctx, const int32_t* slots, int n) {
+  StatePlan P;
+  std::vector<int> gslot(ctx->groups.size(), -1);
+  for (int i = 0; i < n; ++i) {
+    const SlotRef& r = ctx->slots[slots[i]];
+    const HostModel& m = ctx->models[r.model];
+    if (gslot[r.group] < 0) {
+      const HostGroup& hg = *ctx->groups[r.group];
+      StateGroup g{};
+      g.F = hg.dF;
+      g.soa = hg.soa() ? 1 : 0;
+      g.cap = hg.cap;
+      g.size = hg.size;
+      g.frows = (long)hg.frows;
+      g.pos = hg.lay.pos; g.quat = hg.lay.quat; g.vel = hg.lay.vel; g.omg = hg.lay.omg;
+      g.rq = hg.r_q; g.rqd = hg.r_qd;
+      g.topo = hg.dtopo;
+      gslot[r.group] = (int)P.groups.size();
+      P.groups.push_back(g);
+    }
+    P.worlds.push_back(StateWorld{gslot[r.group], r.index, (int)P.nq, (int)P.nv});
+    P.nq += m.nq;
+    P.nv += m.nv;
+  }
+  return P;
+}
+
+size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+}  // namespace
+
+int io_state_in(newt_gpu_ctx* ctx, const int32_t* slots, int n, const float* qpos, const float* qvel) {
+  if (n <= 0) return NEWT_OK;
+  const StatePlan P = plan_state(ctx, slots, n);
+  const size_t gb = up256(P.groups.size() * sizeof(StateGroup)), wb = up256(P.worlds.size() * sizeof(StateWorld));
+  const size_t qb = up256(P.nq * sizeof(float)), vb = P.nv * sizeof(float);
+  int rc = ensure_staging(ctx, 0, (gb + wb + qb + vb) / sizeof(float) + 1);
+  if (rc != NEWT_OK) return rc;
+  char* h = (char*)ctx->io_h;
+  char* d = (char*)ctx->io_d;
+  std::memcpy(h, P.groups.data(), P.groups.size() * sizeof(StateGroup));
+  std::memcpy(h + gb, P.worlds.data(), P.worlds.size() * sizeof(StateWorld));
+  CKW(cudaMemcpyAsync(d, h, gb + wb, cudaMemcpyHostToDevice, ctx->stream));
+  // page-locked caller arrays go by DMA as they are; others through the staging
+  const bool pinned = host_pinned(qpos) && host_pinned(qvel);
+  if (!pinned) {
+    std::memcpy(h + gb + wb, qpos, P.nq * sizeof(float));
+    std::memcpy(h + gb + wb + qb, qvel, vb);
+  }
+  CKW(cudaMemcpyAsync(d + gb + wb, pinned ? (const void*)qpos : (const void*)(h + gb + wb), P.nq * sizeof(float),
+                      cudaMemcpyHostToDevice, ctx->stream));
+  CKW(cudaMemcpyAsync(d + gb + wb + qb, pinned ? (const void*)qvel : (const void*)(h + gb + wb + qb), vb,
+                      cudaMemcpyHostToDevice, ctx->stream));
+  const long threads = 32L * n;
+  state_in<<<(int)((threads + 255) / 256), 256, 0, ctx->stream>>>((const StateGroup*)d, (const StateWorld*)(d + gb), n,
+                                                                   (const float*)(d + gb + wb),
+                                                                   (const float*)(d + gb + wb + qb));
+  ctx->launches++;
+  CKW(cudaGetLastError());
+  CKW(cudaStreamSynchronize(ctx->stream));  // the caller's arrays and the staging are free again
+  return NEWT_OK;
+}
+
+int io_state_out(newt_gpu_ctx* ctx, const int32_t* slots, int n, float* qpos, float* qvel) {
+  if (n <= 0) return NEWT_OK;
+  const StatePlan P = plan_state(ctx, slots, n);
+  const size_t gb = up256(P.groups.size() * sizeof(StateGroup)), wb = up256(P.worlds.size() * sizeof(StateWorld));
+  const size_t qb = up256(P.nq * sizeof(float)), vb = P.nv * sizeof(float);
+  int rc = ensure_staging(ctx, 0, (gb + wb + qb + vb) / sizeof(float) + 1);
+  if (rc != NEWT_OK) return rc;
+  char* h = (char*)ctx->io_h;
+  char* d = (char*)ctx->io_d;
+  std::memcpy(h, P.groups.data(), P.groups.size() * sizeof(StateGroup));
+  std::memcpy(h + gb, P.worlds.data(), P.worlds.size() * sizeof(StateWorld));
+  CKW(cudaMemcpyAsync(d, h, gb + wb, cudaMemcpyHostToDevice, ctx->stream));
+  const long threads = 32L * n;
+  state_out<<<(int)((threads + 255) / 256), 256, 0, ctx->stream>>>((const StateGroup*)d, (const StateWorld*)(d + gb),
+                                                                    n, (float*)(d + gb + wb), (float*)(d + gb + wb + qb));
+  ctx->launches++;
+  CKW(cudaGetLastError());
+  const bool pinned = host_pinned(qpos) && host_pinned(qvel);
+  CKW(cudaMemcpyAsync(pinned ? (void*)qpos : (void*)(h + gb + wb), d + gb + wb, P.nq * sizeof(float),
+                      cudaMemcpyDeviceToHost, ctx->stream));
+  CKW(cudaMemcpyAsync(pinned ? (void*)qvel : (void*)(h + gb + wb + qb), d + gb + wb + qb, vb, cudaMemcpyDeviceToHost,
+                      ctx->stream));
+  CKW(cudaStreamSynchronize(ctx->stream));
+  if (!pinned) {
+    std::memcpy(qpos, h + gb + wb, P.nq * sizeof(float));
+    std::memcpy(qvel, h + gb + wb + qb, vb);
   }
   return NEWT_OK;
 }
