@@ -32,6 +32,8 @@ FILES = [
     "goldens/solver_newton_incline.bin",
     "goldens/solver_tree.bin",
     "goldens/solver_newton_tree.bin",
+    "goldens/condim_torsional.bin",
+    "goldens/condim_rolling.bin",
     "references/double_pendulum_euler.bin",
     "references/ballistic_euler.bin",
     "references/sphere_drop_euler.bin",

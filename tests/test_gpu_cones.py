@@ -4,6 +4,10 @@ against the oracle, whose free-body rows hold newt's anchors
 (tests/test_oracle_cones.py).
 
 Bars:
+  * newt's condim goldens (condim_torsional.bin, condim_rolling.bin, the
+    oracle byte-identical to both): from each snapshot one GPU step within
+    2e-6 m and 2e-4 m/s of the oracle's f32 step, and from the start the GPU
+    within 5e-4 m and 5e-3 m/s of newt's snapshots at steps 50, 200, 1000;
   * newt's anchors (solver_friction_incline.rs, solver_free_bodies.rs,
     condim_torsional.rs, condim_rolling.rs) met by GPU runs: the incline
     holds at 22 and slides at 32 degrees under either cone, the condim-1
@@ -23,7 +27,8 @@ import numpy as np
 import pytest
 
 import oracle_py
-from test_oracle_cones import RK4, _run, incline, roller, spinner
+from test_oracle_cones import RK4, _run, condim_golden_scene, incline, roller, spinner
+from test_oracle_golden import _read_f32
 from tooling_gb300 import Engine, STEP_BATCHED, STEP_PLAIN, scenes
 from tooling_gb300 import api as A
 from tooling_gb300 import model as M
@@ -52,6 +57,39 @@ def _gpu_run(eng, w, q, v, n, mode=STEP_PLAIN):
     eng.free(slots)
     assert not st & 0x3, hex(st)
     return gq, gv
+
+
+def _mj_body(row):
+    """newt's body snapshot (pos, quat xyzw, v_world, omega_body) in MuJoCo
+    layout (pos, quat wxyz; v_world, omega_body)."""
+    return (np.array([row[0], row[1], row[2], row[6], row[3], row[4], row[5]], np.float32),
+            np.array(row[7:13], np.float32))
+
+
+@pytest.mark.parametrize("mode", [STEP_PLAIN, STEP_BATCHED])
+@pytest.mark.parametrize("kind", ["torsional", "rolling"])
+def test_condim_goldens(eng, kind, mode):
+    w, _, _ = condim_golden_scene(kind)
+    gold = _read_f32(f"condim_{kind}.bin").reshape(4, 13)
+    P = M.PackedModels([w])
+    for row in range(4):
+        q, v = _mj_body(gold[row])
+        gq, gv = _gpu_run(eng, w, q, v, 1, mode)
+        rq, rv = oracle_py.run(P, np.zeros(1, np.int32), q, v, None, 1, precision=0, integrator=RK4)
+        assert np.abs(gq - rq).max() < 2e-6 and np.abs(gv - rv).max() < 2e-4, (row, np.abs(gq - rq).max(),
+                                                                                np.abs(gv - rv).max())
+    q, v = _mj_body(gold[0])
+    slots = eng.alloc(eng.upload(P))
+    eng.set_state(slots, q, v)
+    done = 0
+    for row, n in enumerate((50, 200, 1000), start=1):
+        eng.step(n - done, mode)
+        done = n
+        gq, gv = eng.get_state(slots, 7, 6)
+        rq, rv = _mj_body(gold[row])
+        assert np.abs(gq - rq).max() < 5e-4 and np.abs(gv - rv).max() < 5e-3, (n, np.abs(gq - rq).max(),
+                                                                                np.abs(gv - rv).max())
+    eng.free(slots)
 
 
 @pytest.mark.parametrize("cone", [M.CONE_PYRAMIDAL, M.CONE_ELLIPTIC])

@@ -12,11 +12,16 @@ and above half with condim 3.  condim_rolling.rs:60-110: a rolling sphere
 slows monotonically to under half its speed in 4 s with condim 6 (mu_r 0.1)
 and keeps over half with condim 3.  newt states these as bands; the oracle
 meets them, and its elliptic and pyramidal incline runs differ (the cones
-are not the same rule)."""
+are not the same rule).  equality_golden.rs:189-258, 395-420: the oracle's
+f32 mirror is byte-identical to newt's condim_torsional.bin (a sphere spun
+at 8 rad/s on a condim-4 plane, mu_t 0.5) and condim_rolling.bin (a sphere
+rolling at 1 m/s on a condim-6 plane, mu_r 0.1) after 0, 50, 200 and 1000
+RK4 steps under PGS 30."""
 import numpy as np
 import pytest
 
 import oracle_py
+from test_oracle_golden import _read_f32
 from tooling_gb300 import model as M
 
 RK4 = 0
@@ -144,3 +149,41 @@ def test_condim_3_ball_keeps_rolling():
     v0 = float(np.hypot(v[0], v[1]))
     q, v = _run(w, q, v, 800)
     assert float(np.hypot(v[0], v[1])) > 0.5 * v0
+
+
+def condim_golden_scene(kind):
+    """equality_golden.rs:189-258: World::new() (RK4, PGS 30, pyramidal), a
+    1 kg sphere of radius 0.1 on a plane, solref (0.02, 1), the default
+    solimp; newt layout (pos, quat xyzw; v_world, omega_body)."""
+    fr, cd = (0.9, 6) if kind == "rolling" else (0.8, 4)
+    w = M.WorldModel(dt=0.005, gravity=(0.0, 0.0, -9.81), solver=M.SOLVER_PGS, iterations=30,
+                     integrator=M.INTEGRATOR_RK4, cone=M.CONE_PYRAMIDAL)
+    plane = M.static_plane(friction=fr)
+    g = M.Geom(shape=M.SHAPE_SPHERE, body=0, size=(0.1, 0.0, 0.0), friction=fr)
+    for geom in (plane, g):
+        geom.solref, geom.condim = (0.02, 1.0), cd
+        if kind == "rolling":
+            geom.rolling_friction = 0.1
+        else:
+            geom.torsional_friction = 0.5
+    w.add_geom(plane)
+    w.add_body(1.0, M.solid_sphere_inertia(1.0, 0.1))
+    w.add_geom(g)
+    if kind == "rolling":
+        q, v = [0.0, 0.01, 0.1, 0.0, 0.0, 0.0, 1.0], [1.0, 0.0, 0.0, 0.0, 10.0, 0.0]
+    else:
+        q, v = [0.01, 0.0, 0.5, 0.0, 0.0, 0.0, 1.0], [0.0, 0.0, 0.0, 0.0, 0.0, 8.0]
+    return w, np.array(q, np.float32), np.array(v, np.float32)
+
+
+@pytest.mark.parametrize("kind", ["torsional", "rolling"])
+def test_condim_goldens_are_byte_identical(kind):
+    w, q, v = condim_golden_scene(kind)
+    gold = _read_f32(f"condim_{kind}.bin").reshape(4, 13)
+    P = M.PackedModels([w])
+    got = [np.concatenate([q, v])]
+    for n in (50, 200, 1000):
+        qo, vo = oracle_py.run(P, np.zeros(1, np.int32), q, v, None, n, precision=0, layout=1, integrator=0)
+        got.append(np.concatenate([qo, vo]).astype(np.float32))
+    got = np.stack(got)
+    assert got.tobytes() == gold.tobytes(), np.abs(got - gold).max(axis=1)
