@@ -276,15 +276,21 @@ NEWT_API int newt_gpu_get_qacc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t 
  *   FRAMELINVEL          site linear velocity, world (3)
  *   FRAMEANGVEL          parent's angular velocity, world (3)
  *   SUBTREECOM           mass-weighted centre of link `index` and its descendants (3)
- *   ACCELEROMETER        specific force at the site on free body `index`, site frame (3)
+ *   ACCELEROMETER        specific force at the site on free body or link `index`, site frame (3)
  *   TOUCH                summed normal-force magnitudes of the contacts of geom `index` (1)
+ *   FORCE                force link `index`'s parent joint transmits to it, link frame (3)
+ *   TORQUE               the matching torque about the joint anchor, link frame (3)
  * ACCELEROMETER and TOUCH are read on pile worlds as newt's World::step reads
  * them (world.rs:1545-1612, sensor.rs:586-600, 1030-1112): the contacts of
  * the world's last step (any step form) are re-solved at its current state
  * with its solver, giving the body wrenches (F/m + g, Euler's equations) and
  * the normal forces (a contact's row impulses over dt).  A world read before
- * its first step sees no contacts.  Force and torque (trees) are not
- * provided. */
+ * its first step sees no contacts.  ACCELEROMETER on a link, FORCE and
+ * TORQUE are read on trees without geoms (sensor.rs:446-530, 620-647,
+ * 834-1000): qddot from the explicit ABA at the current state with the
+ * world's generalised forces, the links' spatial accelerations, and the RNE
+ * wrench each parent joint transmits; on tree-contact worlds (which would
+ * need the contact re-solve's link wrenches) they are refused. */
 #define NEWT_SENSOR_JOINTPOS 0
 #define NEWT_SENSOR_JOINTVEL 1
 #define NEWT_SENSOR_FRAMEPOS 2
@@ -296,6 +302,8 @@ NEWT_API int newt_gpu_get_qacc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t 
 #define NEWT_SENSOR_SUBTREECOM 8
 #define NEWT_SENSOR_ACCELEROMETER 9
 #define NEWT_SENSOR_TOUCH 10
+#define NEWT_SENSOR_FORCE 11
+#define NEWT_SENSOR_TORQUE 12
 typedef struct newt_sensor_desc {
   int32_t kind;        /* NEWT_SENSOR_* */
   int32_t on_link;     /* 1: `index` is a link of the world's tree, 0: a free body */

@@ -259,6 +259,61 @@ template <class R> static int np_pair_t(int ka, const float* pa, const float* sa
   return buf.len;
 }
 
+// sensor.rs:834-1000 for a tree without external wrenches: qddot from the
+// explicit ABA at the state, each link's spatial velocity and acceleration
+// at its COM in its frame (compute_link_va: a_i = X_i a_parent + S_i qddot_i
+// + v_i x S_i qdot_i), and the wrench its parent joint transmits
+// (compute_link_wrenches: f_i = I_i a_i + v_i x* I_i v_i - (0, m_i R_i^T g),
+// each child's pulled into its parent, leaves to root).
+template <class R> struct LinkDyn { SMotion<R> v, a; SForce<R> f; };
+template <class R> SMotion<R> sm_add(const SMotion<R>& x, const SMotion<R>& y) { return {x.ang + y.ang, x.lin + y.lin}; }
+template <class R> SMotion<R> sm_scale(const SMotion<R>& x, R k) { return {x.ang * k, x.lin * k}; }
+template <class R> SMotion<R> sm_cross(const SMotion<R>& x, const SMotion<R>& y) {  // spatial.rs:60-65
+  return {x.ang.cross(y.ang), x.ang.cross(y.lin) + x.lin.cross(y.ang)};
+}
+template <class R> SForce<R> sf_cross(const SMotion<R>& x, const SForce<R>& f) {  // spatial.rs:71-76
+  return {x.ang.cross(f.tau) + x.lin.cross(f.lin), x.ang.cross(f.lin)};
+}
+template <class R> void tree_link_dynamics(const Tree<R>& t, const std::vector<Pose<R>>& poses, Vec3<R> gravity,
+                                           std::vector<LinkDyn<R>>& out) {
+  const int n = (int)t.links.size();
+  std::vector<Wrench<R>> ext(n, Wrench<R>{Vec3<R>(), Vec3<R>()});
+  std::vector<R> qdd;
+  aba(t, poses, gravity, ext, R(0), qdd);
+  out.assign(n, LinkDyn<R>{});
+  const SMotion<R> z{Vec3<R>(), Vec3<R>()};
+  for (int i = 0; i < n; ++i) {
+    const Link<R>& L = t.links[i];
+    LinkDyn<R>& o = out[i];
+    if (L.type == J_FREE) {
+      const int v = t.v_off[i];
+      o.v = {Vec3<R>(t.qdot[v], t.qdot[v + 1], t.qdot[v + 2]), Vec3<R>(t.qdot[v + 3], t.qdot[v + 4], t.qdot[v + 5])};
+      o.a = {Vec3<R>(qdd[v], qdd[v + 1], qdd[v + 2]), Vec3<R>(qdd[v + 3], qdd[v + 4], qdd[v + 5])};
+      continue;
+    }
+    const Xform<R> x = xup_xform(t, i);
+    const SMotion<R> vp = L.parent >= 0 ? out[L.parent].v : z, ap = L.parent >= 0 ? out[L.parent].a : z;
+    if (L.type == J_FIXED) { o.v = x.motion(vp); o.a = x.motion(ap); continue; }
+    const SMotion<R> S = L.type == J_HINGE ? SMotion<R>{L.axis, L.jc_pos.cross(L.axis)} : SMotion<R>{Vec3<R>(), L.axis};
+    const SMotion<R> sq = sm_scale(S, t.qdot[t.v_off[i]]), sqq = sm_scale(S, qdd[t.v_off[i]]);
+    o.v = sm_add(x.motion(vp), sq);
+    o.a = sm_add(sm_add(x.motion(ap), sqq), sm_cross(o.v, sq));
+  }
+  for (int i = 0; i < n; ++i) {
+    const Link<R>& L = t.links[i];
+    const Mat6<R> I = Mat6<R>::from_spatial_inertia(L.mass, Vec3<R>(), L.inertia);
+    const SForce<R> ia = I.times_motion(out[i].a), iv = I.times_motion(out[i].v);
+    const SForce<R> bias = sf_cross(out[i].v, iv);
+    const Vec3<R> fb = poses[i].o.inverse_rotate((Vec3<R>() + gravity * L.mass)), tb = poses[i].o.inverse_rotate(Vec3<R>());
+    out[i].f = {(ia.tau + bias.tau) - tb, (ia.lin + bias.lin) - fb};
+  }
+  for (int i = n - 1; i >= 1; --i) {
+    const SForce<R> pulled = xup_xform(t, i).transpose_force(out[i].f);
+    SForce<R>& fp = out[t.links[i].parent].f;
+    fp = {fp.tau + pulled.tau, fp.lin + pulled.lin};
+  }
+}
+
 extern "C" {
 
 int oracle_model_dims(const newt_model_desc* d, int* nq, int* nv) { return dims(*d, nq, nv); }
@@ -385,12 +440,14 @@ int oracle_contacts(const newt_model_desc* d, const float* qpos, const float* qv
 // compute_link_va (:834-900) at zero acceleration.  `sensors` holds per sensor
 // (kind, on_link, index) ints in `si` and (local_pos xyz, local_quat xyzw) in
 // `sf`; `out` receives the concatenated values.
-int oracle_sensors(const newt_model_desc* d, const float* qpos, const float* qvel, int precision, int ns,
-                   const int* si, const float* sf, double* out) {
+int oracle_sensors(const newt_model_desc* d, const float* qpos, const float* qvel, const float* qfrc, int precision,
+                   int ns, const int* si, const float* sf, double* out) {
   auto go = [&](auto tag) {
     using R = decltype(tag);
     World<R> w = build_world<R>(*d);
     set_state(w, qpos, qvel, 0);
+    if (qfrc && !w.trees.empty())
+      for (int k = 0; k < w.trees[0].nv(); ++k) w.trees[0].qfrc_applied[k] = qfrc[k];
     std::vector<Pose<R>> poses;
     std::vector<GMotion<R>> v;
     if (!w.trees.empty()) {
@@ -411,12 +468,32 @@ int oracle_sensors(const newt_model_desc* d, const float* qpos, const float* qve
         }
       }
     }
+    std::vector<LinkDyn<R>> dyn;  // accelerometers on links, force and torque
+    for (int k = 0; k < ns && !w.trees.empty() && dyn.empty(); ++k)
+      if ((si[3 * k] == 9 && si[3 * k + 1]) || si[3 * k] == 11 || si[3 * k] == 12)
+        tree_link_dynamics(w.trees[0], poses, w.gravity, dyn);
     int o = 0;
     for (int k = 0; k < ns; ++k) {
       const int kind = si[3 * k], on_link = si[3 * k + 1], idx = si[3 * k + 2];
       const Vec3<R> lp(sf[7 * k], sf[7 * k + 1], sf[7 * k + 2]);
       const Quat<R> lq(sf[7 * k + 3], sf[7 * k + 4], sf[7 * k + 5], sf[7 * k + 6]);
       auto put3 = [&](Vec3<R> x) { out[o++] = (double)x.x; out[o++] = (double)x.y; out[o++] = (double)x.z; };
+      if (kind == 11) { put3(dyn[idx].f.lin); continue; }  // Force (sensor.rs:622-629)
+      if (kind == 12) {  // Torque at the joint anchor, tau - r_jc x F (sensor.rs:630-647)
+        put3(dyn[idx].f.tau - w.trees[0].links[idx].jc_pos.cross(dyn[idx].f.lin));
+        continue;
+      }
+      if (kind == 9) {  // accelerometer on a link (sensor.rs:1030-1087, the Link branch)
+        const Quat<R> ori = poses[idx].o;
+        const SMotion<R>& vb = dyn[idx].v;
+        const SMotion<R>& ab = dyn[idx].a;
+        const Vec3<R> om = ori.rotate(vb.ang), al = ori.rotate(ab.ang);
+        const Vec3<R> acom = ori.rotate(ab.lin + vb.ang.cross(vb.lin));
+        const Vec3<R> r = ori.rotate(lp);
+        const Vec3<R> asite = acom + al.cross(r) + om.cross(om.cross(r));
+        put3((ori * lq).inverse_rotate(asite - w.gravity));
+        continue;
+      }
       if (kind == 0 || kind == 1) {  // JointPos / JointVel
         const Tree<R>& t = w.trees[0];
         out[o++] = (double)(kind == 0 ? t.q[t.q_off[idx]] : t.qdot[t.v_off[idx]]);

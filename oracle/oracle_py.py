@@ -44,7 +44,7 @@ def lib():
         L.oracle_tree_impulses.restype = C.c_int
         L.oracle_tree_impulses_ex.argtypes = [P, P, P, P, C.c_int, C.c_int, P, P, P, C.c_int]
         L.oracle_tree_impulses_ex.restype = C.c_int
-        L.oracle_sensors.argtypes = [P, P, P, C.c_int, C.c_int, P, P, P]
+        L.oracle_sensors.argtypes = [P, P, P, P, C.c_int, C.c_int, P, P, P]
         L.oracle_sensors.restype = C.c_int
         L.oracle_contact_sensors.argtypes = [P, P, P, C.c_int, C.c_int, P, P, P, P, P]
         L.oracle_contact_sensors.restype = C.c_int
@@ -151,18 +151,22 @@ def contact_sensors(packed, index: int, qpos: np.ndarray, qvel: np.ndarray, sens
     return out, qo, vo
 
 
-def sensors(packed, index: int, qpos: np.ndarray, qvel: np.ndarray, sens: np.ndarray, precision: int = 1) -> np.ndarray:
+def sensors(packed, index: int, qpos: np.ndarray, qvel: np.ndarray, sens: np.ndarray, precision: int = 1,
+            qfrc: Optional[np.ndarray] = None) -> np.ndarray:
     """Post-step sensor values of one world at its state (MuJoCo layout);
     `sens` is an array with the fields kind, on_link, index, local_pos,
-    local_quat (the newt_sensor_desc layout)."""
+    local_quat (the newt_sensor_desc layout); `qfrc` the tree's applied
+    generalised forces (newt layout), read by the accelerometer on a link
+    and the force and torque sensors."""
     qpos = np.ascontiguousarray(qpos, dtype=np.float32)
     qvel = np.ascontiguousarray(qvel, dtype=np.float32)
+    qfrc = None if qfrc is None else np.ascontiguousarray(qfrc, dtype=np.float32)
     si = np.ascontiguousarray(np.stack([sens["kind"], sens["on_link"], sens["index"]], 1), np.int32)
     sf = np.ascontiguousarray(np.concatenate([sens["local_pos"], sens["local_quat"]], 1), np.float32)
     D = int(sum(1 if k <= 1 else (4 if k == 3 else 3) for k in sens["kind"]))
     out = np.zeros(D, dtype=np.float64)
     d = C.cast(C.byref(packed.descs[index]), C.c_void_p)
-    lib().oracle_sensors(d, _ptr(qpos), _ptr(qvel), precision, len(sens), _ptr(si), _ptr(sf), _ptr(out))
+    lib().oracle_sensors(d, _ptr(qpos), _ptr(qvel), _ptr(qfrc), precision, len(sens), _ptr(si), _ptr(sf), _ptr(out))
     return out
 
 

@@ -3,7 +3,9 @@
 // sensor's values into the world's output row.  Accelerometer and touch
 // readings on pile worlds come from newt's post-step contact re-solve
 // (pile_kernels.cu: pile_k_reassemble, the solvers, then
-// pile_contact_sensors_kernel), run for the group before its sensors.
+// pile_contact_sensors_kernel), run for the group before its sensors;
+// accelerometer, force and torque readings on trees without geoms from the
+// links' dynamics pass (tree_kernels.cu: tree_sensor_dyn_kernel).
 //
 // Restates, for FP32 on sm_103a:
 //   newt/src/sensor.rs:560-700   evaluate (JointPos, JointVel, FramePos,
@@ -33,6 +35,10 @@ __host__ __device__ int sensor_dim(int kind) {
 __host__ __device__ bool contact_sensor(int kind) {
   return kind == NEWT_SENSOR_ACCELEROMETER || kind == NEWT_SENSOR_TOUCH;
 }
+// kinds read from the links' dynamics pass on trees (tree_sensor_dyn_kernel)
+__host__ __device__ bool dyn_sensor(int kind) {
+  return kind == NEWT_SENSOR_ACCELEROMETER || kind == NEWT_SENSOR_FORCE || kind == NEWT_SENSOR_TORQUE;
+}
 
 NEWT_D Q4 axis_angle(V3 axis, float angle) {  // newt/src/math.rs:574-580
   const float l = sqrtf(len2(axis));
@@ -53,7 +59,7 @@ NEWT_D void write_sensors(const newt_sensor_desc* S, int ns, const Frame* frames
   for (int k = 0; k < ns; ++k) {
     const newt_sensor_desc& s = S[k];
     const int kind = s.kind;
-    if (contact_sensor(kind)) { o += sensor_dim(kind); continue; }  // the contact sensors' kernel
+    if (contact_sensor(kind) || dyn_sensor(kind)) { o += sensor_dim(kind); continue; }  // written apart
     if (kind == NEWT_SENSOR_JOINTPOS) { row[o++] = q[qoff[s.index]]; continue; }
     if (kind == NEWT_SENSOR_JOINTVEL) { row[o++] = qd[voff[s.index]]; continue; }
     if (kind == NEWT_SENSOR_SUBTREECOM) {
@@ -86,9 +92,12 @@ NEWT_D void write_sensors(const newt_sensor_desc* S, int ns, const Frame* frames
 // Tree worlds (trees without geoms and tree-contact worlds): newt layout q/qd
 // in the group's SoA rows.  Frames for link sensors and subtree centres are
 // collected per sensor as the links are walked.
+// `dyn` (trees without geoms, when an accelerometer, force or torque sensor
+// is asked for): the links' dynamics pass, 18 floats per link of each world.
 template <int MAXL>
 __global__ void __launch_bounds__(64) tree_sensors_kernel(TreeGroupDev g, const int* idx, int n,
-                                                         const newt_sensor_desc* S, int ns, float* out, int D) {
+                                                         const newt_sensor_desc* S, int ns, float* out, int D,
+                                                         const float* dyn) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   const int w = idx[t], cap = g.cap, L = g.L;
@@ -156,10 +165,40 @@ __global__ void __launch_bounds__(64) tree_sensors_kernel(TreeGroupDev g, const 
       com[k] = m == 0.f ? v3(0.f, 0.f, 0.f) : acc / m;
       continue;
     }
-    if (s.kind <= NEWT_SENSOR_JOINTVEL || contact_sensor(s.kind)) continue;
+    if (s.kind <= NEWT_SENSOR_JOINTVEL || contact_sensor(s.kind) || dyn_sensor(s.kind)) continue;
     fr[k] = Frame{P[l], O[l], Wn[l], Vn[l], qrot_inv(O[l], Wn[l])};
   }
-  write_sensors(S, ns, fr, q, qd, qoff, voff, out + (size_t)t * D, com);
+  float* row = out + (size_t)t * D;
+  write_sensors(S, ns, fr, q, qd, qoff, voff, row, com);
+  if (!dyn) return;
+  // sensor.rs:620-647 (force; torque at the joint anchor, tau - r_jc x F)
+  // and :1030-1087 (accelerometer, the link branch: the spatial acceleration
+  // made classical with w x v, then the site's point acceleration less g)
+  const V3 grav = v3(g.dtg[cap + w], g.dtg[2 * cap + w], g.dtg[3 * cap + w]);
+  int o = 0;
+  for (int k = 0; k < ns; ++k) {
+    const newt_sensor_desc& s = S[k];
+    const int dim = sensor_dim(s.kind);
+    if (!dyn_sensor(s.kind)) { o += dim; continue; }
+    const int l = s.index;
+    const float* d = dyn + ((size_t)t * L + l) * 18;
+    const V3 vw = v3(d[0], d[1], d[2]), vv = v3(d[3], d[4], d[5]), aw = v3(d[6], d[7], d[8]), av = v3(d[9], d[10], d[11]);
+    const V3 ft = v3(d[12], d[13], d[14]), ff = v3(d[15], d[16], d[17]);
+    V3 r;
+    if (s.kind == NEWT_SENSOR_FORCE) {
+      r = ff;
+    } else if (s.kind == NEWT_SENSOR_TORQUE) {
+      r = ft - cross(v3(g.jc[(3 * l) * cap + w], g.jc[(3 * l + 1) * cap + w], g.jc[(3 * l + 2) * cap + w]), ff);
+    } else {
+      const Q4 ori = O[l];
+      const V3 om = qrot(ori, vw), al = qrot(ori, aw), acom = qrot(ori, av + cross(vw, vv));
+      const V3 rs = qrot(ori, v3(s.local_pos[0], s.local_pos[1], s.local_pos[2]));
+      const V3 asite = acom + cross(al, rs) + cross(om, cross(om, rs));
+      r = qrot_inv(qmul(ori, Q4{s.local_quat[0], s.local_quat[1], s.local_quat[2], s.local_quat[3]}), asite - grav);
+    }
+    row[o] = r.x; row[o + 1] = r.y; row[o + 2] = r.z;
+    o += dim;
+  }
 }
 
 // Pile worlds: free-body poses and velocities from the world-major record.
@@ -188,6 +227,7 @@ int bad(newt_gpu_ctx* ctx, const char* msg) {
 }  // namespace
 
 extern "C" int newt_tree_bucket(int L);
+extern "C" void newt_launch_tree_sensor_dyn(const TreeGroupDev& g, const int* idx, int n, float* out, cudaStream_t st);
 extern "C" void newt_launch_pile_contact_sensors(const PileGroupDev& g, const int* idx, int n,
                                                  const newt_sensor_desc* S, int ns, float* out, int D,
                                                  cudaStream_t st);
@@ -201,12 +241,13 @@ int newt_gpu_read_sensors(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, co
   if (n == 0 || n_sensors == 0) return NEWT_OK;
   cudaSetDevice(ctx->device);
   int D = 0;
-  bool needs_resolve = false;
+  bool needs_resolve = false, needs_dyn = false;
   for (int k = 0; k < n_sensors; ++k) {
-    if (sensors[k].kind < NEWT_SENSOR_JOINTPOS || sensors[k].kind > NEWT_SENSOR_TOUCH)
+    if (sensors[k].kind < NEWT_SENSOR_JOINTPOS || sensors[k].kind > NEWT_SENSOR_TORQUE)
       return bad(ctx, "unknown sensor kind");
     D += sensor_dim(sensors[k].kind);
     needs_resolve = needs_resolve || contact_sensor(sensors[k].kind);
+    needs_dyn = needs_dyn || dyn_sensor(sensors[k].kind);
   }
   // validate every world against every sensor, and group the worlds
   std::vector<std::vector<int>> idx(ctx->groups.size()), rows(ctx->groups.size());
@@ -218,9 +259,12 @@ int newt_gpu_read_sensors(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, co
     const bool tree = m.kind != GK_PILE;
     for (int k = 0; k < n_sensors; ++k) {
       const newt_sensor_desc& d = sensors[k];
-      const bool link_only = d.kind <= NEWT_SENSOR_JOINTVEL || d.kind == NEWT_SENSOR_SUBTREECOM;
-      if (contact_sensor(d.kind) && tree)
-        return bad(ctx, "accelerometer and touch sensors are read on pile worlds (free bodies)");
+      const bool link_only = d.kind <= NEWT_SENSOR_JOINTVEL || d.kind == NEWT_SENSOR_SUBTREECOM ||
+                             d.kind == NEWT_SENSOR_FORCE || d.kind == NEWT_SENSOR_TORQUE;
+      if (d.kind == NEWT_SENSOR_TOUCH && tree) return bad(ctx, "touch sensors are read on pile worlds (free bodies)");
+      if (dyn_sensor(d.kind) && m.kind == GK_TREE_CONTACT)
+        return bad(ctx, "accelerometer, force and torque sensors on tree-contact worlds are not provided (they need "
+                        "the contact re-solve's link wrenches)");
       if ((d.on_link != 0) != tree || (link_only && !d.on_link))
         return bad(ctx, "sensor attachment does not match the world (links for trees, bodies for piles)");
       const int lim = d.kind == NEWT_SENSOR_TOUCH ? m.n_geoms : (tree ? m.n_links : m.n_bodies);
@@ -262,12 +306,20 @@ int newt_gpu_read_sensors(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, co
       }
     } else {
       const TreeGroupDev td = g->tree_dev();
-      switch (newt_tree_bucket(td.L)) {
-        case 8: tree_sensors_kernel<8><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D); break;
-        case 16: tree_sensors_kernel<16><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D); break;
-        case 32: tree_sensors_kernel<32><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D); break;
-        default: tree_sensors_kernel<65><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D); break;
+      float* dyn = nullptr;  // the links' dynamics pass, when a sensor reads it
+      if (needs_dyn) {
+        e = cudaMallocAsync(&dyn, sizeof(float) * 18 * (size_t)cnt * td.L, st);
+        if (e != cudaSuccess) break;
+        newt_launch_tree_sensor_dyn(td, dI + base, cnt, dyn, st);
+        ctx->launches += 1;
       }
+      switch (newt_tree_bucket(td.L)) {
+        case 8: tree_sensors_kernel<8><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn); break;
+        case 16: tree_sensors_kernel<16><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn); break;
+        case 32: tree_sensors_kernel<32><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn); break;
+        default: tree_sensors_kernel<65><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn); break;
+      }
+      if (dyn) cudaFreeAsync(dyn, st);
     }
     e = cudaGetLastError();
     ctx->launches += 1;

@@ -396,6 +396,69 @@ extern "C" int newt_tree_persistent_blocks_per_sm(int bucket) {
   return nb < 1 ? 1 : nb;
 }
 
+// The sensors' dynamics pass for trees without geoms (newt/src/sensor.rs:
+// 446-530, 834-1000): qddot from the explicit ABA at the world's current
+// state and generalised forces, no external wrenches; then per link its
+// spatial acceleration a_i = X_i a_parent + S_i qddot_i + v_i x S_i qdot_i
+// (compute_link_va, the velocities and products the ABA left in its
+// scratch) and the wrench its parent joint transmits, f_i = I_i a_i +
+// v_i x* I_i v_i - (0, m_i R_i^T g), children pulled into parents leaves to
+// root (compute_link_wrenches).  Writes 18 floats per link of each named
+// world: v (angular, linear), a, f (torque, force), link frame at the COM.
+template <int MAXL>
+__global__ void __launch_bounds__(64) tree_sensor_dyn_kernel(TreeGroupDev g, const int* idx, int n, float* out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int w = idx[t], cap = g.cap, nq = g.nq, nv = g.nv, L = g.L;
+  float q[MAXL + 6], qd[MAXL + 5], qf[MAXL + 5], qdd[MAXL + 5];
+  for (int k = 0; k < nq; ++k) q[k] = g.q[k * cap + w];
+  for (int k = 0; k < nv; ++k) { qd[k] = g.qd[k * cap + w]; qf[k] = g.qfrc[k * cap + w]; qdd[k] = 0.f; }
+  LinkScratch scr[MAXL];
+  tree_aba<MAXL>(g, w, q, qd, qf, qdd, scr, 0.f);
+  const V3 grav = v3(g.dtg[cap + w], g.dtg[2 * cap + w], g.dtg[3 * cap + w]);
+  SM6 a[MAXL];
+  SF6 f[MAXL];
+  V3 gb[MAXL];
+  for (int i = 0; i < L; ++i) {
+    const int parent = g.topo[4 * i], jt = g.topo[4 * i + 1], qo = g.topo[4 * i + 2], vo = g.topo[4 * i + 3];
+    const LinkScratch& s = scr[i];
+    if (i == 0) {
+      const Q4 ori = jt == JF ? Q4{q[qo + 3], q[qo + 4], q[qo + 5], q[qo + 6]}
+                              : Q4{g.rootq[w], g.rootq[cap + w], g.rootq[2 * cap + w], g.rootq[3 * cap + w]};
+      gb[0] = qrot_inv(ori, grav);
+      a[0] = jt == JF ? SM6{v3(qdd[vo], qdd[vo + 1], qdd[vo + 2]), v3(qdd[vo + 3], qdd[vo + 4], qdd[vo + 5])}
+                      : SM6{v3(0.f, 0.f, 0.f), v3(0.f, 0.f, 0.f)};
+    } else {
+      gb[i] = mv(s.X.E, gb[parent]);
+      const SM6 xa = px_motion(s.X, a[parent]);
+      a[i] = jt == JX ? xa : smadd(smadd(xa, smscale(s.S, qdd[vo])), s.c);
+    }
+    const float m = g.mass[i * cap + w];
+    ABI I;
+    I.A = S3{g.inert[(6 * i) * cap + w], g.inert[(6 * i + 1) * cap + w], g.inert[(6 * i + 2) * cap + w],
+             g.inert[(6 * i + 3) * cap + w], g.inert[(6 * i + 4) * cap + w], g.inert[(6 * i + 5) * cap + w]};
+    for (int r = 0; r < 3; ++r) for (int c = 0; c < 3; ++c) I.B.m[r][c] = 0.f;
+    I.C = S3{m, m, m, 0.f, 0.f, 0.f};
+    f[i] = sfsub(sfadd(abi_mul(I, a[i]), crf(s.v, abi_mul(I, s.v))), SF6{v3(0.f, 0.f, 0.f), gb[i] * m});
+  }
+  for (int i = L - 1; i >= 1; --i) f[g.topo[4 * i]] = sfadd(f[g.topo[4 * i]], px_force_T(scr[i].X, f[i]));
+  float* o = out + (size_t)t * L * 18;
+  for (int i = 0; i < L; ++i) {
+    const V3 vv[6] = {scr[i].v.w, scr[i].v.v, a[i].w, a[i].v, f[i].t, f[i].f};
+    for (int k = 0; k < 6; ++k) { o[18 * i + 3 * k] = vv[k].x; o[18 * i + 3 * k + 1] = vv[k].y; o[18 * i + 3 * k + 2] = vv[k].z; }
+  }
+}
+
+extern "C" void newt_launch_tree_sensor_dyn(const TreeGroupDev& g, const int* idx, int n, float* out, cudaStream_t st) {
+  const int grid = (n + 63) / 64;
+  if (grid == 0) return;
+  switch (newt_tree_bucket(g.L)) {
+#define X(M) case M: tree_sensor_dyn_kernel<M><<<grid, 64, 0, st>>>(g, idx, n, out); break;
+    NEWT_TREE_BUCKETS(X)
+#undef X
+  }
+}
+
 // Loads the plain-form kernels of every size bucket, so that their first
 // launch creates nothing on the device.  Returns the first CUDA error met.
 extern "C" cudaError_t newt_tree_prepare_kernels() {
