@@ -286,11 +286,14 @@ NEWT_API int newt_gpu_get_qacc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t 
  * with its solver, giving the body wrenches (F/m + g, Euler's equations) and
  * the normal forces (a contact's row impulses over dt).  A world read before
  * its first step sees no contacts.  ACCELEROMETER on a link, FORCE and
- * TORQUE are read on trees without geoms (sensor.rs:446-530, 620-647,
- * 834-1000): qddot from the explicit ABA at the current state with the
- * world's generalised forces, the links' spatial accelerations, and the RNE
- * wrench each parent joint transmits; on tree-contact worlds (which would
- * need the contact re-solve's link wrenches) they are refused. */
+ * TORQUE are read on trees (sensor.rs:446-530, 620-647, 834-1000): qddot
+ * from the explicit ABA at the current state with the world's generalised
+ * forces, the links' spatial accelerations, and the RNE wrench each parent
+ * joint transmits.  On tree-contact worlds the last step's contacts are
+ * first re-solved at the current state with the world's solver
+ * (world.rs:2252-2300, solver.rs:3334-3364): the rows' forces give each
+ * link's external wrench, which the ABA and the RNE take in, and each
+ * contact's normal force, which TOUCH sums. */
 #define NEWT_SENSOR_JOINTPOS 0
 #define NEWT_SENSOR_JOINTVEL 1
 #define NEWT_SENSOR_FRAMEPOS 2

@@ -300,8 +300,14 @@ bool solve_free_bodies_newton(const std::vector<Body<R>>& bodies, const std::vec
 // w.tree_body_wrenches; the per-row impulses go to `impulses_out` if given.
 template <class R>
 void solve_tree_contacts(World<R>& w, const std::vector<Contact<R>>& contacts, bool use_newton, bool implicit,
-                         std::vector<R>* impulses_out = nullptr) {
+                         std::vector<R>* impulses_out = nullptr, std::vector<Wrench<R>>* link_wrenches_out = nullptr,
+                         std::vector<R>* normal_forces_out = nullptr) {
   if (impulses_out) impulses_out->clear();
+  // the sensor inputs (solver.rs:3334-3364): each tree link's contact wrench
+  // (world force and torque about its COM) and each contact's normal force
+  if (link_wrenches_out && !w.trees.empty())
+    link_wrenches_out->assign(w.trees[0].links.size(), Wrench<R>{Vec3<R>(), Vec3<R>()});
+  if (normal_forces_out) normal_forces_out->assign(contacts.size(), R(0));
   if (contacts.empty() || w.dt <= R(0) || w.trees.empty()) return;
   const R dt = w.dt;
   const size_t ntr = w.trees.size(), nbd = w.bodies.size();
@@ -478,6 +484,13 @@ void solve_tree_contacts(World<R>& w, const std::vector<Contact<R>>& contacts, b
         }
   }
   if (impulses_out) *impulses_out = imp;
+  if (normal_forces_out)
+    for (const TBlock<R>& bk : blocks) {
+      R fn = R(0);
+      if (bk.condim == 3) for (int k = 0; k < 4; ++k) fn += imp[bk.start + k];
+      else fn = imp[bk.start];
+      (*normal_forces_out)[bk.contact] = fn / dt;
+    }
   for (int i = 0; i < n; ++i) {
     const R force = imp[i] / dt;
     for (const TComp<R>& cp : rows[i].comps) {
@@ -487,6 +500,10 @@ void solve_tree_contacts(World<R>& w, const std::vector<Contact<R>>& contacts, b
       }
       if (cp.tree >= 0)
         for (size_t s = 0; s < cp.coef.size(); ++s) w.tree_qfrc[cp.tree][s] += cp.coef[s] * force;
+      if (cp.tree >= 0 && link_wrenches_out) {
+        (*link_wrenches_out)[cp.link].f += cp.lin * force;
+        (*link_wrenches_out)[cp.link].t += cp.ang * force;
+      }
     }
   }
 }

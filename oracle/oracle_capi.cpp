@@ -259,11 +259,13 @@ template <class R> static int np_pair_t(int ka, const float* pa, const float* sa
   return buf.len;
 }
 
-// sensor.rs:834-1000 for a tree without external wrenches: qddot from the
+// sensor.rs:834-1000 for a tree under external link wrenches `ext_in` (world
+// force and torque about each COM; none: zero): qddot from the
 // explicit ABA at the state, each link's spatial velocity and acceleration
 // at its COM in its frame (compute_link_va: a_i = X_i a_parent + S_i qddot_i
 // + v_i x S_i qdot_i), and the wrench its parent joint transmits
-// (compute_link_wrenches: f_i = I_i a_i + v_i x* I_i v_i - (0, m_i R_i^T g),
+// (compute_link_wrenches: f_i = I_i a_i + v_i x* I_i v_i - (R_i^T t_ext,i,
+// R_i^T (f_ext,i + m_i g)),
 // each child's pulled into its parent, leaves to root).
 template <class R> struct LinkDyn { SMotion<R> v, a; SForce<R> f; };
 template <class R> SMotion<R> sm_add(const SMotion<R>& x, const SMotion<R>& y) { return {x.ang + y.ang, x.lin + y.lin}; }
@@ -275,9 +277,9 @@ template <class R> SForce<R> sf_cross(const SMotion<R>& x, const SForce<R>& f) {
   return {x.ang.cross(f.tau) + x.lin.cross(f.lin), x.ang.cross(f.lin)};
 }
 template <class R> void tree_link_dynamics(const Tree<R>& t, const std::vector<Pose<R>>& poses, Vec3<R> gravity,
-                                           std::vector<LinkDyn<R>>& out) {
+                                           std::vector<LinkDyn<R>>& out, const std::vector<Wrench<R>>* ext_in = nullptr) {
   const int n = (int)t.links.size();
-  std::vector<Wrench<R>> ext(n, Wrench<R>{Vec3<R>(), Vec3<R>()});
+  std::vector<Wrench<R>> ext = ext_in ? *ext_in : std::vector<Wrench<R>>(n, Wrench<R>{Vec3<R>(), Vec3<R>()});
   std::vector<R> qdd;
   aba(t, poses, gravity, ext, R(0), qdd);
   out.assign(n, LinkDyn<R>{});
@@ -304,7 +306,7 @@ template <class R> void tree_link_dynamics(const Tree<R>& t, const std::vector<P
     const Mat6<R> I = Mat6<R>::from_spatial_inertia(L.mass, Vec3<R>(), L.inertia);
     const SForce<R> ia = I.times_motion(out[i].a), iv = I.times_motion(out[i].v);
     const SForce<R> bias = sf_cross(out[i].v, iv);
-    const Vec3<R> fb = poses[i].o.inverse_rotate((Vec3<R>() + gravity * L.mass)), tb = poses[i].o.inverse_rotate(Vec3<R>());
+    const Vec3<R> fb = poses[i].o.inverse_rotate(ext[i].f + gravity * L.mass), tb = poses[i].o.inverse_rotate(ext[i].t);
     out[i].f = {(ia.tau + bias.tau) - tb, (ia.lin + bias.lin) - fb};
   }
   for (int i = n - 1; i >= 1; --i) {
@@ -607,6 +609,81 @@ int oracle_contact_sensors(const newt_model_desc* d, const float* qpos, const fl
       const Vec3<R> a_proper = a_site - w.gravity;
       const Vec3<R> v = (b.ori * lq).inverse_rotate(a_proper);
       out[o++] = (double)v.x; out[o++] = (double)v.y; out[o++] = (double)v.z;
+    }
+    get_state(w, qpos_out, qvel_out, 0);
+  };
+  if (precision == 0) go(0.0f); else go(0.0);
+  return rc;
+}
+
+// newt's post-step contact sensors for a tree-contact world (world.rs:
+// 1545-1701 build_sensor_inputs with solve_tree_contact_sensor_solution,
+// world.rs:2252-2274; sensor.rs:446-1112): one step from (qpos, qvel) with
+// the tree's applied forces `qfrc` (newt layout, nullable), then the step's
+// tree contacts re-solved at the post-step state with the world's solver
+// and integrator form, giving each link's contact wrench and each
+// contact's normal force (solver.rs:3334-3364).  Kinds: 9 accelerometer on
+// link `index`, 10 touch (geom `index`), 11 force and 12 torque at link
+// `index`'s parent joint (the links' dynamics under those wrenches); other
+// kinds read 0 here.  Writes the readings and the post-step state (MuJoCo
+// layout); returns -1 for a world without a tree.
+int oracle_tree_contact_sensors(const newt_model_desc* d, const float* qpos, const float* qvel, const float* qfrc,
+                                int precision, int ns, const int* si, const float* sf, double* out, double* qpos_out,
+                                double* qvel_out) {
+  int rc = 0;
+  auto go = [&](auto tag) {
+    using R = decltype(tag);
+    World<R> w = build_world<R>(*d);
+    if (w.trees.empty()) { rc = -1; return; }
+    w.integrator = d->integrator == NEWT_INTEGRATOR_RK4 ? 0 : 1;  // the model's own integrator
+    set_state(w, qpos, qvel, 0);
+    if (qfrc)
+      for (int k = 0; k < w.trees[0].nv(); ++k) w.trees[0].qfrc_applied[k] = qfrc[k];
+    std::vector<Contact<R>> contacts;
+    w.detect_contacts(contacts);
+    w.step();
+    std::vector<Contact<R>> tc;
+    for (const Contact<R>& c : contacts)
+      if (w.geoms[c.ga].att_kind() == 2 || w.geoms[c.gb].att_kind() == 2) tc.push_back(c);
+    w.tree_qfrc.assign(w.trees.size(), std::vector<R>());
+    for (size_t t = 0; t < w.trees.size(); ++t) w.tree_qfrc[t].assign(w.trees[t].nv(), R(0));
+    w.tree_body_wrenches.assign(w.bodies.size(), Wrench<R>{Vec3<R>(), Vec3<R>()});
+    std::vector<Wrench<R>> lw;
+    std::vector<R> fn;
+    solve_tree_contacts<R>(w, tc, w.solver_mode == M_NEWTON, w.integrator == 1, nullptr, &lw, &fn);
+    if (lw.empty()) lw.assign(w.trees[0].links.size(), Wrench<R>{Vec3<R>(), Vec3<R>()});
+    std::vector<Pose<R>> poses;
+    forward_kinematics(w.trees[0], poses);
+    std::vector<LinkDyn<R>> dyn;
+    tree_link_dynamics(w.trees[0], poses, w.gravity, dyn, &lw);
+    int o = 0;
+    for (int k = 0; k < ns; ++k) {
+      const int kind = si[3 * k], idx = si[3 * k + 2];
+      const Vec3<R> lp(sf[7 * k], sf[7 * k + 1], sf[7 * k + 2]);
+      const Quat<R> lq(sf[7 * k + 3], sf[7 * k + 4], sf[7 * k + 5], sf[7 * k + 6]);
+      auto put3 = [&](Vec3<R> x) { out[o++] = (double)x.x; out[o++] = (double)x.y; out[o++] = (double)x.z; };
+      if (kind == 10) {  // touch_reading (sensor.rs:1103-1112)
+        R sum = R(0);
+        for (size_t c = 0; c < tc.size(); ++c)
+          if (tc[c].ga == idx || tc[c].gb == idx) sum += fn[c] < R(0) ? -fn[c] : fn[c];
+        out[o++] = (double)sum;
+      } else if (kind == 11) {
+        put3(dyn[idx].f.lin);
+      } else if (kind == 12) {
+        put3(dyn[idx].f.tau - w.trees[0].links[idx].jc_pos.cross(dyn[idx].f.lin));
+      } else if (kind == 9) {
+        const Quat<R> ori = poses[idx].o;
+        const SMotion<R>& vb = dyn[idx].v;
+        const SMotion<R>& ab = dyn[idx].a;
+        const Vec3<R> om = ori.rotate(vb.ang), al = ori.rotate(ab.ang);
+        const Vec3<R> acom = ori.rotate(ab.lin + vb.ang.cross(vb.lin));
+        const Vec3<R> r = ori.rotate(lp);
+        const Vec3<R> asite = acom + al.cross(r) + om.cross(om.cross(r));
+        put3((ori * lq).inverse_rotate(asite - w.gravity));
+      } else {
+        const int dim = kind <= 1 ? 1 : (kind == 3 ? 4 : 3);
+        for (int j = 0; j < dim; ++j) out[o++] = 0.0;
+      }
     }
     get_state(w, qpos_out, qvel_out, 0);
   };

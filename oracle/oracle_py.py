@@ -47,6 +47,8 @@ def lib():
         L.oracle_sensors.argtypes = [P, P, P, P, C.c_int, C.c_int, P, P, P]
         L.oracle_sensors.restype = C.c_int
         L.oracle_contact_sensors.argtypes = [P, P, P, C.c_int, C.c_int, P, P, P, P, P]
+        L.oracle_tree_contact_sensors.argtypes = [P, P, P, P, C.c_int, C.c_int, P, P, P, P, P]
+        L.oracle_tree_contact_sensors.restype = C.c_int
         L.oracle_contact_sensors.restype = C.c_int
         L.oracle_ccd_pair.argtypes = [C.c_int, C.c_int, P, P, C.c_int, P, P, C.c_float, C.c_float, P]
         L.oracle_ccd_pair.restype = C.c_int
@@ -150,6 +152,29 @@ def contact_sensors(packed, index: int, qpos: np.ndarray, qvel: np.ndarray, sens
         raise ValueError("contact sensors take free-body worlds (and a positive definite Newton factor)")
     return out, qo, vo
 
+
+def tree_contact_sensors(packed, index: int, qpos: np.ndarray, qvel: np.ndarray, sens: np.ndarray, precision: int = 1,
+                         qfrc: Optional[np.ndarray] = None):
+    """newt's post-step contact sensors of one tree-contact world: one step
+    from (qpos, qvel) (MuJoCo layout) with the tree's applied forces `qfrc`,
+    the step's tree contacts re-solved at the post-step state; kinds 9
+    accelerometer on a link, 10 touch, 11 force, 12 torque (others read 0).
+    Returns the readings and the post-step (qpos, qvel)."""
+    qpos = np.ascontiguousarray(qpos, dtype=np.float32)
+    qvel = np.ascontiguousarray(qvel, dtype=np.float32)
+    qfrc = None if qfrc is None else np.ascontiguousarray(qfrc, dtype=np.float32)
+    si = np.ascontiguousarray(np.stack([sens["kind"], sens["on_link"], sens["index"]], 1), np.int32)
+    sf = np.ascontiguousarray(np.concatenate([sens["local_pos"], sens["local_quat"]], 1), np.float32)
+    D = int(sum(1 if (k <= 1 or k == 10) else (4 if k == 3 else 3) for k in sens["kind"]))
+    out = np.zeros(D, dtype=np.float64)
+    qo = np.zeros(len(qpos), np.float64)
+    vo = np.zeros(len(qvel), np.float64)
+    d = C.cast(C.byref(packed.descs[index]), C.c_void_p)
+    rc = lib().oracle_tree_contact_sensors(d, _ptr(qpos), _ptr(qvel), _ptr(qfrc), precision, len(sens), _ptr(si),
+                                           _ptr(sf), _ptr(out), _ptr(qo), _ptr(vo))
+    if rc != 0:
+        raise RuntimeError("oracle_tree_contact_sensors failed")
+    return out, qo, vo
 
 def sensors(packed, index: int, qpos: np.ndarray, qvel: np.ndarray, sens: np.ndarray, precision: int = 1,
             qfrc: Optional[np.ndarray] = None) -> np.ndarray:

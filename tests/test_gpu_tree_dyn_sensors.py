@@ -9,7 +9,9 @@ accelerometer paths within 1e-3) and the FP64 oracle within 1e-4 there; on
 64 seven-link chains with random joint torques and on floating trees with a
 swinging arm, every reading no further from the FP64 oracle than twice
 newt's own f32 arithmetic, or within 1e-4 of the reading's size (floor 1)
-where newt's is closer; the forms the GPU refuses are refused."""
+where newt's is closer; the forms the GPU refuses (touch on a tree without
+geoms, force sensors on bodies) are refused.  Tree-contact worlds:
+tests/test_gpu_tree_contact_sensors.py."""
 import numpy as np
 import pytest
 
@@ -140,12 +142,6 @@ class _Offsets:
 
 
 def test_refusals(eng):
-    b = scenes.quadruped_batch(n_worlds=2, first_world=10, solver=M.SOLVER_NEWTON)
-    slots = eng.alloc(eng.upload(b))
-    eng.set_state(slots, b.qpos, b.qvel)
-    with pytest.raises(NewtError):  # tree-contact worlds would need the contact re-solve's link wrenches
-        eng.read_sensors(slots, A.sensors((A.SENSOR_FORCE, 1, 3)))
-    eng.free(slots)
     c = scenes.chain_batch(n_worlds=2, first_world=5)
     slots = eng.alloc(eng.upload(c))
     with pytest.raises(NewtError):

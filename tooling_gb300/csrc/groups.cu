@@ -562,5 +562,7 @@ TcGroupDev HostGroup::tc_dev() const {
   d.iters = dI + (size_t)ri_iters * cap;
   d.scr = (float*)plain_scratch;
   d.sstride = scr_stride;
+  d.sens = nullptr;
+  d.sens_stride = 0;
   return d;
 }

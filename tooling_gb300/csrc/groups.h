@@ -61,6 +61,12 @@ struct TcGroupDev {
   const int* iters;  // per world
   float* scr;        // world-major solver scratch
   long sstride;      // floats per world in `scr`
+  // the contact sensors' re-solve (null in a step): the last step's contacts
+  // solved again at the current state; per world (stride `sens_stride`)
+  // each link's contact wrench (world force, torque about its COM), then per
+  // contact slot (geom a, geom b as int bits, normal force), then the count
+  float* sens;
+  long sens_stride;
 };
 
 // Field offsets (in floats / ints) inside one pile world's record.

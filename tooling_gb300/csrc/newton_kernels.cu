@@ -111,6 +111,19 @@ static __device__ __noinline__ int np_link_pair(int sa, int sb, GPose pa, GPose 
   return 0;  // refused at upload
 }
 
+// A contact row's direction: the normal, or facet f of the pyramid,
+// n +- mu t1, n +- mu t2 (solver.rs:3401-3429, tangent_basis world.rs:3104-3112).
+NEWT_D V3 row_direction(const float* cc, int f) {
+  const V3 n = v3(cc[K_N], cc[K_N + 1], cc[K_N + 2]);
+  if (f < 0) return n;
+  const float mu = cc[K_MU];
+  const V3 ref = fabsf(n.z) < 0.9f ? v3(0.f, 0.f, 1.f) : v3(1.f, 0.f, 0.f);
+  V3 t1 = cross(ref, n);
+  t1 = t1 * (1.f / sqrtf(len2(t1)));
+  const V3 t = f < 2 ? t1 : cross(n, t1);
+  return n + t * ((f & 1) ? -mu : mu);
+}
+
 NEWT_D Q4 q_axis_angle(V3 axis, float angle) {  // math.rs:574-580
   const float l = sqrtf(len2(axis));
   const V3 a = l > 0.f ? axis * (1.f / l) : v3(0.f, 0.f, 0.f);
@@ -403,7 +416,8 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   //      when the tree collides with itself): lane per pair, a warp scan
   //      places each pair's contacts ----
   float* con = wf + lay.con;
-  int ncon = 0;
+  const bool resolve = G.sens != nullptr;  // the contact sensors' re-solve: the last step's contacts, no detection
+  int ncon = resolve ? min(max(__float_as_int(wf[lay.misc]), 0), G.maxc) : 0;
   bool overflow = false;
   auto link_geom_pose = [&](int gi) {
     const float* lp = pose + 7 * G.gtopo[2 * gi + 1];
@@ -413,7 +427,7 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
     gp.q = qmul(lo, Q4{gv(gi, G_QUAT), gv(gi, G_QUAT + 1), gv(gi, G_QUAT + 2), gv(gi, G_QUAT + 3)});
     return gp;
   };
-  for (int base = 0; base < G.npairs; base += 32) {
+  for (int base = 0; base < (resolve ? 0 : G.npairs); base += 32) {
     const int pi = base + lane;
     CRes cr[4];
     int nc = 0, a = 0, b = 0, link = 0, link2 = -1;
@@ -517,14 +531,58 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
     }
     nrows += __shfl_sync(FULL, incl, 31);
   }
-  if (lane == 0) {
+  if (lane == 0 && !resolve) {
     wf[lay.misc] = __int_as_float(ncon);
     wf[lay.misc + 1] = __int_as_float(nrows);
     wf[lay.misc + 2] = __int_as_float(0);
   }
   const int nr = nrows;
+  // the re-solve's sensor inputs (solver.rs:3334-3364): per link the rows'
+  // forces f / dt times their wrench axes (dir x sign, (p - c_link) x
+  // dir x sign), in row order; per contact the facets' impulses summed (a
+  // normal row's own) over dt
+  auto sens_out = [&](int nrow) {
+    float* so = G.sens + (size_t)w * G.sens_stride;
+    for (int l = lane; l < L; l += 32) {
+      V3 fs = v3(0.f, 0.f, 0.f), ts = v3(0.f, 0.f, 0.f);
+      const V3 cl = ldv3(pose + 7 * l);
+      for (int r = 0; r < nrow; ++r) {
+        const float* cc = con + CREC * rcon[r];
+        const int l1 = __float_as_int(cc[K_LINK]), l2 = __float_as_int(cc[K_LINK2]);
+        if (l1 != l && l2 != l) continue;
+        const V3 dir = row_direction(cc, rfac[r]), pt = ldv3(cc + K_POS);
+        const float force = vx[r] / dt;
+        if (l1 == l) {
+          const V3 d = dir * cc[K_SIGN];
+          fs = fs + d * force;
+          ts = ts + cross(pt - cl, d) * force;
+        }
+        if (l2 == l) {
+          const V3 d = dir * -1.f;
+          fs = fs + d * force;
+          ts = ts + cross(pt - cl, d) * force;
+        }
+      }
+      stv3(so + 6 * l, fs);
+      stv3(so + 6 * l + 3, ts);
+    }
+    for (int c = lane; c < ncon; c += 32) {
+      const float* cc = con + CREC * c;
+      const int row = __float_as_int(cc[K_ROW]);
+      float fnorm = 0.f;
+      if (row >= 0 && row < nrow) {
+        if (rfac[row] >= 0) for (int k = 0; k < 4; ++k) fnorm += vx[row + k];
+        else fnorm = vx[row];
+      }
+      so[6 * L + 3 * c] = cc[K_GA];
+      so[6 * L + 3 * c + 1] = cc[K_GB];
+      so[6 * L + 3 * c + 2] = fnorm / dt;
+    }
+    if (lane == 0) so[6 * L + 3 * G.maxc] = __int_as_float(ncon);
+  };
   if (nr == 0) {  // no active contact: qacc stays a_free
-    if (lane == 0 && status) atomicOr(g.status + w, status);
+    if (resolve) sens_out(0);
+    else if (lane == 0 && status) atomicOr(g.status + w, status);
     return;
   }
 
@@ -644,17 +702,9 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
     const int link = __float_as_int(cc[K_LINK]), link2 = __float_as_int(cc[K_LINK2]);
     tw[link] = 1.f;
     if (link2 >= 0) tw[link2] = 1.f;
-    const float sign = cc[K_SIGN], mu = cc[K_MU];
-    const V3 n = ldv3(cc + K_N), pt = ldv3(cc + K_POS);
-    V3 dir = n;
-    const int f = rfac[r];
-    if (f >= 0) {  // pyramidal facets n +- mu t1, n +- mu t2 (solver.rs:3401-3429)
-      const V3 ref = fabsf(n.z) < 0.9f ? v3(0.f, 0.f, 1.f) : v3(1.f, 0.f, 0.f);  // tangent_basis
-      V3 t1 = cross(ref, n);
-      t1 = t1 * (1.f / sqrtf(len2(t1)));
-      const V3 t = f < 2 ? t1 : cross(n, t1);
-      dir = n + t * ((f & 1) ? -mu : mu);
-    }
+    const float sign = cc[K_SIGN];
+    const V3 pt = ldv3(cc + K_POS);
+    const V3 dir = row_direction(cc, rfac[r]);
     for (int k = 0; k < nv; ++k) Jt[(size_t)k * ldj + r] = 0.f;
     chain_columns(g, w, pose, link, pt, [&](int k, V3, V3 tr) { Jt[(size_t)k * ldj + r] = dot(tr, dir) * sign; });
     if (link2 >= 0)  // side b of an in-tree pair: the columns its chain shares with side a's take both
@@ -765,6 +815,10 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
                                   &status);
   }
   __syncwarp();
+  if (resolve) {  // the sensors' inputs only: the step's impulses and accelerations stay as they were
+    sens_out(nr);
+    return;
+  }
 
   // ---- outputs: impulses, J^T f / dt, qacc = a_free + (M + dt B)^-1 J^T f / dt ----
   // Refined trees form the contact force from the kept J^T: Y = L^-1 J^T
@@ -917,6 +971,34 @@ extern "C" int newt_tc_launch(newt_gpu_ctx* ctx, HostGroup* g, int n_steps, cuda
   }
   return timed ? n_steps : 0;
 }
+
+// The contact sensors' re-solve of every world of a tree-contact group at
+// its current state (newt's build_sensor_inputs, world.rs:1545-1701, with
+// solve_tree_contact_sensor_solution, world.rs:2252-2274): a_free at the
+// state into `afree` (cap x nv, as the step's solve sees it; the group's own
+// qacc rows stay the last step's), then tc_k_solve on the last step's
+// contacts writing each link's contact wrench and each contact's normal
+// force to `sens` (TcGroupDev::sens, `sens_stride` floats per world).
+// `cfrc` (cap x nv floats) takes the RK4 worlds' held force.  Returns the
+// launches issued on `st`.
+extern "C" int newt_tc_resolve(newt_gpu_ctx* ctx, HostGroup* g, float* sens, long sens_stride, float* afree,
+                               float* cfrc, cudaStream_t st) {
+  if (g->n == 0) return 0;
+  if (newt_tc_prepare(ctx, g, 0) != NEWT_OK) return -1;
+  TcGroupDev d = g->tc_dev();
+  d.t.qacc = afree;
+  d.t.cfrc = cfrc;
+  d.t.cstride = g->nv;
+  d.sens = sens;
+  d.sens_stride = sens_stride;
+  newt_launch_tree_aba(d.t, st);
+  newt_launch_tc_solve(d, st);
+  return 2;
+}
+
+// Floats per world of the re-solve's output for a group of `L` links and
+// contact capacity `maxc`.
+extern "C" long newt_tc_sens_stride(int L, int maxc) { return (6L * L + 3L * maxc + 1 + 3) / 4 * 4; }
 
 // n_steps env-steps of one tree-contact group on the context's stream (the
 // plain form).

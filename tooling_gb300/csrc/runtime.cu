@@ -358,6 +358,19 @@ int newt_gpu_alloc_worlds(newt_gpu_ctx* ctx, const int32_t* model_ids, int32_t n
     }
     rc = g->flush_model(ctx);
     if (rc != NEWT_OK) return undo(rc);
+    if (g->kind == GK_TREE_CONTACT && g->plain_scratch) {
+      // a new world has no contacts until it steps: the contact sensors'
+      // re-solve reads the slot's stored contact count.  Indices past the
+      // scratch's current extent (the group grew) get a zeroed scratch when
+      // it is next sized.
+      int o_con, o_imp, o_misc;
+      newt_tc_offsets(g->size, g->nv, g->ng, g->maxc, &o_con, &o_imp, &o_misc);
+      const size_t held = g->scr_stride > 0 ? g->plain_scratch_bytes / (sizeof(float) * (size_t)g->scr_stride) : 0;
+      for (int i : idx)
+        if ((size_t)i < held && cudaMemsetAsync((float*)g->plain_scratch + (size_t)i * g->scr_stride + o_misc, 0,
+                                                sizeof(int), ctx->stream) != cudaSuccess)
+          return undo(fail(ctx, NEWT_E_CUDA, "alloc_worlds: clearing the contact list"));
+    }
   }
   return finish(NEWT_OK);
 }

@@ -4,8 +4,10 @@
 // readings on pile worlds come from newt's post-step contact re-solve
 // (pile_kernels.cu: pile_k_reassemble, the solvers, then
 // pile_contact_sensors_kernel), run for the group before its sensors;
-// accelerometer, force and torque readings on trees without geoms from the
-// links' dynamics pass (tree_kernels.cu: tree_sensor_dyn_kernel).
+// accelerometer, force and torque readings on trees from the links' dynamics
+// pass (tree_kernels.cu: tree_sensor_dyn_kernel), on tree-contact worlds
+// under the wrenches of the contact re-solve (newton_kernels.cu:
+// newt_tc_resolve), which also gives their touch readings.
 //
 // Restates, for FP32 on sm_103a:
 //   newt/src/sensor.rs:560-700   evaluate (JointPos, JointVel, FramePos,
@@ -92,12 +94,17 @@ NEWT_D void write_sensors(const newt_sensor_desc* S, int ns, const Frame* frames
 // Tree worlds (trees without geoms and tree-contact worlds): newt layout q/qd
 // in the group's SoA rows.  Frames for link sensors and subtree centres are
 // collected per sensor as the links are walked.
-// `dyn` (trees without geoms, when an accelerometer, force or torque sensor
-// is asked for): the links' dynamics pass, 18 floats per link of each world.
+// `dyn` (when an accelerometer, force or torque sensor is asked for): the
+// links' dynamics pass, 18 floats per link of each world.  `sens`
+// (tree-contact worlds, when a contact-dependent sensor is asked for): the
+// contact re-solve's output (newt_tc_resolve), `sens_stride` floats per
+// world, its contact list after 6 L floats of link wrenches, the count at
+// 6 L + 3 maxc.
 template <int MAXL>
 __global__ void __launch_bounds__(64) tree_sensors_kernel(TreeGroupDev g, const int* idx, int n,
                                                          const newt_sensor_desc* S, int ns, float* out, int D,
-                                                         const float* dyn) {
+                                                         const float* dyn, const float* sens, long sens_stride,
+                                                         int maxc) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   const int w = idx[t], cap = g.cap, L = g.L;
@@ -170,6 +177,22 @@ __global__ void __launch_bounds__(64) tree_sensors_kernel(TreeGroupDev g, const 
   }
   float* row = out + (size_t)t * D;
   write_sensors(S, ns, fr, q, qd, qoff, voff, row, com);
+  if (sens) {  // touch: the re-solved normal forces of the geom's contacts (sensor.rs:1103-1112)
+    const float* so = sens + (size_t)w * sens_stride;
+    const int nc = min(max(__float_as_int(so[6 * L + 3 * maxc]), 0), maxc);
+    int o = 0;
+    for (int k = 0; k < ns; ++k) {
+      if (S[k].kind == NEWT_SENSOR_TOUCH) {
+        float sum = 0.f;
+        for (int c = 0; c < nc; ++c) {
+          const float* cc = so + 6 * L + 3 * c;
+          if (__float_as_int(cc[0]) == S[k].index || __float_as_int(cc[1]) == S[k].index) sum += fabsf(cc[2]);
+        }
+        row[o] = sum;
+      }
+      o += sensor_dim(S[k].kind);
+    }
+  }
   if (!dyn) return;
   // sensor.rs:620-647 (force; torque at the joint anchor, tau - r_jc x F)
   // and :1030-1087 (accelerometer, the link branch: the spatial acceleration
@@ -227,7 +250,11 @@ int bad(newt_gpu_ctx* ctx, const char* msg) {
 }  // namespace
 
 extern "C" int newt_tree_bucket(int L);
-extern "C" void newt_launch_tree_sensor_dyn(const TreeGroupDev& g, const int* idx, int n, float* out, cudaStream_t st);
+extern "C" void newt_launch_tree_sensor_dyn(const TreeGroupDev& g, const int* idx, int n, float* out, const float* sens,
+                                            long sens_stride, cudaStream_t st);
+extern "C" int newt_tc_resolve(newt_gpu_ctx* ctx, HostGroup* g, float* sens, long sens_stride, float* afree,
+                               float* cfrc, cudaStream_t st);
+extern "C" long newt_tc_sens_stride(int L, int maxc);
 extern "C" void newt_launch_pile_contact_sensors(const PileGroupDev& g, const int* idx, int n,
                                                  const newt_sensor_desc* S, int ns, float* out, int D,
                                                  cudaStream_t st);
@@ -261,10 +288,8 @@ int newt_gpu_read_sensors(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, co
       const newt_sensor_desc& d = sensors[k];
       const bool link_only = d.kind <= NEWT_SENSOR_JOINTVEL || d.kind == NEWT_SENSOR_SUBTREECOM ||
                              d.kind == NEWT_SENSOR_FORCE || d.kind == NEWT_SENSOR_TORQUE;
-      if (d.kind == NEWT_SENSOR_TOUCH && tree) return bad(ctx, "touch sensors are read on pile worlds (free bodies)");
-      if (dyn_sensor(d.kind) && m.kind == GK_TREE_CONTACT)
-        return bad(ctx, "accelerometer, force and torque sensors on tree-contact worlds are not provided (they need "
-                        "the contact re-solve's link wrenches)");
+      if (d.kind == NEWT_SENSOR_TOUCH && m.kind == GK_TREE)
+        return bad(ctx, "touch sensors read worlds with contacts (piles, tree-contact worlds)");
       if ((d.on_link != 0) != tree || (link_only && !d.on_link))
         return bad(ctx, "sensor attachment does not match the world (links for trees, bodies for piles)");
       const int lim = d.kind == NEWT_SENSOR_TOUCH ? m.n_geoms : (tree ? m.n_links : m.n_bodies);
@@ -306,20 +331,39 @@ int newt_gpu_read_sensors(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, co
       }
     } else {
       const TreeGroupDev td = g->tree_dev();
+      // tree-contact worlds: the last step's contacts re-solved at the
+      // current state, for the touch readings and as the links' external
+      // wrenches in the dynamics pass
+      float *sens = nullptr, *afree = nullptr, *cfrc = nullptr;
+      long sstride = 0;
+      if (g->kind == GK_TREE_CONTACT && (needs_dyn || needs_resolve)) {
+        sstride = newt_tc_sens_stride(td.L, g->maxc);
+        e = cudaMallocAsync(&sens, sizeof(float) * (size_t)sstride * g->cap, st);
+        if (e == cudaSuccess) e = cudaMallocAsync(&afree, sizeof(float) * (size_t)g->nv * g->cap, st);
+        if (e == cudaSuccess) e = cudaMallocAsync(&cfrc, sizeof(float) * (size_t)g->nv * g->cap, st);
+        if (e != cudaSuccess) break;
+        const int nl = newt_tc_resolve(ctx, g, sens, sstride, afree, cfrc, st);
+        if (nl < 0) { resolve_rc = NEWT_E_CUDA; break; }
+        ctx->launches += nl;
+      }
       float* dyn = nullptr;  // the links' dynamics pass, when a sensor reads it
       if (needs_dyn) {
         e = cudaMallocAsync(&dyn, sizeof(float) * 18 * (size_t)cnt * td.L, st);
         if (e != cudaSuccess) break;
-        newt_launch_tree_sensor_dyn(td, dI + base, cnt, dyn, st);
+        newt_launch_tree_sensor_dyn(td, dI + base, cnt, dyn, sens, sstride, st);
         ctx->launches += 1;
       }
+      const int mc = g->maxc;
       switch (newt_tree_bucket(td.L)) {
-        case 8: tree_sensors_kernel<8><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn); break;
-        case 16: tree_sensors_kernel<16><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn); break;
-        case 32: tree_sensors_kernel<32><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn); break;
-        default: tree_sensors_kernel<65><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn); break;
+        case 8: tree_sensors_kernel<8><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn, sens, sstride, mc); break;
+        case 16: tree_sensors_kernel<16><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn, sens, sstride, mc); break;
+        case 32: tree_sensors_kernel<32><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn, sens, sstride, mc); break;
+        default: tree_sensors_kernel<65><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn, sens, sstride, mc); break;
       }
       if (dyn) cudaFreeAsync(dyn, st);
+      if (sens) cudaFreeAsync(sens, st);
+      if (afree) cudaFreeAsync(afree, st);
+      if (cfrc) cudaFreeAsync(cfrc, st);
     }
     e = cudaGetLastError();
     ctx->launches += 1;

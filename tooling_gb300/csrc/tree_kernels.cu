@@ -37,9 +37,11 @@ struct LinkScratch {
 // layout; writes qdd.  `scr` is MAXL entries of per-link scratch.
 // `idt`: the step folded into the joint damping (dt for semi-implicit Euler,
 // 0 for the explicit RK4 stages).
+// `extb` (nullable): external wrenches per link, link frame at the COM
+// (torque, force), beside gravity.
 template <int MAXL>
 __device__ bool tree_aba(const TreeGroupDev& g, int w, const float* q, const float* qd, const float* qfrc,
-                         float* qdd, LinkScratch* scr, float idt) {
+                         float* qdd, LinkScratch* scr, float idt, const SF6* extb = nullptr) {
   const int L = g.L, cap = g.cap;
   const float dt = idt;
   const V3 grav = v3(g.dtg[cap + w], g.dtg[2 * cap + w], g.dtg[3 * cap + w]);
@@ -100,6 +102,7 @@ __device__ bool tree_aba(const TreeGroupDev& g, int w, const float* q, const flo
     s.IA.C = S3{m, m, m, 0.f, 0.f, 0.f};
     SF6 Iv = abi_mul(s.IA, s.v);
     SF6 ext{v3(0.f, 0.f, 0.f), gb[i] * m};
+    if (extb) ext = sfadd(ext, extb[i]);
     s.pA = sfsub(crf(s.v, Iv), ext);
   }
   // ---- pass 2 (leaves -> root): articulated inertias and biases ----
@@ -405,16 +408,44 @@ extern "C" int newt_tree_persistent_blocks_per_sm(int bucket) {
 // v_i x* I_i v_i - (0, m_i R_i^T g), children pulled into parents leaves to
 // root (compute_link_wrenches).  Writes 18 floats per link of each named
 // world: v (angular, linear), a, f (torque, force), link frame at the COM.
+// `sens` (nullable; tree-contact worlds): the contact re-solve's output
+// (newt_tc_resolve), whose per-link wrenches (world force and torque about
+// each COM, the first 6 L floats of each world's `sens_stride`) act as
+// external wrenches in both passes.
 template <int MAXL>
-__global__ void __launch_bounds__(64) tree_sensor_dyn_kernel(TreeGroupDev g, const int* idx, int n, float* out) {
+__global__ void __launch_bounds__(64) tree_sensor_dyn_kernel(TreeGroupDev g, const int* idx, int n, float* out,
+                                                             const float* sens, long sens_stride) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   const int w = idx[t], cap = g.cap, nq = g.nq, nv = g.nv, L = g.L;
   float q[MAXL + 6], qd[MAXL + 5], qf[MAXL + 5], qdd[MAXL + 5];
   for (int k = 0; k < nq; ++k) q[k] = g.q[k * cap + w];
   for (int k = 0; k < nv; ++k) { qd[k] = g.qd[k * cap + w]; qf[k] = g.qfrc[k * cap + w]; qdd[k] = 0.f; }
+  SF6 extb[MAXL];  // the contact wrenches in each link's frame (orientations by forward kinematics)
+  if (sens) {
+    const float* so = sens + (size_t)w * sens_stride;
+    Q4 O[MAXL];
+    for (int i = 0; i < L; ++i) {
+      const int parent = g.topo[4 * i], jt = g.topo[4 * i + 1], qo = g.topo[4 * i + 2];
+      if (i == 0) {
+        O[0] = jt == JF ? Q4{q[qo + 3], q[qo + 4], q[qo + 5], q[qo + 6]}
+                        : Q4{g.rootq[w], g.rootq[cap + w], g.rootq[2 * cap + w], g.rootq[3 * cap + w]};
+      } else if (jt == JH) {
+        const V3 ax = v3(g.axis[(3 * i) * cap + w], g.axis[(3 * i + 1) * cap + w], g.axis[(3 * i + 2) * cap + w]);
+        const float an = sqrtf(len2(ax));
+        const V3 a = an > 0.f ? ax * (1.f / an) : v3(0.f, 0.f, 0.f);
+        float sn, cs;
+        sincosf(q[qo] * 0.5f, &sn, &cs);
+        O[i] = qmul(O[parent], Q4{a.x * sn, a.y * sn, a.z * sn, cs});
+      } else {
+        O[i] = O[parent];  // slide and fixed joints with identity joint frames
+      }
+      extb[i] = SF6{qrot_inv(O[i], v3(so[6 * i + 3], so[6 * i + 4], so[6 * i + 5])),
+                    qrot_inv(O[i], v3(so[6 * i], so[6 * i + 1], so[6 * i + 2]))};
+    }
+  }
   LinkScratch scr[MAXL];
-  tree_aba<MAXL>(g, w, q, qd, qf, qdd, scr, 0.f);
+  tree_aba<MAXL>(g, w, q, qd, qf, qdd, scr, 0.f, sens ? extb : nullptr);
   const V3 grav = v3(g.dtg[cap + w], g.dtg[2 * cap + w], g.dtg[3 * cap + w]);
   SM6 a[MAXL];
   SF6 f[MAXL];
@@ -439,7 +470,9 @@ __global__ void __launch_bounds__(64) tree_sensor_dyn_kernel(TreeGroupDev g, con
              g.inert[(6 * i + 3) * cap + w], g.inert[(6 * i + 4) * cap + w], g.inert[(6 * i + 5) * cap + w]};
     for (int r = 0; r < 3; ++r) for (int c = 0; c < 3; ++c) I.B.m[r][c] = 0.f;
     I.C = S3{m, m, m, 0.f, 0.f, 0.f};
-    f[i] = sfsub(sfadd(abi_mul(I, a[i]), crf(s.v, abi_mul(I, s.v))), SF6{v3(0.f, 0.f, 0.f), gb[i] * m});
+    SF6 fe{v3(0.f, 0.f, 0.f), gb[i] * m};
+    if (sens) fe = sfadd(fe, extb[i]);
+    f[i] = sfsub(sfadd(abi_mul(I, a[i]), crf(s.v, abi_mul(I, s.v))), fe);
   }
   for (int i = L - 1; i >= 1; --i) f[g.topo[4 * i]] = sfadd(f[g.topo[4 * i]], px_force_T(scr[i].X, f[i]));
   float* o = out + (size_t)t * L * 18;
@@ -449,11 +482,12 @@ __global__ void __launch_bounds__(64) tree_sensor_dyn_kernel(TreeGroupDev g, con
   }
 }
 
-extern "C" void newt_launch_tree_sensor_dyn(const TreeGroupDev& g, const int* idx, int n, float* out, cudaStream_t st) {
+extern "C" void newt_launch_tree_sensor_dyn(const TreeGroupDev& g, const int* idx, int n, float* out, const float* sens,
+                                            long sens_stride, cudaStream_t st) {
   const int grid = (n + 63) / 64;
   if (grid == 0) return;
   switch (newt_tree_bucket(g.L)) {
-#define X(M) case M: tree_sensor_dyn_kernel<M><<<grid, 64, 0, st>>>(g, idx, n, out); break;
+#define X(M) case M: tree_sensor_dyn_kernel<M><<<grid, 64, 0, st>>>(g, idx, n, out, sens, sens_stride); break;
     NEWT_TREE_BUCKETS(X)
 #undef X
   }
