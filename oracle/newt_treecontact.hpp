@@ -1,7 +1,10 @@
 // Oracle (test infrastructure only): the joint tree-contact solve of newt's
-// World::step, for pyramidal condim-3 and condim-1 contacts between tree
-// links and static or free-body geoms, with PGS or Newton.  Never linked into
-// the shipped library.
+// World::step, for contacts between tree links and static or free-body
+// geoms: pyramidal condim-3 facets, condim 1, and the general rows (normal,
+// tangents, torsion, rolling) of condim 3 under the elliptic cone and of
+// condim 4 and 6, with PGS or Newton.  Never linked into the shipped
+// library.  Free bodies' own rolling rows (Body::rolling_friction) are not
+// restated.
 //
 // Sources (paths inside hwang2409/tooling):
 //   newt/src/solver.rs:2805-3366  solve_tree_contacts
@@ -13,11 +16,17 @@
 //                                 world_velocity_from_delta
 //   newt/src/solver.rs:3719-3797  tree_body_invweight0, tree_contact_diag_approx
 //   newt/src/solver.rs:3799-3862  apply_world_impulse, world_pgs_non_negative
+//   newt/src/solver.rs:3863-3874  world_pgs_scalar
+//   newt/src/solver.rs:3973-4003  world_pgs_pair (pyramidal caps, elliptic)
+//   newt/src/solver.rs:3268-3330  the PGS sweep over contact blocks
+//   newt/src/solver.rs:398-411, 441-449  project_elliptic, project_pyramidal
 //   newt/src/solver.rs:1960-1974  contact_regularization_from_diag
 //   newt/src/newton.rs:275-620    NewtonSystem::solve, project,
 //                                 exact_pyramidal_line_search (non-negative
-//                                 projections: the only kind pyramidal
-//                                 condim-3 and condim-1 rows create)
+//                                 projections: under Newton, which takes the
+//                                 pyramidal cone, the general rows' only
+//                                 projection is the normal row's,
+//                                 solver.rs:3164-3196)
 //   newt/src/jacobian.rs:38-120   point_jacobian
 // Every sum runs in newt's order so the float mirror matches byte for byte.
 #pragma once
@@ -36,7 +45,12 @@ template <class R> struct TComp {
   std::vector<R> coef;       // tree: generalised coefficients (nv)
 };
 template <class R> struct TRow { std::vector<TComp<R>> comps; R reg = R(0), diag = R(0), bias = R(0); };
-template <class R> struct TBlock { int contact, start, condim; SolRef<R> sr; SolImp<R> si; R pen, mu; };
+template <class R> struct TBlock {
+  int contact, start, condim; SolRef<R> sr; SolImp<R> si; R pen, mu;
+  R mu_t = R(0), mu_r = R(0);  // combine_torsional_friction, combine_rolling_friction (min)
+  bool facets = true;          // pyramidal condim 3: the four facet rows
+  int nrows = 4;
+};
 
 template <class R> Vec3<R> unit_axis(int k) { return Vec3<R>(R(k == 0), R(k == 1), R(k == 2)); }
 
@@ -88,10 +102,11 @@ void point_jacobian(const Tree<R>& t, const std::vector<Pose<R>>& poses, int lin
   }
 }
 
-// world_jacobian_for_side (solver.rs:3537-3600), linear rows only.
+// world_jacobian_for_side (solver.rs:3537-3600): a linear row along `dir`
+// at the contact point, or an angular one (torsion, rolling) about `dir`.
 template <class R>
 bool side_jacobian(const World<R>& w, const Geom<R>& g, R sign, Vec3<R> cpos, Vec3<R> dir,
-                   const std::vector<std::vector<Pose<R>>>& tp, TComp<R>* out) {
+                   const std::vector<std::vector<Pose<R>>>& tp, TComp<R>* out, bool angular = false) {
   const int kind = g.att_kind();
   if (kind == 0) return false;
   TComp<R> c;
@@ -99,8 +114,8 @@ bool side_jacobian(const World<R>& w, const Geom<R>& g, R sign, Vec3<R> cpos, Ve
     const Body<R>& b = w.bodies[g.body];
     const Vec3<R> arm = cpos - b.pos;
     c.body = g.body;
-    c.lin = dir * sign;
-    c.ang = arm.cross(dir) * sign;
+    c.lin = angular ? Vec3<R>() : dir * sign;
+    c.ang = angular ? dir * sign : arm.cross(dir) * sign;
   } else {
     const Pose<R>& P = tp[g.tree][g.link];
     const Vec3<R> local = P.o.inverse_rotate(cpos - P.p);
@@ -108,10 +123,11 @@ bool side_jacobian(const World<R>& w, const Geom<R>& g, R sign, Vec3<R> cpos, Ve
     point_jacobian(w.trees[g.tree], tp[g.tree], g.link, local, tr, rt);
     c.tree = g.tree;
     c.link = g.link;
-    c.coef.resize(tr.size());
-    for (size_t s = 0; s < tr.size(); ++s) c.coef[s] = tr[s].dot(dir) * sign;
-    c.lin = dir * sign;
-    c.ang = (cpos - P.p).cross(dir * sign);
+    const std::vector<Vec3<R>>& src = angular ? rt : tr;
+    c.coef.resize(src.size());
+    for (size_t s = 0; s < src.size(); ++s) c.coef[s] = src[s].dot(dir) * sign;
+    c.lin = angular ? Vec3<R>() : dir * sign;
+    c.ang = angular ? dir * sign : (cpos - P.p).cross(dir * sign);
   }
   *out = c;
   return true;
@@ -352,25 +368,39 @@ void solve_tree_contacts(World<R>& w, const std::vector<Contact<R>>& contacts, b
     const SolImp<R> si = combine_solimp(ga.solimp, gb.solimp);
     const int condim = ga.condim < gb.condim ? ga.condim : gb.condim;
     const R mu = cmin(ga.friction, gb.friction);
-    if (condim != 1 && condim != 3) throw std::runtime_error("tree contacts: only condim 1 and 3 are restated");
+    if (condim != 1 && condim != 3 && condim != 4 && condim != 6)
+      throw std::runtime_error("tree contacts: condim must be 1, 3, 4 or 6");
     Vec3<R> t1, t2u;
     tangent_basis(c.n, &t1, &t2u);
     const Vec3<R> t2 = c.n.cross(t1);  // isotropic contact_friction_axes
-    std::vector<Vec3<R>> dirs;
-    if (condim == 3) dirs = {c.n + t1 * mu, c.n - t1 * mu, c.n + t2 * mu, c.n - t2 * mu};
-    else dirs = {c.n};
+    // contact_row_directions (solver.rs:3401-3429): direction, angular
+    const bool facets = w.cone == 0 && condim == 3;
+    std::vector<std::pair<Vec3<R>, bool>> dirs;
+    if (facets) {
+      dirs = {{c.n + t1 * mu, false}, {c.n - t1 * mu, false}, {c.n + t2 * mu, false}, {c.n - t2 * mu, false}};
+    } else {
+      dirs.push_back({c.n, false});
+      if (condim >= 3) { dirs.push_back({t1, false}); dirs.push_back({t2, false}); }
+      if (condim >= 4) dirs.push_back({c.n, true});
+      if (condim >= 6) { dirs.push_back({t1, true}); dirs.push_back({t2, true}); }
+    }
     std::vector<TRow<R>> brows;
     bool dynamic = false;
-    for (const Vec3<R>& dir : dirs) {
+    for (const auto& dir : dirs) {
       TRow<R> r;
       TComp<R> comp;
-      if (side_jacobian(w, ga, R(1), c.pos, dir, tp, &comp)) r.comps.push_back(comp);
-      if (side_jacobian(w, gb, R(-1), c.pos, dir, tp, &comp)) r.comps.push_back(comp);
+      if (side_jacobian(w, ga, R(1), c.pos, dir.first, tp, &comp, dir.second)) r.comps.push_back(comp);
+      if (side_jacobian(w, gb, R(-1), c.pos, dir.first, tp, &comp, dir.second)) r.comps.push_back(comp);
       if (!r.comps.empty()) dynamic = true;  // every body or non-mocap tree side is dynamic
       brows.push_back(r);
     }
     if (!dynamic) continue;
-    blocks.push_back({ci, (int)rows.size(), condim, sr, si, pen, mu});
+    TBlock<R> bk{ci, (int)rows.size(), condim, sr, si, pen, mu};
+    bk.mu_t = cmin(ga.torsional_friction, gb.torsional_friction);
+    bk.mu_r = cmin(ga.rolling_friction, gb.rolling_friction);
+    bk.facets = facets;
+    bk.nrows = (int)dirs.size();
+    blocks.push_back(bk);
     for (auto& r : brows) rows.push_back(r);
   }
   const int n = (int)rows.size();
@@ -409,8 +439,8 @@ void solve_tree_contacts(World<R>& w, const std::vector<Contact<R>>& contacts, b
   }
   // regularisation, diagonal and bias per row
   for (const TBlock<R>& bk : blocks) {
-    const bool pyr3 = bk.condim == 3;
-    const int nr = pyr3 ? 4 : 1;
+    const bool pyr3 = bk.facets;
+    const int nr = bk.nrows;
     for (int k = 0; k < nr; ++k) {
       TRow<R>& row = rows[bk.start + k];
       const R imp = impedance_at(-bk.pen, R(0), bk.si);
@@ -445,7 +475,7 @@ void solve_tree_contacts(World<R>& w, const std::vector<Contact<R>>& contacts, b
         vel += bv + tv;
         vf += bf + tf;
       }
-      const R position = -bk.pen;  // pyramidal condim-3 facets and the normal row
+      const R position = (pyr3 || k == 0) ? -bk.pen : R(0);  // facets and the normal row
       const R aref = reference_accel(position, vel, safe_solref(bk.sr, dt), bk.si);
       row.bias = vf - aref * dt;
     }
@@ -454,12 +484,14 @@ void solve_tree_contacts(World<R>& w, const std::vector<Contact<R>>& contacts, b
   if (use_newton) {
     std::vector<R> H = A;
     for (int i = 0; i < n; ++i) H[(size_t)i * n + i] += rows[i].reg;
+    // the normal row, or the four facets, non-negative; the general rows'
+    // friction rows carry no projection under the pyramidal cone
     std::vector<int> nonneg;
     for (const TBlock<R>& bk : blocks)
-      for (int k = 0; k < (bk.condim == 3 ? 4 : 1); ++k) nonneg.push_back(bk.start + k);
+      for (int k = 0; k < (bk.facets ? 4 : 1); ++k) nonneg.push_back(bk.start + k);
     std::vector<R> Ltest;
     bool zero_mu = false;
-    for (const TBlock<R>& bk : blocks) zero_mu = zero_mu || (bk.condim == 3 && bk.mu == R(0));
+    for (const TBlock<R>& bk : blocks) zero_mu = zero_mu || (bk.facets && bk.mu == R(0));
     if (zero_mu && !cholesky(H, n, Ltest)) {  // solver.rs:3215-3232
       R scale = R(0);
       for (R v : H) scale = std::max(scale, rabs(v));
@@ -472,22 +504,52 @@ void solve_tree_contacts(World<R>& w, const std::vector<Contact<R>>& contacts, b
     if (!newton_solve(H, bias, nonneg, max_it, R(1e-7), imp))
       throw std::runtime_error("Newton tree contact solve: Hessian is not positive definite");
   } else {
+    // world_pgs_residual (solver.rs:3838-3849) plus the row's own reg term
+    auto resid = [&](int i) {
+      R s = R(0);
+      for (int col = 0; col < n; ++col) s += A[(size_t)i * n + col] * imp[col];
+      return (rows[i].bias + s) + rows[i].reg * imp[i];
+    };
+    auto nonneg_step = [&](int i) {  // world_pgs_non_negative
+      const R p = imp[i] - resid(i) / rows[i].diag;
+      imp[i] = p < R(0) ? R(0) : p;
+    };
+    auto scalar_step = [&](int i, R cap) {  // world_pgs_scalar, project_pyramidal
+      const R f = imp[i] - resid(i) / rows[i].diag;
+      imp[i] = f > cap ? cap : (f < -cap ? -cap : f);
+    };
+    auto pair_step = [&](int i, int j, R mu_pair, R normal) {  // world_pgs_pair, isotropic
+      if (w.cone == 0) { scalar_step(i, mu_pair * normal); scalar_step(j, mu_pair * normal); return; }
+      const R ri = resid(i), rj = resid(j);
+      const R fi = imp[i] - ri / rows[i].diag, fj = imp[j] - rj / rows[j].diag;
+      R pi = R(0), pj = R(0);  // project_elliptic
+      if (normal > R(0) && mu_pair > R(0)) {
+        const R cap = mu_pair * normal;
+        const R mag2 = fi * fi + fj * fj;
+        if (mag2 <= cap * cap) { pi = fi; pj = fj; }
+        else { const R sc = cap / Sc<R>::sqrt(mag2); pi = fi * sc; pj = fj * sc; }
+      }
+      imp[i] = pi;
+      imp[j] = pj;
+    };
     for (int it = 0; it < w.iterations; ++it)
-      for (const TBlock<R>& bk : blocks)
-        for (int k = 0; k < (bk.condim == 3 ? 4 : 1); ++k) {  // world_pgs_non_negative
-          const int i = bk.start + k;
-          R s = R(0);
-          for (int col = 0; col < n; ++col) s += A[(size_t)i * n + col] * imp[col];
-          const R res = (rows[i].bias + s) + rows[i].reg * imp[i];
-          const R p = imp[i] - res / rows[i].diag;
-          imp[i] = p < R(0) ? R(0) : p;
+      for (const TBlock<R>& bk : blocks) {
+        const int nrm = bk.start;
+        nonneg_step(nrm);
+        if (bk.facets) {
+          for (int k = 1; k < 4; ++k) nonneg_step(nrm + k);
+        } else if (bk.condim >= 3) {
+          pair_step(nrm + 1, nrm + 2, bk.mu, imp[nrm]);
+          if (bk.condim >= 4) scalar_step(nrm + 3, bk.mu_t * imp[nrm]);
+          if (bk.condim >= 6) pair_step(nrm + 4, nrm + 5, bk.mu_r, imp[nrm]);
         }
+      }
   }
   if (impulses_out) *impulses_out = imp;
   if (normal_forces_out)
     for (const TBlock<R>& bk : blocks) {
       R fn = R(0);
-      if (bk.condim == 3) for (int k = 0; k < 4; ++k) fn += imp[bk.start + k];
+      if (bk.facets) for (int k = 0; k < 4; ++k) fn += imp[bk.start + k];
       else fn = imp[bk.start];
       (*normal_forces_out)[bk.contact] = fn / dt;
     }

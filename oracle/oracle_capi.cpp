@@ -373,7 +373,8 @@ int oracle_run(const newt_model_desc* models, int n_worlds, const int* model_of_
 
 // Row impulses of one world's tree-contact solve at its state (MuJoCo
 // layout; the Euler form of the step), in row order: 4 facet rows per
-// pyramidal condim-3 contact, 1 per condim-1 contact.  Also returns the
+// pyramidal condim-3 contact, else the normal row, then the tangent pair
+// (condim 3 and up), torsion (4 and up) and the rolling pair (6).  Also returns the
 // tree's generalised contact forces (nv) when qfrc_out is non-null.
 // integrator: 1 the Euler form of the solve (factors of M + dt B, implicit
 // free ABA), 0 the RK4 form (factors of M, explicit free ABA).
