@@ -115,7 +115,7 @@ typedef struct newt_geom_desc {      /* newt::geom::Geom */
   float solref[2];                   /* timeconst, dampratio */
   float solimp[5];                   /* dmin, dmax, width, midpoint, power */
   float margin, gap;
-  int32_t condim;                    /* 1, 3, 4 or 6 (newt/src/solver.rs:1409-1428); 4 and 6 on pile worlds */
+  int32_t condim;                    /* 1, 3, 4 or 6 (newt/src/solver.rs:1409-1428) */
   uint32_t group, mask;              /* collision filter (newt/src/broadphase.rs:16) */
   float torsional_friction;          /* condim >= 4: torsion cap mu_t f_n (geom.rs:397-403) */
   float rolling_friction;            /* condim 6: rolling cap mu_r f_n (geom.rs:404-409) */
@@ -134,7 +134,7 @@ typedef struct newt_model_desc {     /* one world's model: at most one tree */
                                       * the tree collide; 0: those pairs are skipped */
   int32_t integrator;                /* NEWT_INTEGRATOR_*: World::integrator (newt/src/world.rs:76-84) */
   int32_t cone;                      /* NEWT_CONE_*: SolverConfig::cone (newt/src/solver.rs:75-110);
-                                      * elliptic on pile worlds under PGS */
+                                      * elliptic under PGS (Newton takes the pyramidal cone) */
 } newt_model_desc;
 
 /* ---- context ------------------------------------------------------------ */
@@ -330,7 +330,9 @@ NEWT_API int newt_gpu_get_contacts(newt_gpu_ctx* ctx, int32_t slot, int32_t cap,
  * contact (zeros for an inactive one): 4 pyramidal facet rows; on pile
  * worlds with the elliptic cone or a condim other than 3, 6 slots per
  * contact holding its rows first (facets, or normal, tangents, torsion,
- * rolling as its condim has them) and zeros after. */
+ * rolling as its condim has them) and zeros after.  On tree-contact worlds
+ * the rows of the active contacts only, in contact order, with the same
+ * rows per contact (solver.rs:2880-2990). */
 NEWT_API int newt_gpu_get_impulses(newt_gpu_ctx* ctx, int32_t slot, int32_t cap, int32_t* n_out, float* impulses);
 
 /* ---- timing helpers for the benchmark (CUDA events on the ctx stream) ---- */

@@ -53,7 +53,7 @@ static void tree_rows(HostGroup& g) {
     g.irows = 4;
   }
   if (g.kind == GK_TREE_CONTACT) {  // per-geom model rows (TcGroupDev::geom), solver mode
-    g.r_geom = r; r += 21 * g.ng;
+    g.r_geom = r; r += 22 * g.ng;
     g.ri_mode = 3; g.ri_iters = 4; g.ri_integ = 5;
     g.irows = 6;
   }
@@ -120,7 +120,7 @@ size_t HostGroup::bytes_per_world() const {
   size_t b = frows * sizeof(float) + irows * sizeof(int);
   if (kind == GK_PILE) b += newt_pile_ws_bytes(size, np, maxc);
   if (kind == GK_PILE && pile_newton) b += newt_pile_newton_bytes(maxc);
-  if (kind == GK_TREE_CONTACT) b += newt_tc_ws_bytes(size, nv, ng, maxc);
+  if (kind == GK_TREE_CONTACT) b += newt_tc_ws_bytes(size, nv, ng, maxc, tc_rpc);
   return b;
 }
 
@@ -235,10 +235,15 @@ void HostGroup::setup_tc(const HostModel& m) {
   // pairs of geoms on different links, in newt's auto_pairs order with its
   // filter (world.rs:1042-1069)
   gtopo.assign(3 * ng, 0);
+  tc_rpc = 4;
+  tc_cone = m.cone;
+  tc_general = m.cone != NEWT_CONE_PYRAMIDAL;
   for (int k = 0; k < ng; ++k) {
     gtopo[2 * k] = m.geoms[k].shape;
     gtopo[2 * k + 1] = m.geoms[k].link;
     gtopo[2 * ng + k] = m.geoms[k].condim;
+    if (m.geoms[k].condim == 6) tc_rpc = 6;  // normal, tangent pair, torsion, rolling pair
+    if (m.geoms[k].condim == 4 || m.geoms[k].condim == 6) tc_general = true;
   }
   gpairs.clear();
   maxc = 0;
@@ -321,11 +326,11 @@ void HostGroup::write_model(newt_gpu_ctx*, int w, const HostModel& m) {
     if (kind == GK_TREE_CONTACT) {
       for (int k = 0; k < ng; ++k) {
         const newt_geom_desc& G = m.geoms[k];
-        float rec[21] = {G.size[0], G.size[1], G.size[2], G.local_pos[0], G.local_pos[1], G.local_pos[2],
+        float rec[22] = {G.size[0], G.size[1], G.size[2], G.local_pos[0], G.local_pos[1], G.local_pos[2],
                          G.local_quat[0], G.local_quat[1], G.local_quat[2], G.local_quat[3], G.friction, G.margin,
                          G.gap, G.solref[0], G.solref[1], G.solimp[0], G.solimp[1], G.solimp[2], G.solimp[3],
-                         G.solimp[4], 0.f};
-        for (int f = 0; f < 21; ++f) F(r_geom + 21 * k + f, w) = rec[f];
+                         G.solimp[4], G.torsional_friction, G.rolling_friction};
+        for (int f = 0; f < 22; ++f) F(r_geom + 22 * k + f, w) = rec[f];
       }
       I(ri_mode, w) = m.solver;
       I(ri_iters, w) = m.iterations;
@@ -453,11 +458,11 @@ int HostGroup::read_contacts(newt_gpu_ctx* ctx, int w, int cap_out, int* n_out, 
   if (kind == GK_TREE_CONTACT) {
     // contact records in the world's solver scratch (see newton_kernels.cu)
     int o_con, o_imp, o_misc;
-    newt_tc_offsets(size, nv, ng, maxc, &o_con, &o_imp, &o_misc);
+    newt_tc_offsets(size, nv, ng, maxc, tc_rpc, &o_con, &o_imp, &o_misc);
     *n_out = 0;
     if (!plain_scratch) return NEWT_OK;
     const float* base = (const float*)plain_scratch + (size_t)w * scr_stride;
-    std::vector<float> recs(24 * (size_t)maxc);
+    std::vector<float> recs(TC_CREC * (size_t)maxc);
     int misc[2];
     CKG(cudaStreamSynchronize(ctx->stream));
     CKG(cudaMemcpy(misc, base + o_misc, sizeof(misc), cudaMemcpyDeviceToHost));
@@ -465,7 +470,7 @@ int HostGroup::read_contacts(newt_gpu_ctx* ctx, int w, int cap_out, int* n_out, 
     const int nc = std::min(misc[0], maxc);
     *n_out = nc;
     for (int i = 0; i < nc && i < cap_out; ++i) {
-      const float* c = recs.data() + 24 * i;
+      const float* c = recs.data() + TC_CREC * i;
       if (pairs) { std::memcpy(&pairs[2 * i], &c[0], sizeof(int)); std::memcpy(&pairs[2 * i + 1], &c[1], sizeof(int)); }
       if (data) { for (int k = 0; k < 6; ++k) data[7 * i + k] = c[4 + k]; data[7 * i + 6] = c[10]; }
     }
@@ -488,14 +493,14 @@ int HostGroup::read_contacts(newt_gpu_ctx* ctx, int w, int cap_out, int* n_out, 
 int HostGroup::read_impulses(newt_gpu_ctx* ctx, int w, int cap_out, int* n_out, float* imp) {
   if (kind == GK_TREE_CONTACT) {
     int o_con, o_imp, o_misc;
-    newt_tc_offsets(size, nv, ng, maxc, &o_con, &o_imp, &o_misc);
+    newt_tc_offsets(size, nv, ng, maxc, tc_rpc, &o_con, &o_imp, &o_misc);
     *n_out = 0;
     if (!plain_scratch) return NEWT_OK;
     const float* base = (const float*)plain_scratch + (size_t)w * scr_stride;
     int misc[2];
     CKG(cudaStreamSynchronize(ctx->stream));
     CKG(cudaMemcpy(misc, base + o_misc, sizeof(misc), cudaMemcpyDeviceToHost));
-    const int nr = std::min(misc[1], 4 * maxc);
+    const int nr = std::min(misc[1], tc_rpc * maxc);
     *n_out = nr;
     if (nr > 0 && imp) CKG(cudaMemcpy(imp, base + o_imp, std::min(nr, cap_out) * sizeof(float), cudaMemcpyDeviceToHost));
     return NEWT_OK;
@@ -556,6 +561,7 @@ TcGroupDev HostGroup::tc_dev() const {
   TcGroupDev d;
   d.t = tree_dev();
   d.ng = ng; d.npairs = npairs; d.maxc = maxc;
+  d.rpc = tc_rpc; d.cone = tc_cone; d.general = tc_general ? 1 : 0;
   d.gtopo = dgtopo; d.pairs = dpairs;
   d.geom = dF + (size_t)r_geom * cap;
   d.mode = dI + (size_t)ri_mode * cap;

@@ -48,15 +48,22 @@ struct TreeGroupDev {
 // A tree whose link geoms touch static planes (quadruped worlds): the tree
 // group's SoA layout plus per-geom model rows, the solver mode and a
 // world-major solver scratch.
+// Floats per tree-contact record in the solver scratch (newton_kernels.cu).
+constexpr int TC_CREC = 28;
+
 struct TcGroupDev {
   TreeGroupDev t;
   int ng;            // geoms per world (link geoms and static planes, model order)
   int npairs;        // candidate (static, link geom) pairs, newt's pair order
   int maxc;          // contact capacity per world
+  int rpc;           // row capacity per contact: 6 when a geom has condim 6, else 4
+  int cone;          // NEWT_CONE_* (uniform over the group)
+  int general;       // some contact's rows are not four pyramidal facets or one normal row
   const int* gtopo;  // [2*ng] shape, link (-1 static); [ng] condim; [2*L] subtree masks (lo, hi);
                      // [nv] the link of each DoF
   const int* pairs;  // [2*npairs] geom indices (a < b)
-  const float* geom; // 21 SoA rows per geom: size3 pos3 quat4 fric margin gap solref2 solimp5
+  const float* geom; // 22 SoA rows per geom: size3 pos3 quat4 fric margin gap solref2 solimp5
+                     // torsional rolling
   const int* mode;   // per world: NEWT_SOLVER_PGS | NEWT_SOLVER_NEWTON
   const int* iters;  // per world
   float* scr;        // world-major solver scratch

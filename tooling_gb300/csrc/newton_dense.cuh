@@ -137,10 +137,14 @@ NEWT_D double warp_dot_d(const float* a, const float* b, int n, int lane) {
 // which newt adds a solver-only pivot before it gives up on the factor.  x,
 // b and the scratch vectors d, g, p, s, u, v and brk hold at least nr
 // values.  Returns the iterations taken; ORs NEWT_WS_FP64_FALLBACK,
-// NEWT_WS_NOT_PD (x = 0) and NEWT_WS_ITER_CAP into *status.
+// NEWT_WS_NOT_PD (x = 0) and NEWT_WS_ITER_CAP into *status.  kinds
+// (nullable: every row non-negative): per row a code whose value below -1
+// marks a row without projection (newt's general contact rows under the
+// pyramidal cone, whose tangent, torsion and rolling rows carry none).
 NEWT_D int newton_solve(float* H, int nr, int ld, float* LH, int ldh, double* LHd, float* vx, const float* vb,
                         float* vd, float* vg, float* vp, float* vs, float* vu, float* vv, float* vbrk, int iters,
-                        bool zero_mu, int lane, uint32_t* status) {
+                        bool zero_mu, int lane, uint32_t* status, const int* kinds = nullptr) {
+  auto projected = [&](int r) { return !kinds || kinds[r] >= -1; };
   float mn = 0.f, mx = 0.f;
   int done_it = 0;
   auto copy_h = [&]() {
@@ -199,10 +203,11 @@ NEWT_D int newton_solve(float* H, int nr, int ld, float* LH, int ldh, double* LH
       // ---- exact line search over the projected path (newton.rs:435-556) ----
       for (int r = lane; r < nr; r += 32) {
         const float x = vx[r], d = vd[r];
-        const bool fr = x > 0.f || (x == 0.f && d > 0.f);
+        const bool pr = projected(r);
+        const bool fr = !pr || x > 0.f || (x == 0.f && d > 0.f);
         vp[r] = fr ? x : 0.f;
         vs[r] = fr ? d : 0.f;
-        const float a = (x > 0.f && d < 0.f) ? -x / d : 2.f;  // where x + a d reaches zero
+        const float a = (pr && x > 0.f && d < 0.f) ? -x / d : 2.f;  // where x + a d reaches zero
         vbrk[r] = (a > 0.f && a < 1.f) ? a : 2.f;
       }
       warp_matvec(H, nr, ld, vp, vu, lane);
@@ -256,7 +261,7 @@ NEWT_D int newton_solve(float* H, int nr, int ld, float* LH, int ldh, double* LH
       if (best_a <= 0.f || cur - best_c <= 1.0e-7 * (1.0 + fabs(cur))) break;
       for (int r = lane; r < nr; r += 32) {
         const float x = vx[r] + best_a * vd[r];
-        vx[r] = x < 0.f ? 0.f : x;
+        vx[r] = (projected(r) && x < 0.f) ? 0.f : x;
       }
       __syncwarp();
       done_it = it + 1;

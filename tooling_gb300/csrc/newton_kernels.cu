@@ -74,14 +74,24 @@ using dense::warp_matvec;
 using dense::warp_sum;
 using dense::warp_sumd;
 constexpr int TC_WARPS = 1;  // warps (worlds) per block
-constexpr int CREC = 24;     // floats per contact record
+constexpr int CREC = TC_CREC;  // floats per contact record
 // contact record fields
 // K_LINK: the link of the row's tree side with sign K_SIGN; K_LINK2: for an
-// in-tree pair, the link of side b (sign -1), else -1
+// in-tree pair, the link of side b (sign -1), else -1; K_MUT, K_MUR: the
+// torsional and rolling friction (min of the two geoms'); K_ROW: the first
+// row, -1 for a contact without rows
 enum { K_GA = 0, K_GB = 1, K_LINK = 2, K_SIGN = 3, K_POS = 4, K_N = 7, K_PEN = 10, K_GAP = 11, K_MU = 12,
-       K_SR = 13, K_SI = 15, K_CONDIM = 20, K_ROW = 21, K_LINK2 = 22 };
-constexpr int GREC = 21;  // SoA geom model rows: size3 pos3 quat4 fric margin gap solref2 solimp5
-enum { G_SIZE = 0, G_POS = 3, G_QUAT = 6, G_FRIC = 10, G_MARGIN = 11, G_GAP = 12, G_SR = 13, G_SI = 15 };
+       K_SR = 13, K_SI = 15, K_CONDIM = 20, K_ROW = 21, K_LINK2 = 22, K_MUT = 23, K_MUR = 24 };
+static_assert(K_MUR < CREC, "contact record");
+constexpr int GREC = 22;  // SoA geom model rows: size3 pos3 quat4 fric margin gap solref2 solimp5 torsional rolling
+enum { G_SIZE = 0, G_POS = 3, G_QUAT = 6, G_FRIC = 10, G_MARGIN = 11, G_GAP = 12, G_SR = 13, G_SI = 15, G_TF = 20,
+       G_RF = 21 };
+// Row codes (rfac): 0-3 the pyramidal facets n +- mu t1, n +- mu t2 of a
+// condim-3 contact; otherwise -1 - kind, kind 0 normal, 1-2 the tangents,
+// 3 torsion (angular about n), 4-5 rolling (angular about t1, t2), the rows
+// of contact_row_directions (newt/src/solver.rs:3401-3429).
+enum { R_NORMAL = -1, R_T1 = -2, R_T2 = -3, R_TORSION = -4, R_ROLL1 = -5, R_ROLL2 = -6 };
+NEWT_HD bool row_angular(int f) { return f <= R_TORSION; }
 enum { JF = 0, JX = 1, JH = 2, JS = 3 };
 
 
@@ -115,11 +125,12 @@ static __device__ __noinline__ int np_link_pair(int sa, int sb, GPose pa, GPose 
 // n +- mu t1, n +- mu t2 (solver.rs:3401-3429, tangent_basis world.rs:3104-3112).
 NEWT_D V3 row_direction(const float* cc, int f) {
   const V3 n = v3(cc[K_N], cc[K_N + 1], cc[K_N + 2]);
-  if (f < 0) return n;
+  if (f == R_NORMAL || f == R_TORSION) return n;
   const float mu = cc[K_MU];
   const V3 ref = fabsf(n.z) < 0.9f ? v3(0.f, 0.f, 1.f) : v3(1.f, 0.f, 0.f);
   V3 t1 = cross(ref, n);
   t1 = t1 * (1.f / sqrtf(len2(t1)));
+  if (f < 0) return (f == R_T1 || f == R_ROLL1) ? t1 : cross(n, t1);
   const V3 t = f < 2 ? t1 : cross(n, t1);
   return n + t * ((f & 1) ? -mu : mu);
 }
@@ -170,10 +181,10 @@ struct TcLay {
 };
 NEWT_HD int up4(int n) { return (n + 3) / 4 * 4; }
 constexpr int REFINE_NV = 24;  // DoF above which M is summed and the mass-matrix solve refined in FP64
-NEWT_HD TcLay tc_layout(int L, int nv, int ng, int maxc) {
+NEWT_HD TcLay tc_layout(int L, int nv, int ng, int maxc, int rpc) {
   TcLay t;
   t.L = L; t.nv = nv; t.ng = ng; t.maxc = maxc;
-  t.ld = up4(4 * maxc);
+  t.ld = up4(rpc * maxc);
   int f = 0;
   t.jv = f; f += up4(3 * nv * L);
   t.jw = f; f += up4(3 * nv * L);
@@ -205,9 +216,9 @@ NEWT_HD TcLay tc_layout(int L, int nv, int ng, int maxc) {
 enum { V_X = 0, V_D, V_G, V_B, V_REG, V_DIAG, V_U, V_V, V_P, V_S, N_VEC };
 constexpr int NRS = 20;
 struct TcSmem { int vl, ldr, nrs, vec, rmap, pose, lm, ldf, tw, lh, jy, words; };
-NEWT_HD TcSmem tc_smem(int L, int nv, int maxc) {
+NEWT_HD TcSmem tc_smem(int L, int nv, int maxc, int rpc) {
   TcSmem m;
-  m.ldr = up4(4 * maxc);
+  m.ldr = up4(rpc * maxc);
   m.vl = m.ldr > up4(nv) ? m.ldr : up4(nv);
   m.nrs = m.ldr < NRS ? m.ldr : NRS;
   int f = 0;
@@ -216,7 +227,7 @@ NEWT_HD TcSmem tc_smem(int L, int nv, int maxc) {
   m.pose = f; f += up4(7 * L);
   m.lm = f; f += up4(nv * nv);
   m.ldf = f; f += up4(nv * nv);
-  m.tw = f; f += up4(L);
+  m.tw = f; f += 2 * up4(L);  // translation, then rotation inverse weights per link
   m.lh = f; f += m.nrs * m.nrs;
   m.jy = f; f += up4(nv * m.nrs);
   m.words = f;
@@ -335,8 +346,8 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   const TreeGroupDev& g = G.t;
   if (w >= g.n || !g.live[w]) return;  // uniform per warp
   const int cap = g.cap, L = g.L, nv = g.nv;
-  const TcLay lay = tc_layout(L, nv, G.ng, G.maxc);
-  const TcSmem sm = tc_smem(L, nv, G.maxc);
+  const TcLay lay = tc_layout(L, nv, G.ng, G.maxc, G.rpc);
+  const TcSmem sm = tc_smem(L, nv, G.maxc, G.rpc);
   const int ld = lay.ld, vl = sm.vl;
   float* wf = G.scr + (size_t)w * G.sstride;
   float* sv = tcs + (size_t)warp * sm.words;
@@ -504,20 +515,27 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
       c[K_SI + 3] = gv(a, G_SI + 3);
       c[K_SI + 4] = gv(a, G_SI + 4);
       c[K_CONDIM] = (float)min(G.gtopo[2 * G.ng + a], G.gtopo[2 * G.ng + b]);
+      c[K_MUT] = fminf(gv(a, G_TF), gv(b, G_TF));  // combine_torsional_friction
+      c[K_MUR] = fminf(gv(a, G_RF), gv(b, G_RF));  // combine_rolling_friction
     }
     ncon = ncon + total < G.maxc ? ncon + total : G.maxc;
   }
   if (__any_sync(FULL, overflow)) status |= NEWT_WS_CONTACT_OVERFLOW;
   __syncwarp();
   // rows of the active contacts, in contact order (solver.rs:2881-2890):
-  // lane per contact, a warp scan assigns the row ranges
+  // lane per contact, a warp scan assigns the row ranges; the pyramidal
+  // cone's condim-3 contacts take four facet rows, the others the normal row
+  // and, by condim, the tangent pair, torsion and the rolling pair
   int nrows = 0;
   for (int base = 0; base < ncon; base += 32) {
     const int c = base + lane;
     int k = 0;
+    bool facets = false;
     if (c < ncon) {
       const float* cc = con + CREC * c;
-      if (cc[K_PEN] - cc[K_GAP] > 0.f) k = (int)cc[K_CONDIM] == 3 ? 4 : 1;
+      const int cd = (int)cc[K_CONDIM];
+      facets = G.cone == NEWT_CONE_PYRAMIDAL && cd == 3;
+      if (cc[K_PEN] - cc[K_GAP] > 0.f) k = facets ? 4 : cd;
     }
     int incl = k;
     for (int o = 1; o < 32; o <<= 1) {
@@ -527,7 +545,7 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
     const int start = nrows + incl - k;
     if (c < ncon) {
       con[CREC * c + K_ROW] = __int_as_float(k > 0 ? start : -1);
-      for (int f = 0; f < k; ++f) { rcon[start + f] = c; rfac[start + f] = k == 4 ? f : -1; }
+      for (int f = 0; f < k; ++f) { rcon[start + f] = c; rfac[start + f] = facets ? f : -1 - f; }
     }
     nrows += __shfl_sync(FULL, incl, 31);
   }
@@ -552,15 +570,24 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
         if (l1 != l && l2 != l) continue;
         const V3 dir = row_direction(cc, rfac[r]), pt = ldv3(cc + K_POS);
         const float force = vx[r] / dt;
+        const bool ang = row_angular(rfac[r]);  // wrench (0, dir sign): world_jacobian_for_side
         if (l1 == l) {
           const V3 d = dir * cc[K_SIGN];
-          fs = fs + d * force;
-          ts = ts + cross(pt - cl, d) * force;
+          if (ang) {
+            ts = ts + d * force;
+          } else {
+            fs = fs + d * force;
+            ts = ts + cross(pt - cl, d) * force;
+          }
         }
         if (l2 == l) {
           const V3 d = dir * -1.f;
-          fs = fs + d * force;
-          ts = ts + cross(pt - cl, d) * force;
+          if (ang) {
+            ts = ts + d * force;
+          } else {
+            fs = fs + d * force;
+            ts = ts + cross(pt - cl, d) * force;
+          }
         }
       }
       stv3(so + 6 * l, fs);
@@ -695,6 +722,7 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   const bool keep_j = refine || rk4;
   const int ldj = rows_shared ? sm.nrs : ld;
   float* tw = sv + sm.tw;  // 1 marks a link that owns rows; then its inverse weight
+  float* rw = tw + up4(L);  // the rotation inverse weights (angular rows)
   for (int l = lane; l < L; l += 32) tw[l] = 0.f;
   __syncwarp();
   for (int r = lane; r < nr; r += 32) {
@@ -705,10 +733,17 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
     const float sign = cc[K_SIGN];
     const V3 pt = ldv3(cc + K_POS);
     const V3 dir = row_direction(cc, rfac[r]);
+    // linear rows on the point's translational columns, angular rows on the
+    // link's rotational ones (world_jacobian_for_side, solver.rs:3566-3598)
+    const bool ang = row_angular(rfac[r]);
     for (int k = 0; k < nv; ++k) Jt[(size_t)k * ldj + r] = 0.f;
-    chain_columns(g, w, pose, link, pt, [&](int k, V3, V3 tr) { Jt[(size_t)k * ldj + r] = dot(tr, dir) * sign; });
+    chain_columns(g, w, pose, link, pt, [&](int k, V3 rot, V3 tr) {
+      Jt[(size_t)k * ldj + r] = dot(ang ? rot : tr, dir) * sign;
+    });
     if (link2 >= 0)  // side b of an in-tree pair: the columns its chain shares with side a's take both
-      chain_columns(g, w, pose, link2, pt, [&](int k, V3, V3 tr) { Jt[(size_t)k * ldj + r] -= dot(tr, dir); });
+      chain_columns(g, w, pose, link2, pt, [&](int k, V3 rot, V3 tr) {
+        Jt[(size_t)k * ldj + r] -= dot(ang ? rot : tr, dir);
+      });
     float vel = 0.f, vfree = 0.f;
     for (int k = 0; k < nv; ++k) {
       const float jk = Jt[(size_t)k * ldj + r];
@@ -741,7 +776,26 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
       H[(size_t)c * ld + r] = s;
     }
   // ---- mean inverse weight of each link's COM (tree_body_invweight0): three
-  // lanes per link, one per axis, ten links per round ----
+  // lanes per link, one per axis, ten links per round; the rotation weights
+  // (rows about an axis) first, for groups with angular rows ----
+  if (G.general)
+    for (int l0 = 0; l0 < L; l0 += 10) {
+      const int l = l0 + lane / 3, axis = lane % 3;
+      float s2 = 0.f;
+      if (lane < 30 && l < L && tw[l] != 0.f) {
+        const float* jw = JW + 3 * nv * l;
+        float y[NEWT_MAX_LINKS + 5];
+        for (int k = 0; k < nv; ++k) {
+          float s = jw[3 * k + axis];
+          for (int m = 0; m < k; ++m) s -= LD[m * nv + k] * y[m];
+          y[k] = s / LD[k * nv + k];
+          s2 += y[k] * y[k];
+        }
+      }
+      const float s2y = __shfl_down_sync(0xffffffffu, s2, 1), s2z = __shfl_down_sync(0xffffffffu, s2, 2);
+      if (lane < 30 && axis == 0 && l < L) rw[l] = ((s2 + s2y) + s2z) / 3.f;
+    }
+  __syncwarp();
   for (int l0 = 0; l0 < L; l0 += 10) {
     const int l = l0 + lane / 3, axis = lane % 3;
     float s2 = 0.f;
@@ -769,13 +823,18 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
     const Soft s{cc[K_SR], cc[K_SR + 1], cc[K_SI], cc[K_SI + 1], cc[K_SI + 2], cc[K_SI + 3], (int)cc[K_SI + 4]};
     const float d = impedance_at(-pen, s);
     const bool pyr = rfac[r] >= 0;
-    const int link2 = __float_as_int(cc[K_LINK2]);  // tree_contact_diag_approx sums both tree sides
-    const float twl = tw[__float_as_int(cc[K_LINK])] + (link2 >= 0 ? tw[link2] : 0.f);
+    // tree_contact_diag_approx: both tree sides' translation weights, or
+    // rotation weights for an angular row
+    const int link2 = __float_as_int(cc[K_LINK2]);
+    const float* wt = row_angular(rfac[r]) ? rw : tw;
+    const float twl = wt[__float_as_int(cc[K_LINK])] + (link2 >= 0 ? wt[link2] : 0.f);
     const float base = (1.f - d) / d * (pyr ? twl * (1.f + mu * mu) : twl);
     const float reg = pyr ? 2.f * mu * mu * base : base;
     vreg[r] = reg;
     vdiag[r] = H[(size_t)r * ld + r] + reg;
-    vb[r] = vv[r] - reference_accel(-pen, vu[r], s.tc, s.dr, s, dt) * dt;
+    // the position term drives the facets and the normal row only
+    const float position = (pyr || rfac[r] == R_NORMAL) ? -pen : 0.f;
+    vb[r] = vv[r] - reference_accel(position, vu[r], s.tc, s.dr, s, dt) * dt;
     vx[r] = 0.f;
   }
   __syncwarp();
@@ -783,7 +842,7 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
   const int mode = G.mode[w];
   const int iters = G.iters[w];
   int done_it = 0;
-  if (mode == NEWT_SOLVER_PGS) {
+  if (mode == NEWT_SOLVER_PGS && !G.general) {
     // dense Gauss-Seidel, four non-negative facet steps per pyramidal block
     // (world_pgs_non_negative, solver.rs:3851-3862)
     for (int it = 0; it < iters; ++it)
@@ -796,6 +855,65 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
         __syncwarp();
         if (lane == 0) vx[r] = p < 0.f ? 0.f : p;
         __syncwarp();
+      }
+    done_it = iters;
+  } else if (mode == NEWT_SOLVER_PGS) {
+    // the sweep over contact blocks (solver.rs:3268-3330): the normal row,
+    // then the facets, or the tangent pair capped by the normal impulse
+    // (world_pgs_pair: pyramidal caps or the elliptic projection), torsion
+    // (world_pgs_scalar) and the rolling pair
+    auto resid = [&](int r) {  // world_pgs_residual plus the row's own reg term
+      float s = 0.f;
+      for (int c = lane; c < nr; c += 32) s += H[(size_t)r * ld + c] * vx[c];
+      s = warp_sum(s);
+      return (vb[r] + s) + vreg[r] * vx[r];
+    };
+    auto put = [&](int r, float v) {
+      __syncwarp();
+      if (lane == 0) vx[r] = v;
+      __syncwarp();
+    };
+    auto nonneg = [&](int r) {
+      const float p = vx[r] - resid(r) / vdiag[r];
+      put(r, p < 0.f ? 0.f : p);
+    };
+    auto scalar = [&](int r, float cap) {  // project_pyramidal
+      const float f = vx[r] - resid(r) / vdiag[r];
+      put(r, f > cap ? cap : (f < -cap ? -cap : f));
+    };
+    auto pair = [&](int i, int j, float mu, float normal) {
+      if (G.cone == NEWT_CONE_PYRAMIDAL) {
+        scalar(i, mu * normal);
+        scalar(j, mu * normal);
+        return;
+      }
+      const float ri = resid(i), rj = resid(j);
+      const float fi = vx[i] - ri / vdiag[i], fj = vx[j] - rj / vdiag[j];
+      float pi = 0.f, pj = 0.f;  // project_elliptic (solver.rs:398-411), isotropic
+      if (normal > 0.f && mu > 0.f) {
+        const float c = mu * normal, mag2 = fi * fi + fj * fj;
+        if (mag2 <= c * c) { pi = fi; pj = fj; }
+        else { const float sc = c / sqrtf(mag2); pi = fi * sc; pj = fj * sc; }
+      }
+      __syncwarp();
+      if (lane == 0) { vx[i] = pi; vx[j] = pj; }
+      __syncwarp();
+    };
+    for (int it = 0; it < iters; ++it)
+      for (int c = 0; c < ncon; ++c) {
+        const float* cc = con + CREC * c;
+        const int r0 = __float_as_int(cc[K_ROW]);
+        if (r0 < 0) continue;
+        nonneg(r0);
+        if (rfac[r0] >= 0) {
+          for (int k = 1; k < 4; ++k) nonneg(r0 + k);
+          continue;
+        }
+        const int cd = (int)cc[K_CONDIM];
+        if (cd < 3) continue;
+        pair(r0 + 1, r0 + 2, cc[K_MU], vx[r0]);
+        if (cd >= 4) scalar(r0 + 3, cc[K_MUT] * vx[r0]);
+        if (cd >= 6) pair(r0 + 4, r0 + 5, cc[K_MUR], vx[r0]);
       }
     done_it = iters;
   } else {
@@ -811,8 +929,10 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
     bool zero_mu = false;
     for (int r = lane; r < nr; r += 32) zero_mu = zero_mu || (rfac[r] >= 0 && con[CREC * rcon[r] + K_MU] == 0.f);
     zero_mu = __any_sync(FULL, zero_mu);
+    // under the pyramidal cone the general rows' only projection is the
+    // normal row's (solver.rs:3164-3196): the other rows are free
     done_it = dense::newton_solve(H, nr, ld, LH, ldh, LHd, vx, vb, vd, vg, vp, vs, vu, vv, vreg, iters, zero_mu, lane,
-                                  &status);
+                                  &status, G.general ? rfac : nullptr);
   }
   __syncwarp();
   if (resolve) {  // the sensors' inputs only: the step's impulses and accelerations stay as they were
@@ -879,27 +999,27 @@ __global__ void __launch_bounds__(32 * TC_WARPS) tc_k_solve(TcGroupDev G) {
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-extern "C" size_t newt_tc_ws_bytes(int L, int nv, int ng, int maxc) {
-  return (size_t)tc_layout(L, nv, ng, maxc).words * sizeof(float);
+extern "C" size_t newt_tc_ws_bytes(int L, int nv, int ng, int maxc, int rpc) {
+  return (size_t)tc_layout(L, nv, ng, maxc, rpc).words * sizeof(float);
 }
-extern "C" size_t newt_tc_smem_bytes(int L, int nv, int maxc) {
-  return (size_t)TC_WARPS * tc_smem(L, nv, maxc).words * sizeof(float);
+extern "C" size_t newt_tc_smem_bytes(int L, int nv, int maxc, int rpc) {
+  return (size_t)TC_WARPS * tc_smem(L, nv, maxc, rpc).words * sizeof(float);
 }
 // Kernel attribute for the dynamic shared memory (outside stream capture).
-extern "C" cudaError_t newt_tc_init(int L, int nv, int maxc) {
-  const int bytes = (int)newt_tc_smem_bytes(L, nv, maxc);
+extern "C" cudaError_t newt_tc_init(int L, int nv, int maxc, int rpc) {
+  const int bytes = (int)newt_tc_smem_bytes(L, nv, maxc, rpc);
   if (nv > REFINE_NV) return cudaFuncSetAttribute(tc_k_solve<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   return cudaFuncSetAttribute(tc_k_solve<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 extern "C" void newt_launch_tc_solve(const TcGroupDev& G, cudaStream_t st) {
   const int grid = (G.t.n + TC_WARPS - 1) / TC_WARPS;
   if (grid == 0) return;
-  const size_t bytes = newt_tc_smem_bytes(G.t.L, G.t.nv, G.maxc);
+  const size_t bytes = newt_tc_smem_bytes(G.t.L, G.t.nv, G.maxc, G.rpc);
   if (G.t.nv > REFINE_NV) tc_k_solve<true><<<grid, 32 * TC_WARPS, bytes, st>>>(G);
   else tc_k_solve<false><<<grid, 32 * TC_WARPS, bytes, st>>>(G);
 }
-extern "C" void newt_tc_offsets(int L, int nv, int ng, int maxc, int* con, int* imp, int* misc) {
-  const TcLay t = tc_layout(L, nv, ng, maxc);
+extern "C" void newt_tc_offsets(int L, int nv, int ng, int maxc, int rpc, int* con, int* imp, int* misc) {
+  const TcLay t = tc_layout(L, nv, ng, maxc, rpc);
   *con = t.con;
   *imp = t.imp;
   *misc = t.misc;
@@ -919,7 +1039,7 @@ extern "C" void newt_launch_tree_integrate(const TreeGroupDev& g, cudaStream_t s
 // cannot happen under stream capture.
 extern "C" int newt_tc_prepare(newt_gpu_ctx* ctx, HostGroup* g, int n_steps) {
   if (g->n == 0) return NEWT_OK;
-  const size_t per = newt_tc_ws_bytes(g->size, g->nv, g->ng, g->maxc);
+  const size_t per = newt_tc_ws_bytes(g->size, g->nv, g->ng, g->maxc, g->tc_rpc);
   const size_t need = per * (size_t)g->cap;
   if (g->plain_scratch_bytes < need) {
     if (g->plain_scratch) cudaFree(g->plain_scratch);
@@ -931,7 +1051,7 @@ extern "C" int newt_tc_prepare(newt_gpu_ctx* ctx, HostGroup* g, int n_steps) {
     ctx->graph_dirty = true;
   }
   g->scr_stride = (long)(per / sizeof(float));
-  CKT(newt_tc_init(g->size, g->nv, g->maxc));
+  CKT(newt_tc_init(g->size, g->nv, g->maxc, g->tc_rpc));
   if (ctx->profile) {
     while (ctx->tcev.size() < (size_t)6 * n_steps) {
       cudaEvent_t e;
@@ -949,7 +1069,7 @@ extern "C" int newt_tc_prepare(newt_gpu_ctx* ctx, HostGroup* g, int n_steps) {
 extern "C" int newt_tc_launch(newt_gpu_ctx* ctx, HostGroup* g, int n_steps, cudaStream_t st, bool capturing) {
   if (g->n == 0) return NEWT_OK;
   TcGroupDev d = g->tc_dev();
-  d.t.cfrc = d.scr + tc_layout(g->size, g->nv, g->ng, g->maxc).qfc;
+  d.t.cfrc = d.scr + tc_layout(g->size, g->nv, g->ng, g->maxc, g->tc_rpc).qfc;
   d.t.cstride = d.sstride;
   const bool timed = ctx->profile && ctx->tcev.size() >= (size_t)6 * n_steps;
   auto mark = [&](int s, int k) {

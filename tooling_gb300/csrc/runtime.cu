@@ -160,11 +160,11 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
       } else if (G.shape != NEWT_SHAPE_PLANE) {
         return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "static geoms must be planes");
       }
-      if (G.condim != 3 && G.condim != 1)
-        return fail(ctx, NEWT_E_INVALID, "condim must be 1 or 3 on tree-contact worlds (4 and 6: pile worlds)");
+      if (G.condim != 1 && G.condim != 3 && G.condim != 4 && G.condim != 6)
+        return fail(ctx, NEWT_E_INVALID, "condim must be 1, 3, 4 or 6 (newt/src/solver.rs:1409-1428)");
     }
-    if (d.cone != NEWT_CONE_PYRAMIDAL)
-      return fail(ctx, NEWT_E_INVALID, "tree-contact worlds take the pyramidal cone on the GPU path");
+    if (d.solver == NEWT_SOLVER_NEWTON && d.cone != NEWT_CONE_PYRAMIDAL)
+      return fail(ctx, NEWT_E_INVALID, "the Newton solver takes the pyramidal cone (newt/src/solver.rs:89-91)");
     // in-tree pairs (newt collides geoms of different links of one tree unless
     // its self-collision is off, world.rs:340, 1042-1069): the shape pairs
     // newt has a routine for, as on pile worlds, plus sphere-box
@@ -364,7 +364,7 @@ int newt_gpu_alloc_worlds(newt_gpu_ctx* ctx, const int32_t* model_ids, int32_t n
       // scratch's current extent (the group grew) get a zeroed scratch when
       // it is next sized.
       int o_con, o_imp, o_misc;
-      newt_tc_offsets(g->size, g->nv, g->ng, g->maxc, &o_con, &o_imp, &o_misc);
+      newt_tc_offsets(g->size, g->nv, g->ng, g->maxc, g->tc_rpc, &o_con, &o_imp, &o_misc);
       const size_t held = g->scr_stride > 0 ? g->plain_scratch_bytes / (sizeof(float) * (size_t)g->scr_stride) : 0;
       for (int i : idx)
         if ((size_t)i < held && cudaMemsetAsync((float*)g->plain_scratch + (size_t)i * g->scr_stride + o_misc, 0,

@@ -38,6 +38,7 @@ struct HostModel {
       // shapes, attachments, condim, filters and in-tree collision fix the
       // pair list and the rows
       k += self_coll ? "s" : "n";
+      k += cone == NEWT_CONE_ELLIPTIC ? "e" : "p";
       for (auto& gd : geoms) {
         k += 'g'; k += std::to_string(gd.shape); k += '@'; k += std::to_string(gd.link);
         k += 'c'; k += std::to_string(gd.condim); k += 'f'; k += std::to_string(gd.group); k += '/';
@@ -89,6 +90,8 @@ struct HostGroup {
   int maxc_cap = 0;  // the context's cap on maxc for pile groups (0: none)
   // tree-contact groups: per-geom model rows, geom topology, candidate pairs
   int ng = 0, npairs = 0;
+  int tc_rpc = 4, tc_cone = NEWT_CONE_PYRAMIDAL;  // tree contact: rows per contact, cone
+  bool tc_general = false;  // tree contact: the elliptic cone, or condim 4 or 6 on some geom
   int r_geom = 0, ri_mode = 0, ri_iters = 0;
   std::vector<int> gtopo, gpairs;
   int* dgtopo = nullptr;
@@ -242,7 +245,7 @@ int autotune_batched(newt_gpu_ctx* ctx, int n_steps, int horizon, int32_t* choic
 extern "C" int newt_tree_bucket(int L);
 extern "C" void newt_launch_tree_fused(const TreeGroupDev& g, int base, int count, int n_steps, cudaStream_t st);
 extern "C" void newt_launch_tree_plain(const TreeGroupDev& g, cudaStream_t st);
-extern "C" void newt_tc_offsets(int L, int nv, int ng, int maxc, int* con, int* imp, int* misc);
-extern "C" size_t newt_tc_ws_bytes(int L, int nv, int ng, int maxc);
+extern "C" void newt_tc_offsets(int L, int nv, int ng, int maxc, int rpc, int* con, int* imp, int* misc);
+extern "C" size_t newt_tc_ws_bytes(int L, int nv, int ng, int maxc, int rpc);
 extern "C" size_t newt_pile_ws_bytes(int nb, int np, int maxc);
 extern "C" size_t newt_pile_newton_bytes(int maxc);
