@@ -135,6 +135,8 @@ typedef struct newt_model_desc {     /* one world's model: at most one tree */
   int32_t integrator;                /* NEWT_INTEGRATOR_*: World::integrator (newt/src/world.rs:76-84) */
   int32_t cone;                      /* NEWT_CONE_*: SolverConfig::cone (newt/src/solver.rs:75-110);
                                       * elliptic under PGS (Newton takes the pyramidal cone) */
+  float magnetic_field[3];           /* World::magnetic_field, world frame, read by magnetometers
+                                      * (newt/src/world.rs:118-119; World::new sets (0, -0.5, 0)) */
 } newt_model_desc;
 
 /* ---- context ------------------------------------------------------------ */
@@ -280,6 +282,11 @@ NEWT_API int newt_gpu_get_qacc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t 
  *   TOUCH                summed normal-force magnitudes of the contacts of geom `index` (1)
  *   FORCE                force link `index`'s parent joint transmits to it, link frame (3)
  *   TORQUE               the matching torque about the joint anchor, link frame (3)
+ *   MAGNETOMETER         the model's magnetic_field in the site frame (3)
+ *   RANGEFINDER          distance along the site's +z to the nearest geom of the world, the
+ *                        site's own included (a ray that starts inside a shape hits its far
+ *                        side), -1 when the ray meets none (1; sensor.rs:759-791,
+ *                        scene_query.rs:182-438)
  * ACCELEROMETER and TOUCH are read on pile worlds as newt's World::step reads
  * them (world.rs:1545-1612, sensor.rs:586-600, 1030-1112): the contacts of
  * the world's last step (any step form) are re-solved at its current state
@@ -307,6 +314,8 @@ NEWT_API int newt_gpu_get_qacc(newt_gpu_ctx* ctx, const int32_t* slots, int32_t 
 #define NEWT_SENSOR_TOUCH 10
 #define NEWT_SENSOR_FORCE 11
 #define NEWT_SENSOR_TORQUE 12
+#define NEWT_SENSOR_MAGNETOMETER 13
+#define NEWT_SENSOR_RANGEFINDER 14
 typedef struct newt_sensor_desc {
   int32_t kind;        /* NEWT_SENSOR_* */
   int32_t on_link;     /* 1: `index` is a link of the world's tree, 0: a free body */

@@ -14,6 +14,8 @@
 #include <stdexcept>
 #include <thread>
 #include <vector>
+#include <limits>
+
 #include "../include/newt_gpu.h"
 #include "newt_ccd.hpp"
 #include "newt_step.hpp"
@@ -443,6 +445,118 @@ int oracle_contacts(const newt_model_desc* d, const float* qpos, const float* qv
 // compute_link_va (:834-900) at zero acceleration.  `sensors` holds per sensor
 // (kind, on_link, index) ints in `si` and (local_pos xyz, local_quat xyzw) in
 // `sf`; `out` receives the concatenated values.
+}  // extern "C"
+
+// scene_query.rs:182-438 (ray_vs_geom without meshes): the distance along
+// the ray (origin o, direction dv, in the geom's frame) to the first hit at
+// or beyond 0, or -1.  newt returns the hit also for a ray that starts
+// inside the shape (its far root).
+template <class R> R ray_sphere_at(Vec3<R> c, R radius, Vec3<R> o, Vec3<R> dv) {
+  const Vec3<R> off = o - c;
+  const R a = dv.dot(dv);
+  if (a <= R(0)) return R(-1);
+  const R hb = off.dot(dv), cc = off.dot(off) - radius * radius;
+  const R disc = hb * hb - a * cc;
+  if (disc < R(0)) return R(-1);
+  const R root = Sc<R>::sqrt(disc);
+  const R nr = (-hb - root) / a, fr = (-hb + root) / a;
+  const R t = nr >= R(0) ? nr : fr;
+  return t >= R(0) ? t : R(-1);
+}
+template <class R> R ray_cyl_side(R radius, R hh, Vec3<R> o, Vec3<R> dv) {
+  const R a = dv.x * dv.x + dv.y * dv.y;
+  if (a <= R(1.0e-8)) return R(-1);
+  const R hb = o.x * dv.x + o.y * dv.y, cc = o.x * o.x + o.y * o.y - radius * radius;
+  const R disc = hb * hb - a * cc;
+  if (disc < R(0)) return R(-1);
+  const R root = Sc<R>::sqrt(disc);
+  R best = R(-1);
+  const R ts[2] = {(-hb - root) / a, (-hb + root) / a};
+  for (R t : ts)
+    if (t >= R(0)) {
+      const R z = o.z + dv.z * t;
+      if (z >= -hh && z <= hh && (best < R(0) || t < best)) best = t;
+    }
+  return best;
+}
+template <class R> R ray_geom(int shape, const R* size, Vec3<R> o, Vec3<R> dv) {
+  if (!(dv.dot(dv) > R(0))) return R(-1);
+  auto better = [](R cand, R best) { return cand >= R(0) && (best < R(0) || cand < best); };
+  switch (shape) {
+    case S_SPHERE: return ray_sphere_at(Vec3<R>(), size[0], o, dv);
+    case S_PLANE: {
+      if (dv.z == R(0)) return R(-1);
+      const R t = -o.z / dv.z;
+      return t >= R(0) ? t : R(-1);
+    }
+    case S_BOX: {
+      R nr = -std::numeric_limits<R>::infinity(), fr = std::numeric_limits<R>::infinity();
+      const R oa[3] = {o.x, o.y, o.z}, da[3] = {dv.x, dv.y, dv.z};
+      for (int k = 0; k < 3; ++k) {
+        if (da[k] == R(0)) {
+          if (rabs(oa[k]) > size[k]) return R(-1);
+          continue;
+        }
+        R an = (-size[k] - oa[k]) / da[k], af = (size[k] - oa[k]) / da[k];
+        if (an > af) std::swap(an, af);
+        if (an > nr) nr = an;
+        if (af < fr) fr = af;
+        if (nr > fr) return R(-1);
+      }
+      const R t = nr >= R(0) ? nr : fr;
+      return t >= R(0) ? t : R(-1);
+    }
+    case S_CAPSULE: {
+      R best = ray_cyl_side(size[0], size[1], o, dv);
+      const R lo = ray_sphere_at(Vec3<R>(R(0), R(0), -size[1]), size[0], o, dv);
+      if (better(lo, best)) best = lo;
+      const R hi = ray_sphere_at(Vec3<R>(R(0), R(0), size[1]), size[0], o, dv);
+      if (better(hi, best)) best = hi;
+      return best;
+    }
+    case S_CYLINDER: {
+      R best = ray_cyl_side(size[0], size[1], o, dv);
+      if (dv.z != R(0))
+        for (R z : {-size[1], size[1]}) {
+          const R t = (z - o.z) / dv.z;
+          if (t >= R(0)) {
+            const R px = o.x + dv.x * t, py = o.y + dv.y * t;
+            if (px * px + py * py <= size[0] * size[0] && (best < R(0) || t < best)) best = t;
+          }
+        }
+      return best;
+    }
+    case S_ELLIPSOID: {
+      const Vec3<R> so(o.x / size[0], o.y / size[1], o.z / size[2]), sd(dv.x / size[0], dv.y / size[1], dv.z / size[2]);
+      const R a = sd.dot(sd);
+      if (a <= R(0)) return R(-1);
+      const R hb = so.dot(sd), cc = so.dot(so) - R(1);
+      const R disc = hb * hb - a * cc;
+      if (disc < R(0)) return R(-1);
+      const R root = Sc<R>::sqrt(disc);
+      const R nr = (-hb - root) / a, fr = (-hb + root) / a;
+      const R t = nr >= R(0) ? nr : fr;
+      return t >= R(0) ? t : R(-1);
+    }
+    default: return R(-1);
+  }
+}
+// rangefinder_reading (sensor.rs:759-791): the nearest hit over every geom
+// of the world, -1 for none.
+template <class R> R rangefinder(const World<R>& w, Vec3<R> origin, Vec3<R> dir) {
+  std::vector<Pose<R>> gp;
+  w.geom_poses(gp);
+  R nearest = R(-1);
+  for (size_t i = 0; i < w.geoms.size(); ++i) {
+    const Vec3<R> o = gp[i].o.inverse_rotate(origin - gp[i].p), dv = gp[i].o.inverse_rotate(dir);
+    const R t = ray_geom(w.geoms[i].shape, w.geoms[i].size, o, dv);
+    if (t >= R(0) && (nearest < R(0) || t < nearest)) nearest = t;
+  }
+  return nearest;
+}
+
+extern "C" {
+
 int oracle_sensors(const newt_model_desc* d, const float* qpos, const float* qvel, const float* qfrc, int precision,
                    int ns, const int* si, const float* sf, double* out) {
   auto go = [&](auto tag) {
@@ -530,6 +644,12 @@ int oracle_sensors(const newt_model_desc* d, const float* qpos, const float* qve
       }
       const Quat<R> so = po * lq;
       switch (kind) {
+        case 13:  // Magnetometer (sensor.rs:664-670)
+          put3(so.inverse_rotate(Vec3<R>(d->magnetic_field[0], d->magnetic_field[1], d->magnetic_field[2])));
+          break;
+        case 14:  // Rangefinder along the site's +z (sensor.rs:671-682)
+          out[o++] = (double)rangefinder(w, pp + po.rotate(lp), so.rotate(Vec3<R>(R(0), R(0), R(1))));
+          break;
         case 2: put3(pp + po.rotate(lp)); break;
         case 3: out[o++] = (double)so.x; out[o++] = (double)so.y; out[o++] = (double)so.z; out[o++] = (double)so.w; break;
         case 4: put3(lq.inverse_rotate(wb)); break;

@@ -165,7 +165,7 @@ def tree_contact_sensors(packed, index: int, qpos: np.ndarray, qvel: np.ndarray,
     qfrc = None if qfrc is None else np.ascontiguousarray(qfrc, dtype=np.float32)
     si = np.ascontiguousarray(np.stack([sens["kind"], sens["on_link"], sens["index"]], 1), np.int32)
     sf = np.ascontiguousarray(np.concatenate([sens["local_pos"], sens["local_quat"]], 1), np.float32)
-    D = int(sum(1 if (k <= 1 or k == 10) else (4 if k == 3 else 3) for k in sens["kind"]))
+    D = int(sum(1 if (k <= 1 or k in (10, 14)) else (4 if k == 3 else 3) for k in sens["kind"]))
     out = np.zeros(D, dtype=np.float64)
     qo = np.zeros(len(qpos), np.float64)
     vo = np.zeros(len(qvel), np.float64)
@@ -182,13 +182,14 @@ def sensors(packed, index: int, qpos: np.ndarray, qvel: np.ndarray, sens: np.nda
     `sens` is an array with the fields kind, on_link, index, local_pos,
     local_quat (the newt_sensor_desc layout); `qfrc` the tree's applied
     generalised forces (newt layout), read by the accelerometer on a link
-    and the force and torque sensors."""
+    and the force and torque sensors.  Kinds 13 magnetometer and 14
+    rangefinder read the world's magnetic field and geoms."""
     qpos = np.ascontiguousarray(qpos, dtype=np.float32)
     qvel = np.ascontiguousarray(qvel, dtype=np.float32)
     qfrc = None if qfrc is None else np.ascontiguousarray(qfrc, dtype=np.float32)
     si = np.ascontiguousarray(np.stack([sens["kind"], sens["on_link"], sens["index"]], 1), np.int32)
     sf = np.ascontiguousarray(np.concatenate([sens["local_pos"], sens["local_quat"]], 1), np.float32)
-    D = int(sum(1 if k <= 1 else (4 if k == 3 else 3) for k in sens["kind"]))
+    D = int(sum(1 if (k <= 1 or k in (10, 14)) else (4 if k == 3 else 3) for k in sens["kind"]))
     out = np.zeros(D, dtype=np.float64)
     d = C.cast(C.byref(packed.descs[index]), C.c_void_p)
     lib().oracle_sensors(d, _ptr(qpos), _ptr(qvel), _ptr(qfrc), precision, len(sens), _ptr(si), _ptr(sf), _ptr(out))

@@ -39,7 +39,8 @@ SENSOR_DTYPE = np.dtype([("kind", np.int32), ("on_link", np.int32), ("index", np
 SENSOR_JOINTPOS, SENSOR_JOINTVEL, SENSOR_FRAMEPOS, SENSOR_FRAMEQUAT, SENSOR_GYRO = 0, 1, 2, 3, 4
 SENSOR_VELOCIMETER, SENSOR_FRAMELINVEL, SENSOR_FRAMEANGVEL, SENSOR_SUBTREECOM = 5, 6, 7, 8
 SENSOR_ACCELEROMETER, SENSOR_TOUCH, SENSOR_FORCE, SENSOR_TORQUE = 9, 10, 11, 12
-SENSOR_DIM = {SENSOR_JOINTPOS: 1, SENSOR_JOINTVEL: 1, SENSOR_FRAMEQUAT: 4, SENSOR_TOUCH: 1}
+SENSOR_MAGNETOMETER, SENSOR_RANGEFINDER = 13, 14
+SENSOR_DIM = {SENSOR_JOINTPOS: 1, SENSOR_JOINTVEL: 1, SENSOR_FRAMEQUAT: 4, SENSOR_TOUCH: 1, SENSOR_RANGEFINDER: 1}
 
 
 def sensors(*specs) -> np.ndarray:

@@ -48,8 +48,11 @@ struct TreeGroupDev {
 // A tree whose link geoms touch static planes (quadruped worlds): the tree
 // group's SoA layout plus per-geom model rows, the solver mode and a
 // world-major solver scratch.
-// Floats per tree-contact record in the solver scratch (newton_kernels.cu).
+// Floats per tree-contact record in the solver scratch (newton_kernels.cu),
+// SoA geom model rows per geom of a tree-contact world (size3 pos3 quat4
+// fric margin gap solref2 solimp5 torsional rolling).
 constexpr int TC_CREC = 28;
+constexpr int TC_GREC = 22;
 
 struct TcGroupDev {
   TreeGroupDev t;

@@ -83,7 +83,7 @@ constexpr int CREC = TC_CREC;  // floats per contact record
 enum { K_GA = 0, K_GB = 1, K_LINK = 2, K_SIGN = 3, K_POS = 4, K_N = 7, K_PEN = 10, K_GAP = 11, K_MU = 12,
        K_SR = 13, K_SI = 15, K_CONDIM = 20, K_ROW = 21, K_LINK2 = 22, K_MUT = 23, K_MUR = 24 };
 static_assert(K_MUR < CREC, "contact record");
-constexpr int GREC = 22;  // SoA geom model rows: size3 pos3 quat4 fric margin gap solref2 solimp5 torsional rolling
+constexpr int GREC = TC_GREC;  // SoA geom model rows: size3 pos3 quat4 fric margin gap solref2 solimp5 torsional rolling
 enum { G_SIZE = 0, G_POS = 3, G_QUAT = 6, G_FRIC = 10, G_MARGIN = 11, G_GAP = 12, G_SR = 13, G_SI = 15, G_TF = 20,
        G_RF = 21 };
 // Row codes (rfac): 0-3 the pyramidal facets n +- mu t1, n +- mu t2 of a

@@ -44,6 +44,7 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
   m.solver = d.solver; m.iterations = d.iterations; m.self_coll = d.tree_self_collision;
   m.integrator = d.integrator;
   m.cone = d.cone;
+  for (int k = 0; k < 3; ++k) m.mag[k] = d.magnetic_field[k];
   if (!(d.dt > 0.f)) return fail(ctx, NEWT_E_INVALID, "dt must be > 0");
   if (d.cone != NEWT_CONE_PYRAMIDAL && d.cone != NEWT_CONE_ELLIPTIC) return fail(ctx, NEWT_E_INVALID, "unknown cone");
   if (d.integrator != NEWT_INTEGRATOR_EULER && d.integrator != NEWT_INTEGRATOR_RK4)

@@ -21,6 +21,7 @@ struct HostModel {
   std::vector<newt_geom_desc> geoms;
   float dt = 0.005f, g[3] = {0, 0, -9.81f};
   int solver = 1, iterations = 20, self_coll = 0, integrator = NEWT_INTEGRATOR_EULER, cone = NEWT_CONE_PYRAMIDAL;
+  float mag[3] = {0, -0.5f, 0};  // World::magnetic_field (magnetometers)
   std::string key;  // topo_key(), computed once at upload
   // pile worlds whose rows are not four pyramidal facets per contact
   bool general_rows() const {

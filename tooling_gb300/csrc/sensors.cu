@@ -32,7 +32,8 @@ namespace {
 enum { JF = 0, JX = 1, JH = 2, JS = 3 };
 
 __host__ __device__ int sensor_dim(int kind) {
-  return kind <= NEWT_SENSOR_JOINTVEL || kind == NEWT_SENSOR_TOUCH ? 1 : (kind == NEWT_SENSOR_FRAMEQUAT ? 4 : 3);
+  return kind <= NEWT_SENSOR_JOINTVEL || kind == NEWT_SENSOR_TOUCH || kind == NEWT_SENSOR_RANGEFINDER
+             ? 1 : (kind == NEWT_SENSOR_FRAMEQUAT ? 4 : 3);
 }
 __host__ __device__ bool contact_sensor(int kind) {
   return kind == NEWT_SENSOR_ACCELEROMETER || kind == NEWT_SENSOR_TOUCH;
@@ -55,8 +56,121 @@ NEWT_D Q4 axis_angle(V3 axis, float angle) {  // newt/src/math.rs:574-580
 // velocity.
 struct Frame { V3 p; Q4 o; V3 w_world, v_world, w_body; };
 
+// ray_vs_geom (newt/src/scene_query.rs:182-438, no meshes): the distance
+// along the ray (origin o, direction dv, in the geom's frame) to its first
+// hit at or beyond 0 -- the far root when the ray starts inside -- or -1.
+NEWT_D float ray_sphere_at(V3 c, float r, V3 o, V3 dv) {
+  const V3 off = o - c;
+  const float a = dot(dv, dv);
+  if (a <= 0.f) return -1.f;
+  const float hb = dot(off, dv), cc = dot(off, off) - r * r;
+  const float disc = hb * hb - a * cc;
+  if (disc < 0.f) return -1.f;
+  const float root = sqrtf(disc);
+  const float nr = (-hb - root) / a, fr = (-hb + root) / a;
+  const float t = nr >= 0.f ? nr : fr;
+  return t >= 0.f ? t : -1.f;
+}
+NEWT_D float ray_cyl_side(float r, float hh, V3 o, V3 dv) {
+  const float a = dv.x * dv.x + dv.y * dv.y;
+  if (a <= 1.0e-8f) return -1.f;
+  const float hb = o.x * dv.x + o.y * dv.y, cc = o.x * o.x + o.y * o.y - r * r;
+  const float disc = hb * hb - a * cc;
+  if (disc < 0.f) return -1.f;
+  const float root = sqrtf(disc);
+  float best = -1.f;
+  const float ts[2] = {(-hb - root) / a, (-hb + root) / a};
+  for (int k = 0; k < 2; ++k) {
+    const float t = ts[k];
+    if (t >= 0.f) {
+      const float z = o.z + dv.z * t;
+      if (z >= -hh && z <= hh && (best < 0.f || t < best)) best = t;
+    }
+  }
+  return best;
+}
+NEWT_D float ray_geom(int shape, V3 sz, V3 o, V3 dv) {
+  if (!(dot(dv, dv) > 0.f)) return -1.f;
+  switch (shape) {
+    case NEWT_SHAPE_SPHERE: return ray_sphere_at(v3(0.f, 0.f, 0.f), sz.x, o, dv);
+    case NEWT_SHAPE_PLANE: {
+      if (dv.z == 0.f) return -1.f;
+      const float t = -o.z / dv.z;
+      return t >= 0.f ? t : -1.f;
+    }
+    case NEWT_SHAPE_BOX: {
+      float nr = -INFINITY, fr = INFINITY;
+      const float oa[3] = {o.x, o.y, o.z}, da[3] = {dv.x, dv.y, dv.z}, ea[3] = {sz.x, sz.y, sz.z};
+      for (int k = 0; k < 3; ++k) {
+        if (da[k] == 0.f) {
+          if (fabsf(oa[k]) > ea[k]) return -1.f;
+          continue;
+        }
+        float an = (-ea[k] - oa[k]) / da[k], af = (ea[k] - oa[k]) / da[k];
+        if (an > af) { const float x = an; an = af; af = x; }
+        if (an > nr) nr = an;
+        if (af < fr) fr = af;
+        if (nr > fr) return -1.f;
+      }
+      const float t = nr >= 0.f ? nr : fr;
+      return t >= 0.f ? t : -1.f;
+    }
+    case NEWT_SHAPE_CAPSULE: {
+      float best = ray_cyl_side(sz.x, sz.y, o, dv);
+      const float lo = ray_sphere_at(v3(0.f, 0.f, -sz.y), sz.x, o, dv);
+      if (lo >= 0.f && (best < 0.f || lo < best)) best = lo;
+      const float hi = ray_sphere_at(v3(0.f, 0.f, sz.y), sz.x, o, dv);
+      if (hi >= 0.f && (best < 0.f || hi < best)) best = hi;
+      return best;
+    }
+    case NEWT_SHAPE_CYLINDER: {
+      float best = ray_cyl_side(sz.x, sz.y, o, dv);
+      if (dv.z != 0.f)
+        for (int k = 0; k < 2; ++k) {
+          const float t = ((k ? sz.y : -sz.y) - o.z) / dv.z;
+          if (t >= 0.f) {
+            const float px = o.x + dv.x * t, py = o.y + dv.y * t;
+            if (px * px + py * py <= sz.x * sz.x && (best < 0.f || t < best)) best = t;
+          }
+        }
+      return best;
+    }
+    case NEWT_SHAPE_ELLIPSOID: {
+      const V3 so = v3(o.x / sz.x, o.y / sz.y, o.z / sz.z), sd = v3(dv.x / sz.x, dv.y / sz.y, dv.z / sz.z);
+      const float a = dot(sd, sd);
+      if (a <= 0.f) return -1.f;
+      const float hb = dot(so, sd), cc = dot(so, so) - 1.f;
+      const float disc = hb * hb - a * cc;
+      if (disc < 0.f) return -1.f;
+      const float root = sqrtf(disc);
+      const float nr = (-hb - root) / a, fr = (-hb + root) / a;
+      const float t = nr >= 0.f ? nr : fr;
+      return t >= 0.f ? t : -1.f;
+    }
+    default: return -1.f;
+  }
+}
+// The nearest hit over a world's geoms (rangefinder_reading,
+// sensor.rs:759-791): `geom(i, &shape, &size, &pose)` gives geom i's world pose.
+template <class G>
+NEWT_D float rangefinder(int ng, G geom, V3 origin, V3 dir) {
+  float nearest = -1.f;
+  for (int i = 0; i < ng; ++i) {
+    int shape;
+    V3 sz, gp;
+    Q4 go;
+    geom(i, &shape, &sz, &gp, &go);
+    const float t = ray_geom(shape, sz, qrot_inv(go, origin - gp), qrot_inv(go, dir));
+    if (t >= 0.f && (nearest < 0.f || t < nearest)) nearest = t;
+  }
+  return nearest;
+}
+
+// `mag`: the world's magnetic field; `ng`, `geom`: its geoms (rangefinder).
+template <class G>
 NEWT_D void write_sensors(const newt_sensor_desc* S, int ns, const Frame* frames, const float* q, const float* qd,
-                          const int* qoff, const int* voff, float* row, const V3* subtree_com) {
+                          const int* qoff, const int* voff, float* row, const V3* subtree_com, V3 mag, int ng,
+                          G geom) {
   int o = 0;
   for (int k = 0; k < ns; ++k) {
     const newt_sensor_desc& s = S[k];
@@ -81,6 +195,10 @@ NEWT_D void write_sensors(const newt_sensor_desc* S, int ns, const Frame* frames
         continue;
       }
       case NEWT_SENSOR_GYRO: r = qrot_inv(lq, f.w_body); break;
+      case NEWT_SENSOR_MAGNETOMETER: r = qrot_inv(qmul(f.o, lq), mag); break;  // sensor.rs:664-670
+      case NEWT_SENSOR_RANGEFINDER:  // along the site's +z (sensor.rs:671-682)
+        row[o++] = rangefinder(ng, geom, f.p + qrot(f.o, lp), qrot(qmul(f.o, lq), v3(0.f, 0.f, 1.f)));
+        continue;
       case NEWT_SENSOR_FRAMEANGVEL: r = f.w_world; break;
       default: {  // site linear velocity: origin velocity plus w x (R lp)
         const V3 lin = f.v_world + cross(f.w_world, qrot(f.o, lp));
@@ -104,7 +222,8 @@ template <int MAXL>
 __global__ void __launch_bounds__(64) tree_sensors_kernel(TreeGroupDev g, const int* idx, int n,
                                                          const newt_sensor_desc* S, int ns, float* out, int D,
                                                          const float* dyn, const float* sens, long sens_stride,
-                                                         int maxc) {
+                                                         int maxc, const float* mag, const float* tgeom,
+                                                         const int* tgtopo, int tng) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   const int w = idx[t], cap = g.cap, L = g.L;
@@ -176,7 +295,18 @@ __global__ void __launch_bounds__(64) tree_sensors_kernel(TreeGroupDev g, const 
     fr[k] = Frame{P[l], O[l], Wn[l], Vn[l], qrot_inv(O[l], Wn[l])};
   }
   float* row = out + (size_t)t * D;
-  write_sensors(S, ns, fr, q, qd, qoff, voff, row, com);
+  // the world's geoms (tree-contact worlds; a tree without geoms has none)
+  auto geom = [&](int i, int* shape, V3* sz, V3* gp, Q4* go) {
+    auto gv = [&](int f) { return tgeom[(size_t)(TC_GREC * i + f) * cap + w]; };
+    *shape = tgtopo[2 * i];
+    const int link = tgtopo[2 * i + 1];
+    *sz = v3(gv(0), gv(1), gv(2));
+    const V3 lp = v3(gv(3), gv(4), gv(5));
+    const Q4 lq{gv(6), gv(7), gv(8), gv(9)};
+    if (link < 0) { *gp = lp; *go = lq; }
+    else { *gp = P[link] + qrot(O[link], lp); *go = qmul(O[link], lq); }
+  };
+  write_sensors(S, ns, fr, q, qd, qoff, voff, row, com, v3(mag[3 * t], mag[3 * t + 1], mag[3 * t + 2]), tng, geom);
   if (sens) {  // touch: the re-solved normal forces of the geom's contacts (sensor.rs:1103-1112)
     const float* so = sens + (size_t)w * sens_stride;
     const int nc = min(max(__float_as_int(so[6 * L + 3 * maxc]), 0), maxc);
@@ -226,10 +356,12 @@ __global__ void __launch_bounds__(64) tree_sensors_kernel(TreeGroupDev g, const 
 
 // Pile worlds: free-body poses and velocities from the world-major record.
 __global__ void __launch_bounds__(64) pile_sensors_kernel(PileGroupDev g, const int* idx, int n,
-                                                         const newt_sensor_desc* S, int ns, float* out, int D) {
+                                                         const newt_sensor_desc* S, int ns, float* out, int D,
+                                                         const float* mag) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   const float* F = g.F + (size_t)idx[t] * g.lay.fstride;
+  const int* I = g.I + (size_t)idx[t] * g.lay.istride;
   Frame fr[16];
   for (int k = 0; k < ns && k < 16; ++k) {
     const int b = S[k].index;
@@ -239,7 +371,26 @@ __global__ void __launch_bounds__(64) pile_sensors_kernel(PileGroupDev g, const 
     fr[k] = Frame{v3(F[g.lay.pos + 3 * b], F[g.lay.pos + 3 * b + 1], F[g.lay.pos + 3 * b + 2]), o, qrot(o, wb),
                   v3(F[g.lay.vel + 3 * b], F[g.lay.vel + 3 * b + 1], F[g.lay.vel + 3 * b + 2]), wb};
   }
-  write_sensors(S, ns, fr, nullptr, nullptr, nullptr, nullptr, out + (size_t)t * D, nullptr);
+  // the world's geoms: one per body, then the static planes
+  auto geom = [&](int i, int* shape, V3* sz, V3* gp, Q4* go) {
+    if (i < g.nb) {
+      const Q4 bo{F[g.lay.quat + 4 * i], F[g.lay.quat + 4 * i + 1], F[g.lay.quat + 4 * i + 2], F[g.lay.quat + 4 * i + 3]};
+      const V3 bp = v3(F[g.lay.pos + 3 * i], F[g.lay.pos + 3 * i + 1], F[g.lay.pos + 3 * i + 2]);
+      const Q4 lq{F[g.lay.gquat + 4 * i], F[g.lay.gquat + 4 * i + 1], F[g.lay.gquat + 4 * i + 2], F[g.lay.gquat + 4 * i + 3]};
+      *shape = I[g.lay.shape + i];
+      *sz = v3(F[g.lay.size + 3 * i], F[g.lay.size + 3 * i + 1], F[g.lay.size + 3 * i + 2]);
+      *gp = bp + qrot(bo, v3(F[g.lay.gpos + 3 * i], F[g.lay.gpos + 3 * i + 1], F[g.lay.gpos + 3 * i + 2]));
+      *go = qmul(bo, lq);
+    } else {
+      const float* p = F + g.lay.plane + 7 * (i - g.nb);
+      *shape = NEWT_SHAPE_PLANE;
+      *sz = v3(0.f, 0.f, 0.f);
+      *gp = v3(p[0], p[1], p[2]);
+      *go = Q4{p[3], p[4], p[5], p[6]};
+    }
+  };
+  write_sensors(S, ns, fr, nullptr, nullptr, nullptr, nullptr, out + (size_t)t * D, nullptr,
+                v3(mag[3 * t], mag[3 * t + 1], mag[3 * t + 2]), g.nb + g.np, geom);
 }
 
 int bad(newt_gpu_ctx* ctx, const char* msg) {
@@ -270,7 +421,7 @@ int newt_gpu_read_sensors(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, co
   int D = 0;
   bool needs_resolve = false, needs_dyn = false;
   for (int k = 0; k < n_sensors; ++k) {
-    if (sensors[k].kind < NEWT_SENSOR_JOINTPOS || sensors[k].kind > NEWT_SENSOR_TORQUE)
+    if (sensors[k].kind < NEWT_SENSOR_JOINTPOS || sensors[k].kind > NEWT_SENSOR_RANGEFINDER)
       return bad(ctx, "unknown sensor kind");
     D += sensor_dim(sensors[k].kind);
     needs_resolve = needs_resolve || contact_sensor(sensors[k].kind);
@@ -301,11 +452,22 @@ int newt_gpu_read_sensors(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, co
     idx[r.group].push_back(r.index);
     rows[r.group].push_back(i);
   }
+  // each device row's magnetic field (its world's model), rows grouped as dI
+  std::vector<float> hmag;
+  hmag.reserve(3 * (size_t)n);
+  for (size_t gi = 0; gi < rows.size(); ++gi)
+    for (int i : rows[gi]) {
+      const HostModel& m = ctx->models[ctx->slots[slots[i]].model];
+      hmag.insert(hmag.end(), m.mag, m.mag + 3);
+    }
   cudaStream_t st = ctx->stream;
   newt_sensor_desc* dS = nullptr;
   int* dI = nullptr;
   float* dO = nullptr;
+  float* dM = nullptr;
   cudaError_t e = cudaMallocAsync(&dS, sizeof(newt_sensor_desc) * n_sensors, st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&dM, sizeof(float) * 3 * (size_t)n, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dM, hmag.data(), sizeof(float) * hmag.size(), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMallocAsync(&dI, sizeof(int) * n, st);
   if (e == cudaSuccess) e = cudaMallocAsync(&dO, sizeof(float) * (size_t)n * D, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dS, sensors, sizeof(newt_sensor_desc) * n_sensors, cudaMemcpyHostToDevice, st);
@@ -322,7 +484,7 @@ int newt_gpu_read_sensors(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, co
     const int grid = (cnt + 63) / 64;
     float* o = dO + base * D;
     if (g->kind == GK_PILE) {
-      pile_sensors_kernel<<<grid, 64, 0, st>>>(g->pile_dev(), dI + base, cnt, dS, n_sensors, o, D);
+      pile_sensors_kernel<<<grid, 64, 0, st>>>(g->pile_dev(), dI + base, cnt, dS, n_sensors, o, D, dM + 3 * base);
       if (needs_resolve) {
         resolve_rc = pile_resolve_group(ctx, g);
         if (resolve_rc != NEWT_OK) break;
@@ -354,11 +516,17 @@ int newt_gpu_read_sensors(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, co
         ctx->launches += 1;
       }
       const int mc = g->maxc;
+      const float* mg = dM + 3 * base;
+      // tree-contact worlds' geoms for the rangefinder
+      const bool tc = g->kind == GK_TREE_CONTACT;
+      const float* tg = tc ? g->tc_dev().geom : nullptr;
+      const int* tt = tc ? g->tc_dev().gtopo : nullptr;
+      const int tn = tc ? g->ng : 0;
       switch (newt_tree_bucket(td.L)) {
-        case 8: tree_sensors_kernel<8><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn, sens, sstride, mc); break;
-        case 16: tree_sensors_kernel<16><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn, sens, sstride, mc); break;
-        case 32: tree_sensors_kernel<32><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn, sens, sstride, mc); break;
-        default: tree_sensors_kernel<65><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn, sens, sstride, mc); break;
+        case 8: tree_sensors_kernel<8><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn, sens, sstride, mc, mg, tg, tt, tn); break;
+        case 16: tree_sensors_kernel<16><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn, sens, sstride, mc, mg, tg, tt, tn); break;
+        case 32: tree_sensors_kernel<32><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn, sens, sstride, mc, mg, tg, tt, tn); break;
+        default: tree_sensors_kernel<65><<<grid, 64, 0, st>>>(td, dI + base, cnt, dS, n_sensors, o, D, dyn, sens, sstride, mc, mg, tg, tt, tn); break;
       }
       if (dyn) cudaFreeAsync(dyn, st);
       if (sens) cudaFreeAsync(sens, st);
@@ -373,6 +541,7 @@ int newt_gpu_read_sensors(newt_gpu_ctx* ctx, const int32_t* slots, int32_t n, co
   if (e == cudaSuccess && resolve_rc == NEWT_OK)
     e = cudaMemcpyAsync(host.data(), dO, sizeof(float) * host.size(), cudaMemcpyDeviceToHost, st);
   if (dS) cudaFreeAsync(dS, st);
+  if (dM) cudaFreeAsync(dM, st);
   if (dI) cudaFreeAsync(dI, st);
   if (dO) cudaFreeAsync(dO, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);

@@ -55,6 +55,7 @@ class ModelDesc(C.Structure):
         ("links", C.POINTER(LinkDesc)), ("bodies", C.POINTER(BodyDesc)), ("geoms", C.POINTER(GeomDesc)),
         ("dt", C.c_float), ("gravity", C.c_float * 3), ("solver", C.c_int32), ("iterations", C.c_int32),
         ("tree_self_collision", C.c_int32), ("integrator", C.c_int32), ("cone", C.c_int32),
+        ("magnetic_field", C.c_float * 3),
     ]
 
 
@@ -158,6 +159,7 @@ class WorldModel:
     tree_self_collision: int = 0
     integrator: int = 0  # INTEGRATOR_EULER or INTEGRATOR_RK4
     cone: int = CONE_PYRAMIDAL  # SolverConfig::cone
+    magnetic_field: Sequence[float] = (0.0, -0.5, 0.0)  # World::new's (newt/src/world.rs:332)
     links: List[Link] = field(default_factory=list)
     bodies: List[tuple] = field(default_factory=list)  # (mass, inertia9)
     geoms: List[Geom] = field(default_factory=list)
@@ -228,6 +230,7 @@ class PackedModels:
             md.tree_self_collision = m.tree_self_collision
             md.integrator = m.integrator
             md.cone = m.cone
+            md.magnetic_field[:] = list(m.magnetic_field)
 
     def __len__(self) -> int:
         return len(self.descs)
@@ -275,7 +278,7 @@ class Batch:
     """
 
     def __init__(self, links, n_links, bodies, n_bodies, geoms, n_geoms, dt, gravity, solver, iterations,
-                 self_coll=0, integrator=INTEGRATOR_EULER, cone=CONE_PYRAMIDAL):
+                 self_coll=0, integrator=INTEGRATOR_EULER, cone=CONE_PYRAMIDAL, magnetic_field=(0.0, -0.5, 0.0)):
         self.links = np.ascontiguousarray(links)
         self.bodies = np.ascontiguousarray(bodies)
         self.geoms = np.ascontiguousarray(geoms)
@@ -319,6 +322,7 @@ class Batch:
             d.solver, d.iterations, d.tree_self_collision = int(solver[w]), int(iters[w]), int(self_coll)
             d.integrator = int(integrator)
             d.cone = int(cone)
+            d.magnetic_field[:] = [float(x) for x in magnetic_field]
         self.qpos = np.zeros(int(nq.sum()), np.float32)
         self.qvel = np.zeros(int(nv.sum()), np.float32)
         self.qfrc = np.zeros(int(nv.sum()), np.float32)
