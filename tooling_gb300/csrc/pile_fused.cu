@@ -663,7 +663,24 @@ extern "C" int newt_pile_fused_blocks_per_sm(int shape, int nbm, int cm) {
   with_kernel(shape, [&](auto kern, int gang, int wpw) {
     const int bytes = (int)newt_pile_fused_smem_bytes(gang * wpw, nbm, cm);
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, -1);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 32 * gang, bytes) != cudaSuccess || b < 1) b = 1;
+    // The smallest shared-memory carve-out that holds those b blocks: the
+    // rest of the SM's unified 256 KB stays L1, where the worlds' solver
+    // records (about 12 KB per settled world) live across the sweeps.
+    int dev = 0, per_sm = 0, reserved = 0;
+    cudaFuncAttributes fa;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) == cudaSuccess &&
+        cudaFuncGetAttributes(&fa, kern) == cudaSuccess && per_sm > 0) {
+      const long need = (long)b * ((long)bytes + (long)fa.sharedSizeBytes + reserved);
+      const int pct = (int)std::min(100L, (need * 100 + per_sm - 1) / per_sm);
+      int b2 = 0;
+      if (cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, pct) != cudaSuccess ||
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, kern, 32 * gang, bytes) != cudaSuccess || b2 < b)
+        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, -1);
+    }
   });
   return b;
 }
