@@ -51,9 +51,9 @@ FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 PGS_FLOP_PER_CONTACT_SWEEP = 5 * 235
 # DRAM bytes (read + write) per world and env-step of pile_k_fused, from the
 # ncu capture summarised in profiles/pile_k_fused_2048worlds_settled_full.md
-# (2048 settled worlds, one launch of 25 env-steps: 30.4 MB read + 258.4 MB
+# (2048 settled worlds, one launch of 25 env-steps: 28.8 MB read + 272.5 MB
 # written), scaled by worlds x env-steps
-FUSED_DRAM_BYTES_PER_WORLD_STEP = (30.373632e6 + 258.361344e6) / (2048 * 25)
+FUSED_DRAM_BYTES_PER_WORLD_STEP = (28.797696e6 + 272.532224e6) / (2048 * 25)
 
 
 def pinned_like(a):
