@@ -229,3 +229,33 @@ def test_plain_and_batched_agree(eng, quads):
     q2, v2 = eng.get_state(s2, int(b.nq.sum()), int(b.nv.sum()))
     eng.free(s2)
     assert np.abs(q1 - q2).max() < 1e-5 and np.abs(v1 - v2).max() < 1e-4
+
+
+def _run_engine(items, mode, n=20):
+    """Fresh context: upload and place each (model, qpos, qvel, nq, nv) in
+    order, step n env-steps, return each one's state."""
+    e = Engine(device=0)
+    try:
+        slots = []
+        for P, q, v, nq, nv in items:
+            s = e.alloc(e.upload(P))
+            e.set_state(s, q, v)
+            slots.append((s, nq, nv))
+        e.step(n, mode)
+        return [e.get_state(s, nq, nv) for s, nq, nv in slots]
+    finally:
+        e.close()
+
+
+@pytest.mark.parametrize("mode", [STEP_PLAIN, STEP_BATCHED])
+def test_tree_contact_groups_of_different_sizes_step_together(mode):
+    """A larger tree-contact group placed before a smaller one: both are
+    prepared before either launches, and each steps as it does alone."""
+    b = scenes.quadruped_batch(n_worlds=4, first_world=50)
+    w, q1, v1 = spinner(4, 0.5, M.CONE_ELLIPTIC)
+    quad = (b, b.qpos, b.qvel, int(b.nq.sum()), int(b.nv.sum()))
+    link = (M.PackedModels([as_tree(w)]), q1, v1, 7, 6)
+    together = _run_engine([quad, link], mode)
+    alone = [_run_engine([quad], mode)[0], _run_engine([link], mode)[0]]
+    for (qa, va), (qt, vt) in zip(alone, together):
+        assert np.abs(qa - qt).max() < 1e-5 and np.abs(va - vt).max() < 1e-4

@@ -1006,10 +1006,18 @@ extern "C" size_t newt_tc_smem_bytes(int L, int nv, int maxc, int rpc) {
   return (size_t)TC_WARPS * tc_smem(L, nv, maxc, rpc).words * sizeof(float);
 }
 // Kernel attribute for the dynamic shared memory (outside stream capture).
+// The limit only grows: every tree-contact group of a step is prepared before
+// any of them launches, so a later, smaller group must not lower the limit an
+// earlier, larger one launches with.
 extern "C" cudaError_t newt_tc_init(int L, int nv, int maxc, int rpc) {
   const int bytes = (int)newt_tc_smem_bytes(L, nv, maxc, rpc);
-  if (nv > REFINE_NV) return cudaFuncSetAttribute(tc_k_solve<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  return cudaFuncSetAttribute(tc_k_solve<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  const bool refine = nv > REFINE_NV;
+  cudaFuncAttributes fa;
+  cudaError_t e = refine ? cudaFuncGetAttributes(&fa, tc_k_solve<true>) : cudaFuncGetAttributes(&fa, tc_k_solve<false>);
+  if (e != cudaSuccess) return e;
+  if (bytes <= fa.maxDynamicSharedSizeBytes) return cudaSuccess;
+  return refine ? cudaFuncSetAttribute(tc_k_solve<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)
+                : cudaFuncSetAttribute(tc_k_solve<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 extern "C" void newt_launch_tc_solve(const TcGroupDev& G, cudaStream_t st) {
   const int grid = (G.t.n + TC_WARPS - 1) / TC_WARPS;
