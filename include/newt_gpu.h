@@ -137,6 +137,10 @@ typedef struct newt_model_desc {     /* one world's model: at most one tree */
                                       * elliptic under PGS (Newton takes the pyramidal cone) */
   float magnetic_field[3];           /* World::magnetic_field, world frame, read by magnetometers
                                       * (newt/src/world.rs:118-119; World::new sets (0, -0.5, 0)) */
+  int32_t n_pairs;                   /* World::pair_list (world.rs:136-139): with `pairs` non-null, the */
+  const int32_t* pairs;              /* world collides exactly these n_pairs geom pairs (a, b), in this
+                                      * order, past the group/mask filter and the tree's self-collision
+                                      * switch; null: the automatic pairs.  Tree-contact worlds only. */
 } newt_model_desc;
 
 /* ---- context ------------------------------------------------------------ */

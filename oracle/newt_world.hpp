@@ -985,10 +985,15 @@ template <class R> struct World {
   std::vector<Tree<R>> trees;
   std::vector<Geom<R>> geoms;
   std::vector<char> disabled_self_collision;  // per tree: 1 = in-tree pairs skipped
+  // World::pair_list (world.rs:136-139): explicit pairs, collided in order,
+  // past the filters
+  bool has_pair_list = false;
+  std::vector<std::pair<int, int>> pair_list;
 
   // world.rs:1042-1069 (naive pairs; the contact set equals the broadphase's).
   void auto_pairs(std::vector<std::pair<int, int>>& out) const {
     out.clear();
+    if (has_pair_list) { out = pair_list; return; }
     int n = (int)geoms.size();
     for (int a = 0; a < n; ++a)
       for (int b = a + 1; b < n; ++b) {

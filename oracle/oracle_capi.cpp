@@ -54,6 +54,10 @@ template <class R> World<R> build_world(const newt_model_desc& d) {
     w.trees.push_back(t);
     w.disabled_self_collision.push_back(d.tree_self_collision ? 0 : 1);
   }
+  if (d.pairs) {  // World::pair_list
+    w.has_pair_list = true;
+    for (int k = 0; k < d.n_pairs; ++k) w.pair_list.push_back({d.pairs[2 * k], d.pairs[2 * k + 1]});
+  }
   for (int i = 0; i < d.n_geoms; ++i) {
     const newt_geom_desc& G = d.geoms[i];
     Geom<R> g;

@@ -123,3 +123,53 @@ def test_quadruped_contact_sensors_match_fp64(eng, solver):
         assert (gpu <= np.maximum(1e-3 * scale, 2.0 * newt)).all(), (w, gpu, newt, r64)
         touching += int((r64[:13] > 0.0).sum())
     assert touching >= n, touching  # the legs have landed: about 50 geoms press on the plane
+
+
+def test_gap_alignment_with_pair_list_on_gpu(eng):
+    from test_oracle_tree_contact_sensors import gap_alignment_pair_list_scene
+    w, q, v = gap_alignment_pair_list_scene()
+    P = M.PackedModels([w])
+    slots = eng.alloc(eng.upload(P))
+    eng.set_state(slots, q, v)
+    eng.step(1, STEP_PLAIN)
+    got = eng.read_sensors(slots, GAP)[0]
+    gp, _ = eng.contacts(int(slots[0]))
+    eng.free(slots)
+    r64, _, _ = oracle_py.tree_contact_sensors(P, 0, q, v, GAP, precision=1)
+    assert got[0] > 1.0 and got[1] == 0.0, got
+    assert abs(got[0] - r64[0]) < 1e-3 * max(1.0, abs(r64[0])), (got, r64)
+    rp, _ = oracle_py.contacts(P, 0, q, v)
+    assert np.array_equal(gp, rp), (gp, rp)  # the list's order: the gap contact first
+
+
+def test_explicit_pair_list_order_on_quadrupeds(eng):
+    """An explicit list naming the four shank-plane pairs in reverse order:
+    the GPU's contacts come in that order, as the oracle's, and the step
+    matches the FP64 oracle's within 2e-3 m and 5e-2 m/s."""
+    b = scenes.quadruped_batch(n_worlds=1, first_world=300)
+    rq, rv = oracle_py.run(b, np.arange(1), b.qpos, b.qvel, None, 300, precision=1)
+    w = M.WorldModel(dt=2e-3, solver=M.SOLVER_PGS, iterations=20)
+    for k in range(b.n_links[0]):
+        L = b.links[k]
+        w.push_link(M.Link(parent=int(L["parent"]), joint=int(L["joint"]), axis=tuple(L["axis"]),
+                           jp_pos=tuple(L["jp_pos"]), jp_quat=tuple(L["jp_quat"]), jc_pos=tuple(L["jc_pos"]),
+                           mass=float(L["mass"]), inertia=list(L["inertia"])))
+    for k in range(b.n_geoms[0]):
+        G = b.geoms[k]
+        w.add_geom(M.Geom(shape=int(G["shape"]), link=int(G["link"]), size=tuple(G["size"]),
+                          local_pos=tuple(G["local_pos"]), local_quat=tuple(G["local_quat"]),
+                          friction=float(G["friction"])))
+    w.pair_list = [(13, 0), (10, 0), (7, 0), (4, 0)]  # shank-plane pairs, last leg first, plane second
+    P = M.PackedModels([w])
+    q, v = rq.astype(np.float32), rv.astype(np.float32)
+    slots = eng.alloc(eng.upload(P))
+    eng.set_state(slots, q, v)
+    eng.step(1, STEP_PLAIN)
+    gp, _ = eng.contacts(int(slots[0]))
+    eng.step(9, STEP_PLAIN)
+    gq, gv = eng.get_state(slots, len(q), len(v))
+    eng.free(slots)
+    rp, _ = oracle_py.contacts(P, 0, q, v)
+    assert np.array_equal(gp, rp), (gp, rp)
+    oq, ov = oracle_py.run(P, np.zeros(1, np.int32), q, v, None, 10, precision=1)
+    assert np.abs(gq - oq).max() < 2e-3 and np.abs(gv - ov).max() < 5e-2

@@ -83,3 +83,21 @@ def test_touch_keeps_force_free_gap_contact_alignment(precision):
     r, _, _ = oracle_py.tree_contact_sensors(M.PackedModels([w]), 0, q, v, GAP, precision=precision)
     assert r[0] > 1.0, r
     assert r[1] == 0.0, r
+
+
+def gap_alignment_pair_list_scene():
+    """tree_contacts_solver.rs:366-390 as newt states it: no filters, the two
+    pairs (upper plane, upper sphere) and (lower plane, lower sphere) given
+    as the world's explicit pair list (world.rs:136-139)."""
+    w, q, v = gap_alignment_scene()
+    for g in w.geoms:
+        g.group = g.mask = 0xFFFFFFFF
+    w.pair_list = [(0, 2), (1, 3)]
+    return w, q, v
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_touch_alignment_with_newts_pair_list(precision):
+    w, q, v = gap_alignment_pair_list_scene()
+    r, _, _ = oracle_py.tree_contact_sensors(M.PackedModels([w]), 0, q, v, GAP, precision=precision)
+    assert r[0] > 1.0 and r[1] == 0.0, r

@@ -247,13 +247,25 @@ void HostGroup::setup_tc(const HostModel& m) {
   }
   gpairs.clear();
   maxc = 0;
-  for (int a = 0; a < ng; ++a)
-    for (int b = a + 1; b < ng; ++b) {
+  // World::pair_list, in its order and past the filters, or newt's
+  // automatic pairs
+  std::vector<std::pair<int, int>> cand;
+  if (m.explicit_pairs) {
+    cand = m.pairs;
+  } else {
+    for (int a = 0; a < ng; ++a)
+      for (int b = a + 1; b < ng; ++b) {
+        const newt_geom_desc &A = m.geoms[a], &B = m.geoms[b];
+        if (A.link >= 0 && B.link >= 0 && (!m.self_coll || A.link == B.link)) continue;
+        if (!((A.group & B.mask) != 0u && (B.group & A.mask) != 0u)) continue;
+        cand.push_back({a, b});
+      }
+  }
+  for (const auto& pr : cand) {
+      const int a = pr.first, b = pr.second;
       const newt_geom_desc &A = m.geoms[a], &B = m.geoms[b];
-      if (A.link < 0 && B.link < 0) continue;
+      if (A.link < 0 && B.link < 0) continue;  // two static geoms: no routine, no rows
       const bool in_tree = A.link >= 0 && B.link >= 0;
-      if (in_tree && (!m.self_coll || A.link == B.link)) continue;
-      if (!((A.group & B.mask) != 0u && (B.group & A.mask) != 0u)) continue;
       gpairs.push_back(a);
       gpairs.push_back(b);
       if (in_tree) {  // box-box up to four contacts, capsule-capsule two, sphere pairs one

@@ -45,6 +45,17 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
   m.integrator = d.integrator;
   m.cone = d.cone;
   for (int k = 0; k < 3; ++k) m.mag[k] = d.magnetic_field[k];
+  m.explicit_pairs = d.pairs != nullptr;
+  m.pairs.clear();
+  if (m.explicit_pairs) {
+    if (d.n_pairs < 0) return fail(ctx, NEWT_E_INVALID, "n_pairs must be >= 0");
+    for (int k = 0; k < d.n_pairs; ++k) {
+      const int a = d.pairs[2 * k], b = d.pairs[2 * k + 1];
+      if (a < 0 || b < 0 || a >= d.n_geoms || b >= d.n_geoms || a == b)
+        return fail(ctx, NEWT_E_INVALID, "pair_list entry out of range");
+      m.pairs.push_back({a, b});
+    }
+  }
   if (!(d.dt > 0.f)) return fail(ctx, NEWT_E_INVALID, "dt must be > 0");
   if (d.cone != NEWT_CONE_PYRAMIDAL && d.cone != NEWT_CONE_ELLIPTIC) return fail(ctx, NEWT_E_INVALID, "unknown cone");
   if (d.integrator != NEWT_INTEGRATOR_EULER && d.integrator != NEWT_INTEGRATOR_RK4)
@@ -89,6 +100,9 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
   // classify
   if (d.n_links > 0 && d.n_bodies == 0 && d.n_geoms == 0) { m.kind = GK_TREE; m.size = d.n_links; return NEWT_OK; }
   if (d.n_links == 0 && d.n_bodies > 0) {
+    if (m.explicit_pairs)
+      return fail(ctx, NEWT_E_INVALID, "explicit pair lists are taken on tree-contact worlds (pile worlds enumerate "
+                                       "their pairs on the device)");
     // piles: one geom per body plus static planes
     std::vector<int> per_body(d.n_bodies, 0);
     int np = 0;
@@ -169,21 +183,33 @@ static int classify(newt_gpu_ctx* ctx, const newt_model_desc& d, HostModel& m) {
     // in-tree pairs (newt collides geoms of different links of one tree unless
     // its self-collision is off, world.rs:340, 1042-1069): the shape pairs
     // newt has a routine for, as on pile worlds, plus sphere-box
-    if (d.tree_self_collision)
+    // (an explicit pair list's in-tree pairs are collided whatever the
+    // filters and the switch say)
+    std::vector<std::pair<int, int>> in_tree;
+    if (m.explicit_pairs) {
+      in_tree = m.pairs;
+    } else if (d.tree_self_collision) {
       for (int i = 0; i < d.n_geoms; ++i)
-        for (int j = i + 1; j < d.n_geoms; ++j) {
-          const newt_geom_desc &A = d.geoms[i], &B = d.geoms[j];
-          if (A.link < 0 || B.link < 0 || A.link == B.link) continue;
-          if (!((A.group & B.mask) != 0u && (B.group & A.mask) != 0u)) continue;
-          const int lo = std::min(A.shape, B.shape), hi = std::max(A.shape, B.shape);
-          const bool ok = (lo == NEWT_SHAPE_SPHERE && hi <= NEWT_SHAPE_ELLIPSOID) ||
-                          (lo == NEWT_SHAPE_BOX && hi == NEWT_SHAPE_BOX) ||
-                          (lo == NEWT_SHAPE_CAPSULE && hi == NEWT_SHAPE_CAPSULE);
-          if (!ok)
-            return fail(ctx, NEWT_E_UNSUPPORTED_PAIR,
-                        "in-tree pairs on the GPU path: sphere with sphere, box, capsule, cylinder or ellipsoid, box-box, "
-                        "capsule-capsule (filter the others or disable tree self-collision)");
-        }
+        for (int j = i + 1; j < d.n_geoms; ++j)
+          if ((d.geoms[i].group & d.geoms[j].mask) != 0u && (d.geoms[j].group & d.geoms[i].mask) != 0u)
+            in_tree.push_back({i, j});
+    }
+    for (const auto& pr : in_tree) {
+      const newt_geom_desc &A = d.geoms[pr.first], &B = d.geoms[pr.second];
+      if (A.link < 0 || B.link < 0) continue;
+      if (A.link == B.link) {
+        if (m.explicit_pairs) return fail(ctx, NEWT_E_UNSUPPORTED_PAIR, "pair_list names two geoms of one link");
+        continue;
+      }
+      const int lo = std::min(A.shape, B.shape), hi = std::max(A.shape, B.shape);
+      const bool ok = (lo == NEWT_SHAPE_SPHERE && hi <= NEWT_SHAPE_ELLIPSOID) ||
+                      (lo == NEWT_SHAPE_BOX && hi == NEWT_SHAPE_BOX) ||
+                      (lo == NEWT_SHAPE_CAPSULE && hi == NEWT_SHAPE_CAPSULE);
+      if (!ok)
+        return fail(ctx, NEWT_E_UNSUPPORTED_PAIR,
+                    "in-tree pairs on the GPU path: sphere with sphere, box, capsule, cylinder or ellipsoid, box-box, "
+                    "capsule-capsule (filter the others or disable tree self-collision)");
+    }
     if (d.solver != NEWT_SOLVER_PGS && d.solver != NEWT_SOLVER_NEWTON)
       return fail(ctx, NEWT_E_INVALID, "tree-contact worlds need the PGS or Newton solver");
     m.kind = GK_TREE_CONTACT; m.size = d.n_links;

@@ -22,6 +22,8 @@ struct HostModel {
   float dt = 0.005f, g[3] = {0, 0, -9.81f};
   int solver = 1, iterations = 20, self_coll = 0, integrator = NEWT_INTEGRATOR_EULER, cone = NEWT_CONE_PYRAMIDAL;
   float mag[3] = {0, -0.5f, 0};  // World::magnetic_field (magnetometers)
+  bool explicit_pairs = false;    // World::pair_list given: `pairs`, in order
+  std::vector<std::pair<int, int>> pairs;
   std::string key;  // topo_key(), computed once at upload
   // pile worlds whose rows are not four pyramidal facets per contact
   bool general_rows() const {
@@ -40,6 +42,10 @@ struct HostModel {
       // pair list and the rows
       k += self_coll ? "s" : "n";
       k += cone == NEWT_CONE_ELLIPTIC ? "e" : "p";
+      if (explicit_pairs) {  // the pair list fixes the pairs and their order
+        k += "L";
+        for (auto& pr : pairs) { k += std::to_string(pr.first); k += '-'; k += std::to_string(pr.second); k += ';'; }
+      }
       for (auto& gd : geoms) {
         k += 'g'; k += std::to_string(gd.shape); k += '@'; k += std::to_string(gd.link);
         k += 'c'; k += std::to_string(gd.condim); k += 'f'; k += std::to_string(gd.group); k += '/';

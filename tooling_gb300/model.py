@@ -12,7 +12,7 @@ from __future__ import annotations
 
 import ctypes as C
 from dataclasses import dataclass, field
-from typing import List, Optional, Sequence
+from typing import List, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -55,7 +55,7 @@ class ModelDesc(C.Structure):
         ("links", C.POINTER(LinkDesc)), ("bodies", C.POINTER(BodyDesc)), ("geoms", C.POINTER(GeomDesc)),
         ("dt", C.c_float), ("gravity", C.c_float * 3), ("solver", C.c_int32), ("iterations", C.c_int32),
         ("tree_self_collision", C.c_int32), ("integrator", C.c_int32), ("cone", C.c_int32),
-        ("magnetic_field", C.c_float * 3),
+        ("magnetic_field", C.c_float * 3), ("n_pairs", C.c_int32), ("pairs", C.POINTER(C.c_int32)),
     ]
 
 
@@ -160,6 +160,7 @@ class WorldModel:
     integrator: int = 0  # INTEGRATOR_EULER or INTEGRATOR_RK4
     cone: int = CONE_PYRAMIDAL  # SolverConfig::cone
     magnetic_field: Sequence[float] = (0.0, -0.5, 0.0)  # World::new's (newt/src/world.rs:332)
+    pair_list: Optional[List[Tuple[int, int]]] = None  # World::pair_list: explicit geom pairs, in order
     links: List[Link] = field(default_factory=list)
     bodies: List[tuple] = field(default_factory=list)  # (mass, inertia9)
     geoms: List[Geom] = field(default_factory=list)
@@ -231,6 +232,11 @@ class PackedModels:
             md.integrator = m.integrator
             md.cone = m.cone
             md.magnetic_field[:] = list(m.magnetic_field)
+            if m.pair_list is not None:
+                pl = (C.c_int32 * max(1, 2 * len(m.pair_list)))(*[int(x) for pr in m.pair_list for x in pr])
+                self._keep.append(pl)
+                md.n_pairs = len(m.pair_list)
+                md.pairs = C.cast(pl, C.POINTER(C.c_int32))
 
     def __len__(self) -> int:
         return len(self.descs)
