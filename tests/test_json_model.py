@@ -6,6 +6,7 @@ is held to those programmatic builds field by field here.  arm.json
 (position actuators) and pile.json (meshes, explicit contact pairs) are
 outside the GPU subset and refused.
 """
+import json
 import os
 
 import numpy as np
@@ -85,4 +86,19 @@ def test_options_reach_the_model():
     with pytest.raises(JsonUnsupported):
         load_json('{"integrator": "implicitfast"}')
     with pytest.raises(JsonUnsupported):
-        load_json('{"solver": {"mode": "pgs", "cone": "elliptic"}}')
+        load_json('{"solver": {"mode": "pgs", "cone": "conical"}}')
+
+
+def test_cone_and_explicit_contact_pairs_are_read():
+    """model.rs:1557-1597 (solver.cone) and 1033-1041, 3208-3250
+    (contact_pairs.explicit, each pair stored as (min, max) in list order)."""
+    with open(os.path.join(GOLD, "stack.json")) as f:
+        root = json.load(f)
+    root["solver"] = {"mode": "pgs", "iterations": 30, "cone": "elliptic"}
+    root["contact_pairs"] = {"explicit": [{"a": "middle_box", "b": "ground"}, {"a": "bottom_box", "b": "top_box"}]}
+    w = load_json(json.dumps(root)).model
+    assert w.cone == M.CONE_ELLIPTIC
+    assert w.pair_list == [(0, 2), (1, 3)]
+    root["contact_pairs"] = {"disable": [{"a": "middle_box", "b": "ground"}]}
+    with pytest.raises(JsonUnsupported):
+        load_json(json.dumps(root))

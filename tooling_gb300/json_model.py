@@ -18,9 +18,12 @@ Follows newt/src/model.rs (load_from_path :185, build_scene :778-1142):
     offset / orientation, friction (default 0.5), solref {timeconst,
     dampratio}, solimp {dmin, dmax, width, midpoint, power}, margin, gap,
     condim; collision group and mask all ones.
-Anything else (meshes, height fields, actuators, explicit contact pairs,
-equalities, sensors, tendons, ball joints, joint limits, mocap, rolling or
-torsional friction, more than one tree) raises `JsonUnsupported`.  Axis-angle
+Also the solver's cone (model.rs:1557-1597) and explicit contact pairs
+(`contact_pairs.explicit`, model.rs:1033-1041, 3208-3250; taken by
+tree-contact worlds).  Anything else (meshes, height fields, actuators,
+auto-pair exclusions, equalities, sensors, tendons, ball joints, joint
+limits, mocap, rolling or torsional friction, more than one tree) raises
+`JsonUnsupported`.  Axis-angle
 orientations use numpy's f32 sin/cos (newt's polynomial may differ by an ulp).
 """
 from __future__ import annotations
@@ -34,7 +37,8 @@ import numpy as np
 from . import model as M
 
 f32 = np.float32
-_ROOT_KEYS = {"version", "gravity", "timestep", "integrator", "solver", "bodies", "trees", "geoms", "sites"}
+_ROOT_KEYS = {"version", "gravity", "timestep", "integrator", "solver", "bodies", "trees", "geoms", "sites",
+              "contact_pairs"}
 
 
 class JsonUnsupported(ValueError):
@@ -158,8 +162,10 @@ def load_json(source: str) -> JsonScene:
         mode = sv.get("mode", "penalty")
         w.solver = {"penalty": 0, "pgs": M.SOLVER_PGS, "newton": M.SOLVER_NEWTON}[mode]
         w.iterations = int(sv.get("iterations", 20))
-        if sv.get("cone", "pyramidal") != "pyramidal":
-            raise JsonUnsupported("only the pyramidal cone is on the GPU path")
+        cone = sv.get("cone", "pyramidal")  # model.rs:1557-1597
+        if cone not in ("pyramidal", "elliptic"):
+            raise JsonUnsupported(f"solver.cone {cone!r}")
+        w.cone = M.CONE_ELLIPTIC if cone == "elliptic" else M.CONE_PYRAMIDAL
     scene = JsonScene(w, np.zeros(0, np.float32), np.zeros(0, np.float32))
     qpos, qvel = [], []
     bodies: Dict[str, int] = {}
@@ -248,6 +254,16 @@ def load_json(source: str) -> JsonScene:
         geom.group, geom.mask = 0xFFFFFFFF, 0xFFFFFFFF
         w.add_geom(geom)
         scene.geom_names.append(g["name"])
+    if "contact_pairs" in root:  # model.rs:1033-1041, 3208-3250: explicit pairs, as (min, max)
+        cp = root["contact_pairs"]
+        _keys(cp, ("explicit",), "contact_pairs")  # "disable" (auto-pair exclusions) is outside the subset
+        index = {n: k for k, n in enumerate(scene.geom_names)}
+        pairs = []
+        for i, pr in enumerate(cp.get("explicit", [])):
+            _keys(pr, ("a", "b"), f"contact_pairs.explicit[{i}]")
+            a, b = index[pr["a"]], index[pr["b"]]
+            pairs.append((min(a, b), max(a, b)))
+        w.pair_list = pairs
     scene.site_names = [s.get("name", "") for s in root.get("sites", [])]
     scene.qpos0 = np.array(qpos, np.float32)
     scene.qvel0 = np.array(qvel, np.float32)
