@@ -3,8 +3,8 @@
 newt/tests/model_load.rs builds the same worlds in code and holds the loaded
 ones equal to them (stack.json :194-260, pendulum.json :385-470); the loader
 is held to those programmatic builds field by field here.  arm.json
-(position actuators) and pile.json (meshes, explicit contact pairs) are
-outside the GPU subset and refused.
+(position actuators) and pile.json (meshes) are outside the GPU subset and
+refused.
 """
 import json
 import os
